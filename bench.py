@@ -1,0 +1,325 @@
+"""Benchmark: particle-steps/s of the MPM step on the 2d slump at nel=[640,160].
+
+Workload (the scaled-up 2d slump): L=[64.1584,16.0396] m, nel=[640,160],
+3x3 points per cell -> 365,024 points, 103,201 nodes; cubic B-spline, finite
+strain, FLIP (C_pf=1) with mUSL, F-bar locking fix, damping 0.1, non-associated
+Drucker-Prager with softening; nonlocal averaging off (stated explicitly: the
+reference's threaded nonlocal pass races, nonlocal.jl:29-35).  Cohesion: the
+seeded random field when epgpu.grf is available, else uniform 20 kPa (said in
+the JSON line).  A step = one elastoplastic MPM cycle over all points
+(worflow.jl:80-82), dt from the reference's CFL rule.
+
+Arms:
+  default            the CUDA library through the C ABI (`--precision` fp64|mixed)
+  --impl reference   the reference path on the host cores: the FP64 restatement
+                     (oracle/) with all threads (Julia is not installed)
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(ROOT, "elastoplasm.jl_gb300"), os.path.join(ROOT, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "particle-steps/s on GB300: mixed+learned vs plain FP64, at stated stress error"
+WORKLOAD = "2d slump nel=[640,160], 3x3 points/cell (365,024 points), elastoplastic step"
+
+
+def make_workload():
+    from epgpu import ic_slump
+    fw = {"deform": "finite", "trsfr": "std", "C_pf": 1.0, "musl": True, "locking": True, "damping": 0.1}
+    kw = dict(fwrk=fw, nonloc={"status": False, "ls": 0.5})
+    field = "uniform 20 kPa"
+    try:
+        from epgpu import grf  # noqa: F401
+        kw["grf"] = {"status": True, "covariance": "exponential",
+                     "param": {"Ix": [5.0, 5.0], "mean": 2.0e4, "cov": 0.3, "min": 1.0e3, "seed": 1234}}
+        field = "seeded exponential-covariance random field (mean 20 kPa, CoV 0.3, 5 m, >= 1 kPa)"
+    except ImportError:
+        pass
+    ic, cfg = ic_slump([64.1584, 16.0396], [640, 160], ni=3, **kw)
+    return ic, cfg, field
+
+
+def cfl_dt(mesh, cmpr, vmax):
+    # get_dt (physics.jl:21-26) without the checkpoint clip
+    return 0.5 * max(mesh.h[i] / (vmax[i] + cmpr["c"]) for i in range(mesh.dim))
+
+
+# algorithmic bytes (unique reads + writes) per launch of each FP64 kernel, 2d:
+# per point and per node, from the arrays each kernel must touch once
+ALG_BYTES_FP64_2D = {
+    "bin64": (8 * (2 + 3 + 1) + 8 * 2 + 4 + 8 * 3 + 8 * 16, 0),
+    "p2g64": (8 * 16 + 8 * 7 + 4 + 4 * 16, 4 + 8 * 5),
+    "solve64": (0, 8 * 5 + 2 + 8 * 6),
+    "g2p64": (8 * 16 + 4 + 8 * 4, 8 * 4),
+    "augm64": (8 * 16 + 4 + 8 * 4 + 4 * 16, 4 + 8 * 5),
+    "deform64": (8 * 16 + 4 + 8 * (4 + 1 + 2) + 8 * (4 * 3 + 5), 8 * 2),
+    "dJ64": (8 * 16 + 4 + 8 * 3 + 4 * 16, 4 + 8 * 2),
+    "elast64": (8 * 16 + 4 + 8 * (4 + 4 + 1 + 6) + 8 * (4 + 4 + 4 + 3 + 3), 8),
+    "segsort_nodes": (8 * 16, 4),
+    "node_lists": (4 + 4 * 16, 8 * 2),
+}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_gpu{gpu}.csv")
+        os.makedirs(os.path.dirname(self.path), exist_ok=True)
+        self.proc = None
+        self.gpu = gpu
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        try:
+            self.f.close()
+        except Exception:
+            pass
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in open(self.path):
+                c = [x.strip() for x in line.split(",")]
+                if len(c) < 9:
+                    continue
+                try:
+                    sm.append(float(c[1]))
+                    mx = max(mx, float(c[2]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, c[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(n)
+        except OSError:
+            pass
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons)}
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo" if os.environ.get("EP_BENCH_GLOO") else "nccl")
+    return rank, ws
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(x, ws):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_sample(ic, cfg, seconds_budget=20.0, threads=None):
+    """The FP64 restatement on the host cores: a bounded number of steps of the same workload."""
+    import oracle
+    threads = threads or os.cpu_count() or 1
+    o = oracle.Oracle(ic, cfg["instr"], threads=threads)
+    vmax = np.zeros(ic["mesh"].dim)
+    g = [0.0] * (ic["mesh"].dim - 1) + [-9.81]
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        dt = cfl_dt(ic["mesh"], ic["cmpr"], vmax)
+        vmax = o.step(1, dt, g)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el > seconds_budget or steps >= 50:
+            break
+    o.close()
+    return ic["mpts"].nmp * steps / el, threads, steps, el
+
+
+def run_reference(args, rank, ws):
+    if rank != 0:
+        return
+    ic, cfg, field = make_workload()
+    val, threads, steps, el = cpu_sample(ic, cfg, seconds_budget=max(10.0, 2.0 * args.steps))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": "particle-steps/s", "n_gpus": args.gpus,
+        "steps": steps, "warmup": 0, "ms_per_step": 1e3 * el / steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": f"synthetic ({field})",
+        "config": {"workload": WORKLOAD, "points": ic["mpts"].nmp, "nodes": ic["mesh"].nnodes},
+        "cpu_baseline": {"value": val, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+                         "sample": f"{steps} elastoplastic steps of the full workload on {threads} threads "
+                                   "(Julia is not installed; the FP64 C++ restatement of the reference path)"},
+        "e2e": {"value": val, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank, ws = dist_init()
+    if args.impl == "reference":
+        run_reference(args, rank, ws)
+        return
+    import torch
+    from epgpu import Engine
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    ic, cfg, field = make_workload()
+    cfg["instr"]["gpu"] = {"precision": args.precision, "jaumann": False}
+    mesh, mpts, cmpr = ic["mesh"], ic["mpts"], ic["cmpr"]
+    np_, dim = mpts.nmp, mesh.dim
+    g = [0.0] * (dim - 1) + [-9.81]
+    host0 = mpts.copy()
+    e = Engine(ic, cfg["instr"])
+    vmax = np.zeros(dim)
+    for _ in range(args.warmup):
+        vmax = e.step(1, cfl_dt(mesh, cmpr, vmax), g)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")   # 256 MB > 129 MB L2
+    e.profile(True)
+    l0 = e.stats()["launches"]
+    dev_ms = 0.0
+    barrier(ws)
+    torch.cuda.synchronize()
+    with Clocks(local) as clk:
+        for _ in range(args.steps):
+            flush.fill_(1.0)                       # evict L2 between timed steps
+            torch.cuda.synchronize()
+            vmax = e.step(1, cfl_dt(mesh, cmpr, vmax), g)
+            dev_ms += e.stats()["device_ms"]
+    torch.cuda.synchronize()
+    barrier(ws)
+    launches = e.stats()["launches"] - l0
+    ktimes = e.kernel_times()
+    e.profile(False)
+    tmax = allmax(dev_ms, ws)
+    value = ws * np_ * args.steps / (tmax * 1e-3)
+    plastic = e.stats()["plastic"]
+    # dominant kernel and its roofline
+    dom = max(ktimes.items(), key=lambda kv: kv[1][1])
+    name, (nl, tot) = dom
+    avg_ms = tot / max(nl, 1)
+    ppt, pnode = ALG_BYTES_FP64_2D.get(name, (0, 0))
+    alg = ppt * np_ + pnode * mesh.nnodes
+    peak, peak_kind = peaks()
+    achieved = alg / (avg_ms * 1e-3) / 1e9 if alg else None
+    roof = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": (achieved / peak) if achieved else None, "traffic": None,
+            "peak_source": f"{peak_kind} hbm_gbs", "alg_bytes_per_launch": alg,
+            "avg_launch_ms": avg_ms,
+            "kernel_share": {k: round(v[1] / sum(x[1] for x in ktimes.values()), 4) for k, v in ktimes.items()}}
+    # end to end through the C ABI with host buffers: upload + step + download every step
+    e2e = None
+    if not args.no_e2e:
+        import ctypes as C
+        from epgpu import abi
+        pinned = []
+
+        def pin(a):
+            t = torch.from_numpy(np.ascontiguousarray(a.reshape(-1, order="F"))).pin_memory()
+            pinned.append(t)
+            return t.numpy().reshape(a.shape, order="F")
+
+        hp = host0.copy()
+        for k, v in list(hp.__dict__.items()):
+            if isinstance(v, np.ndarray) and v.dtype == np.float64:
+                setattr(hp, k, pin(v))
+        view = abi.mpts_view(hp)
+        up = sum(getattr(hp, f).nbytes for f in ("x", "v", "l", "l0", "n0", "n", "Omega0", "Omega", "dJ", "J",
+                                                 "rho0", "rho", "c0", "cr", "phi", "dlam", "epII", "sig", "tau",
+                                                 "dvij", "dFij", "Fij", "bij", "eij", "wij", "sJij"))
+        down = up
+        vm = np.zeros(dim)
+        e2 = Engine({"mesh": mesh, "mpts": hp, "cmpr": cmpr}, cfg["instr"])
+        tot = 0.0
+        for k in range(args.warmup + args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            e2._check(e2.lib.epgpu_upload(e2.h, C.byref(view)))
+            vm = e2.step(1, cfl_dt(mesh, cmpr, vm), g)
+            e2._check(e2.lib.epgpu_download(e2.h, C.byref(view)))
+            if k >= args.warmup:
+                tot += time.perf_counter() - t0
+        tot = allmax(tot, ws)
+        e2.close()
+        e2e = {"value": ws * np_ * args.steps / tot, "unit": "particle-steps/s", "h2d_bytes_per_step": up,
+               "d2h_bytes_per_step": down}
+    cpu = None
+    if rank == 0 and ws == 1:
+        ic2, cfg2, _ = make_workload()
+        val, threads, steps, el = cpu_sample(ic2, cfg2, seconds_budget=args.cpu_seconds)
+        cpu = {"value": val, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+               "sample": f"{steps} elastoplastic steps of the same workload, FP64 restatement on {threads} threads"}
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": tmax / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+            "data": f"synthetic slump geometry ({field})",
+            "config": {"workload": WORKLOAD, "precision": args.precision, "points": np_,
+                       "nodes": mesh.nnodes, "l2": "flushed between timed steps (256 MB write)",
+                       "parallelism": f"replicas x{ws}", "plastic_points_last_step": plastic},
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

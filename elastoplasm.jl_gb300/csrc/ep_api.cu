@@ -1,0 +1,695 @@
+// ep_api.cu -- the C ABI of include/epgpu.h: handle life cycle, host <->
+// device transposes (Julia column-major AoS <-> device SoA), the step and the
+// device-resident time loop captured in CUDA graphs.
+#include <climits>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/epgpu.h"
+#include "ep_internal.h"
+
+using namespace ep;
+
+namespace {
+
+thread_local std::string g_create_error;
+constexpr int GRAPH_STEPS = 16;
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t n = 0;
+};
+
+}  // namespace
+
+struct ep_handle {
+    ep_cfg cfg;
+    ep_cmpr cm;
+    int dim = 0, nstr = 0, nn = 0;
+    int np = 0, nnode = 0, ncell = 0;
+    int64_t nel[4] = {0, 0, 0, 0}, nno[4] = {0, 0, 0, 0};
+    cudaStream_t s = nullptr;
+    std::vector<void*> allocs;
+    double* pbuf = nullptr;       // point SoA
+    double* nbuf = nullptr;       // node SoA
+    Fp64Ctx ctx{};
+    Ctl* ctl = nullptr;           // device control block
+    Ctl* hctl = nullptr;          // pinned mirror
+    double* stage = nullptr;      // device staging for AoS transposes
+    size_t stage_n = 0;
+    // fields the step never touches, kept on the host for download
+    std::vector<double> u, pp, du, epV;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    long long graph_kernels[2] = {0, 0};
+    long long launches = 0;
+    int64_t steps = 0;
+    double last_ms = 0.0;
+    double t = 0.0;
+    bool uploaded = false;
+    std::string err;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    Prof prof;
+};
+
+static double bits_to_double(unsigned long long b) {
+    double v;
+    std::memcpy(&v, &b, sizeof(double));
+    return v;
+}
+
+static ep_status fail(ep_handle* h, ep_status st, const std::string& m) {
+    if (h) h->err = m;
+    else g_create_error = m;
+    return st;
+}
+
+static ep_status cuda_fail(ep_handle* h, cudaError_t e, const char* where) {
+    std::string m = std::string(where) + ": " + cudaGetErrorString(e);
+    cudaGetLastError();
+    return fail(h, EP_ERR_CUDA, m);
+}
+
+#define CK(h, call)                                                  \
+    do {                                                             \
+        cudaError_t e__ = (call);                                    \
+        if (e__ != cudaSuccess) return cuda_fail((h), e__, #call);   \
+    } while (0)
+
+template <class T>
+static cudaError_t dalloc(ep_handle* h, T** p, size_t n) {
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, (n ? n : 1) * sizeof(T));
+    if (e == cudaSuccess) {
+        h->allocs.push_back(q);
+        cudaMemset(q, 0, (n ? n : 1) * sizeof(T));
+    }
+    *p = (T*)q;
+    return e;
+}
+
+// AoS (k x np, column-major) -> SoA block (k streams of np)
+__global__ void k_aos_to_soa(const double* __restrict__ in, int k, int np, double* out) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    for (int c = 0; c < k; ++c) out[(size_t)c * np + p] = in[(size_t)c + (size_t)k * p];
+}
+__global__ void k_soa_to_aos(const double* __restrict__ in, int k, int np, double* out) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    for (int c = 0; c < k; ++c) out[(size_t)c + (size_t)k * p] = in[(size_t)c * np + p];
+}
+
+static ep_status put_aos(ep_handle* h, const double* host, int k, double* dev_block) {
+    if (!host) return EP_OK;
+    size_t n = (size_t)k * h->np;
+    if (n == 0) return EP_OK;
+    if (k == 1) {
+        CK(h, cudaMemcpyAsync(dev_block, host, n * sizeof(double), cudaMemcpyHostToDevice, h->s));
+        return EP_OK;
+    }
+    CK(h, cudaMemcpyAsync(h->stage, host, n * sizeof(double), cudaMemcpyHostToDevice, h->s));
+    k_aos_to_soa<<<(h->np + 255) / 256, 256, 0, h->s>>>(h->stage, k, h->np, dev_block);
+    CK(h, cudaGetLastError());
+    CK(h, cudaStreamSynchronize(h->s));   // the staging buffer is reused by the next field
+    return EP_OK;
+}
+
+static ep_status get_aos(ep_handle* h, const double* dev_block, int k, double* host) {
+    if (!host) return EP_OK;
+    size_t n = (size_t)k * h->np;
+    if (n == 0) return EP_OK;
+    if (k == 1) {
+        CK(h, cudaMemcpyAsync(host, dev_block, n * sizeof(double), cudaMemcpyDeviceToHost, h->s));
+        CK(h, cudaStreamSynchronize(h->s));
+        return EP_OK;
+    }
+    k_soa_to_aos<<<(h->np + 255) / 256, 256, 0, h->s>>>(dev_block, k, h->np, h->stage);
+    CK(h, cudaGetLastError());
+    CK(h, cudaMemcpyAsync(host, h->stage, n * sizeof(double), cudaMemcpyDeviceToHost, h->s));
+    CK(h, cudaStreamSynchronize(h->s));
+    return EP_OK;
+}
+
+// point field blocks inside pbuf
+enum Fld {
+    F_X, F_XO, F_V, F_L, F_L0, F_N0, F_N, F_OM0, F_OM, F_DJ, F_J, F_RHO0, F_RHO, F_C0, F_CR, F_TPHI, F_SPHI, F_CPHI,
+    F_DLAM, F_EP, F_SIG, F_TAU, F_DV, F_DF, F_F, F_B, F_EPS, F_W, F_SJ, F_SH, F_COUNT
+};
+
+static int fld_width(Fld f, int d, int ns) {
+    switch (f) {
+        case F_X: case F_XO: case F_V: case F_L: case F_L0: return d;
+        case F_EP: return 2;
+        case F_SIG: case F_TAU: return ns;
+        case F_DV: case F_DF: case F_F: case F_B: case F_EPS: case F_W: case F_SJ: return d * d;
+        case F_SH: return 8 * d;
+        default: return 1;
+    }
+}
+
+static double* fld_ptr(ep_handle* h, Fld f) {
+    size_t off = 0;
+    for (int i = 0; i < (int)f; ++i) off += (size_t)fld_width((Fld)i, h->dim, h->nstr) * h->np;
+    return h->pbuf + off;
+}
+
+extern "C" {
+
+const char* epgpu_version(void) { return "epgpu 0.1 (sm_103a, FP64 oracle-order step)"; }
+
+const char* epgpu_last_error(const ep_handle* h) { return h ? h->err.c_str() : g_create_error.c_str(); }
+
+ep_status epgpu_destroy(ep_handle* h) {
+    if (!h) return EP_ERR_ARG;
+    for (int i = 0; i < 2; ++i)
+        if (h->graph[i]) cudaGraphExecDestroy(h->graph[i]);
+    if (h->s) cudaStreamSynchronize(h->s);
+    for (void* p : h->allocs) cudaFree(p);
+    if (h->hctl) cudaFreeHost(h->hctl);
+    if (h->ev0) cudaEventDestroy(h->ev0);
+    if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->s) cudaStreamDestroy(h->s);
+    delete h;
+    return EP_OK;
+}
+
+ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_view* mesh, int64_t nmp,
+                       ep_handle** out) {
+    g_create_error.clear();
+    if (!cfg || !cmpr || !mesh || !out || nmp < 0) return fail(nullptr, EP_ERR_ARG, "null argument or nmp < 0");
+    *out = nullptr;
+    const int d = cfg->dim;
+    if (d != 2 && d != 3) return fail(nullptr, EP_ERR_UNSUPPORTED, "only 2d and 3d steps are built");
+    if (mesh->dim != d) return fail(nullptr, EP_ERR_ARG, "mesh.dim != cfg.dim");
+    if (cfg->basis < 0 || cfg->basis > 2) return fail(nullptr, EP_ERR_UNSUPPORTED, "unknown basis.which");
+    if (cfg->trsfr != EP_TRSFR_STD && cfg->trsfr != EP_TRSFR_TPIC)
+        return fail(nullptr, EP_ERR_UNSUPPORTED, "only std and tpic transfers are built");
+    if (cfg->deform != EP_DEFORM_FINITE && cfg->deform != EP_DEFORM_INFINITESIMAL)
+        return fail(nullptr, EP_ERR_UNSUPPORTED, "unknown fwrk.deform");
+    if (cfg->constitutive != EP_CONS_DP && cfg->constitutive != EP_CONS_J2)
+        return fail(nullptr, EP_ERR_UNSUPPORTED, "InvalidReturnMapping: only DP and J2 are built");
+    if (cfg->basis == EP_BASIS_GIMPM) {
+        bool fin = cfg->deform == EP_DEFORM_FINITE;
+        int w = cfg->how;
+        bool ok = fin ? (w == EP_HOW_UNDEFORMED || w == EP_HOW_DETFIJ || w == EP_HOW_FII || w == EP_HOW_UII)
+                      : (w == EP_HOW_UNDEFORMED || w == EP_HOW_DETDFIJ || w == EP_HOW_DFII || w == EP_HOW_DUII);
+        if (!ok) return fail(nullptr, EP_ERR_UNSUPPORTED, "basis.how undefined for gimpm in this framework");
+    }
+    if (cfg->precision != EP_PREC_FP64) return fail(nullptr, EP_ERR_UNSUPPORTED, "only the FP64 step is built");
+    if (cfg->nonloc && !(cfg->nonloc_ls > 0.0)) return fail(nullptr, EP_ERR_ARG, "nonloc.ls must be > 0");
+    if (!mesh->x || !mesh->xB || !mesh->bcs) return fail(nullptr, EP_ERR_ARG, "mesh.x, mesh.xB and mesh.bcs are required");
+    long long nnode = 1, ncell = 1;
+    for (int i = 0; i < d; ++i) {
+        if (mesh->nno[i] < 2 || mesh->nel[i] != mesh->nno[i] - 1 || !(mesh->h[i] > 0.0))
+            return fail(nullptr, EP_ERR_ARG, "inconsistent mesh.nel/nno/h");
+        nnode *= mesh->nno[i];
+        ncell *= mesh->nel[i];
+    }
+    if (mesh->nno[d] != nnode || mesh->nel[d] != ncell) return fail(nullptr, EP_ERR_ARG, "mesh.nno/nel totals");
+    const long long NN = d == 2 ? 16 : 64;
+    if (nnode > 16000000LL || ncell > 16000000LL || nmp * NN > (long long)INT_MAX)
+        return fail(nullptr, EP_ERR_UNSUPPORTED, "mesh or point count beyond the 32-bit index range of this build");
+
+    ep_handle* h = new ep_handle();
+    h->cfg = *cfg;
+    h->cm = *cmpr;
+    h->dim = d;
+    h->nstr = d == 2 ? 3 : 6;
+    h->nn = (int)NN;
+    h->np = (int)nmp;
+    h->nnode = (int)nnode;
+    h->ncell = (int)ncell;
+    for (int i = 0; i < 4; ++i) { h->nel[i] = mesh->nel[i]; h->nno[i] = mesh->nno[i]; }
+
+    // per-direction node coordinates, checked to form the tensor-product grid of get_coords
+    std::vector<std::vector<double>> ax(d);
+    auto node_of = [&](const int* i) -> long long {
+        if (d == 2) return i[1] + mesh->nno[1] * (long long)i[0];
+        return i[2] + mesh->nno[2] * (long long)i[0] + mesh->nno[2] * mesh->nno[0] * (long long)i[1];
+    };
+    for (int dd = 0; dd < d; ++dd) {
+        ax[dd].resize(mesh->nno[dd]);
+        for (int k = 0; k < mesh->nno[dd]; ++k) {
+            int i[3] = {0, 0, 0};
+            i[dd] = k;
+            ax[dd][k] = mesh->x[dd + d * node_of(i)];
+        }
+    }
+    for (long long n = 0; n < nnode; ++n) {
+        int i[3];
+        if (d == 2) { i[0] = (int)(n / mesh->nno[1]); i[1] = (int)(n % mesh->nno[1]); }
+        else {
+            long long nzx = mesh->nno[2] * mesh->nno[0];
+            i[1] = (int)(n / nzx);
+            long long r = n % nzx;
+            i[0] = (int)(r / mesh->nno[2]);
+            i[2] = (int)(r % mesh->nno[2]);
+        }
+        for (int dd = 0; dd < d; ++dd)
+            if (mesh->x[dd + d * n] != ax[dd][i[dd]]) {
+                epgpu_destroy(h);
+                return fail(nullptr, EP_ERR_ARG, "mesh.x is not the structured grid of get_coords");
+            }
+    }
+    // optional e2n check against the structured stencil (e2n.jl:20-78)
+    if (mesh->e2n) {
+        for (long long c = 0; c < ncell; ++c) {
+            int e[3];
+            if (d == 2) { e[0] = (int)(c / mesh->nel[1]); e[1] = (int)(c % mesh->nel[1]); }
+            else {
+                long long nzx = mesh->nel[2] * mesh->nel[0];
+                e[1] = (int)(c / nzx);
+                long long r = c % nzx;
+                e[0] = (int)(r / mesh->nel[2]);
+                e[2] = (int)(r % mesh->nel[2]);
+            }
+            for (int s = 0; s < NN; ++s) {
+                int o[3], i[3];
+                if (d == 2) { o[0] = s >> 2; o[1] = s & 3; }
+                else { o[1] = s >> 4; o[0] = (s >> 2) & 3; o[2] = s & 3; }
+                bool ok = true;
+                for (int dd = 0; dd < d; ++dd) {
+                    i[dd] = e[dd] - 1 + o[dd];
+                    ok = ok && i[dd] >= 0 && i[dd] < mesh->nno[dd];
+                }
+                long long want = ok ? node_of(i) + 1 : 0;
+                if (mesh->e2n[s + NN * c] != want) {
+                    epgpu_destroy(h);
+                    return fail(nullptr, EP_ERR_ARG, "mesh.e2n differs from the structured stencil");
+                }
+            }
+        }
+    }
+
+    if (cudaStreamCreateWithFlags(&h->s, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        epgpu_destroy(h);
+        return fail(nullptr, EP_ERR_CUDA, "no CUDA device / stream");
+    }
+    cudaEventCreate(&h->ev0);
+    cudaEventCreate(&h->ev1);
+
+    Geo& g = h->ctx.g;
+    g.dim = d;
+    g.nn = (int)NN;
+    g.ncell = (int)ncell;
+    g.nnode = (int)nnode;
+    std::vector<signed char> cls;
+    for (int dd = 0; dd < d; ++dd) {
+        g.nel[dd] = (int)mesh->nel[dd];
+        g.nno[dd] = (int)mesh->nno[dd];
+        g.h[dd] = mesh->h[dd];
+        g.x0[dd] = mesh->x0[dd];
+        g.xB0[dd] = mesh->xB[dd];
+        g.xB1[dd] = mesh->xB[dd + d];
+        g.nnel[dd] = cfg->nonloc ? (int)ceil(cfg->nonloc_ls / mesh->h[dd]) : 0;
+        double* axd;
+        signed char* cd;
+        if (dalloc(h, &axd, ax[dd].size()) != cudaSuccess || dalloc(h, &cd, ax[dd].size()) != cudaSuccess) {
+            epgpu_destroy(h);
+            return fail(nullptr, EP_ERR_NOMEM, "device allocation (mesh axes)");
+        }
+        cudaMemcpy(axd, ax[dd].data(), ax[dd].size() * sizeof(double), cudaMemcpyHostToDevice);
+        cls.resize(ax[dd].size());
+        for (size_t k = 0; k < ax[dd].size(); ++k) cls[k] = (signed char)bspline_class(ax[dd][k], g.xB0[dd], g.xB1[dd], g.h[dd]);
+        cudaMemcpy(cd, cls.data(), cls.size(), cudaMemcpyHostToDevice);
+        g.ax[dd] = axd;
+        g.cls[dd] = cd;
+    }
+    {
+        std::vector<unsigned char> b((size_t)d * nnode);
+        for (long long n = 0; n < nnode; ++n)
+            for (int dd = 0; dd < d; ++dd) b[(size_t)dd * nnode + n] = mesh->bcs[dd + d * n] ? 1 : 0;
+        unsigned char* bd;
+        if (dalloc(h, &bd, b.size()) != cudaSuccess) {
+            epgpu_destroy(h);
+            return fail(nullptr, EP_ERR_NOMEM, "device allocation (bcs)");
+        }
+        cudaMemcpy(bd, b.data(), b.size(), cudaMemcpyHostToDevice);
+        g.bcs = bd;
+    }
+    Cfg& cf = h->ctx.cf;
+    cf.dim = d; cf.basis = cfg->basis; cf.how = cfg->how; cf.deform = cfg->deform; cf.trsfr = cfg->trsfr;
+    cf.musl = cfg->musl; cf.locking = cfg->locking; cf.cons = cfg->constitutive; cf.nonloc = cfg->nonloc;
+    cf.jaumann = cfg->jaumann; cf.Cpf = cfg->C_pf; cf.damping = cfg->damping; cf.ls = cfg->nonloc_ls;
+    Mat& mt = h->ctx.mt;
+    mt.Kc = cmpr->Kc; mt.Gc = cmpr->Gc; mt.Hp = cmpr->Hp; mt.c = cmpr->c;
+    const int ns = h->nstr;
+    for (int i = 0; i < 36; ++i) { mt.Del[i] = (i < ns * ns) ? cmpr->Del[i] : 0.0; mt.DelLU[i] = mt.Del[i]; }
+    if (ns == 3) lu_factor<3>(mt.DelLU, mt.piv);
+    else lu_factor<6>(mt.DelLU, mt.piv);
+
+    // point and node storage
+    size_t pw = 0;
+    for (int f = 0; f < F_COUNT; ++f) pw += (size_t)fld_width((Fld)f, d, ns);
+    size_t nw = 1 + 4 * (size_t)d + 1;
+    bool ok = dalloc(h, &h->pbuf, pw * (size_t)h->np) == cudaSuccess && dalloc(h, &h->nbuf, nw * (size_t)h->nnode) == cudaSuccess;
+    size_t stage_n = std::max<size_t>((size_t)d * d * h->np, (size_t)h->nn * h->np / 2);
+    stage_n = std::max<size_t>(stage_n, (size_t)d * h->nnode);
+    ok = ok && dalloc(h, &h->stage, stage_n) == cudaSuccess;
+    h->stage_n = stage_n;
+    Sort& S = h->ctx.S;
+    int ntmp = std::max(scan_tmp_ints((int)ncell), scan_tmp_ints((int)nnode));
+    ok = ok && dalloc(h, &S.cell_count, ncell) == cudaSuccess && dalloc(h, &S.cell_start, ncell + 1) == cudaSuccess &&
+         dalloc(h, &S.cell_cursor, ncell) == cudaSuccess && dalloc(h, &S.cell_list, h->np) == cudaSuccess &&
+         dalloc(h, &S.node_count, nnode) == cudaSuccess && dalloc(h, &S.node_start, nnode + 1) == cudaSuccess &&
+         dalloc(h, &S.node_cursor, nnode) == cudaSuccess && dalloc(h, &S.node_list, (size_t)NN * h->np) == cudaSuccess &&
+         dalloc(h, &S.scan_tmp, ntmp) == cudaSuccess;
+    int* p2e = nullptr;
+    ok = ok && dalloc(h, &p2e, h->np) == cudaSuccess;
+    ok = ok && dalloc(h, &h->ctl, 1) == cudaSuccess;
+    if (!ok) {
+        epgpu_destroy(h);
+        return fail(nullptr, EP_ERR_NOMEM, "device allocation (points/nodes)");
+    }
+    if (cudaMallocHost((void**)&h->hctl, sizeof(Ctl)) != cudaSuccess) {
+        cudaGetLastError();
+        epgpu_destroy(h);
+        return fail(nullptr, EP_ERR_NOMEM, "pinned allocation");
+    }
+    std::memset(h->hctl, 0, sizeof(Ctl));
+    P64& P = h->ctx.P;
+    P.np = h->np;
+    for (int i = 0; i < d; ++i) {
+        P.x[i] = fld_ptr(h, F_X) + (size_t)i * h->np;
+        P.xo[i] = fld_ptr(h, F_XO) + (size_t)i * h->np;
+        P.v[i] = fld_ptr(h, F_V) + (size_t)i * h->np;
+        P.l[i] = fld_ptr(h, F_L) + (size_t)i * h->np;
+        P.l0[i] = fld_ptr(h, F_L0) + (size_t)i * h->np;
+    }
+    P.n0 = fld_ptr(h, F_N0); P.n = fld_ptr(h, F_N); P.Om0 = fld_ptr(h, F_OM0); P.Om = fld_ptr(h, F_OM);
+    P.dJ = fld_ptr(h, F_DJ); P.J = fld_ptr(h, F_J); P.rho0 = fld_ptr(h, F_RHO0); P.rho = fld_ptr(h, F_RHO);
+    P.c0 = fld_ptr(h, F_C0); P.cr = fld_ptr(h, F_CR); P.tphi = fld_ptr(h, F_TPHI); P.sphi = fld_ptr(h, F_SPHI);
+    P.cphi = fld_ptr(h, F_CPHI); P.dlam = fld_ptr(h, F_DLAM);
+    P.ep1 = fld_ptr(h, F_EP); P.ep2 = fld_ptr(h, F_EP) + h->np;
+    for (int k = 0; k < ns; ++k) {
+        P.sig[k] = fld_ptr(h, F_SIG) + (size_t)k * h->np;
+        P.tau[k] = fld_ptr(h, F_TAU) + (size_t)k * h->np;
+    }
+    for (int k = 0; k < d * d; ++k) {
+        P.dv[k] = fld_ptr(h, F_DV) + (size_t)k * h->np;
+        P.dF[k] = fld_ptr(h, F_DF) + (size_t)k * h->np;
+        P.F[k] = fld_ptr(h, F_F) + (size_t)k * h->np;
+        P.b[k] = fld_ptr(h, F_B) + (size_t)k * h->np;
+        P.eps[k] = fld_ptr(h, F_EPS) + (size_t)k * h->np;
+        P.w[k] = fld_ptr(h, F_W) + (size_t)k * h->np;
+        P.sJ[k] = fld_ptr(h, F_SJ) + (size_t)k * h->np;
+    }
+    P.SH = fld_ptr(h, F_SH);
+    P.p2e = p2e;
+    N64& N = h->ctx.N;
+    N.m = h->nbuf;
+    for (int i = 0; i < d; ++i) {
+        N.p[i] = h->nbuf + (size_t)(1 + i) * h->nnode;
+        N.oobf[i] = h->nbuf + (size_t)(1 + d + i) * h->nnode;
+        N.a[i] = h->nbuf + (size_t)(1 + 2 * d + i) * h->nnode;
+        N.v[i] = h->nbuf + (size_t)(1 + 3 * d + i) * h->nnode;
+    }
+    N.dJ = h->nbuf + (size_t)(1 + 4 * d) * h->nnode;
+    h->ctx.ctl = h->ctl;
+    h->ctx.np = h->np;
+    h->ctx.launches = &h->launches;
+    h->ctx.prof = nullptr;
+    h->u.assign((size_t)d * h->np, 0.0);
+    h->pp.assign((size_t)d * h->np, 0.0);
+    h->du.assign((size_t)d * d * h->np, 0.0);
+    h->epV.assign((size_t)h->np, 0.0);
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        std::string m = std::string("create: ") + cudaGetErrorString(e);
+        cudaGetLastError();
+        epgpu_destroy(h);
+        return fail(nullptr, EP_ERR_CUDA, m);
+    }
+    *out = h;
+    return EP_OK;
+}
+
+ep_status epgpu_upload(ep_handle* h, const ep_mpts_view* m) {
+    if (!h || !m) return EP_ERR_ARG;
+    if (m->nmp != h->np || m->ndim != h->dim) return fail(h, EP_ERR_ARG, "mpts.nmp/ndim differ from create");
+    const int d = h->dim, ns = h->nstr;
+    if (!m->x || !m->v || !m->Omega0 || !m->Omega || !m->J || !m->rho0 || !m->rho || !m->c0 || !m->cr || !m->phi ||
+        !m->dlam || !m->epII || !m->sig || !m->tau || !m->Fij || !m->bij || !m->l || !m->l0 || !m->n0 || !m->n ||
+        !m->dJ || !m->dvij)
+        return fail(h, EP_ERR_ARG, "a point field read by the step is NULL");
+    ep_status st;
+#define PUT(ptr, k, f) if ((st = put_aos(h, (ptr), (k), fld_ptr(h, (f)))) != EP_OK) return st
+    PUT(m->x, d, F_X); PUT(m->v, d, F_V); PUT(m->l, d, F_L); PUT(m->l0, d, F_L0);
+    PUT(m->n0, 1, F_N0); PUT(m->n, 1, F_N); PUT(m->Omega0, 1, F_OM0); PUT(m->Omega, 1, F_OM); PUT(m->dJ, 1, F_DJ);
+    PUT(m->J, 1, F_J); PUT(m->rho0, 1, F_RHO0); PUT(m->rho, 1, F_RHO); PUT(m->c0, 1, F_C0); PUT(m->cr, 1, F_CR);
+    PUT(m->dlam, 1, F_DLAM); PUT(m->epII, 2, F_EP); PUT(m->sig, ns, F_SIG); PUT(m->tau, ns, F_TAU);
+    PUT(m->dvij, d * d, F_DV); PUT(m->dFij, d * d, F_DF); PUT(m->Fij, d * d, F_F); PUT(m->bij, d * d, F_B);
+    PUT(m->eij, d * d, F_EPS); PUT(m->wij, d * d, F_W); PUT(m->sJij, d * d, F_SJ);
+#undef PUT
+    // tan/sin/cos of the friction angle, evaluated once on the host (material constants)
+    std::vector<double> t((size_t)3 * h->np);
+    for (int p = 0; p < h->np; ++p) {
+        t[p] = tan(m->phi[p]);
+        t[(size_t)h->np + p] = sin(m->phi[p]);
+        t[(size_t)2 * h->np + p] = cos(m->phi[p]);
+    }
+    CK(h, cudaMemcpyAsync(fld_ptr(h, F_TPHI), t.data(), t.size() * sizeof(double), cudaMemcpyHostToDevice, h->s));
+    if (m->u) std::memcpy(h->u.data(), m->u, h->u.size() * sizeof(double));
+    if (m->p) std::memcpy(h->pp.data(), m->p, h->pp.size() * sizeof(double));
+    if (m->duij) std::memcpy(h->du.data(), m->duij, h->du.size() * sizeof(double));
+    if (m->epV) std::memcpy(h->epV.data(), m->epV, h->epV.size() * sizeof(double));
+    std::memset(h->hctl, 0, sizeof(Ctl));
+    for (int i = 0; i < d; ++i) {
+        double v = m->vmax ? m->vmax[i] : 0.0;
+        long long bits;
+        std::memcpy(&bits, &v, sizeof(double));
+        h->hctl->vmax_bits[i] = (unsigned long long)bits;
+    }
+    CK(h, cudaMemcpyAsync(h->ctl, h->hctl, sizeof(Ctl), cudaMemcpyHostToDevice, h->s));
+    CK(h, cudaStreamSynchronize(h->s));
+    h->uploaded = true;
+    return EP_OK;
+}
+
+static ep_status read_ctl(ep_handle* h) {
+    CK(h, cudaMemcpyAsync(h->hctl, h->ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, h->s));
+    CK(h, cudaStreamSynchronize(h->s));
+    CK(h, cudaGetLastError());
+    return EP_OK;
+}
+
+static ep_status kernel_error(ep_handle* h) {
+    int e = h->hctl->err;
+    if (!e) return EP_OK;
+    char buf[160];
+    if (e == EP_ERR_INVALID_POSITION)
+        snprintf(buf, sizeof buf, "Invalid position: a B-spline node of point %d is outside the boundary table xB",
+                 h->hctl->err_info + 1);
+    else if (e == EP_ERR_NONFINITE)
+        snprintf(buf, sizeof buf, "non-finite state at point %d", h->hctl->err_info + 1);
+    else snprintf(buf, sizeof buf, "device error %d (info %d)", e, h->hctl->err_info);
+    return fail(h, (ep_status)e, buf);
+}
+
+ep_status epgpu_step(ep_handle* h, int32_t phase, double dt, const double* g, double* vmax_out) {
+    if (!h || !g) return EP_ERR_ARG;
+    if (!h->uploaded) return fail(h, EP_ERR_STATE, "step before upload");
+    if (phase != 0 && phase != 1) return fail(h, EP_ERR_ARG, "phase must be 0 or 1");
+    ep_status st;
+    if ((st = read_ctl(h)) != EP_OK) return st;
+    h->hctl->dt = dt;
+    for (int i = 0; i < 3; ++i) h->hctl->g[i] = i < h->dim ? g[i] : 0.0;
+    h->hctl->phase = phase;
+    CK(h, cudaMemcpyAsync(h->ctl, h->hctl, sizeof(Ctl), cudaMemcpyHostToDevice, h->s));
+    CK(h, cudaEventRecord(h->ev0, h->s));
+    launch_ctl_begin_step(h->ctl, h->dim, h->s);
+    Fp64Ctx ctx = h->ctx;
+    if (h->prof.on) {
+        ctx.prof = &h->prof;
+        h->prof.begin(h->s);
+    }
+    fp64_step(ctx, phase, h->s);
+    h->launches += 1;
+    CK(h, cudaEventRecord(h->ev1, h->s));
+    CK(h, cudaGetLastError());
+    if ((st = read_ctl(h)) != EP_OK) return st;
+    h->prof.collect();
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+    h->last_ms = ms;
+    h->steps += 1;
+    if (vmax_out)
+        for (int i = 0; i < h->dim; ++i) vmax_out[i] = bits_to_double(h->hctl->vmax_bits[i]);
+    return kernel_error(h);
+}
+
+static ep_status build_graph(ep_handle* h, int phase) {
+    if (h->graph[phase]) return EP_OK;
+    cudaGraph_t gr;
+    long long l0 = h->launches;
+    CK(h, cudaStreamBeginCapture(h->s, cudaStreamCaptureModeThreadLocal));
+    for (int k = 0; k < GRAPH_STEPS; ++k) {
+        launch_ctl_begin_run(h->ctl, h->ctx.g, h->cm.c, h->s);
+        fp64_step(h->ctx, phase, h->s);
+        launch_ctl_end(h->ctl, h->s);
+    }
+    cudaError_t e = cudaStreamEndCapture(h->s, &gr);
+    h->graph_kernels[phase] = h->launches - l0 + 2LL * GRAPH_STEPS;   // + control kernels
+    h->launches = l0;                                                    // capturing launches nothing
+    if (e != cudaSuccess) return cuda_fail(h, e, "graph capture");
+    e = cudaGraphInstantiate(&h->graph[phase], gr, 0);
+    cudaGraphDestroy(gr);
+    if (e != cudaSuccess) return cuda_fail(h, e, "graph instantiate");
+    return EP_OK;
+}
+
+ep_status epgpu_run(ep_handle* h, int32_t phase, double T, double tg, double* t_inout, int64_t* nsteps_out) {
+    if (!h || !t_inout) return EP_ERR_ARG;
+    if (!h->uploaded) return fail(h, EP_ERR_STATE, "run before upload");
+    if (phase != 0 && phase != 1) return fail(h, EP_ERR_ARG, "phase must be 0 or 1");
+    ep_status st;
+    if ((st = read_ctl(h)) != EP_OK) return st;
+    if (h->hctl->err) return kernel_error(h);
+    h->hctl->t = *t_inout;
+    h->hctl->T = T;
+    h->hctl->tg = tg;
+    h->hctl->phase = phase;
+    h->hctl->active = 1;
+    h->hctl->nsteps = 0;
+    CK(h, cudaMemcpyAsync(h->ctl, h->hctl, sizeof(Ctl), cudaMemcpyHostToDevice, h->s));
+    if ((st = build_graph(h, phase)) != EP_OK) return st;
+    CK(h, cudaEventRecord(h->ev0, h->s));
+    int launched = 0;
+    while (true) {
+        CK(h, cudaGraphLaunch(h->graph[phase], h->s));
+        ++launched;
+        if ((st = read_ctl(h)) != EP_OK) return st;
+        if (!h->hctl->active || h->hctl->err) break;
+        if (launched >= (1 << 24)) return fail(h, EP_ERR_TIMEOUT, "time loop did not reach T after 2^28 steps");
+    }
+    CK(h, cudaEventRecord(h->ev1, h->s));
+    CK(h, cudaEventSynchronize(h->ev1));
+    h->launches += launched * h->graph_kernels[phase];
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+    h->last_ms = ms;
+    *t_inout = h->hctl->t;
+    h->t = h->hctl->t;
+    h->steps += h->hctl->nsteps;
+    if (nsteps_out) *nsteps_out = h->hctl->nsteps;
+    return kernel_error(h);
+}
+
+ep_status epgpu_download(ep_handle* h, ep_mpts_view* m) {
+    if (!h || !m) return EP_ERR_ARG;
+    if (m->nmp != h->np || m->ndim != h->dim) return fail(h, EP_ERR_ARG, "mpts.nmp/ndim differ from create");
+    const int d = h->dim, ns = h->nstr;
+    ep_status st;
+    if ((st = read_ctl(h)) != EP_OK) return st;
+#define GET(ptr, k, f) if ((st = get_aos(h, fld_ptr(h, (f)), (k), (ptr))) != EP_OK) return st
+    GET(m->x, d, F_X); GET(m->v, d, F_V); GET(m->l, d, F_L); GET(m->l0, d, F_L0);
+    GET(m->n0, 1, F_N0); GET(m->n, 1, F_N); GET(m->Omega0, 1, F_OM0); GET(m->Omega, 1, F_OM); GET(m->dJ, 1, F_DJ);
+    GET(m->J, 1, F_J); GET(m->rho0, 1, F_RHO0); GET(m->rho, 1, F_RHO); GET(m->c0, 1, F_C0); GET(m->cr, 1, F_CR);
+    GET(m->dlam, 1, F_DLAM); GET(m->epII, 2, F_EP); GET(m->sig, ns, F_SIG); GET(m->tau, ns, F_TAU);
+    GET(m->dvij, d * d, F_DV); GET(m->dFij, d * d, F_DF); GET(m->Fij, d * d, F_F); GET(m->bij, d * d, F_B);
+    GET(m->eij, d * d, F_EPS); GET(m->wij, d * d, F_W); GET(m->sJij, d * d, F_SJ);
+#undef GET
+    if (m->vmax)
+        for (int i = 0; i < d; ++i) m->vmax[i] = bits_to_double(h->hctl->vmax_bits[i]);
+    if (m->u) std::memcpy(m->u, h->u.data(), h->u.size() * sizeof(double));
+    if (m->p) std::memcpy(m->p, h->pp.data(), h->pp.size() * sizeof(double));
+    if (m->duij) std::memcpy(m->duij, h->du.data(), h->du.size() * sizeof(double));
+    if (m->epV) std::memcpy(m->epV, h->epV.data(), h->epV.size() * sizeof(double));
+    if (m->p2e || m->p2n) {
+        std::vector<int> c(h->np);
+        if (h->np) {
+            CK(h, cudaMemcpyAsync(c.data(), h->ctx.P.p2e, sizeof(int) * h->np, cudaMemcpyDeviceToHost, h->s));
+            CK(h, cudaStreamSynchronize(h->s));
+        }
+        for (int p = 0; p < h->np; ++p) {
+            if (m->p2e) m->p2e[p] = (int64_t)c[p] + 1;
+            if (!m->p2n) continue;
+            int e[3];
+            if (d == 2) { e[0] = c[p] / (int)h->nel[1]; e[1] = c[p] % (int)h->nel[1]; }
+            else {
+                int nzx = (int)(h->nel[2] * h->nel[0]);
+                e[1] = c[p] / nzx;
+                int r = c[p] % nzx;
+                e[0] = r / (int)h->nel[2];
+                e[2] = r % (int)h->nel[2];
+            }
+            for (int s = 0; s < h->nn; ++s) {
+                int o[3], i[3];
+                if (d == 2) { o[0] = s >> 2; o[1] = s & 3; }
+                else { o[1] = s >> 4; o[0] = (s >> 2) & 3; o[2] = s & 3; }
+                bool ok = c[p] >= 0;
+                for (int dd = 0; dd < d; ++dd) {
+                    i[dd] = e[dd] - 1 + o[dd];
+                    ok = ok && i[dd] >= 0 && i[dd] < h->nno[dd];
+                }
+                long long id = 0;
+                if (ok) id = (d == 2) ? i[1] + h->nno[1] * (long long)i[0]
+                                      : i[2] + h->nno[2] * (long long)i[0] + h->nno[2] * h->nno[0] * (long long)i[1];
+                m->p2n[s + (int64_t)h->nn * p] = ok ? id + 1 : 0;
+            }
+        }
+    }
+    return EP_OK;
+}
+
+ep_status epgpu_download_mesh(ep_handle* h, ep_mesh_fields* f) {
+    if (!h || !f) return EP_ERR_ARG;
+    const int d = h->dim;
+    const size_t Nn = h->nnode;
+    std::vector<double> buf((size_t)(1 + 4 * d + 1) * Nn);
+    CK(h, cudaMemcpyAsync(buf.data(), h->nbuf, buf.size() * sizeof(double), cudaMemcpyDeviceToHost, h->s));
+    CK(h, cudaStreamSynchronize(h->s));
+    auto aos = [&](size_t base, double* out) {
+        if (!out) return;
+        for (size_t n = 0; n < Nn; ++n)
+            for (int i = 0; i < d; ++i) out[i + d * n] = buf[base + i * Nn + n];
+    };
+    if (f->mi) std::memcpy(f->mi, buf.data(), Nn * sizeof(double));
+    aos(1 * Nn, f->p);
+    aos((1 + d) * Nn, f->oobf);
+    aos((1 + 2 * (size_t)d) * Nn, f->a);
+    aos((1 + 3 * (size_t)d) * Nn, f->v);
+    if (f->dJ) std::memcpy(f->dJ, buf.data() + (1 + 4 * (size_t)d) * Nn, Nn * sizeof(double));
+    return EP_OK;
+}
+
+ep_status epgpu_profile(ep_handle* h, int32_t enable) {
+    if (!h) return EP_ERR_ARG;
+    h->prof.on = enable != 0;
+    if (enable) h->prof.acc.clear();
+    return EP_OK;
+}
+
+ep_status epgpu_profile_read(ep_handle* h, ep_kernel_time* out, int32_t cap, int32_t* count) {
+    if (!h || !count || (cap > 0 && !out)) return EP_ERR_ARG;
+    int i = 0;
+    for (auto& kv : h->prof.acc) {
+        if (i < cap) {
+            std::memset(out[i].name, 0, sizeof(out[i].name));
+            std::strncpy(out[i].name, kv.first.c_str(), sizeof(out[i].name) - 1);
+            out[i].launches = kv.second.first;
+            out[i].total_ms = kv.second.second;
+        }
+        ++i;
+    }
+    *count = i;
+    return EP_OK;
+}
+
+ep_status epgpu_stats(ep_handle* h, ep_stats* out) {
+    if (!h || !out) return EP_ERR_ARG;
+    ep_status st;
+    if ((st = read_ctl(h)) != EP_OK) return st;
+    out->steps = h->steps;
+    out->launches = h->launches;
+    out->device_ms = h->last_ms;
+    out->t = h->t;
+    out->plastic = h->hctl->plastic;
+    return EP_OK;
+}
+
+}  // extern "C"

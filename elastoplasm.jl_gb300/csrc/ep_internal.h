@@ -1,0 +1,94 @@
+// ep_internal.h -- host-side launchers shared between the translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <map>
+#include <string>
+#include <vector>
+
+#include "ep_dev.cuh"
+
+namespace ep {
+
+// CUDA-event timers between consecutive kernels of a step (profiling mode).
+struct Prof {
+    bool on = false;
+    int n = 0;
+    std::vector<cudaEvent_t> ev;
+    std::vector<const char*> name;
+    std::map<std::string, std::pair<long long, double>> acc;
+    void begin(cudaStream_t s) {
+        n = 0;
+        mark("begin", s);
+    }
+    void mark(const char* nm, cudaStream_t s) {
+        if (!on) return;
+        if (n >= (int)ev.size()) {
+            cudaEvent_t e;
+            cudaEventCreate(&e);
+            ev.push_back(e);
+            name.push_back(nullptr);
+        }
+        cudaEventRecord(ev[n], s);
+        name[n] = nm;
+        ++n;
+    }
+    // after the stream was synchronised
+    void collect() {
+        if (!on) return;
+        for (int i = 1; i < n; ++i) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, ev[i - 1], ev[i]);
+            auto& a = acc[name[i]];
+            a.first += 1;
+            a.second += ms;
+        }
+        n = 0;
+    }
+    ~Prof() {
+        for (auto e : ev) cudaEventDestroy(e);
+    }
+};
+
+// Exclusive prefix sum of in[0..n) into out[0..n]; out[n] = total.  `tmp`
+// must hold scan_tmp_ints(n) ints.  Works in place (in == out) too.
+int scan_tmp_ints(int n);
+void launch_exclusive_scan(const int* in, int* out, int n, int* tmp, cudaStream_t s);
+
+// Sort every segment data[start[i]..start[i+1]) ascending (warp per segment).
+void launch_segsort(const int* start, int nseg, int* data, cudaStream_t s);
+
+// Counting-sort placement of points into cells: cell_list[cell_start[c] + k]
+// for the k-th point of cell c seen by the atomic cursor (order fixed by the
+// following launch_segsort).
+void launch_place_cells(const int* p2e, int np, const int* cell_start, int* cursor, int* cell_list,
+                        const Ctl* ctl, cudaStream_t s);
+
+// Point -> cell (the reference's clamp(fld(x - x0, h), 0, nel-1), tplgy.jl:43-96)
+// with a per-cell count; x is dim arrays of np doubles.
+void launch_bin_points(const Geo& g, const double* const* x, int np, int* p2e, int* cell_count,
+                       Ctl* ctl, cudaStream_t s);
+
+// FP64 step launchers (ep_fp64.cu)
+struct Fp64Ctx {
+    Cfg cf;
+    Geo g;
+    Mat mt;
+    Ctl* ctl;
+    P64 P;
+    N64 N;
+    Sort S;
+    int np;
+    long long* launches;
+    Prof* prof;
+};
+void fp64_step(const Fp64Ctx& c, int phase, cudaStream_t s);
+void fp64_check_finite(const Fp64Ctx& c, cudaStream_t s);
+
+// control-block kernels (ep_fp64.cu)
+void launch_ctl_begin_run(Ctl* ctl, const Geo& g, double c, cudaStream_t s);
+void launch_ctl_begin_step(Ctl* ctl, int dim, cudaStream_t s);
+void launch_ctl_end(Ctl* ctl, cudaStream_t s);
+
+}  // namespace ep

@@ -1,0 +1,94 @@
+"""Python driver of the C-ABI library: one device context per (mesh, points, instr).
+
+``Engine`` is what the reference's workflow functions would hold after
+``kwargser`` built the kernel table: ``step`` replaces one MPM cycle
+(workflow/worflow.jl:34-36, 80-82) and ``run`` one checkpoint window of the
+time loop (worflow.jl:27-39, 73-85).  Everything goes through the exported C
+functions of libepgpu.so; there is no CPU fallback: constructing an Engine
+without the built library or without a GPU raises.
+"""
+from __future__ import annotations
+
+import copy
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+
+
+class Engine:
+    def __init__(self, ic: dict, instr: dict, lib_path: str | None = None):
+        self.lib = abi.load_library(lib_path)
+        self.mesh = ic["mesh"]
+        self.mpts = ic["mpts"]
+        self.cmpr = ic["cmpr"]
+        self._cfg = abi.make_cfg(instr)
+        self._cm = abi.make_cmpr(self.cmpr)
+        self._mv = abi.MeshView(self.mesh)
+        h = C.c_void_p()
+        st = self.lib.epgpu_create(C.byref(self._cfg), C.byref(self._cm), C.byref(self._mv.view),
+                                   int(self.mpts.nmp), C.byref(h))
+        if st != abi.EP_OK:
+            raise abi.EPError(st, self.lib.epgpu_last_error(None).decode())
+        self.h = h
+        self.upload(self.mpts)
+
+    # -- plumbing
+    def _check(self, st: int):
+        if st != abi.EP_OK:
+            raise abi.EPError(st, self.lib.epgpu_last_error(self.h).decode())
+
+    def upload(self, mpts):
+        self._check(self.lib.epgpu_upload(self.h, C.byref(abi.mpts_view(mpts))))
+
+    def download(self, mpts=None):
+        mpts = mpts or self.mpts.copy()
+        self._check(self.lib.epgpu_download(self.h, C.byref(abi.mpts_view(mpts, with_topology=True))))
+        return mpts
+
+    def download_mesh(self, mesh=None):
+        mesh = mesh or copy.deepcopy(self.mesh)
+        self._check(self.lib.epgpu_download_mesh(self.h, C.byref(abi.mesh_fields(mesh))))
+        return mesh
+
+    # -- the step
+    def step(self, phase: int, dt: float, g) -> np.ndarray:
+        g = np.zeros(3) + np.pad(np.asarray(g, dtype=np.float64), (0, 3 - len(g)))
+        vmax = np.zeros(3)
+        self._check(self.lib.epgpu_step(self.h, int(phase), float(dt), g.ctypes.data_as(C.POINTER(C.c_double)),
+                                        vmax.ctypes.data_as(C.POINTER(C.c_double))))
+        return vmax[: self.mpts.ndim]
+
+    def run(self, phase: int, T: float, tg: float, t: float):
+        tt = C.c_double(t)
+        n = C.c_int64(0)
+        self._check(self.lib.epgpu_run(self.h, int(phase), float(T), float(tg), C.byref(tt), C.byref(n)))
+        return tt.value, n.value
+
+    def stats(self) -> dict:
+        s = abi.ep_stats()
+        self._check(self.lib.epgpu_stats(self.h, C.byref(s)))
+        return {"steps": s.steps, "launches": s.launches, "device_ms": s.device_ms, "t": s.t,
+                "plastic": s.plastic}
+
+    def profile(self, enable: bool = True):
+        self._check(self.lib.epgpu_profile(self.h, int(enable)))
+
+    def kernel_times(self) -> dict:
+        n = C.c_int32(0)
+        self._check(self.lib.epgpu_profile_read(self.h, None, 0, C.byref(n)))
+        arr = (abi.ep_kernel_time * max(n.value, 1))()
+        self._check(self.lib.epgpu_profile_read(self.h, arr, n.value, C.byref(n)))
+        return {arr[i].name.decode(): (arr[i].launches, arr[i].total_ms) for i in range(n.value)}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.epgpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

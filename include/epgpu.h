@@ -1,0 +1,217 @@
+/*
+ * epgpu.h -- C ABI of the GB300 explicit MPM step for ElastoPlasm.jl.
+ *
+ * The library replaces the body of the reference's time loop: one call of
+ * `shpfun(mpts,mesh,instr); mapsto(mpts,mesh,g,dt,instr); elasto|elastoplast(...)`
+ * (src/home/program/workflow/worflow.jl:34-36 and 80-82) and, for whole
+ * checkpoint windows, the `while T > time.t[1]` loop around it
+ * (worflow.jl:27-39, 73-85).  The kernels it runs are selected by the same
+ * switches that build the reference's kernel table `instr.cairn`
+ * (src/home/api/kwargser.jl:49-60; require.jl:34-88).
+ *
+ * Conventions (mirroring the Julia side, which calls this through `ccall`):
+ *  - host arrays are caller-owned and column-major, exactly the `Point`/`Mesh`
+ *    fields of src/boot/needs/types.jl:38-168 (e.g. `x` is dim x nmp, stored
+ *    point by point); node and element ids are 1-based Int64, 0 = none;
+ *  - the library keeps its own device copy (structure of arrays) between
+ *    `epgpu_upload` and `epgpu_download`;
+ *  - every call returns an `ep_status`; no exception or signal crosses the
+ *    ABI; `epgpu_last_error` gives the message of the last failure;
+ *  - a handle is used by one host thread at a time and owns one CUDA stream.
+ */
+#ifndef EPGPU_H
+#define EPGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EPGPU_ABI_VERSION 1
+
+typedef enum ep_status {
+    EP_OK = 0,
+    EP_ERR_ARG = 1,              /* null pointer, bad size or enum value */
+    EP_ERR_UNSUPPORTED = 2,      /* switch combination not built; the reference throws
+                                    ArgumentError (shpfun.jl:50, mapsto.jl:44, plast.jl:31) */
+    EP_ERR_NONFINITE = 3,        /* NaN/Inf found in the particle state after a step */
+    EP_ERR_TIMEOUT = 5,          /* a bounded device wait gave up */
+    EP_ERR_CUDA = 6,             /* CUDA runtime failure */
+    EP_ERR_INVALID_POSITION = 7, /* B-spline node outside its boundary table: the
+                                    reference's error("Invalid position") (bsmpm.jl:75) */
+    EP_ERR_NOMEM = 8,
+    EP_ERR_STATE = 9             /* calls out of order (step before upload, ...) */
+} ep_status;
+
+/* instr.basis.which (require.jl:39) */
+enum { EP_BASIS_BSMPM = 0, EP_BASIS_GIMPM = 1, EP_BASIS_SMPM = 2 };
+/* instr.basis.how: GIMP domain update (update.jl:7-28) */
+enum { EP_HOW_NONE = 0, EP_HOW_UNDEFORMED = 1, EP_HOW_DETFIJ = 2, EP_HOW_FII = 3, EP_HOW_UII = 4,
+       EP_HOW_DETDFIJ = 5, EP_HOW_DFII = 6, EP_HOW_DUII = 7 };
+/* instr.fwrk.deform / trsfr (require.jl:44-45) */
+enum { EP_DEFORM_FINITE = 0, EP_DEFORM_INFINITESIMAL = 1 };
+enum { EP_TRSFR_STD = 0, EP_TRSFR_TPIC = 1 };
+/* instr.plast.constitutive (require.jl:68) */
+enum { EP_CONS_DP = 0, EP_CONS_J2 = 1 };
+/* device arithmetic */
+enum { EP_PREC_FP64 = 0, EP_PREC_MIXED = 1 };
+/* workflow phase (worflow.jl:23 elastodynamic!, :68 elastoplastic!) */
+enum { EP_PHASE_ELASTODYNAMIC = 0, EP_PHASE_ELASTOPLASTIC = 1 };
+
+/* Switches of `instr` that select kernels (require.jl:34-88). */
+typedef struct ep_cfg {
+    int32_t dim;           /* 2 or 3 = length(L) */
+    int32_t basis;         /* EP_BASIS_*            basis.which */
+    int32_t how;           /* EP_HOW_*              basis.how (gimpm only) */
+    int32_t ghost;         /* basis.ghost (mesh already built with it; informative) */
+    int32_t deform;        /* EP_DEFORM_*           fwrk.deform */
+    int32_t trsfr;         /* EP_TRSFR_*            fwrk.trsfr */
+    double  C_pf;          /* fwrk.C_pf: FLIP fraction of the PIC/FLIP blend */
+    int32_t musl;          /* fwrk.musl */
+    int32_t locking;       /* fwrk.locking: F-bar volumetric locking fix */
+    double  damping;       /* fwrk.damping: grid viscous damping */
+    int32_t constitutive;  /* EP_CONS_*             plast.constitutive */
+    int32_t nonloc;        /* nonloc.status */
+    double  nonloc_ls;     /* nonloc.ls: nonlocal length scale [m] */
+    int32_t precision;     /* EP_PREC_FP64 (drop-in, oracle order) | EP_PREC_MIXED */
+    int32_t jaumann;       /* 0: reference rate (its spin term is identically zero,
+                              elast.jl:77); 1: objective Jaumann rate (not the reference) */
+} ep_cfg;
+
+/* Material constants: the `cmpr` NamedTuple of setup_cmpr (setup_cmpr.jl:120-143). */
+typedef struct ep_cmpr {
+    double E, nu, Kc, Gc;
+    double Del[36];        /* nstr x nstr elastic stiffness, column-major (nstr = 3 | 6) */
+    double Hp;             /* softening/hardening modulus */
+    double c0, cr;         /* peak and residual cohesion defaults (per point values in mpts) */
+    double phi0, phir;
+    double rho0;
+    double c;              /* elastic wave speed used by the CFL step (physics.jl:21-26) */
+} ep_cmpr;
+
+/* Mesh geometry (types.jl:141-168). */
+typedef struct ep_mesh_view {
+    int64_t dim;
+    int64_t nel[4];        /* per direction then total, as mesh.nel: [nx, (ny,) nz, total] */
+    int64_t nno[4];        /* same for nodes */
+    int64_t nn;            /* stencil size 4^dim */
+    double  h[3];
+    double  x0[3];
+    const double*  x;      /* dim x nno[dim]   mesh.x */
+    const double*  xB;     /* dim x 2          mesh.xB */
+    const uint8_t* bcs;    /* dim x nno[dim]   mesh.bcs.status (Julia Bool) */
+    const int64_t* e2n;    /* nn x nel[dim]    mesh.e2n, or NULL; checked when given */
+} ep_mesh_view;
+
+/* Nodal fields for download (types.jl:151-160). */
+typedef struct ep_mesh_fields {
+    double* mi;            /* nno      lumped mass */
+    double* p;             /* dim x nno momentum */
+    double* v;             /* dim x nno velocity */
+    double* a;             /* dim x nno acceleration */
+    double* oobf;          /* dim x nno out-of-balance force */
+    double* dJ;            /* nno      first nno linear slots of mesh.ΔJ (volumetric.jl:8) */
+} ep_mesh_fields;
+
+/* Material-point state (types.jl:38-105); any pointer may be NULL on download. */
+typedef struct ep_mpts_view {
+    int64_t ndim, nmp;
+    double* vmax;                                   /* dim */
+    double *x, *l0, *l;                             /* dim x nmp */
+    double *n0, *n, *Omega0, *Omega, *dJ, *J;       /* nmp */
+    double *u, *v, *p;                              /* dim x nmp (u, p not read by the step) */
+    double *rho0, *rho, *c0, *cr, *phi, *dlam;      /* nmp */
+    double *epII;                                   /* 2 x nmp: accumulated, nonlocal */
+    double *epV;                                    /* nmp */
+    double *sig, *tau;                              /* nstr x nmp Voigt (xx,yy,[zz,yz,xz,]xy) */
+    double *dvij, *duij, *dFij, *Fij, *bij, *eij, *wij, *sJij; /* dim x dim x nmp */
+    int64_t *p2e;                                   /* nmp, 1-based (download only) */
+    int64_t *p2n;                                   /* nn x nmp, 1-based (download only) */
+} ep_mpts_view;
+
+typedef struct ep_stats {
+    int64_t steps;          /* MPM cycles executed since create */
+    int64_t launches;       /* kernels launched since create */
+    double  device_ms;      /* device time of the last epgpu_run/epgpu_step call */
+    double  t;              /* simulated time after the last epgpu_run */
+    int64_t plastic;        /* points with Δλ != 0 after the last step */
+} ep_stats;
+
+/* Per-kernel device time, accumulated while profiling is on (epgpu_profile). */
+typedef struct ep_kernel_time {
+    char    name[32];
+    int64_t launches;
+    double  total_ms;       /* sum of CUDA-event durations on the handle's stream */
+} ep_kernel_time;
+
+typedef struct ep_handle ep_handle;
+
+/* Library version string. */
+const char* epgpu_version(void);
+
+/* Build a device context for `nmp` points on `mesh` with switches `cfg`
+ * (replaces kwargser's kernel table, kwargser.jl:49-60, and the arrays of
+ * setup_mesh/setup_mpts).  Returns EP_ERR_UNSUPPORTED for switch combinations
+ * the reference rejects or this library does not build (apic, MC, camC, 1d). */
+ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_view* mesh,
+                       int64_t nmp, ep_handle** out);
+
+/* Copy the point state in (host AoS -> device SoA). */
+ep_status epgpu_upload(ep_handle* h, const ep_mpts_view* mpts);
+
+/* One MPM cycle with the caller's dt and gravity g[dim]: shpfun + mapsto +
+ * elasto (phase 0) or elastoplast (phase 1) (worflow.jl:34-36, 80-82).
+ * vmax is reset first and the new per-direction maximum |v| is returned in
+ * vmax_out[dim] (the reference's mpts.vmax after n2p, n2p.jl:37). */
+ep_status epgpu_step(ep_handle* h, int32_t phase, double dt, const double* g, double* vmax_out);
+
+/* The reference's inner time loop for one checkpoint window:
+ *   while T > t: dt = min(0.5 max_i h_i/(vmax_i+c), T-t); vmax = 0;
+ *                g = phase 0 ? [0..,-9.81 t/tg] (t <= tg) : [0..,-9.81];
+ *                step; t += dt
+ * (physics.jl:21-26, 80-90; worflow.jl:28-39, 74-85).  The loop runs on the
+ * device in CUDA graphs; *t_inout is read and written back.  nsteps_out may be NULL. */
+ep_status epgpu_run(ep_handle* h, int32_t phase, double T, double tg, double* t_inout,
+                    int64_t* nsteps_out);
+
+/* Copy the point state out (device SoA -> host AoS); NULL fields are skipped. */
+ep_status epgpu_download(ep_handle* h, ep_mpts_view* mpts);
+
+/* Copy the nodal fields of the last step out; NULL fields are skipped. */
+ep_status epgpu_download_mesh(ep_handle* h, ep_mesh_fields* f);
+
+ep_status epgpu_stats(ep_handle* h, ep_stats* out);
+
+/* Per-kernel CUDA-event timers for epgpu_step (the reference only measures whole
+ * kernel groups with BenchmarkTools, test/testset/test_performance.jl:1-58).
+ * enable = 1 resets and starts the accumulators, 0 stops them. */
+ep_status epgpu_profile(ep_handle* h, int32_t enable);
+
+/* Copy up to `cap` accumulated kernel entries out; *count receives how many exist. */
+ep_status epgpu_profile_read(ep_handle* h, ep_kernel_time* out, int32_t cap, int32_t* count);
+
+/* Release every device resource of the handle. */
+ep_status epgpu_destroy(ep_handle* h);
+
+/* Message of the last failure on `h` (or of the last epgpu_create failure when h is NULL). */
+const char* epgpu_last_error(const ep_handle* h);
+
+/* Stand-alone particle binning (the topology kernel p2e2n_{2,3}d, tplgy.jl:43-96)
+ * as a stable counting sort, on device pointers.
+ *   x_dev       dim arrays of nmp doubles, direction-major (x[0..nmp), then y/z)
+ *   p2e_dev     out: nmp int32, 0-based cell of each point (clamped like the reference)
+ *   cell_start  out: ncell+1 int32 offsets into cell_list
+ *   cell_list   out: nmp int32 point ids, grouped by cell, ascending inside a cell
+ * ncell = prod(nel[0..dim)).  The call allocates its scratch (per-cell counters)
+ * on the device and frees it before returning; it runs on `stream`
+ * (cudaStream_t, NULL = legacy default stream) and synchronises it. */
+ep_status epgpu_bin_cells(int32_t dim, const int64_t* nel, const double* h, const double* x0,
+                          const double* x_dev, int64_t nmp, int32_t* p2e_dev,
+                          int32_t* cell_start_dev, int32_t* cell_list_dev, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* EPGPU_H */
