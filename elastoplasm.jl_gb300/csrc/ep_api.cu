@@ -54,6 +54,8 @@ struct ep_handle {
     Prof prof;
 };
 
+void ep::set_global_error(const char* msg) { g_create_error = msg ? msg : ""; }
+
 static double bits_to_double(unsigned long long b) {
     double v;
     std::memcpy(&v, &b, sizeof(double));

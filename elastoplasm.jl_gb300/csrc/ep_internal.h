@@ -70,6 +70,9 @@ void launch_place_cells(const int* p2e, int np, const int* cell_start, int* curs
 void launch_bin_points(const Geo& g, const double* const* x, int np, int* p2e, int* cell_count,
                        Ctl* ctl, cudaStream_t s);
 
+// Message returned by epgpu_last_error(NULL) for calls without a handle (ep_api.cu).
+void set_global_error(const char* msg);
+
 // FP64 step launchers (ep_fp64.cu)
 struct Fp64Ctx {
     Cfg cf;

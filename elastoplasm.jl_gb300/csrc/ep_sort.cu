@@ -6,7 +6,9 @@
 // with atomics, exclusive-scan the counts, place each point with an atomic
 // cursor, then sort every cell's segment by point id (warp bitonic sort), so
 // the result is independent of atomic arrival order: a stable counting sort.
+#include <atomic>
 #include <climits>
+#include <cstdio>
 
 #include "../../include/epgpu.h"
 #include "ep_internal.h"
@@ -262,6 +264,100 @@ extern "C" ep_status epgpu_bin_cells(int32_t dim, const int64_t* nel, const doub
     launch_segsort(cell_start_dev, nc, cell_list_dev, s);
     cudaFreeAsync(scratch, s);
     cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return EP_ERR_CUDA;
+    e = cudaGetLastError();
+    return e == cudaSuccess ? EP_OK : EP_ERR_CUDA;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of the stand-alone binning (include/epgpu.h).
+// Its scratch -- per-cell counters, per-cell cursors and the scan's block
+// totals -- is this file-scope device array, sized for EPGPU_NOALLOC_MAX_CELLS
+// cells.  Host code must not pass `g_bin_scratch` itself to a kernel (on the
+// host the name is only a stand-in, not a device address): the device address
+// is looked up once per device with cudaGetSymbolAddress and cached.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int NOALLOC_TMP_INTS = (EPGPU_NOALLOC_MAX_CELLS + ep::SCAN_CHUNK - 1) / ep::SCAN_CHUNK + 1;
+constexpr int NOALLOC_SCRATCH_INTS = 2 * EPGPU_NOALLOC_MAX_CELLS + NOALLOC_TMP_INTS;
+
+static __device__ __align__(256) int g_bin_scratch[NOALLOC_SCRATCH_INTS];
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::atomic<int*> g_scratch_addr[NOALLOC_MAX_DEVICES];
+
+// Device address of g_bin_scratch on the current device (set-up on first use).
+cudaError_t noalloc_scratch(int** out) {
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return cudaErrorInvalidDevice;
+    int* p = g_scratch_addr[dev].load(std::memory_order_acquire);
+    if (!p) {
+        void* q = nullptr;
+        e = cudaGetSymbolAddress(&q, g_bin_scratch);
+        if (e != cudaSuccess) return e;
+        p = (int*)q;
+        g_scratch_addr[dev].store(p, std::memory_order_release);
+    }
+    *out = p;
+    return cudaSuccess;
+}
+
+}  // namespace
+
+extern "C" ep_status epgpu_bin_cells_noalloc(int32_t dim, const int64_t* nel, const double* h, const double* x0,
+                                             const double* x_dev, int64_t nmp, int32_t* p2e_dev,
+                                             int32_t* cell_start_dev, int32_t* cell_list_dev, void* stream) {
+    using namespace ep;
+    if ((dim != 2 && dim != 3) || !nel || !h || !x0 || nmp < 0) return EP_ERR_ARG;
+    if (nmp > 0 && (!x_dev || !p2e_dev || !cell_list_dev)) return EP_ERR_ARG;
+    if (!cell_start_dev) return EP_ERR_ARG;
+    long long ncell = 1;
+    for (int d = 0; d < dim; ++d) {
+        if (nel[d] <= 0 || !(h[d] > 0.0)) return EP_ERR_ARG;
+        ncell *= nel[d];
+        if (ncell > EPGPU_NOALLOC_MAX_CELLS) break;
+    }
+    if (ncell > EPGPU_NOALLOC_MAX_CELLS) {
+        char msg[160];
+        snprintf(msg, sizeof msg,
+                 "epgpu_bin_cells_noalloc: the mesh has more than the %d cells its static scratch holds; "
+                 "use epgpu_bin_cells", EPGPU_NOALLOC_MAX_CELLS);
+        set_global_error(msg);
+        return EP_ERR_ARG;
+    }
+    if (nmp > INT_MAX) return EP_ERR_ARG;
+    int* scratch = nullptr;
+    cudaError_t e = noalloc_scratch(&scratch);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        set_global_error("epgpu_bin_cells_noalloc: cudaGetSymbolAddress of the static scratch failed");
+        return EP_ERR_CUDA;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    Geo g{};
+    g.dim = dim;
+    for (int d = 0; d < dim; ++d) {
+        g.nel[d] = (int)nel[d];
+        g.h[d] = h[d];
+        g.x0[d] = x0[d];
+    }
+    g.ncell = (int)ncell;
+    const int np = (int)nmp;
+    const int nc = (int)ncell;
+    int* count = scratch;
+    int* cursor = scratch + nc;
+    int* tmp = scratch + 2 * (size_t)nc;
+    // the array keeps the previous call's contents: clear the counters and cursors
+    cudaMemsetAsync(scratch, 0, sizeof(int) * 2 * (size_t)nc, s);
+    const double* xs[3] = {x_dev, x_dev + nmp, dim == 3 ? x_dev + 2 * nmp : nullptr};
+    launch_bin_points(g, xs, np, p2e_dev, count, nullptr, s);
+    launch_exclusive_scan(count, cell_start_dev, nc, tmp, s);
+    launch_place_cells(p2e_dev, np, cell_start_dev, cursor, cell_list_dev, nullptr, s);
+    launch_segsort(cell_start_dev, nc, cell_list_dev, s);
+    e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return EP_ERR_CUDA;
     e = cudaGetLastError();
     return e == cudaSuccess ? EP_OK : EP_ERR_CUDA;

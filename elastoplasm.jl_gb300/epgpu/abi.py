@@ -160,6 +160,8 @@ SIGNATURES = {
     "epgpu_last_error": (C.c_char_p, [C.c_void_p]),
     "epgpu_bin_cells": (C.c_int, [C.c_int32, _I64, _D, _D, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
                                   C.c_void_p, C.c_void_p]),
+    "epgpu_bin_cells_noalloc": (C.c_int, [C.c_int32, _I64, _D, _D, C.c_void_p, C.c_int64, C.c_void_p,
+                                          C.c_void_p, C.c_void_p, C.c_void_p]),
 }
 
 _lib = None

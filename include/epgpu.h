@@ -210,6 +210,28 @@ ep_status epgpu_bin_cells(int32_t dim, const int64_t* nel, const double* h, cons
                           const double* x_dev, int64_t nmp, int32_t* p2e_dev,
                           int32_t* cell_start_dev, int32_t* cell_list_dev, void* stream);
 
+/* Largest cell count epgpu_bin_cells_noalloc accepts (prod(nel[0..dim))). */
+#define EPGPU_NOALLOC_MAX_CELLS 524288
+
+/* epgpu_bin_cells without any device allocation.  It has no counterpart in
+ * the reference: it exists for callers that must not allocate device memory
+ * during the call -- a host framework whose caching allocator already owns
+ * the device memory budget (CUDA.jl's pool, PyTorch), or a pipeline where
+ * cudaMalloc/cudaFree would serialise the device.  The scratch (per-cell
+ * counters and cursors, scan totals: about 4 MB) is one static array in
+ * device memory, held by every GPU that loads the library until the process
+ * exits.  The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture.  All calls share the array and clear what must
+ * start at zero, so calls that overlap on the GPU (different streams or
+ * threads at the same time) race: serialise them.  Inputs, outputs, the
+ * stream and the synchronisation are as for epgpu_bin_cells; a mesh with
+ * more than EPGPU_NOALLOC_MAX_CELLS cells returns EP_ERR_ARG with the reason
+ * in epgpu_last_error(NULL). */
+ep_status epgpu_bin_cells_noalloc(int32_t dim, const int64_t* nel, const double* h, const double* x0,
+                                  const double* x_dev, int64_t nmp, int32_t* p2e_dev,
+                                  int32_t* cell_start_dev, int32_t* cell_list_dev, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
