@@ -52,6 +52,9 @@ struct ep_handle {
     std::string err;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     Prof prof;
+    bool mixed = false;
+    MixedCtx mx{};
+    std::vector<unsigned char> mx_impl;   // host image of the mixed kernels' argument block
 };
 
 void ep::set_global_error(const char* msg) { g_create_error = msg ? msg : ""; }
@@ -160,7 +163,7 @@ static double* fld_ptr(ep_handle* h, Fld f) {
 
 extern "C" {
 
-const char* epgpu_version(void) { return "epgpu 0.1 (sm_103a, FP64 oracle-order step)"; }
+const char* epgpu_version(void) { return "epgpu 0.2 (sm_103a, FP64 oracle-order step, mixed FP32/FP64 step)"; }
 
 const char* epgpu_last_error(const ep_handle* h) { return h ? h->err.c_str() : g_create_error.c_str(); }
 
@@ -200,7 +203,12 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
                       : (w == EP_HOW_UNDEFORMED || w == EP_HOW_DETDFIJ || w == EP_HOW_DFII || w == EP_HOW_DUII);
         if (!ok) return fail(nullptr, EP_ERR_UNSUPPORTED, "basis.how undefined for gimpm in this framework");
     }
-    if (cfg->precision != EP_PREC_FP64) return fail(nullptr, EP_ERR_UNSUPPORTED, "only the FP64 step is built");
+    if (cfg->precision != EP_PREC_FP64 && cfg->precision != EP_PREC_MIXED)
+        return fail(nullptr, EP_ERR_UNSUPPORTED, "unknown precision");
+    if (cfg->precision == EP_PREC_MIXED && d != 2)
+        return fail(nullptr, EP_ERR_UNSUPPORTED, "the mixed-precision step is built for 2d; use EP_PREC_FP64 in 3d");
+    if (cfg->precision == EP_PREC_MIXED && cfg->nonloc)
+        return fail(nullptr, EP_ERR_UNSUPPORTED, "nonlocal averaging is built in the FP64 step only");
     if (cfg->nonloc && !(cfg->nonloc_ls > 0.0)) return fail(nullptr, EP_ERR_ARG, "nonloc.ls must be > 0");
     if (!mesh->x || !mesh->xB || !mesh->bcs) return fail(nullptr, EP_ERR_ARG, "mesh.x, mesh.xB and mesh.bcs are required");
     long long nnode = 1, ncell = 1;
@@ -414,6 +422,94 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
     h->ctx.ctl = h->ctl;
     h->ctx.np = h->np;
     h->ctx.launches = &h->launches;
+    if (cfg->precision == EP_PREC_MIXED) {
+        h->mixed = true;
+        const int np = h->np;
+        const int nc = (int)ncell, nn = (int)nnode;
+        PM pm{};
+        NM nm{};
+        SM sm{};
+        pm.np = np;
+        double* xd = nullptr;
+        float* pf = nullptr;
+        double* pd = nullptr;
+        // doubles: x[2][d], F[d*d], b[3], ep1 ; floats: v[d], tau[3], ep2, dlam, c0, cr, tphi, sphi, cphi, mp, Om0, Om,
+        // l[d], dv[d*d]
+        const size_t ndbl = (size_t)np * (2 * d + d * d + 3 + 1);
+        const size_t nflt = (size_t)np * (d + 3 + 11 + d + d * d);
+        bool ok2 = dalloc(h, &pd, ndbl) == cudaSuccess && dalloc(h, &pf, nflt) == cudaSuccess;
+        int* ints = nullptr;
+        const size_t nint = (size_t)3 * nc + 2 * (size_t)(nc + 1) + 2 * (size_t)np + (size_t)np + 2 * (size_t)(nc + 1);
+        ok2 = ok2 && dalloc(h, &ints, nint) == cudaSuccess;
+        float* nf = nullptr;
+        const size_t nnf = (size_t)nn * (1 + 6 * d + 2);
+        ok2 = ok2 && dalloc(h, &nf, nnf) == cudaSuccess;
+        if (!ok2) {
+            epgpu_destroy(h);
+            return fail(nullptr, EP_ERR_NOMEM, "device allocation (mixed state)");
+        }
+        xd = pd;
+        for (int par = 0; par < 2; ++par)
+            for (int i = 0; i < d; ++i) pm.x[par][i] = xd + (size_t)(par * d + i) * np;
+        double* q = pd + (size_t)2 * d * np;
+        for (int k = 0; k < d * d; ++k) pm.F[k] = q + (size_t)k * np;
+        q += (size_t)d * d * np;
+        for (int k = 0; k < 3; ++k) pm.b[k] = q + (size_t)k * np;
+        q += (size_t)3 * np;
+        pm.ep1 = q;
+        float* f = pf;
+        auto take = [&](size_t n) { float* r = f; f += n * (size_t)np; return r; };
+        for (int i = 0; i < d; ++i) pm.v[i] = take(1);
+        for (int k = 0; k < 3; ++k) pm.tau[k] = take(1);
+        pm.ep2 = take(1); pm.dlam = take(1); pm.c0 = take(1); pm.cr = take(1); pm.tphi = take(1);
+        pm.sphi = take(1); pm.cphi = take(1); pm.mp = take(1); pm.Om0 = take(1); pm.Om = take(1);
+        pm.rho = take(1);
+        for (int i = 0; i < d; ++i) pm.l[i] = take(1);
+        for (int k = 0; k < d * d; ++k) pm.dv[k] = take(1);
+        int* ip = ints;
+        int* sort_zero = ip;
+        sm.count[0] = ip; ip += nc;
+        sm.count[1] = ip; ip += nc;
+        sm.cursor = ip; ip += nc;
+        sm.start[0] = ip; ip += nc + 1;
+        sm.start[1] = ip; ip += nc + 1;
+        sm.list[0] = ip; ip += np;
+        sm.list[1] = ip; ip += np;
+        pm.p2e_next = ip; ip += np;
+        h->mx.scan_in = ip; ip += nc + 1;
+        h->mx.scan_out = ip; ip += nc + 1;
+        sm.scan_tmp = S.scan_tmp;
+        float* g0 = nf;
+        nm.m = g0;
+        for (int i = 0; i < d; ++i) nm.p[i] = g0 + (size_t)(1 + i) * nn;
+        for (int i = 0; i < d; ++i) nm.f[i] = g0 + (size_t)(1 + d + i) * nn;
+        for (int i = 0; i < d; ++i) nm.a[i] = g0 + (size_t)(1 + 2 * d + i) * nn;
+        for (int i = 0; i < d; ++i) nm.v[i] = g0 + (size_t)(1 + 3 * d + i) * nn;
+        for (int i = 0; i < d; ++i) nm.pm[i] = g0 + (size_t)(1 + 4 * d + i) * nn;
+        for (int i = 0; i < d; ++i) nm.vm[i] = g0 + (size_t)(1 + 5 * d + i) * nn;
+        nm.dJacc = g0 + (size_t)(1 + 6 * d) * nn;
+        nm.dJn = g0 + (size_t)(2 + 6 * d) * nn;
+        h->mx.grid_zero = g0;
+        h->mx.grid_zero_bytes = sizeof(float) * (size_t)(1 + 2 * d) * nn;   // m, p, f
+        h->mx.sort_zero = sort_zero;
+        h->mx.sort_zero_bytes = sizeof(int) * (size_t)3 * nc;
+        // compliance (inverse of the 3x3 Del) for ε = Del \ τ
+        double Cmp[9], LU[9], e[3], x[3];
+        int piv[3];
+        for (int i = 0; i < 9; ++i) LU[i] = cmpr->Del[i];
+        lu_factor<3>(LU, piv);
+        for (int j = 0; j < 3; ++j) {
+            for (int i = 0; i < 3; ++i) e[i] = (i == j) ? 1.0 : 0.0;
+            lu_solve<3>(LU, piv, e, x);
+            for (int i = 0; i < 3; ++i) Cmp[i + 3 * j] = x[i];
+        }
+        h->mx_impl.resize(mixed_ctx_size());
+        mixed_ctx_init(h->mx_impl.data(), cf, g, h->ctl, pm, nm, sm, cmpr->Del, Cmp, cmpr->Kc, cmpr->Gc, cmpr->Hp,
+                       cmpr->c);
+        h->mx.impl = h->mx_impl.data();
+        h->mx.launches = &h->launches;
+        h->mx.prof = nullptr;
+    }
     h->ctx.prof = nullptr;
     h->u.assign((size_t)d * h->np, 0.0);
     h->pp.assign((size_t)d * h->np, 0.0);
@@ -467,7 +563,9 @@ ep_status epgpu_upload(ep_handle* h, const ep_mpts_view* m) {
         h->hctl->vmax_bits[i] = (unsigned long long)bits;
     }
     CK(h, cudaMemcpyAsync(h->ctl, h->hctl, sizeof(Ctl), cudaMemcpyHostToDevice, h->s));
+    if (h->mixed) mixed_import(h->mx, h->ctx.P, h->s);
     CK(h, cudaStreamSynchronize(h->s));
+    CK(h, cudaGetLastError());
     h->uploaded = true;
     return EP_OK;
 }
@@ -509,7 +607,13 @@ ep_status epgpu_step(ep_handle* h, int32_t phase, double dt, const double* g, do
         ctx.prof = &h->prof;
         h->prof.begin(h->s);
     }
-    fp64_step(ctx, phase, h->s);
+    if (h->mixed) {
+        MixedCtx mx = h->mx;
+        if (h->prof.on) mx.prof = &h->prof;
+        mixed_step(mx, phase, h->s);
+    } else {
+        fp64_step(ctx, phase, h->s);
+    }
     h->launches += 1;
     CK(h, cudaEventRecord(h->ev1, h->s));
     CK(h, cudaGetLastError());
@@ -531,7 +635,8 @@ static ep_status build_graph(ep_handle* h, int phase) {
     CK(h, cudaStreamBeginCapture(h->s, cudaStreamCaptureModeThreadLocal));
     for (int k = 0; k < GRAPH_STEPS; ++k) {
         launch_ctl_begin_run(h->ctl, h->ctx.g, h->cm.c, h->s);
-        fp64_step(h->ctx, phase, h->s);
+        if (h->mixed) mixed_step(h->mx, phase, h->s);
+        else fp64_step(h->ctx, phase, h->s);
         launch_ctl_end(h->ctl, h->s);
     }
     cudaError_t e = cudaStreamEndCapture(h->s, &gr);
@@ -586,6 +691,10 @@ ep_status epgpu_download(ep_handle* h, ep_mpts_view* m) {
     if (m->nmp != h->np || m->ndim != h->dim) return fail(h, EP_ERR_ARG, "mpts.nmp/ndim differ from create");
     const int d = h->dim, ns = h->nstr;
     ep_status st;
+    if (h->mixed && h->uploaded) {
+        mixed_export(h->mx, h->ctx.P, h->ctx.N, h->s);
+        CK(h, cudaGetLastError());
+    }
     if ((st = read_ctl(h)) != EP_OK) return st;
 #define GET(ptr, k, f) if ((st = get_aos(h, fld_ptr(h, (f)), (k), (ptr))) != EP_OK) return st
     GET(m->x, d, F_X); GET(m->v, d, F_V); GET(m->l, d, F_L); GET(m->l0, d, F_L0);
@@ -642,6 +751,10 @@ ep_status epgpu_download_mesh(ep_handle* h, ep_mesh_fields* f) {
     if (!h || !f) return EP_ERR_ARG;
     const int d = h->dim;
     const size_t Nn = h->nnode;
+    if (h->mixed && h->uploaded) {
+        mixed_export(h->mx, h->ctx.P, h->ctx.N, h->s);
+        CK(h, cudaGetLastError());
+    }
     std::vector<double> buf((size_t)(1 + 4 * d + 1) * Nn);
     CK(h, cudaMemcpyAsync(buf.data(), h->nbuf, buf.size() * sizeof(double), cudaMemcpyDeviceToHost, h->s));
     CK(h, cudaStreamSynchronize(h->s));

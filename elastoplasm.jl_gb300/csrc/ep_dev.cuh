@@ -55,6 +55,8 @@ struct Ctl {
     long long plastic;
     int err;                          // first error code raised by a kernel (0 = none)
     int err_info;
+    int parity;                       // mixed step: which position / cell-list buffer is current
+    int pad_;
 };
 
 struct P64 {

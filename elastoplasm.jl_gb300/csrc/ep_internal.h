@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "ep_dev.cuh"
+#include "ep_mixed.cuh"
 
 namespace ep {
 
@@ -88,6 +89,27 @@ struct Fp64Ctx {
 };
 void fp64_step(const Fp64Ctx& c, int phase, cudaStream_t s);
 void fp64_check_finite(const Fp64Ctx& c, cudaStream_t s);
+
+// mixed-precision step (ep_mixed.cu)
+struct MixedCtx {
+    void* impl;               // host image of the kernels' argument block (MCtx)
+    void* grid_zero;          // node accumulators zeroed at each step start
+    size_t grid_zero_bytes;
+    void* sort_zero;          // both parities' cell counts and the cursor
+    size_t sort_zero_bytes;
+    int* scan_in;
+    int* scan_out;
+    Prof* prof;
+    long long* launches;
+};
+size_t mixed_ctx_size();
+void mixed_ctx_init(void* mem, const Cfg& cf, const Geo& g, Ctl* ctl, const PM& P, const NM& N, const SM& S,
+                    const double* Del, const double* Cmp, double Kc, double Gc, double Hp, double c);
+void mixed_step(const MixedCtx& X, int phase, cudaStream_t s);
+void launch_mixed_scan(const MixedCtx& X, cudaStream_t s);
+void mixed_initial_scan(const MixedCtx& X, cudaStream_t s);
+void mixed_import(const MixedCtx& X, const P64& Q, cudaStream_t s);
+void mixed_export(const MixedCtx& X, const P64& Q, const N64& QN, cudaStream_t s);
 
 // control-block kernels (ep_fp64.cu)
 void launch_ctl_begin_run(Ctl* ctl, const Geo& g, double c, cudaStream_t s);

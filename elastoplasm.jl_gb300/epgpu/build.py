@@ -23,6 +23,7 @@ UNITS = {
     "ep_api.cu": [],
     "ep_sort.cu": [],
     "ep_fp64.cu": ["-fmad=false"],
+    "ep_mixed.cu": [],
 }
 
 
