@@ -214,7 +214,7 @@ def main():
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "mixed_df"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--settle", type=float, default=0.5,
@@ -322,7 +322,7 @@ def main():
         line = {
             "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": tmax / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+            "scaling": "weak", "vs_baseline": None, "dtype": {"fp64": "f64", "mixed": "f32+f64", "mixed_df": "f32 (+f32 pairs)"}[args.precision],
             "data": f"synthetic slump geometry ({field})",
             "config": {"workload": WORKLOAD, "precision": args.precision, "points": np_,
                        "nodes": mesh.nnodes, "l2": "flushed between timed steps (256 MB write)",

@@ -203,11 +203,11 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
                       : (w == EP_HOW_UNDEFORMED || w == EP_HOW_DETDFIJ || w == EP_HOW_DFII || w == EP_HOW_DUII);
         if (!ok) return fail(nullptr, EP_ERR_UNSUPPORTED, "basis.how undefined for gimpm in this framework");
     }
-    if (cfg->precision != EP_PREC_FP64 && cfg->precision != EP_PREC_MIXED)
+    if (cfg->precision != EP_PREC_FP64 && cfg->precision != EP_PREC_MIXED && cfg->precision != EP_PREC_MIXED_DF)
         return fail(nullptr, EP_ERR_UNSUPPORTED, "unknown precision");
-    if (cfg->precision == EP_PREC_MIXED && d != 2)
+    if (cfg->precision != EP_PREC_FP64 && d != 2)
         return fail(nullptr, EP_ERR_UNSUPPORTED, "the mixed-precision step is built for 2d; use EP_PREC_FP64 in 3d");
-    if (cfg->precision == EP_PREC_MIXED && cfg->nonloc)
+    if (cfg->precision != EP_PREC_FP64 && cfg->nonloc)
         return fail(nullptr, EP_ERR_UNSUPPORTED, "nonlocal averaging is built in the FP64 step only");
     if (cfg->nonloc && !(cfg->nonloc_ls > 0.0)) return fail(nullptr, EP_ERR_ARG, "nonloc.ls must be > 0");
     if (!mesh->x || !mesh->xB || !mesh->bcs) return fail(nullptr, EP_ERR_ARG, "mesh.x, mesh.xB and mesh.bcs are required");
@@ -422,24 +422,26 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
     h->ctx.ctl = h->ctl;
     h->ctx.np = h->np;
     h->ctx.launches = &h->launches;
-    if (cfg->precision == EP_PREC_MIXED) {
+    if (cfg->precision == EP_PREC_MIXED || cfg->precision == EP_PREC_MIXED_DF) {
         h->mixed = true;
+        const int acc = cfg->precision == EP_PREC_MIXED_DF ? 1 : 0;
         const int np = h->np;
         const int nc = (int)ncell, nn = (int)nnode;
         PM pm{};
         NM nm{};
         SM sm{};
         pm.np = np;
-        double* xd = nullptr;
-        float* pf = nullptr;
+        // accumulated state: F (d*d), b (3), ep1 as FP64 or as FP32 pairs
+        const size_t nacc = (size_t)(d * d + 3 + 1);
         double* pd = nullptr;
-        // doubles: x[2][d], F[d*d], b[3], ep1 ; floats: v[d], tau[3], ep2, dlam, c0, cr, tphi, sphi, cphi, mp, Om0, Om,
-        // l[d], dv[d*d]
-        const size_t ndbl = (size_t)np * (2 * d + d * d + 3 + 1);
-        const size_t nflt = (size_t)np * (d + 3 + 11 + d + d * d);
-        bool ok2 = dalloc(h, &pd, ndbl) == cudaSuccess && dalloc(h, &pf, nflt) == cudaSuccess;
+        float* pf = nullptr;
+        bool ok2 = true;
+        if (acc == 0) ok2 = dalloc(h, &pd, nacc * np) == cudaSuccess;
+        // floats: dx[2][d], v[d], tau[3], 11 scalars, rho, l[d], dv[d*d], (pairs: 2*nacc)
+        const size_t nflt = (size_t)np * (2 * d + d + 3 + 11 + 1 + d + d * d + (acc ? 2 * nacc : 0));
+        ok2 = ok2 && dalloc(h, &pf, nflt) == cudaSuccess;
         int* ints = nullptr;
-        const size_t nint = (size_t)3 * nc + 2 * (size_t)(nc + 1) + 2 * (size_t)np + (size_t)np + 2 * (size_t)(nc + 1);
+        const size_t nint = (size_t)3 * nc + 2 * (size_t)(nc + 1) + 4 * (size_t)np + (size_t)np + 2 * (size_t)(nc + 1);
         ok2 = ok2 && dalloc(h, &ints, nint) == cudaSuccess;
         float* nf = nullptr;
         const size_t nnf = (size_t)nn * (1 + 6 * d + 2);
@@ -448,24 +450,31 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
             epgpu_destroy(h);
             return fail(nullptr, EP_ERR_NOMEM, "device allocation (mixed state)");
         }
-        xd = pd;
-        for (int par = 0; par < 2; ++par)
-            for (int i = 0; i < d; ++i) pm.x[par][i] = xd + (size_t)(par * d + i) * np;
-        double* q = pd + (size_t)2 * d * np;
-        for (int k = 0; k < d * d; ++k) pm.F[k] = q + (size_t)k * np;
-        q += (size_t)d * d * np;
-        for (int k = 0; k < 3; ++k) pm.b[k] = q + (size_t)k * np;
-        q += (size_t)3 * np;
-        pm.ep1 = q;
         float* f = pf;
         auto take = [&](size_t n) { float* r = f; f += n * (size_t)np; return r; };
+        for (int par = 0; par < 2; ++par)
+            for (int i = 0; i < d; ++i) pm.dx[par][i] = take(1);
         for (int i = 0; i < d; ++i) pm.v[i] = take(1);
         for (int k = 0; k < 3; ++k) pm.tau[k] = take(1);
         pm.ep2 = take(1); pm.dlam = take(1); pm.c0 = take(1); pm.cr = take(1); pm.tphi = take(1);
         pm.sphi = take(1); pm.cphi = take(1); pm.mp = take(1); pm.Om0 = take(1); pm.Om = take(1);
+        take(1);   // spare
         pm.rho = take(1);
         for (int i = 0; i < d; ++i) pm.l[i] = take(1);
         for (int k = 0; k < d * d; ++k) pm.dv[k] = take(1);
+        if (acc == 0) {
+            double* q = pd;
+            for (int k = 0; k < d * d; ++k) pm.Fd[k] = q + (size_t)k * np;
+            q += (size_t)d * d * np;
+            for (int k = 0; k < 3; ++k) pm.bd[k] = q + (size_t)k * np;
+            q += (size_t)3 * np;
+            pm.ep1d = q;
+        } else {
+            for (int k = 0; k < d * d; ++k) { pm.Fh[k] = take(1); pm.Fl[k] = take(1); }
+            for (int k = 0; k < 3; ++k) { pm.bh[k] = take(1); pm.bl[k] = take(1); }
+            pm.ep1h = take(1);
+            pm.ep1l = take(1);
+        }
         int* ip = ints;
         int* sort_zero = ip;
         sm.count[0] = ip; ip += nc;
@@ -475,6 +484,8 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
         sm.start[1] = ip; ip += nc + 1;
         sm.list[0] = ip; ip += np;
         sm.list[1] = ip; ip += np;
+        sm.cellof[0] = ip; ip += np;
+        sm.cellof[1] = ip; ip += np;
         pm.p2e_next = ip; ip += np;
         h->mx.scan_in = ip; ip += nc + 1;
         h->mx.scan_out = ip; ip += nc + 1;
@@ -493,7 +504,7 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
         h->mx.grid_zero_bytes = sizeof(float) * (size_t)(1 + 2 * d) * nn;   // m, p, f
         h->mx.sort_zero = sort_zero;
         h->mx.sort_zero_bytes = sizeof(int) * (size_t)3 * nc;
-        // compliance (inverse of the 3x3 Del) for ε = Del \ τ
+        // compliance (inverse of the 3x3 Del) for ε = Del \\ τ
         double Cmp[9], LU[9], e[3], x[3];
         int piv[3];
         for (int i = 0; i < 9; ++i) LU[i] = cmpr->Del[i];
@@ -505,7 +516,7 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
         }
         h->mx_impl.resize(mixed_ctx_size());
         mixed_ctx_init(h->mx_impl.data(), cf, g, h->ctl, pm, nm, sm, cmpr->Del, Cmp, cmpr->Kc, cmpr->Gc, cmpr->Hp,
-                       cmpr->c);
+                       cmpr->c, acc);
         h->mx.impl = h->mx_impl.data();
         h->mx.launches = &h->launches;
         h->mx.prof = nullptr;

@@ -104,7 +104,7 @@ struct MixedCtx {
 };
 size_t mixed_ctx_size();
 void mixed_ctx_init(void* mem, const Cfg& cf, const Geo& g, Ctl* ctl, const PM& P, const NM& N, const SM& S,
-                    const double* Del, const double* Cmp, double Kc, double Gc, double Hp, double c);
+                    const double* Del, const double* Cmp, double Kc, double Gc, double Hp, double c, int acc);
 void mixed_step(const MixedCtx& X, int phase, cudaStream_t s);
 void launch_mixed_scan(const MixedCtx& X, cudaStream_t s);
 void mixed_initial_scan(const MixedCtx& X, cudaStream_t s);

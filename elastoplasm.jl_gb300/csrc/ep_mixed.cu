@@ -1,37 +1,41 @@
-// ep_mixed.cu -- the mixed-precision MPM step (2d), the fast path.
+// ep_mixed.cu -- the mixed-precision MPM steps (2d), the fast path.
 //
-// Same method and call order as the reference step (worflow.jl:80-82), with
-// transfers and grid arithmetic in FP32 and FP64 where accumulation or
-// cancellation needs it:
-//   * positions, F and b_e are FP64 state; their per-step increments are
-//     formed in FP32 (they are small: dt∇v ~ 1e-4) and added in FP64;
-//   * F-bar carries δJ = ΔJ - 1 instead of ΔJ, so no FP32 cancellation
-//     against 1 happens (volumetric.jl:1-36 in "increment" form);
-//   * log b_e and exp(2ε) of the finite-strain predictor/return
-//     (elast.jl:49-54, DP.jl:63-66) use the closed spectral form of a
-//     symmetric 2x2 tensor A = m I + A_d (A_d deviatoric, eigenvalues m ± r):
+// Same method and call order as the reference step (worflow.jl:80-82); the
+// transfers and the grid arithmetic run in FP32.  What needs more than FP32
+// is kept in a wider accumulator:
+//   * the accumulated kinematic state F, b_e and the accumulated plastic
+//     strain: FP64 ("mixed", ACC = 0) or double-float pairs of FP32 values
+//     ("mixed_df", ACC = 1; GB300 issues FP64 at 1/64 of the FP32 rate, and a
+//     pair carries 48 significand bits with FP32 instructions only).  Their
+//     per-step increments are small (dt∇v ~ 1e-4) and formed in FP32;
+//   * positions: FP32 offsets from the left node of the point's cell
+//     (|offset| < h, so an FP32 ulp is ~1e-7 h); the cell index is exact;
+//   * F-bar carries δJ = ΔJ - 1 instead of ΔJ (volumetric.jl:1-36 in
+//     increment form), so nothing cancels against 1 in FP32;
+//   * log b_e and exp(2ε) (elast.jl:49-54, DP.jl:63-66) use the closed
+//     spectral form of a symmetric 2x2 tensor A = m I + A_d (eigenvalues m ± r):
 //       log A = (log m + ½ log(1 - x²)) I + (atanh(x)/x)/m · A_d,  x = r/m,
-//       exp(2E) = e^{2 e_m} (cosh(2s) I + sinh(2s)/s · E_d),       s² = ½ tr(E_d²),
-//     with log m and e^{2 e_m} (the isotropic part, which carries the
-//     magnitude) in FP64 and the deviatoric factors in FP32 (arguments x², s²
-//     are small invariants).  No explicit eigenvectors are needed.
-//   * the accumulated plastic strain is FP64.
+//       exp(2E) = e^{2 e_m} (cosh(2s) I + sinh(2s)/s · E_d),       s² = ½ tr(E_d²);
+//     the isotropic part (log m, e^{2 e_m}) is FP64 for ACC = 0 and, for
+//     ACC = 1, log1p/expm1 of the deviation from 1 formed exactly from the
+//     double-float state; the deviatoric factors are FP32 functions of the
+//     small invariants x², s².
 //
-// Transfers are cell-centric: one thread per cell walks the points of its
-// cell (cell lists from a counting sort, rebuilt every step) and accumulates
-// its 16 stencil nodes' sums in registers, then adds them to the grid with
-// FP32 atomics -- one atomic per node and quantity per cell instead of per
-// point.  Kernels of one step:
-//   km_p2g    P2G of m, p, f                      (p2n.jl:135-155)      cell
-//   km_solve  grid update                         (solve.jl:14-40)      node
-//   km_g2p    PIC/FLIP, positions, vmax, mUSL P2G, next cell counts
-//             (n2p.jl:14-40, augm.jl:13-25, tplgy.jl:43-62)             cell
-//   km_vmusl  mUSL nodal velocity                 (augm.jl:37-53)       node
-//   scan of the next cell counts
-//   km_fbar   ∇v, δJ and its P2G; next cell lists (deform.jl, volumetric.jl:1-11) cell
-//   km_dJn    nodal δJ                            (volumetric.jl:12-22) node
+// Kernels of one step (c = one quad of 4 lanes per cell, p = one lane per point):
+//   km_p2g    P2G of m, p, f                      (p2n.jl:135-155, 217-240)   c
+//   km_solve  grid update                         (solve.jl:14-40)            node
+//   km_g2p    PIC/FLIP, positions, vmax, next-cell counts, mUSL P2G
+//             (n2p.jl:14-40, tplgy.jl:43-62, augm.jl:13-25)                   c
+//   km_vmusl  mUSL nodal velocity                 (augm.jl:37-53)             node
+//   km_scan_* next-step cell offsets (exclusive scan of the counts)
+//   km_fbar   ∇v, δJ and Σ N m δJ; next-step cell lists (deform.jl:9-18,
+//             volumetric.jl:1-11)                                             c
+//   km_dJn    nodal δJ                            (volumetric.jl:12-22)       node
 //   km_cons   F-bar, F, elastic predictor, DP/J2  (volumetric.jl:23-36, deform.jl,
-//             elast.jl, DP.jl, J2.jl)                                   cell
+//             elast.jl, DP.jl, J2.jl)                                         p
+// In a quad, lane q owns the stencil column q (4 nodes), so the lanes of a
+// quad never add to the same node and each keeps 4 nodes' sums in registers;
+// one FP32 atomic per node and quantity per cell goes to the grid.
 #include <climits>
 
 #include "../../include/epgpu.h"
@@ -114,10 +118,26 @@ __device__ __forceinline__ Axis4 axis4(const Geo& g, int d, int e) {
 }
 
 // weights and gradients of the 4 nodes along one direction for a point at
-// offset dloc = x - x_e (x_e: node e, the left node of the point's cell)
+// offset dloc = x - x_e (x_e: node e, the left node of the point's cell).
+// Cells whose 4 stencil nodes are all interior B-spline nodes use the
+// uniform cubic B-spline in closed form (the t3 piece of bsmpm.jl:32-48
+// evaluated at ξ = f+1, f, f-1, f-2 with f = dloc/h).
 template <int BASIS>
 __device__ __forceinline__ void axis_w(const Axis4& a, float dloc, float h, float ih, float lp, float* w, float* dw,
                                        bool& bad) {
+    if (BASIS == EP_BASIS_BSMPM && a.cls[0] == BS_T3 && a.cls[1] == BS_T3 && a.cls[2] == BS_T3 && a.cls[3] == BS_T3) {
+        const float f = dloc * ih, g = 1.f - f;
+        const float f2 = f * f, g2 = g * g;
+        w[0] = (1.f / 6.f) * g2 * g;
+        w[1] = (0.5f * f - 1.f) * f2 + (2.f / 3.f);
+        w[2] = (0.5f * g - 1.f) * g2 + (2.f / 3.f);
+        w[3] = (1.f / 6.f) * f2 * f;
+        dw[0] = -0.5f * g2 * ih;
+        dw[1] = (1.5f * f - 2.f) * f * ih;
+        dw[2] = (2.f - 1.5f * g) * g * ih;
+        dw[3] = 0.5f * f2 * ih;
+        return;
+    }
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         float f = 0.f, df = 0.f;
@@ -149,96 +169,127 @@ struct MCtx {
     float Cmp[9];       // its inverse (compliance), FP32
     float Kc, Gc, Hp;
     double c;           // wave speed
+    int acc;            // 0: FP64 accumulators, 1: double-float accumulators
 };
-
-// shape function weights of point p in cell (ex, ez), parity buffer cur
-template <int BASIS>
-__device__ __forceinline__ void point_w2(const MCtx& A, const Axis4& ax, const Axis4& az, int p, int cur, double axe,
-                                         double aze, float* wx, float* dwx, float* wz, float* dwz, bool& bad) {
-    const float hx = (float)A.g.h[0], hz = (float)A.g.h[1];
-    const float dx = (float)(A.P.x[cur][0][p] - axe);
-    const float dz = (float)(A.P.x[cur][1][p] - aze);
-    const float lx = BASIS == EP_BASIS_GIMPM ? A.P.l[0][p] : 0.f;
-    const float lz = BASIS == EP_BASIS_GIMPM ? A.P.l[1][p] : 0.f;
-    axis_w<BASIS>(ax, dx, hx, 1.f / hx, lx, wx, dwx, bad);
-    axis_w<BASIS>(az, dz, hz, 1.f / hz, lz, wz, dwz, bad);
-}
 
 __device__ __forceinline__ int node2(const Geo& g, const Axis4& ax, const Axis4& az, int i, int j) {
     return (az.base + j) + g.nno[1] * (ax.base + i);
 }
 
-// ---------------------------------------------------------------------------
-// km_p2g: m, p, f of the 16 stencil nodes of a cell, summed over its points
+// four lanes per cell; lane q owns stencil column q
+struct Quad {
+    int c, q, b, e, ex, ez;
+    bool live;
+};
+
+__device__ __forceinline__ Quad quad_of(const MCtx& A, int cur) {
+    Quad Q;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    Q.c = t >> 2;
+    Q.q = t & 3;
+    Q.live = Q.c < A.g.ncell;
+    Q.b = Q.e = 0;
+    Q.ex = Q.ez = 0;
+    if (Q.live) {
+        Q.b = A.S.start[cur][Q.c];
+        Q.e = A.S.start[cur][Q.c + 1];
+        Q.ex = Q.c / A.g.nel[1];
+        Q.ez = Q.c - Q.ex * A.g.nel[1];
+    }
+    return Q;
+}
+
+// sum over the four lanes of a quad; the mask names only those lanes, which
+// always run the same loop trip count (they walk the same cell)
+__device__ __forceinline__ float quad_sum(float v) {
+    const unsigned m = 0xFu << (threadIdx.x & 28);
+    v += __shfl_xor_sync(m, v, 1);
+    v += __shfl_xor_sync(m, v, 2);
+    return v;
+}
+
+// weights of one stencil column (x) and of all four rows (z) of a point
 template <int BASIS>
-__global__ void __launch_bounds__(128) km_p2g(MCtx A) {
+__device__ __forceinline__ void quad_weights(const MCtx& A, const Axis4& ax, const Axis4& az, int q, int p, int cur,
+                                             float& wx, float& dwx, float* wz, float* dwz, bool& bad) {
+    const float hx = (float)A.g.h[0], hz = (float)A.g.h[1];
+    const float dx = A.P.dx[cur][0][p], dz = A.P.dx[cur][1][p];
+    const float lx = BASIS == EP_BASIS_GIMPM ? A.P.l[0][p] : 0.f;
+    const float lz = BASIS == EP_BASIS_GIMPM ? A.P.l[1][p] : 0.f;
+    float w4[4], d4[4];
+    axis_w<BASIS>(ax, dx, hx, 1.f / hx, lx, w4, d4, bad);
+    wx = q == 0 ? w4[0] : q == 1 ? w4[1] : q == 2 ? w4[2] : w4[3];
+    dwx = q == 0 ? d4[0] : q == 1 ? d4[1] : q == 2 ? d4[2] : d4[3];
+    axis_w<BASIS>(az, dz, hz, 1.f / hz, lz, wz, dwz, bad);
+}
+
+// ---------------------------------------------------------------------------
+// km_p2g: m, p, f (p2n.jl:135-155 std, 217-240 tpic); lane q accumulates its column
+template <int BASIS>
+__global__ void __launch_bounds__(256) km_p2g(MCtx A) {
     EP_ACTIVE(A.ctl);
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= A.g.ncell) return;
     const int cur = A.ctl->parity;
-    const int b = A.S.start[cur][c], e = A.S.start[cur][c + 1];
-    if (b == e) return;
-    const int ex = c / A.g.nel[1], ez = c - ex * A.g.nel[1];
-    const Axis4 ax = axis4(A.g, 0, ex), az = axis4(A.g, 1, ez);
-    const double axe = A.g.ax[0][ex], aze = A.g.ax[1][ez];
+    const Quad Q = quad_of(A, cur);
+    if (!Q.live || Q.b == Q.e) return;
+    const Axis4 ax = axis4(A.g, 0, Q.ex), az = axis4(A.g, 1, Q.ez);
+    const float hx = (float)A.g.h[0], hz = (float)A.g.h[1];
     const float gz = (float)A.ctl->g[1];
     const bool fin = A.cf.deform == EP_DEFORM_FINITE;
     const bool tpic = A.cf.trsfr == EP_TRSFR_TPIC;
-    float am[16], apx[16], apz[16], afx[16], afz[16];
+    const int q = Q.q;
+    float am[4], apx[4], apz[4], afx[4], afz[4];
 #pragma unroll
-    for (int s = 0; s < 16; ++s) am[s] = apx[s] = apz[s] = afx[s] = afz[s] = 0.f;
+    for (int j = 0; j < 4; ++j) am[j] = apx[j] = apz[j] = afx[j] = afz[j] = 0.f;
     bool bad = false;
     const int* list = A.S.list[cur];
-    for (int k = b; k < e; ++k) {
+    for (int k = Q.b; k < Q.e; ++k) {
         const int p = list[k];
-        float wx[4], dwx[4], wz[4], dwz[4];
-        point_w2<BASIS>(A, ax, az, p, cur, axe, aze, wx, dwx, wz, dwz, bad);
+        float wx, dwx, wz[4], dwz[4];
+        quad_weights<BASIS>(A, ax, az, q, p, cur, wx, dwx, wz, dwz, bad);
         const float ms = A.P.mp[p];
         const float vx = A.P.v[0][p], vz = A.P.v[1][p];
-        // Ω σ: finite Ω τ / J = Ω0 τ; infinitesimal Ω σ
-        const float sc = fin ? A.P.Om0[p] : A.P.Om[p];
+        const float sc = fin ? A.P.Om0[p] : A.P.Om[p];          // Ω σ = Ω0 τ (finite) or Ω σ
         const float txx = sc * A.P.tau[0][p], tzz = sc * A.P.tau[1][p], txz = sc * A.P.tau[2][p];
-        float gxx = 0.f, gxz = 0.f, gzx = 0.f, gzz = 0.f, xo = 0.f, zo = 0.f;
+        float vx_i = vx, vz_i = vz, gxz = 0.f, gzz = 0.f, dz = 0.f;
         if (tpic) {
-            gxx = A.P.dv[0][p]; gzx = A.P.dv[1][p]; gxz = A.P.dv[2][p]; gzz = A.P.dv[3][p];
-            xo = (float)(A.P.x[cur][0][p] - axe);
-            zo = (float)(A.P.x[cur][1][p] - aze);
+            // v + ∇v (x_n - x_p) with the previous step's ∇v (p2n.jl:233-235)
+            const float gxx = A.P.dv[0][p], gzx = A.P.dv[1][p];
+            gxz = A.P.dv[2][p];
+            gzz = A.P.dv[3][p];
+            const float ddx = (float)(q - 1) * hx - A.P.dx[cur][0][p];
+            dz = A.P.dx[cur][1][p];
+            vx_i = vx + gxx * ddx;
+            vz_i = vz + gzx * ddx;
         }
-#pragma unroll
-        for (int i = 0; i < 4; ++i)
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const int s = j + 4 * i;
-                const float N = wx[i] * wz[j], Nx = dwx[i] * wz[j], Nz = wx[i] * dwz[j];
-                const float Nm = N * ms;
-                am[s] += Nm;
-                if (!tpic) {
-                    apx[s] += Nm * vx;
-                    apz[s] += Nm * vz;
-                } else {
-                    // δ = x_n - x_p for node (e-1+i, e-1+j)
-                    const float dx = (float)(i - 1) * (float)A.g.h[0] - xo;
-                    const float dz = (float)(j - 1) * (float)A.g.h[1] - zo;
-                    apx[s] += Nm * (vx + gxx * dx + gxz * dz);
-                    apz[s] += Nm * (vz + gzx * dx + gzz * dz);
-                }
-                afx[s] -= Nx * txx + Nz * txz;
-                afz[s] -= (Nx * txz + Nz * tzz) - Nm * gz;
-            }
-    }
-    if (bad) set_err(A.ctl, EP_ERR_INVALID_POSITION, c);
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            if (ax.cls[i] < 0 || az.cls[j] < 0) continue;
-            const int s = j + 4 * i, n = node2(A.g, ax, az, i, j);
-            atomicAdd(&A.N.m[n], am[s]);
-            atomicAdd(&A.N.p[0][n], apx[s]);
-            atomicAdd(&A.N.p[1][n], apz[s]);
-            atomicAdd(&A.N.f[0][n], afx[s]);
-            atomicAdd(&A.N.f[1][n], afz[s]);
+            const float N = wx * wz[j], Nx = dwx * wz[j], Nz = wx * dwz[j];
+            const float Nm = N * ms;
+            am[j] += Nm;
+            if (!tpic) {
+                apx[j] += Nm * vx;
+                apz[j] += Nm * vz;
+            } else {
+                const float ddz = (float)(j - 1) * hz - dz;
+                apx[j] += Nm * (vx_i + gxz * ddz);
+                apz[j] += Nm * (vz_i + gzz * ddz);
+            }
+            afx[j] -= Nx * txx + Nz * txz;
+            afz[j] -= (Nx * txz + Nz * tzz) - Nm * gz;
         }
+    }
+    if (bad) set_err(A.ctl, EP_ERR_INVALID_POSITION, Q.c);
+    if (ax.cls[q] < 0) return;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        if (az.cls[j] < 0) continue;
+        const int n = node2(A.g, ax, az, q, j);
+        atomicAdd(&A.N.m[n], am[j]);
+        atomicAdd(&A.N.p[0][n], apx[j]);
+        atomicAdd(&A.N.p[1][n], apz[j]);
+        atomicAdd(&A.N.f[0][n], afx[j]);
+        atomicAdd(&A.N.f[1][n], afz[j]);
+    }
 }
 
 // km_solve: grid momentum update with damping and Dirichlet masks (solve.jl:14-40)
@@ -275,87 +326,93 @@ __global__ void km_solve(MCtx A) {
     A.N.dJacc[n] = 0.f;
 }
 
-// km_g2p: PIC/FLIP update, new positions, vmax, mUSL momentum P2G, next-cell counts
+// new cell and offset along one direction after a move of the offset o
+// (relative to node e of the old cell), clamped to the mesh like tplgy.jl:49
+__device__ __forceinline__ void recell(const Geo& g, int d, int e, float o, float ih, int& e2, float& o2) {
+    int k = (int)floorf(o * ih);
+    e2 = min(max(e + k, 0), g.nel[d] - 1);
+    o2 = o;
+    if (e2 != e) o2 = o - (float)(g.ax[d][e2] - g.ax[d][e]);
+}
+
+// km_g2p: PIC/FLIP update (n2p.jl:14-40), new positions (cell + offset),
+// vmax, next-cell counts (tplgy.jl:43-62) and the mUSL momentum P2G (augm.jl:13-25)
 template <int BASIS>
-__global__ void __launch_bounds__(128) km_g2p(MCtx A) {
+__global__ void __launch_bounds__(256) km_g2p(MCtx A) {
     EP_ACTIVE(A.ctl);
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
     const int cur = A.ctl->parity, nxt = cur ^ 1;
+    const Quad Q = quad_of(A, cur);
     unsigned vm0 = 0u, vm1 = 0u;
-    if (c < A.g.ncell) {
-        const int b = A.S.start[cur][c], e = A.S.start[cur][c + 1];
-        if (b < e) {
-            const int ex = c / A.g.nel[1], ez = c - ex * A.g.nel[1];
-            const Axis4 ax = axis4(A.g, 0, ex), az = axis4(A.g, 1, ez);
-            const double axe = A.g.ax[0][ex], aze = A.g.ax[1][ez];
-            const double dt = A.ctl->dt;
-            const float dtf = (float)dt, Cpf = (float)A.cf.Cpf;
-            const bool musl = A.cf.musl;
-            int nid[16];
+    if (Q.live && Q.b < Q.e) {
+        const Axis4 ax = axis4(A.g, 0, Q.ex), az = axis4(A.g, 1, Q.ez);
+        const float ihx = 1.f / (float)A.g.h[0], ihz = 1.f / (float)A.g.h[1];
+        const float dtf = (float)A.ctl->dt, Cpf = (float)A.cf.Cpf;
+        const bool musl = A.cf.musl;
+        const int q = Q.q;
+        int nid[4];
 #pragma unroll
-            for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) nid[j] = (ax.cls[q] >= 0 && az.cls[j] >= 0) ? node2(A.g, ax, az, q, j) : -1;
+        float pmx[4] = {0.f, 0.f, 0.f, 0.f}, pmz[4] = {0.f, 0.f, 0.f, 0.f};
+        bool bad = false;
+        for (int k = Q.b; k < Q.e; ++k) {
+            const int p = A.S.list[cur][k];
+            float wx, dwx, wz[4], dwz[4];
+            quad_weights<BASIS>(A, ax, az, q, p, cur, wx, dwx, wz, dwz, bad);
+            float vpx = 0.f, vpz = 0.f, afx = 0.f, afz = 0.f;
 #pragma unroll
-                for (int j = 0; j < 4; ++j)
-                    nid[j + 4 * i] = (ax.cls[i] >= 0 && az.cls[j] >= 0) ? node2(A.g, ax, az, i, j) : -1;
-            float pmx[16], pmz[16];
-#pragma unroll
-            for (int s = 0; s < 16; ++s) pmx[s] = pmz[s] = 0.f;
-            bool bad = false;
-            const double ih0 = 1.0 / A.g.h[0], ih1 = 1.0 / A.g.h[1];
-            for (int k = b; k < e; ++k) {
-                const int p = A.S.list[cur][k];
-                float wx[4], dwx[4], wz[4], dwz[4];
-                point_w2<BASIS>(A, ax, az, p, cur, axe, aze, wx, dwx, wz, dwz, bad);
-                float vpx = 0.f, vpz = 0.f, afx = 0.f, afz = 0.f;
-#pragma unroll
-                for (int s = 0; s < 16; ++s) {
-                    if (nid[s] < 0) continue;
-                    const float N = wx[s >> 2] * wz[s & 3];
-                    vpx += N * __ldg(&A.N.v[0][nid[s]]);
-                    vpz += N * __ldg(&A.N.v[1][nid[s]]);
-                    afx += N * __ldg(&A.N.a[0][nid[s]]);
-                    afz += N * __ldg(&A.N.a[1][nid[s]]);
-                }
-                const float vx = Cpf * (A.P.v[0][p] + dtf * afx) + (1.f - Cpf) * vpx;
-                const float vz = Cpf * (A.P.v[1][p] + dtf * afz) + (1.f - Cpf) * vpz;
+            for (int j = 0; j < 4; ++j) {
+                if (nid[j] < 0) continue;
+                const float N = wx * wz[j];
+                vpx += N * __ldg(&A.N.v[0][nid[j]]);
+                vpz += N * __ldg(&A.N.v[1][nid[j]]);
+                afx += N * __ldg(&A.N.a[0][nid[j]]);
+                afz += N * __ldg(&A.N.a[1][nid[j]]);
+            }
+            vpx = quad_sum(vpx);
+            vpz = quad_sum(vpz);
+            afx = quad_sum(afx);
+            afz = quad_sum(afz);
+            const float vx = Cpf * (A.P.v[0][p] + dtf * afx) + (1.f - Cpf) * vpx;
+            const float vz = Cpf * (A.P.v[1][p] + dtf * afz) + (1.f - Cpf) * vpz;
+            if (q == 0) {
                 A.P.v[0][p] = vx;
                 A.P.v[1][p] = vz;
-                const double xn = A.P.x[cur][0][p] + dt * (double)vpx;
-                const double zn = A.P.x[cur][1][p] + dt * (double)vpz;
-                A.P.x[nxt][0][p] = xn;
-                A.P.x[nxt][1][p] = zn;
                 vm0 = max(vm0, __float_as_uint(fabsf(vx)));
                 vm1 = max(vm1, __float_as_uint(fabsf(vz)));
-                // cell of the new position (clamped as in tplgy.jl:49)
-                double fx = floor((xn - A.g.x0[0]) * ih0), fz = floor((zn - A.g.x0[1]) * ih1);
+                // x += dt v_PIC as a cell offset update, then re-binning (tplgy.jl:49)
+                const float ox = A.P.dx[cur][0][p] + dtf * vpx, oz = A.P.dx[cur][1][p] + dtf * vpz;
                 int c2 = -1;
-                if (isfinite(xn) && isfinite(zn)) {
-                    fx = fmin(fmax(fx, 0.0), (double)(A.g.nel[0] - 1));
-                    fz = fmin(fmax(fz, 0.0), (double)(A.g.nel[1] - 1));
-                    c2 = (int)fz + A.g.nel[1] * (int)fx;
+                if (isfinite(ox) && isfinite(oz)) {
+                    int ex2, ez2;
+                    float o2x, o2z;
+                    recell(A.g, 0, Q.ex, ox, ihx, ex2, o2x);
+                    recell(A.g, 1, Q.ez, oz, ihz, ez2, o2z);
+                    c2 = ez2 + A.g.nel[1] * ex2;
+                    A.P.dx[nxt][0][p] = o2x;
+                    A.P.dx[nxt][1][p] = o2z;
                     atomicAdd(&A.S.count[nxt][c2], 1);
                 } else {
                     set_err(A.ctl, EP_ERR_NONFINITE, p);
                 }
                 A.P.p2e_next[p] = c2;
-                if (musl) {
-                    const float mp = A.P.mp[p];
+            }
+            if (musl) {
+                const float mp = A.P.mp[p];
 #pragma unroll
-                    for (int s = 0; s < 16; ++s) {
-                        const float Nm = wx[s >> 2] * wz[s & 3] * mp;
-                        pmx[s] += Nm * vx;
-                        pmz[s] += Nm * vz;
-                    }
+                for (int j = 0; j < 4; ++j) {
+                    const float Nm = wx * wz[j] * mp;
+                    pmx[j] += Nm * vx;
+                    pmz[j] += Nm * vz;
                 }
             }
-            if (bad) set_err(A.ctl, EP_ERR_INVALID_POSITION, c);
-            if (musl) {
+        }
+        if (bad) set_err(A.ctl, EP_ERR_INVALID_POSITION, Q.c);
+        if (musl) {
 #pragma unroll
-                for (int s = 0; s < 16; ++s) {
-                    if (nid[s] < 0) continue;
-                    atomicAdd(&A.N.pm[0][nid[s]], pmx[s]);
-                    atomicAdd(&A.N.pm[1][nid[s]], pmz[s]);
-                }
+            for (int j = 0; j < 4; ++j) {
+                if (nid[j] < 0) continue;
+                atomicAdd(&A.N.pm[0][nid[j]], pmx[j]);
+                atomicAdd(&A.N.pm[1][nid[j]], pmz[j]);
             }
         }
     }
@@ -382,74 +439,69 @@ __global__ void km_vmusl(MCtx A) {
     }
 }
 
-// velocity gradient of point p from the nodal velocity field vn (deform.jl:9-10)
-__device__ __forceinline__ void grad_v(const float* wx, const float* dwx, const float* wz, const float* dwz,
-                                       const int* nid, float* const* vn, float* gv) {
-    float g00 = 0.f, g01 = 0.f, g10 = 0.f, g11 = 0.f;
-#pragma unroll
-    for (int s = 0; s < 16; ++s) {
-        if (nid[s] < 0) continue;
-        const float Nx = dwx[s >> 2] * wz[s & 3], Nz = wx[s >> 2] * dwz[s & 3];
-        const float vx = __ldg(&vn[0][nid[s]]), vz = __ldg(&vn[1][nid[s]]);
-        g00 += Nx * vx;
-        g01 += Nz * vx;
-        g10 += Nx * vz;
-        g11 += Nz * vz;
-    }
-    gv[0] = g00; gv[1] = g10; gv[2] = g01; gv[3] = g11;   // column-major ∇v[i + 2j] = ∂v_i/∂x_j
-}
-
 __device__ __forceinline__ void place_next(const MCtx& A, int p, int nxt) {
     const int c2 = A.P.p2e_next[p];
     if (c2 < 0) return;
     const int k = atomicAdd(&A.S.cursor[c2], 1);
     const int pos = A.S.start[nxt][c2] + k;
-    if (pos < A.S.start[nxt][c2 + 1]) A.S.list[nxt][pos] = p;
-    else set_err(A.ctl, EP_ERR_CUDA, p);
+    if (pos < A.S.start[nxt][c2 + 1]) {
+        A.S.list[nxt][pos] = p;
+        A.S.cellof[nxt][pos] = c2;
+    } else {
+        set_err(A.ctl, EP_ERR_CUDA, p);
+    }
 }
 
-// km_fbar: δJ = det(I + dt ∇v) - 1 of every point and its P2G Σ N m δJ; builds
-// the next step's cell lists (placement after the scan of the counts)
+// km_fbar: δJ = det(I + dt ∇v) - 1 and its P2G Σ N m δJ (deform.jl:9-18, volumetric.jl:1-11);
+// places the points into the next step's cell lists
 template <int BASIS>
-__global__ void __launch_bounds__(128) km_fbar(MCtx A) {
+__global__ void __launch_bounds__(256) km_fbar(MCtx A) {
     EP_ACTIVE(A.ctl);
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= A.g.ncell) return;
     const int cur = A.ctl->parity, nxt = cur ^ 1;
-    const int b = A.S.start[cur][c], e = A.S.start[cur][c + 1];
-    if (b == e) return;
-    const int ex = c / A.g.nel[1], ez = c - ex * A.g.nel[1];
-    const Axis4 ax = axis4(A.g, 0, ex), az = axis4(A.g, 1, ez);
-    const double axe = A.g.ax[0][ex], aze = A.g.ax[1][ez];
+    const Quad Q = quad_of(A, cur);
+    if (!Q.live || Q.b == Q.e) return;
+    const Axis4 ax = axis4(A.g, 0, Q.ex), az = axis4(A.g, 1, Q.ez);
     const float dtf = (float)A.ctl->dt;
-    int nid[16];
+    const int q = Q.q;
+    int nid[4];
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) nid[j + 4 * i] = (ax.cls[i] >= 0 && az.cls[j] >= 0) ? node2(A.g, ax, az, i, j) : -1;
-    float acc[16];
-#pragma unroll
-    for (int s = 0; s < 16; ++s) acc[s] = 0.f;
+    for (int j = 0; j < 4; ++j) nid[j] = (ax.cls[q] >= 0 && az.cls[j] >= 0) ? node2(A.g, ax, az, q, j) : -1;
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
     bool bad = false;
     float* const* vn = A.cf.musl ? A.N.vm : A.N.v;
-    for (int k = b; k < e; ++k) {
+    const bool fin = A.cf.deform == EP_DEFORM_FINITE;
+    for (int k = Q.b; k < Q.e; ++k) {
         const int p = A.S.list[cur][k];
-        float wx[4], dwx[4], wz[4], dwz[4];
-        point_w2<BASIS>(A, ax, az, p, cur, axe, aze, wx, dwx, wz, dwz, bad);
-        float gv[4];
-        grad_v(wx, dwx, wz, dwz, nid, vn, gv);
-        const float D00 = dtf * gv[0], D10 = dtf * gv[1], D01 = dtf * gv[2], D11 = dtf * gv[3];
+        float wx, dwx, wz[4], dwz[4];
+        quad_weights<BASIS>(A, ax, az, q, p, cur, wx, dwx, wz, dwz, bad);
+        float g00 = 0.f, g01 = 0.f, g10 = 0.f, g11 = 0.f;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            if (nid[j] < 0) continue;
+            const float Nx = dwx * wz[j], Nz = wx * dwz[j];
+            const float vx = __ldg(&vn[0][nid[j]]), vz = __ldg(&vn[1][nid[j]]);
+            g00 += Nx * vx;
+            g01 += Nz * vx;
+            g10 += Nx * vz;
+            g11 += Nz * vz;
+        }
+        g00 = quad_sum(g00);
+        g01 = quad_sum(g01);
+        g10 = quad_sum(g10);
+        g11 = quad_sum(g11);
+        const float D00 = dtf * g00, D10 = dtf * g10, D01 = dtf * g01, D11 = dtf * g11;
         const float dJ = D00 + D11 + (D00 * D11 - D01 * D10);
         // numerator mass ρΩ after the deformation update: finite ρ0Ω0 (unchanged), infinitesimal
         // ρ J Ω0 = m (1 + δJ), so the nodal sum carries m (1+δJ)^2 - m = m δJ (2 + δJ) (volumetric.jl:8)
-        const float mdj = A.P.mp[p] * (A.cf.deform == EP_DEFORM_FINITE ? dJ : dJ * (2.f + dJ));
+        const float mdj = A.P.mp[p] * (fin ? dJ : dJ * (2.f + dJ));
 #pragma unroll
-        for (int s = 0; s < 16; ++s) acc[s] += wx[s >> 2] * wz[s & 3] * mdj;
-        place_next(A, p, nxt);
+        for (int j = 0; j < 4; ++j) acc[j] += wx * wz[j] * mdj;
+        if (q == 0) place_next(A, p, nxt);
     }
+    if (bad) set_err(A.ctl, EP_ERR_INVALID_POSITION, Q.c);
 #pragma unroll
-    for (int s = 0; s < 16; ++s)
-        if (nid[s] >= 0) atomicAdd(&A.N.dJacc[nid[s]], acc[s]);
+    for (int j = 0; j < 4; ++j)
+        if (nid[j] >= 0) atomicAdd(&A.N.dJacc[nid[j]], acc[j]);
 }
 
 // km_dJn: nodal δJ_n = Σ N m δJ / m_n (volumetric.jl:12-22, increment form)
@@ -528,172 +580,259 @@ __device__ __forceinline__ float atanh_over_x(float x2) {
     return 0.5f * (log1pf(x) - log1pf(-x)) / x;
 }
 
-// km_cons: F-bar scaling, F update, elastic predictor and return map, point by point
-template <int BASIS>
-__global__ void __launch_bounds__(128) km_cons(MCtx A, int plastic_phase) {
+// ---------------------------------------------------------------------------
+// accumulated state: FP64 (ACC = 0) or double-float hi + lo (ACC = 1)
+
+// hi + lo += inc (Knuth two-sum, then renormalise); FP32 instructions only
+__device__ __forceinline__ void df_add(float& hi, float& lo, float inc) {
+    const float s = hi + inc;
+    const float bb = s - hi;
+    const float e = (hi - (s - bb)) + (inc - bb) + lo;
+    const float t = s + e;
+    lo = e - (t - s);
+    hi = t;
+}
+
+// hi + lo = 1 + dev exactly representable pair for a deviation dev from 1
+__device__ __forceinline__ void df_one_plus(float dev, float& hi, float& lo) {
+    hi = 1.f + dev;
+    lo = dev - (hi - 1.f);
+}
+
+// b = exp(2ε), ε = (e11, e22, e12), spectral form (DP.jl:65-66), as deviations from 1:
+// b_ii - 1 = (E - 1) + E (cosh 2s - 1 ± sinh(2s)/s ε_d), b_12 = E sinh(2s)/s e12
+__device__ __forceinline__ void exp2eps_dev(float e11, float e22, float e12, float em_expm1, float E, float* dev) {
+    const float ed = 0.5f * (e11 - e22);
+    const float s2 = ed * ed + e12 * e12;
+    float chm1, shs;   // cosh(2s) - 1, sinh(2s)/s
+    if (s2 < 1.0e-4f) {
+        chm1 = s2 * (2.f + s2 * (2.f / 3.f));
+        shs = 2.f * (1.f + s2 * (2.f / 3.f + s2 * (2.f / 15.f)));
+    } else {
+        const float s = sqrtf(s2);
+        chm1 = coshf(2.f * s) - 1.f;
+        shs = sinhf(2.f * s) / s;
+    }
+    dev[0] = em_expm1 + E * (chm1 + shs * ed);
+    dev[1] = em_expm1 + E * (chm1 - shs * ed);
+    dev[2] = E * (shs * e12);
+}
+
+// km_cons: F-bar scaling, F update, elastic predictor and return map, one lane per point
+template <int BASIS, int ACC>
+__global__ void __launch_bounds__(256) km_cons(MCtx A, int plastic_phase) {
     EP_ACTIVE(A.ctl);
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= A.g.ncell) return;
     const int cur = A.ctl->parity, nxt = cur ^ 1;
-    const int b = A.S.start[cur][c], e = A.S.start[cur][c + 1];
-    if (b == e) return;
-    const int ex = c / A.g.nel[1], ez = c - ex * A.g.nel[1];
-    const Axis4 ax = axis4(A.g, 0, ex), az = axis4(A.g, 1, ez);
-    const double axe = A.g.ax[0][ex], aze = A.g.ax[1][ez];
-    const float dtf = (float)A.ctl->dt;
-    int nid[16];
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) nid[j + 4 * i] = (ax.cls[i] >= 0 && az.cls[j] >= 0) ? node2(A.g, ax, az, i, j) : -1;
-    bool bad = false;
-    float* const* vn = A.cf.musl ? A.N.vm : A.N.v;
-    const bool fin = A.cf.deform == EP_DEFORM_FINITE, lock = A.cf.locking;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
     int nplastic = 0;
-    for (int k = b; k < e; ++k) {
-        const int p = A.S.list[cur][k];
+    if (k < A.S.start[cur][A.g.ncell]) {
+        const int p = A.S.list[cur][k], c = A.S.cellof[cur][k];
+        const int ex = c / A.g.nel[1], ez = c - ex * A.g.nel[1];
+        const Axis4 ax = axis4(A.g, 0, ex), az = axis4(A.g, 1, ez);
+        const float hx = (float)A.g.h[0], hz = (float)A.g.h[1];
+        const float dtf = (float)A.ctl->dt;
+        bool bad = false;
+        float* const* vn = A.cf.musl ? A.N.vm : A.N.v;
+        const bool fin = A.cf.deform == EP_DEFORM_FINITE, lock = A.cf.locking;
         float wx[4], dwx[4], wz[4], dwz[4];
-        point_w2<BASIS>(A, ax, az, p, cur, axe, aze, wx, dwx, wz, dwz, bad);
-        float gv[4];
-        grad_v(wx, dwx, wz, dwz, nid, vn, gv);
-        // D = ΔF - I (deform.jl:13)
-        float D[4] = {dtf * gv[0], dtf * gv[1], dtf * gv[2], dtf * gv[3]};
-        if (A.cf.trsfr == EP_TRSFR_TPIC)
-            for (int q = 0; q < 4; ++q) A.P.dv[q][p] = gv[q];
-        // F <- ΔF F with the unscaled ΔF (deform.jl:14); increment in FP32, sum in FP64
         {
-            double F0 = A.P.F[0][p], F1 = A.P.F[1][p], F2 = A.P.F[2][p], F3 = A.P.F[3][p];
-            const float f0 = (float)F0, f1 = (float)F1, f2 = (float)F2, f3 = (float)F3;
-            A.P.F[0][p] = F0 + (double)(D[0] * f0 + D[2] * f1);
-            A.P.F[1][p] = F1 + (double)(D[1] * f0 + D[3] * f1);
-            A.P.F[2][p] = F2 + (double)(D[0] * f2 + D[2] * f3);
-            A.P.F[3][p] = F3 + (double)(D[1] * f2 + D[3] * f3);
-            if (!fin) {
-                // infinitesimal: the mass ρ0 J Ω0 and volume J Ω0 follow J (deform.jl:41-43)
-                const double J = A.P.F[0][p] * A.P.F[3][p] - A.P.F[2][p] * A.P.F[1][p];
-                const float Om = (float)(J * (double)A.P.Om0[p]);
-                A.P.Om[p] = Om;
-                A.P.mp[p] = A.P.rho[p] * Om;        // ρΩ with ρ fixed (the reference's infinitesimal mass)
+            const float lx = BASIS == EP_BASIS_GIMPM ? A.P.l[0][p] : 0.f;
+            const float lz = BASIS == EP_BASIS_GIMPM ? A.P.l[1][p] : 0.f;
+            axis_w<BASIS>(ax, A.P.dx[cur][0][p], hx, 1.f / hx, lx, wx, dwx, bad);
+            axis_w<BASIS>(az, A.P.dx[cur][1][p], hz, 1.f / hz, lz, wz, dwz, bad);
+        }
+        float g00 = 0.f, g01 = 0.f, g10 = 0.f, g11 = 0.f, a = 0.f;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            if (ax.cls[i] < 0) continue;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                if (az.cls[j] < 0) continue;
+                const int n = node2(A.g, ax, az, i, j);
+                const float Nx = dwx[i] * wz[j], Nz = wx[i] * dwz[j];
+                const float vx = __ldg(&vn[0][n]), vz = __ldg(&vn[1][n]);
+                g00 += Nx * vx;
+                g01 += Nz * vx;
+                g10 += Nx * vz;
+                g11 += Nz * vz;
+                if (lock) a += wx[i] * wz[j] * __ldg(&A.N.dJn[n]);
             }
         }
-        // F-bar: ΔF <- (ΔJ̄/ΔJ)^(1/2) ΔF, with ΔJ̄ = Σ N ΔJ_n (volumetric.jl:23-36)
+        // D = ΔF - I = dt ∇v, column-major (deform.jl:13)
+        float D[4] = {dtf * g00, dtf * g10, dtf * g01, dtf * g11};
+        if (A.cf.trsfr == EP_TRSFR_TPIC) {
+            A.P.dv[0][p] = g00; A.P.dv[1][p] = g10; A.P.dv[2][p] = g01; A.P.dv[3][p] = g11;
+        }
+        // F <- ΔF F with the unscaled ΔF (deform.jl:14): F += D F
+        float Jm1 = 0.f;   // J - 1 (infinitesimal mass)
+        if (ACC == 0) {
+            const double F0 = A.P.Fd[0][p], F1 = A.P.Fd[1][p], F2 = A.P.Fd[2][p], F3 = A.P.Fd[3][p];
+            const float f0 = (float)F0, f1 = (float)F1, f2 = (float)F2, f3 = (float)F3;
+            const double N0 = F0 + (double)(D[0] * f0 + D[2] * f1);
+            const double N1 = F1 + (double)(D[1] * f0 + D[3] * f1);
+            const double N2 = F2 + (double)(D[0] * f2 + D[2] * f3);
+            const double N3 = F3 + (double)(D[1] * f2 + D[3] * f3);
+            A.P.Fd[0][p] = N0; A.P.Fd[1][p] = N1; A.P.Fd[2][p] = N2; A.P.Fd[3][p] = N3;
+            if (!fin) Jm1 = (float)(N0 * N3 - N2 * N1 - 1.0);
+        } else {
+            float h0 = A.P.Fh[0][p], h1 = A.P.Fh[1][p], h2 = A.P.Fh[2][p], h3 = A.P.Fh[3][p];
+            float l0 = A.P.Fl[0][p], l1 = A.P.Fl[1][p], l2 = A.P.Fl[2][p], l3 = A.P.Fl[3][p];
+            const float i0 = D[0] * h0 + D[2] * h1, i1 = D[1] * h0 + D[3] * h1;
+            const float i2 = D[0] * h2 + D[2] * h3, i3 = D[1] * h2 + D[3] * h3;
+            df_add(h0, l0, i0); df_add(h1, l1, i1); df_add(h2, l2, i2); df_add(h3, l3, i3);
+            A.P.Fh[0][p] = h0; A.P.Fh[1][p] = h1; A.P.Fh[2][p] = h2; A.P.Fh[3][p] = h3;
+            A.P.Fl[0][p] = l0; A.P.Fl[1][p] = l1; A.P.Fl[2][p] = l2; A.P.Fl[3][p] = l3;
+            if (!fin) {
+                // J - 1 = (F11-1) + (F22-1) + (F11-1)(F22-1) - F12 F21, deviations formed exactly
+                const float a0 = (h0 - 1.f) + l0, a3 = (h3 - 1.f) + l3;
+                Jm1 = a0 + a3 + (a0 * a3 - (h2 + l2) * (h1 + l1));
+            }
+        }
+        if (!fin) {
+            // infinitesimal: volume J Ω0 and mass ρ J Ω0 follow J (deform.jl:41-43)
+            const float Om = A.P.Om0[p] + A.P.Om0[p] * Jm1;
+            A.P.Om[p] = Om;
+            A.P.mp[p] = A.P.rho[p] * Om;
+        }
+        // F-bar: ΔF <- (ΔJ̄/ΔJ)^(1/2) ΔF, ΔJ̄ = Σ N ΔJ_n (volumetric.jl:23-36), increment form
         if (lock) {
             const float dJp = D[0] + D[3] + (D[0] * D[3] - D[2] * D[1]);
-            float a = 0.f;
-#pragma unroll
-            for (int s = 0; s < 16; ++s)
-                if (nid[s] >= 0) a += wx[s >> 2] * wz[s & 3] * __ldg(&A.N.dJn[nid[s]]);
-            const float r1 = (a - dJp) / (1.f + dJp);           // ΔJ̄/ΔJ - 1
-            const float s1 = r1 / (1.f + sqrtf(1.f + r1));      // sqrt(1 + r1) - 1
+            const float r1 = (a - dJp) / (1.f + dJp);          // ΔJ̄/ΔJ - 1
+            const float s1 = r1 / (1.f + sqrtf(1.f + r1));     // sqrt(1 + r1) - 1
             D[0] = D[0] * (1.f + s1) + s1;
             D[1] = D[1] * (1.f + s1);
             D[2] = D[2] * (1.f + s1);
             D[3] = D[3] * (1.f + s1) + s1;
         }
-        float t[3];
+        float tt[3];
         if (fin) {
-            // b <- ΔF b ΔF' = b + (D b + b D' + D b D') (elast.jl:49)
-            double B0 = A.P.b[0][p], B1 = A.P.b[1][p], B2 = A.P.b[2][p];   // b11, b22, b12
-            const float b11 = (float)B0, b22 = (float)B1, b12 = (float)B2;
-            const float M00 = D[0] * b11 + D[2] * b12, M01 = D[0] * b12 + D[2] * b22;   // M = D b
-            const float M10 = D[1] * b11 + D[3] * b12, M11 = D[1] * b12 + D[3] * b22;
-            const float i11 = 2.f * M00 + (M00 * D[0] + M01 * D[2]);
-            const float i22 = 2.f * M11 + (M10 * D[1] + M11 * D[3]);
-            const float i12 = M10 + M01 + (M00 * D[1] + M01 * D[3]);
-            B0 += (double)i11;
-            B1 += (double)i22;
-            B2 += (double)i12;
-            A.P.b[0][p] = B0;
-            A.P.b[1][p] = B1;
-            A.P.b[2][p] = B2;
-            // ε = ½ log b (elast.jl:51-52), spectral form
-            const double m = 0.5 * (B0 + B1);
-            const float dd = (float)(0.5 * (B0 - B1)), q = (float)B2, mf = (float)m;
-            const float x2 = (dd * dd + q * q) / (mf * mf);
-            const float L0 = (float)ep_log(m) + 0.5f * log1pf(-x2);
+            // b <- ΔF b ΔF' = b + (D b + b D' + D b D') (elast.jl:49), then ε = ½ log b (elast.jl:51-52)
+            float b11, b22, b12, mu, dd, qq;
+            if (ACC == 0) {
+                double B0 = A.P.bd[0][p], B1 = A.P.bd[1][p], B2 = A.P.bd[2][p];
+                b11 = (float)B0; b22 = (float)B1; b12 = (float)B2;
+                const float M00 = D[0] * b11 + D[2] * b12, M01 = D[0] * b12 + D[2] * b22;
+                const float M10 = D[1] * b11 + D[3] * b12, M11 = D[1] * b12 + D[3] * b22;
+                B0 += (double)(2.f * M00 + (M00 * D[0] + M01 * D[2]));
+                B1 += (double)(2.f * M11 + (M10 * D[1] + M11 * D[3]));
+                B2 += (double)(M10 + M01 + (M00 * D[1] + M01 * D[3]));
+                A.P.bd[0][p] = B0; A.P.bd[1][p] = B1; A.P.bd[2][p] = B2;
+                const double m = 0.5 * (B0 + B1);
+                dd = (float)(0.5 * (B0 - B1));
+                qq = (float)B2;
+                mu = (float)(m - 1.0);
+                // log m in FP64 (the isotropic part of log b_e)
+                tt[0] = (float)ep_log(m);
+            } else {
+                float h0 = A.P.bh[0][p], h1 = A.P.bh[1][p], h2 = A.P.bh[2][p];
+                float l0 = A.P.bl[0][p], l1 = A.P.bl[1][p], l2 = A.P.bl[2][p];
+                b11 = h0; b22 = h1; b12 = h2;
+                const float M00 = D[0] * b11 + D[2] * b12, M01 = D[0] * b12 + D[2] * b22;
+                const float M10 = D[1] * b11 + D[3] * b12, M11 = D[1] * b12 + D[3] * b22;
+                df_add(h0, l0, 2.f * M00 + (M00 * D[0] + M01 * D[2]));
+                df_add(h1, l1, 2.f * M11 + (M10 * D[1] + M11 * D[3]));
+                df_add(h2, l2, M10 + M01 + (M00 * D[1] + M01 * D[3]));
+                A.P.bh[0][p] = h0; A.P.bh[1][p] = h1; A.P.bh[2][p] = h2;
+                A.P.bl[0][p] = l0; A.P.bl[1][p] = l1; A.P.bl[2][p] = l2;
+                // deviations from 1 formed exactly from the pairs (h - 1 is exact near 1)
+                mu = 0.5f * (((h0 - 1.f) + (h1 - 1.f)) + (l0 + l1));
+                dd = 0.5f * ((h0 - h1) + (l0 - l1));
+                qq = h2 + l2;
+                tt[0] = log1pf(mu);   // log m, m = 1 + μ
+            }
+            const float mf = 1.f + mu;
+            const float x2 = (dd * dd + qq * qq) / (mf * mf);
+            const float L0 = tt[0] + 0.5f * log1pf(-x2);
             const float kd = atanh_over_x(x2) / mf;
-            const float e11 = 0.5f * (L0 + kd * dd), e22 = 0.5f * (L0 - kd * dd), e12 = 0.5f * kd * q;
-            // τ = Del voigt(ε, 2) (elast.jl:54)
+            const float e11 = 0.5f * (L0 + kd * dd), e22 = 0.5f * (L0 - kd * dd), e12 = 0.5f * kd * qq;
             const float v2 = 2.f * e12;
-            t[0] = A.Del[0] * e11 + A.Del[3] * e22 + A.Del[6] * v2;
-            t[1] = A.Del[1] * e11 + A.Del[4] * e22 + A.Del[7] * v2;
-            t[2] = A.Del[2] * e11 + A.Del[5] * e22 + A.Del[8] * v2;
+            tt[0] = A.Del[0] * e11 + A.Del[3] * e22 + A.Del[6] * v2;
+            tt[1] = A.Del[1] * e11 + A.Del[4] * e22 + A.Del[7] * v2;
+            tt[2] = A.Del[2] * e11 + A.Del[5] * e22 + A.Del[8] * v2;
         } else {
             // σ += Del voigt(sym(ΔF) - I, 2) (+ ωσ - σω for the objective rate) (elast.jl:73-78)
-            t[0] = A.P.tau[0][p]; t[1] = A.P.tau[1][p]; t[2] = A.P.tau[2][p];
+            tt[0] = A.P.tau[0][p]; tt[1] = A.P.tau[1][p]; tt[2] = A.P.tau[2][p];
             const float e11 = D[0], e22 = D[3], g12 = D[1] + D[2];
             float d0 = A.Del[0] * e11 + A.Del[3] * e22 + A.Del[6] * g12;
             float d1 = A.Del[1] * e11 + A.Del[4] * e22 + A.Del[7] * g12;
             float d2 = A.Del[2] * e11 + A.Del[5] * e22 + A.Del[8] * g12;
             if (A.cf.jaumann) {
-                const float w = 0.5f * (D[2] - D[1]);                 // ω12
-                d0 += 2.f * w * t[2];
-                d1 -= 2.f * w * t[2];
-                d2 += w * (t[1] - t[0]);
+                const float w = 0.5f * (D[2] - D[1]);
+                d0 += 2.f * w * tt[2];
+                d1 -= 2.f * w * tt[2];
+                d2 += w * (tt[1] - tt[0]);
             }
-            t[0] += d0; t[1] += d1; t[2] += d2;
+            tt[0] += d0; tt[1] += d1; tt[2] += d2;
         }
         if (plastic_phase) {
-            const double ep1 = A.P.ep1[p];
-            const float ep2 = A.cf.nonloc ? A.P.ep2[p] : (float)ep1;
+            float ep1f = ACC == 0 ? (float)A.P.ep1d[p] : A.P.ep1h[p] + A.P.ep1l[p];
+            const float ep2 = A.cf.nonloc ? A.P.ep2[p] : ep1f;
+            bool yielded = false;
+            float inc = 0.f, newg = 0.f;
+            bool absolute = false;
             if (A.cf.cons == EP_CONS_DP) {
-                float dep;
-                const float dl = dp32(t, ep2, A.P.c0[p], A.P.cr[p], A.P.tphi[p], A.Hp, A.Kc, A.Gc, &dep);
+                const float dl = dp32(tt, ep2, A.P.c0[p], A.P.cr[p], A.P.tphi[p], A.Hp, A.Kc, A.Gc, &inc);
                 A.P.dlam[p] = dl;
-                if (dl != 0.f) {
-                    ++nplastic;
-                    A.P.ep1[p] = ep1 + (double)dep;
-                    if (fin) {
-                        // ε = tensor(Del \ τ, ½); b = exp(2ε) (DP.jl:63-66), spectral form
-                        const float e11 = A.Cmp[0] * t[0] + A.Cmp[3] * t[1] + A.Cmp[6] * t[2];
-                        const float e22 = A.Cmp[1] * t[0] + A.Cmp[4] * t[1] + A.Cmp[7] * t[2];
-                        const float e12 = 0.5f * (A.Cmp[2] * t[0] + A.Cmp[5] * t[1] + A.Cmp[8] * t[2]);
-                        const float em = 0.5f * (e11 + e22), ed = 0.5f * (e11 - e22);
-                        const float s2 = ed * ed + e12 * e12;
-                        float ch, shs;   // cosh(2s), sinh(2s)/s
-                        if (s2 < 1.0e-4f) {
-                            ch = 1.f + s2 * (2.f + s2 * (2.f / 3.f));
-                            shs = 2.f * (1.f + s2 * (2.f / 3.f + s2 * (2.f / 15.f)));
-                        } else {
-                            const float s = sqrtf(s2);
-                            ch = coshf(2.f * s);
-                            shs = sinhf(2.f * s) / s;
-                        }
-                        const double E = ep_exp(2.0 * (double)em);
-                        A.P.b[0][p] = E * (double)(ch + shs * ed);
-                        A.P.b[1][p] = E * (double)(ch - shs * ed);
-                        A.P.b[2][p] = E * (double)(shs * e12);
-                    }
-                }
+                yielded = dl != 0.f;
             } else {
-                float g;
-                const float Dl[9] = {A.Del[0], A.Del[1], A.Del[2], A.Del[3], A.Del[4], A.Del[5], A.Del[6], A.Del[7], A.Del[8]};
-                if (j232(t, ep2, A.P.c0[p], A.P.cr[p], A.Hp, Dl, &g)) {
-                    A.P.ep1[p] = (double)g;
-                    if (fin) {
-                        const float e11 = A.Cmp[0] * t[0] + A.Cmp[3] * t[1] + A.Cmp[6] * t[2];
-                        const float e22 = A.Cmp[1] * t[0] + A.Cmp[4] * t[1] + A.Cmp[7] * t[2];
-                        const float e12 = 0.5f * (A.Cmp[2] * t[0] + A.Cmp[5] * t[1] + A.Cmp[8] * t[2]);
-                        const float em = 0.5f * (e11 + e22), ed = 0.5f * (e11 - e22);
-                        const float s2 = ed * ed + e12 * e12;
-                        const float s = sqrtf(s2);
-                        const float ch = coshf(2.f * s), shs = s2 > 0.f ? sinhf(2.f * s) / s : 2.f;
-                        const double E = ep_exp(2.0 * (double)em);
-                        A.P.b[0][p] = E * (double)(ch + shs * ed);
-                        A.P.b[1][p] = E * (double)(ch - shs * ed);
-                        A.P.b[2][p] = E * (double)(shs * e12);
+                const float Dl[9] = {A.Del[0], A.Del[1], A.Del[2], A.Del[3], A.Del[4],
+                                     A.Del[5], A.Del[6], A.Del[7], A.Del[8]};
+                yielded = j232(tt, ep2, A.P.c0[p], A.P.cr[p], A.Hp, Dl, &newg) != 0;
+                absolute = true;
+            }
+            if (yielded) {
+                ++nplastic;
+                if (ACC == 0) {
+                    A.P.ep1d[p] = absolute ? (double)newg : A.P.ep1d[p] + (double)inc;
+                } else {
+                    float h = A.P.ep1h[p], l = A.P.ep1l[p];
+                    if (absolute) { h = newg; l = 0.f; }
+                    else df_add(h, l, inc);
+                    A.P.ep1h[p] = h;
+                    A.P.ep1l[p] = l;
+                }
+                if (fin) {
+                    // ε = tensor(Del \ τ, ½); b = exp(2ε) (DP.jl:63-66)
+                    const float e11 = A.Cmp[0] * tt[0] + A.Cmp[3] * tt[1] + A.Cmp[6] * tt[2];
+                    const float e22 = A.Cmp[1] * tt[0] + A.Cmp[4] * tt[1] + A.Cmp[7] * tt[2];
+                    const float e12 = 0.5f * (A.Cmp[2] * tt[0] + A.Cmp[5] * tt[1] + A.Cmp[8] * tt[2]);
+                    const float em = 0.5f * (e11 + e22);
+                    float E, Em1;
+                    if (ACC == 0) {
+                        const double Ed = ep_exp(2.0 * (double)em);   // e^{2 e_m} in FP64
+                        E = (float)Ed;
+                        Em1 = (float)(Ed - 1.0);
+                    } else {
+                        Em1 = expm1f(2.f * em);
+                        E = 1.f + Em1;
+                    }
+                    float dev[3];
+                    exp2eps_dev(e11, e22, e12, Em1, E, dev);
+                    if (ACC == 0) {
+                        A.P.bd[0][p] = 1.0 + (double)dev[0];
+                        A.P.bd[1][p] = 1.0 + (double)dev[1];
+                        A.P.bd[2][p] = (double)dev[2];
+                    } else {
+                        float h, l;
+                        df_one_plus(dev[0], h, l);
+                        A.P.bh[0][p] = h; A.P.bl[0][p] = l;
+                        df_one_plus(dev[1], h, l);
+                        A.P.bh[1][p] = h; A.P.bl[1][p] = l;
+                        A.P.bh[2][p] = dev[2]; A.P.bl[2][p] = 0.f;
                     }
                 }
             }
         }
-        A.P.tau[0][p] = t[0];
-        A.P.tau[1][p] = t[1];
-        A.P.tau[2][p] = t[2];
-        if (!(isfinite(t[0]) && isfinite(t[1]) && isfinite(t[2]))) set_err(A.ctl, EP_ERR_NONFINITE, p);
+        A.P.tau[0][p] = tt[0];
+        A.P.tau[1][p] = tt[1];
+        A.P.tau[2][p] = tt[2];
+        if (!(isfinite(tt[0]) && isfinite(tt[1]) && isfinite(tt[2]))) set_err(A.ctl, EP_ERR_NONFINITE, p);
         if (!lock) place_next(A, p, nxt);
+        if (bad) set_err(A.ctl, EP_ERR_INVALID_POSITION, c);
     }
-    if (bad) set_err(A.ctl, EP_ERR_INVALID_POSITION, c);
-    if (nplastic) atomicAdd((unsigned long long*)&A.ctl->plastic, (unsigned long long)nplastic);
+    // plastic point count: one atomic per warp
+    const int tot = __reduce_add_sync(0xffffffffu, nplastic);
+    if ((threadIdx.x & 31) == 0 && tot) atomicAdd((unsigned long long*)&A.ctl->plastic, (unsigned long long)tot);
 }
 
 __global__ void km_flip(Ctl* ctl) {
@@ -701,27 +840,132 @@ __global__ void km_flip(Ctl* ctl) {
 }
 
 // ---------------------------------------------------------------------------
-// import / export between the FP64 staging layout (P64, the reference's
-// arrays in SoA) and the mixed state
-__global__ void km_import(MCtx A, P64 Q, int with_topology) {
+// exclusive scan of count[nxt] into start[nxt] (parity read on the device)
+constexpr int MSCAN_BS = 1024, MSCAN_IPT = 4, MSCAN_CHUNK = MSCAN_BS * MSCAN_IPT;
+
+__device__ __forceinline__ int mwarp_scan(int v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += t;
+    }
+    return v;
+}
+
+__device__ __forceinline__ int mblock_scan(int v, int* tot) {
+    __shared__ int ws[33];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int inc = mwarp_scan(v);
+    if (lane == 31) ws[wid] = inc;
+    __syncthreads();
+    if (wid == 0) {
+        int s = lane < nw ? ws[lane] : 0;
+        int si = mwarp_scan(s);
+        if (lane < nw) ws[lane] = si - s;
+        if (lane == 31) ws[32] = si;
+    }
+    __syncthreads();
+    int r = ws[wid] + inc - v;
+    *tot = ws[32];
+    __syncthreads();
+    return r;
+}
+
+// which = 0: scan count[nxt] -> start[nxt] (inside a step); 1: count[cur] -> start[cur] (set-up)
+__global__ void km_scan_local(MCtx A, int which, int* bsum) {
+    if (which == 0 && !A.ctl->active) return;
+    const int par = which == 0 ? (A.ctl->parity ^ 1) : A.ctl->parity;
+    const int n = A.g.ncell;
+    const int* in = A.S.count[par];
+    int* out = A.S.start[par];
+    const int base = blockIdx.x * MSCAN_CHUNK + threadIdx.x * MSCAN_IPT;
+    int v[MSCAN_IPT], s = 0;
+#pragma unroll
+    for (int i = 0; i < MSCAN_IPT; ++i) {
+        v[i] = base + i < n ? in[base + i] : 0;
+        s += v[i];
+    }
+    int tot;
+    int ex = mblock_scan(s, &tot);
+#pragma unroll
+    for (int i = 0; i < MSCAN_IPT; ++i) {
+        if (base + i < n) out[base + i] = ex;
+        ex += v[i];
+    }
+    if (threadIdx.x == 0) bsum[blockIdx.x] = tot;
+}
+
+__global__ void km_scan_sums(MCtx A, int which, int* bsum, int nb) {
+    if (which == 0 && !A.ctl->active) return;
+    const int par = which == 0 ? (A.ctl->parity ^ 1) : A.ctl->parity;
+    const int base = threadIdx.x * MSCAN_IPT;
+    int v[MSCAN_IPT], s = 0;
+#pragma unroll
+    for (int i = 0; i < MSCAN_IPT; ++i) {
+        v[i] = base + i < nb ? bsum[base + i] : 0;
+        s += v[i];
+    }
+    int tot;
+    int ex = mblock_scan(s, &tot);
+#pragma unroll
+    for (int i = 0; i < MSCAN_IPT; ++i) {
+        if (base + i < nb) bsum[base + i] = ex;
+        ex += v[i];
+    }
+    if (threadIdx.x == 0) A.S.start[par][A.g.ncell] = tot;
+}
+
+__global__ void km_scan_add(MCtx A, int which, const int* bsum) {
+    if (which == 0 && !A.ctl->active) return;
+    const int par = which == 0 ? (A.ctl->parity ^ 1) : A.ctl->parity;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < A.g.ncell) A.S.start[par][i] += bsum[i / MSCAN_CHUNK];
+}
+
+static int mixed_scan(const MCtx& A, int which, int* bsum, cudaStream_t s) {
+    const int n = A.g.ncell, nb = (n + MSCAN_CHUNK - 1) / MSCAN_CHUNK;
+    km_scan_local<<<nb, MSCAN_BS, 0, s>>>(A, which, bsum);
+    km_scan_sums<<<1, MSCAN_BS, 0, s>>>(A, which, bsum, nb);
+    if (nb > 1) km_scan_add<<<(n + 255) / 256, 256, 0, s>>>(A, which, bsum);
+    return nb > 1 ? 3 : 2;
+}
+
+// ---------------------------------------------------------------------------
+// import / export between the FP64 staging layout (P64: the reference's
+// arrays as SoA) and the mixed state
+__global__ void km_import(MCtx A, P64 Q) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= A.P.np) return;
-    const int cur = A.ctl->parity;
     for (int d = 0; d < 2; ++d) {
-        A.P.x[cur][d][p] = Q.x[d][p];
         A.P.v[d][p] = (float)Q.v[d][p];
         if (A.cf.basis == EP_BASIS_GIMPM) A.P.l[d][p] = (float)Q.l[d][p];
     }
-    for (int k = 0; k < 4; ++k) {
-        A.P.F[k][p] = Q.F[k][p];
-        if (A.cf.trsfr == EP_TRSFR_TPIC) A.P.dv[k][p] = (float)Q.dv[k][p];
+    const double b12 = 0.5 * (Q.b[2][p] + Q.b[1][p]);
+    const double bsym[3] = {Q.b[0][p], Q.b[3][p], b12};
+    if (A.acc == 0) {
+        for (int k = 0; k < 4; ++k) A.P.Fd[k][p] = Q.F[k][p];
+        for (int k = 0; k < 3; ++k) A.P.bd[k][p] = bsym[k];
+        A.P.ep1d[p] = Q.ep1[p];
+    } else {
+        for (int k = 0; k < 4; ++k) {
+            const float h = (float)Q.F[k][p];
+            A.P.Fh[k][p] = h;
+            A.P.Fl[k][p] = (float)(Q.F[k][p] - (double)h);
+        }
+        for (int k = 0; k < 3; ++k) {
+            const float h = (float)bsym[k];
+            A.P.bh[k][p] = h;
+            A.P.bl[k][p] = (float)(bsym[k] - (double)h);
+        }
+        const float h = (float)Q.ep1[p];
+        A.P.ep1h[p] = h;
+        A.P.ep1l[p] = (float)(Q.ep1[p] - (double)h);
     }
-    A.P.b[0][p] = Q.b[0][p];
-    A.P.b[1][p] = Q.b[3][p];
-    A.P.b[2][p] = 0.5 * (Q.b[2][p] + Q.b[1][p]);
+    if (A.cf.trsfr == EP_TRSFR_TPIC)
+        for (int k = 0; k < 4; ++k) A.P.dv[k][p] = (float)Q.dv[k][p];
     const bool fin = A.cf.deform == EP_DEFORM_FINITE;
     for (int k = 0; k < 3; ++k) A.P.tau[k][p] = (float)(fin ? Q.tau[k][p] : Q.sig[k][p]);
-    A.P.ep1[p] = Q.ep1[p];
     A.P.ep2[p] = (float)Q.ep2[p];
     A.P.dlam[p] = (float)Q.dlam[p];
     A.P.c0[p] = (float)Q.c0[p];
@@ -735,33 +979,73 @@ __global__ void km_import(MCtx A, P64 Q, int with_topology) {
     A.P.rho[p] = (float)Q.rho[p];
 }
 
+// initial cell, offsets and counts from the FP64 positions of the staging layout
+__global__ void km_bin0(MCtx A, P64 Q) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= A.P.np) return;
+    const int cur = A.ctl->parity;
+    const double x = Q.x[0][p], z = Q.x[1][p];
+    int c2 = -1;
+    if (isfinite(x) && isfinite(z)) {
+        const int ex = (int)fmin(fmax(floor((x - A.g.x0[0]) / A.g.h[0]), 0.0), (double)(A.g.nel[0] - 1));
+        const int ez = (int)fmin(fmax(floor((z - A.g.x0[1]) / A.g.h[1]), 0.0), (double)(A.g.nel[1] - 1));
+        c2 = ez + A.g.nel[1] * ex;
+        A.P.dx[cur][0][p] = (float)(x - A.g.ax[0][ex]);
+        A.P.dx[cur][1][p] = (float)(z - A.g.ax[1][ez]);
+        atomicAdd(&A.S.count[cur][c2], 1);
+    } else {
+        set_err(A.ctl, EP_ERR_NONFINITE, p);
+    }
+    A.P.p2e_next[p] = c2;
+}
+
+__global__ void km_place0(MCtx A) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= A.P.np) return;
+    place_next(A, p, A.ctl->parity);
+}
+
 __global__ void km_export(MCtx A, P64 Q) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= A.P.np) return;
     const int cur = A.ctl->parity;
+    const int c = A.P.p2e_next[p];
+    Q.p2e[p] = c;
+    if (c >= 0) {
+        const int ex = c / A.g.nel[1], ez = c - ex * A.g.nel[1];
+        Q.x[0][p] = A.g.ax[0][ex] + (double)A.P.dx[cur][0][p];
+        Q.x[1][p] = A.g.ax[1][ez] + (double)A.P.dx[cur][1][p];
+    }
     for (int d = 0; d < 2; ++d) {
-        Q.x[d][p] = A.P.x[cur][d][p];
         Q.v[d][p] = (double)A.P.v[d][p];
         if (A.cf.basis == EP_BASIS_GIMPM) Q.l[d][p] = (double)A.P.l[d][p];
     }
-    const double F0 = A.P.F[0][p], F1 = A.P.F[1][p], F2 = A.P.F[2][p], F3 = A.P.F[3][p];
-    Q.F[0][p] = F0; Q.F[1][p] = F1; Q.F[2][p] = F2; Q.F[3][p] = F3;
-    const double J = F0 * F3 - F2 * F1;
+    double F[4], B[3], e1;
+    if (A.acc == 0) {
+        for (int k = 0; k < 4; ++k) F[k] = A.P.Fd[k][p];
+        for (int k = 0; k < 3; ++k) B[k] = A.P.bd[k][p];
+        e1 = A.P.ep1d[p];
+    } else {
+        for (int k = 0; k < 4; ++k) F[k] = (double)A.P.Fh[k][p] + (double)A.P.Fl[k][p];
+        for (int k = 0; k < 3; ++k) B[k] = (double)A.P.bh[k][p] + (double)A.P.bl[k][p];
+        e1 = (double)A.P.ep1h[p] + (double)A.P.ep1l[p];
+    }
+    for (int k = 0; k < 4; ++k) Q.F[k][p] = F[k];
+    const double J = F[0] * F[3] - F[2] * F[1];
     Q.J[p] = J;
     Q.Om[p] = J * Q.Om0[p];
     const bool fin = A.cf.deform == EP_DEFORM_FINITE;
     if (fin) {
         Q.rho[p] = Q.rho0[p] / J;
         Q.n[p] = 1.0 - 1.0 / J * (1.0 - Q.n0[p]);
-        const double B0 = A.P.b[0][p], B1 = A.P.b[1][p], B2 = A.P.b[2][p];
-        Q.b[0][p] = B0; Q.b[3][p] = B1; Q.b[1][p] = B2; Q.b[2][p] = B2;
+        Q.b[0][p] = B[0]; Q.b[3][p] = B[1]; Q.b[1][p] = B[2]; Q.b[2][p] = B[2];
         for (int k = 0; k < 3; ++k) {
             Q.tau[k][p] = (double)A.P.tau[k][p];
             Q.sig[k][p] = (double)A.P.tau[k][p] / J;
         }
         // ϵ = ½ log b (FP64, for output)
         double lam[2], V[4], L[2], R[4];
-        eig_sym2(B0, B2, B1, lam, V);
+        eig_sym2(B[0], B[2], B[1], lam, V);
         L[0] = ep_log(lam[0]);
         L[1] = ep_log(lam[1]);
         vdvt<2>(V, L, R);
@@ -771,16 +1055,9 @@ __global__ void km_export(MCtx A, P64 Q) {
     }
     if (A.cf.trsfr == EP_TRSFR_TPIC)
         for (int k = 0; k < 4; ++k) Q.dv[k][p] = (double)A.P.dv[k][p];
-    Q.ep1[p] = A.P.ep1[p];
-    Q.ep2[p] = A.cf.nonloc ? (double)A.P.ep2[p] : A.P.ep1[p];
+    Q.ep1[p] = e1;
+    Q.ep2[p] = A.cf.nonloc ? (double)A.P.ep2[p] : e1;
     Q.dlam[p] = (double)A.P.dlam[p];
-    // element of the current position (for p2e/p2n on download)
-    const double fx = floor((Q.x[0][p] - A.g.x0[0]) / A.g.h[0]), fz = floor((Q.x[1][p] - A.g.x0[1]) / A.g.h[1]);
-    int c2 = -1;
-    if (fx == fx && fz == fz)
-        c2 = (int)fmin(fmax(fz, 0.0), (double)(A.g.nel[1] - 1)) +
-             A.g.nel[1] * (int)fmin(fmax(fx, 0.0), (double)(A.g.nel[0] - 1));
-    Q.p2e[p] = c2;
 }
 
 __global__ void km_export_nodes(MCtx A, N64 Q) {
@@ -796,125 +1073,74 @@ __global__ void km_export_nodes(MCtx A, N64 Q) {
     Q.dJ[n] = 1.0 + (double)A.N.dJn[n];
 }
 
-// initial cell lists (positions of the current buffer)
-__global__ void km_bin0(MCtx A) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= A.P.np) return;
-    const int cur = A.ctl->parity;
-    const double fx = floor((A.P.x[cur][0][p] - A.g.x0[0]) / A.g.h[0]);
-    const double fz = floor((A.P.x[cur][1][p] - A.g.x0[1]) / A.g.h[1]);
-    int c2 = -1;
-    if (isfinite(A.P.x[cur][0][p]) && isfinite(A.P.x[cur][1][p])) {
-        c2 = (int)fmin(fmax(fz, 0.0), (double)(A.g.nel[1] - 1)) +
-             A.g.nel[1] * (int)fmin(fmax(fx, 0.0), (double)(A.g.nel[0] - 1));
-        atomicAdd(&A.S.count[cur][c2], 1);
-    } else {
-        set_err(A.ctl, EP_ERR_NONFINITE, p);
-    }
-    A.P.p2e_next[p] = c2;
-}
-
-__global__ void km_place0(MCtx A) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= A.P.np) return;
-    place_next(A, p, A.ctl->parity);
-}
-
 // ---------------------------------------------------------------------------
-template <int BASIS>
+template <int BASIS, int ACC>
 static void mixed_step_impl(const MixedCtx& X, int phase, cudaStream_t s) {
     const MCtx& A = *(const MCtx*)X.impl;
-    const int nc = A.g.ncell, nn = A.g.nnode;
-    const int TB = 128;
-    const int gc = (nc + TB - 1) / TB, gn = (nn + TB - 1) / TB;
+    const int nc = A.g.ncell, nn = A.g.nnode, np = A.P.np;
+    const int gq = (4 * nc + 255) / 256, gn = (nn + 255) / 256, gp = (np + 255) / 256;
     Prof* pr = (X.prof && X.prof->on) ? X.prof : nullptr;
     auto mark = [&](const char* nm) {
         if (pr) pr->mark(nm, s);
     };
-    // grid accumulators of this step and next-step counters (one contiguous block each)
+    long long L = 0;
     cudaMemsetAsync(X.grid_zero, 0, X.grid_zero_bytes, s);
     cudaMemsetAsync(X.sort_zero, 0, X.sort_zero_bytes, s);   // both parities' counts and the cursor
     mark("memset");
-    km_p2g<BASIS><<<gc, TB, 0, s>>>(A);
+    km_p2g<BASIS><<<gq, 256, 0, s>>>(A);
     mark("p2g");
-    km_solve<<<gn, TB, 0, s>>>(A);
+    km_solve<<<gn, 256, 0, s>>>(A);
     mark("solve");
-    km_g2p<BASIS><<<gc, TB, 0, s>>>(A);
+    km_g2p<BASIS><<<gq, 256, 0, s>>>(A);
     mark("g2p");
-    if (A.cf.musl) { km_vmusl<<<gn, TB, 0, s>>>(A); mark("vmusl"); }
-    launch_mixed_scan(X, s);
+    L += 3;
+    if (A.cf.musl) { km_vmusl<<<gn, 256, 0, s>>>(A); mark("vmusl"); ++L; }
+    L += mixed_scan(A, 0, X.scan_in, s);
     mark("scan");
     if (A.cf.locking) {
-        km_fbar<BASIS><<<gc, TB, 0, s>>>(A);
+        km_fbar<BASIS><<<gq, 256, 0, s>>>(A);
         mark("fbar");
-        km_dJn<<<gn, TB, 0, s>>>(A);
+        km_dJn<<<gn, 256, 0, s>>>(A);
         mark("dJn");
+        L += 2;
     }
-    km_cons<BASIS><<<gc, TB, 0, s>>>(A, phase == EP_PHASE_ELASTOPLASTIC);
-    mark("cons");
+    if (np > 0) {
+        km_cons<BASIS, ACC><<<gp, 256, 0, s>>>(A, phase == EP_PHASE_ELASTOPLASTIC);
+        mark("cons");
+        ++L;
+    }
     km_flip<<<1, 1, 0, s>>>(A.ctl);
-    if (X.launches) *X.launches += 5 + 2 + (nc > 4096 ? 3 : 2) + (A.cf.musl ? 1 : 0) + (A.cf.locking ? 2 : 0);
+    ++L;
+    if (X.launches) *X.launches += L;
+}
+
+template <int ACC>
+static void mixed_step_acc(const MixedCtx& X, int phase, cudaStream_t s) {
+    const MCtx& A = *(const MCtx*)X.impl;
+    if (A.cf.basis == EP_BASIS_BSMPM) mixed_step_impl<EP_BASIS_BSMPM, ACC>(X, phase, s);
+    else if (A.cf.basis == EP_BASIS_GIMPM) mixed_step_impl<EP_BASIS_GIMPM, ACC>(X, phase, s);
+    else mixed_step_impl<EP_BASIS_SMPM, ACC>(X, phase, s);
 }
 
 void mixed_step(const MixedCtx& X, int phase, cudaStream_t s) {
     const MCtx& A = *(const MCtx*)X.impl;
-    if (A.cf.basis == EP_BASIS_BSMPM) mixed_step_impl<EP_BASIS_BSMPM>(X, phase, s);
-    else if (A.cf.basis == EP_BASIS_GIMPM) mixed_step_impl<EP_BASIS_GIMPM>(X, phase, s);
-    else mixed_step_impl<EP_BASIS_SMPM>(X, phase, s);
+    if (A.acc == 0) mixed_step_acc<0>(X, phase, s);
+    else mixed_step_acc<1>(X, phase, s);
 }
 
-// exclusive scan of the next-parity counts into the next-parity starts; the
-// parity lives on the device, so scan both candidate buffers' roles through a
-// tiny selector kernel: copy counts[nxt] to the scan input first
-__global__ void km_sel_counts(MCtx A, int* dst) {
-    const int cur = A.ctl->parity, nxt = cur ^ 1;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < A.g.ncell) dst[i] = A.ctl->active ? A.S.count[nxt][i] : 0;
-}
-__global__ void km_put_starts(MCtx A, const int* src) {
-    if (!A.ctl->active) return;
-    const int cur = A.ctl->parity, nxt = cur ^ 1;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i <= A.g.ncell) A.S.start[nxt][i] = src[i];
-}
+void launch_mixed_scan(const MixedCtx& X, cudaStream_t s) { mixed_scan(*(const MCtx*)X.impl, 0, X.scan_in, s); }
 
-void launch_mixed_scan(const MixedCtx& X, cudaStream_t s) {
-    const MCtx& A = *(const MCtx*)X.impl;
-    const int nc = A.g.ncell;
-    km_sel_counts<<<(nc + 255) / 256, 256, 0, s>>>(A, X.scan_in);
-    launch_exclusive_scan(X.scan_in, X.scan_out, nc, A.S.scan_tmp, s);
-    km_put_starts<<<(nc + 256) / 256, 256, 0, s>>>(A, X.scan_out);
-}
+void mixed_initial_scan(const MixedCtx& X, cudaStream_t s) { mixed_scan(*(const MCtx*)X.impl, 1, X.scan_in, s); }
 
 void mixed_import(const MixedCtx& X, const P64& Q, cudaStream_t s) {
     const MCtx& A = *(const MCtx*)X.impl;
     const int np = A.P.np;
-    if (np > 0) km_import<<<(np + 255) / 256, 256, 0, s>>>(A, Q, 0);
+    if (np > 0) km_import<<<(np + 255) / 256, 256, 0, s>>>(A, Q);
     // initial cell lists for the current parity
     cudaMemsetAsync(X.sort_zero, 0, X.sort_zero_bytes, s);
-    if (np > 0) km_bin0<<<(np + 255) / 256, 256, 0, s>>>(A);
-    // scan counts[cur] -> start[cur]
+    if (np > 0) km_bin0<<<(np + 255) / 256, 256, 0, s>>>(A, Q);
     mixed_initial_scan(X, s);
     if (np > 0) km_place0<<<(np + 255) / 256, 256, 0, s>>>(A);
-}
-
-__global__ void km_sel_counts_cur(MCtx A, int* dst) {
-    const int cur = A.ctl->parity;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < A.g.ncell) dst[i] = A.S.count[cur][i];
-}
-__global__ void km_put_starts_cur(MCtx A, const int* src) {
-    const int cur = A.ctl->parity;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i <= A.g.ncell) A.S.start[cur][i] = src[i];
-}
-
-void mixed_initial_scan(const MixedCtx& X, cudaStream_t s) {
-    const MCtx& A = *(const MCtx*)X.impl;
-    const int nc = A.g.ncell;
-    km_sel_counts_cur<<<(nc + 255) / 256, 256, 0, s>>>(A, X.scan_in);
-    launch_exclusive_scan(X.scan_in, X.scan_out, nc, A.S.scan_tmp, s);
-    km_put_starts_cur<<<(nc + 256) / 256, 256, 0, s>>>(A, X.scan_out);
 }
 
 void mixed_export(const MixedCtx& X, const P64& Q, const N64& QN, cudaStream_t s) {
@@ -928,7 +1154,7 @@ void mixed_export(const MixedCtx& X, const P64& Q, const N64& QN, cudaStream_t s
 size_t mixed_ctx_size() { return sizeof(MCtx); }
 
 void mixed_ctx_init(void* mem, const Cfg& cf, const Geo& g, Ctl* ctl, const PM& P, const NM& N, const SM& S,
-                    const double* Del, const double* Cmp, double Kc, double Gc, double Hp, double c) {
+                    const double* Del, const double* Cmp, double Kc, double Gc, double Hp, double c, int acc) {
     MCtx* A = (MCtx*)mem;
     A->cf = cf;
     A->g = g;
@@ -944,6 +1170,7 @@ void mixed_ctx_init(void* mem, const Cfg& cf, const Geo& g, Ctl* ctl, const PM& 
     A->Gc = (float)Gc;
     A->Hp = (float)Hp;
     A->c = c;
+    A->acc = acc;
 }
 
 }  // namespace ep

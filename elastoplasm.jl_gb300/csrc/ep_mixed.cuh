@@ -1,13 +1,14 @@
-// ep_mixed.cuh -- device data of the mixed-precision step.
+// ep_mixed.cuh -- device data of the mixed-precision steps.
 //
-// Points: FP64 for the accumulated kinematic state (positions, F, b_e) and the
-// accumulated plastic strain; FP32 for velocities, stresses, material
-// constants and every transfer.  Positions are double-buffered (the step reads
-// the positions at its start while G2P writes the new ones); the buffer in use
-// is Ctl::parity, flipped at the end of each executed step.  Cell lists of the
-// points (counting sort, unordered inside a cell) are double-buffered the same
-// way: the step walks the lists of its start positions and builds the lists of
-// the next step.
+// Points: positions as FP32 offsets from the left node of the point's cell
+// (the cell itself is implicit in the per-step cell lists), velocities,
+// stresses and material constants in FP32.  The accumulated state -- the
+// deformation gradient F, the elastic left Cauchy-Green tensor b_e and the
+// accumulated plastic strain -- is either FP64 (precision "mixed") or a
+// double-float pair of FP32 values hi + lo (precision "mixed_df"); only one
+// of the two storages is allocated.  Offsets and cell lists are
+// double-buffered: a step reads the buffer Ctl::parity and writes the other
+// one, and the parity flips at the end of every executed step.
 #pragma once
 
 #include "ep_dev.cuh"
@@ -16,12 +17,18 @@ namespace ep {
 
 struct PM {
     int np;
-    double* x[2][3];   // [parity][direction]
+    float* dx[2][3];   // [parity][direction] x - x_node(e), e = the point's cell
     float* v[3];
-    double* F[9];      // deformation gradient, column-major D x D
-    double* b[6];      // elastic left Cauchy-Green, symmetric: 2d (11,22,12); 3d (11,22,33,23,13,12)
-    float* tau[6];     // Kirchhoff stress (finite) or Cauchy stress (infinitesimal), Voigt
-    double* ep1;       // accumulated plastic strain ϵpII[1]
+    double* Fd[9];     // F, column-major D x D (FP64 storage)
+    float* Fh[9];      // F as hi + lo FP32 pair (double-float storage)
+    float* Fl[9];
+    double* bd[6];     // b_e symmetric: 2d (11, 22, 12)
+    float* bh[6];
+    float* bl[6];
+    double* ep1d;      // accumulated plastic strain ϵpII[1]
+    float* ep1h;
+    float* ep1l;
+    float* tau[6];     // Kirchhoff (finite) or Cauchy (infinitesimal) stress, Voigt
     float* ep2;        // nonlocal ϵpII[2]
     float* dlam;
     float *c0, *cr, *tphi, *sphi, *cphi;
@@ -31,7 +38,7 @@ struct PM {
     float* rho;        // density (infinitesimal: stays at its uploaded value, deform.jl:25-44)
     float* l[3];       // GIMP half lengths
     float* dv[9];      // TPIC: velocity gradient of the previous step
-    int* p2e_next;     // cell of the new position
+    int* p2e_next;     // cell of the position written by the last G2P
 };
 
 struct NM {
@@ -44,7 +51,8 @@ struct NM {
 struct SM {
     int* count[2];
     int* start[2];     // ncell + 1 each
-    int* list[2];
+    int* list[2];      // point ids grouped by cell
+    int* cellof[2];    // cell of each list slot
     int* cursor;
     int* scan_tmp;
 };

@@ -67,7 +67,7 @@ HOW = {None: 0, "undeformed": 1, "detFij": 2, "Fii": 3, "Uii": 4,
 DEFORM = {"finite": 0, "infinitesimal": 1}
 TRSFR = {"std": 0, "tpic": 1}
 CONSTITUTIVE = {"DP": 0, "J2": 1}
-PRECISION = {"fp64": 0, "mixed": 1}
+PRECISION = {"fp64": 0, "mixed": 1, "mixed_df": 2}
 
 
 class UnsupportedError(ValueError):

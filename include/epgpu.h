@@ -54,8 +54,10 @@ enum { EP_DEFORM_FINITE = 0, EP_DEFORM_INFINITESIMAL = 1 };
 enum { EP_TRSFR_STD = 0, EP_TRSFR_TPIC = 1 };
 /* instr.plast.constitutive (require.jl:68) */
 enum { EP_CONS_DP = 0, EP_CONS_J2 = 1 };
-/* device arithmetic */
-enum { EP_PREC_FP64 = 0, EP_PREC_MIXED = 1 };
+/* device arithmetic: FP64 in the reference's order; FP32 transfers with FP64
+ * accumulated state and isotropic log/exp; FP32 transfers with double-float
+ * (FP32 pair) accumulated state */
+enum { EP_PREC_FP64 = 0, EP_PREC_MIXED = 1, EP_PREC_MIXED_DF = 2 };
 /* workflow phase (worflow.jl:23 elastodynamic!, :68 elastoplastic!) */
 enum { EP_PHASE_ELASTODYNAMIC = 0, EP_PHASE_ELASTOPLASTIC = 1 };
 
@@ -74,7 +76,7 @@ typedef struct ep_cfg {
     int32_t constitutive;  /* EP_CONS_*             plast.constitutive */
     int32_t nonloc;        /* nonloc.status */
     double  nonloc_ls;     /* nonloc.ls: nonlocal length scale [m] */
-    int32_t precision;     /* EP_PREC_FP64 (drop-in, oracle order) | EP_PREC_MIXED */
+    int32_t precision;     /* EP_PREC_FP64 (drop-in, oracle order) | EP_PREC_MIXED | EP_PREC_MIXED_DF */
     int32_t jaumann;       /* 0: reference rate (its spin term is identically zero,
                               elast.jl:77); 1: objective Jaumann rate (not the reference) */
 } ep_cfg;

@@ -18,9 +18,12 @@ STRESS_TOL = 1e-5
 DISP_TOL = 1e-4
 
 
-def _mixed(instr):
+PRECISIONS = ["mixed", "mixed_df"]
+
+
+def _mixed(instr, precision="mixed"):
     instr = copy.deepcopy(instr)
-    instr["gpu"] = {"precision": "mixed", "jaumann": False}
+    instr["gpu"] = {"precision": precision, "jaumann": False}
     return instr
 
 
@@ -45,73 +48,78 @@ def _run(o, e, windows):
     return t
 
 
+@pytest.mark.parametrize("precision", PRECISIONS)
 @pytest.mark.parametrize("windows", [((0, 1.0),), ((0, 1.0), (1, 1.5))])
-def test_mixed_config1_vs_oracle(oracle_mod, windows):
+def test_mixed_config1_vs_oracle(oracle_mod, windows, precision):
     from epgpu import Engine, ic_slump
     ic, cfg = ic_slump(*C1, nonloc={"status": False, "ls": 0.5})
     x0 = ic["mpts"].x.copy()
     o = oracle_mod.Oracle(copy.deepcopy(ic), cfg["instr"])
-    e = Engine(copy.deepcopy(ic), _mixed(cfg["instr"]))
+    e = Engine(copy.deepcopy(ic), _mixed(cfg["instr"], precision))
     _run(o, e, windows)
     a, b = e.download(), o.download()
     s, d, r = errors(a, b, x0)
-    print(f"mixed vs fp64 {windows}: stress {s:.3e} displacement {d:.3e} runout {r:.3e}")
+    print(f"{precision} vs fp64 {windows}: stress {s:.3e} displacement {d:.3e} runout {r:.3e}")
     assert s < STRESS_TOL and d < DISP_TOL
     assert np.isfinite(a.bij).all() and np.abs(a.J - b.J).max() < 1e-5
 
 
+@pytest.mark.parametrize("precision", PRECISIONS)
 @pytest.mark.parametrize("deform,trsfr,locking", [("finite", "tpic", True), ("infinitesimal", "std", True),
                                                   ("infinitesimal", "tpic", False), ("finite", "std", False)])
-def test_mixed_switches(oracle_mod, deform, trsfr, locking):
+def test_mixed_switches(oracle_mod, deform, trsfr, locking, precision):
     from epgpu import Engine, ic_slump
     fw = {"deform": deform, "trsfr": trsfr, "C_pf": 0.99, "musl": True, "locking": locking, "damping": 0.1}
     ic, cfg = ic_slump(*C1, fwrk=fw, nonloc={"status": False, "ls": 0.5})
     x0 = ic["mpts"].x.copy()
     o = oracle_mod.Oracle(copy.deepcopy(ic), cfg["instr"])
-    e = Engine(copy.deepcopy(ic), _mixed(cfg["instr"]))
+    e = Engine(copy.deepcopy(ic), _mixed(cfg["instr"], precision))
     _run(o, e, ((0, 1.0), (1, 1.3)))
     s, d, r = errors(e.download(), o.download(), x0)
-    print(f"mixed {deform}/{trsfr}/locking={locking}: stress {s:.3e} displacement {d:.3e} runout {r:.3e}")
+    print(f"{precision} {deform}/{trsfr}/locking={locking}: stress {s:.3e} displacement {d:.3e} runout {r:.3e}")
     assert s < STRESS_TOL and d < DISP_TOL
 
 
 @pytest.mark.parametrize("basis", [{"which": "gimpm", "how": "undeformed", "ghost": True},
                                    {"which": "smpm", "how": None, "ghost": False}])
-def test_mixed_other_bases(oracle_mod, basis):
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_mixed_other_bases(oracle_mod, basis, precision):
     from epgpu import Engine, ic_slump
     ic, cfg = ic_slump(*C1, basis=basis, nonloc={"status": False, "ls": 0.5})
     x0 = ic["mpts"].x.copy()
     o = oracle_mod.Oracle(copy.deepcopy(ic), cfg["instr"])
-    e = Engine(copy.deepcopy(ic), _mixed(cfg["instr"]))
+    e = Engine(copy.deepcopy(ic), _mixed(cfg["instr"], precision))
     _run(o, e, ((0, 1.0), (1, 1.3)))
     s, d, r = errors(e.download(), o.download(), x0)
-    print(f"mixed {basis['which']}: stress {s:.3e} displacement {d:.3e} runout {r:.3e}")
+    print(f"{precision} {basis['which']}: stress {s:.3e} displacement {d:.3e} runout {r:.3e}")
     assert s < STRESS_TOL and d < DISP_TOL
 
 
-def test_mixed_full_all_in_one_config1(oracle_mod):
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_mixed_full_all_in_one_config1(oracle_mod, precision):
     # the whole 15 s workflow; the error grows with plastic flow and softening, so it is reported
     # and held to looser bounds than the short windows
     from epgpu import ic_slump, slump
     ic, cfg = ic_slump(*C1, nonloc={"status": False, "ls": 0.5})
     x0 = ic["mpts"].x.copy()
     cm = copy.deepcopy(cfg)
-    cm["instr"] = _mixed(cfg["instr"])
+    cm["instr"] = _mixed(cfg["instr"], precision)
     out_m = slump(ic, cm, workflow="all-in-one")
     out_o = slump(ic, cfg, workflow="all-in-one", engine_factory=lambda a, b: oracle_mod.Oracle(a, b))
     s, d, r = errors(out_m["ic"]["mpts"], out_o["ic"]["mpts"], x0)
-    print(f"mixed all-in-one ({out_m['steps']} vs {out_o['steps']} steps): stress {s:.3e} displacement {d:.3e} "
+    print(f"{precision} all-in-one ({out_m['steps']} vs {out_o['steps']} steps): stress {s:.3e} displacement {d:.3e} "
           f"runout {r:.3e}")
     assert abs(out_m["steps"] - out_o["steps"]) <= 2
     assert s < 1e-2 and d < 1e-2
 
 
-def test_mixed_nonfinite_reported():
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_mixed_nonfinite_reported(precision):
     from epgpu import Engine, ic_slump
     from epgpu.abi import EPError
     ic, cfg = ic_slump(*C1, nonloc={"status": False, "ls": 0.5})
     ic["mpts"].x[0, 3] = np.inf
-    e = Engine(ic, _mixed(cfg["instr"]))
+    e = Engine(ic, _mixed(cfg["instr"], precision))
     with pytest.raises(EPError) as ex:
         e.step(0, 0.02, [0.0, -9.81])
     assert ex.value.status == 3
