@@ -10,7 +10,9 @@ the JSON line).  A step = one elastoplastic MPM cycle over all points
 (worflow.jl:80-82), dt from the reference's CFL rule.
 
 Arms:
-  default            the CUDA library through the C ABI (`--precision` fp64|mixed)
+  default            the CUDA library through the C ABI (`--precision` mixed_df (default),
+                     mixed or fp64); the plain FP64 step is timed beside it and the
+                     stress error of the timed run against it is stated
   --impl reference   the reference path on the host cores: the FP64 restatement
                      (oracle/) with all threads (Julia is not installed)
 """
@@ -56,8 +58,9 @@ def cfl_dt(mesh, cmpr, vmax):
     return 0.5 * max(mesh.h[i] / (vmax[i] + cmpr["c"]) for i in range(mesh.dim))
 
 
-# algorithmic bytes (unique reads + writes) per launch of each FP64 kernel, 2d:
-# per point and per node, from the arrays each kernel must touch once
+# algorithmic bytes (unique reads + writes) per launch of each kernel, 2d, as
+# (bytes per point, bytes per node), from the arrays each kernel must touch once.
+# FP64 oracle-order step:
 ALG_BYTES_FP64_2D = {
     "bin64": (8 * (2 + 3 + 1) + 8 * 2 + 4 + 8 * 3 + 8 * 16, 0),
     "p2g64": (8 * 16 + 8 * 7 + 4 + 4 * 16, 4 + 8 * 5),
@@ -70,6 +73,28 @@ ALG_BYTES_FP64_2D = {
     "segsort_nodes": (8 * 16, 4),
     "node_lists": (4 + 4 * 16, 8 * 2),
 }
+# mixed step (FP32 point streams; F, b_e, accumulated plastic strain as FP64 or as
+# FP32 pairs, the same bytes), finite strain, std transfer, mUSL, F-bar, DP:
+#   p2g   read list dx2 mp v2 Om0 tau3 (10 x 4 B)            nodes: m p2 f2 (atomics)
+#   solve nodes: read m f2 p2 + 2 mask bytes; write f2 a2 v2 pm2 dJacc
+#   g2p   read list dx2 v2 mp; write v2 dx2 cell + count     nodes: read v2 a2; pm2 (atomics)
+#   vmusl nodes: read m pm2 + masks; write vm2
+#   fbar  read list dx2 mp cell; write list cellof + cursor  nodes: read vm2; dJacc (atomic)
+#   dJn   nodes: read m dJacc; write dJn
+#   cons  read list cellof dx2 F4 b3 ep1 c0 cr tanphi (8-byte F, b, ep1); write F4 b3 ep1 tau3 dlam
+#         nodes: read vm2 dJn
+ALG_BYTES_MIXED_2D = {
+    "p2g": (40, 20),
+    "solve": (0, 22 + 36),
+    "g2p": (24 + 24, 16 + 8),
+    "vmusl": (0, 22),
+    "fbar": (20 + 12, 8 + 4),
+    "dJn": (0, 12),
+    "cons": (4 + 4 + 8 + 32 + 24 + 8 + 12 + 32 + 24 + 8 + 12 + 4, 12),
+}
+# the whole step by the per-point state S and per-node G rule: S = 35 values read or written once
+# (x2 v2 F4 b3 tau3 epII dlam c0 phi Om0 read; x2 v2 F4 b3 tau3 epII dlam written), G = 30 values
+STEP_BYTES = {"fp64": (35 * 8, 30 * 8), "mixed": (35 * 4, 30 * 4), "mixed_df": (35 * 4, 30 * 4)}
 
 
 def peaks():
@@ -214,7 +239,11 @@ def main():
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "mixed_df"])
+    ap.add_argument("--precision", default="mixed_df", choices=["fp64", "mixed", "mixed_df"])
+    ap.add_argument("--fp64-steps", type=int, default=10,
+                    help="steps of the plain FP64 step timed beside the headline (0: skip)")
+    ap.add_argument("--no-check", action="store_true",
+                    help="skip the stress error of the timed run against the FP64 step")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--settle", type=float, default=0.5,
@@ -240,8 +269,10 @@ def main():
         e.run(1, args.settle, 10.0, 0.0)          # the device time loop (epgpu_run) up to t = settle
         host0 = e.download()
     vmax = host0.vmax.copy()
+    dts = []
     for _ in range(args.warmup):
-        vmax = e.step(1, cfl_dt(mesh, cmpr, vmax), g)
+        dts.append(cfl_dt(mesh, cmpr, vmax))
+        vmax = e.step(1, dts[-1], g)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")   # 256 MB > 129 MB L2
     e.profile(True)
     l0 = e.stats()["launches"]
@@ -252,7 +283,8 @@ def main():
         for _ in range(args.steps):
             flush.fill_(1.0)                       # evict L2 between timed steps
             torch.cuda.synchronize()
-            vmax = e.step(1, cfl_dt(mesh, cmpr, vmax), g)
+            dts.append(cfl_dt(mesh, cmpr, vmax))
+            vmax = e.step(1, dts[-1], g)
             dev_ms += e.stats()["device_ms"]
     torch.cuda.synchronize()
     barrier(ws)
@@ -266,15 +298,57 @@ def main():
     dom = max(ktimes.items(), key=lambda kv: kv[1][1])
     name, (nl, tot) = dom
     avg_ms = tot / max(nl, 1)
-    ppt, pnode = ALG_BYTES_FP64_2D.get(name, (0, 0))
+    table = ALG_BYTES_FP64_2D if args.precision == "fp64" else ALG_BYTES_MIXED_2D
+    ppt, pnode = table.get(name, (0, 0))
     alg = ppt * np_ + pnode * mesh.nnodes
     peak, peak_kind = peaks()
     achieved = alg / (avg_ms * 1e-3) / 1e9 if alg else None
+    sp, sn = STEP_BYTES[args.precision]
+    step_bytes = sp * np_ + sn * mesh.nnodes
+    step_gbs = step_bytes / (tmax / args.steps * 1e-3) / 1e9
     roof = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": (achieved / peak) if achieved else None, "traffic": None,
             "peak_source": f"{peak_kind} hbm_gbs", "alg_bytes_per_launch": alg,
             "avg_launch_ms": avg_ms,
-            "kernel_share": {k: round(v[1] / sum(x[1] for x in ktimes.values()), 4) for k, v in ktimes.items()}}
+            "kernel_share": {k: round(v[1] / sum(x[1] for x in ktimes.values()), 4) for k, v in ktimes.items()},
+            "step": {"alg_bytes": step_bytes, "achieved_gbs": step_gbs, "frac": step_gbs / peak}}
+    # the plain FP64 step beside it, and the stress error of this run against the FP64 step replayed
+    # with the same dt sequence from the same state (the FP64 step matches the FP64 oracle bit for bit)
+    fp64 = None
+    check = None
+    if args.precision != "fp64" and (args.fp64_steps > 0 or not args.no_check):
+        ic64, cfg64, _ = make_workload()
+        ic64["mpts"] = host0.copy()
+        cfg64["instr"]["gpu"] = {"precision": "fp64", "jaumann": False}
+        e64 = Engine(ic64, cfg64["instr"])
+        if not args.no_check:
+            for dt in dts:
+                e64.step(1, dt, g)
+            a, b = e.download(), e64.download()
+            x0 = host0.x
+            check = {
+                "steps": len(dts),
+                "stress_rel_l2": float(np.linalg.norm(a.tau - b.tau) / np.linalg.norm(b.tau)),
+                "displacement_rel_l2": float(np.linalg.norm(a.x - b.x) / max(np.linalg.norm(b.x - x0), 1e-300)),
+                "runout_rel": float(abs((a.x[0].max() - x0[0].max()) - (b.x[0].max() - x0[0].max()))
+                                    / max(abs(b.x[0].max() - x0[0].max()), 1e-300)),
+            }
+        if args.fp64_steps > 0:
+            v64 = host0.vmax.copy()
+            e64.upload(host0)
+            for _ in range(3):
+                v64 = e64.step(1, cfl_dt(mesh, cmpr, v64), g)
+            e64.profile(True)
+            ms64 = 0.0
+            for _ in range(args.fp64_steps):
+                flush.fill_(1.0)
+                torch.cuda.synchronize()
+                v64 = e64.step(1, cfl_dt(mesh, cmpr, v64), g)
+                ms64 += e64.stats()["device_ms"]
+            e64.profile(False)
+            fp64 = {"value": np_ * args.fp64_steps / (ms64 * 1e-3), "unit": "particle-steps/s",
+                    "steps": args.fp64_steps, "ms_per_step": ms64 / args.fp64_steps}
+        e64.close()
     # end to end through the C ABI with host buffers: upload + step + download every step
     e2e = None
     if not args.no_e2e:
@@ -329,6 +403,8 @@ def main():
                        "parallelism": f"replicas x{ws}", "plastic_points_last_step": plastic,
                        "settle_s": args.settle},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+            "error_vs_fp64": check, "fp64_step": fp64,
+            "speedup_vs_fp64_step": (value / fp64["value"]) if fp64 else None,
             "clocks": clk.summary(),
         }
         print(json.dumps(line))
