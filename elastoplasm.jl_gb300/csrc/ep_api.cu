@@ -4,12 +4,14 @@
 #include <climits>
 #include <cmath>
 #include <cstdio>
+#include <algorithm>
 #include <cstring>
 #include <string>
 #include <vector>
 
 #include "../../include/epgpu.h"
 #include "ep_internal.h"
+#include "ep_rmap.h"
 
 using namespace ep;
 
@@ -55,6 +57,11 @@ struct ep_handle {
     bool mixed = false;
     MixedCtx mx{};
     std::vector<unsigned char> mx_impl;   // host image of the mixed kernels' argument block
+    // learned return map slots (allocated on first use)
+    float* rm_buf = nullptr;
+    int* rm_int = nullptr;
+    ep_mlp* rm_net = nullptr;
+    int rm_mode = 0;
 };
 
 void ep::set_global_error(const char* msg) { g_create_error = msg ? msg : ""; }
@@ -815,6 +822,76 @@ ep_status epgpu_stats(ep_handle* h, ep_stats* out) {
     out->device_ms = h->last_ms;
     out->t = h->t;
     out->plastic = h->hctl->plastic;
+    return EP_OK;
+}
+
+ep_status epgpu_set_return_map(ep_handle* h, ep_mlp* m, int32_t mode) {
+    if (!h) return EP_ERR_ARG;
+    if (mode != EP_RMAP_EXACT && mode != EP_RMAP_LEARNED && mode != EP_RMAP_RECORD)
+        return fail(h, EP_ERR_ARG, "return map mode must be EP_RMAP_EXACT, _LEARNED or _RECORD");
+    if (mode != EP_RMAP_EXACT) {
+        if (!m) return fail(h, EP_ERR_ARG, "a network is required for the learned and record modes");
+        if (!h->mixed || h->cfg.deform != EP_DEFORM_FINITE || h->cfg.constitutive != EP_CONS_DP || h->dim != 2)
+            return fail(h, EP_ERR_UNSUPPORTED,
+                        "the learned return map stands in for the 2d finite-strain DP return of the mixed step");
+        if (mode == EP_RMAP_RECORD && mlp_record_cap(m) <= 0)
+            return fail(h, EP_ERR_STATE, "the network has no record buffer (epgpu_mlp_record_buffer)");
+    }
+    RmapBufs b{};
+    b.mode = mode;
+    if (mode == EP_RMAP_LEARNED) {
+        const size_t np = (size_t)std::max(h->np, 1);
+        if (!h->rm_buf) {
+            if (dalloc(h, &h->rm_buf, np * (RM_NX + RM_NY + 4)) != cudaSuccess ||
+                dalloc(h, &h->rm_int, np + 1) != cudaSuccess)
+                return fail(h, EP_ERR_NOMEM, "device allocation (learned return map slots)");
+        }
+        b.rx = h->rm_buf;
+        b.ry = h->rm_buf + np * RM_NX;
+        b.raux = h->rm_buf + np * (RM_NX + RM_NY);
+        b.rcount = h->rm_int;
+        b.rpt = h->rm_int + 1;
+        CK(h, cudaMemsetAsync(b.rcount, 0, sizeof(int), h->s));
+    } else if (mode == EP_RMAP_RECORD) {
+        b.rx = mlp_record_x(m);
+        b.ry = mlp_record_t(m);
+        b.rec_count = mlp_record_count(m);
+        b.rec_cap = mlp_record_cap(m);
+    }
+    if (h->mixed) {
+        mixed_set_rmap(h->mx_impl.data(), b);
+        h->mx.net = mode == EP_RMAP_LEARNED ? m : nullptr;
+        for (int k = 0; k < 2; ++k)
+            if (h->graph[k]) {                        // the captured kernels hold the old argument block
+                cudaGraphExecDestroy(h->graph[k]);
+                h->graph[k] = nullptr;
+            }
+    }
+    h->rm_net = m;
+    h->rm_mode = mode;
+    ep_status st;
+    if ((st = read_ctl(h)) != EP_OK) return st;
+    h->hctl->rm_learned = 0;
+    h->hctl->rm_fallback = 0;
+    CK(h, cudaMemcpyAsync(h->ctl, h->hctl, sizeof(Ctl), cudaMemcpyHostToDevice, h->s));
+    CK(h, cudaStreamSynchronize(h->s));
+    return EP_OK;
+}
+
+ep_status epgpu_return_map_stats(ep_handle* h, int64_t* learned, int64_t* fallback, int64_t* recorded) {
+    if (!h) return EP_ERR_ARG;
+    ep_status st;
+    if ((st = read_ctl(h)) != EP_OK) return st;
+    if (learned) *learned = (int64_t)h->hctl->rm_learned;
+    if (fallback) *fallback = (int64_t)h->hctl->rm_fallback;
+    if (recorded) {
+        long long c = 0;
+        if (h->rm_mode == EP_RMAP_RECORD && h->rm_net) {
+            CK(h, cudaMemcpyAsync(&c, mlp_record_count(h->rm_net), sizeof(long long), cudaMemcpyDeviceToHost, h->s));
+            CK(h, cudaStreamSynchronize(h->s));
+        }
+        *recorded = c;
+    }
     return EP_OK;
 }
 

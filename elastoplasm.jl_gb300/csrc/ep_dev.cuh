@@ -57,6 +57,8 @@ struct Ctl {
     int err_info;
     int parity;                       // mixed step: which position / cell-list buffer is current
     int pad_;
+    unsigned long long rm_learned;    // learned return map: points the network returned
+    unsigned long long rm_fallback;   // points sent to the exact FP64 return instead
 };
 
 struct P64 {

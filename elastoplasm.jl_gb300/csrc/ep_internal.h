@@ -10,6 +10,8 @@
 #include "ep_dev.cuh"
 #include "ep_mixed.cuh"
 
+struct ep_mlp;   // learned return map object (include/epgpu.h)
+
 namespace ep {
 
 // CUDA-event timers between consecutive kernels of a step (profiling mode).
@@ -93,6 +95,7 @@ void fp64_check_finite(const Fp64Ctx& c, cudaStream_t s);
 // mixed-precision step (ep_mixed.cu)
 struct MixedCtx {
     void* impl;               // host image of the kernels' argument block (MCtx)
+    ep_mlp* net;              // learned return map (EP_RMAP_LEARNED) or nullptr
     void* grid_zero;          // node accumulators zeroed at each step start
     size_t grid_zero_bytes;
     void* sort_zero;          // both parities' cell counts and the cursor
@@ -106,6 +109,23 @@ size_t mixed_ctx_size();
 void mixed_ctx_init(void* mem, const Cfg& cf, const Geo& g, Ctl* ctl, const PM& P, const NM& N, const SM& S,
                     const double* Del, const double* Cmp, double Kc, double Gc, double Hp, double c, int acc);
 void mixed_step(const MixedCtx& X, int phase, cudaStream_t s);
+// return map of the mixed step: mode EP_RMAP_*, slot buffers of the learned mode
+// (features, outputs, aux, point ids, slot count) or the record buffer of the network
+struct RmapBufs {
+    int mode;
+    float *rx, *ry, *raux;
+    int* rpt;
+    int* rcount;
+    long long* rec_count;
+    long long rec_cap;
+};
+void mixed_set_rmap(void* impl, const RmapBufs& b);
+// network kernels used by the step (ep_mlp.cu)
+void mlp_infer(ep_mlp* m, const float* X, const int* ndev, int cap, float* Y, cudaStream_t s);
+float* mlp_record_x(ep_mlp* m);
+float* mlp_record_t(ep_mlp* m);
+long long* mlp_record_count(ep_mlp* m);
+long long mlp_record_cap(ep_mlp* m);
 void launch_mixed_scan(const MixedCtx& X, cudaStream_t s);
 void mixed_initial_scan(const MixedCtx& X, cudaStream_t s);
 void mixed_import(const MixedCtx& X, const P64& Q, cudaStream_t s);

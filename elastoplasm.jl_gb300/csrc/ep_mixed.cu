@@ -41,6 +41,7 @@
 #include "../../include/epgpu.h"
 #include "ep_internal.h"
 #include "ep_mixed.cuh"
+#include "ep_rmap.h"
 
 namespace ep {
 
@@ -170,6 +171,15 @@ struct MCtx {
     float Kc, Gc, Hp;
     double c;           // wave speed
     int acc;            // 0: FP64 accumulators, 1: double-float accumulators
+    // return map (EP_RMAP_*): learned-mode slots or the record buffer
+    int rmode;
+    float l2g;          // λ / (2G)
+    float *rx, *ry, *raux;
+    int* rpt;
+    int* rcount;
+    long long* rec_count;
+    long long rec_cap;
+    double Deld[9], Cmpd[9], Kd, Gd;   // FP64 copies for the exact fallback
 };
 
 __device__ __forceinline__ int node2(const Geo& g, const Axis4& ax, const Axis4& az, int i, int j) {
@@ -618,15 +628,86 @@ __device__ __forceinline__ void exp2eps_dev(float e11, float e22, float e12, flo
     dev[2] = E * (shs * e12);
 }
 
-// km_cons: F-bar scaling, F update, elastic predictor and return map, one lane per point
+// b_e = exp(2 eps) of a returned log strain (DP.jl:63-66), into the point's accumulated storage
+template <int ACC>
+__device__ __forceinline__ void rebuild_b(const MCtx& A, int p, float e11, float e22, float e12) {
+    const float em = 0.5f * (e11 + e22);
+    float E, Em1;
+    if (ACC == 0) {
+        const double Ed = ep_exp(2.0 * (double)em);   // e^{2 e_m} in FP64
+        E = (float)Ed;
+        Em1 = (float)(Ed - 1.0);
+    } else {
+        Em1 = expm1f(2.f * em);
+        E = 1.f + Em1;
+    }
+    float dev[3];
+    exp2eps_dev(e11, e22, e12, Em1, E, dev);
+    if (ACC == 0) {
+        A.P.bd[0][p] = 1.0 + (double)dev[0];
+        A.P.bd[1][p] = 1.0 + (double)dev[1];
+        A.P.bd[2][p] = (double)dev[2];
+    } else {
+        float h, l;
+        df_one_plus(dev[0], h, l);
+        A.P.bh[0][p] = h; A.P.bl[0][p] = l;
+        df_one_plus(dev[1], h, l);
+        A.P.bh[1][p] = h; A.P.bl[1][p] = l;
+        A.P.bh[2][p] = dev[2]; A.P.bl[2][p] = 0.f;
+    }
+}
+
+template <int ACC>
+__device__ __forceinline__ void add_ep1(const MCtx& A, int p, float inc) {
+    if (ACC == 0) {
+        A.P.ep1d[p] += (double)inc;
+    } else {
+        float h = A.P.ep1h[p], l = A.P.ep1l[p];
+        df_add(h, l, inc);
+        A.P.ep1h[p] = h;
+        A.P.ep1l[p] = l;
+    }
+}
+
+// features of a finite-strain DP trial in the principal frame (ep_rmap.h layout, FP32):
+// x[8], aux = (cos 2θ, sin 2θ, s, c); returns whether the trial leaves the DP surface
+__device__ __forceinline__ bool rm_features32(float e11, float e22, float e12, float coh, float tphi, float Gc,
+                                              float l2g, float* x, float* aux) {
+    const float em = 0.5f * (e11 + e22), ed = 0.5f * (e11 - e22);
+    const float r = sqrtf(ed * ed + e12 * e12);
+    const float s = coh / (2.f * Gc);
+    const float e1 = (em + r) / s, e2 = (em - r) / s;
+    const float tr = e1 + e2;
+    const float t1 = l2g * tr + e1, t2 = l2g * tr + e2;
+    const float P = 0.5f * (t1 + t2), tII = 0.5f * (t1 - t2);
+    const float den = sqrtf(9.f + 12.f * tphi * tphi);
+    const float eta = 3.f * tphi / den, xi = 3.f / den;
+    const float fs = tII + eta * P - xi;
+    x[0] = e1; x[1] = e2; x[2] = 0.f; x[3] = coh * (float)(1.0 / RM_CREF);
+    x[4] = tphi; x[5] = 0.f; x[6] = fmaxf(fs, 0.f); x[7] = 0.f;
+    aux[0] = r > 0.f ? ed / r : 1.f;
+    aux[1] = r > 0.f ? e12 / r : 0.f;
+    aux[2] = s;
+    aux[3] = coh;
+    return (fs > 0.f && P < xi / eta) || P >= xi / eta;
+}
+
+// km_cons: F-bar scaling, F update, elastic predictor and return map, one lane per point.
+// With the learned return map, a trial-yielding point is handed to the network (its
+// features go to a slot; km_rmap_finish completes it); in record mode the exact map runs
+// and the (features, exact label) pair of the point is appended to the record buffer.
 template <int BASIS, int ACC>
 __global__ void __launch_bounds__(256) km_cons(MCtx A, int plastic_phase) {
     EP_ACTIVE(A.ctl);
     const int cur = A.ctl->parity, nxt = cur ^ 1;
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     int nplastic = 0;
+    bool emit = false;
+    float fx[RM_NX], fy[RM_NY], fa[4];
+    int fp = 0;
     if (k < A.S.start[cur][A.g.ncell]) {
         const int p = A.S.list[cur][k], c = A.S.cellof[cur][k];
+        fp = p;
         const int ex = c / A.g.nel[1], ez = c - ex * A.g.nel[1];
         const Axis4 ax = axis4(A.g, 0, ex), az = axis4(A.g, 1, ez);
         const float hx = (float)A.g.h[0], hz = (float)A.g.h[1];
@@ -705,6 +786,7 @@ __global__ void __launch_bounds__(256) km_cons(MCtx A, int plastic_phase) {
             D[3] = D[3] * (1.f + s1) + s1;
         }
         float tt[3];
+        float te11 = 0.f, te22 = 0.f, te12 = 0.f;   // trial log strain (finite)
         if (fin) {
             // b <- ΔF b ΔF' = b + (D b + b D' + D b D') (elast.jl:49), then ε = ½ log b (elast.jl:51-52)
             float b11, b22, b12, mu, dd, qq;
@@ -744,11 +826,13 @@ __global__ void __launch_bounds__(256) km_cons(MCtx A, int plastic_phase) {
             const float x2 = (dd * dd + qq * qq) / (mf * mf);
             const float L0 = tt[0] + 0.5f * log1pf(-x2);
             const float kd = atanh_over_x(x2) / mf;
-            const float e11 = 0.5f * (L0 + kd * dd), e22 = 0.5f * (L0 - kd * dd), e12 = 0.5f * kd * qq;
-            const float v2 = 2.f * e12;
-            tt[0] = A.Del[0] * e11 + A.Del[3] * e22 + A.Del[6] * v2;
-            tt[1] = A.Del[1] * e11 + A.Del[4] * e22 + A.Del[7] * v2;
-            tt[2] = A.Del[2] * e11 + A.Del[5] * e22 + A.Del[8] * v2;
+            te11 = 0.5f * (L0 + kd * dd);
+            te22 = 0.5f * (L0 - kd * dd);
+            te12 = 0.5f * kd * qq;
+            const float v2 = 2.f * te12;
+            tt[0] = A.Del[0] * te11 + A.Del[3] * te22 + A.Del[6] * v2;
+            tt[1] = A.Del[1] * te11 + A.Del[4] * te22 + A.Del[7] * v2;
+            tt[2] = A.Del[2] * te11 + A.Del[5] * te22 + A.Del[8] * v2;
         } else {
             // σ += Del voigt(sym(ΔF) - I, 2) (+ ωσ - σω for the objective rate) (elast.jl:73-78)
             tt[0] = A.P.tau[0][p]; tt[1] = A.P.tau[1][p]; tt[2] = A.P.tau[2][p];
@@ -767,13 +851,24 @@ __global__ void __launch_bounds__(256) km_cons(MCtx A, int plastic_phase) {
         if (plastic_phase) {
             float ep1f = ACC == 0 ? (float)A.P.ep1d[p] : A.P.ep1h[p] + A.P.ep1l[p];
             const float ep2 = A.cf.nonloc ? A.P.ep2[p] : ep1f;
-            bool yielded = false;
+            bool yielded = false, deferred = false;
             float inc = 0.f, newg = 0.f;
             bool absolute = false;
             if (A.cf.cons == EP_CONS_DP) {
-                const float dl = dp32(tt, ep2, A.P.c0[p], A.P.cr[p], A.P.tphi[p], A.Hp, A.Kc, A.Gc, &inc);
-                A.P.dlam[p] = dl;
-                yielded = dl != 0.f;
+                if (A.rmode != EP_RMAP_EXACT && fin) {
+                    const float coh = fmaxf(A.P.c0[p] + A.Hp * ep2, A.P.cr[p]);
+                    const bool ytr = rm_features32(te11, te22, te12, coh, A.P.tphi[p], A.Gc, A.l2g, fx, fa);
+                    deferred = ytr && A.rmode == EP_RMAP_LEARNED;
+                }
+                if (deferred) {
+                    emit = true;              // km_rmap_finish writes τ, Δλ, ϵpII and b_e
+                    ++nplastic;
+                } else {
+                    const float dl = dp32(tt, ep2, A.P.c0[p], A.P.cr[p], A.P.tphi[p], A.Hp, A.Kc, A.Gc, &inc);
+                    A.P.dlam[p] = dl;
+                    yielded = dl != 0.f;
+                    if (yielded && A.rmode == EP_RMAP_RECORD && fin) emit = rm_label(fx, (double)A.l2g, fy) != 0;
+                }
             } else {
                 const float Dl[9] = {A.Del[0], A.Del[1], A.Del[2], A.Del[3], A.Del[4],
                                      A.Del[5], A.Del[6], A.Del[7], A.Del[8]};
@@ -782,44 +877,22 @@ __global__ void __launch_bounds__(256) km_cons(MCtx A, int plastic_phase) {
             }
             if (yielded) {
                 ++nplastic;
-                if (ACC == 0) {
-                    A.P.ep1d[p] = absolute ? (double)newg : A.P.ep1d[p] + (double)inc;
+                if (absolute) {
+                    if (ACC == 0) {
+                        A.P.ep1d[p] = (double)newg;
+                    } else {
+                        A.P.ep1h[p] = newg;
+                        A.P.ep1l[p] = 0.f;
+                    }
                 } else {
-                    float h = A.P.ep1h[p], l = A.P.ep1l[p];
-                    if (absolute) { h = newg; l = 0.f; }
-                    else df_add(h, l, inc);
-                    A.P.ep1h[p] = h;
-                    A.P.ep1l[p] = l;
+                    add_ep1<ACC>(A, p, inc);
                 }
                 if (fin) {
                     // ε = tensor(Del \ τ, ½); b = exp(2ε) (DP.jl:63-66)
                     const float e11 = A.Cmp[0] * tt[0] + A.Cmp[3] * tt[1] + A.Cmp[6] * tt[2];
                     const float e22 = A.Cmp[1] * tt[0] + A.Cmp[4] * tt[1] + A.Cmp[7] * tt[2];
                     const float e12 = 0.5f * (A.Cmp[2] * tt[0] + A.Cmp[5] * tt[1] + A.Cmp[8] * tt[2]);
-                    const float em = 0.5f * (e11 + e22);
-                    float E, Em1;
-                    if (ACC == 0) {
-                        const double Ed = ep_exp(2.0 * (double)em);   // e^{2 e_m} in FP64
-                        E = (float)Ed;
-                        Em1 = (float)(Ed - 1.0);
-                    } else {
-                        Em1 = expm1f(2.f * em);
-                        E = 1.f + Em1;
-                    }
-                    float dev[3];
-                    exp2eps_dev(e11, e22, e12, Em1, E, dev);
-                    if (ACC == 0) {
-                        A.P.bd[0][p] = 1.0 + (double)dev[0];
-                        A.P.bd[1][p] = 1.0 + (double)dev[1];
-                        A.P.bd[2][p] = (double)dev[2];
-                    } else {
-                        float h, l;
-                        df_one_plus(dev[0], h, l);
-                        A.P.bh[0][p] = h; A.P.bl[0][p] = l;
-                        df_one_plus(dev[1], h, l);
-                        A.P.bh[1][p] = h; A.P.bl[1][p] = l;
-                        A.P.bh[2][p] = dev[2]; A.P.bl[2][p] = 0.f;
-                    }
+                    rebuild_b<ACC>(A, p, e11, e22, e12);
                 }
             }
         }
@@ -830,14 +903,161 @@ __global__ void __launch_bounds__(256) km_cons(MCtx A, int plastic_phase) {
         if (!lock) place_next(A, p, nxt);
         if (bad) set_err(A.ctl, EP_ERR_INVALID_POSITION, c);
     }
+    // learned map slots / recorded pairs: one atomic per warp for the warp's points
+    if (A.rmode != EP_RMAP_EXACT) {
+        const unsigned bal = __ballot_sync(0xffffffffu, emit);
+        if (bal) {
+            const int lane = threadIdx.x & 31;
+            const unsigned below = bal & ((1u << lane) - 1u);
+            if (A.rmode == EP_RMAP_LEARNED) {
+                int base = 0;
+                if (lane == 0) base = atomicAdd(A.rcount, __popc(bal));
+                base = __shfl_sync(0xffffffffu, base, 0);
+                if (emit) {
+                    const int slot = base + __popc(below);
+                    float4* dx = reinterpret_cast<float4*>(A.rx + (size_t)slot * RM_NX);
+                    dx[0] = make_float4(fx[0], fx[1], fx[2], fx[3]);
+                    dx[1] = make_float4(fx[4], fx[5], fx[6], fx[7]);
+                    *reinterpret_cast<float4*>(A.raux + (size_t)slot * 4) = make_float4(fa[0], fa[1], fa[2], fa[3]);
+                    A.rpt[slot] = fp;
+                }
+            } else {
+                unsigned long long base = 0;
+                if (lane == 0) base = atomicAdd((unsigned long long*)A.rec_count, (unsigned long long)__popc(bal));
+                base = __shfl_sync(0xffffffffu, base, 0);
+                const long long slot = (long long)base + __popc(below);
+                if (emit && slot < A.rec_cap) {
+                    float4* dx = reinterpret_cast<float4*>(A.rx + (size_t)slot * RM_NX);
+                    dx[0] = make_float4(fx[0], fx[1], fx[2], fx[3]);
+                    dx[1] = make_float4(fx[4], fx[5], fx[6], fx[7]);
+                    *reinterpret_cast<float4*>(A.ry + (size_t)slot * RM_NY) = make_float4(fy[0], fy[1], fy[2], fy[3]);
+                }
+            }
+        }
+    }
     // plastic point count: one atomic per warp
     const int tot = __reduce_add_sync(0xffffffffu, nplastic);
     if ((threadIdx.x & 31) == 0 && tot) atomicAdd((unsigned long long*)&A.ctl->plastic, (unsigned long long)tot);
 }
 
-__global__ void km_flip(Ctl* ctl) {
-    if (ctl->active) ctl->parity ^= 1;
+// km_rmap_finish: the network's returned strains for the slots of km_cons, accepted when
+// the trial lies on the compressive side of the apex, the returned stress is on the yield
+// surface and keeps the trial mean stress (both within 1e-3 c), the principal order is
+// kept and Δλ >= 0; the other slots go to the exact FP64 return (DP.jl:33-66)
+template <int ACC>
+__global__ void __launch_bounds__(256) km_rmap_finish(MCtx A) {
+    EP_ACTIVE(A.ctl);
+    const int n = *A.rcount;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int nl = 0, nf = 0;
+    if (i < n) {
+        const float4 x0 = *reinterpret_cast<const float4*>(A.rx + (size_t)i * RM_NX);
+        const float4 x1 = *reinterpret_cast<const float4*>(A.rx + (size_t)i * RM_NX + 4);
+        const float4 y = *reinterpret_cast<const float4*>(A.ry + (size_t)i * RM_NY);
+        const float4 ax = *reinterpret_cast<const float4*>(A.raux + (size_t)i * 4);
+        const int p = A.rpt[i];
+        const float c2 = ax.x, s2 = ax.y, s = ax.z, coh = ax.w;
+        const float tphi = x1.x, phin = x1.z;
+        const float den = sqrtf(9.f + 12.f * tphi * tphi), eta = 3.f * tphi / den, xi = 3.f * coh / den;
+        bool ok = phin >= (float)RM_PHI_MIN && isfinite(y.x) && isfinite(y.y);
+        float tt[3] = {0.f, 0.f, 0.f}, e11 = 0.f, e22 = 0.f, e12 = 0.f, dl = 0.f;
+        if (ok) {
+            float y0 = y.x, y1 = y.y;
+            if (x1.y == 0.f) {
+                // tan ψ = 0: the exact return's plastic strain increment is deviatoric, so the
+                // volumetric part of the predicted correction is removed (it would accumulate in
+                // the mean stress, which no later return corrects)
+                const float yd = 0.5f * (y0 - y1);
+                y0 = yd;
+                y1 = -yd;
+            }
+            const float e1 = s * (x0.x + phin * y0), e2 = s * (x0.y + phin * y1);
+            const float em = 0.5f * (e1 + e2), r = 0.5f * (e1 - e2);
+            e11 = em + r * c2;
+            e22 = em - r * c2;
+            e12 = r * s2;
+            const float v2 = 2.f * e12;
+            tt[0] = A.Del[0] * e11 + A.Del[3] * e22 + A.Del[6] * v2;
+            tt[1] = A.Del[1] * e11 + A.Del[4] * e22 + A.Del[7] * v2;
+            tt[2] = A.Del[2] * e11 + A.Del[5] * e22 + A.Del[8] * v2;
+            const float P = 0.5f * (tt[0] + tt[1]), d0 = tt[0] - P, d1 = tt[1] - P;
+            const float tII = sqrtf(0.5f * (d0 * d0 + d1 * d1) + tt[2] * tt[2]);
+            const float fs = tII + eta * P - xi;
+            dl = (0.5f * coh * (x0.x - x0.y) - tII) / A.Gc;    // Δλ = (τII,trial - τII) / G (ψ = 0)
+            // ψ = 0 makes the plastic strain increment deviatoric (DP.jl:37, 47-52): the returned
+            // mean stress is the trial one, P_trial = c (λ/2G + 1/2)(x0 + x1)
+            const float Ptr = coh * (A.l2g + 0.5f) * (x0.x + x0.y);
+            // beyond the apex (P >= σm = c / tan ϕ) the exact map may take its tension-apex branch,
+            // which moves the mean stress (DP.jl:53-58): those trials always go to the exact map
+            const bool below_apex = tphi > 0.f ? Ptr < coh / tphi : true;
+            ok = fabsf(fs) <= 1.0e-3f * coh && fabsf(P - Ptr) <= 1.0e-3f * coh && dl >= 0.f && r >= 0.f &&
+                 below_apex && isfinite(fs);
+        }
+        if (ok) {
+            ++nl;
+            add_ep1<ACC>(A, p, dl * 0.57735026918962576f);
+            A.P.dlam[p] = dl;
+            rebuild_b<ACC>(A, p, e11, e22, e12);
+        } else {
+            ++nf;
+            // exact FP64 return of the trial stress rebuilt from the slot
+            const double sd = (double)s;
+            const double q1 = sd * (double)x0.x, q2 = sd * (double)x0.y;
+            const double em = 0.5 * (q1 + q2), r = 0.5 * (q1 - q2);
+            const double te[3] = {em + r * (double)c2, em - r * (double)c2, 2.0 * r * (double)s2};
+            double sv[3];
+            for (int a = 0; a < 3; ++a) sv[a] = A.Deld[a] * te[0] + A.Deld[a + 3] * te[1] + A.Deld[a + 6] * te[2];
+            double inc = 0.0;
+            const double dld = dp_return<3>(sv, 0.0, (double)coh, 0.0, (double)tphi, 0.0, 1.0, 0.0, A.Kd, A.Gd, &inc);
+            A.P.dlam[p] = (float)dld;
+            add_ep1<ACC>(A, p, (float)inc);
+            for (int a = 0; a < 3; ++a) tt[a] = (float)sv[a];
+            if (dld != 0.0) {
+                // b = exp(2 Del \ τ) in FP64
+                double ee[3];
+                for (int a = 0; a < 3; ++a) ee[a] = A.Cmpd[a] * sv[0] + A.Cmpd[a + 3] * sv[1] + A.Cmpd[a + 6] * sv[2];
+                const double m = 0.5 * (ee[0] + ee[1]), ed = 0.5 * (ee[0] - ee[1]), g = 0.5 * ee[2];
+                const double q = sqrt(ed * ed + g * g);
+                const double E = ep_exp(2.0 * m);
+                double ch, shs;
+                if (q < 1.0e-4) {
+                    const double q2s = q * q;
+                    ch = 1.0 + 2.0 * q2s * (1.0 + q2s / 3.0);
+                    shs = 2.0 * (1.0 + q2s * (2.0 / 3.0 + q2s * (2.0 / 15.0)));
+                } else {
+                    const double ep = ep_exp(2.0 * q), em2 = 1.0 / ep;
+                    ch = 0.5 * (ep + em2);
+                    shs = 0.5 * (ep - em2) / q;
+                }
+                const double b0 = E * (ch + shs * ed), b1 = E * (ch - shs * ed), b2 = E * shs * g;
+                if (ACC == 0) {
+                    A.P.bd[0][p] = b0; A.P.bd[1][p] = b1; A.P.bd[2][p] = b2;
+                } else {
+                    const float h0 = (float)b0, h1 = (float)b1, h2 = (float)b2;
+                    A.P.bh[0][p] = h0; A.P.bl[0][p] = (float)(b0 - (double)h0);
+                    A.P.bh[1][p] = h1; A.P.bl[1][p] = (float)(b1 - (double)h1);
+                    A.P.bh[2][p] = h2; A.P.bl[2][p] = (float)(b2 - (double)h2);
+                }
+            }
+        }
+        A.P.tau[0][p] = tt[0];
+        A.P.tau[1][p] = tt[1];
+        A.P.tau[2][p] = tt[2];
+        if (!(isfinite(tt[0]) && isfinite(tt[1]) && isfinite(tt[2]))) set_err(A.ctl, EP_ERR_NONFINITE, p);
+    }
+    const int tl = __reduce_add_sync(0xffffffffu, nl), tf = __reduce_add_sync(0xffffffffu, nf);
+    if ((threadIdx.x & 31) == 0) {
+        if (tl) atomicAdd(&A.ctl->rm_learned, (unsigned long long)tl);
+        if (tf) atomicAdd(&A.ctl->rm_fallback, (unsigned long long)tf);
+    }
 }
+
+__global__ void km_flip(Ctl* ctl, int* rcount) {
+    if (!ctl->active) return;
+    ctl->parity ^= 1;
+    if (rcount) *rcount = 0;   // learned map slots of the next step
+}
+
 
 // ---------------------------------------------------------------------------
 // exclusive scan of count[nxt] into start[nxt] (parity read on the device)
@@ -1108,8 +1328,15 @@ static void mixed_step_impl(const MixedCtx& X, int phase, cudaStream_t s) {
         km_cons<BASIS, ACC><<<gp, 256, 0, s>>>(A, phase == EP_PHASE_ELASTOPLASTIC);
         mark("cons");
         ++L;
+        if (A.rmode == EP_RMAP_LEARNED && X.net && phase == EP_PHASE_ELASTOPLASTIC) {
+            mlp_infer(X.net, A.rx, A.rcount, np, A.ry, s);
+            mark("mlp");
+            km_rmap_finish<ACC><<<gp, 256, 0, s>>>(A);
+            mark("rmap_finish");
+            L += 2;
+        }
     }
-    km_flip<<<1, 1, 0, s>>>(A.ctl);
+    km_flip<<<1, 1, 0, s>>>(A.ctl, A.rmode == EP_RMAP_LEARNED ? A.rcount : nullptr);
     ++L;
     if (X.launches) *X.launches += L;
 }
@@ -1171,6 +1398,30 @@ void mixed_ctx_init(void* mem, const Cfg& cf, const Geo& g, Ctl* ctl, const PM& 
     A->Hp = (float)Hp;
     A->c = c;
     A->acc = acc;
+    for (int i = 0; i < 9; ++i) {
+        A->Deld[i] = Del[i];
+        A->Cmpd[i] = Cmp[i];
+    }
+    A->Kd = Kc;
+    A->Gd = Gc;
+    A->l2g = (float)(Del[3] / (Del[0] - Del[3]));   // λ / (2G) of the plane-strain stiffness
+    A->rmode = EP_RMAP_EXACT;
+    A->rx = A->ry = A->raux = nullptr;
+    A->rpt = A->rcount = nullptr;
+    A->rec_count = nullptr;
+    A->rec_cap = 0;
+}
+
+void mixed_set_rmap(void* mem, const RmapBufs& b) {
+    MCtx* A = (MCtx*)mem;
+    A->rmode = b.mode;
+    A->rx = b.rx;
+    A->ry = b.ry;
+    A->raux = b.raux;
+    A->rpt = b.rpt;
+    A->rcount = b.rcount;
+    A->rec_count = b.rec_count;
+    A->rec_cap = b.rec_cap;
 }
 
 }  // namespace ep

@@ -15,6 +15,7 @@ import numpy as np
 from .config import to_abi
 
 _D = C.POINTER(C.c_double)
+_F = C.POINTER(C.c_float)
 _I64 = C.POINTER(C.c_int64)
 
 EP_OK = 0
@@ -162,7 +163,26 @@ SIGNATURES = {
                                   C.c_void_p, C.c_void_p]),
     "epgpu_bin_cells_noalloc": (C.c_int, [C.c_int32, _I64, _D, _D, C.c_void_p, C.c_int64, C.c_void_p,
                                           C.c_void_p, C.c_void_p, C.c_void_p]),
+    # learned return map
+    "epgpu_mlp_create": (C.c_int, [C.c_uint64, C.c_double, C.POINTER(C.c_void_p)]),
+    "epgpu_mlp_destroy": (C.c_int, [C.c_void_p]),
+    "epgpu_mlp_last_error": (C.c_char_p, [C.c_void_p]),
+    "epgpu_mlp_set_params": (C.c_int, [C.c_void_p, _F, C.c_int64]),
+    "epgpu_mlp_get_params": (C.c_int, [C.c_void_p, _F, C.c_int64]),
+    "epgpu_mlp_forward": (C.c_int, [C.c_void_p, _F, C.c_int64, _F]),
+    "epgpu_mlp_grad": (C.c_int, [C.c_void_p, _F, _F, C.c_int64, _F, _D]),
+    "epgpu_mlp_train": (C.c_int, [C.c_void_p, _F, _F, C.c_int64, C.c_int32, C.c_int32, C.c_float, C.c_uint64,
+                                  _D]),
+    "epgpu_mlp_label": (C.c_int, [_F, C.c_int64, C.c_double, _F]),
+    "epgpu_mlp_record_buffer": (C.c_int, [C.c_void_p, C.c_int64]),
+    "epgpu_mlp_recorded": (C.c_int, [C.c_void_p, _I64, _F, _F, C.c_int64]),
+    "epgpu_set_return_map": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32]),
+    "epgpu_return_map_stats": (C.c_int, [C.c_void_p, _I64, _I64, _I64]),
 }
+
+# learned return map constants (include/epgpu.h)
+MLP_NX, MLP_NY, MLP_NPARAM = 8, 4, 50819
+RMAP = {"exact": 0, "learned": 1, "record": 2}
 
 _lib = None
 

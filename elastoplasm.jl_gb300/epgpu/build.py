@@ -24,6 +24,7 @@ UNITS = {
     "ep_sort.cu": [],
     "ep_fp64.cu": ["-fmad=false"],
     "ep_mixed.cu": [],
+    "ep_mlp.cu": [],
 }
 
 

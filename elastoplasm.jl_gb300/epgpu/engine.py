@@ -82,6 +82,16 @@ class Engine:
         self._check(self.lib.epgpu_profile_read(self.h, arr, n.value, C.byref(n)))
         return {arr[i].name.decode(): (arr[i].launches, arr[i].total_ms) for i in range(n.value)}
 
+    def set_return_map(self, net=None, mode: str = "exact"):
+        """Select the exact, learned (``net``) or recording return map (mixed 2d finite DP only)."""
+        self._net = net                                   # the network must outlive its use
+        self._check(self.lib.epgpu_set_return_map(self.h, net.h if net is not None else None, abi.RMAP[mode]))
+
+    def return_map_stats(self) -> dict:
+        a, b, c = C.c_int64(0), C.c_int64(0), C.c_int64(0)
+        self._check(self.lib.epgpu_return_map_stats(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        return {"learned": a.value, "fallback": b.value, "recorded": c.value}
+
     def close(self):
         if getattr(self, "h", None):
             self.lib.epgpu_destroy(self.h)

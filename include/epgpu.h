@@ -234,6 +234,78 @@ ep_status epgpu_bin_cells_noalloc(int32_t dim, const int64_t* nel, const double*
                                   const double* x_dev, int64_t nmp, int32_t* p2e_dev,
                                   int32_t* cell_start_dev, int32_t* cell_list_dev, void* stream);
 
+/* ---- Learned return map --------------------------------------------------
+ * No counterpart in the reference.  A 6 -> 128 x 4 (SiLU) -> 3 MLP, BF16
+ * operands with FP32 accumulation on the tensor cores, that stands in for the
+ * 2d finite-strain Drucker-Prager return of the mixed-precision step
+ * (elast.jl:51-54 and DP.jl:33-66, which the reference evaluates with an eigen
+ * decomposition, log and exp per point).  It works in the principal frame of
+ * the trial log strain, scaled by the current cohesion c (strains by
+ * s = c / (2G), stresses by c).  A row of features holds EP_MLP_NX floats:
+ *   x0 >= x1 the principal trial strains / s, x2 = 0 (plane strain),
+ *   x3 = c / 2e4 Pa, x4 = tan(phi), x5 = tan(psi) (0), x6 = phi_n = f_s / c >= 0
+ * (the scaled overstress of the trial stress), x7 unused; the network reads
+ * x0..x5.  A row of outputs holds EP_MLP_NY floats (3 used): the plastic
+ * correction per unit overstress, returned strains / s = x[0..2] + phi_n * y.
+ * In the step, with tan(psi) = 0 the volumetric part of y is removed before use
+ * (the exact return's plastic flow is then deviatoric and keeps the mean stress).
+ * Parameters (FP32 master copy, EP_MLP_NPARAM floats): W1 (128 x 6), b1,
+ * W2, b2, W3, b3, W4, b4 (128 x 128 each), W5 (3 x 128), b5, W row-major
+ * (output x input). */
+#define EP_MLP_NX 8
+#define EP_MLP_NY 4
+#define EP_MLP_NPARAM 50819
+
+typedef struct ep_mlp ep_mlp;
+
+enum {
+    EP_RMAP_EXACT = 0,    /* the step's own return map (default) */
+    EP_RMAP_LEARNED = 1,  /* trial-yielding points go through the network; a point whose
+                             returned stress misses the yield surface by more than 1e-3 c,
+                             changes the trial mean stress by more than 1e-3 c (psi = 0
+                             makes the exact return keep it), swaps the principal order,
+                             implies a negative plastic multiplier, or whose trial lies
+                             beyond the apex (P >= c / tan(phi), where the exact map may
+                             move the mean stress), is returned by the exact FP64 map */
+    EP_RMAP_RECORD = 2    /* the exact map runs; (features, exact label) pairs of every
+                             trial-yielding point are appended to the network's record
+                             buffer until it is full */
+};
+
+/* Network with He-initialised weights from `seed`; lambda_over_2G = lambda / (2G)
+ * of the material whose labels it learns (Del[0,1] / (Del[0,0] - Del[0,1])). */
+ep_status epgpu_mlp_create(uint64_t seed, double lambda_over_2G, ep_mlp** out);
+ep_status epgpu_mlp_destroy(ep_mlp* m);
+const char* epgpu_mlp_last_error(ep_mlp* m);
+ep_status epgpu_mlp_set_params(ep_mlp* m, const float* params, int64_t n);
+ep_status epgpu_mlp_get_params(ep_mlp* m, float* params, int64_t n);
+/* y (n x EP_MLP_NY) = network(x (n x EP_MLP_NX)), host buffers. */
+ep_status epgpu_mlp_forward(ep_mlp* m, const float* x, int64_t n, float* y);
+/* Gradient of the loss sum((y - t)^2) / (3 n) over the 3 outputs, from one
+ * forward and backward pass on the tensor cores; t is n x EP_MLP_NY. */
+ep_status epgpu_mlp_grad(ep_mlp* m, const float* x, const float* t, int64_t n, float* grad, double* loss);
+/* `iters` Adam steps (lr, beta 0.9 / 0.999) on mini-batches of `batch` rows drawn
+ * with `seed` from the n rows (x, t) in host memory, or from the record buffer
+ * when x is NULL.  *loss_out receives the loss of the last mini-batch. */
+ep_status epgpu_mlp_train(ep_mlp* m, const float* x, const float* t, int64_t n, int32_t iters, int32_t batch,
+                          float lr, uint64_t seed, double* loss_out);
+/* Exact FP64 labels of feature rows on the host (the reference's DP return
+ * applied in the principal frame); rows that do not yield get y = 0. */
+ep_status epgpu_mlp_label(const float* x, int64_t n, double lambda_over_2G, float* y);
+/* (Re)allocate the record buffer for `capacity` pairs and empty it. */
+ep_status epgpu_mlp_record_buffer(ep_mlp* m, int64_t capacity);
+/* Pairs recorded so far (*count may exceed the capacity: only the first
+ * `capacity` are kept); copies up to `cap` of them to x, t when given. */
+ep_status epgpu_mlp_recorded(ep_mlp* m, int64_t* count, float* x, float* t, int64_t cap);
+
+/* Select the return map of a mixed-precision, finite-strain, Drucker-Prager
+ * handle (EP_ERR_UNSUPPORTED otherwise for modes 1 and 2).  The network must
+ * outlive its use by the handle. */
+ep_status epgpu_set_return_map(ep_handle* h, ep_mlp* m, int32_t mode);
+/* Cumulative counts since the return map was set: points returned by the
+ * network, points sent to the exact fallback, pairs recorded. */
+ep_status epgpu_return_map_stats(ep_handle* h, int64_t* learned, int64_t* fallback, int64_t* recorded);
+
 #ifdef __cplusplus
 }
 #endif
