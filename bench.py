@@ -97,6 +97,15 @@ ALG_BYTES_MIXED_2D = {
 STEP_BYTES = {"fp64": (35 * 8, 30 * 8), "mixed": (35 * 4, 30 * 4), "mixed_df": (35 * 4, 30 * 4)}
 
 
+def bf16_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["bf16_tflops"]), "measured bf16_tflops"
+    except Exception:
+        return 1900.0, "fallback"
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -244,6 +253,12 @@ def main():
                     help="steps of the plain FP64 step timed beside the headline (0: skip)")
     ap.add_argument("--no-check", action="store_true",
                     help="skip the stress error of the timed run against the FP64 step")
+    ap.add_argument("--rmap", default="learned", choices=["learned", "exact"],
+                    help="return map of the mixed step: the learned one (pairs recorded during the settle, "
+                         "trained on the GPU) or the exact one")
+    ap.add_argument("--pairs", type=int, default=16_000_000, help="record buffer capacity (pairs)")
+    ap.add_argument("--train-iters", type=int, default=3000)
+    ap.add_argument("--seed", type=int, default=5)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--settle", type=float, default=0.5,
@@ -263,37 +278,71 @@ def main():
     mesh, mpts, cmpr = ic["mesh"], ic["mpts"], ic["cmpr"]
     np_, dim = mpts.nmp, mesh.dim
     g = [0.0] * (dim - 1) + [-9.81]
+    learned = args.rmap == "learned" and args.precision != "fp64"
     host0 = mpts.copy()
     e = Engine(ic, cfg["instr"])
+    net, train = None, None
+    if learned:
+        # pairs of the exact return recorded during the settle, then training on the GPU
+        from epgpu.mlp import MLP, lambda_over_2G
+        net = MLP(seed=args.seed, l2g=lambda_over_2G(cmpr))
+        net.record_buffer(args.pairs)
+        e.set_return_map(net, "record")
     if args.settle > 0:
         e.run(1, args.settle, 10.0, 0.0)          # the device time loop (epgpu_run) up to t = settle
         host0 = e.download()
-    vmax = host0.vmax.copy()
-    dts = []
-    for _ in range(args.warmup):
-        dts.append(cfl_dt(mesh, cmpr, vmax))
-        vmax = e.step(1, dts[-1], g)
+    if learned:
+        nrec = e.return_map_stats()["recorded"]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        l1 = net.train(iters=args.train_iters, batch=16384, lr=1e-3, seed=1)
+        l2 = net.train(iters=args.train_iters // 2, batch=16384, lr=2e-4, seed=2)
+        torch.cuda.synchronize()
+        train = {"pairs_recorded": int(nrec), "pairs_kept": int(min(nrec, args.pairs)),
+                 "iterations": args.train_iters + args.train_iters // 2, "batch": 16384,
+                 "seconds": time.perf_counter() - t0, "loss": [l1, l2]}
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")   # 256 MB > 129 MB L2
-    e.profile(True)
-    l0 = e.stats()["launches"]
-    dev_ms = 0.0
-    barrier(ws)
-    torch.cuda.synchronize()
-    with Clocks(local) as clk:
-        for _ in range(args.steps):
-            flush.fill_(1.0)                       # evict L2 between timed steps
-            torch.cuda.synchronize()
-            dts.append(cfl_dt(mesh, cmpr, vmax))
-            vmax = e.step(1, dts[-1], g)
-            dev_ms += e.stats()["device_ms"]
-    torch.cuda.synchronize()
-    barrier(ws)
-    launches = e.stats()["launches"] - l0
-    ktimes = e.kernel_times()
-    e.profile(False)
+
+    def timed(engine, k, w, clk=None):
+        """Upload host0, w warm-up and k timed steps (L2 flushed before each); device ms via CUDA events."""
+        engine.upload(host0)
+        vm = host0.vmax.copy()
+        seq = []
+        for _ in range(w):
+            seq.append(cfl_dt(mesh, cmpr, vm))
+            vm = engine.step(1, seq[-1], g)
+        engine.profile(True)
+        l0 = engine.stats()["launches"]
+        ms = 0.0
+        barrier(ws)
+        torch.cuda.synchronize()
+        if clk:
+            clk.__enter__()
+        try:
+            for _ in range(k):
+                flush.fill_(1.0)
+                torch.cuda.synchronize()
+                seq.append(cfl_dt(mesh, cmpr, vm))
+                vm = engine.step(1, seq[-1], g)
+                ms += engine.stats()["device_ms"]
+        finally:
+            if clk:
+                clk.__exit__(None, None, None)
+        torch.cuda.synchronize()
+        barrier(ws)
+        kt = engine.kernel_times()
+        engine.profile(False)
+        return ms, seq, engine.stats()["launches"] - l0, kt
+
+    clk = Clocks(local)
+    if learned:
+        e.set_return_map(net, "learned")
+    dev_ms, dts, launches, ktimes = timed(e, args.steps, args.warmup, clk)
+    rstats = e.return_map_stats() if learned else None
     tmax = allmax(dev_ms, ws)
     value = ws * np_ * args.steps / (tmax * 1e-3)
     plastic = e.stats()["plastic"]
+    final = e.download()
     # dominant kernel and its roofline
     dom = max(ktimes.items(), key=lambda kv: kv[1][1])
     name, (nl, tot) = dom
@@ -312,6 +361,22 @@ def main():
             "avg_launch_ms": avg_ms,
             "kernel_share": {k: round(v[1] / sum(x[1] for x in ktimes.values()), 4) for k, v in ktimes.items()},
             "step": {"alg_bytes": step_bytes, "achieved_gbs": step_gbs, "frac": step_gbs / peak}}
+    if learned and "mlp" in ktimes:
+        # the network on the tensor cores: 2 (6*128 + 3*128^2 + 128*3) flop per evaluated point
+        nl_, tot_ = ktimes["mlp"]
+        slots = (rstats["learned"] + rstats["fallback"]) / max(args.steps + args.warmup, 1)
+        tf = 100608.0 * slots / (tot_ / nl_ * 1e-3) / 1e12
+        bf = bf16_peak()
+        roof["mlp"] = {"bound": "tensor", "points_per_launch": slots, "avg_launch_ms": tot_ / nl_,
+                       "achieved": tf, "unit": "TFLOP/s", "peak": bf[0], "frac": tf / bf[0],
+                       "peak_source": bf[1]}
+    # the exact-map mixed step beside the learned one
+    exact = None
+    if learned:
+        e.set_return_map(None, "exact")
+        ms_x, _, _, _ = timed(e, args.steps, args.warmup)
+        exact = {"value": ws * np_ * args.steps / (allmax(ms_x, ws) * 1e-3), "unit": "particle-steps/s",
+                 "ms_per_step": ms_x / args.steps}
     # the plain FP64 step beside it, and the stress error of this run against the FP64 step replayed
     # with the same dt sequence from the same state (the FP64 step matches the FP64 oracle bit for bit)
     fp64 = None
@@ -324,7 +389,7 @@ def main():
         if not args.no_check:
             for dt in dts:
                 e64.step(1, dt, g)
-            a, b = e.download(), e64.download()
+            a, b = final, e64.download()
             x0 = host0.x
             check = {
                 "steps": len(dts),
@@ -334,18 +399,7 @@ def main():
                                     / max(abs(b.x[0].max() - x0[0].max()), 1e-300)),
             }
         if args.fp64_steps > 0:
-            v64 = host0.vmax.copy()
-            e64.upload(host0)
-            for _ in range(3):
-                v64 = e64.step(1, cfl_dt(mesh, cmpr, v64), g)
-            e64.profile(True)
-            ms64 = 0.0
-            for _ in range(args.fp64_steps):
-                flush.fill_(1.0)
-                torch.cuda.synchronize()
-                v64 = e64.step(1, cfl_dt(mesh, cmpr, v64), g)
-                ms64 += e64.stats()["device_ms"]
-            e64.profile(False)
+            ms64, _, _, _ = timed(e64, args.fp64_steps, 3)
             fp64 = {"value": np_ * args.fp64_steps / (ms64 * 1e-3), "unit": "particle-steps/s",
                     "steps": args.fp64_steps, "ms_per_step": ms64 / args.fp64_steps}
         e64.close()
@@ -372,6 +426,8 @@ def main():
         down = up
         vm = np.zeros(dim)
         e2 = Engine({"mesh": mesh, "mpts": hp, "cmpr": cmpr}, cfg["instr"])
+        if learned:
+            e2.set_return_map(net, "learned")
         tot = 0.0
         for k in range(args.warmup + args.steps):
             torch.cuda.synchronize()
@@ -393,18 +449,29 @@ def main():
         cpu = {"value": val, "unit": "particle-steps/s", "cores": threads, "kind": "port",
                "sample": f"{steps} elastoplastic steps of the same workload, FP64 restatement on {threads} threads"}
     if rank == 0:
+        rm = None
+        if learned:
+            n_eval = rstats["learned"] + rstats["fallback"]
+            rm = {"return_map": "learned (BF16 tensor-core MLP, exact FP64 fallback)",
+                  "fallback_rate": rstats["fallback"] / max(n_eval, 1), "points_evaluated": n_eval,
+                  "training": train, "exact_map_step": exact,
+                  "speedup_vs_exact_map": value / exact["value"] if exact else None}
         line = {
             "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": tmax / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": {"fp64": "f64", "mixed": "f32+f64", "mixed_df": "f32 (+f32 pairs)"}[args.precision],
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": {"fp64": "f64", "mixed": "f32+f64", "mixed_df": "f32 (+f32 pairs)"}[args.precision]
+            + (" + bf16 MLP" if learned else ""),
             "data": f"synthetic slump geometry ({field})",
-            "config": {"workload": WORKLOAD, "precision": args.precision, "points": np_,
+            "config": {"workload": WORKLOAD, "precision": args.precision,
+                       "return_map": "learned" if learned else "exact", "points": np_,
                        "nodes": mesh.nnodes, "l2": "flushed between timed steps (256 MB write)",
                        "parallelism": f"replicas x{ws}", "plastic_points_last_step": plastic,
                        "settle_s": args.settle},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
             "error_vs_fp64": check, "fp64_step": fp64,
             "speedup_vs_fp64_step": (value / fp64["value"]) if fp64 else None,
+            "learned_return_map": rm,
             "clocks": clk.summary(),
         }
         print(json.dumps(line))

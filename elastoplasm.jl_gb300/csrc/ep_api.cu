@@ -843,15 +843,17 @@ ep_status epgpu_set_return_map(ep_handle* h, ep_mlp* m, int32_t mode) {
         const size_t np = (size_t)std::max(h->np, 1);
         if (!h->rm_buf) {
             if (dalloc(h, &h->rm_buf, np * (RM_NX + RM_NY + 4)) != cudaSuccess ||
-                dalloc(h, &h->rm_int, np + 1) != cudaSuccess)
+                dalloc(h, &h->rm_int, 2 * np + 2) != cudaSuccess)
                 return fail(h, EP_ERR_NOMEM, "device allocation (learned return map slots)");
         }
         b.rx = h->rm_buf;
         b.ry = h->rm_buf + np * RM_NX;
         b.raux = h->rm_buf + np * (RM_NX + RM_NY);
         b.rcount = h->rm_int;
-        b.rpt = h->rm_int + 1;
-        CK(h, cudaMemsetAsync(b.rcount, 0, sizeof(int), h->s));
+        b.fbcount = h->rm_int + 1;
+        b.rpt = h->rm_int + 2;
+        b.fblist = h->rm_int + 2 + np;
+        CK(h, cudaMemsetAsync(b.rcount, 0, 2 * sizeof(int), h->s));
     } else if (mode == EP_RMAP_RECORD) {
         b.rx = mlp_record_x(m);
         b.ry = mlp_record_t(m);

@@ -116,6 +116,8 @@ struct RmapBufs {
     float *rx, *ry, *raux;
     int* rpt;
     int* rcount;
+    int* fbcount;
+    int* fblist;
     long long* rec_count;
     long long rec_cap;
 };

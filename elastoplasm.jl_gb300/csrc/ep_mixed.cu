@@ -177,6 +177,8 @@ struct MCtx {
     float *rx, *ry, *raux;
     int* rpt;
     int* rcount;
+    int* fbcount;       // learned mode: slots the network's output was rejected for
+    int* fblist;
     long long* rec_count;
     long long rec_cap;
     double Deld[9], Cmpd[9], Kd, Gd;   // FP64 copies for the exact fallback
@@ -949,13 +951,13 @@ __global__ void __launch_bounds__(256) km_rmap_finish(MCtx A) {
     EP_ACTIVE(A.ctl);
     const int n = *A.rcount;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    int nl = 0, nf = 0;
+    int nl = 0;
+    bool reject = false;
     if (i < n) {
         const float4 x0 = *reinterpret_cast<const float4*>(A.rx + (size_t)i * RM_NX);
         const float4 x1 = *reinterpret_cast<const float4*>(A.rx + (size_t)i * RM_NX + 4);
         const float4 y = *reinterpret_cast<const float4*>(A.ry + (size_t)i * RM_NY);
         const float4 ax = *reinterpret_cast<const float4*>(A.raux + (size_t)i * 4);
-        const int p = A.rpt[i];
         const float c2 = ax.x, s2 = ax.y, s = ax.z, coh = ax.w;
         const float tphi = x1.x, phin = x1.z;
         const float den = sqrtf(9.f + 12.f * tphi * tphi), eta = 3.f * tphi / den, xi = 3.f * coh / den;
@@ -995,67 +997,96 @@ __global__ void __launch_bounds__(256) km_rmap_finish(MCtx A) {
         }
         if (ok) {
             ++nl;
+            const int p = A.rpt[i];
             add_ep1<ACC>(A, p, dl * 0.57735026918962576f);
             A.P.dlam[p] = dl;
             rebuild_b<ACC>(A, p, e11, e22, e12);
+            A.P.tau[0][p] = tt[0];
+            A.P.tau[1][p] = tt[1];
+            A.P.tau[2][p] = tt[2];
         } else {
-            ++nf;
-            // exact FP64 return of the trial stress rebuilt from the slot
-            const double sd = (double)s;
-            const double q1 = sd * (double)x0.x, q2 = sd * (double)x0.y;
-            const double em = 0.5 * (q1 + q2), r = 0.5 * (q1 - q2);
-            const double te[3] = {em + r * (double)c2, em - r * (double)c2, 2.0 * r * (double)s2};
-            double sv[3];
-            for (int a = 0; a < 3; ++a) sv[a] = A.Deld[a] * te[0] + A.Deld[a + 3] * te[1] + A.Deld[a + 6] * te[2];
-            double inc = 0.0;
-            const double dld = dp_return<3>(sv, 0.0, (double)coh, 0.0, (double)tphi, 0.0, 1.0, 0.0, A.Kd, A.Gd, &inc);
-            A.P.dlam[p] = (float)dld;
-            add_ep1<ACC>(A, p, (float)inc);
-            for (int a = 0; a < 3; ++a) tt[a] = (float)sv[a];
-            if (dld != 0.0) {
-                // b = exp(2 Del \ τ) in FP64
-                double ee[3];
-                for (int a = 0; a < 3; ++a) ee[a] = A.Cmpd[a] * sv[0] + A.Cmpd[a + 3] * sv[1] + A.Cmpd[a + 6] * sv[2];
-                const double m = 0.5 * (ee[0] + ee[1]), ed = 0.5 * (ee[0] - ee[1]), g = 0.5 * ee[2];
-                const double q = sqrt(ed * ed + g * g);
-                const double E = ep_exp(2.0 * m);
-                double ch, shs;
-                if (q < 1.0e-4) {
-                    const double q2s = q * q;
-                    ch = 1.0 + 2.0 * q2s * (1.0 + q2s / 3.0);
-                    shs = 2.0 * (1.0 + q2s * (2.0 / 3.0 + q2s * (2.0 / 15.0)));
-                } else {
-                    const double ep = ep_exp(2.0 * q), em2 = 1.0 / ep;
-                    ch = 0.5 * (ep + em2);
-                    shs = 0.5 * (ep - em2) / q;
-                }
-                const double b0 = E * (ch + shs * ed), b1 = E * (ch - shs * ed), b2 = E * shs * g;
-                if (ACC == 0) {
-                    A.P.bd[0][p] = b0; A.P.bd[1][p] = b1; A.P.bd[2][p] = b2;
-                } else {
-                    const float h0 = (float)b0, h1 = (float)b1, h2 = (float)b2;
-                    A.P.bh[0][p] = h0; A.P.bl[0][p] = (float)(b0 - (double)h0);
-                    A.P.bh[1][p] = h1; A.P.bl[1][p] = (float)(b1 - (double)h1);
-                    A.P.bh[2][p] = h2; A.P.bl[2][p] = (float)(b2 - (double)h2);
-                }
-            }
+            reject = true;
         }
-        A.P.tau[0][p] = tt[0];
-        A.P.tau[1][p] = tt[1];
-        A.P.tau[2][p] = tt[2];
-        if (!(isfinite(tt[0]) && isfinite(tt[1]) && isfinite(tt[2]))) set_err(A.ctl, EP_ERR_NONFINITE, p);
     }
-    const int tl = __reduce_add_sync(0xffffffffu, nl), tf = __reduce_add_sync(0xffffffffu, nf);
-    if ((threadIdx.x & 31) == 0) {
-        if (tl) atomicAdd(&A.ctl->rm_learned, (unsigned long long)tl);
-        if (tf) atomicAdd(&A.ctl->rm_fallback, (unsigned long long)tf);
+    // rejected slots -> the fallback list (one atomic per warp)
+    const unsigned bal = __ballot_sync(0xffffffffu, reject);
+    if (bal) {
+        const int lane = threadIdx.x & 31;
+        int base = 0;
+        if (lane == 0) base = atomicAdd(A.fbcount, __popc(bal));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (reject) A.fblist[base + __popc(bal & ((1u << lane) - 1u))] = i;
     }
+    const int tl = __reduce_add_sync(0xffffffffu, nl);
+    if ((threadIdx.x & 31) == 0 && tl) atomicAdd(&A.ctl->rm_learned, (unsigned long long)tl);
 }
 
-__global__ void km_flip(Ctl* ctl, int* rcount) {
+// km_rmap_fallback: the exact FP64 return (DP.jl:33-66) of the rejected slots, on the
+// trial stress rebuilt from the slot, then b_e = exp(2 Del \ τ) in FP64
+template <int ACC>
+__global__ void __launch_bounds__(256) km_rmap_fallback(MCtx A) {
+    EP_ACTIVE(A.ctl);
+    const int n = *A.fbcount;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) {
+        const int i = A.fblist[k];
+        const float4 x0 = *reinterpret_cast<const float4*>(A.rx + (size_t)i * RM_NX);
+        const float4 x1 = *reinterpret_cast<const float4*>(A.rx + (size_t)i * RM_NX + 4);
+        const float4 ax = *reinterpret_cast<const float4*>(A.raux + (size_t)i * 4);
+        const int p = A.rpt[i];
+        const float c2 = ax.x, s2 = ax.y, s = ax.z, coh = ax.w;
+        const float tphi = x1.x;
+        const double sd = (double)s;
+        const double q1 = sd * (double)x0.x, q2 = sd * (double)x0.y;
+        const double em = 0.5 * (q1 + q2), r = 0.5 * (q1 - q2);
+        const double te[3] = {em + r * (double)c2, em - r * (double)c2, 2.0 * r * (double)s2};
+        double sv[3];
+        for (int a = 0; a < 3; ++a) sv[a] = A.Deld[a] * te[0] + A.Deld[a + 3] * te[1] + A.Deld[a + 6] * te[2];
+        double inc = 0.0;
+        const double dld = dp_return<3>(sv, 0.0, (double)coh, 0.0, (double)tphi, 0.0, 1.0, 0.0, A.Kd, A.Gd, &inc);
+        A.P.dlam[p] = (float)dld;
+        add_ep1<ACC>(A, p, (float)inc);
+        if (dld != 0.0) {
+            double ee[3];
+            for (int a = 0; a < 3; ++a) ee[a] = A.Cmpd[a] * sv[0] + A.Cmpd[a + 3] * sv[1] + A.Cmpd[a + 6] * sv[2];
+            const double m = 0.5 * (ee[0] + ee[1]), ed = 0.5 * (ee[0] - ee[1]), g = 0.5 * ee[2];
+            const double qq = sqrt(ed * ed + g * g);
+            const double E = ep_exp(2.0 * m);
+            double ch, shs;
+            if (qq < 1.0e-4) {
+                const double q2s = qq * qq;
+                ch = 1.0 + 2.0 * q2s * (1.0 + q2s / 3.0);
+                shs = 2.0 * (1.0 + q2s * (2.0 / 3.0 + q2s * (2.0 / 15.0)));
+            } else {
+                const double ep = ep_exp(2.0 * qq), em2 = 1.0 / ep;
+                ch = 0.5 * (ep + em2);
+                shs = 0.5 * (ep - em2) / qq;
+            }
+            const double b0 = E * (ch + shs * ed), b1 = E * (ch - shs * ed), b2 = E * shs * g;
+            if (ACC == 0) {
+                A.P.bd[0][p] = b0; A.P.bd[1][p] = b1; A.P.bd[2][p] = b2;
+            } else {
+                const float h0 = (float)b0, h1 = (float)b1, h2 = (float)b2;
+                A.P.bh[0][p] = h0; A.P.bl[0][p] = (float)(b0 - (double)h0);
+                A.P.bh[1][p] = h1; A.P.bl[1][p] = (float)(b1 - (double)h1);
+                A.P.bh[2][p] = h2; A.P.bl[2][p] = (float)(b2 - (double)h2);
+            }
+        }
+        const float t0 = (float)sv[0], t1 = (float)sv[1], t2 = (float)sv[2];
+        A.P.tau[0][p] = t0;
+        A.P.tau[1][p] = t1;
+        A.P.tau[2][p] = t2;
+        if (!(isfinite(t0) && isfinite(t1) && isfinite(t2))) set_err(A.ctl, EP_ERR_NONFINITE, p);
+    }
+    const int tf = __reduce_add_sync(0xffffffffu, k < n ? 1 : 0);
+    if ((threadIdx.x & 31) == 0 && tf) atomicAdd(&A.ctl->rm_fallback, (unsigned long long)tf);
+}
+
+__global__ void km_flip(Ctl* ctl, int* rcount, int* fbcount) {
     if (!ctl->active) return;
     ctl->parity ^= 1;
-    if (rcount) *rcount = 0;   // learned map slots of the next step
+    if (rcount) *rcount = 0;   // learned map slots and fallbacks of the next step
+    if (fbcount) *fbcount = 0;
 }
 
 
@@ -1333,10 +1364,13 @@ static void mixed_step_impl(const MixedCtx& X, int phase, cudaStream_t s) {
             mark("mlp");
             km_rmap_finish<ACC><<<gp, 256, 0, s>>>(A);
             mark("rmap_finish");
-            L += 2;
+            km_rmap_fallback<ACC><<<gp, 256, 0, s>>>(A);
+            mark("rmap_fallback");
+            L += 3;
         }
     }
-    km_flip<<<1, 1, 0, s>>>(A.ctl, A.rmode == EP_RMAP_LEARNED ? A.rcount : nullptr);
+    const bool lrn = A.rmode == EP_RMAP_LEARNED;
+    km_flip<<<1, 1, 0, s>>>(A.ctl, lrn ? A.rcount : nullptr, lrn ? A.fbcount : nullptr);
     ++L;
     if (X.launches) *X.launches += L;
 }
@@ -1408,6 +1442,7 @@ void mixed_ctx_init(void* mem, const Cfg& cf, const Geo& g, Ctl* ctl, const PM& 
     A->rmode = EP_RMAP_EXACT;
     A->rx = A->ry = A->raux = nullptr;
     A->rpt = A->rcount = nullptr;
+    A->fbcount = A->fblist = nullptr;
     A->rec_count = nullptr;
     A->rec_cap = 0;
 }
@@ -1420,6 +1455,8 @@ void mixed_set_rmap(void* mem, const RmapBufs& b) {
     A->raux = b.raux;
     A->rpt = b.rpt;
     A->rcount = b.rcount;
+    A->fbcount = b.fbcount;
+    A->fblist = b.fblist;
     A->rec_count = b.rec_count;
     A->rec_cap = b.rec_cap;
 }

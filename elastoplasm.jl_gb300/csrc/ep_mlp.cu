@@ -54,16 +54,26 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
     __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
     return *reinterpret_cast<uint32_t*>(&h);
 }
-__device__ __forceinline__ float silu(float z) { return z / (1.f + __expf(-z)); }
+// SiLU through the hardware tanh: silu(z) = z sigmoid(z), sigmoid(z) = (1 + tanh(z / 2)) / 2.
+// tanh.approx has a relative error near 2^-11, below the BF16 rounding of the activations.
+__device__ __forceinline__ float tanh_approx(float x) {
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float silu(float z) {
+    const float hz = 0.5f * z;
+    return fmaf(hz, tanh_approx(hz), hz);
+}
 __device__ __forceinline__ float dsilu(float z) {
-    const float s = 1.f / (1.f + __expf(-z));
+    const float s = fmaf(0.5f, tanh_approx(0.5f * z), 0.5f);
     return s * (1.f + z * (1.f - s));
 }
 
 // ---------------------------------------------------------------------------
-// forward, fused over the five layers; one CTA (8 warps) per SM walks tiles of
+// forward, fused over the five layers; one CTA (16 warps) per SM walks tiles of
 // 128 rows.  Warp w reads TMEM lanes 32 (w % 4) .. + 31 (its rows) and the
-// column half w / 4 of every accumulator.
+// column quarter w / 4 of every accumulator.
 struct FwdArgs {
     const float* X;       // rows of RM_NX floats (the first 6 are the inputs)
     int n;                // rows, or (ndev != nullptr) the capacity
@@ -78,7 +88,9 @@ struct FwdArgs {
 constexpr int FWD_SH = 0, FWD_SX = FWD_SH + MT * W * 2, FWD_SW = FWD_SX + MT * KIN * 2;
 constexpr int FWD_BAR = FWD_SW + IMG_BYTES, FWD_SMEM = FWD_BAR + 32;
 
-__global__ void __launch_bounds__(256, 1) km_mlp_fwd(FwdArgs a) {
+constexpr int FWD_THREADS = 512;
+
+__global__ void __launch_bounds__(FWD_THREADS, 1) km_mlp_fwd(FwdArgs a) {
     extern __shared__ __align__(128) uint8_t sm[];
     uint8_t* sH = sm + FWD_SH;
     uint8_t* sX = sm + FWD_SX;
@@ -114,7 +126,7 @@ __global__ void __launch_bounds__(256, 1) km_mlp_fwd(FwdArgs a) {
     const float* bias = reinterpret_cast<const float*>(sW + IBIAS);
     const uint32_t aX = tc::smem_u32(sX), aH = tc::smem_u32(sH), aW = tc::smem_u32(sW);
     const uint32_t id128 = tc::idesc_bf16(MT, W), id16 = tc::idesc_bf16(MT, NO);
-    const int q = warp & 3, half = warp >> 2;
+    const int q = warp & 3, cq = warp >> 2;        // lane quarter, column quarter
     const int row = 32 * q + lane;
     const uint32_t trow = tbase + ((uint32_t)(32 * q) << 16);
     uint32_t ph = 0;
@@ -155,14 +167,19 @@ __global__ void __launch_bounds__(256, 1) km_mlp_fwd(FwdArgs a) {
             const float* b = bias + (l - 1) * W;
             const int r = r0 + row;
 #pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                const int col = 64 * half + 16 * c;
-                float v[16];
+            for (int c = 0; c < 2; ++c) {
+                const int col = 32 * cq + 16 * c;
+                float v[16], bb[16];
                 tc::tmem_ld16(trow + (uint32_t)col, v);
+#pragma unroll
+                for (int i = 0; i < 16; i += 4) {
+                    const float4 t4 = *reinterpret_cast<const float4*>(b + col + i);
+                    bb[i] = t4.x; bb[i + 1] = t4.y; bb[i + 2] = t4.z; bb[i + 3] = t4.w;
+                }
                 uint32_t hb[8];
 #pragma unroll
                 for (int i = 0; i < 16; i += 2) {
-                    const float z0 = v[i] + b[col + i], z1 = v[i + 1] + b[col + i + 1];
+                    const float z0 = v[i] + bb[i], z1 = v[i + 1] + bb[i + 1];
                     v[i] = z0;
                     v[i + 1] = z1;
                     hb[i >> 1] = pack_bf16(silu(z0), silu(z1));
@@ -201,7 +218,7 @@ __global__ void __launch_bounds__(256, 1) km_mlp_fwd(FwdArgs a) {
         ok = __syncthreads_and(ok);
         if (!ok) break;
         tc::fence_after_sync();
-        if (half == 0) {
+        if (cq == 0) {
             float v[16];
             tc::tmem_ld16(trow + W, v);
             const int r = r0 + row;
@@ -543,6 +560,18 @@ __global__ void km_mlp_gather(const float* DX, const float* DT, long long N, con
     *reinterpret_cast<float4*>(T + (size_t)r * RM_NY) = *reinterpret_cast<const float4*>(DT + (size_t)k * RM_NY);
 }
 
+// failure detection: a wait on an mbarrier that nothing arrives at gives up after `ns`
+__global__ void km_wait_selftest(uint64_t ns, int* out) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        tc::mbar_init(&bar, 1);
+        tc::mbar_fence_init();
+    }
+    __syncthreads();
+    const bool ok = tc::mbar_wait(&bar, 0, ns);
+    if (threadIdx.x == 0) out[0] = ok ? 0 : 1;
+}
+
 }  // namespace mlp
 
 // ---------------------------------------------------------------------------
@@ -598,7 +627,7 @@ static void mlp_fwd_launch(ep_mlp* m, const float* X, int n, const int* ndev, fl
     a.err = m->d.err;
     const int tiles = (n + MT - 1) / MT;
     const int grid = ndev ? m->sms : std::max(1, std::min(tiles, m->sms));
-    km_mlp_fwd<<<grid, 256, FWD_SMEM, s>>>(a);
+    km_mlp_fwd<<<grid, FWD_THREADS, FWD_SMEM, s>>>(a);
 }
 
 void mlp_infer(ep_mlp* m, const float* X, const int* ndev, int cap, float* Y, cudaStream_t s) {
@@ -929,6 +958,21 @@ ep_status epgpu_mlp_train(ep_mlp* m, const float* x, const float* t, int64_t n, 
     }
     if (loss_out) *loss_out = l;
     return st;
+}
+
+ep_status epgpu_selftest_wait_timeout(int64_t timeout_ns) {
+    if (timeout_ns <= 0 || timeout_ns > 2000000000LL) return EP_ERR_ARG;
+    int* d = nullptr;
+    int r = -1;
+    cudaError_t e = cudaMalloc(&d, sizeof(int));
+    if (e == cudaSuccess) {
+        km_wait_selftest<<<1, 32>>>((uint64_t)timeout_ns, d);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(&r, d, sizeof(int), cudaMemcpyDeviceToHost);
+    if (d) cudaFree(d);
+    if (e != cudaSuccess) return mcuda(nullptr, e, "wait self test");
+    return r == 1 ? EP_ERR_TIMEOUT : EP_OK;
 }
 
 ep_status epgpu_mlp_label(const float* x, int64_t n, double lambda_over_2G, float* y) {

@@ -177,6 +177,7 @@ SIGNATURES = {
     "epgpu_mlp_record_buffer": (C.c_int, [C.c_void_p, C.c_int64]),
     "epgpu_mlp_recorded": (C.c_int, [C.c_void_p, _I64, _F, _F, C.c_int64]),
     "epgpu_set_return_map": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32]),
+    "epgpu_selftest_wait_timeout": (C.c_int, [C.c_int64]),
     "epgpu_return_map_stats": (C.c_int, [C.c_void_p, _I64, _I64, _I64]),
 }
 

@@ -298,6 +298,12 @@ ep_status epgpu_mlp_record_buffer(ep_mlp* m, int64_t capacity);
  * `capacity` are kept); copies up to `cap` of them to x, t when given. */
 ep_status epgpu_mlp_recorded(ep_mlp* m, int64_t* count, float* x, float* t, int64_t cap);
 
+/* Failure-detection self test (no counterpart in the reference): one CTA waits on
+ * an mbarrier that nothing arrives at, with the bounded wait every tensor-core
+ * kernel of the library uses.  Returns EP_ERR_TIMEOUT once the wait gave up after
+ * timeout_ns (the expected outcome; the context stays usable), EP_OK if it did not. */
+ep_status epgpu_selftest_wait_timeout(int64_t timeout_ns);
+
 /* Select the return map of a mixed-precision, finite-strain, Drucker-Prager
  * handle (EP_ERR_UNSUPPORTED otherwise for modes 1 and 2).  The network must
  * outlive its use by the handle. */

@@ -212,3 +212,21 @@ def test_learned_step_against_the_oracle(oracle_mod, trained_net, hp):
     assert results["trained"][0] < 1e-3
     assert results["untrained"][1] > 0.8
     assert results["trained"][1] < 0.5 and results["trained"][1] < 0.5 * results["untrained"][1]
+
+
+def test_bounded_wait_reports_a_timeout_and_the_context_survives():
+    """A wait that never completes (an mbarrier nothing arrives at) gives up after its limit
+    and reports EP_ERR_TIMEOUT; the next tensor-core launch works."""
+    import time
+    from epgpu import abi
+    from epgpu.mlp import MLP
+    import mlp_oracle as mo
+    lib = abi.load_library()
+    t0 = time.perf_counter()
+    st = lib.epgpu_selftest_wait_timeout(50_000_000)       # 50 ms
+    el = time.perf_counter() - t0
+    assert st == 5 and 0.04 < el < 5.0
+    net = MLP(seed=1, l2g=L2G)
+    x = mo.sample_trials(256, L2G, seed=1)
+    y = net.forward(x)
+    assert np.isfinite(y).all()
