@@ -58,6 +58,12 @@ class ep_mpts_view(C.Structure):
                 + [("p2e", _I64), ("p2n", _I64)])
 
 
+class ep_grf(C.Structure):
+    _fields_ = [("dim", C.c_int32), ("covariance", C.c_int32), ("nh", C.c_int32), ("pad_", C.c_int32),
+                ("ell", C.c_double * 3), ("mean", C.c_double), ("std", C.c_double), ("vmin", C.c_double),
+                ("seed", C.c_uint64)]
+
+
 class ep_kernel_time(C.Structure):
     _fields_ = [("name", C.c_char * 32), ("launches", C.c_int64), ("total_ms", C.c_double)]
 
@@ -178,6 +184,8 @@ SIGNATURES = {
     "epgpu_mlp_recorded": (C.c_int, [C.c_void_p, _I64, _F, _F, C.c_int64]),
     "epgpu_set_return_map": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32]),
     "epgpu_selftest_wait_timeout": (C.c_int, [C.c_int64]),
+    "epgpu_grf_spectrum": (C.c_int, [C.POINTER(ep_grf), _D, _D]),
+    "epgpu_grf_points": (C.c_int, [C.POINTER(ep_grf), _D, C.c_int64, _D]),
     "epgpu_return_map_stats": (C.c_int, [C.c_void_p, _I64, _I64, _I64]),
 }
 

@@ -25,6 +25,7 @@ UNITS = {
     "ep_fp64.cu": ["-fmad=false"],
     "ep_mixed.cu": [],
     "ep_mlp.cu": [],
+    "ep_grf.cu": [],
 }
 
 

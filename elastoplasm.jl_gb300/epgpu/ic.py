@@ -225,7 +225,7 @@ def setup_cmpr(mesh, E=1.0e6, nu=0.3, rho0=2700.0, **over):
 
 
 # ----------------------------------------------------------------------------- points
-def mpts_populate(mesh, cmpr, instr, ni=2, grf=None):
+def mpts_populate(mesh, cmpr, instr, ni=2, grf_fn=None):
     """Regular lattice of points, ``ni`` per cell and direction (mpts_populate.jl:26-56)."""
     h, xB = mesh.h, mesh.xB
     ax = []
@@ -243,22 +243,22 @@ def mpts_populate(mesh, cmpr, instr, ni=2, grf=None):
         X[:, 1] = np.repeat(y, len(x) * len(z))
         X[:, 2] = np.tile(z, len(x) * len(y))
     if instr["grf"]["status"]:
-        if grf is None:
+        if grf_fn is None:
             from .grf import cohesion_field
-            grf = cohesion_field
-        c0 = grf(X, cmpr, instr, mesh)
+            grf_fn = cohesion_field
+        c0 = grf_fn(X, cmpr, instr, mesh)
     else:
         c0 = np.ones(X.shape[0]) * cmpr["c0"]
     return {"ni": ni, "x": X, "c0": c0}
 
 
-def get_slump(mesh, cmpr, instr, ni=2, lz=12.80, grf=None):
+def get_slump(mesh, cmpr, instr, ni=2, lz=12.80, grf_fn=None):
     """Slump geometry filter (utils/setup/mpts/get_slump.jl:18-95).
 
     Only the last of the 200 line points decides (the loop overwrites ``pos``),
     and ``shuffle`` is dropped because its result is unused (get_slump.jl:88).
     """
-    out = mpts_populate(mesh, cmpr, instr, ni=ni, grf=grf)
+    out = mpts_populate(mesh, cmpr, instr, ni=ni, grf_fn=grf_fn)
     wl = 0.15 * lz
     X, c0 = out["x"], out["c0"]
     keep = X[:, -1] <= lz - (0.5 * mesh.h[-1] / ni)
@@ -377,7 +377,7 @@ def setup_time(instr, te=0.0, tg=0.0, tep=0.0):
 
 
 # ----------------------------------------------------------------------------- entry points
-def ic_slump(L, nel, ni=2, cmpr_over=None, grf=None, **kwargs):
+def ic_slump(L, nel, ni=2, cmpr_over=None, grf_fn=None, **kwargs):
     """``ic_slump(L, nel; kwargs...)`` (script/example/slump.jl:22-49).
 
     Returns ``(ic, cfg)`` like the reference: ``ic`` holds ``mesh``, ``mpts``,
@@ -389,7 +389,7 @@ def ic_slump(L, nel, ni=2, cmpr_over=None, grf=None, **kwargs):
     geom = get_geom(nel, L, instr)
     mesh = setup_mesh(instr, geom)
     cmpr = setup_cmpr(mesh, **(cmpr_over or {}))
-    mpts = setup_mpts(mesh, cmpr, get_slump(mesh, cmpr, instr, ni=ni, grf=grf))
+    mpts = setup_mpts(mesh, cmpr, get_slump(mesh, cmpr, instr, ni=ni, grf_fn=grf_fn))
     time = setup_time(instr, te=10.0, tg=10.0, tep=5.0)
     ic = {"mesh": mesh, "mpts": mpts, "cmpr": cmpr, "time": time}
     cfg = {"instr": instr, "misc": {"file": f"{mesh.dim}d_{instr['fwrk']['trsfr']}"}}

@@ -298,6 +298,33 @@ ep_status epgpu_mlp_record_buffer(ep_mlp* m, int64_t capacity);
  * `capacity` are kept); copies up to `cap` of them to x, t when given. */
 ep_status epgpu_mlp_recorded(ep_mlp* m, int64_t* count, float* x, float* t, int64_t cap);
 
+/* ---- Random fields -------------------------------------------------------
+ * Seeded Gaussian random field at the points (cohesion fields of the scaled-up
+ * slumps).  The reference's generator (utils/setup/mpts/GRF.jl:66-141) draws a
+ * Gaussian-covariance field on a grid; its exponential branch is not wired in
+ * (mpts_populate.jl:49-51).  This one is the randomization (spectral) method
+ * evaluated at the point positions: value = max(mean + f(x), vmin) with
+ * f = std / sqrt(nh) sum_k [xi_k cos(kappa_k . x) + eta_k sin(kappa_k . x)],
+ * correlation rho(|dx / ell|), rho(r) = exp(-r) (exponential) or exp(-r^2)
+ * (Gaussian).  The spectrum comes from one splitmix64 stream of `seed`. */
+enum { EP_GRF_GAUSSIAN = 0, EP_GRF_EXPONENTIAL = 1 };
+typedef struct ep_grf {
+    int32_t dim;           /* 2 or 3 */
+    int32_t covariance;    /* EP_GRF_* */
+    int32_t nh;            /* harmonics (the reference uses 5000) */
+    int32_t pad_;
+    double  ell[3];        /* correlation lengths per direction */
+    double  mean, std, vmin;
+    uint64_t seed;
+} ep_grf;
+
+/* The harmonics of the field on the host: kappa (nh x dim, row-major), amplitudes
+ * (nh x 2: xi, eta). */
+ep_status epgpu_grf_spectrum(const ep_grf* g, double* kappa, double* amplitudes);
+/* Field values at np points x (dim x np column-major, the layout of mpts.x),
+ * evaluated on the GPU into out (np, host). */
+ep_status epgpu_grf_points(const ep_grf* g, const double* x, int64_t np, double* out);
+
 /* Failure-detection self test (no counterpart in the reference): one CTA waits on
  * an mbarrier that nothing arrives at, with the bounded wait every tensor-core
  * kernel of the library uses.  Returns EP_ERR_TIMEOUT once the wait gave up after
