@@ -437,6 +437,345 @@ __global__ void __launch_bounds__(256) km_g2p(MCtx A) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// Point-parallel transfers over the sorted cell lists: lane = one list slot, so
+// the lanes of a cell are adjacent in a warp.  A scatter sums each node's
+// contributions over the lanes of the same cell with a segmented warp reduction
+// (towards the first lane of the cell), and that lane issues one FP32 atomic
+// per node and quantity.  Gathers read the cell's 16 nodes through L1.
+struct Seg {
+    int lane, last, steps;   // last lane of this lane's cell in the warp; reduction steps
+    bool head;               // first lane of its cell in the warp
+};
+
+// segments of equal cell ids c (c < 0: not a point)
+__device__ __forceinline__ Seg seg_of(int c) {
+    Seg s;
+    s.lane = threadIdx.x & 31;
+    const int up = __shfl_up_sync(0xffffffffu, c, 1);
+    const unsigned heads = __ballot_sync(0xffffffffu, s.lane == 0 || c != up);
+    s.head = (heads >> s.lane) & 1u;
+    const unsigned after = s.lane == 31 ? 0u : (heads & ~((2u << s.lane) - 1u));
+    s.last = after ? (__ffs(after) - 2) : 31;
+    const int len = __reduce_max_sync(0xffffffffu, (unsigned)(s.last - s.lane + 1));
+    s.steps = len <= 1 ? 0 : len <= 2 ? 1 : len <= 4 ? 2 : len <= 8 ? 3 : len <= 16 ? 4 : 5;
+    return s;
+}
+
+// sum of v over the lanes [lane, last] of the segment (meaningful at the segment head)
+__device__ __forceinline__ float seg_sum(float v, const Seg& s) {
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+        if (i >= s.steps) break;
+        const int o = 1 << i;
+        const float t = __shfl_down_sync(0xffffffffu, v, o);
+        if (s.lane + o <= s.last) v += t;
+    }
+    return v;
+}
+
+// the point of list slot k with its cell's stencil and the shape values along both axes
+struct PtW {
+    int p, c, ex, ez;
+    Axis4 ax, az;
+    float wx[4], dwx[4], wz[4], dwz[4];
+    float dx, dz;
+};
+
+template <int BASIS>
+__device__ __forceinline__ bool point_of(const MCtx& A, int cur, int k, int n, PtW& W, bool& bad) {
+    if (k >= n) {
+        W.p = -1;
+        W.c = -1;
+        return false;
+    }
+    W.p = A.S.list[cur][k];
+    W.c = A.S.cellof[cur][k];
+    W.ex = W.c / A.g.nel[1];
+    W.ez = W.c - W.ex * A.g.nel[1];
+    W.ax = axis4(A.g, 0, W.ex);
+    W.az = axis4(A.g, 1, W.ez);
+    const float hx = (float)A.g.h[0], hz = (float)A.g.h[1];
+    W.dx = A.P.dx[cur][0][W.p];
+    W.dz = A.P.dx[cur][1][W.p];
+    const float lx = BASIS == EP_BASIS_GIMPM ? A.P.l[0][W.p] : 0.f;
+    const float lz = BASIS == EP_BASIS_GIMPM ? A.P.l[1][W.p] : 0.f;
+    axis_w<BASIS>(W.ax, W.dx, hx, 1.f / hx, lx, W.wx, W.dwx, bad);
+    axis_w<BASIS>(W.az, W.dz, hz, 1.f / hz, lz, W.wz, W.dwz, bad);
+    return true;
+}
+
+// km_p2g_seg: m, p, f (p2n.jl:135-155 std, 217-240 tpic), one lane per point
+template <int BASIS>
+__global__ void __launch_bounds__(256) km_p2g_seg(MCtx A) {
+    EP_ACTIVE(A.ctl);
+    const int cur = A.ctl->parity;
+    const int n = A.S.start[cur][A.g.ncell];
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    bool bad = false;
+    PtW W;
+    const bool live = point_of<BASIS>(A, cur, k, n, W, bad);
+    const Seg S = seg_of(W.c);
+    const float hx = (float)A.g.h[0], hz = (float)A.g.h[1];
+    const float gz = (float)A.ctl->g[1];
+    const bool fin = A.cf.deform == EP_DEFORM_FINITE;
+    const bool tpic = A.cf.trsfr == EP_TRSFR_TPIC;
+    float ms = 0.f, vx = 0.f, vz = 0.f, txx = 0.f, tzz = 0.f, txz = 0.f, gxx = 0.f, gzx = 0.f, gxz = 0.f, gzz = 0.f;
+    if (live) {
+        const int p = W.p;
+        ms = A.P.mp[p];
+        vx = A.P.v[0][p];
+        vz = A.P.v[1][p];
+        const float sc = fin ? A.P.Om0[p] : A.P.Om[p];          // Ω σ = Ω0 τ (finite) or Ω σ
+        txx = sc * A.P.tau[0][p];
+        tzz = sc * A.P.tau[1][p];
+        txz = sc * A.P.tau[2][p];
+        if (tpic) {
+            gxx = A.P.dv[0][p];
+            gzx = A.P.dv[1][p];
+            gxz = A.P.dv[2][p];
+            gzz = A.P.dv[3][p];
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            float N = 0.f, Nx = 0.f, Nz = 0.f;
+            if (live) {
+                N = W.wx[i] * W.wz[j];
+                Nx = W.dwx[i] * W.wz[j];
+                Nz = W.wx[i] * W.dwz[j];
+            }
+            const float Nm = N * ms;
+            float px, pz;
+            if (!tpic) {
+                px = Nm * vx;
+                pz = Nm * vz;
+            } else {
+                // v + ∇v (x_n - x_p) with the previous step's ∇v (p2n.jl:233-235)
+                const float ddx = (float)(i - 1) * hx - W.dx, ddz = (float)(j - 1) * hz - W.dz;
+                px = Nm * (vx + gxx * ddx + gxz * ddz);
+                pz = Nm * (vz + gzx * ddx + gzz * ddz);
+            }
+            const float fx = -(Nx * txx + Nz * txz);
+            const float fz = -((Nx * txz + Nz * tzz) - Nm * gz);
+            const float sm = seg_sum(Nm, S), spx = seg_sum(px, S), spz = seg_sum(pz, S);
+            const float sfx = seg_sum(fx, S), sfz = seg_sum(fz, S);
+            if (S.head && live && W.ax.cls[i] >= 0 && W.az.cls[j] >= 0) {
+                const int nd = node2(A.g, W.ax, W.az, i, j);
+                atomicAdd(&A.N.m[nd], sm);
+                atomicAdd(&A.N.p[0][nd], spx);
+                atomicAdd(&A.N.p[1][nd], spz);
+                atomicAdd(&A.N.f[0][nd], sfx);
+                atomicAdd(&A.N.f[1][nd], sfz);
+            }
+        }
+    }
+    if (bad) set_err(A.ctl, EP_ERR_INVALID_POSITION, W.c);
+}
+
+// km_g2p_seg: PIC/FLIP (n2p.jl:14-40), new cell + offset, vmax, next-cell counts
+// (tplgy.jl:43-62) and the mUSL momentum P2G (augm.jl:13-25), one lane per point
+template <int BASIS>
+__global__ void __launch_bounds__(256) km_g2p_seg(MCtx A) {
+    EP_ACTIVE(A.ctl);
+    const int cur = A.ctl->parity, nxt = cur ^ 1;
+    const int n = A.S.start[cur][A.g.ncell];
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    bool bad = false;
+    PtW W;
+    const bool live = point_of<BASIS>(A, cur, k, n, W, bad);
+    const Seg S = seg_of(W.c);
+    const float ihx = 1.f / (float)A.g.h[0], ihz = 1.f / (float)A.g.h[1];
+    const float dtf = (float)A.ctl->dt, Cpf = (float)A.cf.Cpf;
+    unsigned vm0 = 0u, vm1 = 0u;
+    float vx = 0.f, vz = 0.f, mp = 0.f;
+    int c2 = -1;
+    if (live) {
+        float vpx = 0.f, vpz = 0.f, afx = 0.f, afz = 0.f;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            if (W.ax.cls[i] < 0) continue;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                if (W.az.cls[j] < 0) continue;
+                const int nd = node2(A.g, W.ax, W.az, i, j);
+                const float N = W.wx[i] * W.wz[j];
+                vpx += N * __ldg(&A.N.v[0][nd]);
+                vpz += N * __ldg(&A.N.v[1][nd]);
+                afx += N * __ldg(&A.N.a[0][nd]);
+                afz += N * __ldg(&A.N.a[1][nd]);
+            }
+        }
+        const int p = W.p;
+        vx = Cpf * (A.P.v[0][p] + dtf * afx) + (1.f - Cpf) * vpx;
+        vz = Cpf * (A.P.v[1][p] + dtf * afz) + (1.f - Cpf) * vpz;
+        A.P.v[0][p] = vx;
+        A.P.v[1][p] = vz;
+        vm0 = __float_as_uint(fabsf(vx));
+        vm1 = __float_as_uint(fabsf(vz));
+        // x += dt v_PIC as a cell offset update, then re-binning (tplgy.jl:49)
+        const float ox = W.dx + dtf * vpx, oz = W.dz + dtf * vpz;
+        if (isfinite(ox) && isfinite(oz)) {
+            int ex2, ez2;
+            float o2x, o2z;
+            recell(A.g, 0, W.ex, ox, ihx, ex2, o2x);
+            recell(A.g, 1, W.ez, oz, ihz, ez2, o2z);
+            c2 = ez2 + A.g.nel[1] * ex2;
+            A.P.dx[nxt][0][p] = o2x;
+            A.P.dx[nxt][1][p] = o2z;
+        } else {
+            set_err(A.ctl, EP_ERR_NONFINITE, p);
+        }
+        A.P.p2e_next[p] = c2;
+        mp = A.P.mp[p];
+    }
+    {
+        // next-cell counts: one atomic per distinct cell of the warp
+        const unsigned mm = __match_any_sync(0xffffffffu, c2);
+        if (c2 >= 0 && S.lane == __ffs(mm) - 1) atomicAdd(&A.S.count[nxt][c2], __popc(mm));
+    }
+    if (A.cf.musl) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const float Nm = live ? W.wx[i] * W.wz[j] * mp : 0.f;
+                const float sx = seg_sum(Nm * vx, S), sz = seg_sum(Nm * vz, S);
+                if (S.head && live && W.ax.cls[i] >= 0 && W.az.cls[j] >= 0) {
+                    const int nd = node2(A.g, W.ax, W.az, i, j);
+                    atomicAdd(&A.N.pm[0][nd], sx);
+                    atomicAdd(&A.N.pm[1][nd], sz);
+                }
+            }
+        }
+    }
+    if (bad) set_err(A.ctl, EP_ERR_INVALID_POSITION, W.c);
+    // vmax over the warp, one atomic per warp (non-negative floats order like their bits)
+    vm0 = __reduce_max_sync(0xffffffffu, vm0);
+    vm1 = __reduce_max_sync(0xffffffffu, vm1);
+    if (S.lane == 0) {
+        if (vm0) atomicMax(&A.ctl->vmax_bits[0], (unsigned long long)__double_as_longlong((double)__uint_as_float(vm0)));
+        if (vm1) atomicMax(&A.ctl->vmax_bits[1], (unsigned long long)__double_as_longlong((double)__uint_as_float(vm1)));
+    }
+}
+
+// km_p2g_tile: m, p, f (p2n.jl:135-155 std, 217-240 tpic).  A CTA owns 64
+// consecutive cells, whose points form one slice of the sorted list.  The slice
+// is staged through shared memory in chunks of one point per thread (point data
+// and shape values computed once per point), then four lanes per cell -- lane q
+// owns stencil column q -- accumulate the column's 4 nodes x 5 quantities in
+// registers over the cell's staged points, and add them to the grid with one
+// FP32 atomic per node and quantity.
+constexpr int TP_CELLS = 64, TP_THREADS = 256, TP_STRIDE = 29;   // floats per staged point (odd: no bank conflicts)
+
+template <int BASIS>
+__global__ void __launch_bounds__(TP_THREADS) km_p2g_tile(MCtx A) {
+    EP_ACTIVE(A.ctl);
+    __shared__ float sp[TP_THREADS * TP_STRIDE];
+    const int cur = A.ctl->parity;
+    const int c0 = blockIdx.x * TP_CELLS;
+    if (c0 >= A.g.ncell) return;
+    const int c1 = min(c0 + TP_CELLS, A.g.ncell);
+    const int* start = A.S.start[cur];
+    const int b0 = start[c0], b1 = start[c1];
+    if (b0 == b1) return;
+    const int t = threadIdx.x;
+    const int q = t & 3, cl = c0 + (t >> 2);          // this lane's cell and stencil column
+    const bool cell_ok = cl < c1;
+    const int pb = cell_ok ? start[cl] : 0, pe = cell_ok ? start[cl + 1] : 0;
+    const float hx = (float)A.g.h[0], hz = (float)A.g.h[1];
+    const float gz = (float)A.ctl->g[1];
+    const bool fin = A.cf.deform == EP_DEFORM_FINITE;
+    const bool tpic = A.cf.trsfr == EP_TRSFR_TPIC;
+    float am[4], apx[4], apz[4], afx[4], afz[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) am[j] = apx[j] = apz[j] = afx[j] = afz[j] = 0.f;
+    bool bad = false;
+    for (int ch = b0; ch < b1; ch += TP_THREADS) {
+        // stage one point per thread
+        const int k = ch + t;
+        if (k < b1) {
+            const int p = A.S.list[cur][k], c = A.S.cellof[cur][k];
+            const int ex = c / A.g.nel[1], ez = c - ex * A.g.nel[1];
+            const Axis4 ax = axis4(A.g, 0, ex), az = axis4(A.g, 1, ez);
+            const float dx = A.P.dx[cur][0][p], dz = A.P.dx[cur][1][p];
+            const float lx = BASIS == EP_BASIS_GIMPM ? A.P.l[0][p] : 0.f;
+            const float lz = BASIS == EP_BASIS_GIMPM ? A.P.l[1][p] : 0.f;
+            float* s = sp + t * TP_STRIDE;
+            axis_w<BASIS>(ax, dx, hx, 1.f / hx, lx, s + 0, s + 4, bad);      // wx, dwx
+            axis_w<BASIS>(az, dz, hz, 1.f / hz, lz, s + 8, s + 12, bad);     // wz, dwz
+            const float sc = fin ? A.P.Om0[p] : A.P.Om[p];                  // Ω σ = Ω0 τ (finite) or Ω σ
+            s[16] = A.P.mp[p];
+            s[17] = A.P.v[0][p];
+            s[18] = A.P.v[1][p];
+            s[19] = sc * A.P.tau[0][p];
+            s[20] = sc * A.P.tau[1][p];
+            s[21] = sc * A.P.tau[2][p];
+            if (tpic) {
+                s[22] = dx;
+                s[23] = dz;
+                s[24] = A.P.dv[0][p];
+                s[25] = A.P.dv[1][p];
+                s[26] = A.P.dv[2][p];
+                s[27] = A.P.dv[3][p];
+            }
+        }
+        __syncthreads();
+        // this lane's cell: its points inside the chunk
+        const int lo = max(pb, ch), hi = min(pe, min(ch + TP_THREADS, b1));
+        for (int kk = lo; kk < hi; ++kk) {
+            const float* s = sp + (kk - ch) * TP_STRIDE;
+            const float wq = s[q], dwq = s[4 + q];
+            const float ms = s[16], vx = s[17], vz = s[18], txx = s[19], tzz = s[20], txz = s[21];
+            float vxi = vx, vzi = vz, gxz = 0.f, gzz = 0.f, dzp = 0.f;
+            if (tpic) {
+                // v + ∇v (x_n - x_p) with the previous step's ∇v (p2n.jl:233-235)
+                const float ddx = (float)(q - 1) * hx - s[22];
+                dzp = s[23];
+                vxi = vx + s[24] * ddx;
+                vzi = vz + s[25] * ddx;
+                gxz = s[26];
+                gzz = s[27];
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const float wz = s[8 + j], dwz = s[12 + j];
+                const float N = wq * wz, Nx = dwq * wz, Nz = wq * dwz;
+                const float Nm = N * ms;
+                am[j] += Nm;
+                if (!tpic) {
+                    apx[j] += Nm * vx;
+                    apz[j] += Nm * vz;
+                } else {
+                    const float ddz = (float)(j - 1) * hz - dzp;
+                    apx[j] += Nm * (vxi + gxz * ddz);
+                    apz[j] += Nm * (vzi + gzz * ddz);
+                }
+                afx[j] -= Nx * txx + Nz * txz;
+                afz[j] -= (Nx * txz + Nz * tzz) - Nm * gz;
+            }
+        }
+        __syncthreads();
+    }
+    if (bad) set_err(A.ctl, EP_ERR_INVALID_POSITION, c0);
+    if (!cell_ok || pb == pe) return;
+    const int ex = cl / A.g.nel[1], ez = cl - ex * A.g.nel[1];
+    const Axis4 ax = axis4(A.g, 0, ex), az = axis4(A.g, 1, ez);
+    if (ax.cls[q] < 0) return;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        if (az.cls[j] < 0) continue;
+        const int n = node2(A.g, ax, az, q, j);
+        atomicAdd(&A.N.m[n], am[j]);
+        atomicAdd(&A.N.p[0][n], apx[j]);
+        atomicAdd(&A.N.p[1][n], apz[j]);
+        atomicAdd(&A.N.f[0][n], afx[j]);
+        atomicAdd(&A.N.f[1][n], afz[j]);
+    }
+}
+
 // km_vmusl: mUSL nodal velocity v = p/m with Dirichlet masks (augm.jl:37-53)
 __global__ void km_vmusl(MCtx A) {
     EP_ACTIVE(A.ctl);
@@ -456,6 +795,23 @@ __device__ __forceinline__ void place_next(const MCtx& A, int p, int nxt) {
     if (c2 < 0) return;
     const int k = atomicAdd(&A.S.cursor[c2], 1);
     const int pos = A.S.start[nxt][c2] + k;
+    if (pos < A.S.start[nxt][c2 + 1]) {
+        A.S.list[nxt][pos] = p;
+        A.S.cellof[nxt][pos] = c2;
+    } else {
+        set_err(A.ctl, EP_ERR_CUDA, p);
+    }
+}
+
+// place_next for a whole warp: one cursor atomic per distinct cell (c2 < 0: nothing to place)
+__device__ __forceinline__ void place_next_warp(const MCtx& A, int p, int c2, int nxt, int lane) {
+    const unsigned mm = __match_any_sync(0xffffffffu, c2);
+    const int leader = __ffs(mm) - 1;
+    int base = 0;
+    if (lane == leader && c2 >= 0) base = atomicAdd(&A.S.cursor[c2], __popc(mm));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (c2 < 0) return;
+    const int pos = A.S.start[nxt][c2] + base + __popc(mm & ((1u << lane) - 1u));
     if (pos < A.S.start[nxt][c2 + 1]) {
         A.S.list[nxt][pos] = p;
         A.S.cellof[nxt][pos] = c2;
@@ -514,6 +870,58 @@ __global__ void __launch_bounds__(256) km_fbar(MCtx A) {
 #pragma unroll
     for (int j = 0; j < 4; ++j)
         if (nid[j] >= 0) atomicAdd(&A.N.dJacc[nid[j]], acc[j]);
+}
+
+// km_fbar_seg: δJ = det(I + dt ∇v) - 1 and its P2G Σ N m δJ (deform.jl:9-18,
+// volumetric.jl:1-11), one lane per point; places the points into the next lists
+template <int BASIS>
+__global__ void __launch_bounds__(256) km_fbar_seg(MCtx A) {
+    EP_ACTIVE(A.ctl);
+    const int cur = A.ctl->parity, nxt = cur ^ 1;
+    const int n = A.S.start[cur][A.g.ncell];
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    bool bad = false;
+    PtW W;
+    const bool live = point_of<BASIS>(A, cur, k, n, W, bad);
+    const Seg S = seg_of(W.c);
+    const float dtf = (float)A.ctl->dt;
+    float* const* vn = A.cf.musl ? A.N.vm : A.N.v;
+    const bool fin = A.cf.deform == EP_DEFORM_FINITE;
+    float mdj = 0.f;
+    if (live) {
+        float g00 = 0.f, g01 = 0.f, g10 = 0.f, g11 = 0.f;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            if (W.ax.cls[i] < 0) continue;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                if (W.az.cls[j] < 0) continue;
+                const int nd = node2(A.g, W.ax, W.az, i, j);
+                const float Nx = W.dwx[i] * W.wz[j], Nz = W.wx[i] * W.dwz[j];
+                const float vx = __ldg(&vn[0][nd]), vz = __ldg(&vn[1][nd]);
+                g00 += Nx * vx;
+                g01 += Nz * vx;
+                g10 += Nx * vz;
+                g11 += Nz * vz;
+            }
+        }
+        const float D00 = dtf * g00, D10 = dtf * g10, D01 = dtf * g01, D11 = dtf * g11;
+        const float dJ = D00 + D11 + (D00 * D11 - D01 * D10);
+        // numerator mass ρΩ after the deformation update: finite ρ0Ω0 (unchanged), infinitesimal
+        // ρ J Ω0 = m (1 + δJ), so the nodal sum carries m (1+δJ)^2 - m = m δJ (2 + δJ) (volumetric.jl:8)
+        mdj = A.P.mp[W.p] * (fin ? dJ : dJ * (2.f + dJ));
+    }
+    place_next_warp(A, live ? W.p : -1, live ? A.P.p2e_next[W.p] : -1, nxt, S.lane);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float v = seg_sum(live ? W.wx[i] * W.wz[j] * mdj : 0.f, S);
+            if (S.head && live && W.ax.cls[i] >= 0 && W.az.cls[j] >= 0)
+                atomicAdd(&A.N.dJacc[node2(A.g, W.ax, W.az, i, j)], v);
+        }
+    }
+    if (bad) set_err(A.ctl, EP_ERR_INVALID_POSITION, W.c);
 }
 
 // km_dJn: nodal δJ_n = Σ N m δJ / m_n (volumetric.jl:12-22, increment form)
@@ -1330,6 +1738,7 @@ static void mixed_step_impl(const MixedCtx& X, int phase, cudaStream_t s) {
     const MCtx& A = *(const MCtx*)X.impl;
     const int nc = A.g.ncell, nn = A.g.nnode, np = A.P.np;
     const int gq = (4 * nc + 255) / 256, gn = (nn + 255) / 256, gp = (np + 255) / 256;
+    const int gs = gp > 0 ? gp : 1;   // point-parallel transfers (an empty list still launches)
     Prof* pr = (X.prof && X.prof->on) ? X.prof : nullptr;
     auto mark = [&](const char* nm) {
         if (pr) pr->mark(nm, s);
@@ -1338,18 +1747,18 @@ static void mixed_step_impl(const MixedCtx& X, int phase, cudaStream_t s) {
     cudaMemsetAsync(X.grid_zero, 0, X.grid_zero_bytes, s);
     cudaMemsetAsync(X.sort_zero, 0, X.sort_zero_bytes, s);   // both parities' counts and the cursor
     mark("memset");
-    km_p2g<BASIS><<<gq, 256, 0, s>>>(A);
+    km_p2g_tile<BASIS><<<(nc + TP_CELLS - 1) / TP_CELLS, TP_THREADS, 0, s>>>(A);
     mark("p2g");
     km_solve<<<gn, 256, 0, s>>>(A);
     mark("solve");
-    km_g2p<BASIS><<<gq, 256, 0, s>>>(A);
+    km_g2p_seg<BASIS><<<gs, 256, 0, s>>>(A);
     mark("g2p");
     L += 3;
     if (A.cf.musl) { km_vmusl<<<gn, 256, 0, s>>>(A); mark("vmusl"); ++L; }
     L += mixed_scan(A, 0, X.scan_in, s);
     mark("scan");
     if (A.cf.locking) {
-        km_fbar<BASIS><<<gq, 256, 0, s>>>(A);
+        km_fbar_seg<BASIS><<<gs, 256, 0, s>>>(A);
         mark("fbar");
         km_dJn<<<gn, 256, 0, s>>>(A);
         mark("dJn");
