@@ -45,6 +45,7 @@ struct ep_handle {
     // fields the step never touches, kept on the host for download
     std::vector<double> u, pp, du, epV;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    cudaGraph_t graph_def[2] = {nullptr, nullptr};   // kept: a batch embeds it as a child graph
     long long graph_kernels[2] = {0, 0};
     long long launches = 0;
     int64_t steps = 0;
@@ -174,10 +175,19 @@ const char* epgpu_version(void) { return "epgpu 0.2 (sm_103a, FP64 oracle-order 
 
 const char* epgpu_last_error(const ep_handle* h) { return h ? h->err.c_str() : g_create_error.c_str(); }
 
+// the captured graphs hold the kernels' argument blocks by value: dropped whenever those change
+static void drop_graphs(ep_handle* h) {
+    for (int i = 0; i < 2; ++i) {
+        if (h->graph[i]) cudaGraphExecDestroy(h->graph[i]);
+        if (h->graph_def[i]) cudaGraphDestroy(h->graph_def[i]);
+        h->graph[i] = nullptr;
+        h->graph_def[i] = nullptr;
+    }
+}
+
 ep_status epgpu_destroy(ep_handle* h) {
     if (!h) return EP_ERR_ARG;
-    for (int i = 0; i < 2; ++i)
-        if (h->graph[i]) cudaGraphExecDestroy(h->graph[i]);
+    drop_graphs(h);
     if (h->s) cudaStreamSynchronize(h->s);
     for (void* p : h->allocs) cudaFree(p);
     if (h->hctl) cudaFreeHost(h->hctl);
@@ -525,6 +535,7 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
         mixed_ctx_init(h->mx_impl.data(), cf, g, h->ctl, pm, nm, sm, cmpr->Del, Cmp, cmpr->Kc, cmpr->Gc, cmpr->Hp,
                        cmpr->c, acc);
         h->mx.impl = h->mx_impl.data();
+        h->mx.p2g_tile = 64;
         h->mx.launches = &h->launches;
         h->mx.prof = nullptr;
     }
@@ -662,8 +673,11 @@ static ep_status build_graph(ep_handle* h, int phase) {
     h->launches = l0;                                                    // capturing launches nothing
     if (e != cudaSuccess) return cuda_fail(h, e, "graph capture");
     e = cudaGraphInstantiate(&h->graph[phase], gr, 0);
-    cudaGraphDestroy(gr);
-    if (e != cudaSuccess) return cuda_fail(h, e, "graph instantiate");
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(gr);
+        return cuda_fail(h, e, "graph instantiate");
+    }
+    h->graph_def[phase] = gr;
     return EP_OK;
 }
 
@@ -863,11 +877,7 @@ ep_status epgpu_set_return_map(ep_handle* h, ep_mlp* m, int32_t mode) {
     if (h->mixed) {
         mixed_set_rmap(h->mx_impl.data(), b);
         h->mx.net = mode == EP_RMAP_LEARNED ? m : nullptr;
-        for (int k = 0; k < 2; ++k)
-            if (h->graph[k]) {                        // the captured kernels hold the old argument block
-                cudaGraphExecDestroy(h->graph[k]);
-                h->graph[k] = nullptr;
-            }
+        drop_graphs(h);                               // the captured kernels hold the old argument block
     }
     h->rm_net = m;
     h->rm_mode = mode;
@@ -894,6 +904,287 @@ ep_status epgpu_return_map_stats(ep_handle* h, int64_t* learned, int64_t* fallba
         }
         *recorded = c;
     }
+    return EP_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Batched ensemble (no counterpart in the reference, which runs one slump per
+// process): independent instances, each with its own mesh, points, switches and
+// time loop, advanced together.  Every instance keeps its own device state and
+// 16-step graph; the batch graph holds those graphs as child nodes with no
+// dependencies between them, so one launch advances every instance by up to 16
+// of its own steps (instances past their window return at once), followed by one
+// kernel that gathers the instances' active / error words.
+__global__ void k_batch_flags(Ctl* const* ctls, int n, int* flags) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) flags[i] = (ctls[i]->active ? 1 : 0) | (ctls[i]->err ? 2 : 0);
+}
+
+struct ep_batch {
+    std::vector<ep_handle*> h;
+    cudaStream_t s = nullptr;
+    cudaGraphExec_t exec[2] = {nullptr, nullptr};
+    Ctl** dctl = nullptr;         // device array of the instances' control blocks
+    int* dflags = nullptr;
+    int* hflags = nullptr;        // pinned
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    double last_ms = 0.0;
+    long long launches = 0;
+    std::string err;
+};
+
+static ep_status bfail(ep_batch* b, ep_status st, const std::string& m) {
+    if (b) b->err = m;
+    else g_create_error = m;
+    return st;
+}
+#define BCK(b, call)                                                                   \
+    do {                                                                               \
+        cudaError_t e__ = (call);                                                      \
+        if (e__ != cudaSuccess) {                                                      \
+            cudaGetLastError();                                                        \
+            return bfail((b), EP_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e__)); \
+        }                                                                              \
+    } while (0)
+
+static void batch_drop(ep_batch* b) {
+    for (int k = 0; k < 2; ++k)
+        if (b->exec[k]) {
+            cudaGraphExecDestroy(b->exec[k]);
+            b->exec[k] = nullptr;
+        }
+}
+
+ep_status epgpu_batch_destroy(ep_batch* b) {
+    if (!b) return EP_ERR_ARG;
+    if (b->s) cudaStreamSynchronize(b->s);
+    batch_drop(b);
+    for (ep_handle* h : b->h) epgpu_destroy(h);
+    if (b->dctl) cudaFree(b->dctl);
+    if (b->dflags) cudaFree(b->dflags);
+    if (b->hflags) cudaFreeHost(b->hflags);
+    if (b->ev0) cudaEventDestroy(b->ev0);
+    if (b->ev1) cudaEventDestroy(b->ev1);
+    if (b->s) cudaStreamDestroy(b->s);
+    delete b;
+    return EP_OK;
+}
+
+ep_status epgpu_batch_create(int32_t n, const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_view* mesh,
+                             const int64_t* nmp, ep_batch** out) {
+    g_create_error.clear();
+    if (n <= 0 || !cfg || !cmpr || !mesh || !nmp || !out) return bfail(nullptr, EP_ERR_ARG, "null argument or n <= 0");
+    *out = nullptr;
+    ep_batch* b = new ep_batch();
+    for (int i = 0; i < n; ++i) {
+        ep_handle* h = nullptr;
+        ep_status st = epgpu_create(&cfg[i], &cmpr[i], &mesh[i], nmp[i], &h);
+        if (st != EP_OK) {
+            std::string m = "instance " + std::to_string(i) + ": " + g_create_error;
+            epgpu_batch_destroy(b);
+            return bfail(nullptr, st, m);
+        }
+        b->h.push_back(h);
+    }
+    std::vector<Ctl*> c(n);
+    for (int i = 0; i < n; ++i) c[i] = b->h[i]->ctl;
+    cudaError_t e = cudaStreamCreateWithFlags(&b->s, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&b->dctl, sizeof(Ctl*) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&b->dflags, sizeof(int) * n);
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&b->hflags, sizeof(int) * n);
+    if (e == cudaSuccess) e = cudaMemcpy(b->dctl, c.data(), sizeof(Ctl*) * n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaEventCreate(&b->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&b->ev1);
+    if (e != cudaSuccess) {
+        std::string m = std::string("batch create: ") + cudaGetErrorString(e);
+        cudaGetLastError();
+        epgpu_batch_destroy(b);
+        return bfail(nullptr, EP_ERR_CUDA, m);
+    }
+    *out = b;
+    return EP_OK;
+}
+
+const char* epgpu_batch_last_error(ep_batch* b) { return b ? b->err.c_str() : g_create_error.c_str(); }
+
+ep_handle* epgpu_batch_instance(ep_batch* b, int32_t i) {
+    if (!b || i < 0 || i >= (int)b->h.size()) return nullptr;
+    return b->h[i];
+}
+
+ep_status epgpu_batch_upload(ep_batch* b, int32_t i, const ep_mpts_view* m) {
+    if (!b || i < 0 || i >= (int)b->h.size()) return EP_ERR_ARG;
+    ep_status st = epgpu_upload(b->h[i], m);
+    if (st != EP_OK) return bfail(b, st, "instance " + std::to_string(i) + ": " + b->h[i]->err);
+    return EP_OK;
+}
+
+ep_status epgpu_batch_download(ep_batch* b, int32_t i, ep_mpts_view* m) {
+    if (!b || i < 0 || i >= (int)b->h.size()) return EP_ERR_ARG;
+    cudaStreamSynchronize(b->s);
+    ep_status st = epgpu_download(b->h[i], m);
+    if (st != EP_OK) return bfail(b, st, "instance " + std::to_string(i) + ": " + b->h[i]->err);
+    return EP_OK;
+}
+
+static ep_status batch_graph(ep_batch* b, int phase) {
+    if (b->exec[phase]) return EP_OK;
+    const int n = (int)b->h.size();
+    for (int i = 0; i < n; ++i) {
+        ep_status st = build_graph(b->h[i], phase);
+        if (st != EP_OK) return bfail(b, st, "instance " + std::to_string(i) + ": " + b->h[i]->err);
+    }
+    cudaGraph_t g;
+    BCK(b, cudaGraphCreate(&g, 0));
+    std::vector<cudaGraphNode_t> kids(n);
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < n && e == cudaSuccess; ++i)
+        e = cudaGraphAddChildGraphNode(&kids[i], g, nullptr, 0, b->h[i]->graph_def[phase]);
+    if (e == cudaSuccess) {
+        cudaKernelNodeParams kp{};
+        void* args[] = {(void*)&b->dctl, (void*)&n, (void*)&b->dflags};
+        kp.func = (void*)k_batch_flags;
+        kp.gridDim = dim3((n + 127) / 128);
+        kp.blockDim = dim3(128);
+        kp.sharedMemBytes = 0;
+        kp.kernelParams = args;
+        kp.extra = nullptr;
+        cudaGraphNode_t fl;
+        e = cudaGraphAddKernelNode(&fl, g, kids.data(), n, &kp);
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec[phase], g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return bfail(b, EP_ERR_CUDA, std::string("batch graph: ") + cudaGetErrorString(e));
+    }
+    return EP_OK;
+}
+
+ep_status epgpu_batch_run(ep_batch* b, int32_t phase, double T, double tg, double* t_inout, int64_t* nsteps_out) {
+    if (!b || !t_inout) return EP_ERR_ARG;
+    if (phase != 0 && phase != 1) return bfail(b, EP_ERR_ARG, "phase must be 0 or 1");
+    const int n = (int)b->h.size();
+    ep_status st;
+    for (int i = 0; i < n; ++i) {
+        ep_handle* h = b->h[i];
+        if (!h->uploaded) return bfail(b, EP_ERR_STATE, "instance " + std::to_string(i) + " not uploaded");
+        if ((st = read_ctl(h)) != EP_OK) return bfail(b, st, h->err);
+        if (h->hctl->err) {
+            kernel_error(h);
+            return bfail(b, (ep_status)h->hctl->err, "instance " + std::to_string(i) + ": " + h->err);
+        }
+        h->hctl->t = t_inout[i];
+        h->hctl->T = T;
+        h->hctl->tg = tg;
+        h->hctl->phase = phase;
+        h->hctl->active = 1;
+        h->hctl->nsteps = 0;
+        BCK(b, cudaMemcpyAsync(h->ctl, h->hctl, sizeof(Ctl), cudaMemcpyHostToDevice, h->s));
+    }
+    if ((st = batch_graph(b, phase)) != EP_OK) return st;
+    for (ep_handle* h : b->h) BCK(b, cudaStreamSynchronize(h->s));
+    BCK(b, cudaEventRecord(b->ev0, b->s));
+    long long launched = 0;
+    int failed = -1;
+    while (true) {
+        BCK(b, cudaGraphLaunch(b->exec[phase], b->s));
+        ++launched;
+        BCK(b, cudaMemcpyAsync(b->hflags, b->dflags, sizeof(int) * n, cudaMemcpyDeviceToHost, b->s));
+        BCK(b, cudaStreamSynchronize(b->s));
+        bool any = false;
+        for (int i = 0; i < n; ++i) {
+            if (b->hflags[i] & 2) failed = i;
+            if (b->hflags[i] & 1) any = true;
+        }
+        if (failed >= 0 || !any) break;
+        if (launched >= (1 << 24)) return bfail(b, EP_ERR_TIMEOUT, "batch time loop did not reach T");
+    }
+    BCK(b, cudaEventRecord(b->ev1, b->s));
+    BCK(b, cudaEventSynchronize(b->ev1));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, b->ev0, b->ev1);
+    b->last_ms = ms;
+    for (int i = 0; i < n; ++i) {
+        ep_handle* h = b->h[i];
+        if ((st = read_ctl(h)) != EP_OK) return bfail(b, st, h->err);
+        h->launches += launched * h->graph_kernels[phase];
+        h->t = h->hctl->t;
+        h->steps += h->hctl->nsteps;
+        t_inout[i] = h->hctl->t;
+        if (nsteps_out) nsteps_out[i] = h->hctl->nsteps;
+    }
+    b->launches += launched;
+    if (failed >= 0) {
+        ep_handle* h = b->h[failed];
+        st = kernel_error(h);
+        return bfail(b, st == EP_OK ? EP_ERR_CUDA : st, "instance " + std::to_string(failed) + ": " + h->err);
+    }
+    return EP_OK;
+}
+
+// Tile-shape autotuner: time steps of dt = 0 (positions, velocities and stresses do not
+// change; the lists are rebuilt with the same contents) of every instance with each P2G
+// tile shape, keep the fastest for all instances.
+ep_status epgpu_batch_autotune(ep_batch* b, int32_t phase, int32_t* tile_out, double* ms_out) {
+    if (!b || (phase != 0 && phase != 1)) return EP_ERR_ARG;
+    const int n = (int)b->h.size();
+    const int tiles[3] = {16, 32, 64};
+    double best = 1e300;
+    int pick = 64;
+    ep_status st;
+    for (int i = 0; i < n; ++i) {
+        ep_handle* h = b->h[i];
+        if (!h->mixed) return bfail(b, EP_ERR_UNSUPPORTED, "the tile autotuner is for the mixed-precision step");
+        if (h->rm_mode == EP_RMAP_LEARNED)
+            return bfail(b, EP_ERR_STATE, "autotune with the exact return map (the network's outputs move states)");
+        if ((st = read_ctl(h)) != EP_OK) return bfail(b, st, h->err);
+        h->hctl->dt = 0.0;
+        for (int k = 0; k < 3; ++k) h->hctl->g[k] = 0.0;
+        h->hctl->phase = phase;
+        BCK(b, cudaMemcpyAsync(h->ctl, h->hctl, sizeof(Ctl), cudaMemcpyHostToDevice, h->s));
+        BCK(b, cudaStreamSynchronize(h->s));
+    }
+    for (int c = 0; c < 3; ++c) {
+        for (int rep = 0; rep < 4; ++rep) {
+            if (rep == 1) BCK(b, cudaEventRecord(b->ev0, b->s));
+            for (ep_handle* h : b->h) {
+                MixedCtx mx = h->mx;
+                mx.p2g_tile = tiles[c];
+                mx.launches = nullptr;
+                mx.prof = nullptr;
+                launch_ctl_begin_step(h->ctl, h->dim, b->s);
+                mixed_step(mx, phase, b->s);
+            }
+        }
+        BCK(b, cudaEventRecord(b->ev1, b->s));
+        BCK(b, cudaEventSynchronize(b->ev1));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, b->ev0, b->ev1);
+        if (ms_out) ms_out[c] = ms / 3.0;
+        if (ms < best) {
+            best = ms;
+            pick = tiles[c];
+        }
+    }
+    for (ep_handle* h : b->h) {
+        if ((st = read_ctl(h)) != EP_OK) return bfail(b, st, h->err);
+        if (h->hctl->err) {
+            kernel_error(h);
+            return bfail(b, (ep_status)h->hctl->err, h->err);
+        }
+        h->mx.p2g_tile = pick;
+        drop_graphs(h);
+    }
+    batch_drop(b);
+    if (tile_out) *tile_out = pick;
+    return EP_OK;
+}
+
+ep_status epgpu_batch_stats(ep_batch* b, double* device_ms, int64_t* graph_launches) {
+    if (!b) return EP_ERR_ARG;
+    if (device_ms) *device_ms = b->last_ms;
+    if (graph_launches) *graph_launches = b->launches;
     return EP_OK;
 }
 

@@ -104,6 +104,7 @@ struct MixedCtx {
     int* scan_out;
     Prof* prof;
     long long* launches;
+    int p2g_tile;             // cells per CTA of the P2G kernel: 16, 32 or 64 (autotuned)
 };
 size_t mixed_ctx_size();
 void mixed_ctx_init(void* mem, const Cfg& cf, const Geo& g, Ctl* ctl, const PM& P, const NM& N, const SM& S,

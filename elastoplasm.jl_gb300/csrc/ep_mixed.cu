@@ -661,17 +661,19 @@ __global__ void __launch_bounds__(256) km_g2p_seg(MCtx A) {
     }
 }
 
-// km_p2g_tile: m, p, f (p2n.jl:135-155 std, 217-240 tpic).  A CTA owns 64
-// consecutive cells, whose points form one slice of the sorted list.  The slice
+// km_p2g_tile: m, p, f (p2n.jl:135-155 std, 217-240 tpic).  A CTA owns TP_CELLS
+// (16, 32 or 64: the tile shape the autotuner picks) consecutive cells, whose
+// points form one slice of the sorted list.  The slice
 // is staged through shared memory in chunks of one point per thread (point data
 // and shape values computed once per point), then four lanes per cell -- lane q
 // owns stencil column q -- accumulate the column's 4 nodes x 5 quantities in
 // registers over the cell's staged points, and add them to the grid with one
 // FP32 atomic per node and quantity.
-constexpr int TP_CELLS = 64, TP_THREADS = 256, TP_STRIDE = 29;   // floats per staged point (odd: no bank conflicts)
+constexpr int TP_STRIDE = 29;   // floats per staged point (odd: no bank conflicts)
 
-template <int BASIS>
-__global__ void __launch_bounds__(TP_THREADS) km_p2g_tile(MCtx A) {
+template <int BASIS, int TP_CELLS>
+__global__ void __launch_bounds__(4 * TP_CELLS) km_p2g_tile(MCtx A) {
+    constexpr int TP_THREADS = 4 * TP_CELLS;
     EP_ACTIVE(A.ctl);
     __shared__ float sp[TP_THREADS * TP_STRIDE];
     const int cur = A.ctl->parity;
@@ -1747,7 +1749,9 @@ static void mixed_step_impl(const MixedCtx& X, int phase, cudaStream_t s) {
     cudaMemsetAsync(X.grid_zero, 0, X.grid_zero_bytes, s);
     cudaMemsetAsync(X.sort_zero, 0, X.sort_zero_bytes, s);   // both parities' counts and the cursor
     mark("memset");
-    km_p2g_tile<BASIS><<<(nc + TP_CELLS - 1) / TP_CELLS, TP_THREADS, 0, s>>>(A);
+    if (X.p2g_tile == 16) km_p2g_tile<BASIS, 16><<<(nc + 15) / 16, 64, 0, s>>>(A);
+    else if (X.p2g_tile == 32) km_p2g_tile<BASIS, 32><<<(nc + 31) / 32, 128, 0, s>>>(A);
+    else km_p2g_tile<BASIS, 64><<<(nc + 63) / 64, 256, 0, s>>>(A);
     mark("p2g");
     km_solve<<<gn, 256, 0, s>>>(A);
     mark("solve");

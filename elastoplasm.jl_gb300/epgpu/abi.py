@@ -184,6 +184,16 @@ SIGNATURES = {
     "epgpu_mlp_recorded": (C.c_int, [C.c_void_p, _I64, _F, _F, C.c_int64]),
     "epgpu_set_return_map": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32]),
     "epgpu_selftest_wait_timeout": (C.c_int, [C.c_int64]),
+    "epgpu_batch_create": (C.c_int, [C.c_int32, C.POINTER(ep_cfg), C.POINTER(ep_cmpr), C.POINTER(ep_mesh_view),
+                                     _I64, C.POINTER(C.c_void_p)]),
+    "epgpu_batch_upload": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(ep_mpts_view)]),
+    "epgpu_batch_download": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(ep_mpts_view)]),
+    "epgpu_batch_run": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_double, _D, _I64]),
+    "epgpu_batch_autotune": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), _D]),
+    "epgpu_batch_stats": (C.c_int, [C.c_void_p, _D, _I64]),
+    "epgpu_batch_instance": (C.c_void_p, [C.c_void_p, C.c_int32]),
+    "epgpu_batch_last_error": (C.c_char_p, [C.c_void_p]),
+    "epgpu_batch_destroy": (C.c_int, [C.c_void_p]),
     "epgpu_grf_spectrum": (C.c_int, [C.POINTER(ep_grf), _D, _D]),
     "epgpu_grf_points": (C.c_int, [C.POINTER(ep_grf), _D, C.c_int64, _D]),
     "epgpu_return_map_stats": (C.c_int, [C.c_void_p, _I64, _I64, _I64]),

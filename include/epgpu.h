@@ -234,6 +234,34 @@ ep_status epgpu_bin_cells_noalloc(int32_t dim, const int64_t* nel, const double*
                                   const double* x_dev, int64_t nmp, int32_t* p2e_dev,
                                   int32_t* cell_start_dev, int32_t* cell_list_dev, void* stream);
 
+/* ---- Batched ensemble -----------------------------------------------------
+ * No counterpart in the reference (one slump per Julia process).  n independent
+ * instances -- each its own mesh, points, switches, material and time loop --
+ * advance together: every instance keeps its device state and its 16-step graph,
+ * and one launch of the batch graph (the instances' graphs as independent child
+ * nodes) advances each of them by up to 16 of its own CFL steps. */
+typedef struct ep_batch ep_batch;
+
+/* cfg, cmpr, mesh, nmp: arrays of n, one entry per instance (as epgpu_create). */
+ep_status epgpu_batch_create(int32_t n, const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_view* mesh,
+                             const int64_t* nmp, ep_batch** out);
+ep_status epgpu_batch_upload(ep_batch* b, int32_t i, const ep_mpts_view* m);
+ep_status epgpu_batch_download(ep_batch* b, int32_t i, ep_mpts_view* m);
+/* One checkpoint window of every instance's time loop (worflow.jl:27-44 /
+ * 73-85): instance i runs from t_inout[i] to T with its own dt; on return
+ * t_inout[i] = T (or where an error stopped it) and nsteps_out[i] its steps. */
+ep_status epgpu_batch_run(ep_batch* b, int32_t phase, double T, double tg, double* t_inout, int64_t* nsteps_out);
+/* Tile-shape autotuner of the mixed step: times dt = 0 steps (they leave the
+ * state unchanged) of all instances with P2G tiles of 16, 32 and 64 cells per
+ * CTA and keeps the fastest; ms_out (3) receives the mean batch-step time of each. */
+ep_status epgpu_batch_autotune(ep_batch* b, int32_t phase, int32_t* tile_out, double* ms_out);
+/* Device time of the last epgpu_batch_run and the batch-graph launches so far. */
+ep_status epgpu_batch_stats(ep_batch* b, double* device_ms, int64_t* graph_launches);
+/* The handle of instance i (epgpu_stats, epgpu_set_return_map, ...); owned by the batch. */
+ep_handle* epgpu_batch_instance(ep_batch* b, int32_t i);
+const char* epgpu_batch_last_error(ep_batch* b);
+ep_status epgpu_batch_destroy(ep_batch* b);
+
 /* ---- Learned return map --------------------------------------------------
  * No counterpart in the reference.  A 6 -> 128 x 4 (SiLU) -> 3 MLP, BF16
  * operands with FP32 accumulation on the tensor cores, that stands in for the

@@ -45,3 +45,13 @@ def test_create_rejects_bad_arguments_without_gpu():
                           C.byref(h))
     assert st == 2 and b"transfer" in lib.epgpu_last_error(None)
     assert lib.epgpu_destroy(None) == 1
+
+
+def test_batch_rejects_bad_arguments_without_gpu():
+    import ctypes as C
+    from epgpu import abi
+    lib = abi.load_library()
+    h = C.c_void_p()
+    assert lib.epgpu_batch_create(0, None, None, None, None, C.byref(h)) == 1
+    assert lib.epgpu_batch_destroy(None) == 1
+    assert lib.epgpu_batch_instance(None, 0) is None

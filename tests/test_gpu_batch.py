@@ -1,0 +1,76 @@
+"""The batched ensemble: instances advanced together match the same instances run one by
+one; the tile autotuner leaves the state unchanged."""
+import copy
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _instances():
+    from epgpu import ic_slump
+    out = []
+    for nx, ni, phi in ((40, 2, 20.0), (48, 2, 30.0), (40, 3, 25.0), (64, 2, 17.5)):
+        ic, cfg = ic_slump([64.1584, 16.0396], [nx, nx // 4], ni=ni, cmpr_over={"phi0": math.radians(phi)},
+                           nonloc={"status": False, "ls": 0.5})
+        instr = copy.deepcopy(cfg["instr"])
+        instr["gpu"] = {"precision": "mixed_df", "jaumann": False}
+        out.append((ic, instr))
+    return out
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def test_batch_matches_single_instances():
+    from epgpu import Engine
+    from epgpu.batch import Batch
+    inst = _instances()
+    b = Batch([copy.deepcopy(ic) for ic, _ in inst], [i for _, i in inst])
+    t, n0 = b.run(0, 1.0)
+    assert np.all(t == 1.0) and np.all(n0 > 0)
+    t, n1 = b.run(1, 1.5)
+    assert np.all(t == 1.5)
+    for k, (ic, instr) in enumerate(inst):
+        e = Engine(copy.deepcopy(ic), instr)
+        e.run(0, 1.0, 10.0, 0.0)
+        _, m1 = e.run(1, 1.5, 10.0, 1.0)
+        a, r = b.download(k), e.download()
+        s, d = _rel(a.tau, r.tau), _rel(a.x, r.x)
+        print(f"instance {k} ({ic['mpts'].nmp} points, {n0[k]}+{n1[k]} steps): stress {s:.2e} position {d:.2e}")
+        assert n1[k] == m1
+        assert s < 1e-4 and d < 1e-6
+    st = b.stats()
+    assert st["graph_launches"] > 0 and st["device_ms"] > 0
+
+
+def test_autotune_keeps_the_state():
+    from epgpu.batch import Batch
+    inst = _instances()
+    b = Batch([copy.deepcopy(ic) for ic, _ in inst], [i for _, i in inst])
+    b.run(0, 1.0)
+    before = [b.download(k) for k in range(b.n)]
+    tile, ms = b.autotune(phase=0)
+    print(f"autotune: tile {tile}, ms per batch step {ms}")
+    assert tile in (16, 32, 64) and all(v > 0 for v in ms.values())
+    for k in range(b.n):
+        a = b.download(k)
+        assert np.abs(a.x - before[k].x).max() == 0.0
+        assert _rel(a.tau, before[k].tau) < 1e-6
+    t, _ = b.run(0, 1.5)                       # the run continues with the chosen tile
+    assert np.all(t == 1.5)
+
+
+def test_batch_reports_instance_errors():
+    from epgpu import abi
+    from epgpu.batch import Batch
+    inst = _instances()[:2]
+    ics = [copy.deepcopy(ic) for ic, _ in inst]
+    ics[1]["mpts"].x[0, 5] = np.nan
+    b = Batch(ics, [i for _, i in inst])
+    with pytest.raises(abi.EPError) as ex:
+        b.run(0, 1.0)
+    assert "instance 1" in str(ex.value)
