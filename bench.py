@@ -300,6 +300,8 @@ def main():
     ap.add_argument("--train-iters", type=int, default=3000)
     ap.add_argument("--seed", type=int, default=5)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--deterministic", action="store_true",
+                    help="mixed step without floating-point atomics (bitwise reproducible)")
     ap.add_argument("--workload", default="c2", choices=["c2", "c4"],
                     help="c2: the nel=[640,160] slump (headline); c4: the batched ensemble")
     ap.add_argument("--instances", type=int, default=256)
@@ -321,7 +323,7 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     ic, cfg, field = make_workload()
-    cfg["instr"]["gpu"] = {"precision": args.precision, "jaumann": False}
+    cfg["instr"]["gpu"] = {"precision": args.precision, "jaumann": False, "deterministic": args.deterministic}
     mesh, mpts, cmpr = ic["mesh"], ic["mpts"], ic["cmpr"]
     np_, dim = mpts.nmp, mesh.dim
     g = [0.0] * (dim - 1) + [-9.81]
@@ -511,7 +513,8 @@ def main():
             + (" + bf16 MLP" if learned else ""),
             "data": f"synthetic slump geometry ({field})",
             "config": {"workload": WORKLOAD, "precision": args.precision,
-                       "return_map": "learned" if learned else "exact", "points": np_,
+                       "return_map": "learned" if learned else "exact", "deterministic": args.deterministic,
+                       "points": np_,
                        "nodes": mesh.nnodes, "l2": "flushed between timed steps (256 MB write)",
                        "parallelism": f"replicas x{ws}", "plastic_points_last_step": plastic,
                        "settle_s": args.settle},

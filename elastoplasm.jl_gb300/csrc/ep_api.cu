@@ -361,7 +361,7 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
     Cfg& cf = h->ctx.cf;
     cf.dim = d; cf.basis = cfg->basis; cf.how = cfg->how; cf.deform = cfg->deform; cf.trsfr = cfg->trsfr;
     cf.musl = cfg->musl; cf.locking = cfg->locking; cf.cons = cfg->constitutive; cf.nonloc = cfg->nonloc;
-    cf.jaumann = cfg->jaumann; cf.Cpf = cfg->C_pf; cf.damping = cfg->damping; cf.ls = cfg->nonloc_ls;
+    cf.jaumann = cfg->jaumann; cf.det = cfg->deterministic != 0; cf.Cpf = cfg->C_pf; cf.damping = cfg->damping; cf.ls = cfg->nonloc_ls;
     Mat& mt = h->ctx.mt;
     mt.Kc = cmpr->Kc; mt.Gc = cmpr->Gc; mt.Hp = cmpr->Hp; mt.c = cmpr->c;
     const int ns = h->nstr;
@@ -536,6 +536,14 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
                        cmpr->c, acc);
         h->mx.impl = h->mx_impl.data();
         h->mx.p2g_tile = 64;
+        if (cf.det) {
+            float *part = nullptr, *ptmp = nullptr;
+            if (dalloc(h, &part, (size_t)nc * 16 * 5) != cudaSuccess || dalloc(h, &ptmp, (size_t)np) != cudaSuccess) {
+                epgpu_destroy(h);
+                return fail(nullptr, EP_ERR_NOMEM, "device allocation (deterministic partials)");
+            }
+            mixed_set_det(h->mx_impl.data(), part, ptmp);
+        }
         h->mx.launches = &h->launches;
         h->mx.prof = nullptr;
     }

@@ -22,6 +22,7 @@ namespace ep {
 
 struct Cfg {
     int dim, basis, how, deform, trsfr, musl, locking, cons, nonloc, jaumann;
+    int det;            // mixed step without floating-point atomics
     double Cpf, damping, ls;
 };
 

@@ -123,6 +123,8 @@ struct RmapBufs {
     long long rec_cap;
 };
 void mixed_set_rmap(void* impl, const RmapBufs& b);
+// deterministic mode buffers: per-cell node partials (ncell x 16 x 5) and one float per point
+void mixed_set_det(void* impl, float* part, float* ptmp);
 // network kernels used by the step (ep_mlp.cu)
 void mlp_infer(ep_mlp* m, const float* X, const int* ndev, int cap, float* Y, cudaStream_t s);
 float* mlp_record_x(ep_mlp* m);

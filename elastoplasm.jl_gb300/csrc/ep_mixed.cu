@@ -37,6 +37,7 @@
 // quad never add to the same node and each keeps 4 nodes' sums in registers;
 // one FP32 atomic per node and quantity per cell goes to the grid.
 #include <climits>
+#include <type_traits>
 
 #include "../../include/epgpu.h"
 #include "ep_internal.h"
@@ -182,6 +183,9 @@ struct MCtx {
     long long* rec_count;
     long long rec_cap;
     double Deld[9], Cmpd[9], Kd, Gd;   // FP64 copies for the exact fallback
+    // deterministic mode: per-cell node partials (ncell x 16 x up to 5) and a per-point value
+    float* part;
+    float* ptmp;
 };
 
 __device__ __forceinline__ int node2(const Geo& g, const Axis4& ax, const Axis4& az, int i, int j) {
@@ -577,7 +581,7 @@ __global__ void __launch_bounds__(256) km_p2g_seg(MCtx A) {
 
 // km_g2p_seg: PIC/FLIP (n2p.jl:14-40), new cell + offset, vmax, next-cell counts
 // (tplgy.jl:43-62) and the mUSL momentum P2G (augm.jl:13-25), one lane per point
-template <int BASIS>
+template <int BASIS, bool DET>
 __global__ void __launch_bounds__(256) km_g2p_seg(MCtx A) {
     EP_ACTIVE(A.ctl);
     const int cur = A.ctl->parity, nxt = cur ^ 1;
@@ -636,7 +640,7 @@ __global__ void __launch_bounds__(256) km_g2p_seg(MCtx A) {
         const unsigned mm = __match_any_sync(0xffffffffu, c2);
         if (c2 >= 0 && S.lane == __ffs(mm) - 1) atomicAdd(&A.S.count[nxt][c2], __popc(mm));
     }
-    if (A.cf.musl) {
+    if (A.cf.musl && !DET) {
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
 #pragma unroll
@@ -671,7 +675,7 @@ __global__ void __launch_bounds__(256) km_g2p_seg(MCtx A) {
 // FP32 atomic per node and quantity.
 constexpr int TP_STRIDE = 29;   // floats per staged point (odd: no bank conflicts)
 
-template <int BASIS, int TP_CELLS>
+template <int BASIS, int TP_CELLS, bool DET>
 __global__ void __launch_bounds__(4 * TP_CELLS) km_p2g_tile(MCtx A) {
     constexpr int TP_THREADS = 4 * TP_CELLS;
     EP_ACTIVE(A.ctl);
@@ -763,6 +767,15 @@ __global__ void __launch_bounds__(4 * TP_CELLS) km_p2g_tile(MCtx A) {
     }
     if (bad) set_err(A.ctl, EP_ERR_INVALID_POSITION, c0);
     if (!cell_ok || pb == pe) return;
+    if (DET) {
+        // the cell's partial sums, node (q, j) of its stencil; km_gather adds them in a fixed order
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            float* o = A.part + ((size_t)cl * 16 + q * 4 + j) * 5;
+            o[0] = am[j]; o[1] = apx[j]; o[2] = apz[j]; o[3] = afx[j]; o[4] = afz[j];
+        }
+        return;
+    }
     const int ex = cl / A.g.nel[1], ez = cl - ex * A.g.nel[1];
     const Axis4 ax = axis4(A.g, 0, ex), az = axis4(A.g, 1, ez);
     if (ax.cls[q] < 0) return;
@@ -775,6 +788,127 @@ __global__ void __launch_bounds__(4 * TP_CELLS) km_p2g_tile(MCtx A) {
         atomicAdd(&A.N.p[1][n], apz[j]);
         atomicAdd(&A.N.f[0][n], afx[j]);
         atomicAdd(&A.N.f[1][n], afz[j]);
+    }
+}
+
+// Deterministic scatters of the mUSL momentum (KIND 1: m v per point, augm.jl:13-25) and of
+// Σ N m δJ (KIND 2: the per-point value left in ptmp by km_fbar_seg, volumetric.jl:1-11): the
+// tile staging of km_p2g_tile, each cell's points summed in list (point id) order into the
+// cell's node partials.
+template <int BASIS, int TP_CELLS, int KIND>
+__global__ void __launch_bounds__(4 * TP_CELLS) km_aux_tile(MCtx A) {
+    constexpr int TP_THREADS = 4 * TP_CELLS, NQ = KIND == 1 ? 2 : 1, ST = 11;
+    EP_ACTIVE(A.ctl);
+    __shared__ float sp[TP_THREADS * ST];
+    const int cur = A.ctl->parity;
+    const int c0 = blockIdx.x * TP_CELLS;
+    if (c0 >= A.g.ncell) return;
+    const int c1 = min(c0 + TP_CELLS, A.g.ncell);
+    const int* start = A.S.start[cur];
+    const int b0 = start[c0], b1 = start[c1];
+    if (b0 == b1) return;
+    const int t = threadIdx.x;
+    const int q = t & 3, cl = c0 + (t >> 2);
+    const bool cell_ok = cl < c1;
+    const int pb = cell_ok ? start[cl] : 0, pe = cell_ok ? start[cl + 1] : 0;
+    const float hx = (float)A.g.h[0], hz = (float)A.g.h[1];
+    float acc[4][NQ];
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int v = 0; v < NQ; ++v) acc[j][v] = 0.f;
+    bool bad = false;
+    for (int ch = b0; ch < b1; ch += TP_THREADS) {
+        const int k = ch + t;
+        if (k < b1) {
+            const int p = A.S.list[cur][k], c = A.S.cellof[cur][k];
+            const int ex = c / A.g.nel[1], ez = c - ex * A.g.nel[1];
+            const Axis4 ax = axis4(A.g, 0, ex), az = axis4(A.g, 1, ez);
+            const float lx = BASIS == EP_BASIS_GIMPM ? A.P.l[0][p] : 0.f;
+            const float lz = BASIS == EP_BASIS_GIMPM ? A.P.l[1][p] : 0.f;
+            float* s = sp + t * ST;
+            float dw[4];
+            axis_w<BASIS>(ax, A.P.dx[cur][0][p], hx, 1.f / hx, lx, s + 0, dw, bad);
+            axis_w<BASIS>(az, A.P.dx[cur][1][p], hz, 1.f / hz, lz, s + 4, dw, bad);
+            if (KIND == 1) {
+                const float mp = A.P.mp[p];
+                s[8] = mp * A.P.v[0][p];
+                s[9] = mp * A.P.v[1][p];
+            } else {
+                s[8] = A.ptmp[p];
+            }
+        }
+        __syncthreads();
+        const int lo = max(pb, ch), hi = min(pe, min(ch + TP_THREADS, b1));
+        for (int kk = lo; kk < hi; ++kk) {
+            const float* s = sp + (kk - ch) * ST;
+            const float wq = s[q];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const float N = wq * s[4 + j];
+#pragma unroll
+                for (int v = 0; v < NQ; ++v) acc[j][v] += N * s[8 + v];
+            }
+        }
+        __syncthreads();
+    }
+    if (bad) set_err(A.ctl, EP_ERR_INVALID_POSITION, c0);
+    if (!cell_ok || pb == pe) return;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int v = 0; v < NQ; ++v) A.part[((size_t)cl * 16 + q * 4 + j) * NQ + v] = acc[j][v];
+}
+
+// node sums of the per-cell partials: the cells whose stencil holds node (ix, jz) are
+// ex = ix + 1 - q, ez = jz + 1 - r (q, r = 0..3), visited in that fixed order
+template <int NQ>
+__global__ void km_gather(MCtx A, float* o0, float* o1, float* o2, float* o3, float* o4) {
+    EP_ACTIVE(A.ctl);
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= A.g.nnode) return;
+    const int cur = A.ctl->parity;
+    const int nz = A.g.nno[1], ix = n / nz, jz = n - ix * nz;
+    const int* start = A.S.start[cur];
+    float acc[NQ];
+#pragma unroll
+    for (int v = 0; v < NQ; ++v) acc[v] = 0.f;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int ex = ix + 1 - q;
+        if (ex < 0 || ex >= A.g.nel[0]) continue;
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const int ez = jz + 1 - r;
+            if (ez < 0 || ez >= A.g.nel[1]) continue;
+            const int c = ez + A.g.nel[1] * ex;
+            if (start[c] == start[c + 1]) continue;
+            const float* pp = A.part + ((size_t)c * 16 + q * 4 + r) * NQ;
+#pragma unroll
+            for (int v = 0; v < NQ; ++v) acc[v] += pp[v];
+        }
+    }
+    float* outs[5] = {o0, o1, o2, o3, o4};
+#pragma unroll
+    for (int v = 0; v < NQ; ++v) outs[v][n] = acc[v];
+}
+
+// point ids of each cell's list segment in ascending order (deterministic summation order)
+__global__ void km_sort_cells(MCtx A, int which) {
+    if (which == 0 && !A.ctl->active) return;
+    const int par = which == 0 ? (A.ctl->parity ^ 1) : A.ctl->parity;
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= A.g.ncell) return;
+    int* L = A.S.list[par];
+    const int b = A.S.start[par][c], e = A.S.start[par][c + 1];
+    for (int i = b + 1; i < e; ++i) {
+        const int v = L[i];
+        int j = i - 1;
+        while (j >= b && L[j] > v) {
+            L[j + 1] = L[j];
+            --j;
+        }
+        L[j + 1] = v;
     }
 }
 
@@ -876,7 +1010,7 @@ __global__ void __launch_bounds__(256) km_fbar(MCtx A) {
 
 // km_fbar_seg: δJ = det(I + dt ∇v) - 1 and its P2G Σ N m δJ (deform.jl:9-18,
 // volumetric.jl:1-11), one lane per point; places the points into the next lists
-template <int BASIS>
+template <int BASIS, bool DET>
 __global__ void __launch_bounds__(256) km_fbar_seg(MCtx A) {
     EP_ACTIVE(A.ctl);
     const int cur = A.ctl->parity, nxt = cur ^ 1;
@@ -914,6 +1048,11 @@ __global__ void __launch_bounds__(256) km_fbar_seg(MCtx A) {
         mdj = A.P.mp[W.p] * (fin ? dJ : dJ * (2.f + dJ));
     }
     place_next_warp(A, live ? W.p : -1, live ? A.P.p2e_next[W.p] : -1, nxt, S.lane);
+    if (DET) {
+        if (live) A.ptmp[W.p] = mdj;             // km_aux_tile<.., 2> scatters it
+        if (bad) set_err(A.ctl, EP_ERR_INVALID_POSITION, W.c);
+        return;
+    }
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
 #pragma unroll
@@ -1735,34 +1874,67 @@ __global__ void km_export_nodes(MCtx A, N64 Q) {
 }
 
 // ---------------------------------------------------------------------------
-template <int BASIS, int ACC>
+template <int BASIS, int TC, int KIND>
+static void launch_tile(const MCtx& A, cudaStream_t s) {
+    const int nc = A.g.ncell;
+    if (KIND == 0) km_p2g_tile<BASIS, TC, true><<<(nc + TC - 1) / TC, 4 * TC, 0, s>>>(A);
+    else km_aux_tile<BASIS, TC, KIND><<<(nc + TC - 1) / TC, 4 * TC, 0, s>>>(A);
+}
+
+// one step of the mixed path; DET = no floating-point atomics (per-cell partials + node gathers)
+template <int BASIS, int ACC, bool DET>
 static void mixed_step_impl(const MixedCtx& X, int phase, cudaStream_t s) {
     const MCtx& A = *(const MCtx*)X.impl;
     const int nc = A.g.ncell, nn = A.g.nnode, np = A.P.np;
-    const int gq = (4 * nc + 255) / 256, gn = (nn + 255) / 256, gp = (np + 255) / 256;
+    const int gn = (nn + 255) / 256, gp = (np + 255) / 256, gc = (nc + 255) / 256;
     const int gs = gp > 0 ? gp : 1;   // point-parallel transfers (an empty list still launches)
     Prof* pr = (X.prof && X.prof->on) ? X.prof : nullptr;
     auto mark = [&](const char* nm) {
         if (pr) pr->mark(nm, s);
     };
+    auto tile = [&](auto kind) {
+        constexpr int K = decltype(kind)::value;
+        if (X.p2g_tile == 16) launch_tile<BASIS, 16, K>(A, s);
+        else if (X.p2g_tile == 32) launch_tile<BASIS, 32, K>(A, s);
+        else launch_tile<BASIS, 64, K>(A, s);
+    };
     long long L = 0;
     cudaMemsetAsync(X.grid_zero, 0, X.grid_zero_bytes, s);
     cudaMemsetAsync(X.sort_zero, 0, X.sort_zero_bytes, s);   // both parities' counts and the cursor
     mark("memset");
-    if (X.p2g_tile == 16) km_p2g_tile<BASIS, 16><<<(nc + 15) / 16, 64, 0, s>>>(A);
-    else if (X.p2g_tile == 32) km_p2g_tile<BASIS, 32><<<(nc + 31) / 32, 128, 0, s>>>(A);
-    else km_p2g_tile<BASIS, 64><<<(nc + 63) / 64, 256, 0, s>>>(A);
+    if (DET) {
+        tile(std::integral_constant<int, 0>());
+        km_gather<5><<<gn, 256, 0, s>>>(A, A.N.m, A.N.p[0], A.N.p[1], A.N.f[0], A.N.f[1]);
+        L += 1;
+    } else if (X.p2g_tile == 16) km_p2g_tile<BASIS, 16, false><<<(nc + 15) / 16, 64, 0, s>>>(A);
+    else if (X.p2g_tile == 32) km_p2g_tile<BASIS, 32, false><<<(nc + 31) / 32, 128, 0, s>>>(A);
+    else km_p2g_tile<BASIS, 64, false><<<(nc + 63) / 64, 256, 0, s>>>(A);
     mark("p2g");
     km_solve<<<gn, 256, 0, s>>>(A);
     mark("solve");
-    km_g2p_seg<BASIS><<<gs, 256, 0, s>>>(A);
+    km_g2p_seg<BASIS, DET><<<gs, 256, 0, s>>>(A);
     mark("g2p");
     L += 3;
-    if (A.cf.musl) { km_vmusl<<<gn, 256, 0, s>>>(A); mark("vmusl"); ++L; }
+    if (A.cf.musl) {
+        if (DET) {
+            tile(std::integral_constant<int, 1>());
+            km_gather<2><<<gn, 256, 0, s>>>(A, A.N.pm[0], A.N.pm[1], nullptr, nullptr, nullptr);
+            mark("musl");
+            L += 2;
+        }
+        km_vmusl<<<gn, 256, 0, s>>>(A);
+        mark("vmusl");
+        ++L;
+    }
     L += mixed_scan(A, 0, X.scan_in, s);
     mark("scan");
     if (A.cf.locking) {
-        km_fbar_seg<BASIS><<<gs, 256, 0, s>>>(A);
+        km_fbar_seg<BASIS, DET><<<gs, 256, 0, s>>>(A);
+        if (DET) {
+            tile(std::integral_constant<int, 2>());
+            km_gather<1><<<gn, 256, 0, s>>>(A, A.N.dJacc, nullptr, nullptr, nullptr, nullptr);
+            L += 2;
+        }
         mark("fbar");
         km_dJn<<<gn, 256, 0, s>>>(A);
         mark("dJn");
@@ -1782,24 +1954,34 @@ static void mixed_step_impl(const MixedCtx& X, int phase, cudaStream_t s) {
             L += 3;
         }
     }
+    if (DET) {
+        km_sort_cells<<<gc, 256, 0, s>>>(A, 0);   // the next step's lists in point-id order
+        mark("sort");
+        ++L;
+    }
     const bool lrn = A.rmode == EP_RMAP_LEARNED;
     km_flip<<<1, 1, 0, s>>>(A.ctl, lrn ? A.rcount : nullptr, lrn ? A.fbcount : nullptr);
     ++L;
     if (X.launches) *X.launches += L;
 }
 
-template <int ACC>
+template <int ACC, bool DET>
 static void mixed_step_acc(const MixedCtx& X, int phase, cudaStream_t s) {
     const MCtx& A = *(const MCtx*)X.impl;
-    if (A.cf.basis == EP_BASIS_BSMPM) mixed_step_impl<EP_BASIS_BSMPM, ACC>(X, phase, s);
-    else if (A.cf.basis == EP_BASIS_GIMPM) mixed_step_impl<EP_BASIS_GIMPM, ACC>(X, phase, s);
-    else mixed_step_impl<EP_BASIS_SMPM, ACC>(X, phase, s);
+    if (A.cf.basis == EP_BASIS_BSMPM) mixed_step_impl<EP_BASIS_BSMPM, ACC, DET>(X, phase, s);
+    else if (A.cf.basis == EP_BASIS_GIMPM) mixed_step_impl<EP_BASIS_GIMPM, ACC, DET>(X, phase, s);
+    else mixed_step_impl<EP_BASIS_SMPM, ACC, DET>(X, phase, s);
 }
 
 void mixed_step(const MixedCtx& X, int phase, cudaStream_t s) {
     const MCtx& A = *(const MCtx*)X.impl;
-    if (A.acc == 0) mixed_step_acc<0>(X, phase, s);
-    else mixed_step_acc<1>(X, phase, s);
+    if (A.cf.det) {
+        if (A.acc == 0) mixed_step_acc<0, true>(X, phase, s);
+        else mixed_step_acc<1, true>(X, phase, s);
+    } else {
+        if (A.acc == 0) mixed_step_acc<0, false>(X, phase, s);
+        else mixed_step_acc<1, false>(X, phase, s);
+    }
 }
 
 void launch_mixed_scan(const MixedCtx& X, cudaStream_t s) { mixed_scan(*(const MCtx*)X.impl, 0, X.scan_in, s); }
@@ -1815,6 +1997,7 @@ void mixed_import(const MixedCtx& X, const P64& Q, cudaStream_t s) {
     if (np > 0) km_bin0<<<(np + 255) / 256, 256, 0, s>>>(A, Q);
     mixed_initial_scan(X, s);
     if (np > 0) km_place0<<<(np + 255) / 256, 256, 0, s>>>(A);
+    if (A.cf.det) km_sort_cells<<<(A.g.ncell + 255) / 256, 256, 0, s>>>(A, 1);
 }
 
 void mixed_export(const MixedCtx& X, const P64& Q, const N64& QN, cudaStream_t s) {
@@ -1858,6 +2041,14 @@ void mixed_ctx_init(void* mem, const Cfg& cf, const Geo& g, Ctl* ctl, const PM& 
     A->fbcount = A->fblist = nullptr;
     A->rec_count = nullptr;
     A->rec_cap = 0;
+    A->part = nullptr;
+    A->ptmp = nullptr;
+}
+
+void mixed_set_det(void* mem, float* part, float* ptmp) {
+    MCtx* A = (MCtx*)mem;
+    A->part = part;
+    A->ptmp = ptmp;
 }
 
 void mixed_set_rmap(void* mem, const RmapBufs& b) {

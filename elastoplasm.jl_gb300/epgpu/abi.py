@@ -29,7 +29,7 @@ class ep_cfg(C.Structure):
                 ("deform", C.c_int32), ("trsfr", C.c_int32), ("C_pf", C.c_double), ("musl", C.c_int32),
                 ("locking", C.c_int32), ("damping", C.c_double), ("constitutive", C.c_int32),
                 ("nonloc", C.c_int32), ("nonloc_ls", C.c_double), ("precision", C.c_int32),
-                ("jaumann", C.c_int32)]
+                ("jaumann", C.c_int32), ("deterministic", C.c_int32)]
 
 
 class ep_cmpr(C.Structure):

@@ -37,7 +37,7 @@ def require(what: str = "instr") -> dict:
         "plot": {"status": True, "freq": 1.0, "what": ["epII"], "dims": (500.0, 250.0)},
         "perf": {"status": False},
         # GB300 build switches (absent from the reference; defaults keep its behaviour)
-        "gpu": {"precision": "fp64", "jaumann": False},
+        "gpu": {"precision": "fp64", "jaumann": False, "deterministic": False},
     }
 
 
@@ -129,4 +129,5 @@ def to_abi(instr: dict) -> dict:
         "nonloc_ls": float(instr["nonloc"]["ls"]),
         "precision": PRECISION[prec],
         "jaumann": int(bool(gpu.get("jaumann", False))),
+        "deterministic": int(bool(gpu.get("deterministic", False))),
     }

@@ -79,6 +79,10 @@ typedef struct ep_cfg {
     int32_t precision;     /* EP_PREC_FP64 (drop-in, oracle order) | EP_PREC_MIXED | EP_PREC_MIXED_DF */
     int32_t jaumann;       /* 0: reference rate (its spin term is identically zero,
                               elast.jl:77); 1: objective Jaumann rate (not the reference) */
+    int32_t deterministic; /* mixed precisions: 1 = no floating-point atomics (each cell's points
+                              summed in point-id order into per-cell node partials, nodes
+                              summing their cells in a fixed order): bitwise reproducible runs.
+                              The FP64 step is always deterministic. */
 } ep_cfg;
 
 /* Material constants: the `cmpr` NamedTuple of setup_cmpr (setup_cmpr.jl:120-143). */

@@ -123,3 +123,59 @@ def test_mixed_nonfinite_reported(precision):
     with pytest.raises(EPError) as ex:
         e.step(0, 0.02, [0.0, -9.81])
     assert ex.value.status == 3
+
+
+def _det(instr, precision="mixed_df"):
+    instr = copy.deepcopy(instr)
+    instr["gpu"] = {"precision": precision, "jaumann": False, "deterministic": True}
+    return instr
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("deform,trsfr,musl,locking", [("finite", "std", True, True), ("infinitesimal", "tpic", False, True),
+                                                       ("finite", "std", True, False)])
+def test_deterministic_mode_is_bitwise_reproducible(oracle_mod, precision, deform, trsfr, musl, locking):
+    """No floating-point atomics: two runs give identical bits, and the run stays within the
+    mixed-precision tolerance of the FP64 oracle."""
+    from epgpu import Engine, ic_slump
+    fw = {"deform": deform, "trsfr": trsfr, "C_pf": 1.0, "musl": musl, "locking": locking, "damping": 0.1}
+    ic, cfg = ic_slump(*C1, fwrk=fw, nonloc={"status": False, "ls": 0.5})
+    x0 = ic["mpts"].x.copy()
+    outs = []
+    for _ in range(2):
+        e = Engine(copy.deepcopy(ic), _det(cfg["instr"], precision))
+        _run_engine(e, ((0, 1.0), (1, 1.5)))
+        outs.append(e.download())
+        e.close()
+    a, b = outs
+    for f in ("x", "v", "tau", "Fij", "bij", "epII"):
+        assert np.array_equal(np.asarray(getattr(a, f)), np.asarray(getattr(b, f))), f
+    o = oracle_mod.Oracle(copy.deepcopy(ic), cfg["instr"])
+    _run_engine(o, ((0, 1.0), (1, 1.5)))
+    s, d, r = errors(a, o.download(), x0)
+    print(f"deterministic {precision} {deform}/{trsfr}/musl={musl}/locking={locking}: stress {s:.3e} displacement {d:.3e}")
+    assert s < STRESS_TOL and d < DISP_TOL
+
+
+def test_deterministic_all_in_one_reproducible(oracle_mod):
+    from epgpu import ic_slump, slump
+    ic, cfg = ic_slump(*C1, nonloc={"status": False, "ls": 0.5})
+    x0 = ic["mpts"].x.copy()
+    cm = copy.deepcopy(cfg)
+    cm["instr"] = _det(cfg["instr"])
+    a = slump(ic, cm, workflow="all-in-one")
+    b = slump(ic, cm, workflow="all-in-one")
+    assert a["steps"] == b["steps"]
+    assert np.array_equal(a["ic"]["mpts"].tau, b["ic"]["mpts"].tau)
+    assert np.array_equal(a["ic"]["mpts"].x, b["ic"]["mpts"].x)
+    out_o = slump(ic, cfg, workflow="all-in-one", engine_factory=lambda p, q: oracle_mod.Oracle(p, q))
+    s, d, r = errors(a["ic"]["mpts"], out_o["ic"]["mpts"], x0)
+    print(f"deterministic all-in-one ({a['steps']} steps): stress {s:.3e} displacement {d:.3e} runout {r:.3e}")
+    assert s < 1e-2 and d < 1e-2
+
+
+def _run_engine(e, windows):
+    t = 0.0
+    for phase, T in windows:
+        t, _ = e.run(phase, T, 10.0, t)
+    return t
