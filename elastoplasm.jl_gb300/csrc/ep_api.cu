@@ -222,8 +222,11 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
     }
     if (cfg->precision != EP_PREC_FP64 && cfg->precision != EP_PREC_MIXED && cfg->precision != EP_PREC_MIXED_DF)
         return fail(nullptr, EP_ERR_UNSUPPORTED, "unknown precision");
-    if (cfg->precision != EP_PREC_FP64 && d != 2)
-        return fail(nullptr, EP_ERR_UNSUPPORTED, "the mixed-precision step is built for 2d; use EP_PREC_FP64 in 3d");
+    if (cfg->precision != EP_PREC_FP64 && d == 3 && cfg->deform == EP_DEFORM_FINITE)
+        return fail(nullptr, EP_ERR_UNSUPPORTED,
+                    "the mixed-precision 3d step is built for infinitesimal strain; use EP_PREC_FP64 for finite strain in 3d");
+    if (cfg->precision != EP_PREC_FP64 && d == 3 && cfg->deterministic)
+        return fail(nullptr, EP_ERR_UNSUPPORTED, "the deterministic mode is built for the 2d mixed step");
     if (cfg->precision != EP_PREC_FP64 && cfg->nonloc)
         return fail(nullptr, EP_ERR_UNSUPPORTED, "nonlocal averaging is built in the FP64 step only");
     if (cfg->nonloc && !(cfg->nonloc_ls > 0.0)) return fail(nullptr, EP_ERR_ARG, "nonloc.ls must be > 0");
@@ -448,14 +451,15 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
         NM nm{};
         SM sm{};
         pm.np = np;
-        // accumulated state: F (d*d), b (3), ep1 as FP64 or as FP32 pairs
-        const size_t nacc = (size_t)(d * d + 3 + 1);
+        // accumulated state: F (d*d), b (3 | 6), ep1 as FP64 or as FP32 pairs
+        const int nsym = d == 2 ? 3 : 6;
+        const size_t nacc = (size_t)(d * d + nsym + 1);
         double* pd = nullptr;
         float* pf = nullptr;
         bool ok2 = true;
         if (acc == 0) ok2 = dalloc(h, &pd, nacc * np) == cudaSuccess;
-        // floats: dx[2][d], v[d], tau[3], 11 scalars, rho, l[d], dv[d*d], (pairs: 2*nacc)
-        const size_t nflt = (size_t)np * (2 * d + d + 3 + 11 + 1 + d + d * d + (acc ? 2 * nacc : 0));
+        // floats: dx[2][d], v[d], tau[nsym], 11 scalars, rho, l[d], dv[d*d], (pairs: 2*nacc)
+        const size_t nflt = (size_t)np * (2 * d + d + nsym + 11 + 1 + d + d * d + (acc ? 2 * nacc : 0));
         ok2 = ok2 && dalloc(h, &pf, nflt) == cudaSuccess;
         int* ints = nullptr;
         const size_t nint = (size_t)3 * nc + 2 * (size_t)(nc + 1) + 4 * (size_t)np + (size_t)np + 2 * (size_t)(nc + 1);
@@ -472,7 +476,7 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
         for (int par = 0; par < 2; ++par)
             for (int i = 0; i < d; ++i) pm.dx[par][i] = take(1);
         for (int i = 0; i < d; ++i) pm.v[i] = take(1);
-        for (int k = 0; k < 3; ++k) pm.tau[k] = take(1);
+        for (int k = 0; k < nsym; ++k) pm.tau[k] = take(1);
         pm.ep2 = take(1); pm.dlam = take(1); pm.c0 = take(1); pm.cr = take(1); pm.tphi = take(1);
         pm.sphi = take(1); pm.cphi = take(1); pm.mp = take(1); pm.Om0 = take(1); pm.Om = take(1);
         take(1);   // spare
@@ -483,12 +487,12 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
             double* q = pd;
             for (int k = 0; k < d * d; ++k) pm.Fd[k] = q + (size_t)k * np;
             q += (size_t)d * d * np;
-            for (int k = 0; k < 3; ++k) pm.bd[k] = q + (size_t)k * np;
-            q += (size_t)3 * np;
+            for (int k = 0; k < nsym; ++k) pm.bd[k] = q + (size_t)k * np;
+            q += (size_t)nsym * np;
             pm.ep1d = q;
         } else {
             for (int k = 0; k < d * d; ++k) { pm.Fh[k] = take(1); pm.Fl[k] = take(1); }
-            for (int k = 0; k < 3; ++k) { pm.bh[k] = take(1); pm.bl[k] = take(1); }
+            for (int k = 0; k < nsym; ++k) { pm.bh[k] = take(1); pm.bl[k] = take(1); }
             pm.ep1h = take(1);
             pm.ep1l = take(1);
         }
@@ -521,15 +525,17 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
         h->mx.grid_zero_bytes = sizeof(float) * (size_t)(1 + 2 * d) * nn;   // m, p, f
         h->mx.sort_zero = sort_zero;
         h->mx.sort_zero_bytes = sizeof(int) * (size_t)3 * nc;
-        // compliance (inverse of the 3x3 Del) for ε = Del \\ τ
-        double Cmp[9], LU[9], e[3], x[3];
-        int piv[3];
-        for (int i = 0; i < 9; ++i) LU[i] = cmpr->Del[i];
-        lu_factor<3>(LU, piv);
-        for (int j = 0; j < 3; ++j) {
-            for (int i = 0; i < 3; ++i) e[i] = (i == j) ? 1.0 : 0.0;
-            lu_solve<3>(LU, piv, e, x);
-            for (int i = 0; i < 3; ++i) Cmp[i + 3 * j] = x[i];
+        // compliance (inverse of the nstr x nstr Del) for ε = Del \\ τ
+        double Cmp[36], LU[36], e[6], x[6];
+        int piv[6];
+        for (int i = 0; i < nsym * nsym; ++i) LU[i] = cmpr->Del[i];
+        if (nsym == 3) lu_factor<3>(LU, piv);
+        else lu_factor<6>(LU, piv);
+        for (int j = 0; j < nsym; ++j) {
+            for (int i = 0; i < nsym; ++i) e[i] = (i == j) ? 1.0 : 0.0;
+            if (nsym == 3) lu_solve<3>(LU, piv, e, x);
+            else lu_solve<6>(LU, piv, e, x);
+            for (int i = 0; i < nsym; ++i) Cmp[i + nsym * j] = x[i];
         }
         h->mx_impl.resize(mixed_ctx_size());
         mixed_ctx_init(h->mx_impl.data(), cf, g, h->ctl, pm, nm, sm, cmpr->Del, Cmp, cmpr->Kc, cmpr->Gc, cmpr->Hp,

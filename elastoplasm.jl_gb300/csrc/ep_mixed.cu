@@ -160,6 +160,24 @@ __device__ __forceinline__ void axis_w(const Axis4& a, float dloc, float h, floa
     }
 }
 
+// GIMP weight the stencil loses to nodes outside the grid along one direction (GIMP
+// and the linear hat sum to one on the full line; the B-spline boundary pieces sum to one
+// inside the mesh): the F-bar average Σ N ΔJ_n runs over the existing nodes only
+// (volumetric.jl:23-36), so Σ N - 1 = Π_d (1 - miss_d) - 1 enters its increment form
+template <int BASIS>
+__device__ __forceinline__ float axis_miss(const Axis4& a, float dloc, float h, float lp) {
+    float m = 0.f;
+    if (BASIS != EP_BASIS_GIMPM) return m;
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        if (a.cls[k] < 0) {
+            float f, df;
+            gimp32(dloc + h * (float)(1 - k), h, lp, f, df);
+            m += f;
+        }
+    return m;
+}
+
 struct MCtx {
     Cfg cf;
     Geo g;
@@ -167,8 +185,8 @@ struct MCtx {
     PM P;
     NM N;
     SM S;
-    float Del[9];       // FP32 copy of the 3x3 stiffness (2d)
-    float Cmp[9];       // its inverse (compliance), FP32
+    float Del[36];      // FP32 copy of the nstr x nstr stiffness (3x3 in 2d, 6x6 in 3d), column-major
+    float Cmp[36];      // its inverse (compliance), FP32
     float Kc, Gc, Hp;
     double c;           // wave speed
     int acc;            // 0: FP64 accumulators, 1: double-float accumulators
@@ -182,7 +200,7 @@ struct MCtx {
     int* fblist;
     long long* rec_count;
     long long rec_cap;
-    double Deld[9], Cmpd[9], Kd, Gd;   // FP64 copies for the exact fallback
+    double Deld[36], Cmpd[36], Kd, Gd;   // FP64 copies for the exact fallback
     // deterministic mode: per-cell node partials (ncell x 16 x up to 5) and a per-point value
     float* part;
     float* ptmp;
@@ -308,33 +326,35 @@ __global__ void __launch_bounds__(256) km_p2g(MCtx A) {
     }
 }
 
-// km_solve: grid momentum update with damping and Dirichlet masks (solve.jl:14-40)
+// km_solve: grid momentum update with damping and Dirichlet masks (solve.jl:14-40), 2d and 3d
 __global__ void km_solve(MCtx A) {
     EP_ACTIVE(A.ctl);
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= A.g.nnode) return;
+    const int D = A.g.dim;
     const float dt = (float)A.ctl->dt, eta = (float)A.cf.damping;
     const float m = A.N.m[n];
-    float a[2] = {0.f, 0.f}, v[2] = {0.f, 0.f};
+    float a[3] = {0.f, 0.f, 0.f}, v[3] = {0.f, 0.f, 0.f}, f[3] = {0.f, 0.f, 0.f};
     if (m != 0.f) {
-        float f[2] = {A.N.f[0][n], A.N.f[1][n]};
-        const float pm[2] = {A.N.p[0][n], A.N.p[1][n]};
+        float pm[3] = {0.f, 0.f, 0.f};
+        for (int d = 0; d < D; ++d) {
+            f[d] = A.N.f[d][n];
+            pm[d] = A.N.p[d][n];
+        }
         const float mi = 1.f / m;
-#pragma unroll
-        for (int d = 0; d < 2; ++d) {
+        for (int d = 0; d < D; ++d) {
             if (A.g.bcs[(size_t)d * A.g.nnode + n]) continue;
-            const float nrm = sqrtf(f[0] * f[0] + f[1] * f[1]);
+            // the norm sees the components damped so far (solve.jl:29)
+            const float nrm = sqrtf(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);
             const float pv = pm[d] * mi;
             const float sg = pv > 0.f ? 1.f : (pv < 0.f ? -1.f : 0.f);
             if (fabsf(pv) >= 1.0e-3f) f[d] -= eta * nrm * sg;
             a[d] = f[d] * mi;
             v[d] = (pm[d] + dt * f[d]) * mi;
         }
-        A.N.f[0][n] = f[0];
-        A.N.f[1][n] = f[1];
+        for (int d = 0; d < D; ++d) A.N.f[d][n] = f[d];
     }
-#pragma unroll
-    for (int d = 0; d < 2; ++d) {
+    for (int d = 0; d < D; ++d) {
         A.N.a[d][n] = a[d];
         A.N.v[d][n] = v[d];
         A.N.pm[d][n] = 0.f;
@@ -918,8 +938,7 @@ __global__ void km_vmusl(MCtx A) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= A.g.nnode) return;
     const float m = A.N.m[n];
-#pragma unroll
-    for (int d = 0; d < 2; ++d) {
+    for (int d = 0; d < A.g.dim; ++d) {
         float v = 0.f;
         if (m != 0.f && !A.g.bcs[(size_t)d * A.g.nnode + n]) v = A.N.pm[d][n] * (1.f / m);
         A.N.vm[d][n] = v;
@@ -1050,16 +1069,15 @@ __global__ void __launch_bounds__(256) km_fbar_seg(MCtx A) {
     place_next_warp(A, live ? W.p : -1, live ? A.P.p2e_next[W.p] : -1, nxt, S.lane);
     if (DET) {
         if (live) A.ptmp[W.p] = mdj;             // km_aux_tile<.., 2> scatters it
-        if (bad) set_err(A.ctl, EP_ERR_INVALID_POSITION, W.c);
-        return;
-    }
+    } else {
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
+        for (int i = 0; i < 4; ++i) {
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const float v = seg_sum(live ? W.wx[i] * W.wz[j] * mdj : 0.f, S);
-            if (S.head && live && W.ax.cls[i] >= 0 && W.az.cls[j] >= 0)
-                atomicAdd(&A.N.dJacc[node2(A.g, W.ax, W.az, i, j)], v);
+            for (int j = 0; j < 4; ++j) {
+                const float v = seg_sum(live ? W.wx[i] * W.wz[j] * mdj : 0.f, S);
+                if (S.head && live && W.ax.cls[i] >= 0 && W.az.cls[j] >= 0)
+                    atomicAdd(&A.N.dJacc[node2(A.g, W.ax, W.az, i, j)], v);
+            }
         }
     }
     if (bad) set_err(A.ctl, EP_ERR_INVALID_POSITION, W.c);
@@ -1121,7 +1139,7 @@ __device__ __forceinline__ int j232(float* s, float ep2, float c0, float cr, flo
     float f = yield(s, kap, n);
     if (!(f > 0.f)) return 0;
     float g0 = ep2;
-    for (int it = 1; fabsf(f) > 1.0e-9f && it < 20; ++it) {
+    for (int it = 1; fabsf(f) > fmaxf(1.0e-9f, 2.0e-7f * kap) && it < 20; ++it) {
         float row[3];
         for (int j = 0; j < 3; ++j) row[j] = n[0] * D[3 * j] + n[1] * D[1 + 3 * j] + n[2] * D[2 + 3 * j];
         const float dl = f / (row[0] * n[0] + row[1] * n[1] + row[2] * n[2]);
@@ -1328,8 +1346,14 @@ __global__ void __launch_bounds__(256) km_cons(MCtx A, int plastic_phase) {
         }
         // F-bar: ΔF <- (ΔJ̄/ΔJ)^(1/2) ΔF, ΔJ̄ = Σ N ΔJ_n (volumetric.jl:23-36), increment form
         if (lock) {
+            float sm1 = 0.f;      // Σ N - 1 over the existing nodes (GIMP next to a mesh edge)
+            if (BASIS == EP_BASIS_GIMPM) {
+                const float mx = axis_miss<BASIS>(ax, A.P.dx[cur][0][p], hx, A.P.l[0][p]);
+                const float mz = axis_miss<BASIS>(az, A.P.dx[cur][1][p], hz, A.P.l[1][p]);
+                sm1 = -(mx + mz) + mx * mz;
+            }
             const float dJp = D[0] + D[3] + (D[0] * D[3] - D[2] * D[1]);
-            const float r1 = (a - dJp) / (1.f + dJp);          // ΔJ̄/ΔJ - 1
+            const float r1 = (sm1 + a - dJp) / (1.f + dJp);    // ΔJ̄/ΔJ - 1
             const float s1 = r1 / (1.f + sqrtf(1.f + r1));     // sqrt(1 + r1) - 1
             D[0] = D[0] * (1.f + s1) + s1;
             D[1] = D[1] * (1.f + s1);
@@ -1734,26 +1758,51 @@ static int mixed_scan(const MCtx& A, int which, int* bsum, cudaStream_t s) {
 // ---------------------------------------------------------------------------
 // import / export between the FP64 staging layout (P64: the reference's
 // arrays as SoA) and the mixed state
+// cell index of per-direction element indices: 2d ez + nz ex (tplgy.jl:49), 3d ez + nz ex + nz nx ey (tplgy.jl:82)
+__device__ __forceinline__ int cell_of(const Geo& g, const int* e) {
+    return g.dim == 2 ? e[1] + g.nel[1] * e[0] : e[2] + g.nel[2] * e[0] + g.nel[2] * g.nel[0] * e[1];
+}
+__device__ __forceinline__ void cell_dec(const Geo& g, int c, int* e) {
+    if (g.dim == 2) {
+        e[0] = c / g.nel[1];
+        e[1] = c - e[0] * g.nel[1];
+    } else {
+        const int nzx = g.nel[2] * g.nel[0];
+        e[1] = c / nzx;
+        const int r = c - e[1] * nzx;
+        e[0] = r / g.nel[2];
+        e[2] = r - e[0] * g.nel[2];
+    }
+}
+
+// symmetric storage of b: 2d (11, 22, 12), 3d Voigt (11, 22, 33, 23, 13, 12); Q.b is column-major D x D
+__device__ __forceinline__ int sym_i(int D, int k) { return D == 2 ? (k == 2 ? 0 : k) : (k < 3 ? k : (k == 3 ? 1 : 0)); }
+__device__ __forceinline__ int sym_j(int D, int k) { return D == 2 ? (k == 2 ? 1 : k) : (k < 3 ? k : (k == 5 ? 1 : 2)); }
+
 __global__ void km_import(MCtx A, P64 Q) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= A.P.np) return;
-    for (int d = 0; d < 2; ++d) {
+    const int D = A.g.dim, NS = D == 2 ? 3 : 6;
+    for (int d = 0; d < D; ++d) {
         A.P.v[d][p] = (float)Q.v[d][p];
         if (A.cf.basis == EP_BASIS_GIMPM) A.P.l[d][p] = (float)Q.l[d][p];
     }
-    const double b12 = 0.5 * (Q.b[2][p] + Q.b[1][p]);
-    const double bsym[3] = {Q.b[0][p], Q.b[3][p], b12};
+    double bsym[6];
+    for (int k = 0; k < NS; ++k) {
+        const int i = sym_i(D, k), j = sym_j(D, k);
+        bsym[k] = 0.5 * (Q.b[i + D * j][p] + Q.b[j + D * i][p]);
+    }
     if (A.acc == 0) {
-        for (int k = 0; k < 4; ++k) A.P.Fd[k][p] = Q.F[k][p];
-        for (int k = 0; k < 3; ++k) A.P.bd[k][p] = bsym[k];
+        for (int k = 0; k < D * D; ++k) A.P.Fd[k][p] = Q.F[k][p];
+        for (int k = 0; k < NS; ++k) A.P.bd[k][p] = bsym[k];
         A.P.ep1d[p] = Q.ep1[p];
     } else {
-        for (int k = 0; k < 4; ++k) {
+        for (int k = 0; k < D * D; ++k) {
             const float h = (float)Q.F[k][p];
             A.P.Fh[k][p] = h;
             A.P.Fl[k][p] = (float)(Q.F[k][p] - (double)h);
         }
-        for (int k = 0; k < 3; ++k) {
+        for (int k = 0; k < NS; ++k) {
             const float h = (float)bsym[k];
             A.P.bh[k][p] = h;
             A.P.bl[k][p] = (float)(bsym[k] - (double)h);
@@ -1763,9 +1812,9 @@ __global__ void km_import(MCtx A, P64 Q) {
         A.P.ep1l[p] = (float)(Q.ep1[p] - (double)h);
     }
     if (A.cf.trsfr == EP_TRSFR_TPIC)
-        for (int k = 0; k < 4; ++k) A.P.dv[k][p] = (float)Q.dv[k][p];
+        for (int k = 0; k < D * D; ++k) A.P.dv[k][p] = (float)Q.dv[k][p];
     const bool fin = A.cf.deform == EP_DEFORM_FINITE;
-    for (int k = 0; k < 3; ++k) A.P.tau[k][p] = (float)(fin ? Q.tau[k][p] : Q.sig[k][p]);
+    for (int k = 0; k < NS; ++k) A.P.tau[k][p] = (float)(fin ? Q.tau[k][p] : Q.sig[k][p]);
     A.P.ep2[p] = (float)Q.ep2[p];
     A.P.dlam[p] = (float)Q.dlam[p];
     A.P.c0[p] = (float)Q.c0[p];
@@ -1783,15 +1832,21 @@ __global__ void km_import(MCtx A, P64 Q) {
 __global__ void km_bin0(MCtx A, P64 Q) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= A.P.np) return;
-    const int cur = A.ctl->parity;
-    const double x = Q.x[0][p], z = Q.x[1][p];
+    const int cur = A.ctl->parity, D = A.g.dim;
     int c2 = -1;
-    if (isfinite(x) && isfinite(z)) {
-        const int ex = (int)fmin(fmax(floor((x - A.g.x0[0]) / A.g.h[0]), 0.0), (double)(A.g.nel[0] - 1));
-        const int ez = (int)fmin(fmax(floor((z - A.g.x0[1]) / A.g.h[1]), 0.0), (double)(A.g.nel[1] - 1));
-        c2 = ez + A.g.nel[1] * ex;
-        A.P.dx[cur][0][p] = (float)(x - A.g.ax[0][ex]);
-        A.P.dx[cur][1][p] = (float)(z - A.g.ax[1][ez]);
+    bool fin = true;
+    double x[3];
+    for (int d = 0; d < D; ++d) {
+        x[d] = Q.x[d][p];
+        fin = fin && isfinite(x[d]);
+    }
+    if (fin) {
+        int e[3];
+        for (int d = 0; d < D; ++d) {
+            e[d] = (int)fmin(fmax(floor((x[d] - A.g.x0[d]) / A.g.h[d]), 0.0), (double)(A.g.nel[d] - 1));
+            A.P.dx[cur][d][p] = (float)(x[d] - A.g.ax[d][e[d]]);
+        }
+        c2 = cell_of(A.g, e);
         atomicAdd(&A.S.count[cur][c2], 1);
     } else {
         set_err(A.ctl, EP_ERR_NONFINITE, p);
@@ -1808,34 +1863,37 @@ __global__ void km_place0(MCtx A) {
 __global__ void km_export(MCtx A, P64 Q) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= A.P.np) return;
-    const int cur = A.ctl->parity;
+    const int cur = A.ctl->parity, D = A.g.dim, NS = D == 2 ? 3 : 6;
     const int c = A.P.p2e_next[p];
     Q.p2e[p] = c;
     if (c >= 0) {
-        const int ex = c / A.g.nel[1], ez = c - ex * A.g.nel[1];
-        Q.x[0][p] = A.g.ax[0][ex] + (double)A.P.dx[cur][0][p];
-        Q.x[1][p] = A.g.ax[1][ez] + (double)A.P.dx[cur][1][p];
+        int e[3];
+        cell_dec(A.g, c, e);
+        for (int d = 0; d < D; ++d) Q.x[d][p] = A.g.ax[d][e[d]] + (double)A.P.dx[cur][d][p];
     }
-    for (int d = 0; d < 2; ++d) {
+    for (int d = 0; d < D; ++d) {
         Q.v[d][p] = (double)A.P.v[d][p];
         if (A.cf.basis == EP_BASIS_GIMPM) Q.l[d][p] = (double)A.P.l[d][p];
     }
-    double F[4], B[3], e1;
+    double F[9], B[6], e1;
     if (A.acc == 0) {
-        for (int k = 0; k < 4; ++k) F[k] = A.P.Fd[k][p];
-        for (int k = 0; k < 3; ++k) B[k] = A.P.bd[k][p];
+        for (int k = 0; k < D * D; ++k) F[k] = A.P.Fd[k][p];
+        for (int k = 0; k < NS; ++k) B[k] = A.P.bd[k][p];
         e1 = A.P.ep1d[p];
     } else {
-        for (int k = 0; k < 4; ++k) F[k] = (double)A.P.Fh[k][p] + (double)A.P.Fl[k][p];
-        for (int k = 0; k < 3; ++k) B[k] = (double)A.P.bh[k][p] + (double)A.P.bl[k][p];
+        for (int k = 0; k < D * D; ++k) F[k] = (double)A.P.Fh[k][p] + (double)A.P.Fl[k][p];
+        for (int k = 0; k < NS; ++k) B[k] = (double)A.P.bh[k][p] + (double)A.P.bl[k][p];
         e1 = (double)A.P.ep1h[p] + (double)A.P.ep1l[p];
     }
-    for (int k = 0; k < 4; ++k) Q.F[k][p] = F[k];
-    const double J = F[0] * F[3] - F[2] * F[1];
+    for (int k = 0; k < D * D; ++k) Q.F[k][p] = F[k];
+    const double J = D == 2 ? F[0] * F[3] - F[2] * F[1]
+                            : F[0] * (F[4] * F[8] - F[7] * F[5]) - F[3] * (F[1] * F[8] - F[7] * F[2]) +
+                                  F[6] * (F[1] * F[5] - F[4] * F[2]);
     Q.J[p] = J;
     Q.Om[p] = J * Q.Om0[p];
     const bool fin = A.cf.deform == EP_DEFORM_FINITE;
     if (fin) {
+        // finite strain (2d): b, τ, σ = τ / J and ϵ = ½ log b (FP64, for output)
         Q.rho[p] = Q.rho0[p] / J;
         Q.n[p] = 1.0 - 1.0 / J * (1.0 - Q.n0[p]);
         Q.b[0][p] = B[0]; Q.b[3][p] = B[1]; Q.b[1][p] = B[2]; Q.b[2][p] = B[2];
@@ -1843,7 +1901,6 @@ __global__ void km_export(MCtx A, P64 Q) {
             Q.tau[k][p] = (double)A.P.tau[k][p];
             Q.sig[k][p] = (double)A.P.tau[k][p] / J;
         }
-        // ϵ = ½ log b (FP64, for output)
         double lam[2], V[4], L[2], R[4];
         eig_sym2(B[0], B[2], B[1], lam, V);
         L[0] = ep_log(lam[0]);
@@ -1851,10 +1908,10 @@ __global__ void km_export(MCtx A, P64 Q) {
         vdvt<2>(V, L, R);
         for (int k = 0; k < 4; ++k) Q.eps[k][p] = 0.5 * R[k];
     } else {
-        for (int k = 0; k < 3; ++k) Q.sig[k][p] = (double)A.P.tau[k][p];
+        for (int k = 0; k < NS; ++k) Q.sig[k][p] = (double)A.P.tau[k][p];
     }
     if (A.cf.trsfr == EP_TRSFR_TPIC)
-        for (int k = 0; k < 4; ++k) Q.dv[k][p] = (double)A.P.dv[k][p];
+        for (int k = 0; k < D * D; ++k) Q.dv[k][p] = (double)A.P.dv[k][p];
     Q.ep1[p] = e1;
     Q.ep2[p] = A.cf.nonloc ? (double)A.P.ep2[p] : e1;
     Q.dlam[p] = (double)A.P.dlam[p];
@@ -1864,13 +1921,604 @@ __global__ void km_export_nodes(MCtx A, N64 Q) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= A.g.nnode) return;
     Q.m[n] = A.N.m[n];
-    for (int d = 0; d < 2; ++d) {
+    for (int d = 0; d < A.g.dim; ++d) {
         Q.p[d][n] = A.cf.musl ? A.N.pm[d][n] : A.N.p[d][n];
         Q.v[d][n] = A.cf.musl ? A.N.vm[d][n] : A.N.v[d][n];
         Q.a[d][n] = A.N.a[d][n];
         Q.oobf[d][n] = A.N.f[d][n];
     }
     Q.dJ[n] = 1.0 + (double)A.N.dJn[n];
+}
+
+// ===========================================================================
+// 3d mixed step (infinitesimal strain: config 3's GIMP / TPIC / J2 and the DP
+// variants).  Node id iz + nno_z ix + nno_z nno_x iy, cell ez + nz ex + nz nx ey
+// (get_coords.jl:36-52, tplgy.jl:82); Voigt order (xx, yy, zz, yz, xz, xy).
+__device__ __forceinline__ int node3(const Geo& g, const Axis4& ax, const Axis4& ay, const Axis4& az, int i, int j,
+                                     int k) {
+    return (az.base + k) + g.nno[2] * (ax.base + i) + g.nno[2] * g.nno[0] * (ay.base + j);
+}
+
+// FP32 J2 return in 3d (J2.jl:21-76 restated as in ep_scalar.h); the iteration stops at
+// |f| <= max(1e-9, 2e-7 kappa), the resolution of an FP32 stress
+__device__ __forceinline__ int j2f6(float* s, float ep2, float c0, float cr, float Hp, const float* D, float* g) {
+    auto yield = [&](const float* v, float kap, float* n) {
+        const float P = (v[0] + v[1] + v[2]) * (1.f / 3.f);
+        float x[6];
+        for (int i = 0; i < 3; ++i) x[i] = v[i] - P;
+        for (int i = 3; i < 6; ++i) x[i] = v[i];
+        const float j2 = 0.5f * (x[0] * x[0] + x[1] * x[1] + x[2] * x[2] + 2.f * (x[3] * x[3] + x[4] * x[4] + x[5] * x[5]));
+        const float xn = sqrtf(2.f * j2);
+        for (int i = 0; i < 6; ++i) n[i] = x[i] / xn;
+        return xn - kap;
+    };
+    float kap = fmaxf(cr, c0 + Hp * ep2), n[6];
+    float f = yield(s, kap, n);
+    if (!(f > 0.f)) return 0;
+    float g0 = ep2;
+    for (int it = 1; fabsf(f) > fmaxf(1.0e-9f, 2.0e-7f * kap) && it < 20; ++it) {
+        float row[6];
+        for (int j = 0; j < 6; ++j) {
+            float a = 0.f;
+            for (int i = 0; i < 6; ++i) a += n[i] * D[i + 6 * j];
+            row[j] = a;
+        }
+        float den = 0.f;
+        for (int j = 0; j < 6; ++j) den += row[j] * n[j];
+        const float dl = f / den;
+        for (int i = 0; i < 6; ++i) {
+            float a = 0.f;
+            for (int j = 0; j < 6; ++j) a += D[i + 6 * j] * n[j];
+            s[i] -= dl * a;
+        }
+        g0 += dl;
+        kap = fmaxf(cr, c0 + Hp * g0);
+        f = yield(s, kap, n);
+    }
+    *g = g0;
+    return 1;
+}
+
+// FP32 Drucker-Prager in 3d (DP.jl:33-98, outer cone DP.jl:19-21, ψ = 0); returns Δλ
+__device__ __forceinline__ float dpf6(float* s, float ep2, float c0, float cr, float sphi, float cphi, float Kc,
+                                      float Gc, float Hp, float* dep) {
+    float coh = c0 + Hp * ep2;
+    if (coh < cr) coh = cr;
+    const float P = (s[0] + s[1] + s[2]) * (1.f / 3.f);
+    float t[6];
+    for (int i = 0; i < 3; ++i) t[i] = s[i] - P;
+    for (int i = 3; i < 6; ++i) t[i] = s[i];
+    const float tII = sqrtf(0.5f * (t[0] * t[0] + t[1] * t[1] + t[2] * t[2]) + t[3] * t[3] + t[4] * t[4] + t[5] * t[5]);
+    const float sq3 = 1.7320508075688772f;
+    const float eta = 6.f * sphi / (sq3 * (3.f + sphi)), xi = 6.f * coh * cphi / (sq3 * (3.f + sphi));
+    const float sm = xi / eta, tP = xi - eta * sm;
+    const float fs = tII + eta * P - xi;
+    const float h = tII - tP - sqrtf(1.f + eta * eta) * (P - sm);
+    float dl = 0.f;
+    *dep = 0.f;
+    if ((fs > 0.f && P < sm) || (h > 0.f && P >= sm)) {
+        dl = fs / Gc;
+        const float r = (xi - eta * P) / tII;
+        for (int i = 0; i < 6; ++i) s[i] = t[i] * r + (i < 3 ? P : 0.f);
+        *dep = dl * 0.57735026918962576f;
+    }
+    if (h <= 0.f && P >= sm) {
+        dl = (P - sm) / Kc;
+        const float Pn = sm - P, r = 0.f / tII;
+        for (int i = 0; i < 6; ++i) s[i] = t[i] * r + (i < 3 ? Pn : 0.f);
+        *dep = 1.41421356237309505f * dl / 3.f;
+    }
+    return dl;
+}
+
+// det(I + D) - 1 of a 3x3 increment, without cancellation: tr D + principal minors + det D
+__device__ __forceinline__ float det1p_m1(const float* D) {
+    const float m2 = (D[0] * D[4] - D[3] * D[1]) + (D[0] * D[8] - D[6] * D[2]) + (D[4] * D[8] - D[7] * D[5]);
+    const float d3 = D[0] * (D[4] * D[8] - D[7] * D[5]) - D[3] * (D[1] * D[8] - D[7] * D[2]) +
+                     D[6] * (D[1] * D[5] - D[4] * D[2]);
+    return (D[0] + D[4] + D[8]) + m2 + d3;
+}
+
+struct PtW3 {
+    int p, c, e[3];
+    Axis4 a[3];
+    float w[3][4], dw[3][4];
+    float o[3];
+};
+
+template <int BASIS>
+__device__ __forceinline__ bool point3(const MCtx& A, int cur, int k, int n, PtW3& W, bool& bad) {
+    if (k >= n) {
+        W.p = -1;
+        W.c = -1;
+        return false;
+    }
+    W.p = A.S.list[cur][k];
+    W.c = A.S.cellof[cur][k];
+    cell_dec(A.g, W.c, W.e);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        W.a[d] = axis4(A.g, d, W.e[d]);
+        const float h = (float)A.g.h[d];
+        W.o[d] = A.P.dx[cur][d][W.p];
+        const float l = BASIS == EP_BASIS_GIMPM ? A.P.l[d][W.p] : 0.f;
+        axis_w<BASIS>(W.a[d], W.o[d], h, 1.f / h, l, W.w[d], W.dw[d], bad);
+    }
+    return true;
+}
+
+// km_p2g_tile3: m, p, f in 3d (p2n.jl:58-102 std, 140-191 tpic).  TC cells per CTA; 16 lanes per
+// cell, lane (qx, qy) owns the stencil column of 4 z-nodes
+constexpr int TP3_STRIDE = 47;
+
+template <int BASIS, int TC>
+__global__ void __launch_bounds__(16 * TC) km_p2g_tile3(MCtx A) {
+    constexpr int TH = 16 * TC;
+    EP_ACTIVE(A.ctl);
+    __shared__ float sp[TH * TP3_STRIDE];
+    const int cur = A.ctl->parity;
+    const int c0 = blockIdx.x * TC;
+    if (c0 >= A.g.ncell) return;
+    const int c1 = min(c0 + TC, A.g.ncell);
+    const int* start = A.S.start[cur];
+    const int b0 = start[c0], b1 = start[c1];
+    if (b0 == b1) return;
+    const int t = threadIdx.x;
+    const int l16 = t & 15, qx = l16 & 3, qy = l16 >> 2, cl = c0 + (t >> 4);
+    const bool cell_ok = cl < c1;
+    const int pb = cell_ok ? start[cl] : 0, pe = cell_ok ? start[cl + 1] : 0;
+    const float hx = (float)A.g.h[0], hy = (float)A.g.h[1], hz = (float)A.g.h[2];
+    const float gz = (float)A.ctl->g[2];
+    const bool tpic = A.cf.trsfr == EP_TRSFR_TPIC;
+    float am[4], ap[3][4], af[3][4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        am[j] = 0.f;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) ap[d][j] = af[d][j] = 0.f;
+    }
+    bool bad = false;
+    for (int ch = b0; ch < b1; ch += TH) {
+        const int k = ch + t;
+        if (k < b1) {
+            const int p = A.S.list[cur][k], c = A.S.cellof[cur][k];
+            int e[3];
+            cell_dec(A.g, c, e);
+            float* s = sp + t * TP3_STRIDE;
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                const Axis4 ax = axis4(A.g, d, e[d]);
+                const float h = (float)A.g.h[d];
+                const float o = A.P.dx[cur][d][p];
+                const float l = BASIS == EP_BASIS_GIMPM ? A.P.l[d][p] : 0.f;
+                axis_w<BASIS>(ax, o, h, 1.f / h, l, s + 8 * d, s + 8 * d + 4, bad);
+                if (tpic) s[34 + d] = o;
+            }
+            const float sc = A.P.Om[p];                    // infinitesimal: Ω σ
+            s[24] = A.P.mp[p];
+            s[25] = A.P.v[0][p];
+            s[26] = A.P.v[1][p];
+            s[27] = A.P.v[2][p];
+#pragma unroll
+            for (int v = 0; v < 6; ++v) s[28 + v] = sc * A.P.tau[v][p];
+            if (tpic)
+#pragma unroll
+                for (int v = 0; v < 9; ++v) s[37 + v] = A.P.dv[v][p];
+        }
+        __syncthreads();
+        const int lo = max(pb, ch), hi = min(pe, min(ch + TH, b1));
+        for (int kk = lo; kk < hi; ++kk) {
+            const float* s = sp + (kk - ch) * TP3_STRIDE;
+            const float wxy = s[qx] * s[8 + qy], gx = s[4 + qx] * s[8 + qy], gy = s[qx] * s[12 + qy];
+            const float ms = s[24];
+            const float sxx = s[28], syy = s[29], szz = s[30], syz = s[31], sxz = s[32], sxy = s[33];
+            float v0 = s[25], v1 = s[26], v2 = s[27], G[9], dlt0 = 0.f, dlt1 = 0.f, dz0 = 0.f;
+            if (tpic) {
+                // v + ∇v (x_n - x_p) with the previous step's ∇v (p2n.jl:157-158)
+                dlt0 = (float)(qx - 1) * hx - s[34];
+                dlt1 = (float)(qy - 1) * hy - s[35];
+                dz0 = s[36];
+#pragma unroll
+                for (int v = 0; v < 9; ++v) G[v] = s[37 + v];
+                v0 += G[0] * dlt0 + G[3] * dlt1;
+                v1 += G[1] * dlt0 + G[4] * dlt1;
+                v2 += G[2] * dlt0 + G[5] * dlt1;
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const float wz = s[16 + j], dwz = s[20 + j];
+                const float N = wxy * wz, Nx = gx * wz, Ny = gy * wz, Nz = wxy * dwz;
+                const float Nm = N * ms;
+                am[j] += Nm;
+                if (!tpic) {
+                    ap[0][j] += Nm * s[25];
+                    ap[1][j] += Nm * s[26];
+                    ap[2][j] += Nm * s[27];
+                } else {
+                    const float dz = (float)(j - 1) * hz - dz0;
+                    ap[0][j] += Nm * (v0 + G[6] * dz);
+                    ap[1][j] += Nm * (v1 + G[7] * dz);
+                    ap[2][j] += Nm * (v2 + G[8] * dz);
+                }
+                af[0][j] -= Nx * sxx + Ny * sxy + Nz * sxz;
+                af[1][j] -= Nx * sxy + Ny * syy + Nz * syz;
+                af[2][j] -= (Nx * sxz + Ny * syz + Nz * szz) - Nm * gz;
+            }
+        }
+        __syncthreads();
+    }
+    if (bad) set_err(A.ctl, EP_ERR_INVALID_POSITION, c0);
+    if (!cell_ok || pb == pe) return;
+    int e[3];
+    cell_dec(A.g, cl, e);
+    const Axis4 ax = axis4(A.g, 0, e[0]), ay = axis4(A.g, 1, e[1]), az = axis4(A.g, 2, e[2]);
+    if (ax.cls[qx] < 0 || ay.cls[qy] < 0) return;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        if (az.cls[j] < 0) continue;
+        const int n = node3(A.g, ax, ay, az, qx, qy, j);
+        atomicAdd(&A.N.m[n], am[j]);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            atomicAdd(&A.N.p[d][n], ap[d][j]);
+            atomicAdd(&A.N.f[d][n], af[d][j]);
+        }
+    }
+}
+
+// km_g2p_seg3: PIC/FLIP (n2p.jl:14-40), new cell + offset, vmax, next-cell counts and the
+// mUSL momentum P2G (augm.jl:13-25) in 3d, one lane per point
+template <int BASIS>
+__global__ void __launch_bounds__(256) km_g2p_seg3(MCtx A) {
+    EP_ACTIVE(A.ctl);
+    const int cur = A.ctl->parity, nxt = cur ^ 1;
+    const int n = A.S.start[cur][A.g.ncell];
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    bool bad = false;
+    PtW3 W;
+    const bool live = point3<BASIS>(A, cur, k, n, W, bad);
+    const Seg S = seg_of(W.c);
+    const float dtf = (float)A.ctl->dt, Cpf = (float)A.cf.Cpf;
+    unsigned vm[3] = {0u, 0u, 0u};
+    float v[3] = {0.f, 0.f, 0.f}, mp = 0.f;
+    int c2 = -1;
+    if (live) {
+        float vp[3] = {0.f, 0.f, 0.f}, af[3] = {0.f, 0.f, 0.f};
+#pragma unroll 1
+        for (int j = 0; j < 4; ++j) {
+            if (W.a[1].cls[j] < 0) continue;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                if (W.a[0].cls[i] < 0) continue;
+                const float wxy = W.w[0][i] * W.w[1][j];
+#pragma unroll
+                for (int kz = 0; kz < 4; ++kz) {
+                    if (W.a[2].cls[kz] < 0) continue;
+                    const int nd = node3(A.g, W.a[0], W.a[1], W.a[2], i, j, kz);
+                    const float N = wxy * W.w[2][kz];
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) {
+                        vp[d] += N * __ldg(&A.N.v[d][nd]);
+                        af[d] += N * __ldg(&A.N.a[d][nd]);
+                    }
+                }
+            }
+        }
+        const int p = W.p;
+        int e2[3];
+        float o2[3];
+        bool fin = true;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            v[d] = Cpf * (A.P.v[d][p] + dtf * af[d]) + (1.f - Cpf) * vp[d];
+            A.P.v[d][p] = v[d];
+            vm[d] = __float_as_uint(fabsf(v[d]));
+            const float o = W.o[d] + dtf * vp[d];
+            fin = fin && isfinite(o);
+            if (isfinite(o)) recell(A.g, d, W.e[d], o, 1.f / (float)A.g.h[d], e2[d], o2[d]);
+        }
+        if (fin) {
+            c2 = cell_of(A.g, e2);
+#pragma unroll
+            for (int d = 0; d < 3; ++d) A.P.dx[nxt][d][p] = o2[d];
+        } else {
+            set_err(A.ctl, EP_ERR_NONFINITE, p);
+        }
+        A.P.p2e_next[p] = c2;
+        mp = A.P.mp[p];
+    }
+    {
+        const unsigned mm = __match_any_sync(0xffffffffu, c2);
+        if (c2 >= 0 && S.lane == __ffs(mm) - 1) atomicAdd(&A.S.count[nxt][c2], __popc(mm));
+    }
+    if (A.cf.musl) {
+#pragma unroll 1
+        for (int j = 0; j < 4; ++j)
+#pragma unroll 1
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int kz = 0; kz < 4; ++kz) {
+                    const float Nm = live ? W.w[0][i] * W.w[1][j] * W.w[2][kz] * mp : 0.f;
+                    const float s0 = seg_sum(Nm * v[0], S), s1 = seg_sum(Nm * v[1], S), s2 = seg_sum(Nm * v[2], S);
+                    if (S.head && live && W.a[0].cls[i] >= 0 && W.a[1].cls[j] >= 0 && W.a[2].cls[kz] >= 0) {
+                        const int nd = node3(A.g, W.a[0], W.a[1], W.a[2], i, j, kz);
+                        atomicAdd(&A.N.pm[0][nd], s0);
+                        atomicAdd(&A.N.pm[1][nd], s1);
+                        atomicAdd(&A.N.pm[2][nd], s2);
+                    }
+                }
+    }
+    if (bad) set_err(A.ctl, EP_ERR_INVALID_POSITION, W.c);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) vm[d] = __reduce_max_sync(0xffffffffu, vm[d]);
+    if (S.lane == 0)
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+            if (vm[d])
+                atomicMax(&A.ctl->vmax_bits[d], (unsigned long long)__double_as_longlong((double)__uint_as_float(vm[d])));
+}
+
+// ∇v of a point in 3d: g[i + 3 j] = Σ_n ∂N/∂x_j v_i(n) (deform.jl:9-10), optionally a = Σ N δJ_n
+__device__ __forceinline__ void grad3(const MCtx& A, const PtW3& W, float* const* vn, float* g, bool lock, float* a) {
+#pragma unroll
+    for (int i = 0; i < 9; ++i) g[i] = 0.f;
+    float s = 0.f;
+#pragma unroll 1
+    for (int j = 0; j < 4; ++j) {
+        if (W.a[1].cls[j] < 0) continue;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            if (W.a[0].cls[i] < 0) continue;
+#pragma unroll
+            for (int kz = 0; kz < 4; ++kz) {
+                if (W.a[2].cls[kz] < 0) continue;
+                const int nd = node3(A.g, W.a[0], W.a[1], W.a[2], i, j, kz);
+                const float dN[3] = {W.dw[0][i] * W.w[1][j] * W.w[2][kz], W.w[0][i] * W.dw[1][j] * W.w[2][kz],
+                                     W.w[0][i] * W.w[1][j] * W.dw[2][kz]};
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const float vc = __ldg(&vn[c][nd]);
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) g[c + 3 * d] += dN[d] * vc;
+                }
+                if (lock) s += W.w[0][i] * W.w[1][j] * W.w[2][kz] * __ldg(&A.N.dJn[nd]);
+            }
+        }
+    }
+    *a = s;
+}
+
+// km_fbar_seg3: δJ = det(I + dt ∇v) - 1 and Σ N m δJ (deform.jl:9-18, volumetric.jl:1-11) in 3d
+template <int BASIS>
+__global__ void __launch_bounds__(256) km_fbar_seg3(MCtx A) {
+    EP_ACTIVE(A.ctl);
+    const int cur = A.ctl->parity, nxt = cur ^ 1;
+    const int n = A.S.start[cur][A.g.ncell];
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    bool bad = false;
+    PtW3 W;
+    const bool live = point3<BASIS>(A, cur, k, n, W, bad);
+    const Seg S = seg_of(W.c);
+    const float dtf = (float)A.ctl->dt;
+    float* const* vn = A.cf.musl ? A.N.vm : A.N.v;
+    const bool fin = A.cf.deform == EP_DEFORM_FINITE;
+    float mdj = 0.f;
+    if (live) {
+        float g[9], unused;
+        grad3(A, W, vn, g, false, &unused);
+        float D[9];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) D[i] = dtf * g[i];
+        const float dJ = det1p_m1(D);
+        mdj = A.P.mp[W.p] * (fin ? dJ : dJ * (2.f + dJ));
+    }
+    place_next_warp(A, live ? W.p : -1, live ? A.P.p2e_next[W.p] : -1, nxt, S.lane);
+#pragma unroll 1
+    for (int j = 0; j < 4; ++j)
+#pragma unroll 1
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int kz = 0; kz < 4; ++kz) {
+                const float v = seg_sum(live ? W.w[0][i] * W.w[1][j] * W.w[2][kz] * mdj : 0.f, S);
+                if (S.head && live && W.a[0].cls[i] >= 0 && W.a[1].cls[j] >= 0 && W.a[2].cls[kz] >= 0)
+                    atomicAdd(&A.N.dJacc[node3(A.g, W.a[0], W.a[1], W.a[2], i, j, kz)], v);
+            }
+    if (bad) set_err(A.ctl, EP_ERR_INVALID_POSITION, W.c);
+}
+
+// km_cons3: F-bar, F, infinitesimal elastic predictor (elast.jl:69-80) and J2 / DP returns in 3d,
+// one lane per sorted point
+template <int BASIS, int ACC>
+__global__ void __launch_bounds__(256) km_cons3(MCtx A, int plastic_phase) {
+    EP_ACTIVE(A.ctl);
+    const int cur = A.ctl->parity, nxt = cur ^ 1;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    int nplastic = 0;
+    const int n = A.S.start[cur][A.g.ncell];
+    if (k < n) {
+        bool bad = false;
+        PtW3 W;
+        point3<BASIS>(A, cur, k, n, W, bad);
+        const int p = W.p;
+        const float dtf = (float)A.ctl->dt;
+        const bool lock = A.cf.locking;
+        float g[9], a = 0.f;
+        grad3(A, W, A.cf.musl ? A.N.vm : A.N.v, g, lock, &a);
+        float D[9];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) D[i] = dtf * g[i];
+        if (A.cf.trsfr == EP_TRSFR_TPIC)
+#pragma unroll
+            for (int i = 0; i < 9; ++i) A.P.dv[i][p] = g[i];
+        // F <- ΔF F = F + D F (deform.jl:35-40), with the unscaled ΔF
+        float Fdev[9];     // F - I, exact from the stored state
+        if (ACC == 0) {
+            double F[9];
+#pragma unroll
+            for (int i = 0; i < 9; ++i) F[i] = A.P.Fd[i][p];
+            float f[9];
+#pragma unroll
+            for (int i = 0; i < 9; ++i) f[i] = (float)F[i];
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+                    const float inc = D[r] * f[3 * c] + D[r + 3] * f[1 + 3 * c] + D[r + 6] * f[2 + 3 * c];
+                    const double nv = F[r + 3 * c] + (double)inc;
+                    A.P.Fd[r + 3 * c][p] = nv;
+                    Fdev[r + 3 * c] = (float)(nv - (r == c ? 1.0 : 0.0));
+                }
+        } else {
+            float h[9], l[9];
+#pragma unroll
+            for (int i = 0; i < 9; ++i) {
+                h[i] = A.P.Fh[i][p];
+                l[i] = A.P.Fl[i][p];
+            }
+            float inc[9];
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+#pragma unroll
+                for (int r = 0; r < 3; ++r) inc[r + 3 * c] = D[r] * h[3 * c] + D[r + 3] * h[1 + 3 * c] + D[r + 6] * h[2 + 3 * c];
+#pragma unroll
+            for (int i = 0; i < 9; ++i) {
+                df_add(h[i], l[i], inc[i]);
+                A.P.Fh[i][p] = h[i];
+                A.P.Fl[i][p] = l[i];
+                const bool dg = i == 0 || i == 4 || i == 8;
+                Fdev[i] = dg ? (h[i] - 1.f) + l[i] : h[i] + l[i];
+            }
+        }
+        // infinitesimal: volume J Ω0 and mass ρ J Ω0 follow J (deform.jl:41-43)
+        const float Jm1 = det1p_m1(Fdev);
+        const float Om = A.P.Om0[p] + A.P.Om0[p] * Jm1;
+        A.P.Om[p] = Om;
+        A.P.mp[p] = A.P.rho[p] * Om;
+        // F-bar: ΔF <- (ΔJ̄/ΔJ)^(1/3) ΔF (volumetric.jl:23-36), increment form
+        if (lock) {
+            float sm1 = 0.f;      // Σ N - 1 over the existing nodes (GIMP next to a mesh edge)
+            if (BASIS == EP_BASIS_GIMPM) {
+                float ms[3];
+#pragma unroll
+                for (int d = 0; d < 3; ++d) ms[d] = axis_miss<BASIS>(W.a[d], W.o[d], (float)A.g.h[d], A.P.l[d][p]);
+                sm1 = -(ms[0] + ms[1] + ms[2]) + (ms[0] * ms[1] + ms[0] * ms[2] + ms[1] * ms[2]) - ms[0] * ms[1] * ms[2];
+            }
+            const float dJp = det1p_m1(D);
+            const float r1 = (sm1 + a - dJp) / (1.f + dJp);
+            const float s1 = expm1f(log1pf(r1) * (1.f / 3.f));
+#pragma unroll
+            for (int i = 0; i < 9; ++i) D[i] = D[i] * (1.f + s1) + ((i == 0 || i == 4 || i == 8) ? s1 : 0.f);
+        }
+        // σ += Del voigt(sym(ΔF) - I, 2) (+ ωσ - σω for the objective rate)
+        float tt[6], de[6];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) tt[i] = A.P.tau[i][p];
+        de[0] = D[0]; de[1] = D[4]; de[2] = D[8];
+        de[3] = D[5] + D[7];        // 2 ε_yz
+        de[4] = D[2] + D[6];        // 2 ε_xz
+        de[5] = D[1] + D[3];        // 2 ε_xy
+        float ds[6];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) {
+            float s = 0.f;
+#pragma unroll
+            for (int j = 0; j < 6; ++j) s += A.Del[i + 6 * j] * de[j];
+            ds[i] = s;
+        }
+        if (A.cf.jaumann) {
+            // W = skew(D); ωσ - σω in Voigt components
+            const float w01 = 0.5f * (D[3] - D[1]), w02 = 0.5f * (D[6] - D[2]), w12 = 0.5f * (D[7] - D[5]);
+            const float S[3][3] = {{tt[0], tt[5], tt[4]}, {tt[5], tt[1], tt[3]}, {tt[4], tt[3], tt[2]}};
+            const float Wm[3][3] = {{0.f, w01, w02}, {-w01, 0.f, w12}, {-w02, -w12, 0.f}};
+            float R[3][3];
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) {
+                    float s = 0.f;
+                    for (int q = 0; q < 3; ++q) s += Wm[i][q] * S[q][j] - S[i][q] * Wm[q][j];
+                    R[i][j] = s;
+                }
+            ds[0] += R[0][0]; ds[1] += R[1][1]; ds[2] += R[2][2];
+            ds[3] += R[1][2]; ds[4] += R[0][2]; ds[5] += R[0][1];
+        }
+#pragma unroll
+        for (int i = 0; i < 6; ++i) tt[i] += ds[i];
+        if (plastic_phase) {
+            const float ep1f = ACC == 0 ? (float)A.P.ep1d[p] : A.P.ep1h[p] + A.P.ep1l[p];
+            const float ep2 = A.cf.nonloc ? A.P.ep2[p] : ep1f;
+            if (A.cf.cons == EP_CONS_DP) {
+                float inc = 0.f;
+                const float dl = dpf6(tt, ep2, A.P.c0[p], A.P.cr[p], A.P.sphi[p], A.P.cphi[p], A.Kc, A.Gc, A.Hp, &inc);
+                A.P.dlam[p] = dl;
+                if (dl != 0.f) {
+                    ++nplastic;
+                    add_ep1<ACC>(A, p, inc);
+                }
+            } else {
+                float newg = 0.f;
+                if (j2f6(tt, ep2, A.P.c0[p], A.P.cr[p], A.Hp, A.Del, &newg)) {
+                    ++nplastic;
+                    if (ACC == 0) {
+                        A.P.ep1d[p] = (double)newg;
+                    } else {
+                        A.P.ep1h[p] = newg;
+                        A.P.ep1l[p] = 0.f;
+                    }
+                }
+            }
+        }
+        bool okv = true;
+#pragma unroll
+        for (int i = 0; i < 6; ++i) {
+            A.P.tau[i][p] = tt[i];
+            okv = okv && isfinite(tt[i]);
+        }
+        if (!okv) set_err(A.ctl, EP_ERR_NONFINITE, p);
+        if (!lock) place_next(A, p, nxt);
+        if (bad) set_err(A.ctl, EP_ERR_INVALID_POSITION, W.c);
+    }
+    const int tot = __reduce_add_sync(0xffffffffu, nplastic);
+    if ((threadIdx.x & 31) == 0 && tot) atomicAdd((unsigned long long*)&A.ctl->plastic, (unsigned long long)tot);
+}
+
+template <int BASIS, int ACC>
+static void mixed_step3_impl(const MixedCtx& X, int phase, cudaStream_t s) {
+    const MCtx& A = *(const MCtx*)X.impl;
+    const int nc = A.g.ncell, nn = A.g.nnode, np = A.P.np;
+    const int gn = (nn + 255) / 256, gp = (np + 255) / 256;
+    const int gs = gp > 0 ? gp : 1;
+    Prof* pr = (X.prof && X.prof->on) ? X.prof : nullptr;
+    auto mark = [&](const char* nm) {
+        if (pr) pr->mark(nm, s);
+    };
+    long long L = 0;
+    cudaMemsetAsync(X.grid_zero, 0, X.grid_zero_bytes, s);
+    cudaMemsetAsync(X.sort_zero, 0, X.sort_zero_bytes, s);
+    mark("memset");
+    km_p2g_tile3<BASIS, 16><<<(nc + 15) / 16, 256, 0, s>>>(A);
+    mark("p2g");
+    km_solve<<<gn, 256, 0, s>>>(A);
+    mark("solve");
+    km_g2p_seg3<BASIS><<<gs, 256, 0, s>>>(A);
+    mark("g2p");
+    L += 3;
+    if (A.cf.musl) { km_vmusl<<<gn, 256, 0, s>>>(A); mark("vmusl"); ++L; }
+    L += mixed_scan(A, 0, X.scan_in, s);
+    mark("scan");
+    if (A.cf.locking) {
+        km_fbar_seg3<BASIS><<<gs, 256, 0, s>>>(A);
+        mark("fbar");
+        km_dJn<<<gn, 256, 0, s>>>(A);
+        mark("dJn");
+        L += 2;
+    }
+    if (np > 0) {
+        km_cons3<BASIS, ACC><<<gp, 256, 0, s>>>(A, phase == EP_PHASE_ELASTOPLASTIC);
+        mark("cons");
+        ++L;
+    }
+    km_flip<<<1, 1, 0, s>>>(A.ctl, nullptr, nullptr);
+    ++L;
+    if (X.launches) *X.launches += L;
 }
 
 // ---------------------------------------------------------------------------
@@ -1975,6 +2623,19 @@ static void mixed_step_acc(const MixedCtx& X, int phase, cudaStream_t s) {
 
 void mixed_step(const MixedCtx& X, int phase, cudaStream_t s) {
     const MCtx& A = *(const MCtx*)X.impl;
+    if (A.g.dim == 3) {
+        const int b = A.cf.basis;
+        if (A.acc == 0) {
+            if (b == EP_BASIS_BSMPM) mixed_step3_impl<EP_BASIS_BSMPM, 0>(X, phase, s);
+            else if (b == EP_BASIS_GIMPM) mixed_step3_impl<EP_BASIS_GIMPM, 0>(X, phase, s);
+            else mixed_step3_impl<EP_BASIS_SMPM, 0>(X, phase, s);
+        } else {
+            if (b == EP_BASIS_BSMPM) mixed_step3_impl<EP_BASIS_BSMPM, 1>(X, phase, s);
+            else if (b == EP_BASIS_GIMPM) mixed_step3_impl<EP_BASIS_GIMPM, 1>(X, phase, s);
+            else mixed_step3_impl<EP_BASIS_SMPM, 1>(X, phase, s);
+        }
+        return;
+    }
     if (A.cf.det) {
         if (A.acc == 0) mixed_step_acc<0, true>(X, phase, s);
         else mixed_step_acc<1, true>(X, phase, s);
@@ -2019,19 +2680,18 @@ void mixed_ctx_init(void* mem, const Cfg& cf, const Geo& g, Ctl* ctl, const PM& 
     A->P = P;
     A->N = N;
     A->S = S;
-    for (int i = 0; i < 9; ++i) {
-        A->Del[i] = (float)Del[i];
-        A->Cmp[i] = (float)Cmp[i];
+    const int ns = g.dim == 2 ? 3 : 6;
+    for (int i = 0; i < 36; ++i) {
+        A->Del[i] = i < ns * ns ? (float)Del[i] : 0.f;
+        A->Cmp[i] = i < ns * ns ? (float)Cmp[i] : 0.f;
+        A->Deld[i] = i < ns * ns ? Del[i] : 0.0;
+        A->Cmpd[i] = i < ns * ns ? Cmp[i] : 0.0;
     }
     A->Kc = (float)Kc;
     A->Gc = (float)Gc;
     A->Hp = (float)Hp;
     A->c = c;
     A->acc = acc;
-    for (int i = 0; i < 9; ++i) {
-        A->Deld[i] = Del[i];
-        A->Cmpd[i] = Cmp[i];
-    }
     A->Kd = Kc;
     A->Gd = Gc;
     A->l2g = (float)(Del[3] / (Del[0] - Del[3]));   // λ / (2G) of the plane-strain stiffness

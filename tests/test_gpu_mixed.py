@@ -81,6 +81,7 @@ def test_mixed_switches(oracle_mod, deform, trsfr, locking, precision):
 
 
 @pytest.mark.parametrize("basis", [{"which": "gimpm", "how": "undeformed", "ghost": True},
+                                   {"which": "gimpm", "how": "undeformed", "ghost": False},
                                    {"which": "smpm", "how": None, "ghost": False}])
 @pytest.mark.parametrize("precision", PRECISIONS)
 def test_mixed_other_bases(oracle_mod, basis, precision):
