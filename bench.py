@@ -282,6 +282,92 @@ def batch_bench(args, rank, ws):
         print(json.dumps(line))
 
 
+def c3_bench(args, rank, ws):
+    """The 3d slump (nel=[320,80,80], 2x2x2 points per cell): particle-steps/s of the mixed 3d step."""
+    import torch
+    from epgpu import Engine, ic_slump
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    t0 = time.perf_counter()
+    kw = {"basis": {"which": "gimpm", "how": "undeformed", "ghost": True},
+          "fwrk": {"deform": "infinitesimal", "trsfr": "tpic", "C_pf": 0.0, "musl": False, "locking": False,
+                   "damping": 0.1},
+          "plast": {"status": True, "constitutive": "J2"}, "nonloc": {"status": False, "ls": 0.5}}
+    ic, cfg = ic_slump([64.1584, 16.0396, 16.0396], [320, 80, 80], ni=2,
+                       cmpr_over={"E": 1.0e7, "rho0": 2000.0, "c0": 5.0e4, "Hp": 1.0e5}, **kw)
+    setup_s = time.perf_counter() - t0
+    mesh, mpts, cmpr = ic["mesh"], ic["mpts"], ic["cmpr"]
+    np_ = mpts.nmp
+    g = [0.0, 0.0, -9.81]
+    instr = dict(cfg["instr"])
+    instr["gpu"] = {"precision": args.precision if args.precision != "fp64" else "mixed_df", "jaumann": False}
+    e = Engine(ic, instr)
+    e.run(1, args.settle, 10.0, 0.0)
+    host0 = e.download()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def timed(engine, k, w, clk=None):
+        engine.upload(host0)
+        vm = host0.vmax.copy()
+        seq = []
+        for _ in range(w):
+            seq.append(cfl_dt(mesh, cmpr, vm))
+            vm = engine.step(1, seq[-1], g)
+        engine.profile(True)
+        ms = 0.0
+        if clk:
+            clk.__enter__()
+        for _ in range(k):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            seq.append(cfl_dt(mesh, cmpr, vm))
+            vm = engine.step(1, seq[-1], g)
+            ms += engine.stats()["device_ms"]
+        if clk:
+            clk.__exit__(None, None, None)
+        kt = engine.kernel_times()
+        engine.profile(False)
+        return ms, seq, kt
+
+    clk = Clocks(local)
+    ms, dts, kt = timed(e, args.steps, args.warmup, clk)
+    final = e.download()
+    e.close()
+    value = np_ * args.steps / (ms * 1e-3)
+    tot = sum(v[1] for v in kt.values())
+    # the FP64 step beside it (and the error of the timed run against it, same dt sequence)
+    instr64 = dict(cfg["instr"])
+    instr64["gpu"] = {"precision": "fp64", "jaumann": False}
+    e64 = Engine({"mesh": mesh, "mpts": host0.copy(), "cmpr": cmpr}, instr64)
+    t64 = 0.0
+    for dt in dts:
+        e64.step(1, dt, g)
+        t64 += e64.stats()["device_ms"]
+    b = e64.download()
+    e64.close()
+    x0 = host0.x
+    line = {
+        "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (+f32 pairs)" if instr["gpu"]["precision"] == "mixed_df" else "f32+f64",
+        "data": "synthetic 3d slump geometry, uniform cohesion 50 kPa",
+        "config": {"workload": "3d slump L=[64.1584,16.0396,16.0396], nel=[320,80,80], 2x2x2 points/cell, GIMP "
+                               "(ghost), TPIC (PIC), USL, infinitesimal J2 (E=1e7, rho=2000, c0=50 kPa, H=1e5)",
+                   "points": np_, "nodes": mesh.nnodes, "setup_s": setup_s, "settle_s": args.settle,
+                   "precision": instr["gpu"]["precision"], "l2": "flushed between timed steps (256 MB write)"},
+        "kernel_share": {k: round(v[1] / tot, 4) for k, v in kt.items()},
+        "fp64_step": {"ms_per_step": t64 / len(dts), "value": np_ * len(dts) / (t64 * 1e-3),
+                      "unit": "particle-steps/s"},
+        "speedup_vs_fp64_step": (value / (np_ * len(dts) / (t64 * 1e-3))) if t64 > 0 else None,
+        "error_vs_fp64": {"steps": len(dts),
+                          "stress_rel_l2": float(np.linalg.norm(final.sig - b.sig) / np.linalg.norm(b.sig)),
+                          "displacement_rel_l2": float(np.linalg.norm(final.x - b.x) / max(np.linalg.norm(b.x - x0), 1e-300))},
+        "clocks": clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -302,8 +388,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--deterministic", action="store_true",
                     help="mixed step without floating-point atomics (bitwise reproducible)")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c4"],
-                    help="c2: the nel=[640,160] slump (headline); c4: the batched ensemble")
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4"],
+                    help="c2: the nel=[640,160] slump (headline); c3: the 3d slump; c4: the batched ensemble")
     ap.add_argument("--instances", type=int, default=256)
     ap.add_argument("--window", type=float, default=0.05, help="simulated seconds timed in the c4 workload")
     ap.add_argument("--no-e2e", action="store_true")
@@ -317,6 +403,9 @@ def main():
         return
     if args.workload == "c4":
         batch_bench(args, rank, ws)
+        return
+    if args.workload == "c3":
+        c3_bench(args, rank, ws)
         return
     import torch
     from epgpu import Engine
