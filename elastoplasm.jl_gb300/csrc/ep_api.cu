@@ -227,8 +227,8 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
                     "the mixed-precision 3d step is built for infinitesimal strain; use EP_PREC_FP64 for finite strain in 3d");
     if (cfg->precision != EP_PREC_FP64 && d == 3 && cfg->deterministic)
         return fail(nullptr, EP_ERR_UNSUPPORTED, "the deterministic mode is built for the 2d mixed step");
-    if (cfg->precision != EP_PREC_FP64 && cfg->nonloc)
-        return fail(nullptr, EP_ERR_UNSUPPORTED, "nonlocal averaging is built in the FP64 step only");
+    if (cfg->precision != EP_PREC_FP64 && cfg->nonloc && d == 3)
+        return fail(nullptr, EP_ERR_UNSUPPORTED, "nonlocal averaging of the mixed step is built in 2d (FP64 step in 3d)");
     if (cfg->nonloc && !(cfg->nonloc_ls > 0.0)) return fail(nullptr, EP_ERR_ARG, "nonloc.ls must be > 0");
     if (!mesh->x || !mesh->xB || !mesh->bcs) return fail(nullptr, EP_ERR_ARG, "mesh.x, mesh.xB and mesh.bcs are required");
     long long nnode = 1, ncell = 1;
@@ -462,7 +462,8 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
         const size_t nflt = (size_t)np * (2 * d + d + nsym + 11 + 1 + d + d * d + (acc ? 2 * nacc : 0));
         ok2 = ok2 && dalloc(h, &pf, nflt) == cudaSuccess;
         int* ints = nullptr;
-        const size_t nint = (size_t)3 * nc + 2 * (size_t)(nc + 1) + 4 * (size_t)np + (size_t)np + 2 * (size_t)(nc + 1);
+        const size_t nint = (size_t)3 * nc + 2 * (size_t)(nc + 1) + 4 * (size_t)np + (size_t)np + 2 * (size_t)(nc + 1) +
+                            (cfg->nonloc ? 2 * (size_t)np : 0);
         ok2 = ok2 && dalloc(h, &ints, nint) == cudaSuccess;
         float* nf = nullptr;
         const size_t nnf = (size_t)nn * (1 + 6 * d + 2);
@@ -510,6 +511,10 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
         pm.p2e_next = ip; ip += np;
         h->mx.scan_in = ip; ip += nc + 1;
         h->mx.scan_out = ip; ip += nc + 1;
+        if (cfg->nonloc) {
+            pm.pcell[0] = ip; ip += np;
+            pm.pcell[1] = ip; ip += np;
+        }
         sm.scan_tmp = S.scan_tmp;
         float* g0 = nf;
         nm.m = g0;

@@ -653,6 +653,7 @@ __global__ void __launch_bounds__(256) km_g2p_seg(MCtx A) {
             set_err(A.ctl, EP_ERR_NONFINITE, p);
         }
         A.P.p2e_next[p] = c2;
+        if (A.P.pcell[nxt]) A.P.pcell[nxt][p] = c2;
         mp = A.P.mp[p];
     }
     {
@@ -1664,6 +1665,143 @@ __global__ void km_flip(Ctl* ctl, int* rcount, int* fbcount) {
 
 
 // ---------------------------------------------------------------------------
+// km_nonlocal: nonlocal averaging of ϵpII in the reference's serial visiting order
+// (nonlocal.jl:18-47 with plast.jl:51-59), one warp per point, 2d.  Same sums as the FP64
+// step (for a point p with Δλ != 0 from the previous return and N(p) the points of the
+// cells within ±ceil(ls/h) of p's cell at the step start):
+//   W[p]  = Σ_{r in N(p), r plastic, r < p} ω(r,p) + Σ_{q in N(p), not (q plastic and q < p)} ω(p,q)
+//   ϵ2[p] = Σ_{q in N(p), not (q plastic and q < p)} (ω(p,q) / W[p]) ϵ1[q]
+// in ascending id order, ω = (d/ls) exp(-(d/ls)^2), d from the positions after G2P (cell
+// node coordinate in FP64 + FP32 offset); ϵ2 = ϵ1 when W <= 1e-16, 0 for non-plastic points.
+constexpr int NLM_CAP = 2048;
+
+template <int ACC>
+__device__ __forceinline__ float ep1_of(const MCtx& A, int q) {
+    return ACC == 0 ? (float)A.P.ep1d[q] : A.P.ep1h[q] + A.P.ep1l[q];
+}
+
+template <int ACC>
+__global__ void __launch_bounds__(32) km_nonlocal(MCtx A) {
+    EP_ACTIVE(A.ctl);
+    __shared__ int qs[NLM_CAP];
+    __shared__ float om[NLM_CAP];
+    const int p = blockIdx.x, lane = threadIdx.x;
+    if (p >= A.P.np) return;
+    const int cur = A.ctl->parity, nxt = cur ^ 1;
+    const int cp = A.P.pcell[cur][p], cn = A.P.pcell[nxt][p];
+    if (A.P.dlam[p] == 0.f || cp < 0 || cn < 0) {
+        if (lane == 0) A.P.ep2[p] = 0.f;
+        return;
+    }
+    const int n1 = A.g.nel[1];
+    const int ex = cp / n1, ez = cp - ex * n1;
+    const int lo0 = max(ex - A.g.nnel[0], 0), hi0 = min(ex + A.g.nnel[0], A.g.nel[0] - 1);
+    const int lo1 = max(ez - A.g.nnel[1], 0), hi1 = min(ez + A.g.nnel[1], n1 - 1);
+    const int* start = A.S.start[cur];
+    const int* list = A.S.list[cur];
+    int L = 0;
+    for (int a = lo0; a <= hi0; ++a) L += start[hi1 + n1 * a + 1] - start[lo1 + n1 * a];
+    const double ls = A.cf.ls;
+    const int exn = cn / n1, ezn = cn - exn * n1;
+    const double xp0 = A.g.ax[0][exn] + (double)A.P.dx[nxt][0][p];
+    const double xp1 = A.g.ax[1][ezn] + (double)A.P.dx[nxt][1][p];
+    auto omega = [&](int q) {
+        const int cq = A.P.pcell[nxt][q];
+        const int eq = cq / n1, fq = cq - eq * n1;
+        const double xi = xp0 - (A.g.ax[0][eq] + (double)A.P.dx[nxt][0][q]);
+        const double et = xp1 - (A.g.ax[1][fq] + (double)A.P.dx[nxt][1][q]);
+        const float r = (float)(sqrt(xi * xi + et * et) / ls);
+        return r * expf(-(r * r));
+    };
+    if (L <= NLM_CAP) {
+        // candidate ids in cell order (each column's cells are one contiguous slice of the list)
+        int pos = 0;
+        for (int a = lo0; a <= hi0; ++a) {
+            const int b = start[lo1 + n1 * a], n = start[hi1 + n1 * a + 1] - b;
+            for (int k = lane; k < n; k += 32) qs[pos + k] = list[b + k];
+            pos += n;
+        }
+        int P2 = 32;
+        while (P2 < L) P2 <<= 1;
+        for (int k = L + lane; k < P2; k += 32) qs[k] = INT_MAX;
+        __syncwarp();
+        // bitonic sort into ascending point id (the reference's serial order)
+        for (int k = 2; k <= P2; k <<= 1)
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                for (int t = lane; t < P2; t += 32) {
+                    const int q = t ^ j;
+                    if (q > t) {
+                        const int a = qs[t], c = qs[q];
+                        const bool asc = (t & k) == 0;
+                        if ((a > c) == asc) {
+                            qs[t] = c;
+                            qs[q] = a;
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+        for (int t = lane; t < L; t += 32) om[t] = omega(qs[t]);
+        __syncwarp();
+        if (lane == 0) {
+            float W = 0.f;
+            for (int t = 0; t < L; ++t) {
+                const int q = qs[t];
+                if (q >= p) break;
+                if (A.P.dlam[q] != 0.f) W += om[t];
+            }
+            for (int t = 0; t < L; ++t) {
+                const int q = qs[t];
+                if (q < p && A.P.dlam[q] != 0.f) continue;
+                W += om[t];
+            }
+            float s = 0.f;
+            if (!(W > 1e-16f)) {
+                s = ep1_of<ACC>(A, p);
+            } else {
+                for (int t = 0; t < L; ++t) {
+                    const int q = qs[t];
+                    if (q < p && A.P.dlam[q] != 0.f) continue;
+                    s += (om[t] / W) * ep1_of<ACC>(A, q);
+                }
+            }
+            A.P.ep2[p] = s;
+        }
+        return;
+    }
+    // more candidates than the shared buffer holds: walk them in ascending order by repeated
+    // minimum selection (slow, same sums)
+    if (lane != 0) return;
+    float W = 0.f;
+    for (int pass = 0; pass < 3; ++pass) {
+        float s = 0.f;
+        int last = -1;
+        if (pass == 2 && !(W > 1e-16f)) {
+            A.P.ep2[p] = ep1_of<ACC>(A, p);
+            return;
+        }
+        while (true) {
+            int best = INT_MAX;
+            for (int a = lo0; a <= hi0; ++a)
+                for (int k = start[lo1 + n1 * a]; k < start[hi1 + n1 * a + 1]; ++k) {
+                    const int q = list[k];
+                    if (q > last && q < best) best = q;
+                }
+            if (best == INT_MAX) break;
+            last = best;
+            const int q = best;
+            const bool plq = A.P.dlam[q] != 0.f;
+            if (pass == 0 && !(q < p && plq)) continue;
+            if (pass >= 1 && (q < p && plq)) continue;
+            const float w = omega(q);
+            if (pass < 2) W += w;
+            else s += (w / W) * ep1_of<ACC>(A, q);
+        }
+        if (pass == 2) A.P.ep2[p] = s;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // exclusive scan of count[nxt] into start[nxt] (parity read on the device)
 constexpr int MSCAN_BS = 1024, MSCAN_IPT = 4, MSCAN_CHUNK = MSCAN_BS * MSCAN_IPT;
 
@@ -1852,6 +1990,7 @@ __global__ void km_bin0(MCtx A, P64 Q) {
         set_err(A.ctl, EP_ERR_NONFINITE, p);
     }
     A.P.p2e_next[p] = c2;
+    if (A.P.pcell[cur]) A.P.pcell[cur][p] = c2;
 }
 
 __global__ void km_place0(MCtx A) {
@@ -2587,6 +2726,11 @@ static void mixed_step_impl(const MixedCtx& X, int phase, cudaStream_t s) {
         km_dJn<<<gn, 256, 0, s>>>(A);
         mark("dJn");
         L += 2;
+    }
+    if (np > 0 && A.cf.nonloc && phase == EP_PHASE_ELASTOPLASTIC) {
+        km_nonlocal<ACC><<<np, 32, 0, s>>>(A);
+        mark("nonlocal");
+        ++L;
     }
     if (np > 0) {
         km_cons<BASIS, ACC><<<gp, 256, 0, s>>>(A, phase == EP_PHASE_ELASTOPLASTIC);

@@ -39,6 +39,7 @@ struct PM {
     float* l[3];       // GIMP half lengths
     float* dv[9];      // TPIC: velocity gradient of the previous step
     int* p2e_next;     // cell of the position written by the last G2P
+    int* pcell[2];     // [parity] cell of each point (nonlocal averaging: the cell at the step start)
 };
 
 struct NM {

@@ -180,3 +180,42 @@ def _run_engine(e, windows):
     for phase, T in windows:
         t, _ = e.run(phase, T, 10.0, t)
     return t
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("det", [False, True])
+def test_mixed_nonlocal_vs_oracle(oracle_mod, precision, det):
+    """Nonlocal averaging (on by default in the reference, ls = 0.5) in the mixed step."""
+    from epgpu import Engine, ic_slump
+    ic, cfg = ic_slump(*C1)
+    assert cfg["instr"]["nonloc"]["status"]
+    x0 = ic["mpts"].x.copy()
+    o = oracle_mod.Oracle(copy.deepcopy(ic), cfg["instr"])
+    instr = copy.deepcopy(cfg["instr"])
+    instr["gpu"] = {"precision": precision, "jaumann": False, "deterministic": det}
+    e = Engine(copy.deepcopy(ic), instr)
+    _run(o, e, ((0, 1.0), (1, 1.6)))
+    a, b = e.download(), o.download()
+    s, d, r = errors(a, b, x0)
+    ep = float(np.abs(a.epII[1] - b.epII[1]).max() / max(np.abs(b.epII[1]).max(), 1e-300))
+    print(f"{precision} det={det} nonlocal: stress {s:.3e} displacement {d:.3e} epII[2] {ep:.3e} "
+          f"plastic {int((b.dlam != 0).sum())}")
+    assert s < STRESS_TOL and d < DISP_TOL
+    assert ep < 1e-4
+    assert (b.epII[1] != 0).sum() > 0
+
+
+def test_mixed_nonlocal_all_in_one(oracle_mod):
+    # the reference's default switches (nonlocal on) through the whole 15 s workflow
+    from epgpu import ic_slump, slump
+    ic, cfg = ic_slump(*C1)
+    x0 = ic["mpts"].x.copy()
+    cm = copy.deepcopy(cfg)
+    cm["instr"] = _mixed(cfg["instr"], "mixed_df")
+    out_m = slump(ic, cm, workflow="all-in-one")
+    out_o = slump(ic, cfg, workflow="all-in-one", engine_factory=lambda a, b: oracle_mod.Oracle(a, b))
+    s, d, r = errors(out_m["ic"]["mpts"], out_o["ic"]["mpts"], x0)
+    print(f"nonlocal all-in-one ({out_m['steps']} vs {out_o['steps']} steps): stress {s:.3e} displacement {d:.3e} "
+          f"runout {r:.3e}")
+    assert abs(out_m["steps"] - out_o["steps"]) <= 2
+    assert s < 1e-2 and d < 1e-2

@@ -104,7 +104,7 @@ def test_record_mode_pairs_are_exact_labels():
     assert np.all(np.isin(tphi, np.round(np.tan(np.radians([20.0, 7.5])), 5)))
 
 
-def _train_on_step_pairs(l2g, iters=1500):
+def _train_on_step_pairs(l2g, iters=3000):
     """Pairs recorded from the c1 slump plus synthetic trials around the yield surface."""
     from epgpu.mlp import MLP
     import mlp_oracle as mo
@@ -116,7 +116,7 @@ def _train_on_step_pairs(l2g, iters=1500):
     e.run(1, 13.0, 10.0, 10.0)
     n, xr, tr = net.recorded(copy=200_000)
     e.close()
-    xs = mo.sample_trials(300_000, l2g, seed=8, spread=0.5)
+    xs = mo.sample_trials(50_000, l2g, seed=8, spread=0.5)
     ts, _ = mo.label(xs, l2g)
     X = np.concatenate([xr, xs])
     T = np.concatenate([tr, ts])
