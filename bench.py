@@ -368,6 +368,139 @@ def c3_bench(args, rank, ws):
         print(json.dumps(line))
 
 
+def c5_bench(args, rank, ws):
+    """The 3d slump of config 3 with finite-strain Drucker-Prager (phi = 25 deg) and a seeded cohesion
+    field: particle-steps/s of the mixed 3d step with the learned return map (pairs of the exact map
+    recorded during the settle, the network trained on the GPU), the exact-map step and the FP64 step
+    beside it, and the error of the learned run against the FP64 step replayed with the same dt."""
+    import torch
+    from epgpu import Engine, ic_slump
+    from epgpu.mlp import MLP, lambda_over_2G
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    t0 = time.perf_counter()
+    kw = {"basis": {"which": "gimpm", "how": "undeformed", "ghost": True},
+          "fwrk": {"deform": "finite", "trsfr": "tpic", "C_pf": 0.0, "musl": False, "locking": False, "damping": 0.1},
+          "nonloc": {"status": False, "ls": 0.5},
+          "grf": {"status": True, "covariance": "exponential",
+                  "param": {"Ix": [5.0, 5.0, 5.0], "mean": 2.0e4, "cov": 0.3, "min": 1.0e3, "seed": 1234}}}
+    phi = 25.0 * np.pi / 180.0
+    ic, cfg = ic_slump([64.1584, 16.0396, 16.0396], [320, 80, 80], ni=2,
+                       cmpr_over={"E": 1.0e7, "rho0": 2000.0, "phi0": phi, "phir": phi}, **kw)
+    setup_s = time.perf_counter() - t0
+    mesh, mpts, cmpr = ic["mesh"], ic["mpts"], ic["cmpr"]
+    np_ = mpts.nmp
+    g = [0.0, 0.0, -9.81]
+    instr = dict(cfg["instr"])
+    prec = args.precision if args.precision != "fp64" else "mixed_df"
+    instr["gpu"] = {"precision": prec, "jaumann": False}
+    e = Engine(ic, instr)
+    learned = args.rmap == "learned"
+    net, train = None, None
+    if learned:
+        net = MLP(seed=args.seed, l2g=lambda_over_2G(cmpr))
+        net.record_buffer(args.pairs)
+        e.set_return_map(net, "record")
+    e.run(1, args.settle, 10.0, 0.0)
+    host0 = e.download()
+    if learned:
+        nrec = e.return_map_stats()["recorded"]
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        it = args.train_iters
+        losses = [net.train(iters=it, batch=16384, lr=1e-3, seed=1),
+                  net.train(iters=it // 2, batch=16384, lr=2e-4, seed=2),
+                  net.train(iters=it // 2, batch=16384, lr=4e-5, seed=3)]
+        torch.cuda.synchronize()
+        train = {"pairs_recorded": int(nrec), "pairs_kept": int(min(nrec, args.pairs)), "iterations": 2 * it,
+                 "batch": 16384, "seconds": time.perf_counter() - t1, "loss": losses}
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def timed(engine, k, w, clk=None):
+        engine.upload(host0)
+        vm = host0.vmax.copy()
+        seq = []
+        for _ in range(w):
+            seq.append(cfl_dt(mesh, cmpr, vm))
+            vm = engine.step(1, seq[-1], g)
+        engine.profile(True)
+        l0 = engine.stats()["launches"]
+        ms = 0.0
+        if clk:
+            clk.__enter__()
+        for _ in range(k):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            seq.append(cfl_dt(mesh, cmpr, vm))
+            vm = engine.step(1, seq[-1], g)
+            ms += engine.stats()["device_ms"]
+        if clk:
+            clk.__exit__(None, None, None)
+        kt = engine.kernel_times()
+        engine.profile(False)
+        return ms, seq, kt, engine.stats()["launches"] - l0
+
+    clk = Clocks(local)
+    if learned:
+        e.set_return_map(net, "learned")
+    ms, dts, kt, launches = timed(e, args.steps, args.warmup, clk)
+    rstats = e.return_map_stats() if learned else None
+    final = e.download()
+    value = np_ * args.steps / (ms * 1e-3)
+    tot = sum(v[1] for v in kt.values())
+    exact = None
+    if learned:
+        e.set_return_map(None, "exact")
+        ms_x, _, _, _ = timed(e, args.steps, args.warmup)
+        exact = {"value": np_ * args.steps / (ms_x * 1e-3), "unit": "particle-steps/s", "ms_per_step": ms_x / args.steps}
+    e.close()
+    instr64 = dict(cfg["instr"])
+    instr64["gpu"] = {"precision": "fp64", "jaumann": False}
+    e64 = Engine({"mesh": mesh, "mpts": host0.copy(), "cmpr": cmpr}, instr64)
+    t64 = 0.0
+    for dt in dts:
+        e64.step(1, dt, g)
+        t64 += e64.stats()["device_ms"]
+    b = e64.download()
+    e64.close()
+    v64 = np_ * len(dts) / (t64 * 1e-3)
+    bf = bf16_peak()
+    mlp = None
+    if learned and "mlp" in kt:
+        nl_, tot_ = kt["mlp"]
+        slots = (rstats["learned"] + rstats["fallback"]) / max(args.steps + args.warmup, 1)
+        tf = 100608.0 * slots / (tot_ / nl_ * 1e-3) / 1e12
+        mlp = {"bound": "tensor", "points_per_launch": slots, "avg_launch_ms": tot_ / nl_, "achieved": tf,
+               "unit": "TFLOP/s", "peak": bf[0], "frac": tf / bf[0], "peak_source": bf[1]}
+    line = {
+        "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (+f32 pairs)" if prec == "mixed_df" else "f32+f64",
+        "data": "synthetic 3d slump geometry, seeded exponential-covariance cohesion field (mean 20 kPa, CoV 0.3, "
+                "5 m, >= 1 kPa)",
+        "config": {"workload": "3d slump L=[64.1584,16.0396,16.0396], nel=[320,80,80], 2x2x2 points/cell, GIMP "
+                               "(ghost), TPIC (PIC), USL, finite-strain DP (phi=25 deg, E=1e7, rho=2000), "
+                               + ("learned return map" if learned else "exact return map"),
+                   "points": np_, "nodes": mesh.nnodes, "setup_s": setup_s, "settle_s": args.settle,
+                   "precision": prec, "l2": "flushed between timed steps (256 MB write)"},
+        "gpu_launches": launches,
+        "kernel_share": {k: round(v[1] / tot, 4) for k, v in kt.items()},
+        "learned_return_map": ({"train": train, "stats": rstats,
+                                "fallback_rate": rstats["fallback"] / max(rstats["learned"] + rstats["fallback"], 1),
+                                "mlp_roofline": mlp} if learned else None),
+        "exact_map_step": exact,
+        "fp64_step": {"ms_per_step": t64 / len(dts), "value": v64, "unit": "particle-steps/s"},
+        "speedup_vs_fp64_step": value / v64 if t64 > 0 else None,
+        "error_vs_fp64": {"steps": len(dts),
+                          "stress_rel_l2": float(np.linalg.norm(final.tau - b.tau) / np.linalg.norm(b.tau)),
+                          "displacement_rel_l2": float(np.linalg.norm(final.x - b.x) /
+                                                       max(np.linalg.norm(b.x - host0.x), 1e-300))},
+        "clocks": clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -388,8 +521,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--deterministic", action="store_true",
                     help="mixed step without floating-point atomics (bitwise reproducible)")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4"],
-                    help="c2: the nel=[640,160] slump (headline); c3: the 3d slump; c4: the batched ensemble")
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5"],
+                    help="c2: the nel=[640,160] slump (headline); c3: the 3d slump; c4: the batched ensemble; "
+                         "c5: the 3d slump with finite-strain DP and the learned return map")
     ap.add_argument("--instances", type=int, default=256)
     ap.add_argument("--window", type=float, default=0.05, help="simulated seconds timed in the c4 workload")
     ap.add_argument("--no-e2e", action="store_true")
@@ -406,6 +540,9 @@ def main():
         return
     if args.workload == "c3":
         c3_bench(args, rank, ws)
+        return
+    if args.workload == "c5":
+        c5_bench(args, rank, ws)
         return
     import torch
     from epgpu import Engine
@@ -435,10 +572,11 @@ def main():
         t0 = time.perf_counter()
         l1 = net.train(iters=args.train_iters, batch=16384, lr=1e-3, seed=1)
         l2 = net.train(iters=args.train_iters // 2, batch=16384, lr=2e-4, seed=2)
+        l3 = net.train(iters=args.train_iters // 2, batch=16384, lr=4e-5, seed=3)
         torch.cuda.synchronize()
         train = {"pairs_recorded": int(nrec), "pairs_kept": int(min(nrec, args.pairs)),
-                 "iterations": args.train_iters + args.train_iters // 2, "batch": 16384,
-                 "seconds": time.perf_counter() - t0, "loss": [l1, l2]}
+                 "iterations": 2 * args.train_iters, "batch": 16384,
+                 "seconds": time.perf_counter() - t0, "loss": [l1, l2, l3]}
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")   # 256 MB > 129 MB L2
 
     def timed(engine, k, w, clk=None):

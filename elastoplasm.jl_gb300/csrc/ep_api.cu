@@ -222,9 +222,6 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
     }
     if (cfg->precision != EP_PREC_FP64 && cfg->precision != EP_PREC_MIXED && cfg->precision != EP_PREC_MIXED_DF)
         return fail(nullptr, EP_ERR_UNSUPPORTED, "unknown precision");
-    if (cfg->precision != EP_PREC_FP64 && d == 3 && cfg->deform == EP_DEFORM_FINITE)
-        return fail(nullptr, EP_ERR_UNSUPPORTED,
-                    "the mixed-precision 3d step is built for infinitesimal strain; use EP_PREC_FP64 for finite strain in 3d");
     if (cfg->precision != EP_PREC_FP64 && d == 3 && cfg->deterministic)
         return fail(nullptr, EP_ERR_UNSUPPORTED, "the deterministic mode is built for the 2d mixed step");
     if (cfg->precision != EP_PREC_FP64 && cfg->nonloc && d == 3)
@@ -864,9 +861,9 @@ ep_status epgpu_set_return_map(ep_handle* h, ep_mlp* m, int32_t mode) {
         return fail(h, EP_ERR_ARG, "return map mode must be EP_RMAP_EXACT, _LEARNED or _RECORD");
     if (mode != EP_RMAP_EXACT) {
         if (!m) return fail(h, EP_ERR_ARG, "a network is required for the learned and record modes");
-        if (!h->mixed || h->cfg.deform != EP_DEFORM_FINITE || h->cfg.constitutive != EP_CONS_DP || h->dim != 2)
+        if (!h->mixed || h->cfg.deform != EP_DEFORM_FINITE || h->cfg.constitutive != EP_CONS_DP)
             return fail(h, EP_ERR_UNSUPPORTED,
-                        "the learned return map stands in for the 2d finite-strain DP return of the mixed step");
+                        "the learned return map stands in for the finite-strain DP return of the mixed step");
         if (mode == EP_RMAP_RECORD && mlp_record_cap(m) <= 0)
             return fail(h, EP_ERR_STATE, "the network has no record buffer (epgpu_mlp_record_buffer)");
     }
@@ -874,8 +871,9 @@ ep_status epgpu_set_return_map(ep_handle* h, ep_mlp* m, int32_t mode) {
     b.mode = mode;
     if (mode == EP_RMAP_LEARNED) {
         const size_t np = (size_t)std::max(h->np, 1);
+        const size_t naux = h->dim == 2 ? 4 : 12;    // per slot: (cos 2θ, sin 2θ, s, c) or (V, s, c, 0)
         if (!h->rm_buf) {
-            if (dalloc(h, &h->rm_buf, np * (RM_NX + RM_NY + 4)) != cudaSuccess ||
+            if (dalloc(h, &h->rm_buf, np * (RM_NX + RM_NY + naux)) != cudaSuccess ||
                 dalloc(h, &h->rm_int, 2 * np + 2) != cudaSuccess)
                 return fail(h, EP_ERR_NOMEM, "device allocation (learned return map slots)");
         }

@@ -2032,20 +2032,34 @@ __global__ void km_export(MCtx A, P64 Q) {
     Q.Om[p] = J * Q.Om0[p];
     const bool fin = A.cf.deform == EP_DEFORM_FINITE;
     if (fin) {
-        // finite strain (2d): b, τ, σ = τ / J and ϵ = ½ log b (FP64, for output)
+        // finite strain: b, τ, σ = τ / J and ϵ = ½ log b (FP64, for output)
         Q.rho[p] = Q.rho0[p] / J;
         Q.n[p] = 1.0 - 1.0 / J * (1.0 - Q.n0[p]);
-        Q.b[0][p] = B[0]; Q.b[3][p] = B[1]; Q.b[1][p] = B[2]; Q.b[2][p] = B[2];
-        for (int k = 0; k < 3; ++k) {
+        for (int k = 0; k < NS; ++k) {
             Q.tau[k][p] = (double)A.P.tau[k][p];
             Q.sig[k][p] = (double)A.P.tau[k][p] / J;
         }
-        double lam[2], V[4], L[2], R[4];
-        eig_sym2(B[0], B[2], B[1], lam, V);
-        L[0] = ep_log(lam[0]);
-        L[1] = ep_log(lam[1]);
-        vdvt<2>(V, L, R);
-        for (int k = 0; k < 4; ++k) Q.eps[k][p] = 0.5 * R[k];
+        if (D == 2) {
+            Q.b[0][p] = B[0]; Q.b[3][p] = B[1]; Q.b[1][p] = B[2]; Q.b[2][p] = B[2];
+            double lam[2], V[4], L[2], R[4];
+            eig_sym2(B[0], B[2], B[1], lam, V);
+            L[0] = ep_log(lam[0]);
+            L[1] = ep_log(lam[1]);
+            vdvt<2>(V, L, R);
+            for (int k = 0; k < 4; ++k) Q.eps[k][p] = 0.5 * R[k];
+        } else {
+            double Bt[9], lam[3], V[9], L[3], R[9];
+            for (int k = 0; k < 6; ++k) {
+                const int i = sym_i(3, k), j = sym_j(3, k);
+                Bt[i + 3 * j] = B[k];
+                Bt[j + 3 * i] = B[k];
+            }
+            for (int k = 0; k < 9; ++k) Q.b[k][p] = Bt[k];
+            eig_sym3(Bt, lam, V);
+            for (int k = 0; k < 3; ++k) L[k] = ep_log(lam[k]);
+            vdvt<3>(V, L, R);
+            for (int k = 0; k < 9; ++k) Q.eps[k][p] = 0.5 * R[k];
+        }
     } else {
         for (int k = 0; k < NS; ++k) Q.sig[k][p] = (double)A.P.tau[k][p];
     }
@@ -2209,6 +2223,7 @@ __global__ void __launch_bounds__(16 * TC) km_p2g_tile3(MCtx A) {
     const float hx = (float)A.g.h[0], hy = (float)A.g.h[1], hz = (float)A.g.h[2];
     const float gz = (float)A.ctl->g[2];
     const bool tpic = A.cf.trsfr == EP_TRSFR_TPIC;
+    const bool fin = A.cf.deform == EP_DEFORM_FINITE;
     float am[4], ap[3][4], af[3][4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
@@ -2233,7 +2248,7 @@ __global__ void __launch_bounds__(16 * TC) km_p2g_tile3(MCtx A) {
                 axis_w<BASIS>(ax, o, h, 1.f / h, l, s + 8 * d, s + 8 * d + 4, bad);
                 if (tpic) s[34 + d] = o;
             }
-            const float sc = A.P.Om[p];                    // infinitesimal: Ω σ
+            const float sc = fin ? A.P.Om0[p] : A.P.Om[p];  // Ω σ = Ω0 τ (finite) or Ω σ
             s[24] = A.P.mp[p];
             s[25] = A.P.v[0][p];
             s[26] = A.P.v[1][p];
@@ -2465,20 +2480,264 @@ __global__ void __launch_bounds__(256) km_fbar_seg3(MCtx A) {
     if (bad) set_err(A.ctl, EP_ERR_INVALID_POSITION, W.c);
 }
 
-// km_cons3: F-bar, F, infinitesimal elastic predictor (elast.jl:69-80) and J2 / DP returns in 3d,
-// one lane per sorted point
-template <int BASIS, int ACC>
+// ---------------------------------------------------------------------------
+// 3d finite strain.  b_e is kept as its deviation M = b_e - I (formed exactly from the FP64 value
+// or the hi + lo pair), so the eigenvalues mu of M carry the strain to the relative precision of
+// the arithmetic: ε_i = ½ log(1 + mu_i) (elast.jl:51-52).  FP32: cyclic Jacobi on M (Golub & Van
+// Loan, Matrix Computations, sym.Schur2 and the cyclic Jacobi method, the algorithm of ep_scalar.h
+// eig_sym3); FP64 storage ("mixed"): eig_sym3 itself on M in FP64.
+
+// one rotation zeroing a[P][Q] of the symmetric a, accumulated into the columns of v
+template <int P, int Q>
+__device__ __forceinline__ void jrot3f(float (&a)[3][3], float (&v)[3][3]) {
+    constexpr int R = 3 - P - Q;
+    const float apq = a[P][Q];
+    if (apq == 0.f) return;
+    const float th = (a[Q][Q] - a[P][P]) / (2.f * apq);
+    const float t = fabsf(th) > 1.0e15f ? 0.5f / th : copysignf(1.f, th) / (fabsf(th) + sqrtf(1.f + th * th));
+    const float c = 1.f / sqrtf(1.f + t * t), sn = t * c;
+    a[P][P] -= t * apq;
+    a[Q][Q] += t * apq;
+    a[P][Q] = a[Q][P] = 0.f;
+    const float arp = a[R][P], arq = a[R][Q];
+    a[R][P] = a[P][R] = c * arp - sn * arq;
+    a[R][Q] = a[Q][R] = sn * arp + c * arq;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const float vp = v[i][P], vq = v[i][Q];
+        v[i][P] = c * vp - sn * vq;
+        v[i][Q] = sn * vp + c * vq;
+    }
+}
+
+// eigenvalues (diagonal of a on return) and eigenvectors (columns of v) of a symmetric 3x3;
+// sweeps stop once the off-diagonal sum is below 1e-8 of the matrix norm (the eigenvalue error
+// it leaves is below that, Weyl)
+__device__ __forceinline__ void eig3f(float (&a)[3][3], float (&v)[3][3]) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) v[i][j] = i == j ? 1.f : 0.f;
+    const float nrm = fabsf(a[0][0]) + fabsf(a[1][1]) + fabsf(a[2][2]) +
+                      2.f * (fabsf(a[0][1]) + fabsf(a[0][2]) + fabsf(a[1][2]));
+#pragma unroll 1
+    for (int sw = 0; sw < 8; ++sw) {
+        if (fabsf(a[0][1]) + fabsf(a[0][2]) + fabsf(a[1][2]) <= 1.0e-8f * nrm) break;
+        jrot3f<0, 1>(a, v);
+        jrot3f<0, 2>(a, v);
+        jrot3f<1, 2>(a, v);
+    }
+}
+
+// sym index k (Voigt xx, yy, zz, yz, xz, xy) -> (i, j)
+__host__ __device__ constexpr int vi3(int k) { return k < 3 ? k : (k == 3 ? 1 : 0); }
+__host__ __device__ constexpr int vj3(int k) { return k < 3 ? k : (k == 5 ? 1 : 2); }
+
+// Voigt components of V diag(d) V'
+template <typename R>
+__device__ __forceinline__ void vdv3(const R (&V)[3][3], const R* d, R* out) {
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        const int i = vi3(k), j = vj3(k);
+        out[k] = V[i][0] * V[j][0] * d[0] + V[i][1] * V[j][1] * d[1] + V[i][2] * V[j][2] * d[2];
+    }
+}
+
+// b_e = V diag(exp 2ε) V' (DP.jl:63-66) of returned principal log strains, into the point's
+// accumulated storage as I + V diag(expm1 2ε) V'
+template <int ACC, typename R>
+__device__ __forceinline__ void rebuild_b3(const MCtx& A, int p, const R (&V)[3][3], const R* eps) {
+    R d[3], dev[6];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        if (ACC == 0) d[i] = (R)(ep_exp(2.0 * (double)eps[i]) - 1.0);
+        else d[i] = (R)expm1f(2.f * (float)eps[i]);
+    }
+    vdv3<R>(V, d, dev);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        if (ACC == 0) {
+            A.P.bd[k][p] = (k < 3 ? 1.0 : 0.0) + (double)dev[k];
+        } else {
+            float h, l;
+            if (k < 3) {
+                df_one_plus((float)dev[k], h, l);
+            } else {
+                h = (float)dev[k];
+                l = 0.f;
+            }
+            A.P.bh[k][p] = h;
+            A.P.bl[k][p] = l;
+        }
+    }
+}
+
+// b <- ΔF b ΔF' = b + (T + T' + T D'), T = D b (elast.jl:49), then the trial principal log
+// strains ε (elast.jl:51-52) and the eigenvectors V of b (columns)
+template <int ACC, typename R>
+__device__ __forceinline__ void trial_log_strain3(const MCtx& A, int p, const float* D, R (&V)[3][3], R* eps) {
+    float bf[3][3];
+    double Bd[6];
+    float Bh[6], Bl[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        if (ACC == 0) {
+            Bd[k] = A.P.bd[k][p];
+            bf[vi3(k)][vj3(k)] = bf[vj3(k)][vi3(k)] = (float)Bd[k];
+        } else {
+            Bh[k] = A.P.bh[k][p];
+            Bl[k] = A.P.bl[k][p];
+            bf[vi3(k)][vj3(k)] = bf[vj3(k)][vi3(k)] = Bh[k];
+        }
+    }
+    float T[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) T[i][j] = D[i] * bf[0][j] + D[i + 3] * bf[1][j] + D[i + 6] * bf[2][j];
+    R M[3][3];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        const int i = vi3(k), j = vj3(k);
+        const float inc = T[i][j] + T[j][i] + (T[i][0] * D[j] + T[i][1] * D[j + 3] + T[i][2] * D[j + 6]);
+        R m;
+        if (ACC == 0) {
+            Bd[k] += (double)inc;
+            A.P.bd[k][p] = Bd[k];
+            m = (R)(k < 3 ? Bd[k] - 1.0 : Bd[k]);
+        } else {
+            df_add(Bh[k], Bl[k], inc);
+            A.P.bh[k][p] = Bh[k];
+            A.P.bl[k][p] = Bl[k];
+            m = (R)(k < 3 ? (Bh[k] - 1.f) + Bl[k] : Bh[k] + Bl[k]);
+        }
+        M[i][j] = M[j][i] = m;
+    }
+    if (ACC == 0) {
+        double a[9], lam[3], W[9];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) a[i + 3 * j] = (double)M[i][j];
+        eig_sym3(a, lam, W);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            eps[i] = (R)(0.5 * ep_log(1.0 + lam[i]));
+#pragma unroll
+            for (int j = 0; j < 3; ++j) V[i][j] = (R)W[i + 3 * j];
+        }
+    } else {
+        float a[3][3], v[3][3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) a[i][j] = (float)M[i][j];
+        eig3f(a, v);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            eps[i] = (R)(0.5f * log1pf(a[i][i]));
+#pragma unroll
+            for (int j = 0; j < 3; ++j) V[i][j] = (R)v[i][j];
+        }
+    }
+}
+
+// eigenvalues and eigenvectors of the strain tensor of an engineering Voigt strain
+// (xx, yy, zz, 2yz, 2xz, 2xy): tensor_from_voigt(ε, ½) of DP.jl:63-64, FP32 or FP64
+template <typename R>
+__device__ __forceinline__ void eig_voigt3(const float* ev, R (&V)[3][3], R* lam) {
+    if (sizeof(R) == 8) {
+        double a[9], l[3], W[9];
+        a[0] = ev[0]; a[4] = ev[1]; a[8] = ev[2];
+        a[5] = a[7] = 0.5 * (double)ev[3];
+        a[2] = a[6] = 0.5 * (double)ev[4];
+        a[1] = a[3] = 0.5 * (double)ev[5];
+        eig_sym3(a, l, W);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            lam[i] = (R)l[i];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) V[i][j] = (R)W[i + 3 * j];
+        }
+    } else {
+        float a[3][3], v[3][3];
+        a[0][0] = ev[0]; a[1][1] = ev[1]; a[2][2] = ev[2];
+        a[1][2] = a[2][1] = 0.5f * ev[3];
+        a[0][2] = a[2][0] = 0.5f * ev[4];
+        a[0][1] = a[1][0] = 0.5f * ev[5];
+        eig3f(a, v);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            lam[i] = (R)a[i][i];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) V[i][j] = (R)v[i][j];
+        }
+    }
+}
+
+// 3d features of a finite-strain DP trial (ep_rmap.h layout, x7 = 1) from its principal log
+// strains: sorted descending, V's columns with them; aux = V (column-major), s, c
+__device__ __forceinline__ bool rm_features3(const float* eps_in, const float (&Vin)[3][3], float coh, float tphi,
+                                             float Gc, float l2g, float* x, float* aux) {
+    float e[3] = {eps_in[0], eps_in[1], eps_in[2]};
+    int o[3] = {0, 1, 2};
+    auto cswap = [&](int a, int b) {
+        if (e[a] < e[b]) {
+            const float t = e[a]; e[a] = e[b]; e[b] = t;
+            const int q = o[a]; o[a] = o[b]; o[b] = q;
+        }
+    };
+    cswap(0, 1);
+    cswap(1, 2);
+    cswap(0, 1);
+    const float s = coh / (2.f * Gc);
+    const float e1 = e[0] / s, e2 = e[1] / s, e3 = e[2] / s;
+    const float tr = e1 + e2 + e3;
+    const float t1 = l2g * tr + e1, t2 = l2g * tr + e2, t3 = l2g * tr + e3;
+    const float P = (t1 + t2 + t3) * (1.f / 3.f);
+    const float d1 = t1 - P, d2 = t2 - P, d3 = t3 - P;
+    const float tII = sqrtf(0.5f * (d1 * d1 + d2 * d2 + d3 * d3));
+    const float rr = rsqrtf(1.f + tphi * tphi), sphi = tphi * rr, cphi = rr;
+    const float eta = 6.f * sphi / (1.7320508075688772f * (3.f + sphi));
+    const float xi = 6.f * cphi / (1.7320508075688772f * (3.f + sphi));
+    const float fs = tII + eta * P - xi;
+    x[0] = e1; x[1] = e2; x[2] = e3; x[3] = coh * (float)(1.0 / RM_CREF);
+    x[4] = tphi; x[5] = 0.f; x[6] = fmaxf(fs, 0.f); x[7] = 1.f;
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            const int oc = o[c];
+            aux[i + 3 * c] = oc == 0 ? Vin[i][0] : (oc == 1 ? Vin[i][1] : Vin[i][2]);
+        }
+    aux[9] = s;
+    aux[10] = coh;
+    aux[11] = 0.f;
+    return (fs > 0.f && P < xi / eta) || P >= xi / eta;
+}
+
+// km_cons3: F-bar, F, the elastic predictor -- finite (log strain / Kirchhoff, elast.jl:45-56) or
+// infinitesimal (elast.jl:69-80) -- and the J2 / DP returns in 3d, one lane per sorted point.
+// Finite strain works in the principal frame of the trial b_e: with the isotropic stiffness the
+// trial Kirchhoff stress, both returns and b_e = exp(2 Del \ τ) (DP.jl:63-66) are coaxial with it.
+// With the learned return map a trial-yielding DP point is handed to the network as in 2d.
+template <int BASIS, int ACC, bool FIN>
 __global__ void __launch_bounds__(256) km_cons3(MCtx A, int plastic_phase) {
+    using R = typename std::conditional<ACC == 0, double, float>::type;
     EP_ACTIVE(A.ctl);
     const int cur = A.ctl->parity, nxt = cur ^ 1;
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     int nplastic = 0;
     const int n = A.S.start[cur][A.g.ncell];
+    bool emit = false;
+    float fx[RM_NX], fy[RM_NY], fa[12];
+    int fp = 0;
     if (k < n) {
         bool bad = false;
         PtW3 W;
         point3<BASIS>(A, cur, k, n, W, bad);
         const int p = W.p;
+        fp = p;
         const float dtf = (float)A.ctl->dt;
         const bool lock = A.cf.locking;
         float g[9], a = 0.f;
@@ -2489,7 +2748,7 @@ __global__ void __launch_bounds__(256) km_cons3(MCtx A, int plastic_phase) {
         if (A.cf.trsfr == EP_TRSFR_TPIC)
 #pragma unroll
             for (int i = 0; i < 9; ++i) A.P.dv[i][p] = g[i];
-        // F <- ΔF F = F + D F (deform.jl:35-40), with the unscaled ΔF
+        // F <- ΔF F = F + D F (deform.jl:13-16, 35-40), with the unscaled ΔF
         float Fdev[9];     // F - I, exact from the stored state
         if (ACC == 0) {
             double F[9];
@@ -2528,11 +2787,13 @@ __global__ void __launch_bounds__(256) km_cons3(MCtx A, int plastic_phase) {
                 Fdev[i] = dg ? (h[i] - 1.f) + l[i] : h[i] + l[i];
             }
         }
-        // infinitesimal: volume J Ω0 and mass ρ J Ω0 follow J (deform.jl:41-43)
-        const float Jm1 = det1p_m1(Fdev);
-        const float Om = A.P.Om0[p] + A.P.Om0[p] * Jm1;
-        A.P.Om[p] = Om;
-        A.P.mp[p] = A.P.rho[p] * Om;
+        if (!FIN) {
+            // infinitesimal: volume J Ω0 and mass ρ J Ω0 follow J (deform.jl:41-43)
+            const float Jm1 = det1p_m1(Fdev);
+            const float Om = A.P.Om0[p] + A.P.Om0[p] * Jm1;
+            A.P.Om[p] = Om;
+            A.P.mp[p] = A.P.rho[p] * Om;
+        }
         // F-bar: ΔF <- (ΔJ̄/ΔJ)^(1/3) ΔF (volumetric.jl:23-36), increment form
         if (lock) {
             float sm1 = 0.f;      // Σ N - 1 over the existing nodes (GIMP next to a mesh edge)
@@ -2548,75 +2809,342 @@ __global__ void __launch_bounds__(256) km_cons3(MCtx A, int plastic_phase) {
 #pragma unroll
             for (int i = 0; i < 9; ++i) D[i] = D[i] * (1.f + s1) + ((i == 0 || i == 4 || i == 8) ? s1 : 0.f);
         }
-        // σ += Del voigt(sym(ΔF) - I, 2) (+ ωσ - σω for the objective rate)
-        float tt[6], de[6];
+        float tt[6];
+        bool deferred = false, voigt_done = false;
+        if (FIN) {
+            R V[3][3], eps[3];
+            trial_log_strain3<ACC, R>(A, p, D, V, eps);
+            // trial principal Kirchhoff stress τ = Del voigt(ε) (elast.jl:53-54), zero shear
+            float tp[6];
 #pragma unroll
-        for (int i = 0; i < 6; ++i) tt[i] = A.P.tau[i][p];
-        de[0] = D[0]; de[1] = D[4]; de[2] = D[8];
-        de[3] = D[5] + D[7];        // 2 ε_yz
-        de[4] = D[2] + D[6];        // 2 ε_xz
-        de[5] = D[1] + D[3];        // 2 ε_xy
-        float ds[6];
-#pragma unroll
-        for (int i = 0; i < 6; ++i) {
-            float s = 0.f;
-#pragma unroll
-            for (int j = 0; j < 6; ++j) s += A.Del[i + 6 * j] * de[j];
-            ds[i] = s;
-        }
-        if (A.cf.jaumann) {
-            // W = skew(D); ωσ - σω in Voigt components
-            const float w01 = 0.5f * (D[3] - D[1]), w02 = 0.5f * (D[6] - D[2]), w12 = 0.5f * (D[7] - D[5]);
-            const float S[3][3] = {{tt[0], tt[5], tt[4]}, {tt[5], tt[1], tt[3]}, {tt[4], tt[3], tt[2]}};
-            const float Wm[3][3] = {{0.f, w01, w02}, {-w01, 0.f, w12}, {-w02, -w12, 0.f}};
-            float R[3][3];
             for (int i = 0; i < 3; ++i)
-                for (int j = 0; j < 3; ++j) {
-                    float s = 0.f;
-                    for (int q = 0; q < 3; ++q) s += Wm[i][q] * S[q][j] - S[i][q] * Wm[q][j];
-                    R[i][j] = s;
-                }
-            ds[0] += R[0][0]; ds[1] += R[1][1]; ds[2] += R[2][2];
-            ds[3] += R[1][2]; ds[4] += R[0][2]; ds[5] += R[0][1];
-        }
+                tp[i] = A.Del[i] * (float)eps[0] + A.Del[i + 6] * (float)eps[1] + A.Del[i + 12] * (float)eps[2];
+            tp[3] = tp[4] = tp[5] = 0.f;
+            bool yielded = false;
+            if (plastic_phase) {
+                const float ep1f = ACC == 0 ? (float)A.P.ep1d[p] : A.P.ep1h[p] + A.P.ep1l[p];
+                const float ep2 = A.cf.nonloc ? A.P.ep2[p] : ep1f;
+                if (A.cf.cons == EP_CONS_DP) {
+                    if (A.rmode != EP_RMAP_EXACT) {
+                        const float coh = fmaxf(A.P.c0[p] + A.Hp * ep2, A.P.cr[p]);
+                        const float ef[3] = {(float)eps[0], (float)eps[1], (float)eps[2]};
+                        float Vf[3][3];
 #pragma unroll
-        for (int i = 0; i < 6; ++i) tt[i] += ds[i];
-        if (plastic_phase) {
-            const float ep1f = ACC == 0 ? (float)A.P.ep1d[p] : A.P.ep1h[p] + A.P.ep1l[p];
-            const float ep2 = A.cf.nonloc ? A.P.ep2[p] : ep1f;
-            if (A.cf.cons == EP_CONS_DP) {
-                float inc = 0.f;
-                const float dl = dpf6(tt, ep2, A.P.c0[p], A.P.cr[p], A.P.sphi[p], A.P.cphi[p], A.Kc, A.Gc, A.Hp, &inc);
-                A.P.dlam[p] = dl;
-                if (dl != 0.f) {
-                    ++nplastic;
-                    add_ep1<ACC>(A, p, inc);
-                }
-            } else {
-                float newg = 0.f;
-                if (j2f6(tt, ep2, A.P.c0[p], A.P.cr[p], A.Hp, A.Del, &newg)) {
-                    ++nplastic;
-                    if (ACC == 0) {
-                        A.P.ep1d[p] = (double)newg;
+                        for (int i = 0; i < 3; ++i)
+#pragma unroll
+                            for (int j = 0; j < 3; ++j) Vf[i][j] = (float)V[i][j];
+                        const bool ytr = rm_features3(ef, Vf, coh, A.P.tphi[p], A.Gc, A.l2g, fx, fa);
+                        deferred = ytr && A.rmode == EP_RMAP_LEARNED;
+                    }
+                    if (deferred) {
+                        emit = true;              // km_rmap_finish3 writes τ, Δλ, ϵpII and b_e
+                        ++nplastic;
                     } else {
-                        A.P.ep1h[p] = newg;
-                        A.P.ep1l[p] = 0.f;
+                        float inc = 0.f;
+                        const float dl = dpf6(tp, ep2, A.P.c0[p], A.P.cr[p], A.P.sphi[p], A.P.cphi[p], A.Kc, A.Gc,
+                                              A.Hp, &inc);
+                        A.P.dlam[p] = dl;
+                        yielded = dl != 0.f;
+                        if (yielded) add_ep1<ACC>(A, p, inc);
+                        if (yielded && A.rmode == EP_RMAP_RECORD) emit = rm_label(fx, (double)A.l2g, fy) != 0;
+                    }
+                } else {
+                    // J2 (J2.jl:21-76): its flow Del n with the tensor shear components of n is not
+                    // coaxial with the trial, so it runs on the Voigt stress, and b_e is rebuilt
+                    // from a second eigen-decomposition of ε = tensor(Del \ τ, ½)
+                    {
+                        const R td[3] = {(R)tp[0], (R)tp[1], (R)tp[2]};
+                        R tv[6];
+                        vdv3<R>(V, td, tv);
+#pragma unroll
+                        for (int i = 0; i < 6; ++i) tt[i] = (float)tv[i];
+                    }
+                    float newg = 0.f;
+                    if (j2f6(tt, ep2, A.P.c0[p], A.P.cr[p], A.Hp, A.Del, &newg)) {
+                        ++nplastic;
+                        if (ACC == 0) {
+                            A.P.ep1d[p] = (double)newg;
+                        } else {
+                            A.P.ep1h[p] = newg;
+                            A.P.ep1l[p] = 0.f;
+                        }
+                        float ev[6];
+#pragma unroll
+                        for (int i = 0; i < 6; ++i) {
+                            float acc = 0.f;
+#pragma unroll
+                            for (int j = 0; j < 6; ++j) acc += A.Cmp[i + 6 * j] * tt[j];
+                            ev[i] = acc;
+                        }
+                        R W[3][3], lam[3];
+                        eig_voigt3<R>(ev, W, lam);
+                        rebuild_b3<ACC, R>(A, p, W, lam);
+                    }
+                    voigt_done = true;
+                }
+                if (yielded) {
+                    ++nplastic;
+                    // ε = Del \ τ in the principal frame, b = V diag(exp 2ε) V' (DP.jl:63-66)
+                    R er[3];
+#pragma unroll
+                    for (int i = 0; i < 3; ++i)
+                        er[i] = (R)(A.Cmp[i] * tp[0] + A.Cmp[i + 6] * tp[1] + A.Cmp[i + 12] * tp[2]);
+                    rebuild_b3<ACC, R>(A, p, V, er);
+                }
+            }
+            if (!deferred && !voigt_done) {
+                const R td[3] = {(R)tp[0], (R)tp[1], (R)tp[2]};
+                R tv[6];
+                vdv3<R>(V, td, tv);
+#pragma unroll
+                for (int i = 0; i < 6; ++i) tt[i] = (float)tv[i];
+            }
+        } else {
+            // σ += Del voigt(sym(ΔF) - I, 2) (+ ωσ - σω for the objective rate)
+            float de[6];
+#pragma unroll
+            for (int i = 0; i < 6; ++i) tt[i] = A.P.tau[i][p];
+            de[0] = D[0]; de[1] = D[4]; de[2] = D[8];
+            de[3] = D[5] + D[7];        // 2 ε_yz
+            de[4] = D[2] + D[6];        // 2 ε_xz
+            de[5] = D[1] + D[3];        // 2 ε_xy
+            float ds[6];
+#pragma unroll
+            for (int i = 0; i < 6; ++i) {
+                float sacc = 0.f;
+#pragma unroll
+                for (int j = 0; j < 6; ++j) sacc += A.Del[i + 6 * j] * de[j];
+                ds[i] = sacc;
+            }
+            if (A.cf.jaumann) {
+                // W = skew(D); ωσ - σω in Voigt components
+                const float w01 = 0.5f * (D[3] - D[1]), w02 = 0.5f * (D[6] - D[2]), w12 = 0.5f * (D[7] - D[5]);
+                const float S[3][3] = {{tt[0], tt[5], tt[4]}, {tt[5], tt[1], tt[3]}, {tt[4], tt[3], tt[2]}};
+                const float Wm[3][3] = {{0.f, w01, w02}, {-w01, 0.f, w12}, {-w02, -w12, 0.f}};
+                float Rm[3][3];
+                for (int i = 0; i < 3; ++i)
+                    for (int j = 0; j < 3; ++j) {
+                        float sacc = 0.f;
+                        for (int q = 0; q < 3; ++q) sacc += Wm[i][q] * S[q][j] - S[i][q] * Wm[q][j];
+                        Rm[i][j] = sacc;
+                    }
+                ds[0] += Rm[0][0]; ds[1] += Rm[1][1]; ds[2] += Rm[2][2];
+                ds[3] += Rm[1][2]; ds[4] += Rm[0][2]; ds[5] += Rm[0][1];
+            }
+#pragma unroll
+            for (int i = 0; i < 6; ++i) tt[i] += ds[i];
+            if (plastic_phase) {
+                const float ep1f = ACC == 0 ? (float)A.P.ep1d[p] : A.P.ep1h[p] + A.P.ep1l[p];
+                const float ep2 = A.cf.nonloc ? A.P.ep2[p] : ep1f;
+                if (A.cf.cons == EP_CONS_DP) {
+                    float inc = 0.f;
+                    const float dl = dpf6(tt, ep2, A.P.c0[p], A.P.cr[p], A.P.sphi[p], A.P.cphi[p], A.Kc, A.Gc, A.Hp, &inc);
+                    A.P.dlam[p] = dl;
+                    if (dl != 0.f) {
+                        ++nplastic;
+                        add_ep1<ACC>(A, p, inc);
+                    }
+                } else {
+                    float newg = 0.f;
+                    if (j2f6(tt, ep2, A.P.c0[p], A.P.cr[p], A.Hp, A.Del, &newg)) {
+                        ++nplastic;
+                        if (ACC == 0) {
+                            A.P.ep1d[p] = (double)newg;
+                        } else {
+                            A.P.ep1h[p] = newg;
+                            A.P.ep1l[p] = 0.f;
+                        }
                     }
                 }
             }
         }
-        bool okv = true;
+        if (!deferred) {
+            bool okv = true;
 #pragma unroll
-        for (int i = 0; i < 6; ++i) {
-            A.P.tau[i][p] = tt[i];
-            okv = okv && isfinite(tt[i]);
+            for (int i = 0; i < 6; ++i) {
+                A.P.tau[i][p] = tt[i];
+                okv = okv && isfinite(tt[i]);
+            }
+            if (!okv) set_err(A.ctl, EP_ERR_NONFINITE, p);
         }
-        if (!okv) set_err(A.ctl, EP_ERR_NONFINITE, p);
         if (!lock) place_next(A, p, nxt);
         if (bad) set_err(A.ctl, EP_ERR_INVALID_POSITION, W.c);
     }
+    // learned map slots / recorded pairs: one atomic per warp for the warp's points
+    if (FIN && A.rmode != EP_RMAP_EXACT) {
+        const unsigned bal = __ballot_sync(0xffffffffu, emit);
+        if (bal) {
+            const int lane = threadIdx.x & 31;
+            const unsigned below = bal & ((1u << lane) - 1u);
+            if (A.rmode == EP_RMAP_LEARNED) {
+                int base = 0;
+                if (lane == 0) base = atomicAdd(A.rcount, __popc(bal));
+                base = __shfl_sync(0xffffffffu, base, 0);
+                if (emit) {
+                    const int slot = base + __popc(below);
+                    float4* dx = reinterpret_cast<float4*>(A.rx + (size_t)slot * RM_NX);
+                    dx[0] = make_float4(fx[0], fx[1], fx[2], fx[3]);
+                    dx[1] = make_float4(fx[4], fx[5], fx[6], fx[7]);
+                    float4* da = reinterpret_cast<float4*>(A.raux + (size_t)slot * 12);
+                    da[0] = make_float4(fa[0], fa[1], fa[2], fa[3]);
+                    da[1] = make_float4(fa[4], fa[5], fa[6], fa[7]);
+                    da[2] = make_float4(fa[8], fa[9], fa[10], fa[11]);
+                    A.rpt[slot] = fp;
+                }
+            } else {
+                unsigned long long base = 0;
+                if (lane == 0) base = atomicAdd((unsigned long long*)A.rec_count, (unsigned long long)__popc(bal));
+                base = __shfl_sync(0xffffffffu, base, 0);
+                const long long slot = (long long)base + __popc(below);
+                if (emit && slot < A.rec_cap) {
+                    float4* dx = reinterpret_cast<float4*>(A.rx + (size_t)slot * RM_NX);
+                    dx[0] = make_float4(fx[0], fx[1], fx[2], fx[3]);
+                    dx[1] = make_float4(fx[4], fx[5], fx[6], fx[7]);
+                    *reinterpret_cast<float4*>(A.ry + (size_t)slot * RM_NY) = make_float4(fy[0], fy[1], fy[2], fy[3]);
+                }
+            }
+        }
+    }
     const int tot = __reduce_add_sync(0xffffffffu, nplastic);
     if ((threadIdx.x & 31) == 0 && tot) atomicAdd((unsigned long long*)&A.ctl->plastic, (unsigned long long)tot);
+}
+
+// km_rmap_finish3: the network's returned principal strains for the slots of km_cons3 (3d),
+// accepted under the tests of km_rmap_finish (compressive side of the apex, on the yield
+// surface and at the trial mean stress within 1e-3 c, principal order kept, Δλ >= 0)
+template <int ACC>
+__global__ void __launch_bounds__(256) km_rmap_finish3(MCtx A) {
+    using R = typename std::conditional<ACC == 0, double, float>::type;
+    EP_ACTIVE(A.ctl);
+    const int n = *A.rcount;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int nl = 0;
+    bool reject = false;
+    if (i < n) {
+        const float4 x0 = *reinterpret_cast<const float4*>(A.rx + (size_t)i * RM_NX);
+        const float4 x1 = *reinterpret_cast<const float4*>(A.rx + (size_t)i * RM_NX + 4);
+        const float4 y = *reinterpret_cast<const float4*>(A.ry + (size_t)i * RM_NY);
+        const float* ax = A.raux + (size_t)i * 12;
+        const float s = ax[9], coh = ax[10];
+        const float tphi = x1.x, phin = x1.z;
+        const float rr = rsqrtf(1.f + tphi * tphi), sphi = tphi * rr, cphi = rr;
+        const float eta = 6.f * sphi / (1.7320508075688772f * (3.f + sphi));
+        const float xi = 6.f * coh * cphi / (1.7320508075688772f * (3.f + sphi));
+        bool ok = phin >= (float)RM_PHI_MIN && isfinite(y.x) && isfinite(y.y) && isfinite(y.z);
+        float e[3] = {0.f, 0.f, 0.f}, tp[3] = {0.f, 0.f, 0.f}, dl = 0.f;
+        if (ok) {
+            const float xs[3] = {x0.x, x0.y, x0.z};
+            // the correction in the trial's frame (ep_rmap.h rm_frame3); tan ψ = 0: the exact
+            // return shrinks the deviator radially (DP.jl:81-86), so only the component along the
+            // trial deviator q is kept (in 2d this is the deviatoric projection of km_rmap_finish)
+            float fm[3], fq[3], fr[3];
+            rm_frame3<float>(xs[0], xs[1], xs[2], fm, fq, fr);
+            const float c0 = x1.y == 0.f ? 0.f : y.x, c2 = x1.y == 0.f ? 0.f : y.z;
+            float yv[3];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) yv[j] = c0 * fm[j] + y.y * fq[j] + c2 * fr[j];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) e[j] = s * (xs[j] + phin * yv[j]);
+#pragma unroll
+            for (int j = 0; j < 3; ++j) tp[j] = A.Del[j] * e[0] + A.Del[j + 6] * e[1] + A.Del[j + 12] * e[2];
+            const float P = (tp[0] + tp[1] + tp[2]) * (1.f / 3.f);
+            const float d0 = tp[0] - P, d1 = tp[1] - P, d2 = tp[2] - P;
+            const float tII = sqrtf(0.5f * (d0 * d0 + d1 * d1 + d2 * d2));
+            const float fs = tII + eta * P - xi;
+            const float xm = (xs[0] + xs[1] + xs[2]) * (1.f / 3.f);
+            const float q0 = xs[0] - xm, q1 = xs[1] - xm, q2 = xs[2] - xm;
+            const float tIItr = coh * sqrtf(0.5f * (q0 * q0 + q1 * q1 + q2 * q2));
+            dl = (tIItr - tII) / A.Gc;                          // ψ = 0: Δλ = (τII,trial - τII) / G
+            const float Ptr = coh * (A.l2g + (1.f / 3.f)) * (xs[0] + xs[1] + xs[2]);
+            const bool below_apex = tphi > 0.f ? Ptr < coh / tphi : true;
+            ok = fabsf(fs) <= 1.0e-3f * coh && fabsf(P - Ptr) <= 1.0e-3f * coh && dl >= 0.f && e[0] >= e[1] &&
+                 e[1] >= e[2] && below_apex && isfinite(fs);
+        }
+        if (ok) {
+            ++nl;
+            const int p = A.rpt[i];
+            add_ep1<ACC>(A, p, dl * 0.57735026918962576f);
+            A.P.dlam[p] = dl;
+            R V[3][3], er[3], td[3], tv[6];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                er[c] = (R)e[c];
+                td[c] = (R)tp[c];
+#pragma unroll
+                for (int r = 0; r < 3; ++r) V[r][c] = (R)ax[r + 3 * c];
+            }
+            rebuild_b3<ACC, R>(A, p, V, er);
+            vdv3<R>(V, td, tv);
+#pragma unroll
+            for (int k = 0; k < 6; ++k) A.P.tau[k][p] = (float)tv[k];
+        } else {
+            reject = true;
+        }
+    }
+    const unsigned bal = __ballot_sync(0xffffffffu, reject);
+    if (bal) {
+        const int lane = threadIdx.x & 31;
+        int base = 0;
+        if (lane == 0) base = atomicAdd(A.fbcount, __popc(bal));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (reject) A.fblist[base + __popc(bal & ((1u << lane) - 1u))] = i;
+    }
+    const int tl = __reduce_add_sync(0xffffffffu, nl);
+    if ((threadIdx.x & 31) == 0 && tl) atomicAdd(&A.ctl->rm_learned, (unsigned long long)tl);
+}
+
+// km_rmap_fallback3: the exact FP64 return (DP.jl:69-98) of the rejected 3d slots in the principal
+// frame of the trial, then b_e = V diag(exp 2 Del \ τ) V' and τ = V diag(τ) V' in FP64
+template <int ACC>
+__global__ void __launch_bounds__(256) km_rmap_fallback3(MCtx A) {
+    EP_ACTIVE(A.ctl);
+    const int n = *A.fbcount;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) {
+        const int i = A.fblist[k];
+        const float4 x0 = *reinterpret_cast<const float4*>(A.rx + (size_t)i * RM_NX);
+        const float* ax = A.raux + (size_t)i * 12;
+        const int p = A.rpt[i];
+        const double sd = (double)ax[9], coh = (double)ax[10];
+        const double te[3] = {sd * (double)x0.x, sd * (double)x0.y, sd * (double)x0.z};
+        double sv[6], V[3][3];
+        for (int a = 0; a < 3; ++a) sv[a] = A.Deld[a] * te[0] + A.Deld[a + 6] * te[1] + A.Deld[a + 12] * te[2];
+        sv[3] = sv[4] = sv[5] = 0.0;
+        for (int c = 0; c < 3; ++c)
+            for (int r = 0; r < 3; ++r) V[r][c] = (double)ax[r + 3 * c];
+        double inc = 0.0;
+        const double dld = dp_return<6>(sv, 0.0, coh, 0.0, 0.0, (double)A.P.sphi[p], (double)A.P.cphi[p], 0.0, A.Kd,
+                                        A.Gd, &inc);
+        A.P.dlam[p] = (float)dld;
+        add_ep1<ACC>(A, p, (float)inc);
+        if (dld != 0.0) {
+            double er[3];
+            for (int a = 0; a < 3; ++a) er[a] = A.Cmpd[a] * sv[0] + A.Cmpd[a + 6] * sv[1] + A.Cmpd[a + 12] * sv[2];
+            double d[3], dev[6];
+            for (int a = 0; a < 3; ++a) d[a] = ep_exp(2.0 * er[a]) - 1.0;
+            vdv3<double>(V, d, dev);
+            for (int q = 0; q < 6; ++q) {
+                if (ACC == 0) {
+                    A.P.bd[q][p] = (q < 3 ? 1.0 : 0.0) + dev[q];
+                } else {
+                    const double bv = (q < 3 ? 1.0 : 0.0) + dev[q];
+                    const float h = (float)bv;
+                    A.P.bh[q][p] = h;
+                    A.P.bl[q][p] = (float)(bv - (double)h);
+                }
+            }
+        }
+        double tv[6];
+        vdv3<double>(V, sv, tv);
+        bool okv = true;
+        for (int q = 0; q < 6; ++q) {
+            A.P.tau[q][p] = (float)tv[q];
+            okv = okv && isfinite(tv[q]);
+        }
+        if (!okv) set_err(A.ctl, EP_ERR_NONFINITE, p);
+    }
+    const int tf = __reduce_add_sync(0xffffffffu, k < n ? 1 : 0);
+    if ((threadIdx.x & 31) == 0 && tf) atomicAdd(&A.ctl->rm_fallback, (unsigned long long)tf);
 }
 
 template <int BASIS, int ACC>
@@ -2651,11 +3179,22 @@ static void mixed_step3_impl(const MixedCtx& X, int phase, cudaStream_t s) {
         L += 2;
     }
     if (np > 0) {
-        km_cons3<BASIS, ACC><<<gp, 256, 0, s>>>(A, phase == EP_PHASE_ELASTOPLASTIC);
+        if (A.cf.deform == EP_DEFORM_FINITE) km_cons3<BASIS, ACC, true><<<gp, 256, 0, s>>>(A, phase == EP_PHASE_ELASTOPLASTIC);
+        else km_cons3<BASIS, ACC, false><<<gp, 256, 0, s>>>(A, phase == EP_PHASE_ELASTOPLASTIC);
         mark("cons");
         ++L;
+        if (A.rmode == EP_RMAP_LEARNED && X.net && phase == EP_PHASE_ELASTOPLASTIC) {
+            mlp_infer(X.net, A.rx, A.rcount, np, A.ry, s);
+            mark("mlp");
+            km_rmap_finish3<ACC><<<gp, 256, 0, s>>>(A);
+            mark("rmap_finish");
+            km_rmap_fallback3<ACC><<<gp, 256, 0, s>>>(A);
+            mark("rmap_fallback");
+            L += 3;
+        }
     }
-    km_flip<<<1, 1, 0, s>>>(A.ctl, nullptr, nullptr);
+    const bool lrn = A.rmode == EP_RMAP_LEARNED;
+    km_flip<<<1, 1, 0, s>>>(A.ctl, lrn ? A.rcount : nullptr, lrn ? A.fbcount : nullptr);
     ++L;
     if (X.launches) *X.launches += L;
 }
@@ -2838,7 +3377,7 @@ void mixed_ctx_init(void* mem, const Cfg& cf, const Geo& g, Ctl* ctl, const PM& 
     A->acc = acc;
     A->Kd = Kc;
     A->Gd = Gc;
-    A->l2g = (float)(Del[3] / (Del[0] - Del[3]));   // λ / (2G) of the plane-strain stiffness
+    A->l2g = (float)(Del[1] / (Del[0] - Del[1]));   // λ / (2G): Del(2,1) = λ, Del(1,1) = λ + 2G
     A->rmode = EP_RMAP_EXACT;
     A->rx = A->ry = A->raux = nullptr;
     A->rpt = A->rcount = nullptr;

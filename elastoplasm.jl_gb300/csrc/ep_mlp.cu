@@ -539,6 +539,28 @@ __global__ void km_mlp_pack(const float* P, uint8_t* img) {
     }
 }
 
+// mean of the 3 used target columns over the data set (rows: *ndev clamped to N, or N)
+__global__ void km_mlp_tmean(const float* __restrict__ T, long long N, const long long* ndev, double* acc) {
+    const long long n = ndev ? min(*ndev, N) : N;
+    double s[NOUT] = {};
+    for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long long)gridDim.x * blockDim.x)
+#pragma unroll
+        for (int k = 0; k < NOUT; ++k) s[k] += (double)T[(size_t)r * RM_NY + k];
+#pragma unroll
+    for (int k = 0; k < NOUT; ++k) {
+        double v = s[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31) == 0) atomicAdd(&acc[k], v);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&acc[NOUT], (double)n);
+}
+
+__global__ void km_mlp_setbias(float* P, const double* acc) {
+    const int k = threadIdx.x;
+    if (k < NOUT && acc[NOUT] > 0.0) P[OB5 + k] = (float)(acc[k] / acc[NOUT]);
+}
+
 // random mini-batch: rows idx = hash(seed, step, r) mod N of the data set
 __device__ __forceinline__ uint64_t mix64(uint64_t z) {
     z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
@@ -611,6 +633,7 @@ struct ep_mlp {
     const float* graph_dx = nullptr;
     long long graph_n = 0;
     int sms = 0;
+    bool fresh = true;                // initial weights: the first training call sets the output bias
 };
 
 namespace ep {
@@ -763,7 +786,8 @@ static void init_params(std::vector<float>& P, uint64_t seed) {
     P.assign(NPARAM, 0.f);
     for (int l = 1; l <= 5; ++l) {
         const int ni = n_in(l), no = n_out(l);
-        const double sd = std::sqrt((l == 5 ? 1.0 : 2.0) / ni);
+        // He initialisation; the output layer starts 10x smaller (its bias starts at the mean target)
+        const double sd = l == 5 ? 0.1 * std::sqrt(1.0 / ni) : std::sqrt(2.0 / ni);
         for (int k = 0; k < ni * no; ++k) {
             const double u1 = unif(), u2 = unif();
             P[w_off(l) + k] = (float)(sd * std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2));
@@ -810,6 +834,7 @@ ep_status epgpu_mlp_create(uint64_t seed, double lambda_over_2G, ep_mlp** out) {
         epgpu_mlp_destroy(m);
         return st;
     }
+    m->fresh = true;
     *out = m;
     return EP_OK;
 }
@@ -840,6 +865,7 @@ ep_status epgpu_mlp_set_params(ep_mlp* m, const float* p, int64_t n) {
     km_mlp_pack<<<(3 * W * W + 255) / 256, 256, 0, m->s>>>(m->d.P, m->d.img);
     MCK(m, cudaGetLastError());
     MCK(m, cudaStreamSynchronize(m->s));
+    m->fresh = false;
     return EP_OK;
 }
 
@@ -919,6 +945,18 @@ ep_status epgpu_mlp_train(ep_mlp* m, const float* x, const float* t, int64_t n, 
     }
     ep_status st;
     if ((st = ensure_batch(m, batch)) != EP_OK) return st;
+    if (m->fresh) {
+        // first training of the initial weights: the output bias starts at the mean target
+        double* acc = nullptr;
+        MCK(m, cudaMalloc(&acc, (NOUT + 1) * sizeof(double)));
+        tmp.push_back(reinterpret_cast<float*>(acc));
+        MCK(m, cudaMemsetAsync(acc, 0, (NOUT + 1) * sizeof(double), m->s));
+        km_mlp_tmean<<<m->sms, 256, 0, m->s>>>(DT, N, ndev, acc);
+        km_mlp_setbias<<<1, 32, 0, m->s>>>(d.P, acc);
+        km_mlp_pack<<<(3 * W * W + 255) / 256, 256, 0, m->s>>>(d.P, d.img);
+        MCK(m, cudaGetLastError());
+        m->fresh = false;
+    }
     MCK(m, cudaMemsetAsync(d.loss, 0, sizeof(double), m->s));
     // one iteration = gather, forward, backward, Adam, repack; captured once per (data, batch, lr, seed)
     if (!m->train_graph || m->graph_batch != batch || m->graph_lr != lr || m->graph_seed != seed ||

@@ -318,7 +318,9 @@ ep_status epgpu_mlp_forward(ep_mlp* m, const float* x, int64_t n, float* y);
 ep_status epgpu_mlp_grad(ep_mlp* m, const float* x, const float* t, int64_t n, float* grad, double* loss);
 /* `iters` Adam steps (lr, beta 0.9 / 0.999) on mini-batches of `batch` rows drawn
  * with `seed` from the n rows (x, t) in host memory, or from the record buffer
- * when x is NULL.  *loss_out receives the loss of the last mini-batch. */
+ * when x is NULL.  *loss_out receives the loss of the last mini-batch.  The first
+ * call on a network's initial weights (epgpu_mlp_create, not set_params) sets the
+ * output bias to the mean target of the data first. */
 ep_status epgpu_mlp_train(ep_mlp* m, const float* x, const float* t, int64_t n, int32_t iters, int32_t batch,
                           float lr, uint64_t seed, double* loss_out);
 /* Exact FP64 labels of feature rows on the host (the reference's DP return

@@ -122,6 +122,7 @@ def _train_on_step_pairs(l2g, iters=3000):
     T = np.concatenate([tr, ts])
     loss = net.train(X, T, iters=iters, batch=8192, lr=1e-3, seed=3)
     loss = net.train(X, T, iters=iters // 2, batch=8192, lr=2e-4, seed=4)
+    loss = net.train(X, T, iters=iters // 2, batch=8192, lr=4e-5, seed=5)
     return net, n, loss
 
 
@@ -212,6 +213,109 @@ def test_learned_step_against_the_oracle(oracle_mod, trained_net, hp):
     assert results["trained"][0] < 1e-3
     assert results["untrained"][1] > 0.8
     assert results["trained"][1] < 0.5 and results["trained"][1] < 0.5 * results["untrained"][1]
+
+
+C1_3D = ([64.1584, 16.0396, 16.0396], [16, 4, 4])
+WIN_3D = ((0, 2.0), (1, 3.0))
+
+
+def _engine3(precision="mixed_df"):
+    from epgpu import Engine, ic_slump
+    ic, cfg = ic_slump(*C1_3D, nonloc={"status": False, "ls": 0.5})
+    instr = copy.deepcopy(cfg["instr"])
+    instr["gpu"] = {"precision": precision, "jaumann": False}
+    return ic, cfg, Engine(copy.deepcopy(ic), instr)
+
+
+def test_record_mode_pairs_are_exact_labels_3d():
+    """3d finite-strain DP (the reference's defaults in 3d): recorded rows carry three sorted
+    principal strains and the 3d flag, and their targets are the exact outer-cone return."""
+    from epgpu.mlp import MLP, lambda_over_2G
+    import mlp_oracle as mo
+    ic, cfg, e = _engine3()
+    l2g = lambda_over_2G(ic["cmpr"])
+    net = MLP(seed=0, l2g=l2g)
+    net.record_buffer(100_000)
+    e.set_return_map(net, "record")
+    t = 0.0
+    for phase, T in WIN_3D:
+        t, _ = e.run(phase, T, 10.0, t)
+    n, x, tg = net.recorded(copy=100_000)
+    e.close()
+    print(f"3d: recorded {n} pairs")
+    assert n > 100
+    assert np.all(x[:, 7] == 1.0) and np.all(x[:, 0] >= x[:, 1]) and np.all(x[:, 1] >= x[:, 2])
+    y, ok = mo.label(x, l2g)
+    assert ok.all()
+    np.testing.assert_allclose(tg, y, rtol=1e-5, atol=1e-5)
+
+
+@pytest.fixture(scope="module")
+def trained_net_3d():
+    from epgpu.mlp import MLP, lambda_over_2G
+    import mlp_oracle as mo
+    ic, cfg, e = _engine3()
+    l2g = lambda_over_2G(ic["cmpr"])
+    net = MLP(seed=5, l2g=l2g)
+    net.record_buffer(200_000)
+    e.set_return_map(net, "record")
+    t = 0.0
+    for phase, T in ((0, 2.0), (1, 4.0)):
+        t, _ = e.run(phase, T, 10.0, t)
+    n, xr, tr = net.recorded(copy=200_000)
+    e.close()
+    xs = mo.sample_trials(50_000, l2g, seed=8, spread=0.5, dim=3)
+    ts, _ = mo.label(xs, l2g)
+    X, T = np.concatenate([xr, xs]), np.concatenate([tr, ts])
+    net.train(X, T, iters=3000, batch=8192, lr=1e-3, seed=3)
+    net.train(X, T, iters=1500, batch=8192, lr=2e-4, seed=4)
+    loss = net.train(X, T, iters=1500, batch=8192, lr=4e-5, seed=5)
+    return net, n, loss, l2g
+
+
+def test_learned_step_against_the_oracle_3d(oracle_mod, trained_net_3d):
+    """The 3d learned step (network + exact FP64 fallback) against the FP64 oracle, with the
+    trained network's gain over an untrained one in the fallback rate."""
+    from epgpu.mlp import MLP
+    import mlp_oracle as mo
+    net, npairs, loss, l2g = trained_net_3d
+    ic, cfg, _e = _engine3()
+    _e.close()
+    o = oracle_mod.Oracle(copy.deepcopy(ic), cfg["instr"])
+    t = 0.0
+    for phase, T in WIN_3D:
+        t, _ = o.run(phase, T, 10.0, t)
+    b = o.download()
+    results = {}
+    for name, m in (("exact", None), ("untrained", MLP(seed=5, l2g=l2g)), ("trained", net)):
+        _, _, e = _engine3()
+        t = 0.0
+        for phase, T in WIN_3D:
+            if phase == 1 and m is not None:
+                e.set_return_map(m, "learned")
+            t, _ = e.run(phase, T, 10.0, t)
+        a = e.download()
+        st = e.return_map_stats()
+        e.close()
+        frac = st["fallback"] / max(st["learned"] + st["fallback"], 1)
+        results[name] = (_rel(a.tau, b.tau), frac, st)
+        print(f"3d {name}: stress err vs FP64 oracle {results[name][0]:.2e}; fallback {frac:.3f} {st} "
+              f"(trained on {npairs} recorded pairs, final loss {loss:.2e})")
+    assert results["exact"][0] < 1e-5
+    assert results["trained"][0] < 1e-3
+    assert results["untrained"][1] > 0.8
+    assert results["trained"][1] < 0.5 * results["untrained"][1]
+    # accepted outputs on fresh 3d trials: within a few 1e-3 c of the exact return
+    xs = mo.sample_trials(50_000, l2g, seed=21, spread=1.0, dim=3)
+    y = net.forward(xs)
+    ok, tr = mo.accept3(xs, y, l2g)
+    ye, _ = mo.label(xs, l2g)
+    em, q, rr = mo.frame3(xs[:, :3])
+    ce = ye[:, 0:1] * em + ye[:, 1:2] * q + ye[:, 2:3] * rr
+    te = mo.trial_stress3(xs[:, :3].astype(np.float64) + xs[:, 6:7].astype(np.float64) * ce, l2g)
+    err = np.abs(tr - te).max(axis=1)
+    print(f"3d accepted {ok.mean():.3f}; accepted error / c: max {err[ok].max():.2e}")
+    assert ok.mean() > 0.5 and err[ok].max() < 5e-3
 
 
 def test_bounded_wait_reports_a_timeout_and_the_context_survives():
