@@ -293,7 +293,8 @@ def c3_bench(args, rank, ws):
           "fwrk": {"deform": "infinitesimal", "trsfr": "tpic", "C_pf": 0.0, "musl": False, "locking": False,
                    "damping": 0.1},
           "plast": {"status": True, "constitutive": "J2"}, "nonloc": {"status": False, "ls": 0.5}}
-    ic, cfg = ic_slump([64.1584, 16.0396, 16.0396], [320, 80, 80], ni=2,
+    nel = [int(v) for v in args.nel_3d.split(",")]
+    ic, cfg = ic_slump([64.1584, 16.0396, 16.0396], nel, ni=2,
                        cmpr_over={"E": 1.0e7, "rho0": 2000.0, "c0": 5.0e4, "Hp": 1.0e5}, **kw)
     setup_s = time.perf_counter() - t0
     mesh, mpts, cmpr = ic["mesh"], ic["mpts"], ic["cmpr"]
@@ -351,7 +352,7 @@ def c3_bench(args, rank, ws):
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 (+f32 pairs)" if instr["gpu"]["precision"] == "mixed_df" else "f32+f64",
         "data": "synthetic 3d slump geometry, uniform cohesion 50 kPa",
-        "config": {"workload": "3d slump L=[64.1584,16.0396,16.0396], nel=[320,80,80], 2x2x2 points/cell, GIMP "
+        "config": {"workload": f"3d slump L=[64.1584,16.0396,16.0396], nel={nel}, 2x2x2 points/cell, GIMP "
                                "(ghost), TPIC (PIC), USL, infinitesimal J2 (E=1e7, rho=2000, c0=50 kPa, H=1e5)",
                    "points": np_, "nodes": mesh.nnodes, "setup_s": setup_s, "settle_s": args.settle,
                    "precision": instr["gpu"]["precision"], "l2": "flushed between timed steps (256 MB write)"},
@@ -385,7 +386,8 @@ def c5_bench(args, rank, ws):
           "grf": {"status": True, "covariance": "exponential",
                   "param": {"Ix": [5.0, 5.0, 5.0], "mean": 2.0e4, "cov": 0.3, "min": 1.0e3, "seed": 1234}}}
     phi = 25.0 * np.pi / 180.0
-    ic, cfg = ic_slump([64.1584, 16.0396, 16.0396], [320, 80, 80], ni=2,
+    nel = [int(v) for v in args.nel_3d.split(",")]
+    ic, cfg = ic_slump([64.1584, 16.0396, 16.0396], nel, ni=2,
                        cmpr_over={"E": 1.0e7, "rho0": 2000.0, "phi0": phi, "phir": phi}, **kw)
     setup_s = time.perf_counter() - t0
     mesh, mpts, cmpr = ic["mesh"], ic["mpts"], ic["cmpr"]
@@ -478,7 +480,7 @@ def c5_bench(args, rank, ws):
         "vs_baseline": None, "dtype": "f32 (+f32 pairs)" if prec == "mixed_df" else "f32+f64",
         "data": "synthetic 3d slump geometry, seeded exponential-covariance cohesion field (mean 20 kPa, CoV 0.3, "
                 "5 m, >= 1 kPa)",
-        "config": {"workload": "3d slump L=[64.1584,16.0396,16.0396], nel=[320,80,80], 2x2x2 points/cell, GIMP "
+        "config": {"workload": f"3d slump L=[64.1584,16.0396,16.0396], nel={nel}, 2x2x2 points/cell, GIMP "
                                "(ghost), TPIC (PIC), USL, finite-strain DP (phi=25 deg, E=1e7, rho=2000), "
                                + ("learned return map" if learned else "exact return map"),
                    "points": np_, "nodes": mesh.nnodes, "setup_s": setup_s, "settle_s": args.settle,
@@ -524,6 +526,7 @@ def main():
     ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5"],
                     help="c2: the nel=[640,160] slump (headline); c3: the 3d slump; c4: the batched ensemble; "
                          "c5: the 3d slump with finite-strain DP and the learned return map")
+    ap.add_argument("--nel-3d", default="320,80,80", help="cells of the 3d workloads (c3, c5)")
     ap.add_argument("--instances", type=int, default=256)
     ap.add_argument("--window", type=float, default=0.05, help="simulated seconds timed in the c4 workload")
     ap.add_argument("--no-e2e", action="store_true")
