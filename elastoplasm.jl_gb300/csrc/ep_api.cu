@@ -42,11 +42,17 @@ struct ep_handle {
     Ctl* hctl = nullptr;          // pinned mirror
     double* stage = nullptr;      // device staging for AoS transposes
     size_t stage_n = 0;
-    // fields the step never touches, kept on the host for download
-    std::vector<double> u, pp, du, epV;
+    // upload/download: one staging slot per multi-component field (no sync between fields), the
+    // fields the step never touches (u, p, ∇u, ϵpV) on the device as the caller gave them, and
+    // tan/sin/cos of ϕ recomputed only when ϕ changes
+    double* xfer = nullptr;
+    double* pass = nullptr;
+    std::vector<double> phi_cache, tphi_host;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     cudaGraph_t graph_def[2] = {nullptr, nullptr};   // kept: a batch embeds it as a child graph
     long long graph_kernels[2] = {0, 0};
+    cudaGraphExec_t step_graph[2] = {nullptr, nullptr};   // one step (epgpu_step), dt and g from Ctl
+    long long step_kernels[2] = {0, 0};
     long long launches = 0;
     int64_t steps = 0;
     double last_ms = 0.0;
@@ -115,34 +121,36 @@ __global__ void k_soa_to_aos(const double* __restrict__ in, int k, int np, doubl
     for (int c = 0; c < k; ++c) out[(size_t)c + (size_t)k * p] = in[(size_t)c * np + p];
 }
 
-static ep_status put_aos(ep_handle* h, const double* host, int k, double* dev_block) {
-    if (!host) return EP_OK;
+// host AoS field (k components per point) -> device SoA block; multi-component fields go through
+// their own slot of the staging area at `off` (advanced), so the copies and transposes of all
+// fields queue on the stream without waiting for one another
+static ep_status put_aos(ep_handle* h, const double* host, int k, double* dev_block, size_t& off) {
     size_t n = (size_t)k * h->np;
-    if (n == 0) return EP_OK;
+    if (k > 1) off += n;
+    if (!host || n == 0) return EP_OK;
     if (k == 1) {
         CK(h, cudaMemcpyAsync(dev_block, host, n * sizeof(double), cudaMemcpyHostToDevice, h->s));
         return EP_OK;
     }
-    CK(h, cudaMemcpyAsync(h->stage, host, n * sizeof(double), cudaMemcpyHostToDevice, h->s));
-    k_aos_to_soa<<<(h->np + 255) / 256, 256, 0, h->s>>>(h->stage, k, h->np, dev_block);
+    double* st = h->xfer + (off - n);
+    CK(h, cudaMemcpyAsync(st, host, n * sizeof(double), cudaMemcpyHostToDevice, h->s));
+    k_aos_to_soa<<<(h->np + 255) / 256, 256, 0, h->s>>>(st, k, h->np, dev_block);
     CK(h, cudaGetLastError());
-    CK(h, cudaStreamSynchronize(h->s));   // the staging buffer is reused by the next field
     return EP_OK;
 }
 
-static ep_status get_aos(ep_handle* h, const double* dev_block, int k, double* host) {
-    if (!host) return EP_OK;
+static ep_status get_aos(ep_handle* h, const double* dev_block, int k, double* host, size_t& off) {
     size_t n = (size_t)k * h->np;
-    if (n == 0) return EP_OK;
+    if (k > 1) off += n;
+    if (!host || n == 0) return EP_OK;
     if (k == 1) {
         CK(h, cudaMemcpyAsync(host, dev_block, n * sizeof(double), cudaMemcpyDeviceToHost, h->s));
-        CK(h, cudaStreamSynchronize(h->s));
         return EP_OK;
     }
-    k_soa_to_aos<<<(h->np + 255) / 256, 256, 0, h->s>>>(dev_block, k, h->np, h->stage);
+    double* st = h->xfer + (off - n);
+    k_soa_to_aos<<<(h->np + 255) / 256, 256, 0, h->s>>>(dev_block, k, h->np, st);
     CK(h, cudaGetLastError());
-    CK(h, cudaMemcpyAsync(host, h->stage, n * sizeof(double), cudaMemcpyDeviceToHost, h->s));
-    CK(h, cudaStreamSynchronize(h->s));
+    CK(h, cudaMemcpyAsync(host, st, n * sizeof(double), cudaMemcpyDeviceToHost, h->s));
     return EP_OK;
 }
 
@@ -180,8 +188,10 @@ static void drop_graphs(ep_handle* h) {
     for (int i = 0; i < 2; ++i) {
         if (h->graph[i]) cudaGraphExecDestroy(h->graph[i]);
         if (h->graph_def[i]) cudaGraphDestroy(h->graph_def[i]);
+        if (h->step_graph[i]) cudaGraphExecDestroy(h->step_graph[i]);
         h->graph[i] = nullptr;
         h->graph_def[i] = nullptr;
+        h->step_graph[i] = nullptr;
     }
 }
 
@@ -378,6 +388,11 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
     stage_n = std::max<size_t>(stage_n, (size_t)d * h->nnode);
     ok = ok && dalloc(h, &h->stage, stage_n) == cudaSuccess;
     h->stage_n = stage_n;
+    // staging slots of the multi-component point fields: x v l l0 (d each), ϵpII (2), σ τ (ns each),
+    // ∇v ΔF F b ϵ ω σJ (d² each); pass-through u, p (d each), ∇u (d²), ϵpV (1)
+    ok = ok && dalloc(h, &h->xfer, (size_t)(4 * d + 2 + 2 * ns + 7 * d * d) * h->np) == cudaSuccess;
+    ok = ok && dalloc(h, &h->pass, (size_t)(2 * d + d * d + 1) * h->np) == cudaSuccess;
+    if (ok && h->np) ok = cudaMemset(h->pass, 0, (size_t)(2 * d + d * d + 1) * h->np * sizeof(double)) == cudaSuccess;
     Sort& S = h->ctx.S;
     int ntmp = std::max(scan_tmp_ints((int)ncell), scan_tmp_ints((int)nnode));
     ok = ok && dalloc(h, &S.cell_count, ncell) == cudaSuccess && dalloc(h, &S.cell_start, ncell + 1) == cudaSuccess &&
@@ -556,10 +571,6 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
         h->mx.prof = nullptr;
     }
     h->ctx.prof = nullptr;
-    h->u.assign((size_t)d * h->np, 0.0);
-    h->pp.assign((size_t)d * h->np, 0.0);
-    h->du.assign((size_t)d * d * h->np, 0.0);
-    h->epV.assign((size_t)h->np, 0.0);
     cudaError_t e = cudaDeviceSynchronize();
     if (e != cudaSuccess) {
         std::string m = std::string("create: ") + cudaGetErrorString(e);
@@ -580,7 +591,8 @@ ep_status epgpu_upload(ep_handle* h, const ep_mpts_view* m) {
         !m->dJ || !m->dvij)
         return fail(h, EP_ERR_ARG, "a point field read by the step is NULL");
     ep_status st;
-#define PUT(ptr, k, f) if ((st = put_aos(h, (ptr), (k), fld_ptr(h, (f)))) != EP_OK) return st
+    size_t off = 0;
+#define PUT(ptr, k, f) if ((st = put_aos(h, (ptr), (k), fld_ptr(h, (f)), off)) != EP_OK) return st
     PUT(m->x, d, F_X); PUT(m->v, d, F_V); PUT(m->l, d, F_L); PUT(m->l0, d, F_L0);
     PUT(m->n0, 1, F_N0); PUT(m->n, 1, F_N); PUT(m->Omega0, 1, F_OM0); PUT(m->Omega, 1, F_OM); PUT(m->dJ, 1, F_DJ);
     PUT(m->J, 1, F_J); PUT(m->rho0, 1, F_RHO0); PUT(m->rho, 1, F_RHO); PUT(m->c0, 1, F_C0); PUT(m->cr, 1, F_CR);
@@ -588,18 +600,30 @@ ep_status epgpu_upload(ep_handle* h, const ep_mpts_view* m) {
     PUT(m->dvij, d * d, F_DV); PUT(m->dFij, d * d, F_DF); PUT(m->Fij, d * d, F_F); PUT(m->bij, d * d, F_B);
     PUT(m->eij, d * d, F_EPS); PUT(m->wij, d * d, F_W); PUT(m->sJij, d * d, F_SJ);
 #undef PUT
-    // tan/sin/cos of the friction angle, evaluated once on the host (material constants)
-    std::vector<double> t((size_t)3 * h->np);
-    for (int p = 0; p < h->np; ++p) {
-        t[p] = tan(m->phi[p]);
-        t[(size_t)h->np + p] = sin(m->phi[p]);
-        t[(size_t)2 * h->np + p] = cos(m->phi[p]);
+    // tan/sin/cos of the friction angle, evaluated on the host (material constants), again only
+    // when ϕ differs from the last upload
+    const size_t np = (size_t)h->np;
+    if (h->phi_cache.size() != np || (np && std::memcmp(h->phi_cache.data(), m->phi, np * sizeof(double)) != 0)) {
+        CK(h, cudaStreamSynchronize(h->s));          // tphi_host may still be read by the last copy
+        h->tphi_host.resize(3 * np);
+        double* t = h->tphi_host.data();
+        for (size_t p = 0; p < np; ++p) {
+            t[p] = tan(m->phi[p]);
+            t[np + p] = sin(m->phi[p]);
+            t[2 * np + p] = cos(m->phi[p]);
+        }
+        h->phi_cache.assign(m->phi, m->phi + np);
+        CK(h, cudaMemcpyAsync(fld_ptr(h, F_TPHI), t, 3 * np * sizeof(double), cudaMemcpyHostToDevice, h->s));
     }
-    CK(h, cudaMemcpyAsync(fld_ptr(h, F_TPHI), t.data(), t.size() * sizeof(double), cudaMemcpyHostToDevice, h->s));
-    if (m->u) std::memcpy(h->u.data(), m->u, h->u.size() * sizeof(double));
-    if (m->p) std::memcpy(h->pp.data(), m->p, h->pp.size() * sizeof(double));
-    if (m->duij) std::memcpy(h->du.data(), m->duij, h->du.size() * sizeof(double));
-    if (m->epV) std::memcpy(h->epV.data(), m->epV, h->epV.size() * sizeof(double));
+    {
+        const size_t dn = (size_t)d * np;
+        if (m->u) CK(h, cudaMemcpyAsync(h->pass, m->u, dn * sizeof(double), cudaMemcpyHostToDevice, h->s));
+        if (m->p) CK(h, cudaMemcpyAsync(h->pass + dn, m->p, dn * sizeof(double), cudaMemcpyHostToDevice, h->s));
+        if (m->duij)
+            CK(h, cudaMemcpyAsync(h->pass + 2 * dn, m->duij, d * dn * sizeof(double), cudaMemcpyHostToDevice, h->s));
+        if (m->epV)
+            CK(h, cudaMemcpyAsync(h->pass + (2 + d) * dn, m->epV, np * sizeof(double), cudaMemcpyHostToDevice, h->s));
+    }
     std::memset(h->hctl, 0, sizeof(Ctl));
     for (int i = 0; i < d; ++i) {
         double v = m->vmax ? m->vmax[i] : 0.0;
@@ -635,6 +659,26 @@ static ep_status kernel_error(ep_handle* h) {
     return fail(h, (ep_status)e, buf);
 }
 
+// one step captured once per phase: epgpu_step replays it (no per-kernel host launches); the
+// eager path stays for per-kernel profiling (events between kernels)
+static ep_status build_step_graph(ep_handle* h, int phase) {
+    if (h->step_graph[phase]) return EP_OK;
+    cudaGraph_t gr;
+    long long l0 = h->launches;
+    CK(h, cudaStreamBeginCapture(h->s, cudaStreamCaptureModeThreadLocal));
+    launch_ctl_begin_step(h->ctl, h->dim, h->s);
+    if (h->mixed) mixed_step(h->mx, phase, h->s);
+    else fp64_step(h->ctx, phase, h->s);
+    cudaError_t e = cudaStreamEndCapture(h->s, &gr);
+    h->step_kernels[phase] = h->launches - l0 + 1;    // + the control kernel
+    h->launches = l0;
+    if (e != cudaSuccess) return cuda_fail(h, e, "step graph capture");
+    e = cudaGraphInstantiate(&h->step_graph[phase], gr, 0);
+    cudaGraphDestroy(gr);
+    if (e != cudaSuccess) return cuda_fail(h, e, "step graph instantiate");
+    return EP_OK;
+}
+
 ep_status epgpu_step(ep_handle* h, int32_t phase, double dt, const double* g, double* vmax_out) {
     if (!h || !g) return EP_ERR_ARG;
     if (!h->uploaded) return fail(h, EP_ERR_STATE, "step before upload");
@@ -644,22 +688,26 @@ ep_status epgpu_step(ep_handle* h, int32_t phase, double dt, const double* g, do
     h->hctl->dt = dt;
     for (int i = 0; i < 3; ++i) h->hctl->g[i] = i < h->dim ? g[i] : 0.0;
     h->hctl->phase = phase;
+    if (!h->prof.on && (st = build_step_graph(h, phase)) != EP_OK) return st;
     CK(h, cudaMemcpyAsync(h->ctl, h->hctl, sizeof(Ctl), cudaMemcpyHostToDevice, h->s));
     CK(h, cudaEventRecord(h->ev0, h->s));
-    launch_ctl_begin_step(h->ctl, h->dim, h->s);
-    Fp64Ctx ctx = h->ctx;
-    if (h->prof.on) {
+    if (!h->prof.on) {
+        CK(h, cudaGraphLaunch(h->step_graph[phase], h->s));
+        h->launches += h->step_kernels[phase];
+    } else {
+        launch_ctl_begin_step(h->ctl, h->dim, h->s);
+        Fp64Ctx ctx = h->ctx;
         ctx.prof = &h->prof;
         h->prof.begin(h->s);
+        if (h->mixed) {
+            MixedCtx mx = h->mx;
+            mx.prof = &h->prof;
+            mixed_step(mx, phase, h->s);
+        } else {
+            fp64_step(ctx, phase, h->s);
+        }
+        h->launches += 1;
     }
-    if (h->mixed) {
-        MixedCtx mx = h->mx;
-        if (h->prof.on) mx.prof = &h->prof;
-        mixed_step(mx, phase, h->s);
-    } else {
-        fp64_step(ctx, phase, h->s);
-    }
-    h->launches += 1;
     CK(h, cudaEventRecord(h->ev1, h->s));
     CK(h, cudaGetLastError());
     if ((st = read_ctl(h)) != EP_OK) return st;
@@ -744,7 +792,8 @@ ep_status epgpu_download(ep_handle* h, ep_mpts_view* m) {
         CK(h, cudaGetLastError());
     }
     if ((st = read_ctl(h)) != EP_OK) return st;
-#define GET(ptr, k, f) if ((st = get_aos(h, fld_ptr(h, (f)), (k), (ptr))) != EP_OK) return st
+    size_t off = 0;
+#define GET(ptr, k, f) if ((st = get_aos(h, fld_ptr(h, (f)), (k), (ptr), off)) != EP_OK) return st
     GET(m->x, d, F_X); GET(m->v, d, F_V); GET(m->l, d, F_L); GET(m->l0, d, F_L0);
     GET(m->n0, 1, F_N0); GET(m->n, 1, F_N); GET(m->Omega0, 1, F_OM0); GET(m->Omega, 1, F_OM); GET(m->dJ, 1, F_DJ);
     GET(m->J, 1, F_J); GET(m->rho0, 1, F_RHO0); GET(m->rho, 1, F_RHO); GET(m->c0, 1, F_C0); GET(m->cr, 1, F_CR);
@@ -754,10 +803,16 @@ ep_status epgpu_download(ep_handle* h, ep_mpts_view* m) {
 #undef GET
     if (m->vmax)
         for (int i = 0; i < d; ++i) m->vmax[i] = bits_to_double(h->hctl->vmax_bits[i]);
-    if (m->u) std::memcpy(m->u, h->u.data(), h->u.size() * sizeof(double));
-    if (m->p) std::memcpy(m->p, h->pp.data(), h->pp.size() * sizeof(double));
-    if (m->duij) std::memcpy(m->duij, h->du.data(), h->du.size() * sizeof(double));
-    if (m->epV) std::memcpy(m->epV, h->epV.data(), h->epV.size() * sizeof(double));
+    {
+        const size_t np = (size_t)h->np, dn = (size_t)d * np;
+        if (m->u) CK(h, cudaMemcpyAsync(m->u, h->pass, dn * sizeof(double), cudaMemcpyDeviceToHost, h->s));
+        if (m->p) CK(h, cudaMemcpyAsync(m->p, h->pass + dn, dn * sizeof(double), cudaMemcpyDeviceToHost, h->s));
+        if (m->duij)
+            CK(h, cudaMemcpyAsync(m->duij, h->pass + 2 * dn, d * dn * sizeof(double), cudaMemcpyDeviceToHost, h->s));
+        if (m->epV)
+            CK(h, cudaMemcpyAsync(m->epV, h->pass + (2 + d) * dn, np * sizeof(double), cudaMemcpyDeviceToHost, h->s));
+        CK(h, cudaStreamSynchronize(h->s));
+    }
     if (m->p2e || m->p2n) {
         std::vector<int> c(h->np);
         if (h->np) {

@@ -1596,7 +1596,7 @@ __global__ void __launch_bounds__(256) km_rmap_finish(MCtx A) {
 }
 
 // km_rmap_fallback: the exact FP64 return (DP.jl:33-66) of the rejected slots, on the
-// trial stress rebuilt from the slot, then b_e = exp(2 Del \ τ) in FP64
+// trial stress rebuilt from the slot, then b_e = exp(2 Del \ τ) (DP.jl:63-66)
 template <int ACC>
 __global__ void __launch_bounds__(256) km_rmap_fallback(MCtx A) {
     EP_ACTIVE(A.ctl);
@@ -1621,30 +1621,12 @@ __global__ void __launch_bounds__(256) km_rmap_fallback(MCtx A) {
         A.P.dlam[p] = (float)dld;
         add_ep1<ACC>(A, p, (float)inc);
         if (dld != 0.0) {
+            // ε = Del \ τ of the FP64 return, b_e = exp(2ε) as the exact mixed step forms it (deviation
+            // form, rebuild_b): every FP64 instruction costs a warp the FP64 pipe's issue time on GB300
+            // (1/64 of the FP32 rate), and this pass is a one-lane chain
             double ee[3];
             for (int a = 0; a < 3; ++a) ee[a] = A.Cmpd[a] * sv[0] + A.Cmpd[a + 3] * sv[1] + A.Cmpd[a + 6] * sv[2];
-            const double m = 0.5 * (ee[0] + ee[1]), ed = 0.5 * (ee[0] - ee[1]), g = 0.5 * ee[2];
-            const double qq = sqrt(ed * ed + g * g);
-            const double E = ep_exp(2.0 * m);
-            double ch, shs;
-            if (qq < 1.0e-4) {
-                const double q2s = qq * qq;
-                ch = 1.0 + 2.0 * q2s * (1.0 + q2s / 3.0);
-                shs = 2.0 * (1.0 + q2s * (2.0 / 3.0 + q2s * (2.0 / 15.0)));
-            } else {
-                const double ep = ep_exp(2.0 * qq), em2 = 1.0 / ep;
-                ch = 0.5 * (ep + em2);
-                shs = 0.5 * (ep - em2) / qq;
-            }
-            const double b0 = E * (ch + shs * ed), b1 = E * (ch - shs * ed), b2 = E * shs * g;
-            if (ACC == 0) {
-                A.P.bd[0][p] = b0; A.P.bd[1][p] = b1; A.P.bd[2][p] = b2;
-            } else {
-                const float h0 = (float)b0, h1 = (float)b1, h2 = (float)b2;
-                A.P.bh[0][p] = h0; A.P.bl[0][p] = (float)(b0 - (double)h0);
-                A.P.bh[1][p] = h1; A.P.bl[1][p] = (float)(b1 - (double)h1);
-                A.P.bh[2][p] = h2; A.P.bl[2][p] = (float)(b2 - (double)h2);
-            }
+            rebuild_b<ACC>(A, p, (float)ee[0], (float)ee[1], (float)(0.5 * ee[2]));
         }
         const float t0 = (float)sv[0], t1 = (float)sv[1], t2 = (float)sv[2];
         A.P.tau[0][p] = t0;
