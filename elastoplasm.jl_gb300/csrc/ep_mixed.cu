@@ -167,14 +167,15 @@ __device__ __forceinline__ void axis_w(const Axis4& a, float dloc, float h, floa
 template <int BASIS>
 __device__ __forceinline__ float axis_miss(const Axis4& a, float dloc, float h, float lp) {
     float m = 0.f;
-    if (BASIS != EP_BASIS_GIMPM) return m;
+    if (BASIS == EP_BASIS_GIMPM) {
 #pragma unroll
-    for (int k = 0; k < 4; ++k)
-        if (a.cls[k] < 0) {
-            float f, df;
-            gimp32(dloc + h * (float)(1 - k), h, lp, f, df);
-            m += f;
-        }
+        for (int k = 0; k < 4; ++k)
+            if (a.cls[k] < 0) {
+                float f, df;
+                gimp32(dloc + h * (float)(1 - k), h, lp, f, df);
+                m += f;
+            }
+    }
     return m;
 }
 
@@ -1516,6 +1517,41 @@ __global__ void __launch_bounds__(256) km_cons(MCtx A, int plastic_phase) {
     if ((threadIdx.x & 31) == 0 && tot) atomicAdd((unsigned long long*)&A.ctl->plastic, (unsigned long long)tot);
 }
 
+// rmap_fallback_slot: the exact FP64 return (DP.jl:33-66) of the rejected slots, on the
+// trial stress rebuilt from the slot, then b_e = exp(2 Del \ τ) (DP.jl:63-66)
+template <int ACC>
+__device__ __noinline__ void rmap_fallback_slot(const MCtx& A, int i) {
+    const float4 x0 = *reinterpret_cast<const float4*>(A.rx + (size_t)i * RM_NX);
+    const float4 x1 = *reinterpret_cast<const float4*>(A.rx + (size_t)i * RM_NX + 4);
+    const float4 ax = *reinterpret_cast<const float4*>(A.raux + (size_t)i * 4);
+    const int p = A.rpt[i];
+    const float c2 = ax.x, s2 = ax.y, s = ax.z, coh = ax.w;
+    const float tphi = x1.x;
+    const double sd = (double)s;
+    const double q1 = sd * (double)x0.x, q2 = sd * (double)x0.y;
+    const double em = 0.5 * (q1 + q2), r = 0.5 * (q1 - q2);
+    const double te[3] = {em + r * (double)c2, em - r * (double)c2, 2.0 * r * (double)s2};
+    double sv[3];
+    for (int a = 0; a < 3; ++a) sv[a] = A.Deld[a] * te[0] + A.Deld[a + 3] * te[1] + A.Deld[a + 6] * te[2];
+    double inc = 0.0;
+    const double dld = dp_return<3>(sv, 0.0, (double)coh, 0.0, (double)tphi, 0.0, 1.0, 0.0, A.Kd, A.Gd, &inc);
+    A.P.dlam[p] = (float)dld;
+    add_ep1<ACC>(A, p, (float)inc);
+    if (dld != 0.0) {
+        // ε = Del \ τ of the FP64 return, b_e = exp(2ε) as the exact mixed step forms it (deviation
+        // form, rebuild_b): every FP64 instruction costs a warp the FP64 pipe's issue time on GB300
+        // (1/64 of the FP32 rate), and this pass is a one-lane chain
+        double ee[3];
+        for (int a = 0; a < 3; ++a) ee[a] = A.Cmpd[a] * sv[0] + A.Cmpd[a + 3] * sv[1] + A.Cmpd[a + 6] * sv[2];
+        rebuild_b<ACC>(A, p, (float)ee[0], (float)ee[1], (float)(0.5 * ee[2]));
+    }
+    const float t0 = (float)sv[0], t1 = (float)sv[1], t2 = (float)sv[2];
+    A.P.tau[0][p] = t0;
+    A.P.tau[1][p] = t1;
+    A.P.tau[2][p] = t2;
+    if (!(isfinite(t0) && isfinite(t1) && isfinite(t2))) set_err(A.ctl, EP_ERR_NONFINITE, p);
+}
+
 // km_rmap_finish: the network's returned strains for the slots of km_cons, accepted when
 // the trial lies on the compressive side of the apex, the returned stress is on the yield
 // surface and keeps the trial mean stress (both within 1e-3 c), the principal order is
@@ -1524,8 +1560,10 @@ template <int ACC>
 __global__ void __launch_bounds__(256) km_rmap_finish(MCtx A) {
     EP_ACTIVE(A.ctl);
     const int n = *A.rcount;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    int nl = 0;
+    int nl = 0, nf = 0;
+    // grid-stride over the slots (the count is on the device; the grid is a few CTAs per SM)
+    for (int i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x) {
+    const int i = i0 + threadIdx.x;
     bool reject = false;
     if (i < n) {
         const float4 x0 = *reinterpret_cast<const float4*>(A.rx + (size_t)i * RM_NX);
@@ -1582,59 +1620,15 @@ __global__ void __launch_bounds__(256) km_rmap_finish(MCtx A) {
             reject = true;
         }
     }
-    // rejected slots -> the fallback list (one atomic per warp)
-    const unsigned bal = __ballot_sync(0xffffffffu, reject);
-    if (bal) {
-        const int lane = threadIdx.x & 31;
-        int base = 0;
-        if (lane == 0) base = atomicAdd(A.fbcount, __popc(bal));
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (reject) A.fblist[base + __popc(bal & ((1u << lane) - 1u))] = i;
+    // rejected slots: the exact FP64 return right here (a few per thousand slots; the one-lane FP64
+    // chain overlaps the other warps' work instead of a pass of its own)
+    if (reject) {
+        rmap_fallback_slot<ACC>(A, i);
+        ++nf;
     }
-    const int tl = __reduce_add_sync(0xffffffffu, nl);
+    }
+    const int tl = __reduce_add_sync(0xffffffffu, nl), tf = __reduce_add_sync(0xffffffffu, nf);
     if ((threadIdx.x & 31) == 0 && tl) atomicAdd(&A.ctl->rm_learned, (unsigned long long)tl);
-}
-
-// km_rmap_fallback: the exact FP64 return (DP.jl:33-66) of the rejected slots, on the
-// trial stress rebuilt from the slot, then b_e = exp(2 Del \ τ) (DP.jl:63-66)
-template <int ACC>
-__global__ void __launch_bounds__(256) km_rmap_fallback(MCtx A) {
-    EP_ACTIVE(A.ctl);
-    const int n = *A.fbcount;
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < n) {
-        const int i = A.fblist[k];
-        const float4 x0 = *reinterpret_cast<const float4*>(A.rx + (size_t)i * RM_NX);
-        const float4 x1 = *reinterpret_cast<const float4*>(A.rx + (size_t)i * RM_NX + 4);
-        const float4 ax = *reinterpret_cast<const float4*>(A.raux + (size_t)i * 4);
-        const int p = A.rpt[i];
-        const float c2 = ax.x, s2 = ax.y, s = ax.z, coh = ax.w;
-        const float tphi = x1.x;
-        const double sd = (double)s;
-        const double q1 = sd * (double)x0.x, q2 = sd * (double)x0.y;
-        const double em = 0.5 * (q1 + q2), r = 0.5 * (q1 - q2);
-        const double te[3] = {em + r * (double)c2, em - r * (double)c2, 2.0 * r * (double)s2};
-        double sv[3];
-        for (int a = 0; a < 3; ++a) sv[a] = A.Deld[a] * te[0] + A.Deld[a + 3] * te[1] + A.Deld[a + 6] * te[2];
-        double inc = 0.0;
-        const double dld = dp_return<3>(sv, 0.0, (double)coh, 0.0, (double)tphi, 0.0, 1.0, 0.0, A.Kd, A.Gd, &inc);
-        A.P.dlam[p] = (float)dld;
-        add_ep1<ACC>(A, p, (float)inc);
-        if (dld != 0.0) {
-            // ε = Del \ τ of the FP64 return, b_e = exp(2ε) as the exact mixed step forms it (deviation
-            // form, rebuild_b): every FP64 instruction costs a warp the FP64 pipe's issue time on GB300
-            // (1/64 of the FP32 rate), and this pass is a one-lane chain
-            double ee[3];
-            for (int a = 0; a < 3; ++a) ee[a] = A.Cmpd[a] * sv[0] + A.Cmpd[a + 3] * sv[1] + A.Cmpd[a + 6] * sv[2];
-            rebuild_b<ACC>(A, p, (float)ee[0], (float)ee[1], (float)(0.5 * ee[2]));
-        }
-        const float t0 = (float)sv[0], t1 = (float)sv[1], t2 = (float)sv[2];
-        A.P.tau[0][p] = t0;
-        A.P.tau[1][p] = t1;
-        A.P.tau[2][p] = t2;
-        if (!(isfinite(t0) && isfinite(t1) && isfinite(t2))) set_err(A.ctl, EP_ERR_NONFINITE, p);
-    }
-    const int tf = __reduce_add_sync(0xffffffffu, k < n ? 1 : 0);
     if ((threadIdx.x & 31) == 0 && tf) atomicAdd(&A.ctl->rm_fallback, (unsigned long long)tf);
 }
 
@@ -2991,6 +2985,52 @@ __global__ void __launch_bounds__(256) km_cons3(MCtx A, int plastic_phase) {
     if ((threadIdx.x & 31) == 0 && tot) atomicAdd((unsigned long long*)&A.ctl->plastic, (unsigned long long)tot);
 }
 
+// rmap_fallback_slot3: the exact FP64 return (DP.jl:69-98) of the rejected 3d slots in the principal
+// frame of the trial, then b_e = V diag(exp 2 Del \ τ) V' and τ = V diag(τ) V' in FP64
+template <int ACC>
+__device__ __noinline__ void rmap_fallback_slot3(const MCtx& A, int i) {
+    const float4 x0 = *reinterpret_cast<const float4*>(A.rx + (size_t)i * RM_NX);
+    const float* ax = A.raux + (size_t)i * 12;
+    const int p = A.rpt[i];
+    const double sd = (double)ax[9], coh = (double)ax[10];
+    const double te[3] = {sd * (double)x0.x, sd * (double)x0.y, sd * (double)x0.z};
+    double sv[6], V[3][3];
+    for (int a = 0; a < 3; ++a) sv[a] = A.Deld[a] * te[0] + A.Deld[a + 6] * te[1] + A.Deld[a + 12] * te[2];
+    sv[3] = sv[4] = sv[5] = 0.0;
+    for (int c = 0; c < 3; ++c)
+        for (int r = 0; r < 3; ++r) V[r][c] = (double)ax[r + 3 * c];
+    double inc = 0.0;
+    const double dld = dp_return<6>(sv, 0.0, coh, 0.0, 0.0, (double)A.P.sphi[p], (double)A.P.cphi[p], 0.0, A.Kd,
+                                    A.Gd, &inc);
+    A.P.dlam[p] = (float)dld;
+    add_ep1<ACC>(A, p, (float)inc);
+    if (dld != 0.0) {
+        double er[3];
+        for (int a = 0; a < 3; ++a) er[a] = A.Cmpd[a] * sv[0] + A.Cmpd[a + 6] * sv[1] + A.Cmpd[a + 12] * sv[2];
+        double d[3], dev[6];
+        for (int a = 0; a < 3; ++a) d[a] = ep_exp(2.0 * er[a]) - 1.0;
+        vdv3<double>(V, d, dev);
+        for (int q = 0; q < 6; ++q) {
+            if (ACC == 0) {
+                A.P.bd[q][p] = (q < 3 ? 1.0 : 0.0) + dev[q];
+            } else {
+                const double bv = (q < 3 ? 1.0 : 0.0) + dev[q];
+                const float h = (float)bv;
+                A.P.bh[q][p] = h;
+                A.P.bl[q][p] = (float)(bv - (double)h);
+            }
+        }
+    }
+    double tv[6];
+    vdv3<double>(V, sv, tv);
+    bool okv = true;
+    for (int q = 0; q < 6; ++q) {
+        A.P.tau[q][p] = (float)tv[q];
+        okv = okv && isfinite(tv[q]);
+    }
+    if (!okv) set_err(A.ctl, EP_ERR_NONFINITE, p);
+}
+
 // km_rmap_finish3: the network's returned principal strains for the slots of km_cons3 (3d),
 // accepted under the tests of km_rmap_finish (compressive side of the apex, on the yield
 // surface and at the trial mean stress within 1e-3 c, principal order kept, Δλ >= 0)
@@ -2999,8 +3039,9 @@ __global__ void __launch_bounds__(256) km_rmap_finish3(MCtx A) {
     using R = typename std::conditional<ACC == 0, double, float>::type;
     EP_ACTIVE(A.ctl);
     const int n = *A.rcount;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    int nl = 0;
+    int nl = 0, nf = 0;
+    for (int i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x) {
+    const int i = i0 + threadIdx.x;
     bool reject = false;
     if (i < n) {
         const float4 x0 = *reinterpret_cast<const float4*>(A.rx + (size_t)i * RM_NX);
@@ -3063,70 +3104,28 @@ __global__ void __launch_bounds__(256) km_rmap_finish3(MCtx A) {
             reject = true;
         }
     }
-    const unsigned bal = __ballot_sync(0xffffffffu, reject);
-    if (bal) {
-        const int lane = threadIdx.x & 31;
-        int base = 0;
-        if (lane == 0) base = atomicAdd(A.fbcount, __popc(bal));
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (reject) A.fblist[base + __popc(bal & ((1u << lane) - 1u))] = i;
+    // rejected slots: the exact FP64 return right here (a few per thousand slots; the one-lane FP64
+    // chain overlaps the other warps' work instead of a pass of its own)
+    if (reject) {
+        rmap_fallback_slot3<ACC>(A, i);
+        ++nf;
     }
-    const int tl = __reduce_add_sync(0xffffffffu, nl);
+    }
+    const int tl = __reduce_add_sync(0xffffffffu, nl), tf = __reduce_add_sync(0xffffffffu, nf);
     if ((threadIdx.x & 31) == 0 && tl) atomicAdd(&A.ctl->rm_learned, (unsigned long long)tl);
+    if ((threadIdx.x & 31) == 0 && tf) atomicAdd(&A.ctl->rm_fallback, (unsigned long long)tf);
 }
 
-// km_rmap_fallback3: the exact FP64 return (DP.jl:69-98) of the rejected 3d slots in the principal
-// frame of the trial, then b_e = V diag(exp 2 Del \ τ) V' and τ = V diag(τ) V' in FP64
-template <int ACC>
-__global__ void __launch_bounds__(256) km_rmap_fallback3(MCtx A) {
-    EP_ACTIVE(A.ctl);
-    const int n = *A.fbcount;
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < n) {
-        const int i = A.fblist[k];
-        const float4 x0 = *reinterpret_cast<const float4*>(A.rx + (size_t)i * RM_NX);
-        const float* ax = A.raux + (size_t)i * 12;
-        const int p = A.rpt[i];
-        const double sd = (double)ax[9], coh = (double)ax[10];
-        const double te[3] = {sd * (double)x0.x, sd * (double)x0.y, sd * (double)x0.z};
-        double sv[6], V[3][3];
-        for (int a = 0; a < 3; ++a) sv[a] = A.Deld[a] * te[0] + A.Deld[a + 6] * te[1] + A.Deld[a + 12] * te[2];
-        sv[3] = sv[4] = sv[5] = 0.0;
-        for (int c = 0; c < 3; ++c)
-            for (int r = 0; r < 3; ++r) V[r][c] = (double)ax[r + 3 * c];
-        double inc = 0.0;
-        const double dld = dp_return<6>(sv, 0.0, coh, 0.0, 0.0, (double)A.P.sphi[p], (double)A.P.cphi[p], 0.0, A.Kd,
-                                        A.Gd, &inc);
-        A.P.dlam[p] = (float)dld;
-        add_ep1<ACC>(A, p, (float)inc);
-        if (dld != 0.0) {
-            double er[3];
-            for (int a = 0; a < 3; ++a) er[a] = A.Cmpd[a] * sv[0] + A.Cmpd[a + 6] * sv[1] + A.Cmpd[a + 12] * sv[2];
-            double d[3], dev[6];
-            for (int a = 0; a < 3; ++a) d[a] = ep_exp(2.0 * er[a]) - 1.0;
-            vdv3<double>(V, d, dev);
-            for (int q = 0; q < 6; ++q) {
-                if (ACC == 0) {
-                    A.P.bd[q][p] = (q < 3 ? 1.0 : 0.0) + dev[q];
-                } else {
-                    const double bv = (q < 3 ? 1.0 : 0.0) + dev[q];
-                    const float h = (float)bv;
-                    A.P.bh[q][p] = h;
-                    A.P.bl[q][p] = (float)(bv - (double)h);
-                }
-            }
-        }
-        double tv[6];
-        vdv3<double>(V, sv, tv);
-        bool okv = true;
-        for (int q = 0; q < 6; ++q) {
-            A.P.tau[q][p] = (float)tv[q];
-            okv = okv && isfinite(tv[q]);
-        }
-        if (!okv) set_err(A.ctl, EP_ERR_NONFINITE, p);
+// SMs of the current device (grids of the slot kernels, whose counts live on the device)
+static int sm_count() {
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0, v = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess)
+            n = v;
+        if (n <= 0) n = 1;
     }
-    const int tf = __reduce_add_sync(0xffffffffu, k < n ? 1 : 0);
-    if ((threadIdx.x & 31) == 0 && tf) atomicAdd(&A.ctl->rm_fallback, (unsigned long long)tf);
+    return n;
 }
 
 template <int BASIS, int ACC>
@@ -3168,11 +3167,9 @@ static void mixed_step3_impl(const MixedCtx& X, int phase, cudaStream_t s) {
         if (A.rmode == EP_RMAP_LEARNED && X.net && phase == EP_PHASE_ELASTOPLASTIC) {
             mlp_infer(X.net, A.rx, A.rcount, np, A.ry, s);
             mark("mlp");
-            km_rmap_finish3<ACC><<<gp, 256, 0, s>>>(A);
+            km_rmap_finish3<ACC><<<std::min(gp, 4 * sm_count()), 256, 0, s>>>(A);
             mark("rmap_finish");
-            km_rmap_fallback3<ACC><<<gp, 256, 0, s>>>(A);
-            mark("rmap_fallback");
-            L += 3;
+            L += 2;
         }
     }
     const bool lrn = A.rmode == EP_RMAP_LEARNED;
@@ -3260,11 +3257,9 @@ static void mixed_step_impl(const MixedCtx& X, int phase, cudaStream_t s) {
         if (A.rmode == EP_RMAP_LEARNED && X.net && phase == EP_PHASE_ELASTOPLASTIC) {
             mlp_infer(X.net, A.rx, A.rcount, np, A.ry, s);
             mark("mlp");
-            km_rmap_finish<ACC><<<gp, 256, 0, s>>>(A);
+            km_rmap_finish<ACC><<<std::min(gp, 4 * sm_count()), 256, 0, s>>>(A);
             mark("rmap_finish");
-            km_rmap_fallback<ACC><<<gp, 256, 0, s>>>(A);
-            mark("rmap_fallback");
-            L += 3;
+            L += 2;
         }
     }
     if (DET) {
