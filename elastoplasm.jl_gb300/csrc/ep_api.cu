@@ -538,6 +538,13 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
         for (int i = 0; i < d; ++i) nm.vm[i] = g0 + (size_t)(1 + 5 * d + i) * nn;
         nm.dJacc = g0 + (size_t)(1 + 6 * d) * nn;
         nm.dJn = g0 + (size_t)(2 + 6 * d) * nn;
+        float4* pk = nullptr;
+        if (d == 2 && dalloc(h, &pk, (size_t)2 * nn) != cudaSuccess) {
+            epgpu_destroy(h);
+            return fail(nullptr, EP_ERR_NOMEM, "device allocation (packed node values)");
+        }
+        nm.va4 = pk;
+        nm.vg4 = pk ? pk + nn : nullptr;
         h->mx.grid_zero = g0;
         h->mx.grid_zero_bytes = sizeof(float) * (size_t)(1 + 2 * d) * nn;   // m, p, f
         h->mx.sort_zero = sort_zero;

@@ -361,6 +361,10 @@ __global__ void km_solve(MCtx A) {
         A.N.pm[d][n] = 0.f;
     }
     A.N.dJacc[n] = 0.f;
+    if (D == 2) {
+        A.N.va4[n] = make_float4(v[0], v[1], a[0], a[1]);
+        if (!A.cf.musl) A.N.vg4[n] = make_float4(v[0], v[1], 0.f, 0.f);
+    }
 }
 
 // new cell and offset along one direction after a move of the offset o
@@ -627,10 +631,11 @@ __global__ void __launch_bounds__(256) km_g2p_seg(MCtx A) {
                 if (W.az.cls[j] < 0) continue;
                 const int nd = node2(A.g, W.ax, W.az, i, j);
                 const float N = W.wx[i] * W.wz[j];
-                vpx += N * __ldg(&A.N.v[0][nd]);
-                vpz += N * __ldg(&A.N.v[1][nd]);
-                afx += N * __ldg(&A.N.a[0][nd]);
-                afz += N * __ldg(&A.N.a[1][nd]);
+                const float4 q = __ldg(&A.N.va4[nd]);
+                vpx += N * q.x;
+                vpz += N * q.y;
+                afx += N * q.z;
+                afz += N * q.w;
             }
         }
         const int p = W.p;
@@ -940,11 +945,14 @@ __global__ void km_vmusl(MCtx A) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= A.g.nnode) return;
     const float m = A.N.m[n];
+    float vv[3] = {0.f, 0.f, 0.f};
     for (int d = 0; d < A.g.dim; ++d) {
         float v = 0.f;
         if (m != 0.f && !A.g.bcs[(size_t)d * A.g.nnode + n]) v = A.N.pm[d][n] * (1.f / m);
         A.N.vm[d][n] = v;
+        vv[d] = v;
     }
+    if (A.g.dim == 2) A.N.vg4[n] = make_float4(vv[0], vv[1], 0.f, 0.f);
 }
 
 __device__ __forceinline__ void place_next(const MCtx& A, int p, int nxt) {
@@ -1042,7 +1050,6 @@ __global__ void __launch_bounds__(256) km_fbar_seg(MCtx A) {
     const bool live = point_of<BASIS>(A, cur, k, n, W, bad);
     const Seg S = seg_of(W.c);
     const float dtf = (float)A.ctl->dt;
-    float* const* vn = A.cf.musl ? A.N.vm : A.N.v;
     const bool fin = A.cf.deform == EP_DEFORM_FINITE;
     float mdj = 0.f;
     if (live) {
@@ -1055,7 +1062,8 @@ __global__ void __launch_bounds__(256) km_fbar_seg(MCtx A) {
                 if (W.az.cls[j] < 0) continue;
                 const int nd = node2(A.g, W.ax, W.az, i, j);
                 const float Nx = W.dwx[i] * W.wz[j], Nz = W.wx[i] * W.dwz[j];
-                const float vx = __ldg(&vn[0][nd]), vz = __ldg(&vn[1][nd]);
+                const float2 q = __ldg(reinterpret_cast<const float2*>(&A.N.vg4[nd]));
+                const float vx = q.x, vz = q.y;
                 g00 += Nx * vx;
                 g01 += Nz * vx;
                 g10 += Nx * vz;
@@ -1091,7 +1099,9 @@ __global__ void km_dJn(MCtx A) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= A.g.nnode) return;
     const float m = A.N.m[n];
-    A.N.dJn[n] = (m == 0.f) ? 0.f : A.N.dJacc[n] / m;
+    const float dj = (m == 0.f) ? 0.f : A.N.dJacc[n] / m;
+    A.N.dJn[n] = dj;
+    if (A.g.dim == 2) reinterpret_cast<float*>(A.N.vg4)[4 * (size_t)n + 2] = dj;
 }
 
 // FP32 Drucker-Prager (DP.jl:33-98) on Voigt stress s[3]; returns Δλ and its ϵpII increment
@@ -1284,7 +1294,6 @@ __global__ void __launch_bounds__(256) km_cons(MCtx A, int plastic_phase) {
         const float hx = (float)A.g.h[0], hz = (float)A.g.h[1];
         const float dtf = (float)A.ctl->dt;
         bool bad = false;
-        float* const* vn = A.cf.musl ? A.N.vm : A.N.v;
         const bool fin = A.cf.deform == EP_DEFORM_FINITE, lock = A.cf.locking;
         float wx[4], dwx[4], wz[4], dwz[4];
         {
@@ -1302,12 +1311,13 @@ __global__ void __launch_bounds__(256) km_cons(MCtx A, int plastic_phase) {
                 if (az.cls[j] < 0) continue;
                 const int n = node2(A.g, ax, az, i, j);
                 const float Nx = dwx[i] * wz[j], Nz = wx[i] * dwz[j];
-                const float vx = __ldg(&vn[0][n]), vz = __ldg(&vn[1][n]);
+                const float4 q = __ldg(&A.N.vg4[n]);
+                const float vx = q.x, vz = q.y;
                 g00 += Nx * vx;
                 g01 += Nz * vx;
                 g10 += Nx * vz;
                 g11 += Nz * vz;
-                if (lock) a += wx[i] * wz[j] * __ldg(&A.N.dJn[n]);
+                if (lock) a += wx[i] * wz[j] * q.z;
             }
         }
         // D = ΔF - I = dt ∇v, column-major (deform.jl:13)

@@ -47,6 +47,11 @@ struct NM {
     float *p[3], *f[3], *a[3], *v[3], *pm[3], *vm[3];
     float* dJacc;      // Σ N m δJ
     float* dJn;        // nodal δJ = ΔJ_n - 1
+    // 2d: the values the point kernels gather, packed per node so that each of the 16 stencil
+    // nodes is one 16-byte load: (v_x, v_z, a_x, a_z) after the grid update, and (the velocity
+    // ∇v is taken of (v or the mUSL v), δJ_n, 0) for the F-bar and constitutive kernels
+    float4* va4;
+    float4* vg4;
 };
 
 struct SM {
