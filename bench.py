@@ -271,14 +271,31 @@ def batch_bench(args, rank, ws):
     # plastic phase from t = 0 (as the single-slump workload), then the tile autotuner
     b.run(1, args.settle)
     tile, tms = b.autotune(phase=1)
+    tuning = b.tuning()
+    scheme = b.scheme()
     T = args.settle
-    b.run(1, T + 0.01)                                      # warm-up window (graphs with the chosen tile)
+    b.run(1, T + 0.01)                                      # warm-up window (the chosen scheme and tile)
     T += 0.01
     with Clocks(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
         t, ns = b.run(1, T + args.window)
     st = b.stats()
     ps = float((np_i * ns).sum())
     value = ps / (st["device_ms"] * 1e-3)
+    T += args.window
+    # the other schemes over the next windows of the same length, for the record
+    other = []
+    if tuning["kernels_available"]:
+        for oth in ("phases", "persistent", "graphs"):
+            if oth == scheme:
+                continue
+            b.set_scheme(oth)
+            b.run(1, T + 0.01)
+            T += 0.01
+            _, ns2 = b.run(1, T + args.window)
+            T += args.window
+            st2 = b.stats()
+            other.append({"scheme": oth, "value": float((np_i * ns2).sum()) / (st2["device_ms"] * 1e-3),
+                          "unit": "particle-steps/s"})
     line = {
         "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": ws, "steps": int(ns.max()),
         "warmup": 1, "ms_per_step": st["device_ms"] / max(float(ns.mean()), 1.0), "higher_is_better": True,
@@ -289,7 +306,10 @@ def batch_bench(args, rank, ws):
                    "instances": args.instances, "points": int(np_i.sum()), "window_s": args.window,
                    "meshes_drawn_again": int(sum(d[4] for d in desc)),
                    "steps_per_instance": [int(ns.min()), int(ns.max())], "p2g_tile": tile,
-                   "autotune_ms_per_batch_step": tms, "setup_s": setup_s,
+                   "autotune_ms_per_batch_step": tms, "scheme": scheme,
+                   "autotune_ms_by_scheme": {k: ({str(t): v for t, v in d.items()} if isinstance(d, dict) else d)
+                                             for k, d in tuning.items()},
+                   "other_schemes": other, "setup_s": setup_s,
                    "l2": "working set > L2 (129 MB)", "precision": "mixed_df", "return_map": "exact"},
         "gpu_launches": None, "batch_graph_launches": st["graph_launches"], "clocks": clk.summary(),
     }

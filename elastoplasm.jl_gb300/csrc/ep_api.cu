@@ -53,6 +53,7 @@ struct ep_handle {
     long long graph_kernels[2] = {0, 0};
     cudaGraphExec_t step_graph[2] = {nullptr, nullptr};   // one step (epgpu_step), dt and g from Ctl
     long long step_kernels[2] = {0, 0};
+    int graph_gen = 0;            // bumped whenever the captured kernels' arguments change
     long long launches = 0;
     int64_t steps = 0;
     double last_ms = 0.0;
@@ -185,6 +186,7 @@ const char* epgpu_last_error(const ep_handle* h) { return h ? h->err.c_str() : g
 
 // the captured graphs hold the kernels' argument blocks by value: dropped whenever those change
 static void drop_graphs(ep_handle* h) {
+    ++h->graph_gen;
     for (int i = 0; i < 2; ++i) {
         if (h->graph[i]) cudaGraphExecDestroy(h->graph[i]);
         if (h->graph_def[i]) cudaGraphDestroy(h->graph_def[i]);
@@ -1010,6 +1012,17 @@ struct ep_batch {
     double last_ms = 0.0;
     long long launches = 0;
     std::string err;
+    // one persistent kernel for all instances (2d mixed, exact map), else per-instance graphs
+    void* pimpl = nullptr;
+    bool ptried = false;
+    std::string pwhy;
+    int tile = 64;
+    // -1 default (phase kernels when the batch qualifies), 0 instance graphs, 1 persistent kernel,
+    // 2 phase kernels over all instances
+    int scheme = -1;
+    double tune_ms[9] = {};       // autotuner: schemes 0, 1, 2 x tiles 16 / 32 / 64
+    int used_scheme() const { return pimpl ? (scheme < 0 ? 2 : scheme) : 0; }
+    std::vector<int> gens;        // the instances' graph generations the batch graphs were built from
 };
 
 static ep_status bfail(ep_batch* b, ep_status st, const std::string& m) {
@@ -1032,6 +1045,32 @@ static void batch_drop(ep_batch* b) {
             cudaGraphExecDestroy(b->exec[k]);
             b->exec[k] = nullptr;
         }
+    if (b->pimpl) mixed_batch_destroy(b->pimpl);
+    b->pimpl = nullptr;
+    b->ptried = false;
+}
+
+// the persistent kernel's context, when every instance qualifies (built from the instances' current
+// argument blocks; rebuilt after any of them changed)
+static void batch_persistent(ep_batch* b) {
+    const int n = (int)b->h.size();
+    std::vector<int> g(n);
+    for (int i = 0; i < n; ++i) g[i] = b->h[i]->graph_gen;
+    if (g != b->gens) {
+        batch_drop(b);
+        b->gens = g;
+    }
+    if (b->ptried) return;
+    b->ptried = true;
+    std::vector<const MixedCtx*> xs(n);
+    for (int i = 0; i < n; ++i) {
+        if (!b->h[i]->mixed) {
+            b->pwhy = "FP64 instances run on the per-instance graphs";
+            return;
+        }
+        xs[i] = &b->h[i]->mx;
+    }
+    b->pimpl = mixed_batch_create(xs.data(), n, &b->pwhy);
 }
 
 ep_status epgpu_batch_destroy(ep_batch* b) {
@@ -1107,8 +1146,35 @@ ep_status epgpu_batch_download(ep_batch* b, int32_t i, ep_mpts_view* m) {
 }
 
 static ep_status batch_graph(ep_batch* b, int phase) {
+    batch_persistent(b);
     if (b->exec[phase]) return EP_OK;
     const int n = (int)b->h.size();
+    if (b->used_scheme() == 2) {
+        cudaGraph_t g;
+        BCK(b, cudaStreamBeginCapture(b->s, cudaStreamCaptureModeThreadLocal));
+        mixed_batch_phase_steps(b->pimpl, phase == EP_PHASE_ELASTOPLASTIC, GRAPH_STEPS, b->tile, 0, b->s);
+        mixed_batch_flags(b->pimpl, b->dflags, b->s);
+        cudaError_t e = cudaStreamEndCapture(b->s, &g);
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec[phase], g, 0);
+        if (e == cudaSuccess) cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return bfail(b, EP_ERR_CUDA, std::string("phase-kernel batch graph: ") + cudaGetErrorString(e));
+        }
+        return EP_OK;
+    }
+    if (b->used_scheme() == 1) {
+        cudaGraph_t g;
+        BCK(b, cudaGraphCreate(&g, 0));
+        cudaError_t e = mixed_batch_graph(b->pimpl, phase == EP_PHASE_ELASTOPLASTIC, GRAPH_STEPS, b->tile, b->dflags, g);
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec[phase], g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return bfail(b, EP_ERR_CUDA, std::string("persistent batch graph: ") + cudaGetErrorString(e));
+        }
+        return EP_OK;
+    }
     for (int i = 0; i < n; ++i) {
         ep_status st = build_graph(b->h[i], phase);
         if (st != EP_OK) return bfail(b, st, "instance " + std::to_string(i) + ": " + b->h[i]->err);
@@ -1172,10 +1238,13 @@ ep_status epgpu_batch_run(ep_batch* b, int32_t phase, double T, double tg, doubl
         BCK(b, cudaMemcpyAsync(b->hflags, b->dflags, sizeof(int) * n, cudaMemcpyDeviceToHost, b->s));
         BCK(b, cudaStreamSynchronize(b->s));
         bool any = false;
+        bool stuck = false;
         for (int i = 0; i < n; ++i) {
             if (b->hflags[i] & 2) failed = i;
             if (b->hflags[i] & 1) any = true;
+            if (b->hflags[i] & 4) stuck = true;
         }
+        if (stuck) return bfail(b, EP_ERR_TIMEOUT, "persistent batch kernel: a grid barrier wait gave up");
         if (failed >= 0 || !any) break;
         if (launched >= (1 << 24)) return bfail(b, EP_ERR_TIMEOUT, "batch time loop did not reach T");
     }
@@ -1187,7 +1256,7 @@ ep_status epgpu_batch_run(ep_batch* b, int32_t phase, double T, double tg, doubl
     for (int i = 0; i < n; ++i) {
         ep_handle* h = b->h[i];
         if ((st = read_ctl(h)) != EP_OK) return bfail(b, st, h->err);
-        h->launches += launched * h->graph_kernels[phase];
+        h->launches += launched * (b->used_scheme() != 0 ? 1 : h->graph_kernels[phase]);
         h->t = h->hctl->t;
         h->steps += h->hctl->nsteps;
         t_inout[i] = h->hctl->t;
@@ -1221,31 +1290,77 @@ ep_status epgpu_batch_autotune(ep_batch* b, int32_t phase, int32_t* tile_out, do
         h->hctl->dt = 0.0;
         for (int k = 0; k < 3; ++k) h->hctl->g[k] = 0.0;
         h->hctl->phase = phase;
+        h->hctl->active = 1;
+        for (int k = 0; k < 3; ++k) h->hctl->vmax_bits[k] = 0ull;
         BCK(b, cudaMemcpyAsync(h->ctl, h->hctl, sizeof(Ctl), cudaMemcpyHostToDevice, h->s));
         BCK(b, cudaStreamSynchronize(h->s));
     }
-    for (int c = 0; c < 3; ++c) {
-        for (int rep = 0; rep < 4; ++rep) {
-            if (rep == 1) BCK(b, cudaEventRecord(b->ev0, b->s));
-            for (ep_handle* h : b->h) {
-                MixedCtx mx = h->mx;
-                mx.p2g_tile = tiles[c];
-                mx.launches = nullptr;
-                mx.prof = nullptr;
-                launch_ctl_begin_step(h->ctl, h->dim, b->s);
-                mixed_step(mx, phase, b->s);
+    batch_persistent(b);
+    int pick_scheme = 0;
+    for (int k = 0; k < 9; ++k) b->tune_ms[k] = 0.0;
+    // schemes timed: the instances' own step graphs (as child graphs of one batch graph) when the
+    // batch does not qualify for the others; else the persistent kernel and the phase kernels,
+    // each with the control blocks as set above
+    for (int sc = b->pimpl ? 1 : 0; sc < (b->pimpl ? 3 : 1); ++sc) {
+        for (int c = 0; c < 3; ++c) {
+            // scheme 0 as it runs: every instance's step (control kernel + mixed step with this tile)
+            // captured as a child graph of one batch graph with no dependencies between them
+            cudaGraphExec_t tg = nullptr;
+            if (sc == 0) {
+                cudaGraph_t g;
+                BCK(b, cudaGraphCreate(&g, 0));
+                cudaError_t e = cudaSuccess;
+                for (size_t i = 0; i < b->h.size() && e == cudaSuccess; ++i) {
+                    ep_handle* h = b->h[i];
+                    MixedCtx mx = h->mx;
+                    mx.p2g_tile = tiles[c];
+                    mx.launches = nullptr;
+                    mx.prof = nullptr;
+                    cudaGraph_t hg;
+                    e = cudaStreamBeginCapture(b->s, cudaStreamCaptureModeThreadLocal);
+                    if (e == cudaSuccess) {
+                        launch_ctl_begin_step(h->ctl, h->dim, b->s);
+                        mixed_step(mx, phase, b->s);
+                        e = cudaStreamEndCapture(b->s, &hg);
+                    }
+                    if (e == cudaSuccess) {
+                        cudaGraphNode_t node;
+                        e = cudaGraphAddChildGraphNode(&node, g, nullptr, 0, hg);
+                        cudaGraphDestroy(hg);
+                    }
+                }
+                if (e == cudaSuccess) e = cudaGraphInstantiate(&tg, g, 0);
+                cudaGraphDestroy(g);
+                if (e != cudaSuccess) {
+                    cudaGetLastError();
+                    return bfail(b, EP_ERR_CUDA, std::string("autotune graph: ") + cudaGetErrorString(e));
+                }
+            }
+            for (int rep = 0; rep < 4; ++rep) {
+                if (rep == 1) BCK(b, cudaEventRecord(b->ev0, b->s));
+                if (sc == 1) BCK(b, mixed_batch_launch(b->pimpl, phase == EP_PHASE_ELASTOPLASTIC, 1, tiles[c], 1, b->s));
+                else if (sc == 2) mixed_batch_phase_steps(b->pimpl, phase == EP_PHASE_ELASTOPLASTIC, 1, tiles[c], 1, b->s);
+                else BCK(b, cudaGraphLaunch(tg, b->s));
+            }
+            BCK(b, cudaGetLastError());
+            if (tg) {
+                BCK(b, cudaStreamSynchronize(b->s));
+                cudaGraphExecDestroy(tg);
+            }
+            BCK(b, cudaEventRecord(b->ev1, b->s));
+            BCK(b, cudaEventSynchronize(b->ev1));
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, b->ev0, b->ev1);
+            b->tune_ms[3 * sc + c] = ms / 3.0;
+            if (ms < best) {
+                best = ms;
+                pick = tiles[c];
+                pick_scheme = sc;
             }
         }
-        BCK(b, cudaEventRecord(b->ev1, b->s));
-        BCK(b, cudaEventSynchronize(b->ev1));
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, b->ev0, b->ev1);
-        if (ms_out) ms_out[c] = ms / 3.0;
-        if (ms < best) {
-            best = ms;
-            pick = tiles[c];
-        }
     }
+    if (ms_out)
+        for (int c = 0; c < 3; ++c) ms_out[c] = b->tune_ms[3 * pick_scheme + c];
     for (ep_handle* h : b->h) {
         if ((st = read_ctl(h)) != EP_OK) return bfail(b, st, h->err);
         if (h->hctl->err) {
@@ -1255,8 +1370,38 @@ ep_status epgpu_batch_autotune(ep_batch* b, int32_t phase, int32_t* tile_out, do
         h->mx.p2g_tile = pick;
         drop_graphs(h);
     }
+    if (b->pimpl && mixed_batch_error(b->pimpl)) return bfail(b, EP_ERR_TIMEOUT, "persistent batch kernel: a grid barrier wait gave up");
     batch_drop(b);
+    b->tile = pick;
+    b->scheme = pick_scheme;
     if (tile_out) *tile_out = pick;
+    return EP_OK;
+}
+
+int32_t epgpu_batch_scheme(ep_batch* b) {
+    if (!b) return -1;
+    batch_persistent(b);
+    return b->used_scheme();
+}
+
+ep_status epgpu_batch_set_scheme(ep_batch* b, int32_t scheme) {
+    if (!b || scheme < -1 || scheme > 2) return EP_ERR_ARG;
+    batch_persistent(b);
+    if (scheme >= 1 && !b->pimpl) return bfail(b, EP_ERR_UNSUPPORTED, "batch kernels over all instances: " + b->pwhy);
+    for (int k = 0; k < 2; ++k)
+        if (b->exec[k]) {
+            cudaGraphExecDestroy(b->exec[k]);
+            b->exec[k] = nullptr;
+        }
+    b->scheme = scheme;
+    return EP_OK;
+}
+
+ep_status epgpu_batch_tuning(ep_batch* b, double* ms9, int32_t* persistent_available) {
+    if (!b || !ms9) return EP_ERR_ARG;
+    batch_persistent(b);
+    for (int k = 0; k < 9; ++k) ms9[k] = b->tune_ms[k];
+    if (persistent_available) *persistent_available = b->pimpl ? 1 : 0;
     return EP_OK;
 }
 

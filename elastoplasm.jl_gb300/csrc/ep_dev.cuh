@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "../../include/epgpu.h"
 #include "ep_scalar.h"
 
 namespace ep {
@@ -92,6 +93,47 @@ struct Sort {
 
 __device__ __forceinline__ void set_err(Ctl* c, int code, int info) {
     if (atomicCAS(&c->err, 0, code) == 0) c->err_info = info;
+}
+
+// Start of a step of the device time loop (worflow.jl:28-39/74-85): the window is over once t
+// reaches T; dt = min(0.5 max_i h_i / (vmax_i + c), T - t) (physics.jl:21-26), vmax reset, gravity
+// ramped over tg in the elastodynamic phase (physics.jl:60-90).  One thread.
+__device__ __forceinline__ void ctl_begin_run(Ctl* c, int dim, double h0, double h1, double h2, double cw) {
+    if (c->err) {
+        c->active = 0;
+        return;
+    }
+    if (!(c->T > c->t)) {
+        c->active = 0;
+        return;
+    }
+    double hh[3] = {h0, h1, h2};
+    double cm = 0.0;
+    for (int i = 0; i < dim; ++i) {
+        double vm = __longlong_as_double((long long)c->vmax_bits[i]);
+        double q = hh[i] / (vm + cw);
+        if (i == 0 || q > cm || q != q) cm = q;
+    }
+    double a = 0.5 * cm, b = c->T - c->t;
+    c->dt = (a < b) ? a : b;
+    for (int i = 0; i < 3; ++i) c->vmax_bits[i] = 0ull;
+    double G = 9.81;
+    if (c->phase == EP_PHASE_ELASTODYNAMIC && c->t <= c->tg) G = 9.81 * c->t / c->tg;
+    for (int i = 0; i < 3; ++i) c->g[i] = 0.0;
+    c->g[dim - 1] = -G;
+    c->active = 1;
+    c->plastic = 0;
+}
+
+// end of an executed step: t += dt
+__device__ __forceinline__ void ctl_end(Ctl* c) {
+    if (!c->active) return;
+    if (c->err) {
+        c->active = 0;
+        return;
+    }
+    c->t = c->t + c->dt;
+    c->nsteps += 1;
 }
 
 // Element of a point, as p2e2n_{2,3}d computes it (tplgy.jl:43-96):

@@ -730,30 +730,7 @@ __global__ void k_retmap64(Cfg cf, Mat mt, Ctl* ctl, P64 P) {
 // ---------------------------------------------------------------------------
 // control block
 __global__ void k_ctl_begin_run(Ctl* c, int dim, double h0, double h1, double h2, double cw) {
-    if (c->err) {
-        c->active = 0;
-        return;
-    }
-    if (!(c->T > c->t)) {
-        c->active = 0;
-        return;
-    }
-    double hh[3] = {h0, h1, h2};
-    double cm = 0.0;
-    for (int i = 0; i < dim; ++i) {
-        double vm = __longlong_as_double((long long)c->vmax_bits[i]);
-        double q = hh[i] / (vm + cw);
-        if (i == 0 || q > cm || q != q) cm = q;
-    }
-    double a = 0.5 * cm, b = c->T - c->t;
-    c->dt = (a < b) ? a : b;
-    for (int i = 0; i < 3; ++i) c->vmax_bits[i] = 0ull;
-    double G = 9.81;
-    if (c->phase == EP_PHASE_ELASTODYNAMIC && c->t <= c->tg) G = 9.81 * c->t / c->tg;
-    for (int i = 0; i < 3; ++i) c->g[i] = 0.0;
-    c->g[dim - 1] = -G;
-    c->active = 1;
-    c->plastic = 0;
+    ctl_begin_run(c, dim, h0, h1, h2, cw);
 }
 
 __global__ void k_ctl_begin_step(Ctl* c) {
@@ -762,15 +739,7 @@ __global__ void k_ctl_begin_step(Ctl* c) {
     c->plastic = 0;
 }
 
-__global__ void k_ctl_end(Ctl* c) {
-    if (!c->active) return;
-    if (c->err) {
-        c->active = 0;
-        return;
-    }
-    c->t = c->t + c->dt;
-    c->nsteps += 1;
-}
+__global__ void k_ctl_end(Ctl* c) { ctl_end(c); }
 
 void launch_ctl_begin_run(Ctl* ctl, const Geo& g, double c, cudaStream_t s) {
     k_ctl_begin_run<<<1, 1, 0, s>>>(ctl, g.dim, g.h[0], g.h[1], g.h[2], c);

@@ -107,6 +107,14 @@ struct MixedCtx {
     int p2g_tile;             // cells per CTA of the P2G kernel: 16, 32 or 64 (autotuned)
 };
 size_t mixed_ctx_size();
+// persistent batch kernel over n 2d mixed instances (nullptr + reason when the batch is not eligible)
+void* mixed_batch_create(const MixedCtx* const* xs, int n, std::string* why);
+void mixed_batch_destroy(void* b);
+cudaError_t mixed_batch_graph(void* b, int plastic, int steps, int tile, int* dflags, cudaGraph_t g);
+cudaError_t mixed_batch_launch(void* b, int plastic, int steps, int tile, int keep_ctl, cudaStream_t s);
+int mixed_batch_error(void* b);
+void mixed_batch_phase_steps(void* b, int plastic, int steps, int tile, int keep_ctl, cudaStream_t s);
+void mixed_batch_flags(void* b, int* dflags, cudaStream_t s);
 void mixed_ctx_init(void* mem, const Cfg& cf, const Geo& g, Ctl* ctl, const PM& P, const NM& N, const SM& S,
                     const double* Del, const double* Cmp, double Kc, double Gc, double Hp, double c, int acc);
 void mixed_step(const MixedCtx& X, int phase, cudaStream_t s);

@@ -328,9 +328,9 @@ __global__ void __launch_bounds__(256) km_p2g(MCtx A) {
 }
 
 // km_solve: grid momentum update with damping and Dirichlet masks (solve.jl:14-40), 2d and 3d
-__global__ void km_solve(MCtx A) {
+__device__ __forceinline__ void solve_body(const MCtx& A, int bid) {
     EP_ACTIVE(A.ctl);
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = bid * blockDim.x + threadIdx.x;
     if (n >= A.g.nnode) return;
     const int D = A.g.dim;
     const float dt = (float)A.ctl->dt, eta = (float)A.cf.damping;
@@ -366,6 +366,9 @@ __global__ void km_solve(MCtx A) {
         if (!A.cf.musl) A.N.vg4[n] = make_float4(v[0], v[1], 0.f, 0.f);
     }
 }
+
+__global__ void km_solve(MCtx A) { solve_body(A, blockIdx.x); }
+
 
 // new cell and offset along one direction after a move of the offset o
 // (relative to node e of the old cell), clamped to the mesh like tplgy.jl:49
@@ -607,11 +610,11 @@ __global__ void __launch_bounds__(256) km_p2g_seg(MCtx A) {
 // km_g2p_seg: PIC/FLIP (n2p.jl:14-40), new cell + offset, vmax, next-cell counts
 // (tplgy.jl:43-62) and the mUSL momentum P2G (augm.jl:13-25), one lane per point
 template <int BASIS, bool DET>
-__global__ void __launch_bounds__(256) km_g2p_seg(MCtx A) {
+__device__ __forceinline__ void g2p_seg_body(const MCtx& A, int bid) {
     EP_ACTIVE(A.ctl);
     const int cur = A.ctl->parity, nxt = cur ^ 1;
     const int n = A.S.start[cur][A.g.ncell];
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int k = bid * blockDim.x + threadIdx.x;
     bool bad = false;
     PtW W;
     const bool live = point_of<BASIS>(A, cur, k, n, W, bad);
@@ -631,7 +634,7 @@ __global__ void __launch_bounds__(256) km_g2p_seg(MCtx A) {
                 if (W.az.cls[j] < 0) continue;
                 const int nd = node2(A.g, W.ax, W.az, i, j);
                 const float N = W.wx[i] * W.wz[j];
-                const float4 q = __ldg(&A.N.va4[nd]);
+                const float4 q = A.N.va4[nd];
                 vpx += N * q.x;
                 vpz += N * q.y;
                 afx += N * q.z;
@@ -692,6 +695,12 @@ __global__ void __launch_bounds__(256) km_g2p_seg(MCtx A) {
     }
 }
 
+template <int BASIS, bool DET>
+__global__ void __launch_bounds__(256) km_g2p_seg(MCtx A) {
+    g2p_seg_body<BASIS, DET>(A, blockIdx.x);
+}
+
+
 // km_p2g_tile: m, p, f (p2n.jl:135-155 std, 217-240 tpic).  A CTA owns TP_CELLS
 // (16, 32 or 64: the tile shape the autotuner picks) consecutive cells, whose
 // points form one slice of the sorted list.  The slice
@@ -702,13 +711,19 @@ __global__ void __launch_bounds__(256) km_g2p_seg(MCtx A) {
 // FP32 atomic per node and quantity.
 constexpr int TP_STRIDE = 29;   // floats per staged point (odd: no bank conflicts)
 
-template <int BASIS, int TP_CELLS, bool DET>
-__global__ void __launch_bounds__(4 * TP_CELLS) km_p2g_tile(MCtx A) {
-    constexpr int TP_THREADS = 4 * TP_CELLS;
+// NT: threads of the block (the staging width); 4 TP_CELLS of them accumulate, the rest only stage
+template <int BASIS, int TP_CELLS, bool DET, int NT = 4 * TP_CELLS>
+__device__ __forceinline__ void p2g_tile_body(const MCtx& A, int bid) {
+    static_assert(NT >= 4 * TP_CELLS, "a P2G tile needs 4 lanes per cell");
+    constexpr int TP_THREADS = NT;
+    if (blockDim.x != NT) {                  // launch shape and body disagree: report, touch nothing
+        if (threadIdx.x == 0) set_err(A.ctl, EP_ERR_ARG, -1);
+        return;
+    }
     EP_ACTIVE(A.ctl);
     __shared__ float sp[TP_THREADS * TP_STRIDE];
     const int cur = A.ctl->parity;
-    const int c0 = blockIdx.x * TP_CELLS;
+    const int c0 = bid * TP_CELLS;
     if (c0 >= A.g.ncell) return;
     const int c1 = min(c0 + TP_CELLS, A.g.ncell);
     const int* start = A.S.start[cur];
@@ -817,6 +832,12 @@ __global__ void __launch_bounds__(4 * TP_CELLS) km_p2g_tile(MCtx A) {
         atomicAdd(&A.N.f[1][n], afz[j]);
     }
 }
+
+template <int BASIS, int TP_CELLS, bool DET>
+__global__ void __launch_bounds__(4 * TP_CELLS) km_p2g_tile(MCtx A) {
+    p2g_tile_body<BASIS, TP_CELLS, DET>(A, blockIdx.x);
+}
+
 
 // Deterministic scatters of the mUSL momentum (KIND 1: m v per point, augm.jl:13-25) and of
 // Σ N m δJ (KIND 2: the per-point value left in ptmp by km_fbar_seg, volumetric.jl:1-11): the
@@ -940,9 +961,9 @@ __global__ void km_sort_cells(MCtx A, int which) {
 }
 
 // km_vmusl: mUSL nodal velocity v = p/m with Dirichlet masks (augm.jl:37-53)
-__global__ void km_vmusl(MCtx A) {
+__device__ __forceinline__ void vmusl_body(const MCtx& A, int bid) {
     EP_ACTIVE(A.ctl);
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = bid * blockDim.x + threadIdx.x;
     if (n >= A.g.nnode) return;
     const float m = A.N.m[n];
     float vv[3] = {0.f, 0.f, 0.f};
@@ -954,6 +975,9 @@ __global__ void km_vmusl(MCtx A) {
     }
     if (A.g.dim == 2) A.N.vg4[n] = make_float4(vv[0], vv[1], 0.f, 0.f);
 }
+
+__global__ void km_vmusl(MCtx A) { vmusl_body(A, blockIdx.x); }
+
 
 __device__ __forceinline__ void place_next(const MCtx& A, int p, int nxt) {
     const int c2 = A.P.p2e_next[p];
@@ -1040,11 +1064,11 @@ __global__ void __launch_bounds__(256) km_fbar(MCtx A) {
 // km_fbar_seg: δJ = det(I + dt ∇v) - 1 and its P2G Σ N m δJ (deform.jl:9-18,
 // volumetric.jl:1-11), one lane per point; places the points into the next lists
 template <int BASIS, bool DET>
-__global__ void __launch_bounds__(256) km_fbar_seg(MCtx A) {
+__device__ __forceinline__ void fbar_seg_body(const MCtx& A, int bid) {
     EP_ACTIVE(A.ctl);
     const int cur = A.ctl->parity, nxt = cur ^ 1;
     const int n = A.S.start[cur][A.g.ncell];
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int k = bid * blockDim.x + threadIdx.x;
     bool bad = false;
     PtW W;
     const bool live = point_of<BASIS>(A, cur, k, n, W, bad);
@@ -1062,7 +1086,7 @@ __global__ void __launch_bounds__(256) km_fbar_seg(MCtx A) {
                 if (W.az.cls[j] < 0) continue;
                 const int nd = node2(A.g, W.ax, W.az, i, j);
                 const float Nx = W.dwx[i] * W.wz[j], Nz = W.wx[i] * W.dwz[j];
-                const float2 q = __ldg(reinterpret_cast<const float2*>(&A.N.vg4[nd]));
+                const float2 q = *reinterpret_cast<const float2*>(&A.N.vg4[nd]);
                 const float vx = q.x, vz = q.y;
                 g00 += Nx * vx;
                 g01 += Nz * vx;
@@ -1093,16 +1117,25 @@ __global__ void __launch_bounds__(256) km_fbar_seg(MCtx A) {
     if (bad) set_err(A.ctl, EP_ERR_INVALID_POSITION, W.c);
 }
 
+template <int BASIS, bool DET>
+__global__ void __launch_bounds__(256) km_fbar_seg(MCtx A) {
+    fbar_seg_body<BASIS, DET>(A, blockIdx.x);
+}
+
+
 // km_dJn: nodal δJ_n = Σ N m δJ / m_n (volumetric.jl:12-22, increment form)
-__global__ void km_dJn(MCtx A) {
+__device__ __forceinline__ void dJn_body(const MCtx& A, int bid) {
     EP_ACTIVE(A.ctl);
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = bid * blockDim.x + threadIdx.x;
     if (n >= A.g.nnode) return;
     const float m = A.N.m[n];
     const float dj = (m == 0.f) ? 0.f : A.N.dJacc[n] / m;
     A.N.dJn[n] = dj;
     if (A.g.dim == 2) reinterpret_cast<float*>(A.N.vg4)[4 * (size_t)n + 2] = dj;
 }
+
+__global__ void km_dJn(MCtx A) { dJn_body(A, blockIdx.x); }
+
 
 // FP32 Drucker-Prager (DP.jl:33-98) on Voigt stress s[3]; returns Δλ and its ϵpII increment
 __device__ __forceinline__ float dp32(float* s, float ep2, float c0, float cr, float tphi, float Hp, float Kc, float Gc,
@@ -1278,10 +1311,10 @@ __device__ __forceinline__ bool rm_features32(float e11, float e22, float e12, f
 // features go to a slot; km_rmap_finish completes it); in record mode the exact map runs
 // and the (features, exact label) pair of the point is appended to the record buffer.
 template <int BASIS, int ACC>
-__global__ void __launch_bounds__(256) km_cons(MCtx A, int plastic_phase) {
+__device__ __forceinline__ void cons_body(const MCtx& A, int bid, int plastic_phase) {
     EP_ACTIVE(A.ctl);
     const int cur = A.ctl->parity, nxt = cur ^ 1;
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int k = bid * blockDim.x + threadIdx.x;
     int nplastic = 0;
     bool emit = false;
     float fx[RM_NX], fy[RM_NY], fa[4];
@@ -1311,7 +1344,7 @@ __global__ void __launch_bounds__(256) km_cons(MCtx A, int plastic_phase) {
                 if (az.cls[j] < 0) continue;
                 const int n = node2(A.g, ax, az, i, j);
                 const float Nx = dwx[i] * wz[j], Nz = wx[i] * dwz[j];
-                const float4 q = __ldg(&A.N.vg4[n]);
+                const float4 q = A.N.vg4[n];
                 const float vx = q.x, vz = q.y;
                 g00 += Nx * vx;
                 g01 += Nz * vx;
@@ -1526,6 +1559,12 @@ __global__ void __launch_bounds__(256) km_cons(MCtx A, int plastic_phase) {
     const int tot = __reduce_add_sync(0xffffffffu, nplastic);
     if ((threadIdx.x & 31) == 0 && tot) atomicAdd((unsigned long long*)&A.ctl->plastic, (unsigned long long)tot);
 }
+
+template <int BASIS, int ACC>
+__global__ void __launch_bounds__(256) km_cons(MCtx A, int plastic_phase) {
+    cons_body<BASIS, ACC>(A, blockIdx.x, plastic_phase);
+}
+
 
 // rmap_fallback_slot: the exact FP64 return (DP.jl:33-66) of the rejected slots, on the
 // trial stress rebuilt from the slot, then b_e = exp(2 Del \ τ) (DP.jl:63-66)
@@ -3126,6 +3165,298 @@ __global__ void __launch_bounds__(256) km_rmap_finish3(MCtx A) {
     if ((threadIdx.x & 31) == 0 && tf) atomicAdd(&A.ctl->rm_fallback, (unsigned long long)tf);
 }
 
+// ===========================================================================
+// Batched ensemble as one persistent kernel (config 4): n independent 2d mixed-step instances, each
+// with its own mesh, points, control block and time window, advanced by one cooperative kernel that
+// loops over up to `steps` steps; each phase of the step (the kernels of mixed_step_impl) walks the
+// virtual blocks of all instances (instance i owns blocks off[i] .. off[i+1] - 1), and a grid barrier
+// separates the phases.  Instances past their window return from every phase at once (EP_ACTIVE).
+// Barrier waits are bounded (1 s, %globaltimer); a wait that gives up sets the error word, and every
+// block then skips the remaining phases.
+struct BInst {
+    float* gz;              // m, p, f of the instance's nodes (zeroed at each step start)
+    long long gzn;
+    int* sz;                // both parities' cell counts and the cursor
+    long long szn;
+};
+
+struct BatchArgs {
+    const MCtx* ctx;        // n argument blocks
+    const BInst* inst;
+    int n;
+    const int* off;         // 3 (n + 1): virtual-block prefix sums of P2G tiles, point blocks, node blocks
+    int steps;
+    int plastic_phase;
+    int any_musl, any_lock;
+    int keep_ctl;           // 1: dt and g as the host set them (the autotuner's dt = 0 steps)
+    unsigned* bar;          // [0] arrivals, [1] generation
+    int* err;
+};
+
+__device__ __forceinline__ unsigned long long gtimer() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// grid-wide barrier of the cooperative launch (all blocks resident): arrival counter and generation
+__device__ __forceinline__ bool grid_sync(const BatchArgs& B) {
+    __shared__ int ok_s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = *(volatile int*)B.err == 0;
+        if (ok) {
+            volatile unsigned* gen = B.bar + 1;
+            const unsigned g = *gen;
+            __threadfence();
+            const unsigned arrived = atomicAdd(B.bar, 1u) + 1u;
+            if (arrived == gridDim.x) {
+                atomicExch(B.bar, 0u);
+                __threadfence();
+                atomicAdd(B.bar + 1, 1u);
+            } else {
+                const unsigned long long t0 = gtimer();
+                while (*gen == g) {
+                    if (*(volatile int*)B.err) {
+                        ok = 0;
+                        break;
+                    }
+                    if (gtimer() - t0 > 1000000000ull) {
+                        atomicExch(B.err, 1);
+                        ok = 0;
+                        break;
+                    }
+                    __nanosleep(100);
+                }
+            }
+            __threadfence();
+        }
+        ok_s = ok;
+    }
+    __syncthreads();
+    return ok_s != 0;
+}
+
+// the instance owning virtual block vb: the largest i with off[i] <= vb (off[n] > vb)
+__device__ __forceinline__ int inst_of(const int* off, int n, int vb) {
+    int lo = 0, hi = n;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (off[mid] <= vb) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// the next-step cell starts of one instance by one block (count[nxt] -> start[nxt], total at ncell)
+__device__ __forceinline__ void scan_block_body(const MCtx& A) {
+    EP_ACTIVE(A.ctl);
+    const int par = A.ctl->parity ^ 1;
+    const int n = A.g.ncell;
+    const int* in = A.S.count[par];
+    int* out = A.S.start[par];
+    int run = 0;
+    for (int c0 = 0; c0 < n; c0 += blockDim.x * MSCAN_IPT) {
+        const int base = c0 + threadIdx.x * MSCAN_IPT;
+        int v[MSCAN_IPT], sum = 0;
+#pragma unroll
+        for (int i = 0; i < MSCAN_IPT; ++i) {
+            v[i] = base + i < n ? in[base + i] : 0;
+            sum += v[i];
+        }
+        int tot;
+        int ex = mblock_scan(sum, &tot) + run;
+#pragma unroll
+        for (int i = 0; i < MSCAN_IPT; ++i) {
+            if (base + i < n) out[base + i] = ex;
+            ex += v[i];
+        }
+        run += tot;
+    }
+    if (threadIdx.x == 0) out[n] = run;
+}
+
+template <int BASIS, int ACC, int TC>
+__global__ void __launch_bounds__(256, 3) km_batch_steps(BatchArgs B) {
+    const int n = B.n;
+    const int* offT = B.off;
+    const int* offP = B.off + (n + 1);
+    const int* offN = B.off + 2 * (n + 1);
+    const int nT = offT[n], nP = offP[n], nN = offN[n];
+    bool ok = true;
+    for (int st = 0; st < B.steps && ok; ++st) {
+        // step start: control blocks (ctl_begin_run) and the zeroed accumulators of mixed_step_impl
+        for (int i = blockIdx.x; i < n; i += gridDim.x) {
+            const MCtx& A = B.ctx[i];
+            if (threadIdx.x == 0 && !B.keep_ctl) ctl_begin_run(A.ctl, A.g.dim, A.g.h[0], A.g.h[1], A.g.h[2], A.c);
+            const BInst& I = B.inst[i];
+            for (long long k = threadIdx.x; k < I.gzn; k += blockDim.x) I.gz[k] = 0.f;
+            for (long long k = threadIdx.x; k < I.szn; k += blockDim.x) I.sz[k] = 0;
+        }
+        if (!(ok = grid_sync(B))) break;
+        for (int vb = blockIdx.x; vb < nT; vb += gridDim.x) {
+            const int i = inst_of(offT, n, vb);
+            p2g_tile_body<BASIS, TC, false, 256>(B.ctx[i], vb - offT[i]);
+        }
+        if (!(ok = grid_sync(B))) break;
+        for (int vb = blockIdx.x; vb < nN; vb += gridDim.x) {
+            const int i = inst_of(offN, n, vb);
+            solve_body(B.ctx[i], vb - offN[i]);
+        }
+        if (!(ok = grid_sync(B))) break;
+        for (int vb = blockIdx.x; vb < nP; vb += gridDim.x) {
+            const int i = inst_of(offP, n, vb);
+            g2p_seg_body<BASIS, false>(B.ctx[i], vb - offP[i]);
+        }
+        if (!(ok = grid_sync(B))) break;
+        if (B.any_musl) {
+            for (int vb = blockIdx.x; vb < nN; vb += gridDim.x) {
+                const int i = inst_of(offN, n, vb);
+                if (B.ctx[i].cf.musl) vmusl_body(B.ctx[i], vb - offN[i]);
+            }
+            if (!(ok = grid_sync(B))) break;
+        }
+        for (int i = blockIdx.x; i < n; i += gridDim.x) scan_block_body(B.ctx[i]);
+        if (!(ok = grid_sync(B))) break;
+        if (B.any_lock) {
+            for (int vb = blockIdx.x; vb < nP; vb += gridDim.x) {
+                const int i = inst_of(offP, n, vb);
+                if (B.ctx[i].cf.locking) fbar_seg_body<BASIS, false>(B.ctx[i], vb - offP[i]);
+            }
+            if (!(ok = grid_sync(B))) break;
+            for (int vb = blockIdx.x; vb < nN; vb += gridDim.x) {
+                const int i = inst_of(offN, n, vb);
+                if (B.ctx[i].cf.locking) dJn_body(B.ctx[i], vb - offN[i]);
+            }
+            if (!(ok = grid_sync(B))) break;
+        }
+        for (int vb = blockIdx.x; vb < nP; vb += gridDim.x) {
+            const int i = inst_of(offP, n, vb);
+            if (B.ctx[i].P.np > 0) cons_body<BASIS, ACC>(B.ctx[i], vb - offP[i], B.plastic_phase);
+        }
+        if (!(ok = grid_sync(B))) break;
+        // step end: parity flip (km_flip) and t += dt (ctl_end)
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+            Ctl* c = B.ctx[i].ctl;
+            if (c->active) c->parity ^= 1;
+            ctl_end(c);
+        }
+        if (!(ok = grid_sync(B))) break;
+    }
+}
+
+// The same phases as kernels of their own over all instances (one launch per phase and step,
+// 16 steps per graph): no grid barriers, each phase at its own occupancy.
+__global__ void __launch_bounds__(256) kb_begin(BatchArgs B) {
+    const int i = blockIdx.x;
+    const MCtx& A = B.ctx[i];
+    if (threadIdx.x == 0 && !B.keep_ctl) ctl_begin_run(A.ctl, A.g.dim, A.g.h[0], A.g.h[1], A.g.h[2], A.c);
+    const BInst& I = B.inst[i];
+    for (long long k = threadIdx.x; k < I.gzn; k += blockDim.x) I.gz[k] = 0.f;
+    for (long long k = threadIdx.x; k < I.szn; k += blockDim.x) I.sz[k] = 0;
+}
+template <int BASIS, int TC>
+__global__ void __launch_bounds__(4 * TC) kb_p2g(BatchArgs B) {
+    const int vb = blockIdx.x, i = inst_of(B.off, B.n, vb);
+    p2g_tile_body<BASIS, TC, false>(B.ctx[i], vb - B.off[i]);
+}
+__global__ void __launch_bounds__(256) kb_solve(BatchArgs B) {
+    const int* o = B.off + 2 * (B.n + 1);
+    const int vb = blockIdx.x, i = inst_of(o, B.n, vb);
+    solve_body(B.ctx[i], vb - o[i]);
+}
+template <int BASIS>
+__global__ void __launch_bounds__(256) kb_g2p(BatchArgs B) {
+    const int* o = B.off + (B.n + 1);
+    const int vb = blockIdx.x, i = inst_of(o, B.n, vb);
+    g2p_seg_body<BASIS, false>(B.ctx[i], vb - o[i]);
+}
+__global__ void __launch_bounds__(256) kb_vmusl(BatchArgs B) {
+    const int* o = B.off + 2 * (B.n + 1);
+    const int vb = blockIdx.x, i = inst_of(o, B.n, vb);
+    if (B.ctx[i].cf.musl) vmusl_body(B.ctx[i], vb - o[i]);
+}
+__global__ void __launch_bounds__(256) kb_scan(BatchArgs B) { scan_block_body(B.ctx[blockIdx.x]); }
+template <int BASIS>
+__global__ void __launch_bounds__(256) kb_fbar(BatchArgs B) {
+    const int* o = B.off + (B.n + 1);
+    const int vb = blockIdx.x, i = inst_of(o, B.n, vb);
+    if (B.ctx[i].cf.locking) fbar_seg_body<BASIS, false>(B.ctx[i], vb - o[i]);
+}
+__global__ void __launch_bounds__(256) kb_dJn(BatchArgs B) {
+    const int* o = B.off + 2 * (B.n + 1);
+    const int vb = blockIdx.x, i = inst_of(o, B.n, vb);
+    if (B.ctx[i].cf.locking) dJn_body(B.ctx[i], vb - o[i]);
+}
+template <int BASIS, int ACC>
+__global__ void __launch_bounds__(256) kb_cons(BatchArgs B) {
+    const int* o = B.off + (B.n + 1);
+    const int vb = blockIdx.x, i = inst_of(o, B.n, vb);
+    if (B.ctx[i].P.np > 0) cons_body<BASIS, ACC>(B.ctx[i], vb - o[i], B.plastic_phase);
+}
+__global__ void kb_end(BatchArgs B) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < B.n) {
+        Ctl* c = B.ctx[i].ctl;
+        if (c->active) c->parity ^= 1;
+        ctl_end(c);
+    }
+}
+
+template <int BASIS, int ACC, int TC>
+static void batch_phase_steps_t(const BatchArgs& a, const int* nblk, int steps, cudaStream_t s) {
+    const int n = a.n;
+    for (int st = 0; st < steps; ++st) {
+        kb_begin<<<n, 256, 0, s>>>(a);
+        kb_p2g<BASIS, TC><<<nblk[0], 4 * TC, 0, s>>>(a);
+        kb_solve<<<nblk[2], 256, 0, s>>>(a);
+        kb_g2p<BASIS><<<nblk[1], 256, 0, s>>>(a);
+        if (a.any_musl) kb_vmusl<<<nblk[2], 256, 0, s>>>(a);
+        kb_scan<<<n, 256, 0, s>>>(a);
+        if (a.any_lock) {
+            kb_fbar<BASIS><<<nblk[1], 256, 0, s>>>(a);
+            kb_dJn<<<nblk[2], 256, 0, s>>>(a);
+        }
+        kb_cons<BASIS, ACC><<<nblk[1], 256, 0, s>>>(a);
+        kb_end<<<(n + 255) / 256, 256, 0, s>>>(a);
+    }
+}
+
+struct BatchImpl {
+    MCtx* ctx = nullptr;
+    BInst* inst = nullptr;
+    int* off = nullptr;
+    unsigned* bar = nullptr;
+    int* err = nullptr;
+    int n = 0, basis = 0, acc = 0, any_musl = 0, any_lock = 0;
+    int grid[3] = {0, 0, 0};      // resident blocks per tile shape 16 / 32 / 64
+    int nblk[3][3] = {};          // per tile shape: total virtual blocks of tiles, points, nodes
+};
+
+template <int BASIS, int ACC, int TC>
+static const void* batch_fn() {
+    return (const void*)km_batch_steps<BASIS, ACC, TC>;
+}
+
+template <int BASIS, int ACC>
+static const void* batch_fn_tc(int tile) {
+    return tile == 16 ? batch_fn<BASIS, ACC, 16>() : (tile == 32 ? batch_fn<BASIS, ACC, 32>() : batch_fn<BASIS, ACC, 64>());
+}
+
+static const void* batch_kernel(int basis, int acc, int tile) {
+    if (basis == EP_BASIS_BSMPM) return acc ? batch_fn_tc<EP_BASIS_BSMPM, 1>(tile) : batch_fn_tc<EP_BASIS_BSMPM, 0>(tile);
+    if (basis == EP_BASIS_GIMPM) return acc ? batch_fn_tc<EP_BASIS_GIMPM, 1>(tile) : batch_fn_tc<EP_BASIS_GIMPM, 0>(tile);
+    return acc ? batch_fn_tc<EP_BASIS_SMPM, 1>(tile) : batch_fn_tc<EP_BASIS_SMPM, 0>(tile);
+}
+
+__global__ void km_batch_flags(const MCtx* ctx, int n, const int* berr, int* flags) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const Ctl* c = ctx[i].ctl;
+        flags[i] = (c->active ? 1 : 0) | (c->err ? 2 : 0) | (*berr ? 4 : 0);
+    }
+}
+
 // SMs of the current device (grids of the slot kernels, whose counts live on the device)
 static int sm_count() {
     static int n = 0;
@@ -3379,6 +3710,196 @@ void mixed_set_det(void* mem, float* part, float* ptmp) {
     MCtx* A = (MCtx*)mem;
     A->part = part;
     A->ptmp = ptmp;
+}
+
+// ---------------------------------------------------------------------------
+// persistent batch (host side)
+void* mixed_batch_create(const MixedCtx* const* xs, int n, std::string* why) {
+    auto no = [&](const std::string& m) -> void* {
+        if (why) *why = m;
+        return nullptr;
+    };
+    if (n <= 0) return no("empty batch");
+    std::vector<MCtx> host((size_t)n);
+    std::vector<BInst> inst((size_t)n);
+    std::vector<int> off((size_t)3 * (n + 1), 0);
+    int basis = -1, acc = -1, musl = 0, lock = 0;
+    for (int i = 0; i < n; ++i) {
+        const MCtx& A = *(const MCtx*)xs[i]->impl;
+        if (A.g.dim != 2) return no("the persistent batch kernel runs 2d instances");
+        if (A.cf.det || A.cf.nonloc || A.rmode != EP_RMAP_EXACT)
+            return no("deterministic mode, nonlocal averaging and the learned map run on the per-instance graphs");
+        if (basis < 0) {
+            basis = A.cf.basis;
+            acc = A.acc;
+        } else if (basis != A.cf.basis || acc != A.acc) {
+            return no("instances differ in basis or precision");
+        }
+        musl |= A.cf.musl ? 1 : 0;
+        lock |= A.cf.locking ? 1 : 0;
+        host[i] = A;
+        inst[i].gz = (float*)xs[i]->grid_zero;
+        inst[i].gzn = (long long)(xs[i]->grid_zero_bytes / sizeof(float));
+        inst[i].sz = (int*)xs[i]->sort_zero;
+        inst[i].szn = (long long)(xs[i]->sort_zero_bytes / sizeof(int));
+    }
+    BatchImpl* b = new BatchImpl();
+    b->n = n;
+    b->basis = basis;
+    b->acc = acc;
+    b->any_musl = musl;
+    b->any_lock = lock;
+    cudaError_t e = cudaMalloc(&b->ctx, sizeof(MCtx) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&b->inst, sizeof(BInst) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&b->off, sizeof(int) * 3 * 3 * (n + 1));
+    if (e == cudaSuccess) e = cudaMalloc(&b->bar, 2 * sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMalloc(&b->err, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemcpy(b->ctx, host.data(), sizeof(MCtx) * n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(b->inst, inst.data(), sizeof(BInst) * n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(b->bar, 0, 2 * sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMemset(b->err, 0, sizeof(int));
+    // virtual-block offsets per P2G tile shape: tiles of 16 / 32 / 64 cells, points and nodes by 256
+    const int tiles[3] = {16, 32, 64};
+    for (int t = 0; t < 3 && e == cudaSuccess; ++t) {
+        for (int i = 0; i < n; ++i) {
+            const MCtx& A = host[i];
+            const int nT = (A.g.ncell + tiles[t] - 1) / tiles[t];
+            const int nP = std::max(1, (A.P.np + 255) / 256);
+            const int nN = (A.g.nnode + 255) / 256;
+            off[i + 1] = off[i] + nT;
+            off[(n + 1) + i + 1] = off[(n + 1) + i] + nP;
+            off[2 * (n + 1) + i + 1] = off[2 * (n + 1) + i] + nN;
+        }
+        e = cudaMemcpy(b->off + (size_t)t * 3 * (n + 1), off.data(), sizeof(int) * 3 * (n + 1), cudaMemcpyHostToDevice);
+        b->nblk[t][0] = off[n];
+        b->nblk[t][1] = off[(n + 1) + n];
+        b->nblk[t][2] = off[2 * (n + 1) + n];
+        int dev = 0, sms = 0, per = 0;
+        if (e == cudaSuccess) e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_kernel(basis, acc, tiles[t]), 256, 0);
+        b->grid[t] = std::max(1, per) * sms;
+    }
+    if (e != cudaSuccess) {
+        if (why) *why = std::string("persistent batch: ") + cudaGetErrorString(e);
+        cudaGetLastError();
+        mixed_batch_destroy(b);
+        return nullptr;
+    }
+    return b;
+}
+
+void mixed_batch_destroy(void* p) {
+    BatchImpl* b = (BatchImpl*)p;
+    if (!b) return;
+    cudaFree(b->ctx);
+    cudaFree(b->inst);
+    cudaFree(b->off);
+    cudaFree(b->bar);
+    cudaFree(b->err);
+    delete b;
+}
+
+static BatchArgs batch_args(const BatchImpl* b, int plastic, int steps, int tile, int keep_ctl) {
+    const int t = tile == 16 ? 0 : (tile == 32 ? 1 : 2);
+    BatchArgs a;
+    a.ctx = b->ctx;
+    a.inst = b->inst;
+    a.n = b->n;
+    a.off = b->off + (size_t)t * 3 * (b->n + 1);
+    a.steps = steps;
+    a.plastic_phase = plastic;
+    a.any_musl = b->any_musl;
+    a.any_lock = b->any_lock;
+    a.keep_ctl = keep_ctl;
+    a.bar = b->bar;
+    a.err = b->err;
+    return a;
+}
+
+// graph of one persistent launch: barrier words reset, the cooperative kernel, the flags gather
+cudaError_t mixed_batch_graph(void* p, int plastic, int steps, int tile, int* dflags, cudaGraph_t g) {
+    BatchImpl* b = (BatchImpl*)p;
+    const int t = tile == 16 ? 0 : (tile == 32 ? 1 : 2);
+    cudaGraphNode_t ms, kn, fl;
+    cudaMemsetParams mp{};
+    mp.dst = b->bar;
+    mp.value = 0;
+    mp.elementSize = 4;
+    mp.width = 2;
+    mp.height = 1;
+    mp.pitch = 0;
+    cudaError_t e = cudaGraphAddMemsetNode(&ms, g, nullptr, 0, &mp);
+    BatchArgs a = batch_args(b, plastic, steps, tile, 0);
+    void* args[] = {(void*)&a};
+    cudaKernelNodeParams kp{};
+    kp.func = (void*)batch_kernel(b->basis, b->acc, tile);
+    kp.gridDim = dim3(b->grid[t]);
+    kp.blockDim = dim3(256);
+    kp.sharedMemBytes = 0;
+    kp.kernelParams = args;
+    if (e == cudaSuccess) e = cudaGraphAddKernelNode(&kn, g, &ms, 1, &kp);
+    if (e == cudaSuccess) {
+        cudaLaunchAttributeValue v{};
+        v.cooperative = 1;
+        e = cudaGraphKernelNodeSetAttribute(kn, cudaLaunchAttributeCooperative, &v);
+    }
+    const MCtx* cx = b->ctx;
+    int n = b->n;
+    const int* be = b->err;
+    void* fargs[] = {(void*)&cx, (void*)&n, (void*)&be, (void*)&dflags};
+    cudaKernelNodeParams fp{};
+    fp.func = (void*)km_batch_flags;
+    fp.gridDim = dim3((n + 127) / 128);
+    fp.blockDim = dim3(128);
+    fp.kernelParams = fargs;
+    if (e == cudaSuccess) e = cudaGraphAddKernelNode(&fl, g, &kn, 1, &fp);
+    return e;
+}
+
+// one eager cooperative launch (the autotuner)
+cudaError_t mixed_batch_launch(void* p, int plastic, int steps, int tile, int keep_ctl, cudaStream_t s) {
+    BatchImpl* b = (BatchImpl*)p;
+    const int t = tile == 16 ? 0 : (tile == 32 ? 1 : 2);
+    cudaError_t e = cudaMemsetAsync(b->bar, 0, 2 * sizeof(unsigned), s);
+    BatchArgs a = batch_args(b, plastic, steps, tile, keep_ctl);
+    void* args[] = {(void*)&a};
+    if (e == cudaSuccess)
+        e = cudaLaunchCooperativeKernel(batch_kernel(b->basis, b->acc, tile), dim3(b->grid[t]), dim3(256), args, 0, s);
+    return e;
+}
+
+// the phase-kernel scheme: `steps` steps of every instance as phase kernels on stream s (captured
+// into the batch graph by the caller, or launched eagerly by the autotuner)
+void mixed_batch_phase_steps(void* p, int plastic, int steps, int tile, int keep_ctl, cudaStream_t s) {
+    BatchImpl* b = (BatchImpl*)p;
+    const int t = tile == 16 ? 0 : (tile == 32 ? 1 : 2);
+    const BatchArgs a = batch_args(b, plastic, steps, tile, keep_ctl);
+    const int* nb = b->nblk[t];
+#define EP_BPS(BS, AC)                                                      \
+    if (tile == 16) batch_phase_steps_t<BS, AC, 16>(a, nb, steps, s);       \
+    else if (tile == 32) batch_phase_steps_t<BS, AC, 32>(a, nb, steps, s);  \
+    else batch_phase_steps_t<BS, AC, 64>(a, nb, steps, s)
+    if (b->basis == EP_BASIS_BSMPM) {
+        if (b->acc) { EP_BPS(EP_BASIS_BSMPM, 1); } else { EP_BPS(EP_BASIS_BSMPM, 0); }
+    } else if (b->basis == EP_BASIS_GIMPM) {
+        if (b->acc) { EP_BPS(EP_BASIS_GIMPM, 1); } else { EP_BPS(EP_BASIS_GIMPM, 0); }
+    } else {
+        if (b->acc) { EP_BPS(EP_BASIS_SMPM, 1); } else { EP_BPS(EP_BASIS_SMPM, 0); }
+    }
+#undef EP_BPS
+}
+
+void mixed_batch_flags(void* p, int* dflags, cudaStream_t s) {
+    BatchImpl* b = (BatchImpl*)p;
+    km_batch_flags<<<(b->n + 127) / 128, 128, 0, s>>>(b->ctx, b->n, b->err, dflags);
+}
+
+int mixed_batch_error(void* p) {
+    BatchImpl* b = (BatchImpl*)p;
+    int v = 0;
+    if (cudaMemcpy(&v, b->err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return 1;
+    return v;
 }
 
 void mixed_set_rmap(void* mem, const RmapBufs& b) {

@@ -191,6 +191,9 @@ SIGNATURES = {
     "epgpu_batch_run": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_double, _D, _I64]),
     "epgpu_batch_autotune": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), _D]),
     "epgpu_batch_stats": (C.c_int, [C.c_void_p, _D, _I64]),
+    "epgpu_batch_scheme": (C.c_int32, [C.c_void_p]),
+    "epgpu_batch_tuning": (C.c_int, [C.c_void_p, _D, C.POINTER(C.c_int32)]),
+    "epgpu_batch_set_scheme": (C.c_int, [C.c_void_p, C.c_int32]),
     "epgpu_batch_instance": (C.c_void_p, [C.c_void_p, C.c_int32]),
     "epgpu_batch_last_error": (C.c_char_p, [C.c_void_p]),
     "epgpu_batch_destroy": (C.c_int, [C.c_void_p]),

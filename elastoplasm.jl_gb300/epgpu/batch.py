@@ -19,6 +19,9 @@ import numpy as np
 from . import abi
 
 
+SCHEMES = ("graphs", "persistent", "phases")
+
+
 class Batch:
     def __init__(self, ics: list, instrs: list):
         self.lib = abi.load_library()
@@ -70,7 +73,29 @@ class Batch:
         ms = C.c_double(0.0)
         nl = C.c_int64(0)
         self._check(self.lib.epgpu_batch_stats(self.h, C.byref(ms), C.byref(nl)))
-        return {"device_ms": ms.value, "graph_launches": nl.value}
+        return {"device_ms": ms.value, "graph_launches": nl.value, "scheme": self.scheme()}
+
+    def tuning(self) -> dict:
+        """The autotuner's ms per batch step, per scheme and P2G tile."""
+        ms = np.zeros(9)
+        av = C.c_int32(0)
+        self._check(self.lib.epgpu_batch_tuning(self.h, ms.ctypes.data_as(C.POINTER(C.c_double)), C.byref(av)))
+        out = {name: dict(zip((16, 32, 64), ms[3 * k:3 * k + 3])) for k, name in enumerate(SCHEMES)}
+        out["kernels_available"] = bool(av.value)
+        return out
+
+    def set_scheme(self, scheme: str):
+        """"graphs", "persistent", "phases" or "auto" (the phase kernels when the batch qualifies)."""
+        code = -1 if scheme == "auto" else SCHEMES.index(scheme)
+        self._check(self.lib.epgpu_batch_set_scheme(self.h, code))
+
+    def scheme(self) -> str:
+        """The scheme the batch runs: "graphs" (the instances' own graphs), "persistent" (one
+        cooperative kernel) or "phases" (one kernel per phase over all instances)."""
+        return SCHEMES[self.lib.epgpu_batch_scheme(self.h)]
+
+    def persistent(self) -> bool:
+        return self.scheme() == "persistent"
 
     def close(self):
         if getattr(self, "h", None):

@@ -241,9 +241,14 @@ ep_status epgpu_bin_cells_noalloc(int32_t dim, const int64_t* nel, const double*
 /* ---- Batched ensemble -----------------------------------------------------
  * No counterpart in the reference (one slump per Julia process).  n independent
  * instances -- each its own mesh, points, switches, material and time loop --
- * advance together: every instance keeps its device state and its 16-step graph,
- * and one launch of the batch graph (the instances' graphs as independent child
- * nodes) advances each of them by up to 16 of its own CFL steps. */
+ * advance together, by up to 16 of their own CFL steps per launch of a CUDA graph.
+ * When every instance is a 2d mixed-precision step with the exact return map (no
+ * deterministic mode, no nonlocal averaging) and the same basis and precision,
+ * each phase of the step walks the blocks of all instances, either as one
+ * persistent cooperative kernel (grid barriers between the phases; scheme 1) or as
+ * one kernel per phase (scheme 2, the default); the autotuner picks between them.
+ * Otherwise (scheme 0) each instance keeps its 16-step graph and the batch graph
+ * holds those graphs as independent child nodes. */
 typedef struct ep_batch ep_batch;
 
 /* cfg, cmpr, mesh, nmp: arrays of n, one entry per instance (as epgpu_create). */
@@ -255,10 +260,21 @@ ep_status epgpu_batch_download(ep_batch* b, int32_t i, ep_mpts_view* m);
  * 73-85): instance i runs from t_inout[i] to T with its own dt; on return
  * t_inout[i] = T (or where an error stopped it) and nsteps_out[i] its steps. */
 ep_status epgpu_batch_run(ep_batch* b, int32_t phase, double T, double tg, double* t_inout, int64_t* nsteps_out);
-/* Tile-shape autotuner of the mixed step: times dt = 0 steps (they leave the
- * state unchanged) of all instances with P2G tiles of 16, 32 and 64 cells per
- * CTA and keeps the fastest; ms_out (3) receives the mean batch-step time of each. */
+/* Autotuner of the mixed step: times dt = 0 steps (they leave the state unchanged)
+ * of all instances with P2G tiles of 16, 32 and 64 cells per CTA -- on the persistent
+ * kernel and on the phase kernels when the batch qualifies, else on the instances'
+ * own step graphs -- and keeps the fastest scheme and tile; ms_out (3) receives the
+ * mean batch-step time of each tile in the chosen scheme. */
 ep_status epgpu_batch_autotune(ep_batch* b, int32_t phase, int32_t* tile_out, double* ms_out);
+/* The scheme the batch runs: 0 per-instance graphs, 1 persistent kernel, 2 phase kernels. */
+int32_t epgpu_batch_scheme(ep_batch* b);
+/* Force the scheme (0, 1, 2; EP_ERR_UNSUPPORTED when the batch does not qualify for
+ * 1 or 2), or -1 back to the default. */
+ep_status epgpu_batch_set_scheme(ep_batch* b, int32_t scheme);
+/* The autotuner's timings (ms per batch step): ms9[3 s + k] for scheme s and the P2G
+ * tile 16 / 32 / 64 (k = 0 / 1 / 2), 0 where not timed; *kernels_available: whether
+ * the batch qualifies for schemes 1 and 2. */
+ep_status epgpu_batch_tuning(ep_batch* b, double* ms9, int32_t* kernels_available);
 /* Device time of the last epgpu_batch_run and the batch-graph launches so far. */
 ep_status epgpu_batch_stats(ep_batch* b, double* device_ms, int64_t* graph_launches);
 /* The handle of instance i (epgpu_stats, epgpu_set_return_map, ...); owned by the batch. */

@@ -1,5 +1,6 @@
-"""The batched ensemble: instances advanced together match the same instances run one by
-one; the tile autotuner leaves the state unchanged."""
+"""The batched ensemble: instances advanced together (one persistent kernel, or the instances'
+own graphs) match the same instances run one by one; the tile autotuner leaves the state
+unchanged."""
 import copy
 import math
 
@@ -25,11 +26,20 @@ def _rel(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
 
-def test_batch_matches_single_instances():
+@pytest.mark.parametrize("path", ["phases", "persistent", "graphs"])
+def test_batch_matches_single_instances(path):
+    """The three batch schemes against the instances run alone: the phase kernels over all
+    instances (the default), the persistent kernel (both: all instances 2d mixed, exact map) and
+    the instances' own graphs (here because one instance runs in the deterministic mode)."""
     from epgpu import Engine
     from epgpu.batch import Batch
     inst = _instances()
+    if path == "graphs":
+        inst[2][1]["gpu"]["deterministic"] = True
     b = Batch([copy.deepcopy(ic) for ic, _ in inst], [i for _, i in inst])
+    if path == "persistent":
+        b.set_scheme("persistent")
+    assert b.scheme() == path
     t, n0 = b.run(0, 1.0)
     assert np.all(t == 1.0) and np.all(n0 > 0)
     t, n1 = b.run(1, 1.5)
@@ -54,7 +64,7 @@ def test_autotune_keeps_the_state():
     b.run(0, 1.0)
     before = [b.download(k) for k in range(b.n)]
     tile, ms = b.autotune(phase=0)
-    print(f"autotune: tile {tile}, ms per batch step {ms}")
+    print(f"autotune: tile {tile}, scheme {b.scheme()}, ms per batch step {b.tuning()}")
     assert tile in (16, 32, 64) and all(v > 0 for v in ms.values())
     for k in range(b.n):
         a = b.download(k)
