@@ -2747,7 +2747,7 @@ __device__ __forceinline__ bool rm_features3(const float* eps_in, const float (&
 // trial Kirchhoff stress, both returns and b_e = exp(2 Del \ τ) (DP.jl:63-66) are coaxial with it.
 // With the learned return map a trial-yielding DP point is handed to the network as in 2d.
 template <int BASIS, int ACC, bool FIN>
-__global__ void __launch_bounds__(256) km_cons3(MCtx A, int plastic_phase) {
+__global__ void __launch_bounds__(256, 3) km_cons3(MCtx A, int plastic_phase) {
     using R = typename std::conditional<ACC == 0, double, float>::type;
     EP_ACTIVE(A.ctl);
     const int cur = A.ctl->parity, nxt = cur ^ 1;
