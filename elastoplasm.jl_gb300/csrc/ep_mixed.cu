@@ -2230,7 +2230,7 @@ __device__ __forceinline__ bool point3(const MCtx& A, int cur, int k, int n, PtW
 constexpr int TP3_STRIDE = 47;
 
 template <int BASIS, int TC>
-__global__ void __launch_bounds__(16 * TC, 3) km_p2g_tile3(MCtx A) {
+__global__ void __launch_bounds__(16 * TC, 4) km_p2g_tile3(MCtx A) {
     constexpr int TH = 16 * TC;
     EP_ACTIVE(A.ctl);
     __shared__ float sp[TH * TP3_STRIDE];

@@ -70,10 +70,22 @@ __device__ __forceinline__ float dsilu(float z) {
     return s * (1.f + z * (1.f - s));
 }
 
+// named barriers of one 256-thread group (ids 1 and 2; 0 is __syncthreads)
+__device__ __forceinline__ void grp_sync(int id) { asm volatile("bar.sync %0, 256;" ::"r"(id) : "memory"); }
+__device__ __forceinline__ bool grp_sync_and(int id, bool v) {
+    int r;
+    asm volatile("{\n\t.reg .pred p, q;\n\tsetp.ne.s32 p, %1, 0;\n\tbar.red.and.pred q, %2, 256, p;\n\tselp.s32 %0, 1, 0, q;\n\t}"
+                 : "=r"(r)
+                 : "r"((int)v), "r"(id)
+                 : "memory");
+    return r != 0;
+}
+
 // ---------------------------------------------------------------------------
-// forward, fused over the five layers; one CTA (16 warps) per SM walks tiles of
-// 128 rows.  Warp w reads TMEM lanes 32 (w % 4) .. + 31 (its rows) and the
-// column quarter w / 4 of every accumulator.
+// forward, fused over the five layers; one CTA (16 warps) per SM, two groups of 8 warps
+// each walking its own tiles of 128 rows, so that one group's epilogue overlaps the other's
+// MMAs.  Warp w of a group reads TMEM lanes 32 (w % 4) .. + 31 (its rows) and the column
+// half (w % 8) / 4 of every accumulator of its group.
 struct FwdArgs {
     const float* X;       // rows of RM_NX floats (the first 6 are the inputs)
     int n;                // rows, or (ndev != nullptr) the capacity
@@ -85,35 +97,38 @@ struct FwdArgs {
     int* err;             // set to 1 when a wait times out
 };
 
-constexpr int FWD_SH = 0, FWD_SX = FWD_SH + MT * W * 2, FWD_SW = FWD_SX + MT * KIN * 2;
+// two 128-row tiles in flight per CTA: group g (warps 8g .. 8g + 7) owns activation buffer FWD_SH + g
+// and input buffer FWD_SX + g, TMEM columns 256 g .. 256 g + 255 and mbarrier 1 + g; the weights
+// are shared
+constexpr int FWD_SH = 0, FWD_SX = FWD_SH + 2 * MT * W * 2, FWD_SW = FWD_SX + 2 * MT * KIN * 2;
 constexpr int FWD_BAR = FWD_SW + IMG_BYTES, FWD_SMEM = FWD_BAR + 32;
+static_assert(FWD_SW % 128 == 0 && FWD_BAR % 8 == 0, "shared layout alignment");
 
 constexpr int FWD_THREADS = 512;
 
 __global__ void __launch_bounds__(FWD_THREADS, 1) km_mlp_fwd(FwdArgs a) {
     extern __shared__ __align__(128) uint8_t sm[];
-    uint8_t* sH = sm + FWD_SH;
-    uint8_t* sX = sm + FWD_SX;
     uint8_t* sW = sm + FWD_SW;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(sm + FWD_BAR);
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + FWD_BAR + 16);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sm + FWD_BAR);       // [0] weights, [1 + g] group g's MMAs
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + FWD_BAR + 24);
     const int n = a.ndev ? min(*a.ndev, a.n) : a.n;
     const int ntiles = (n + MT - 1) / MT;
-    if ((int)blockIdx.x >= ntiles) return;                  // the whole CTA, before any shared state
+    if (2 * (int)blockIdx.x >= ntiles) return;              // the whole CTA, before any shared state
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (tid == 0) {
         tc::mbar_init(&bar[0], 1);
         tc::mbar_init(&bar[1], 1);
+        tc::mbar_init(&bar[2], 1);
         tc::mbar_fence_init();
     }
     if (warp == 0) {
-        tc::tmem_alloc(tslot, 256);
+        tc::tmem_alloc(tslot, 512);
         tc::tmem_relinquish();
     }
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
-    const uint32_t tbase = *tslot;
+    const uint32_t tall = *tslot;
     if (tid == 0) {
         tc::mbar_arrive_expect_tx(&bar[0], IMG_BYTES);
         for (int o = 0; o < IMG_BYTES; o += 32768) {
@@ -123,17 +138,24 @@ __global__ void __launch_bounds__(FWD_THREADS, 1) km_mlp_fwd(FwdArgs a) {
     }
     bool ok = tc::mbar_wait(&bar[0], 0);
     ok = __syncthreads_and(ok);
+    // group g: its own tiles, buffers, accumulator columns and barrier; the two groups' MMAs
+    // queue on the tensor core while the other group runs its epilogue
+    const int g = warp >> 3, gt = tid & 255, gw = warp & 7;
+    uint8_t* sH = sm + FWD_SH + g * (MT * W * 2);
+    uint8_t* sX = sm + FWD_SX + g * (MT * KIN * 2);
+    uint64_t* gbar = &bar[1 + g];
+    const uint32_t tbase = tall + (uint32_t)(256 * g);
     const float* bias = reinterpret_cast<const float*>(sW + IBIAS);
     const uint32_t aX = tc::smem_u32(sX), aH = tc::smem_u32(sH), aW = tc::smem_u32(sW);
     const uint32_t id128 = tc::idesc_bf16(MT, W), id16 = tc::idesc_bf16(MT, NO);
-    const int q = warp & 3, cq = warp >> 2;        // lane quarter, column quarter
+    const int q = gw & 3, ch = gw >> 2;            // lane quarter, column half (64 columns)
     const int row = 32 * q + lane;
     const uint32_t trow = tbase + ((uint32_t)(32 * q) << 16);
     uint32_t ph = 0;
-    for (int tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
+    for (int tile = 2 * blockIdx.x + g; ok && tile < ntiles; tile += 2 * gridDim.x) {
         const int r0 = tile * MT;
-        if (tid < MT) {
-            const int r = r0 + tid;
+        if (gt < MT) {
+            const int r = r0 + gt;
             float f[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
             if (r < n) {
                 const float4 u = *reinterpret_cast<const float4*>(a.X + (size_t)r * RM_NX);
@@ -142,8 +164,8 @@ __global__ void __launch_bounds__(FWD_THREADS, 1) km_mlp_fwd(FwdArgs a) {
             }
             const uint4 lo = make_uint4(pack_bf16(f[0], f[1]), pack_bf16(f[2], f[3]), pack_bf16(f[4], f[5]), 0u);
             const uint4 zz = make_uint4(0u, 0u, 0u, 0u);
-            *reinterpret_cast<uint4*>(sX + tc::kmajor_off(tid, 0, KIN)) = lo;
-            *reinterpret_cast<uint4*>(sX + tc::kmajor_off(tid, 8, KIN)) = zz;
+            *reinterpret_cast<uint4*>(sX + tc::kmajor_off(gt, 0, KIN)) = lo;
+            *reinterpret_cast<uint4*>(sX + tc::kmajor_off(gt, 8, KIN)) = zz;
             if (a.Hst && r < n) {
                 uint4* d = reinterpret_cast<uint4*>(a.Hst + (size_t)r * KIN);
                 d[0] = lo;
@@ -152,23 +174,23 @@ __global__ void __launch_bounds__(FWD_THREADS, 1) km_mlp_fwd(FwdArgs a) {
         }
         tc::fence_async_smem();
         tc::fence_before_sync();
-        __syncthreads();
-        if (tid == 0) {
+        grp_sync(1 + g);
+        if (gt == 0) {
             tc::fence_after_sync();
             tc::mma_bf16(tbase, tc::sdesc(aX, 128, 256), tc::sdesc(aW + IW1, 128, 256), id128, 0);
-            tc::mma_commit(&bar[1]);
+            tc::mma_commit(gbar);
         }
         for (int l = 1; l <= 4; ++l) {
-            ok = tc::mbar_wait(&bar[1], ph);
+            ok = tc::mbar_wait(gbar, ph);
             ph ^= 1;
-            ok = __syncthreads_and(ok);
+            ok = grp_sync_and(1 + g, ok);
             if (!ok) break;
             tc::fence_after_sync();
             const float* b = bias + (l - 1) * W;
             const int r = r0 + row;
 #pragma unroll
-            for (int c = 0; c < 2; ++c) {
-                const int col = 32 * cq + 16 * c;
+            for (int c = 0; c < 4; ++c) {
+                const int col = 64 * ch + 16 * c;
                 float v[16], bb[16];
                 tc::tmem_ld16(trow + (uint32_t)col, v);
 #pragma unroll
@@ -201,24 +223,24 @@ __global__ void __launch_bounds__(FWD_THREADS, 1) km_mlp_fwd(FwdArgs a) {
             }
             tc::fence_async_smem();
             tc::fence_before_sync();
-            __syncthreads();
-            if (tid == 0) {
+            grp_sync(1 + g);
+            if (gt == 0) {
                 tc::fence_after_sync();
                 const bool last = l == 4;
                 const uint32_t wl = last ? aW + IW5 : aW + IW2 + (uint32_t)(l - 1) * (W * W * 2);
                 for (int kc = 0; kc < W / 16; ++kc)
                     tc::mma_bf16(last ? tbase + W : tbase, tc::sdesc(aH + 256u * kc, 128, 2048),
                                  tc::sdesc(wl + 256u * kc, 128, 2048), last ? id16 : id128, kc > 0);
-                tc::mma_commit(&bar[1]);
+                tc::mma_commit(gbar);
             }
         }
         if (!ok) break;
-        ok = tc::mbar_wait(&bar[1], ph);
+        ok = tc::mbar_wait(gbar, ph);
         ph ^= 1;
-        ok = __syncthreads_and(ok);
+        ok = grp_sync_and(1 + g, ok);
         if (!ok) break;
         tc::fence_after_sync();
-        if (cq == 0) {
+        if (ch == 0) {
             float v[16];
             tc::tmem_ld16(trow + W, v);
             const int r = r0 + row;
@@ -228,12 +250,12 @@ __global__ void __launch_bounds__(FWD_THREADS, 1) km_mlp_fwd(FwdArgs a) {
             }
         }
         tc::fence_before_sync();
-        __syncthreads();
+        grp_sync(1 + g);
     }
-    if (!ok && tid == 0 && a.err) atomicExch(a.err, 1);
+    if (!ok && gt == 0 && a.err) atomicExch(a.err, 1);
     tc::fence_before_sync();
     __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(tbase, 256);
+    if (warp == 0) tc::tmem_dealloc(tall, 512);
 }
 
 // ---------------------------------------------------------------------------
@@ -649,7 +671,7 @@ static void mlp_fwd_launch(ep_mlp* m, const float* X, int n, const int* ndev, fl
     a.Zst = train ? m->d.Z : nullptr;
     a.err = m->d.err;
     const int tiles = (n + MT - 1) / MT;
-    const int grid = ndev ? m->sms : std::max(1, std::min(tiles, m->sms));
+    const int grid = ndev ? m->sms : std::max(1, std::min((tiles + 1) / 2, m->sms));   // 2 tiles in flight per CTA
     km_mlp_fwd<<<grid, FWD_THREADS, FWD_SMEM, s>>>(a);
 }
 
