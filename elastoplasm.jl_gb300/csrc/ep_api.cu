@@ -236,8 +236,6 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
         return fail(nullptr, EP_ERR_UNSUPPORTED, "unknown precision");
     if (cfg->precision != EP_PREC_FP64 && d == 3 && cfg->deterministic)
         return fail(nullptr, EP_ERR_UNSUPPORTED, "the deterministic mode is built for the 2d mixed step");
-    if (cfg->precision != EP_PREC_FP64 && cfg->nonloc && d == 3)
-        return fail(nullptr, EP_ERR_UNSUPPORTED, "nonlocal averaging of the mixed step is built in 2d (FP64 step in 3d)");
     if (cfg->nonloc && !(cfg->nonloc_ls > 0.0)) return fail(nullptr, EP_ERR_ARG, "nonloc.ls must be > 0");
     if (!mesh->x || !mesh->xB || !mesh->bcs) return fail(nullptr, EP_ERR_ARG, "mesh.x, mesh.xB and mesh.bcs are required");
     long long nnode = 1, ncell = 1;

@@ -2404,6 +2404,7 @@ __global__ void __launch_bounds__(256) km_g2p_seg3(MCtx A) {
             set_err(A.ctl, EP_ERR_NONFINITE, p);
         }
         A.P.p2e_next[p] = c2;
+        if (A.P.pcell[nxt]) A.P.pcell[nxt][p] = c2;
         mp = A.P.mp[p];
     }
     {
@@ -2503,6 +2504,137 @@ __global__ void __launch_bounds__(256) km_fbar_seg3(MCtx A) {
                     atomicAdd(&A.N.dJacc[node3(A.g, W.a[0], W.a[1], W.a[2], i, j, kz)], v);
             }
     if (bad) set_err(A.ctl, EP_ERR_INVALID_POSITION, W.c);
+}
+
+// km_nonlocal3: the nonlocal averaging of km_nonlocal in 3d (the FP64 step's k_nonlocal64<3>):
+// candidates from the cells within ±nnel of p's step-start cell, in ascending id order, the
+// distance in the first two coordinates (x, y) as the reference forms it (nonlocal.jl:27-28)
+template <int ACC>
+__global__ void __launch_bounds__(32) km_nonlocal3(MCtx A) {
+    EP_ACTIVE(A.ctl);
+    __shared__ int qs[NLM_CAP];
+    __shared__ float om[NLM_CAP];
+    const int p = blockIdx.x, lane = threadIdx.x;
+    if (p >= A.P.np) return;
+    const int cur = A.ctl->parity, nxt = cur ^ 1;
+    const int cp = A.P.pcell[cur][p], cn = A.P.pcell[nxt][p];
+    if (A.P.dlam[p] == 0.f || cp < 0 || cn < 0) {
+        if (lane == 0) A.P.ep2[p] = 0.f;
+        return;
+    }
+    int e[3];
+    cell_dec(A.g, cp, e);
+    int lo[3], hi[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        lo[d] = max(e[d] - A.g.nnel[d], 0);
+        hi[d] = min(e[d] + A.g.nnel[d], A.g.nel[d] - 1);
+    }
+    const int nz = A.g.nel[2], nzx = A.g.nel[2] * A.g.nel[0];
+    const int* start = A.S.start[cur];
+    const int* list = A.S.list[cur];
+    // each (y, x) column's z-run of cells is one contiguous slice of the list
+    int L = 0;
+    for (int k = lo[1]; k <= hi[1]; ++k)
+        for (int a = lo[0]; a <= hi[0]; ++a) L += start[hi[2] + nz * a + nzx * k + 1] - start[lo[2] + nz * a + nzx * k];
+    const double ls = A.cf.ls;
+    int en[3];
+    cell_dec(A.g, cn, en);
+    const double xp0 = A.g.ax[0][en[0]] + (double)A.P.dx[nxt][0][p];
+    const double xp1 = A.g.ax[1][en[1]] + (double)A.P.dx[nxt][1][p];
+    auto omega = [&](int q) {
+        int eq[3];
+        cell_dec(A.g, A.P.pcell[nxt][q], eq);
+        const double xi = xp0 - (A.g.ax[0][eq[0]] + (double)A.P.dx[nxt][0][q]);
+        const double et = xp1 - (A.g.ax[1][eq[1]] + (double)A.P.dx[nxt][1][q]);
+        const float r = (float)(sqrt(xi * xi + et * et) / ls);
+        return r * expf(-(r * r));
+    };
+    if (L <= NLM_CAP) {
+        int pos = 0;
+        for (int k = lo[1]; k <= hi[1]; ++k)
+            for (int a = lo[0]; a <= hi[0]; ++a) {
+                const int b = start[lo[2] + nz * a + nzx * k], n = start[hi[2] + nz * a + nzx * k + 1] - b;
+                for (int t = lane; t < n; t += 32) qs[pos + t] = list[b + t];
+                pos += n;
+            }
+        int P2 = 32;
+        while (P2 < L) P2 <<= 1;
+        for (int t = L + lane; t < P2; t += 32) qs[t] = INT_MAX;
+        __syncwarp();
+        for (int kk = 2; kk <= P2; kk <<= 1)
+            for (int j = kk >> 1; j > 0; j >>= 1) {
+                for (int t = lane; t < P2; t += 32) {
+                    const int q = t ^ j;
+                    if (q > t) {
+                        const int x = qs[t], c = qs[q];
+                        const bool asc = (t & kk) == 0;
+                        if ((x > c) == asc) {
+                            qs[t] = c;
+                            qs[q] = x;
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+        for (int t = lane; t < L; t += 32) om[t] = omega(qs[t]);
+        __syncwarp();
+        if (lane == 0) {
+            float W = 0.f;
+            for (int t = 0; t < L; ++t) {
+                const int q = qs[t];
+                if (q >= p) break;
+                if (A.P.dlam[q] != 0.f) W += om[t];
+            }
+            for (int t = 0; t < L; ++t) {
+                const int q = qs[t];
+                if (q < p && A.P.dlam[q] != 0.f) continue;
+                W += om[t];
+            }
+            float sum = 0.f;
+            if (!(W > 1e-16f)) {
+                sum = ep1_of<ACC>(A, p);
+            } else {
+                for (int t = 0; t < L; ++t) {
+                    const int q = qs[t];
+                    if (q < p && A.P.dlam[q] != 0.f) continue;
+                    sum += (om[t] / W) * ep1_of<ACC>(A, q);
+                }
+            }
+            A.P.ep2[p] = sum;
+        }
+        return;
+    }
+    // more candidates than the shared buffer holds: ascending order by repeated minimum selection
+    if (lane != 0) return;
+    float W = 0.f;
+    for (int pass = 0; pass < 3; ++pass) {
+        float sum = 0.f;
+        int last = -1;
+        if (pass == 2 && !(W > 1e-16f)) {
+            A.P.ep2[p] = ep1_of<ACC>(A, p);
+            return;
+        }
+        while (true) {
+            int best = INT_MAX;
+            for (int k = lo[1]; k <= hi[1]; ++k)
+                for (int a = lo[0]; a <= hi[0]; ++a)
+                    for (int t = start[lo[2] + nz * a + nzx * k]; t < start[hi[2] + nz * a + nzx * k + 1]; ++t) {
+                        const int q = list[t];
+                        if (q > last && q < best) best = q;
+                    }
+            if (best == INT_MAX) break;
+            last = best;
+            const int q = best;
+            const bool plq = A.P.dlam[q] != 0.f;
+            if (pass == 0 && !(q < p && plq)) continue;
+            if (pass >= 1 && (q < p && plq)) continue;
+            const float w = omega(q);
+            if (pass < 2) W += w;
+            else sum += (w / W) * ep1_of<ACC>(A, q);
+        }
+        if (pass == 2) A.P.ep2[p] = sum;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -3499,6 +3631,11 @@ static void mixed_step3_impl(const MixedCtx& X, int phase, cudaStream_t s) {
         km_dJn<<<gn, 256, 0, s>>>(A);
         mark("dJn");
         L += 2;
+    }
+    if (np > 0 && A.cf.nonloc && phase == EP_PHASE_ELASTOPLASTIC) {
+        km_nonlocal3<ACC><<<np, 32, 0, s>>>(A);
+        mark("nonlocal");
+        ++L;
     }
     if (np > 0) {
         if (A.cf.deform == EP_DEFORM_FINITE) km_cons3<BASIS, ACC, true><<<gp, 256, 0, s>>>(A, phase == EP_PHASE_ELASTOPLASTIC);

@@ -1,6 +1,6 @@
 """The mixed-precision 3d step against the FP64 oracle: infinitesimal strain with the config-3
 switches (GIMP / TPIC / J2), the B-spline basis, DP and standard USL with mUSL and F-bar; finite
-strain with the reference's defaults, the config-5 switches and J2."""
+strain with the reference's defaults, the config-5 switches and J2; nonlocal averaging."""
 import copy
 
 import numpy as np
@@ -99,6 +99,11 @@ FIN_CASES = {
     "finite_dp_config5_noghost": (dict(basis={"which": "gimpm", "how": "undeformed", "ghost": False}, fwrk=C5_FWRK),
                                   C5_OVER, 1e-2, False),
     "finite_j2_fbar": (dict(**J2), {"c0": 5.0e4, "Hp": 1.0e5}, 0.0, False),
+    # nonlocal averaging on (the reference's default): ϵpII[2] from the neighbourhood sums
+    "finite_dp_defaults_nonlocal": (dict(nonloc={"status": True, "ls": 0.5}), None, 0.0, False),
+    "infinitesimal_dp_musl_fbar_nonlocal": ({"fwrk": {"deform": "infinitesimal", "trsfr": "std", "C_pf": 1.0,
+                                                      "musl": True, "locking": True, "damping": 0.1},
+                                             "nonloc": {"status": True, "ls": 0.5}}, None, 0.0, False),
 }
 
 
@@ -120,7 +125,9 @@ def _fp64_spread(oracle_mod, kw, over, shift, windows=((0, 2.0), (1, 3.0)), eps=
 
 def _compare_fin(oracle_mod, kw, over, shift, precision, windows=((0, 2.0), (1, 3.0))):
     from epgpu import Engine, ic_slump
-    ic, cfg = ic_slump(*C1_3D, cmpr_over=over, nonloc={"status": False, "ls": 0.5}, **kw)
+    kw = copy.deepcopy(kw)
+    nl = kw.pop("nonloc", {"status": False, "ls": 0.5})
+    ic, cfg = ic_slump(*C1_3D, cmpr_over=over, nonloc=nl, **kw)
     if over and "c0" in over:
         ic["mpts"].c0[:] = over["c0"]
     ic["mpts"].x += shift * ic["mesh"].h[0]
@@ -137,7 +144,8 @@ def _compare_fin(oracle_mod, kw, over, shift, precision, windows=((0, 2.0), (1, 
         t = te
     a, b = e.download(), o.download()
     e.close()
-    s = float(np.linalg.norm(a.tau - b.tau) / np.linalg.norm(b.tau))
+    fld = "tau" if cfg["instr"]["fwrk"]["deform"] == "finite" else "sig"     # Kirchhoff or Cauchy stress
+    s = float(np.linalg.norm(getattr(a, fld) - getattr(b, fld)) / np.linalg.norm(getattr(b, fld)))
     d = float(np.linalg.norm(a.x - b.x) / max(np.linalg.norm(b.x - x0), 1e-300))
     return a, b, s, d
 
@@ -154,6 +162,10 @@ def test_mixed3d_finite_vs_oracle(oracle_mod, case, precision):
         spread = _fp64_spread(oracle_mod, kw, over, shift)
         tol = max(STRESS_TOL, 3.0 * spread)
         print(f"FP64 stress change under a 1e-7 h position perturbation: {spread:.2e}")
+    if "nonloc" in kw:
+        de2 = np.abs(a.epII[1] - b.epII[1]).max() / max(np.abs(b.epII[1]).max(), 1e-300)
+        print(f"ϵpII[2] (nonlocal) max rel diff {de2:.2e}, points with ϵpII[2] > 0: {int((b.epII[1] > 0).sum())}")
+        assert (b.epII[1] > 0).sum() > 100 and de2 < 1e-4
     print(f"3d {case} {precision}: stress {s:.3e} (bound {tol:.1e}) displacement {d:.3e} b_e {db:.2e} "
           f"plastic points {nplastic} of {b.epII.shape[1]}")
     assert nplastic > 100
@@ -161,5 +173,6 @@ def test_mixed3d_finite_vs_oracle(oracle_mod, case, precision):
     assert np.abs(a.Fij - b.Fij).max() < 1e-5 and db < (1e-5 if not conditioned else 1e-4)
     # σ = τ / J of the downloaded state (the reference's σ field is the one formed at the start of
     # the last step's P2G, p2n.jl:12-21, one step older)
-    sig_now = b.tau / np.asarray(b.J).reshape(1, -1)
+    fin = kw.get("fwrk", {}).get("deform", "finite") == "finite"
+    sig_now = b.tau / np.asarray(b.J).reshape(1, -1) if fin else b.sig
     np.testing.assert_allclose(a.sig, sig_now, rtol=0, atol=10 * tol * np.abs(sig_now).max())
