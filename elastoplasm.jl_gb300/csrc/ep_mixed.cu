@@ -609,7 +609,8 @@ __global__ void __launch_bounds__(256) km_p2g_seg(MCtx A) {
 
 // km_g2p_seg: PIC/FLIP (n2p.jl:14-40), new cell + offset, vmax, next-cell counts
 // (tplgy.jl:43-62) and the mUSL momentum P2G (augm.jl:13-25), one lane per point
-template <int BASIS, bool DET>
+// MSEG: the mUSL momentum scatter by segmented warp sums here (else km_aux_tile<.., 1, ..> does it)
+template <int BASIS, bool DET, bool MSEG = !DET>
 __device__ __forceinline__ void g2p_seg_body(const MCtx& A, int bid) {
     EP_ACTIVE(A.ctl);
     const int cur = A.ctl->parity, nxt = cur ^ 1;
@@ -670,7 +671,7 @@ __device__ __forceinline__ void g2p_seg_body(const MCtx& A, int bid) {
         const unsigned mm = __match_any_sync(0xffffffffu, c2);
         if (c2 >= 0 && S.lane == __ffs(mm) - 1) atomicAdd(&A.S.count[nxt][c2], __popc(mm));
     }
-    if (A.cf.musl && !DET) {
+    if (A.cf.musl && MSEG) {
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
 #pragma unroll
@@ -695,9 +696,9 @@ __device__ __forceinline__ void g2p_seg_body(const MCtx& A, int bid) {
     }
 }
 
-template <int BASIS, bool DET>
+template <int BASIS, bool DET, bool MSEG = !DET>
 __global__ void __launch_bounds__(256) km_g2p_seg(MCtx A) {
-    g2p_seg_body<BASIS, DET>(A, blockIdx.x);
+    g2p_seg_body<BASIS, DET, MSEG>(A, blockIdx.x);
 }
 
 
@@ -843,7 +844,8 @@ __global__ void __launch_bounds__(4 * TP_CELLS) km_p2g_tile(MCtx A) {
 // Σ N m δJ (KIND 2: the per-point value left in ptmp by km_fbar_seg, volumetric.jl:1-11): the
 // tile staging of km_p2g_tile, each cell's points summed in list (point id) order into the
 // cell's node partials.
-template <int BASIS, int TP_CELLS, int KIND>
+// ATOMIC: the cell sums go to the nodes with FP32 atomics (else per-cell partials for km_gather)
+template <int BASIS, int TP_CELLS, int KIND, bool ATOMIC = false>
 __global__ void __launch_bounds__(4 * TP_CELLS) km_aux_tile(MCtx A) {
     constexpr int TP_THREADS = 4 * TP_CELLS, NQ = KIND == 1 ? 2 : 1, ST = 11;
     EP_ACTIVE(A.ctl);
@@ -902,10 +904,27 @@ __global__ void __launch_bounds__(4 * TP_CELLS) km_aux_tile(MCtx A) {
     }
     if (bad) set_err(A.ctl, EP_ERR_INVALID_POSITION, c0);
     if (!cell_ok || pb == pe) return;
+    if (ATOMIC) {
+        const int ex = cl / A.g.nel[1], ez = cl - ex * A.g.nel[1];
+        const Axis4 ax = axis4(A.g, 0, ex), az = axis4(A.g, 1, ez);
+        if (ax.cls[q] < 0) return;
 #pragma unroll
-    for (int j = 0; j < 4; ++j)
+        for (int j = 0; j < 4; ++j) {
+            if (az.cls[j] < 0) continue;
+            const int n = node2(A.g, ax, az, q, j);
+            if (KIND == 1) {
+                atomicAdd(&A.N.pm[0][n], acc[j][0]);
+                atomicAdd(&A.N.pm[1][n], acc[j][NQ - 1]);
+            } else {
+                atomicAdd(&A.N.dJacc[n], acc[j][0]);
+            }
+        }
+    } else {
 #pragma unroll
-        for (int v = 0; v < NQ; ++v) A.part[((size_t)cl * 16 + q * 4 + j) * NQ + v] = acc[j][v];
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int v = 0; v < NQ; ++v) A.part[((size_t)cl * 16 + q * 4 + j) * NQ + v] = acc[j][v];
+    }
 }
 
 // node sums of the per-cell partials: the cells whose stencil holds node (ix, jz) are
@@ -3695,7 +3714,8 @@ static void mixed_step_impl(const MixedCtx& X, int phase, cudaStream_t s) {
     mark("p2g");
     km_solve<<<gn, 256, 0, s>>>(A);
     mark("solve");
-    km_g2p_seg<BASIS, DET><<<gs, 256, 0, s>>>(A);
+    if (DET) km_g2p_seg<BASIS, true><<<gs, 256, 0, s>>>(A);
+    else km_g2p_seg<BASIS, false, false><<<gs, 256, 0, s>>>(A);
     mark("g2p");
     L += 3;
     if (A.cf.musl) {
@@ -3704,6 +3724,13 @@ static void mixed_step_impl(const MixedCtx& X, int phase, cudaStream_t s) {
             km_gather<2><<<gn, 256, 0, s>>>(A, A.N.pm[0], A.N.pm[1], nullptr, nullptr, nullptr);
             mark("musl");
             L += 2;
+        } else {
+            // the mUSL momentum P2G (augm.jl:13-25) in the tile form, FP32 atomics per node
+            if (X.p2g_tile == 16) km_aux_tile<BASIS, 16, 1, true><<<(nc + 15) / 16, 64, 0, s>>>(A);
+            else if (X.p2g_tile == 32) km_aux_tile<BASIS, 32, 1, true><<<(nc + 31) / 32, 128, 0, s>>>(A);
+            else km_aux_tile<BASIS, 64, 1, true><<<(nc + 63) / 64, 256, 0, s>>>(A);
+            mark("musl");
+            ++L;
         }
         km_vmusl<<<gn, 256, 0, s>>>(A);
         mark("vmusl");
