@@ -37,7 +37,19 @@ METRIC = "particle-steps/s on GB300: mixed+learned vs plain FP64, at stated stre
 WORKLOAD = "2d slump nel=[640,160], 3x3 points/cell (365,024 points), elastoplastic step"
 
 
-def make_workload():
+def oracle_cohesion(X, cmpr, instr, mesh):
+    """The same seeded cohesion field from the CPU restatement (oracle/grf_oracle.py), for the
+    reference arm, which runs none of the library's kernels."""
+    import grf_oracle
+    p = dict(instr["grf"].get("param", {}))
+    mean = float(p.get("mean", cmpr["c0"]))
+    dim = mesh.dim
+    return grf_oracle.field(X, dim, instr["grf"].get("covariance", "gaussian"), list(p.get("Ix", [2.5] * 3))[:dim],
+                            mean, float(p.get("cov", 0.3)) * mean, float(p.get("min", cmpr["cr"])),
+                            int(p.get("Nh", 5000)), int(p.get("seed", 1234)))
+
+
+def make_workload(grf_fn=None):
     from epgpu import ic_slump
     fw = {"deform": "finite", "trsfr": "std", "C_pf": 1.0, "musl": True, "locking": True, "damping": 0.1}
     kw = dict(fwrk=fw, nonloc={"status": False, "ls": 0.5})
@@ -49,7 +61,7 @@ def make_workload():
         field = "seeded exponential-covariance random field (mean 20 kPa, CoV 0.3, 5 m, >= 1 kPa)"
     except ImportError:
         pass
-    ic, cfg = ic_slump([64.1584, 16.0396], [640, 160], ni=3, **kw)
+    ic, cfg = ic_slump([64.1584, 16.0396], [640, 160], ni=3, grf_fn=grf_fn, **kw)
     return ic, cfg, field
 
 
@@ -237,17 +249,32 @@ def cpu_sample(ic, cfg, seconds_budget=20.0, threads=None):
 def run_reference(args, rank, ws):
     if rank != 0:
         return
-    ic, cfg, field = make_workload()
+    ic, cfg, field = make_workload(grf_fn=oracle_cohesion)
     if args.settle > 0:
         import oracle
         o = oracle.Oracle(ic, cfg["instr"], threads=os.cpu_count() or 1)
         o.run(1, args.settle, 10.0, 0.0)
         ic["mpts"] = o.download()
         o.close()
-    val, threads, steps, el = cpu_sample(ic, cfg, seconds_budget=max(10.0, 2.0 * args.steps))
+    # W untimed and K timed steps of the whole workload on all host threads (one CPU step is ~40 ms
+    # on 16 Grace cores at nel=[640,160])
+    import oracle
+    threads = os.cpu_count() or 1
+    o = oracle.Oracle(ic, cfg["instr"], threads=threads)
+    vmax = ic["mpts"].vmax.copy()
+    g = [0.0] * (ic["mesh"].dim - 1) + [-9.81]
+    for _ in range(args.warmup):
+        vmax = o.step(1, cfl_dt(ic["mesh"], ic["cmpr"], vmax), g)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        vmax = o.step(1, cfl_dt(ic["mesh"], ic["cmpr"], vmax), g)
+    el = time.perf_counter() - t0
+    o.close()
+    steps = args.steps
+    val = ic["mpts"].nmp * steps / el
     line = {
         "impl": "reference", "metric": METRIC, "value": val, "unit": "particle-steps/s", "n_gpus": args.gpus,
-        "steps": steps, "warmup": 0, "ms_per_step": 1e3 * el / steps, "higher_is_better": True,
+        "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": f"synthetic ({field})",
         "config": {"workload": WORKLOAD, "points": ic["mpts"].nmp, "nodes": ic["mesh"].nnodes},
         "cpu_baseline": {"value": val, "unit": "particle-steps/s", "cores": threads, "kind": "port",
