@@ -471,7 +471,7 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
         bool ok2 = true;
         if (acc == 0) ok2 = dalloc(h, &pd, nacc * np) == cudaSuccess;
         // floats: dx[2][d], v[d], tau[nsym], 11 scalars, rho, l[d], dv[d*d], (pairs: 2*nacc)
-        const size_t nflt = (size_t)np * (2 * d + d + nsym + 11 + 1 + d + d * d + (acc ? 2 * nacc : 0));
+        const size_t nflt = (size_t)np * (2 * d + d + nsym + 11 + 1 + 2 * d + d * d + (acc ? 2 * nacc : 0));
         ok2 = ok2 && dalloc(h, &pf, nflt) == cudaSuccess;
         int* ints = nullptr;
         const size_t nint = (size_t)3 * nc + 2 * (size_t)(nc + 1) + 4 * (size_t)np + (size_t)np + 2 * (size_t)(nc + 1) +
@@ -495,6 +495,7 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
         take(1);   // spare
         pm.rho = take(1);
         for (int i = 0; i < d; ++i) pm.l[i] = take(1);
+        for (int i = 0; i < d; ++i) pm.l0[i] = take(1);
         for (int k = 0; k < d * d; ++k) pm.dv[k] = take(1);
         if (acc == 0) {
             double* q = pd;

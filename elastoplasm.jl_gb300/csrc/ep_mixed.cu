@@ -1302,6 +1302,117 @@ __device__ __forceinline__ void add_ep1(const MCtx& A, int p, float inc) {
     }
 }
 
+// one rotation zeroing a[P][Q] of the symmetric a, accumulated into the columns of v
+template <int P, int Q>
+__device__ __forceinline__ void jrot3f(float (&a)[3][3], float (&v)[3][3]) {
+    constexpr int R = 3 - P - Q;
+    const float apq = a[P][Q];
+    if (apq == 0.f) return;
+    const float th = (a[Q][Q] - a[P][P]) / (2.f * apq);
+    const float t = fabsf(th) > 1.0e15f ? 0.5f / th : copysignf(1.f, th) / (fabsf(th) + sqrtf(1.f + th * th));
+    const float c = 1.f / sqrtf(1.f + t * t), sn = t * c;
+    a[P][P] -= t * apq;
+    a[Q][Q] += t * apq;
+    a[P][Q] = a[Q][P] = 0.f;
+    const float arp = a[R][P], arq = a[R][Q];
+    a[R][P] = a[P][R] = c * arp - sn * arq;
+    a[R][Q] = a[Q][R] = sn * arp + c * arq;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const float vp = v[i][P], vq = v[i][Q];
+        v[i][P] = c * vp - sn * vq;
+        v[i][Q] = sn * vp + c * vq;
+    }
+}
+
+// eigenvalues (diagonal of a on return) and eigenvectors (columns of v) of a symmetric 3x3;
+// sweeps stop once the off-diagonal sum is below 1e-8 of the matrix norm (the eigenvalue error
+// it leaves is below that, Weyl)
+__device__ __forceinline__ void eig3f(float (&a)[3][3], float (&v)[3][3]) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) v[i][j] = i == j ? 1.f : 0.f;
+    const float nrm = fabsf(a[0][0]) + fabsf(a[1][1]) + fabsf(a[2][2]) +
+                      2.f * (fabsf(a[0][1]) + fabsf(a[0][2]) + fabsf(a[1][2]));
+#pragma unroll 1
+    for (int sw = 0; sw < 8; ++sw) {
+        if (fabsf(a[0][1]) + fabsf(a[0][2]) + fabsf(a[1][2]) <= 1.0e-8f * nrm) break;
+        jrot3f<0, 1>(a, v);
+        jrot3f<0, 2>(a, v);
+        jrot3f<1, 2>(a, v);
+    }
+}
+
+// det(I + D) - 1 of a 3x3 increment, without cancellation: tr D + principal minors + det D
+__device__ __forceinline__ float det1p_m1(const float* D) {
+    const float m2 = (D[0] * D[4] - D[3] * D[1]) + (D[0] * D[8] - D[6] * D[2]) + (D[4] * D[8] - D[7] * D[5]);
+    const float d3 = D[0] * (D[4] * D[8] - D[7] * D[5]) - D[3] * (D[1] * D[8] - D[7] * D[2]) +
+                     D[6] * (D[1] * D[5] - D[4] * D[2]);
+    return (D[0] + D[4] + D[8]) + m2 + d3;
+}
+
+// GIMP domain update (domain.jl:1-52 via update.jl:7-28), after F <- ΔF F with the unscaled ΔF.
+// ℓ from ℓ0 and the new F (det F, F_ii, U_ii of U = sqrt(F'F)) or from ℓ and ΔF (det ΔF, ΔF_ii,
+// U_ii of sqrt(ΔF'ΔF)).  Both tensors come in as deviations from I, column-major DIM x DIM (D = ΔF -
+// I, Fd = F - I), and every rule is applied as ℓ + ℓ (f - 1) with f - 1 formed without cancellation,
+// so that the per-step rounding of the incremental rules stays far below the increment itself.
+template <int DIM>
+__device__ __forceinline__ void gimp_domain(const MCtx& A, int p, const float* D, const float* Fd) {
+    const int how = A.cf.how;
+    if (how == EP_HOW_UNDEFORMED || how == EP_HOW_NONE) return;
+    const bool rel0 = how == EP_HOW_DETFIJ || how == EP_HOW_FII || how == EP_HOW_UII;   // from ℓ0
+    const float* M = rel0 ? Fd : D;
+    float fm1[3];
+    if (how == EP_HOW_DETFIJ || how == EP_HOW_DETDFIJ) {
+        const float j = DIM == 2 ? M[0] + M[3] + (M[0] * M[3] - M[2] * M[1]) : det1p_m1(M);
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) fm1[d] = j;
+    } else if (how == EP_HOW_FII || how == EP_HOW_DFII) {
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) fm1[d] = M[d + DIM * d];
+    } else {
+        // (I + M)'(I + M) - I = M + M' + M'M; U - I = Σ_k (sqrt(1 + μ_k) - 1) v_k v_k' over its
+        // eigenpairs, sqrt(1 + μ) - 1 = μ / (1 + sqrt(1 + μ))
+        float E[DIM][DIM];
+#pragma unroll
+        for (int i = 0; i < DIM; ++i)
+#pragma unroll
+            for (int j = 0; j < DIM; ++j) {
+                float acc = M[j + DIM * i] + M[i + DIM * j];
+#pragma unroll
+                for (int k = 0; k < DIM; ++k) acc += M[k + DIM * i] * M[k + DIM * j];
+                E[i][j] = acc;
+            }
+        if constexpr (DIM == 2) {
+            const float m = 0.5f * (E[0][0] + E[1][1]), q = 0.5f * (E[0][0] - E[1][1]);
+            const float r = sqrtf(q * q + E[0][1] * E[0][1]);
+            const float mu1 = m + r, mu2 = m - r;
+            const float s1 = mu1 / (1.f + sqrtf(1.f + mu1)), s2 = mu2 / (1.f + sqrtf(1.f + mu2));
+            const float c2 = r > 0.f ? q / r : 1.f;   // cos 2θ of the first eigenvector
+            fm1[0] = 0.5f * (s1 + s2) + 0.5f * (s1 - s2) * c2;
+            fm1[1] = 0.5f * (s1 + s2) - 0.5f * (s1 - s2) * c2;
+        } else {
+            float a[3][3], v[3][3];
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) a[i][j] = E[i][j];
+            eig3f(a, v);
+            float sk[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) sk[k] = a[k][k] / (1.f + sqrtf(1.f + a[k][k]));
+#pragma unroll
+            for (int d = 0; d < 3; ++d) fm1[d] = v[d][0] * v[d][0] * sk[0] + v[d][1] * v[d][1] * sk[1] + v[d][2] * v[d][2] * sk[2];
+        }
+    }
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        const float l = rel0 ? A.P.l0[d][p] : A.P.l[d][p];
+        A.P.l[d][p] = l + l * fm1[d];
+    }
+}
+
 // features of a finite-strain DP trial in the principal frame (ep_rmap.h layout, FP32):
 // x[8], aux = (cos 2θ, sin 2θ, s, c); returns whether the trial leaves the DP surface
 __device__ __forceinline__ bool rm_features32(float e11, float e22, float e12, float coh, float tphi, float Gc,
@@ -1348,12 +1459,11 @@ __device__ __forceinline__ void cons_body(const MCtx& A, int bid, int plastic_ph
         bool bad = false;
         const bool fin = A.cf.deform == EP_DEFORM_FINITE, lock = A.cf.locking;
         float wx[4], dwx[4], wz[4], dwz[4];
-        {
-            const float lx = BASIS == EP_BASIS_GIMPM ? A.P.l[0][p] : 0.f;
-            const float lz = BASIS == EP_BASIS_GIMPM ? A.P.l[1][p] : 0.f;
-            axis_w<BASIS>(ax, A.P.dx[cur][0][p], hx, 1.f / hx, lx, wx, dwx, bad);
-            axis_w<BASIS>(az, A.P.dx[cur][1][p], hz, 1.f / hz, lz, wz, dwz, bad);
-        }
+        // the half lengths of the step's shape functions (the domain update below rewrites ℓ)
+        const float lx = BASIS == EP_BASIS_GIMPM ? A.P.l[0][p] : 0.f;
+        const float lz = BASIS == EP_BASIS_GIMPM ? A.P.l[1][p] : 0.f;
+        axis_w<BASIS>(ax, A.P.dx[cur][0][p], hx, 1.f / hx, lx, wx, dwx, bad);
+        axis_w<BASIS>(az, A.P.dx[cur][1][p], hz, 1.f / hz, lz, wz, dwz, bad);
         float g00 = 0.f, g01 = 0.f, g10 = 0.f, g11 = 0.f, a = 0.f;
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
@@ -1379,6 +1489,7 @@ __device__ __forceinline__ void cons_body(const MCtx& A, int bid, int plastic_ph
         }
         // F <- ΔF F with the unscaled ΔF (deform.jl:14): F += D F
         float Jm1 = 0.f;   // J - 1 (infinitesimal mass)
+        float Fd[4];       // the new F - I (GIMP domain updates)
         if (ACC == 0) {
             const double F0 = A.P.Fd[0][p], F1 = A.P.Fd[1][p], F2 = A.P.Fd[2][p], F3 = A.P.Fd[3][p];
             const float f0 = (float)F0, f1 = (float)F1, f2 = (float)F2, f3 = (float)F3;
@@ -1387,6 +1498,7 @@ __device__ __forceinline__ void cons_body(const MCtx& A, int bid, int plastic_ph
             const double N2 = F2 + (double)(D[0] * f2 + D[2] * f3);
             const double N3 = F3 + (double)(D[1] * f2 + D[3] * f3);
             A.P.Fd[0][p] = N0; A.P.Fd[1][p] = N1; A.P.Fd[2][p] = N2; A.P.Fd[3][p] = N3;
+            Fd[0] = (float)(N0 - 1.0); Fd[1] = (float)N1; Fd[2] = (float)N2; Fd[3] = (float)(N3 - 1.0);
             if (!fin) Jm1 = (float)(N0 * N3 - N2 * N1 - 1.0);
         } else {
             float h0 = A.P.Fh[0][p], h1 = A.P.Fh[1][p], h2 = A.P.Fh[2][p], h3 = A.P.Fh[3][p];
@@ -1396,11 +1508,10 @@ __device__ __forceinline__ void cons_body(const MCtx& A, int bid, int plastic_ph
             df_add(h0, l0, i0); df_add(h1, l1, i1); df_add(h2, l2, i2); df_add(h3, l3, i3);
             A.P.Fh[0][p] = h0; A.P.Fh[1][p] = h1; A.P.Fh[2][p] = h2; A.P.Fh[3][p] = h3;
             A.P.Fl[0][p] = l0; A.P.Fl[1][p] = l1; A.P.Fl[2][p] = l2; A.P.Fl[3][p] = l3;
-            if (!fin) {
-                // J - 1 = (F11-1) + (F22-1) + (F11-1)(F22-1) - F12 F21, deviations formed exactly
-                const float a0 = (h0 - 1.f) + l0, a3 = (h3 - 1.f) + l3;
-                Jm1 = a0 + a3 + (a0 * a3 - (h2 + l2) * (h1 + l1));
-            }
+            // deviations from I formed exactly
+            Fd[0] = (h0 - 1.f) + l0; Fd[1] = h1 + l1; Fd[2] = h2 + l2; Fd[3] = (h3 - 1.f) + l3;
+            // J - 1 = (F11-1) + (F22-1) + (F11-1)(F22-1) - F12 F21
+            if (!fin) Jm1 = Fd[0] + Fd[3] + (Fd[0] * Fd[3] - Fd[2] * Fd[1]);
         }
         if (!fin) {
             // infinitesimal: volume J Ω0 and mass ρ J Ω0 follow J (deform.jl:41-43)
@@ -1408,12 +1519,13 @@ __device__ __forceinline__ void cons_body(const MCtx& A, int bid, int plastic_ph
             A.P.Om[p] = Om;
             A.P.mp[p] = A.P.rho[p] * Om;
         }
+        if (BASIS == EP_BASIS_GIMPM) gimp_domain<2>(A, p, D, Fd);
         // F-bar: ΔF <- (ΔJ̄/ΔJ)^(1/2) ΔF, ΔJ̄ = Σ N ΔJ_n (volumetric.jl:23-36), increment form
         if (lock) {
             float sm1 = 0.f;      // Σ N - 1 over the existing nodes (GIMP next to a mesh edge)
             if (BASIS == EP_BASIS_GIMPM) {
-                const float mx = axis_miss<BASIS>(ax, A.P.dx[cur][0][p], hx, A.P.l[0][p]);
-                const float mz = axis_miss<BASIS>(az, A.P.dx[cur][1][p], hz, A.P.l[1][p]);
+                const float mx = axis_miss<BASIS>(ax, A.P.dx[cur][0][p], hx, lx);
+                const float mz = axis_miss<BASIS>(az, A.P.dx[cur][1][p], hz, lz);
                 sm1 = -(mx + mz) + mx * mz;
             }
             const float dJp = D[0] + D[3] + (D[0] * D[3] - D[2] * D[1]);
@@ -1967,7 +2079,10 @@ __global__ void km_import(MCtx A, P64 Q) {
     const int D = A.g.dim, NS = D == 2 ? 3 : 6;
     for (int d = 0; d < D; ++d) {
         A.P.v[d][p] = (float)Q.v[d][p];
-        if (A.cf.basis == EP_BASIS_GIMPM) A.P.l[d][p] = (float)Q.l[d][p];
+        if (A.cf.basis == EP_BASIS_GIMPM) {
+            A.P.l[d][p] = (float)Q.l[d][p];
+            A.P.l0[d][p] = (float)Q.l0[d][p];
+        }
     }
     double bsym[6];
     for (int k = 0; k < NS; ++k) {
@@ -2206,14 +2321,6 @@ __device__ __forceinline__ float dpf6(float* s, float ep2, float c0, float cr, f
         *dep = 1.41421356237309505f * dl / 3.f;
     }
     return dl;
-}
-
-// det(I + D) - 1 of a 3x3 increment, without cancellation: tr D + principal minors + det D
-__device__ __forceinline__ float det1p_m1(const float* D) {
-    const float m2 = (D[0] * D[4] - D[3] * D[1]) + (D[0] * D[8] - D[6] * D[2]) + (D[4] * D[8] - D[7] * D[5]);
-    const float d3 = D[0] * (D[4] * D[8] - D[7] * D[5]) - D[3] * (D[1] * D[8] - D[7] * D[2]) +
-                     D[6] * (D[1] * D[5] - D[4] * D[2]);
-    return (D[0] + D[4] + D[8]) + m2 + d3;
 }
 
 struct PtW3 {
@@ -2663,48 +2770,6 @@ __global__ void __launch_bounds__(32) km_nonlocal3(MCtx A) {
 // Loan, Matrix Computations, sym.Schur2 and the cyclic Jacobi method, the algorithm of ep_scalar.h
 // eig_sym3); FP64 storage ("mixed"): eig_sym3 itself on M in FP64.
 
-// one rotation zeroing a[P][Q] of the symmetric a, accumulated into the columns of v
-template <int P, int Q>
-__device__ __forceinline__ void jrot3f(float (&a)[3][3], float (&v)[3][3]) {
-    constexpr int R = 3 - P - Q;
-    const float apq = a[P][Q];
-    if (apq == 0.f) return;
-    const float th = (a[Q][Q] - a[P][P]) / (2.f * apq);
-    const float t = fabsf(th) > 1.0e15f ? 0.5f / th : copysignf(1.f, th) / (fabsf(th) + sqrtf(1.f + th * th));
-    const float c = 1.f / sqrtf(1.f + t * t), sn = t * c;
-    a[P][P] -= t * apq;
-    a[Q][Q] += t * apq;
-    a[P][Q] = a[Q][P] = 0.f;
-    const float arp = a[R][P], arq = a[R][Q];
-    a[R][P] = a[P][R] = c * arp - sn * arq;
-    a[R][Q] = a[Q][R] = sn * arp + c * arq;
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        const float vp = v[i][P], vq = v[i][Q];
-        v[i][P] = c * vp - sn * vq;
-        v[i][Q] = sn * vp + c * vq;
-    }
-}
-
-// eigenvalues (diagonal of a on return) and eigenvectors (columns of v) of a symmetric 3x3;
-// sweeps stop once the off-diagonal sum is below 1e-8 of the matrix norm (the eigenvalue error
-// it leaves is below that, Weyl)
-__device__ __forceinline__ void eig3f(float (&a)[3][3], float (&v)[3][3]) {
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int j = 0; j < 3; ++j) v[i][j] = i == j ? 1.f : 0.f;
-    const float nrm = fabsf(a[0][0]) + fabsf(a[1][1]) + fabsf(a[2][2]) +
-                      2.f * (fabsf(a[0][1]) + fabsf(a[0][2]) + fabsf(a[1][2]));
-#pragma unroll 1
-    for (int sw = 0; sw < 8; ++sw) {
-        if (fabsf(a[0][1]) + fabsf(a[0][2]) + fabsf(a[1][2]) <= 1.0e-8f * nrm) break;
-        jrot3f<0, 1>(a, v);
-        jrot3f<0, 2>(a, v);
-        jrot3f<1, 2>(a, v);
-    }
-}
-
 // sym index k (Voigt xx, yy, zz, yz, xz, xy) -> (i, j)
 __host__ __device__ constexpr int vi3(int k) { return k < 3 ? k : (k == 3 ? 1 : 0); }
 __host__ __device__ constexpr int vj3(int k) { return k < 3 ? k : (k == 5 ? 1 : 2); }
@@ -2963,6 +3028,18 @@ __global__ void __launch_bounds__(256, 3) km_cons3(MCtx A, int plastic_phase) {
                 Fdev[i] = dg ? (h[i] - 1.f) + l[i] : h[i] + l[i];
             }
         }
+        // Σ N - 1 over the existing nodes (GIMP next to a mesh edge), from the step's half lengths:
+        // taken before the domain update rewrites ℓ
+        float sm1 = 0.f;
+        if (BASIS == EP_BASIS_GIMPM) {
+            if (lock) {
+                float ms[3];
+#pragma unroll
+                for (int d = 0; d < 3; ++d) ms[d] = axis_miss<BASIS>(W.a[d], W.o[d], (float)A.g.h[d], A.P.l[d][p]);
+                sm1 = -(ms[0] + ms[1] + ms[2]) + (ms[0] * ms[1] + ms[0] * ms[2] + ms[1] * ms[2]) - ms[0] * ms[1] * ms[2];
+            }
+            gimp_domain<3>(A, p, D, Fdev);
+        }
         if (!FIN) {
             // infinitesimal: volume J Ω0 and mass ρ J Ω0 follow J (deform.jl:41-43)
             const float Jm1 = det1p_m1(Fdev);
@@ -2972,13 +3049,6 @@ __global__ void __launch_bounds__(256, 3) km_cons3(MCtx A, int plastic_phase) {
         }
         // F-bar: ΔF <- (ΔJ̄/ΔJ)^(1/3) ΔF (volumetric.jl:23-36), increment form
         if (lock) {
-            float sm1 = 0.f;      // Σ N - 1 over the existing nodes (GIMP next to a mesh edge)
-            if (BASIS == EP_BASIS_GIMPM) {
-                float ms[3];
-#pragma unroll
-                for (int d = 0; d < 3; ++d) ms[d] = axis_miss<BASIS>(W.a[d], W.o[d], (float)A.g.h[d], A.P.l[d][p]);
-                sm1 = -(ms[0] + ms[1] + ms[2]) + (ms[0] * ms[1] + ms[0] * ms[2] + ms[1] * ms[2]) - ms[0] * ms[1] * ms[2];
-            }
             const float dJp = det1p_m1(D);
             const float r1 = (sm1 + a - dJp) / (1.f + dJp);
             const float s1 = expm1f(log1pf(r1) * (1.f / 3.f));

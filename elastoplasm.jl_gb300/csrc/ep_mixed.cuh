@@ -37,6 +37,7 @@ struct PM {
     float* Om;         // current volume (infinitesimal: J Ω0)
     float* rho;        // density (infinitesimal: stays at its uploaded value, deform.jl:25-44)
     float* l[3];       // GIMP half lengths
+    float* l0[3];      // GIMP initial half lengths (domain updates relative to them, domain.jl:1-52)
     float* dv[9];      // TPIC: velocity gradient of the previous step
     int* p2e_next;     // cell of the position written by the last G2P
     int* pcell[2];     // [parity] cell of each point (nonlocal averaging: the cell at the step start)

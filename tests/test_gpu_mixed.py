@@ -96,6 +96,28 @@ def test_mixed_other_bases(oracle_mod, basis, precision):
     assert s < STRESS_TOL and d < DISP_TOL
 
 
+@pytest.mark.parametrize("how", ["detFij", "Fii", "Uii", "detΔFij", "ΔFii", "ΔUii"])
+def test_mixed_gimp_domain_updates(oracle_mod, how):
+    """The GIMP domain rules of basis.how (domain.jl:1-52): finite strain from ℓ0 and F, infinitesimal
+    from ℓ and ΔF, against the FP64 oracle (stress, displacement and the half lengths ℓ)."""
+    from epgpu import Engine, ic_slump
+    fwrk = {"deform": "finite" if "Δ" not in how else "infinitesimal", "trsfr": "std", "C_pf": 1.0,
+            "musl": True, "locking": True, "damping": 0.1}
+    ic, cfg = ic_slump(*C1, basis={"which": "gimpm", "how": how, "ghost": False}, fwrk=fwrk,
+                       nonloc={"status": False, "ls": 0.5})
+    x0, l0 = ic["mpts"].x.copy(), ic["mpts"].l.copy()
+    o = oracle_mod.Oracle(copy.deepcopy(ic), cfg["instr"])
+    e = Engine(copy.deepcopy(ic), _mixed(cfg["instr"], "mixed_df"))
+    _run(o, e, ((0, 2.0), (1, 2.5)))
+    a, b = e.download(), o.download()
+    s, d, r = errors(a, b, x0)
+    dl = np.abs(a.l - b.l).max() / np.abs(b.l).max()
+    moved = np.abs(b.l - l0).max() / np.abs(l0).max()
+    print(f"gimpm how={how}: stress {s:.3e} displacement {d:.3e} half lengths {dl:.2e} (they moved by {moved:.2e})")
+    assert moved > 1e-5
+    assert s < STRESS_TOL and d < DISP_TOL and dl < 1e-5
+
+
 @pytest.mark.parametrize("precision", PRECISIONS)
 def test_mixed_full_all_in_one_config1(oracle_mod, precision):
     # the whole 15 s workflow; the error grows with plastic flow and softening, so it is reported

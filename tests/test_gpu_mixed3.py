@@ -99,6 +99,11 @@ FIN_CASES = {
     "finite_dp_config5_noghost": (dict(basis={"which": "gimpm", "how": "undeformed", "ghost": False}, fwrk=C5_FWRK),
                                   C5_OVER, 1e-2, False),
     "finite_j2_fbar": (dict(**J2), {"c0": 5.0e4, "Hp": 1.0e5}, 0.0, False),
+    # GIMP domain rules (domain.jl:1-52) on the config-5 switches without ghost nodes
+    "finite_dp_gimp_Uii": (dict(basis={"which": "gimpm", "how": "Uii", "ghost": False}, fwrk=C5_FWRK),
+                           C5_OVER, 1e-2, False),
+    "infinitesimal_dp_gimp_dUii": (dict(basis={"which": "gimpm", "how": "ΔUii", "ghost": False},
+                                        fwrk={**C5_FWRK, "deform": "infinitesimal"}), C5_OVER, 1e-2, False),
     # nonlocal averaging on (the reference's default): ϵpII[2] from the neighbourhood sums
     "finite_dp_defaults_nonlocal": (dict(nonloc={"status": True, "ls": 0.5}), None, 0.0, False),
     "infinitesimal_dp_musl_fbar_nonlocal": ({"fwrk": {"deform": "infinitesimal", "trsfr": "std", "C_pf": 1.0,
@@ -174,5 +179,9 @@ def test_mixed3d_finite_vs_oracle(oracle_mod, case, precision):
     # σ = τ / J of the downloaded state (the reference's σ field is the one formed at the start of
     # the last step's P2G, p2n.jl:12-21, one step older)
     fin = kw.get("fwrk", {}).get("deform", "finite") == "finite"
+    if kw.get("basis", {}).get("how") not in (None, "undeformed"):
+        dl = np.abs(a.l - b.l).max() / np.abs(b.l).max()
+        print(f"half lengths: max rel diff {dl:.2e}")
+        assert dl < 1e-5
     sig_now = b.tau / np.asarray(b.J).reshape(1, -1) if fin else b.sig
     np.testing.assert_allclose(a.sig, sig_now, rtol=0, atol=10 * tol * np.abs(sig_now).max())
