@@ -369,7 +369,8 @@ def c3_bench(args, rank, ws):
     np_ = mpts.nmp
     g = [0.0, 0.0, -9.81]
     instr = dict(cfg["instr"])
-    instr["gpu"] = {"precision": args.precision if args.precision != "fp64" else "mixed_df", "jaumann": False}
+    instr["gpu"] = {"precision": args.precision if args.precision != "fp64" else "mixed_df", "jaumann": False,
+                    "deterministic": args.deterministic}
     e = Engine(ic, instr)
     e.run(1, args.settle, 10.0, 0.0)
     host0 = e.download()
@@ -421,7 +422,8 @@ def c3_bench(args, rank, ws):
         "config": {"workload": f"3d slump L=[64.1584,16.0396,16.0396], nel={nel}, 2x2x2 points/cell, GIMP "
                                "(ghost), TPIC (PIC), USL, infinitesimal J2 (E=1e7, rho=2000, c0=50 kPa, H=1e5)",
                    "points": np_, "nodes": mesh.nnodes, "setup_s": setup_s, "settle_s": args.settle,
-                   "precision": instr["gpu"]["precision"], "l2": "flushed between timed steps (256 MB write)"},
+                   "precision": instr["gpu"]["precision"], "deterministic": args.deterministic,
+                   "l2": "flushed between timed steps (256 MB write)"},
         "kernel_share": {k: round(v[1] / tot, 4) for k, v in kt.items()},
         "fp64_step": {"ms_per_step": t64 / len(dts), "value": np_ * len(dts) / (t64 * 1e-3),
                       "unit": "particle-steps/s"},

@@ -122,39 +122,6 @@ __global__ void k_soa_to_aos(const double* __restrict__ in, int k, int np, doubl
     for (int c = 0; c < k; ++c) out[(size_t)c + (size_t)k * p] = in[(size_t)c * np + p];
 }
 
-// host AoS field (k components per point) -> device SoA block; multi-component fields go through
-// their own slot of the staging area at `off` (advanced), so the copies and transposes of all
-// fields queue on the stream without waiting for one another
-static ep_status put_aos(ep_handle* h, const double* host, int k, double* dev_block, size_t& off) {
-    size_t n = (size_t)k * h->np;
-    if (k > 1) off += n;
-    if (!host || n == 0) return EP_OK;
-    if (k == 1) {
-        CK(h, cudaMemcpyAsync(dev_block, host, n * sizeof(double), cudaMemcpyHostToDevice, h->s));
-        return EP_OK;
-    }
-    double* st = h->xfer + (off - n);
-    CK(h, cudaMemcpyAsync(st, host, n * sizeof(double), cudaMemcpyHostToDevice, h->s));
-    k_aos_to_soa<<<(h->np + 255) / 256, 256, 0, h->s>>>(st, k, h->np, dev_block);
-    CK(h, cudaGetLastError());
-    return EP_OK;
-}
-
-static ep_status get_aos(ep_handle* h, const double* dev_block, int k, double* host, size_t& off) {
-    size_t n = (size_t)k * h->np;
-    if (k > 1) off += n;
-    if (!host || n == 0) return EP_OK;
-    if (k == 1) {
-        CK(h, cudaMemcpyAsync(host, dev_block, n * sizeof(double), cudaMemcpyDeviceToHost, h->s));
-        return EP_OK;
-    }
-    double* st = h->xfer + (off - n);
-    k_soa_to_aos<<<(h->np + 255) / 256, 256, 0, h->s>>>(dev_block, k, h->np, st);
-    CK(h, cudaGetLastError());
-    CK(h, cudaMemcpyAsync(host, st, n * sizeof(double), cudaMemcpyDeviceToHost, h->s));
-    return EP_OK;
-}
-
 // point field blocks inside pbuf
 enum Fld {
     F_X, F_XO, F_V, F_L, F_L0, F_N0, F_N, F_OM0, F_OM, F_DJ, F_J, F_RHO0, F_RHO, F_C0, F_CR, F_TPHI, F_SPHI, F_CPHI,
@@ -234,8 +201,6 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
     }
     if (cfg->precision != EP_PREC_FP64 && cfg->precision != EP_PREC_MIXED && cfg->precision != EP_PREC_MIXED_DF)
         return fail(nullptr, EP_ERR_UNSUPPORTED, "unknown precision");
-    if (cfg->precision != EP_PREC_FP64 && d == 3 && cfg->deterministic)
-        return fail(nullptr, EP_ERR_UNSUPPORTED, "the deterministic mode is built for the 2d mixed step");
     if (cfg->nonloc && !(cfg->nonloc_ls > 0.0)) return fail(nullptr, EP_ERR_ARG, "nonloc.ls must be > 0");
     if (!mesh->x || !mesh->xB || !mesh->bcs) return fail(nullptr, EP_ERR_ARG, "mesh.x, mesh.xB and mesh.bcs are required");
     long long nnode = 1, ncell = 1;
@@ -569,7 +534,9 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
         h->mx.p2g_tile = 64;
         if (cf.det) {
             float *part = nullptr, *ptmp = nullptr;
-            if (dalloc(h, &part, (size_t)nc * 16 * 5) != cudaSuccess || dalloc(h, &ptmp, (size_t)np) != cudaSuccess) {
+            // per-cell node partials: 16 slots x (m, p, f) in 2d, 64 slots x (m, p, f) in 3d
+            const size_t nslot = d == 3 ? (size_t)64 * 7 : (size_t)16 * 5;
+            if (dalloc(h, &part, (size_t)nc * nslot) != cudaSuccess || dalloc(h, &ptmp, (size_t)np) != cudaSuccess) {
                 epgpu_destroy(h);
                 return fail(nullptr, EP_ERR_NOMEM, "device allocation (deterministic partials)");
             }
@@ -590,26 +557,151 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
     return EP_OK;
 }
 
+// Point-field transfers.  Host fields are AoS (k components per point, column-major k x np); the
+// device blocks are SoA.  A host buffer that the runtime reports as page-locked and mapped
+// (cudaHostAlloc, cudaHostRegister, a pinned tensor) is read or written in place by k_xfer, one
+// launch over all such fields that also transposes; any other buffer goes through the copy engine
+// (multi-component fields through their slot of the staging area) and k_aos_to_soa/k_soa_to_aos.
+// The host link is the bound either way; one kernel over all fields saves the per-copy setup of
+// the ~30 separate copies.
+constexpr int XF_MAX = 32, XF_EPT = 8, XF_BS = 256;
+struct XferTab {
+    const double* src[XF_MAX];
+    double* dst[XF_MAX];
+    long long cnt[XF_MAX];   // elements (k x np)
+    int k[XF_MAX];
+    int b0[XF_MAX + 1];      // first block of each field
+    int n, dir;              // dir 0: host AoS -> device SoA; 1: device SoA -> host AoS
+};
+
+// XF_EPT elements per thread, all loads issued before the stores (many requests in flight on
+// the host link); element j of the AoS side is component j % k of point j / k
+__global__ void __launch_bounds__(XF_BS) k_xfer(const XferTab T) {
+    const int b = blockIdx.x;
+    int e = 0;
+    while (e + 1 < T.n && T.b0[e + 1] <= b) ++e;
+    const long long n = T.cnt[e], base = (long long)(b - T.b0[e]) * XF_BS * XF_EPT;
+    const int k = T.k[e];
+    const long long np = n / k;
+    const double* __restrict__ src = T.src[e];
+    double* __restrict__ dst = T.dst[e];
+    double v[XF_EPT];
+#pragma unroll
+    for (int i = 0; i < XF_EPT; ++i) {
+        const long long j = base + (long long)i * XF_BS + threadIdx.x;
+        if (j < n) {
+            const long long q = j / k, c = j - q * k;
+            v[i] = T.dir == 0 ? src[j] : src[c * np + q];
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < XF_EPT; ++i) {
+        const long long j = base + (long long)i * XF_BS + threadIdx.x;
+        if (j < n) {
+            const long long q = j / k, c = j - q * k;
+            if (T.dir == 0) dst[c * np + q] = v[i];
+            else dst[j] = v[i];
+        }
+    }
+}
+
+// the device address of a mapped page-locked host buffer, else null (pageable memory)
+static double* mapped_host(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return (a.type == cudaMemoryTypeHost && a.devicePointer) ? (double*)a.devicePointer : nullptr;
+}
+
+struct XField {
+    double* host;
+    int k;
+    double* dev;
+    size_t n;
+    double* stage;   // staging slot (k > 1)
+};
+
+// every point field of the view in transfer order, then the pass-through fields (u, p, ∇u, ϵpV:
+// stored as given, k = 1)
+static std::vector<XField> xfer_fields(ep_handle* h, const ep_mpts_view* m) {
+    const int d = h->dim, ns = h->nstr;
+    const size_t np = (size_t)h->np, dn = (size_t)d * np;
+    std::vector<XField> f;
+    size_t off = 0;
+    auto add = [&](const double* host, int k, double* dev) {
+        const size_t n = (size_t)k * np;
+        double* st = nullptr;
+        if (k > 1) {
+            st = h->xfer + off;
+            off += n;
+        }
+        if (host && n) f.push_back({const_cast<double*>(host), k, dev, n, st});
+    };
+    auto raw = [&](const double* host, double* dev, size_t n) {
+        if (host && n) f.push_back({const_cast<double*>(host), 1, dev, n, nullptr});
+    };
+    add(m->x, d, fld_ptr(h, F_X)); add(m->v, d, fld_ptr(h, F_V)); add(m->l, d, fld_ptr(h, F_L));
+    add(m->l0, d, fld_ptr(h, F_L0)); add(m->n0, 1, fld_ptr(h, F_N0)); add(m->n, 1, fld_ptr(h, F_N));
+    add(m->Omega0, 1, fld_ptr(h, F_OM0)); add(m->Omega, 1, fld_ptr(h, F_OM)); add(m->dJ, 1, fld_ptr(h, F_DJ));
+    add(m->J, 1, fld_ptr(h, F_J)); add(m->rho0, 1, fld_ptr(h, F_RHO0)); add(m->rho, 1, fld_ptr(h, F_RHO));
+    add(m->c0, 1, fld_ptr(h, F_C0)); add(m->cr, 1, fld_ptr(h, F_CR)); add(m->dlam, 1, fld_ptr(h, F_DLAM));
+    add(m->epII, 2, fld_ptr(h, F_EP)); add(m->sig, ns, fld_ptr(h, F_SIG)); add(m->tau, ns, fld_ptr(h, F_TAU));
+    add(m->dvij, d * d, fld_ptr(h, F_DV)); add(m->dFij, d * d, fld_ptr(h, F_DF)); add(m->Fij, d * d, fld_ptr(h, F_F));
+    add(m->bij, d * d, fld_ptr(h, F_B)); add(m->eij, d * d, fld_ptr(h, F_EPS)); add(m->wij, d * d, fld_ptr(h, F_W));
+    add(m->sJij, d * d, fld_ptr(h, F_SJ));
+    raw(m->u, h->pass, dn);
+    raw(m->p, h->pass + dn, dn);
+    raw(m->duij, h->pass + 2 * dn, (size_t)d * dn);
+    raw(m->epV, h->pass + (2 + d) * dn, np);
+    return f;
+}
+
+// fields on mapped host memory -> the k_xfer table; the rest -> `rest`
+static void xfer_split(std::vector<XField>& f, int dir, XferTab& T, int& nblk, std::vector<XField*>& rest) {
+    T.n = 0;
+    T.dir = dir;
+    nblk = 0;
+    for (auto& x : f) {
+        double* hp = T.n < XF_MAX ? mapped_host(x.host) : nullptr;
+        if (!hp) {
+            rest.push_back(&x);
+            continue;
+        }
+        T.src[T.n] = dir == 0 ? hp : x.dev;
+        T.dst[T.n] = dir == 0 ? x.dev : hp;
+        T.cnt[T.n] = (long long)x.n;
+        T.k[T.n] = x.k;
+        T.b0[T.n] = nblk;
+        nblk += (int)((x.n + (size_t)XF_BS * XF_EPT - 1) / ((size_t)XF_BS * XF_EPT));
+        ++T.n;
+    }
+    T.b0[T.n] = nblk;
+}
+
 ep_status epgpu_upload(ep_handle* h, const ep_mpts_view* m) {
     if (!h || !m) return EP_ERR_ARG;
     if (m->nmp != h->np || m->ndim != h->dim) return fail(h, EP_ERR_ARG, "mpts.nmp/ndim differ from create");
-    const int d = h->dim, ns = h->nstr;
+    const int d = h->dim;
     if (!m->x || !m->v || !m->Omega0 || !m->Omega || !m->J || !m->rho0 || !m->rho || !m->c0 || !m->cr || !m->phi ||
         !m->dlam || !m->epII || !m->sig || !m->tau || !m->Fij || !m->bij || !m->l || !m->l0 || !m->n0 || !m->n ||
         !m->dJ || !m->dvij)
         return fail(h, EP_ERR_ARG, "a point field read by the step is NULL");
-    ep_status st;
-    size_t off = 0;
-#define PUT(ptr, k, f) if ((st = put_aos(h, (ptr), (k), fld_ptr(h, (f)), off)) != EP_OK) return st
-    PUT(m->x, d, F_X); PUT(m->v, d, F_V); PUT(m->l, d, F_L); PUT(m->l0, d, F_L0);
-    PUT(m->n0, 1, F_N0); PUT(m->n, 1, F_N); PUT(m->Omega0, 1, F_OM0); PUT(m->Omega, 1, F_OM); PUT(m->dJ, 1, F_DJ);
-    PUT(m->J, 1, F_J); PUT(m->rho0, 1, F_RHO0); PUT(m->rho, 1, F_RHO); PUT(m->c0, 1, F_C0); PUT(m->cr, 1, F_CR);
-    PUT(m->dlam, 1, F_DLAM); PUT(m->epII, 2, F_EP); PUT(m->sig, ns, F_SIG); PUT(m->tau, ns, F_TAU);
-    PUT(m->dvij, d * d, F_DV); PUT(m->dFij, d * d, F_DF); PUT(m->Fij, d * d, F_F); PUT(m->bij, d * d, F_B);
-    PUT(m->eij, d * d, F_EPS); PUT(m->wij, d * d, F_W); PUT(m->sJij, d * d, F_SJ);
-#undef PUT
+    // the copies (back to back on the copy engine), then one k_xfer over the mapped host buffers
+    std::vector<XField> f = xfer_fields(h, m);
+    std::vector<XField*> rest;
+    XferTab T;
+    int nblk = 0;
+    xfer_split(f, 0, T, nblk, rest);
+    for (XField* x : rest)
+        CK(h, cudaMemcpyAsync(x->k > 1 ? x->stage : x->dev, x->host, x->n * sizeof(double), cudaMemcpyHostToDevice, h->s));
+    if (T.n) {
+        k_xfer<<<nblk, XF_BS, 0, h->s>>>(T);
+        CK(h, cudaGetLastError());
+    }
     // tan/sin/cos of the friction angle, evaluated on the host (material constants), again only
-    // when ϕ differs from the last upload
+    // when ϕ differs from the last upload (the comparison runs while the transfers are in flight)
     const size_t np = (size_t)h->np;
     if (h->phi_cache.size() != np || (np && std::memcmp(h->phi_cache.data(), m->phi, np * sizeof(double)) != 0)) {
         CK(h, cudaStreamSynchronize(h->s));          // tphi_host may still be read by the last copy
@@ -623,15 +715,9 @@ ep_status epgpu_upload(ep_handle* h, const ep_mpts_view* m) {
         h->phi_cache.assign(m->phi, m->phi + np);
         CK(h, cudaMemcpyAsync(fld_ptr(h, F_TPHI), t, 3 * np * sizeof(double), cudaMemcpyHostToDevice, h->s));
     }
-    {
-        const size_t dn = (size_t)d * np;
-        if (m->u) CK(h, cudaMemcpyAsync(h->pass, m->u, dn * sizeof(double), cudaMemcpyHostToDevice, h->s));
-        if (m->p) CK(h, cudaMemcpyAsync(h->pass + dn, m->p, dn * sizeof(double), cudaMemcpyHostToDevice, h->s));
-        if (m->duij)
-            CK(h, cudaMemcpyAsync(h->pass + 2 * dn, m->duij, d * dn * sizeof(double), cudaMemcpyHostToDevice, h->s));
-        if (m->epV)
-            CK(h, cudaMemcpyAsync(h->pass + (2 + d) * dn, m->epV, np * sizeof(double), cudaMemcpyHostToDevice, h->s));
-    }
+    for (XField* x : rest)
+        if (x->k > 1) k_aos_to_soa<<<(h->np + 255) / 256, 256, 0, h->s>>>(x->stage, x->k, h->np, x->dev);
+    CK(h, cudaGetLastError());
     std::memset(h->hctl, 0, sizeof(Ctl));
     for (int i = 0; i < d; ++i) {
         double v = m->vmax ? m->vmax[i] : 0.0;
@@ -793,34 +879,29 @@ ep_status epgpu_run(ep_handle* h, int32_t phase, double T, double tg, double* t_
 ep_status epgpu_download(ep_handle* h, ep_mpts_view* m) {
     if (!h || !m) return EP_ERR_ARG;
     if (m->nmp != h->np || m->ndim != h->dim) return fail(h, EP_ERR_ARG, "mpts.nmp/ndim differ from create");
-    const int d = h->dim, ns = h->nstr;
+    const int d = h->dim;
     ep_status st;
     if (h->mixed && h->uploaded) {
         mixed_export(h->mx, h->ctx.P, h->ctx.N, h->s);
         CK(h, cudaGetLastError());
     }
     if ((st = read_ctl(h)) != EP_OK) return st;
-    size_t off = 0;
-#define GET(ptr, k, f) if ((st = get_aos(h, fld_ptr(h, (f)), (k), (ptr), off)) != EP_OK) return st
-    GET(m->x, d, F_X); GET(m->v, d, F_V); GET(m->l, d, F_L); GET(m->l0, d, F_L0);
-    GET(m->n0, 1, F_N0); GET(m->n, 1, F_N); GET(m->Omega0, 1, F_OM0); GET(m->Omega, 1, F_OM); GET(m->dJ, 1, F_DJ);
-    GET(m->J, 1, F_J); GET(m->rho0, 1, F_RHO0); GET(m->rho, 1, F_RHO); GET(m->c0, 1, F_C0); GET(m->cr, 1, F_CR);
-    GET(m->dlam, 1, F_DLAM); GET(m->epII, 2, F_EP); GET(m->sig, ns, F_SIG); GET(m->tau, ns, F_TAU);
-    GET(m->dvij, d * d, F_DV); GET(m->dFij, d * d, F_DF); GET(m->Fij, d * d, F_F); GET(m->bij, d * d, F_B);
-    GET(m->eij, d * d, F_EPS); GET(m->wij, d * d, F_W); GET(m->sJij, d * d, F_SJ);
-#undef GET
+    // one k_xfer into the mapped host buffers; the other fields transposed into staging, then
+    // copied back to back
+    std::vector<XField> f = xfer_fields(h, m);
+    std::vector<XField*> rest;
+    XferTab T;
+    int nblk = 0;
+    xfer_split(f, 1, T, nblk, rest);
+    if (T.n) k_xfer<<<nblk, XF_BS, 0, h->s>>>(T);
+    for (XField* x : rest)
+        if (x->k > 1) k_soa_to_aos<<<(h->np + 255) / 256, 256, 0, h->s>>>(x->dev, x->k, h->np, x->stage);
+    CK(h, cudaGetLastError());
+    for (XField* x : rest)
+        CK(h, cudaMemcpyAsync(x->host, x->k > 1 ? x->stage : x->dev, x->n * sizeof(double), cudaMemcpyDeviceToHost, h->s));
     if (m->vmax)
         for (int i = 0; i < d; ++i) m->vmax[i] = bits_to_double(h->hctl->vmax_bits[i]);
-    {
-        const size_t np = (size_t)h->np, dn = (size_t)d * np;
-        if (m->u) CK(h, cudaMemcpyAsync(m->u, h->pass, dn * sizeof(double), cudaMemcpyDeviceToHost, h->s));
-        if (m->p) CK(h, cudaMemcpyAsync(m->p, h->pass + dn, dn * sizeof(double), cudaMemcpyDeviceToHost, h->s));
-        if (m->duij)
-            CK(h, cudaMemcpyAsync(m->duij, h->pass + 2 * dn, d * dn * sizeof(double), cudaMemcpyDeviceToHost, h->s));
-        if (m->epV)
-            CK(h, cudaMemcpyAsync(m->epV, h->pass + (2 + d) * dn, np * sizeof(double), cudaMemcpyDeviceToHost, h->s));
-        CK(h, cudaStreamSynchronize(h->s));
-    }
+    CK(h, cudaStreamSynchronize(h->s));
     if (m->p2e || m->p2n) {
         std::vector<int> c(h->np);
         if (h->np) {

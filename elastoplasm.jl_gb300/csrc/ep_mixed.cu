@@ -2355,7 +2355,8 @@ __device__ __forceinline__ bool point3(const MCtx& A, int cur, int k, int n, PtW
 // cell, lane (qx, qy) owns the stencil column of 4 z-nodes
 constexpr int TP3_STRIDE = 47;
 
-template <int BASIS, int TC>
+// DET: each cell's node sums go to its 64 x 7 partials (m, p, f) for km_gather3 instead of FP32 atomics
+template <int BASIS, int TC, bool DET = false>
 __global__ void __launch_bounds__(16 * TC, 4) km_p2g_tile3(MCtx A) {
     constexpr int TH = 16 * TC;
     EP_ACTIVE(A.ctl);
@@ -2454,6 +2455,17 @@ __global__ void __launch_bounds__(16 * TC, 4) km_p2g_tile3(MCtx A) {
     }
     if (bad) set_err(A.ctl, EP_ERR_INVALID_POSITION, c0);
     if (!cell_ok || pb == pe) return;
+    if (DET) {
+        // stencil slot (qx, qy, j) of the cell, all 64 written; km_gather3 adds them in a fixed order
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            float* o = A.part + ((size_t)cl * 64 + l16 * 4 + j) * 7;
+            o[0] = am[j];
+            o[1] = ap[0][j]; o[2] = ap[1][j]; o[3] = ap[2][j];
+            o[4] = af[0][j]; o[5] = af[1][j]; o[6] = af[2][j];
+        }
+        return;
+    }
     int e[3];
     cell_dec(A.g, cl, e);
     const Axis4 ax = axis4(A.g, 0, e[0]), ay = axis4(A.g, 1, e[1]), az = axis4(A.g, 2, e[2]);
@@ -2471,9 +2483,120 @@ __global__ void __launch_bounds__(16 * TC, 4) km_p2g_tile3(MCtx A) {
     }
 }
 
+// Deterministic scatters in 3d, the tile staging of km_p2g_tile3: the mUSL momentum (KIND 1: m v per
+// point, augm.jl:13-25) and Σ N m δJ (KIND 2: the per-point value left in ptmp by km_fbar_seg3,
+// volumetric.jl:1-11), each cell's points summed in list (point id) order into its 64 x NQ partials
+template <int BASIS, int TC, int KIND>
+__global__ void __launch_bounds__(16 * TC) km_aux_tile3(MCtx A) {
+    constexpr int TH = 16 * TC, NQ = KIND == 1 ? 3 : 1, ST = 17;
+    EP_ACTIVE(A.ctl);
+    __shared__ float sp[TH * ST];
+    const int cur = A.ctl->parity;
+    const int c0 = blockIdx.x * TC;
+    if (c0 >= A.g.ncell) return;
+    const int c1 = min(c0 + TC, A.g.ncell);
+    const int* start = A.S.start[cur];
+    const int b0 = start[c0], b1 = start[c1];
+    if (b0 == b1) return;
+    const int t = threadIdx.x;
+    const int l16 = t & 15, qx = l16 & 3, qy = l16 >> 2, cl = c0 + (t >> 4);
+    const bool cell_ok = cl < c1;
+    const int pb = cell_ok ? start[cl] : 0, pe = cell_ok ? start[cl + 1] : 0;
+    float acc[4][NQ];
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int v = 0; v < NQ; ++v) acc[j][v] = 0.f;
+    bool bad = false;
+    for (int ch = b0; ch < b1; ch += TH) {
+        const int k = ch + t;
+        if (k < b1) {
+            const int p = A.S.list[cur][k], c = A.S.cellof[cur][k];
+            int e[3];
+            cell_dec(A.g, c, e);
+            float* s = sp + t * ST;
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                const Axis4 ax = axis4(A.g, d, e[d]);
+                const float h = (float)A.g.h[d];
+                const float l = BASIS == EP_BASIS_GIMPM ? A.P.l[d][p] : 0.f;
+                float dw[4];
+                axis_w<BASIS>(ax, A.P.dx[cur][d][p], h, 1.f / h, l, s + 4 * d, dw, bad);
+            }
+            if (KIND == 1) {
+                const float mp = A.P.mp[p];
+#pragma unroll
+                for (int d = 0; d < 3; ++d) s[12 + d] = mp * A.P.v[d][p];
+            } else {
+                s[12] = A.ptmp[p];
+            }
+        }
+        __syncthreads();
+        const int lo = max(pb, ch), hi = min(pe, min(ch + TH, b1));
+        for (int kk = lo; kk < hi; ++kk) {
+            const float* s = sp + (kk - ch) * ST;
+            const float wxy = s[qx] * s[4 + qy];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const float N = wxy * s[8 + j];
+#pragma unroll
+                for (int v = 0; v < NQ; ++v) acc[j][v] += N * s[12 + v];
+            }
+        }
+        __syncthreads();
+    }
+    if (bad) set_err(A.ctl, EP_ERR_INVALID_POSITION, c0);
+    if (!cell_ok || pb == pe) return;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int v = 0; v < NQ; ++v) A.part[((size_t)cl * 64 + l16 * 4 + j) * NQ + v] = acc[j][v];
+}
+
+// node sums of the 3d per-cell partials: node (iy, ix, iz) is slot (qx, qy, r) of the cell
+// (ey, ex, ez) = (iy + 1 - qy, ix + 1 - qx, iz + 1 - r); cells visited in that fixed order
+template <int NQ>
+__global__ void km_gather3(MCtx A, float* o0, float* o1, float* o2, float* o3, float* o4, float* o5, float* o6) {
+    EP_ACTIVE(A.ctl);
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= A.g.nnode) return;
+    const int cur = A.ctl->parity;
+    const int nz = A.g.nno[2], nzx = nz * A.g.nno[0];
+    const int iy = n / nzx, rem = n - iy * nzx, ix = rem / nz, iz = rem - ix * nz;
+    const int ncz = A.g.nel[2], nczx = ncz * A.g.nel[0];
+    const int* start = A.S.start[cur];
+    float acc[NQ];
+#pragma unroll
+    for (int v = 0; v < NQ; ++v) acc[v] = 0.f;
+#pragma unroll 1
+    for (int qy = 0; qy < 4; ++qy) {
+        const int ey = iy + 1 - qy;
+        if (ey < 0 || ey >= A.g.nel[1]) continue;
+#pragma unroll 1
+        for (int qx = 0; qx < 4; ++qx) {
+            const int ex = ix + 1 - qx;
+            if (ex < 0 || ex >= A.g.nel[0]) continue;
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const int ez = iz + 1 - r;
+                if (ez < 0 || ez >= ncz) continue;
+                const int c = ez + ncz * ex + nczx * ey;
+                if (start[c] == start[c + 1]) continue;
+                const float* pp = A.part + ((size_t)c * 64 + (qx + 4 * qy) * 4 + r) * NQ;
+#pragma unroll
+                for (int v = 0; v < NQ; ++v) acc[v] += pp[v];
+            }
+        }
+    }
+    float* outs[7] = {o0, o1, o2, o3, o4, o5, o6};
+#pragma unroll
+    for (int v = 0; v < NQ; ++v) outs[v][n] = acc[v];
+}
+
 // km_g2p_seg3: PIC/FLIP (n2p.jl:14-40), new cell + offset, vmax, next-cell counts and the
 // mUSL momentum P2G (augm.jl:13-25) in 3d, one lane per point
-template <int BASIS>
+// DET: the momentum P2G is left to km_aux_tile3<.., 1> (no FP32 atomics)
+template <int BASIS, bool DET = false>
 __global__ void __launch_bounds__(256) km_g2p_seg3(MCtx A) {
     EP_ACTIVE(A.ctl);
     const int cur = A.ctl->parity, nxt = cur ^ 1;
@@ -2537,7 +2660,7 @@ __global__ void __launch_bounds__(256) km_g2p_seg3(MCtx A) {
         const unsigned mm = __match_any_sync(0xffffffffu, c2);
         if (c2 >= 0 && S.lane == __ffs(mm) - 1) atomicAdd(&A.S.count[nxt][c2], __popc(mm));
     }
-    if (A.cf.musl) {
+    if (!DET && A.cf.musl) {
 #pragma unroll 1
         for (int j = 0; j < 4; ++j)
 #pragma unroll 1
@@ -2595,7 +2718,8 @@ __device__ __forceinline__ void grad3(const MCtx& A, const PtW3& W, float* const
 }
 
 // km_fbar_seg3: δJ = det(I + dt ∇v) - 1 and Σ N m δJ (deform.jl:9-18, volumetric.jl:1-11) in 3d
-template <int BASIS>
+// DET: the point's m δJ goes to ptmp for km_aux_tile3<.., 2> (no FP32 atomics)
+template <int BASIS, bool DET = false>
 __global__ void __launch_bounds__(256) km_fbar_seg3(MCtx A) {
     EP_ACTIVE(A.ctl);
     const int cur = A.ctl->parity, nxt = cur ^ 1;
@@ -2619,6 +2743,11 @@ __global__ void __launch_bounds__(256) km_fbar_seg3(MCtx A) {
         mdj = A.P.mp[W.p] * (fin ? dJ : dJ * (2.f + dJ));
     }
     place_next_warp(A, live ? W.p : -1, live ? A.P.p2e_next[W.p] : -1, nxt, S.lane);
+    if (DET) {
+        if (live) A.ptmp[W.p] = mdj;
+        if (bad) set_err(A.ctl, EP_ERR_INVALID_POSITION, W.c);
+        return;
+    }
 #pragma unroll 1
     for (int j = 0; j < 4; ++j)
 #pragma unroll 1
@@ -3690,11 +3819,12 @@ static int sm_count() {
     return n;
 }
 
-template <int BASIS, int ACC>
+// one 3d step; DET = no floating-point atomics (per-cell partials + node gathers, point-id ordered lists)
+template <int BASIS, int ACC, bool DET>
 static void mixed_step3_impl(const MixedCtx& X, int phase, cudaStream_t s) {
     const MCtx& A = *(const MCtx*)X.impl;
     const int nc = A.g.ncell, nn = A.g.nnode, np = A.P.np;
-    const int gn = (nn + 255) / 256, gp = (np + 255) / 256;
+    const int gn = (nn + 255) / 256, gp = (np + 255) / 256, gc = (nc + 255) / 256, gt = (nc + 15) / 16;
     const int gs = gp > 0 ? gp : 1;
     Prof* pr = (X.prof && X.prof->on) ? X.prof : nullptr;
     auto mark = [&](const char* nm) {
@@ -3704,18 +3834,37 @@ static void mixed_step3_impl(const MixedCtx& X, int phase, cudaStream_t s) {
     cudaMemsetAsync(X.grid_zero, 0, X.grid_zero_bytes, s);
     cudaMemsetAsync(X.sort_zero, 0, X.sort_zero_bytes, s);
     mark("memset");
-    km_p2g_tile3<BASIS, 16><<<(nc + 15) / 16, 256, 0, s>>>(A);
+    km_p2g_tile3<BASIS, 16, DET><<<gt, 256, 0, s>>>(A);
+    if (DET) {
+        km_gather3<7><<<gn, 256, 0, s>>>(A, A.N.m, A.N.p[0], A.N.p[1], A.N.p[2], A.N.f[0], A.N.f[1], A.N.f[2]);
+        ++L;
+    }
     mark("p2g");
     km_solve<<<gn, 256, 0, s>>>(A);
     mark("solve");
-    km_g2p_seg3<BASIS><<<gs, 256, 0, s>>>(A);
+    km_g2p_seg3<BASIS, DET><<<gs, 256, 0, s>>>(A);
     mark("g2p");
     L += 3;
-    if (A.cf.musl) { km_vmusl<<<gn, 256, 0, s>>>(A); mark("vmusl"); ++L; }
+    if (A.cf.musl) {
+        if (DET) {
+            km_aux_tile3<BASIS, 16, 1><<<gt, 256, 0, s>>>(A);
+            km_gather3<3><<<gn, 256, 0, s>>>(A, A.N.pm[0], A.N.pm[1], A.N.pm[2], nullptr, nullptr, nullptr, nullptr);
+            mark("musl");
+            L += 2;
+        }
+        km_vmusl<<<gn, 256, 0, s>>>(A);
+        mark("vmusl");
+        ++L;
+    }
     L += mixed_scan(A, 0, X.scan_in, s);
     mark("scan");
     if (A.cf.locking) {
-        km_fbar_seg3<BASIS><<<gs, 256, 0, s>>>(A);
+        km_fbar_seg3<BASIS, DET><<<gs, 256, 0, s>>>(A);
+        if (DET) {
+            km_aux_tile3<BASIS, 16, 2><<<gt, 256, 0, s>>>(A);
+            km_gather3<1><<<gn, 256, 0, s>>>(A, A.N.dJacc, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
+            L += 2;
+        }
         mark("fbar");
         km_dJn<<<gn, 256, 0, s>>>(A);
         mark("dJn");
@@ -3738,6 +3887,11 @@ static void mixed_step3_impl(const MixedCtx& X, int phase, cudaStream_t s) {
             mark("rmap_finish");
             L += 2;
         }
+    }
+    if (DET) {
+        km_sort_cells<<<gc, 256, 0, s>>>(A, 0);   // the next step's lists in point-id order
+        mark("sort");
+        ++L;
     }
     const bool lrn = A.rmode == EP_RMAP_LEARNED;
     km_flip<<<1, 1, 0, s>>>(A.ctl, lrn ? A.rcount : nullptr, lrn ? A.fbcount : nullptr);
@@ -3860,14 +4014,23 @@ void mixed_step(const MixedCtx& X, int phase, cudaStream_t s) {
     const MCtx& A = *(const MCtx*)X.impl;
     if (A.g.dim == 3) {
         const int b = A.cf.basis;
+        auto run = [&](auto acc, auto det) {
+            constexpr int AC = decltype(acc)::value;
+            constexpr bool DT = decltype(det)::value;
+            if (b == EP_BASIS_BSMPM) mixed_step3_impl<EP_BASIS_BSMPM, AC, DT>(X, phase, s);
+            else if (b == EP_BASIS_GIMPM) mixed_step3_impl<EP_BASIS_GIMPM, AC, DT>(X, phase, s);
+            else mixed_step3_impl<EP_BASIS_SMPM, AC, DT>(X, phase, s);
+        };
+        using I0 = std::integral_constant<int, 0>;
+        using I1 = std::integral_constant<int, 1>;
+        using BF = std::integral_constant<bool, false>;
+        using BT = std::integral_constant<bool, true>;
         if (A.acc == 0) {
-            if (b == EP_BASIS_BSMPM) mixed_step3_impl<EP_BASIS_BSMPM, 0>(X, phase, s);
-            else if (b == EP_BASIS_GIMPM) mixed_step3_impl<EP_BASIS_GIMPM, 0>(X, phase, s);
-            else mixed_step3_impl<EP_BASIS_SMPM, 0>(X, phase, s);
+            if (A.cf.det) run(I0(), BT());
+            else run(I0(), BF());
         } else {
-            if (b == EP_BASIS_BSMPM) mixed_step3_impl<EP_BASIS_BSMPM, 1>(X, phase, s);
-            else if (b == EP_BASIS_GIMPM) mixed_step3_impl<EP_BASIS_GIMPM, 1>(X, phase, s);
-            else mixed_step3_impl<EP_BASIS_SMPM, 1>(X, phase, s);
+            if (A.cf.det) run(I1(), BT());
+            else run(I1(), BF());
         }
         return;
     }

@@ -128,18 +128,24 @@ def _fp64_spread(oracle_mod, kw, over, shift, windows=((0, 2.0), (1, 3.0)), eps=
     return float(np.linalg.norm(a.tau - b.tau) / np.linalg.norm(a.tau))
 
 
-def _compare_fin(oracle_mod, kw, over, shift, precision, windows=((0, 2.0), (1, 3.0))):
-    from epgpu import Engine, ic_slump
+def _fin_ic(kw, over, shift):
+    from epgpu import ic_slump
     kw = copy.deepcopy(kw)
     nl = kw.pop("nonloc", {"status": False, "ls": 0.5})
     ic, cfg = ic_slump(*C1_3D, cmpr_over=over, nonloc=nl, **kw)
     if over and "c0" in over:
         ic["mpts"].c0[:] = over["c0"]
     ic["mpts"].x += shift * ic["mesh"].h[0]
+    return ic, cfg
+
+
+def _compare_fin(oracle_mod, kw, over, shift, precision, windows=((0, 2.0), (1, 3.0)), det=False):
+    from epgpu import Engine
+    ic, cfg = _fin_ic(kw, over, shift)
     x0 = ic["mpts"].x.copy()
     o = oracle_mod.Oracle(copy.deepcopy(ic), cfg["instr"])
     instr = copy.deepcopy(cfg["instr"])
-    instr["gpu"] = {"precision": precision, "jaumann": False}
+    instr["gpu"] = {"precision": precision, "jaumann": False, "deterministic": det}
     e = Engine(copy.deepcopy(ic), instr)
     t = 0.0
     for phase, T in windows:
@@ -185,3 +191,30 @@ def test_mixed3d_finite_vs_oracle(oracle_mod, case, precision):
         assert dl < 1e-5
     sig_now = b.tau / np.asarray(b.J).reshape(1, -1) if fin else b.sig
     np.testing.assert_allclose(a.sig, sig_now, rtol=0, atol=10 * tol * np.abs(sig_now).max())
+
+
+DET_CASES = [("finite_dp_defaults", "mixed"), ("finite_dp_defaults", "mixed_df"),
+             ("finite_dp_gimp_Uii", "mixed_df"), ("infinitesimal_dp_musl_fbar_nonlocal", "mixed_df")]
+
+
+@pytest.mark.parametrize("case,precision", DET_CASES)
+def test_mixed3d_deterministic_is_bitwise_reproducible(oracle_mod, case, precision):
+    """The 3d deterministic mode (no floating-point atomics: per-cell node partials summed in
+    point-id order, nodes adding their <= 64 cells in a fixed order): two runs give identical bits,
+    and the run stays within the tolerance of the FP64 oracle."""
+    from epgpu import Engine
+    kw, over, shift, _ = FIN_CASES[case]
+    a, b, s, d = _compare_fin(oracle_mod, kw, over, shift, precision, det=True)
+    ic, cfg = _fin_ic(kw, over, shift)
+    instr = copy.deepcopy(cfg["instr"])
+    instr["gpu"] = {"precision": precision, "jaumann": False, "deterministic": True}
+    e = Engine(ic, instr)
+    t = 0.0
+    for phase, T in ((0, 2.0), (1, 3.0)):
+        t, _ = e.run(phase, T, 10.0, t)
+    a2 = e.download()
+    e.close()
+    for f in ("x", "v", "tau", "Fij", "bij", "epII", "l"):
+        assert np.array_equal(np.asarray(getattr(a, f)), np.asarray(getattr(a2, f))), f
+    print(f"3d deterministic {case} {precision}: stress {s:.3e} displacement {d:.3e}")
+    assert s < STRESS_TOL and d < DISP_TOL
