@@ -939,6 +939,80 @@ ep_status epgpu_download(ep_handle* h, ep_mpts_view* m) {
     return EP_OK;
 }
 
+// savlot's plot fields (plot.jl:27-135) from the FP64 SoA state, one row of np per requested field in
+// bit order; products and sums rounded one by one as plot.jl's broadcasts do (no contraction)
+struct FieldSrc {
+    const double *s0, *s1, *s2, *eps, *ep, *u, *epv, *c0, *n, *J, *rho, *om, *x, *z;
+    int dim;
+};
+
+__global__ void k_fields(const FieldSrc S, uint32_t what, int np, double* out) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    int row = 0;
+    auto put = [&](double v) { out[(size_t)row++ * np + p] = v; };
+    if (what & EP_FIELD_P) {
+        if (S.dim == 2) put(-__dadd_rn(S.s0[p], S.s1[p]) / 2.0 / 1e3);
+        else put(-__dadd_rn(__dadd_rn(S.s0[p], S.s1[p]), S.s2[p]) / 3.0 / 1e3);
+    }
+    if (what & EP_FIELD_SIGXX) put(S.s0[p] / 1e3);
+    if (what & EP_FIELD_EPSXX) put(S.eps[p]);
+    if (what & EP_FIELD_EPII) put(S.ep[p]);
+    if (what & EP_FIELD_EPV) put(S.epv[p]);
+    if (what & EP_FIELD_DU) {
+        const double a = S.u[(size_t)S.dim * p], b = S.u[(size_t)S.dim * p + 1];
+        put(sqrt(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b))));
+    }
+    if (what & EP_FIELD_COH0) put(S.c0[p] / 1e3);
+    if (what & EP_FIELD_PHI0) ++row;   // ϕ is not held on the device: the host fills this row
+    if (what & EP_FIELD_N) put(S.n[p]);
+    if (what & EP_FIELD_J) put(S.J[p]);
+    if (what & EP_FIELD_MS) put(__dmul_rn(S.rho[p], S.om[p]));
+    if (what & EP_FIELD_X) put(S.x[p]);
+    if (what & EP_FIELD_Z) put(S.z[p]);
+}
+
+ep_status epgpu_fields(ep_handle* h, uint32_t what, double* out) {
+    if (!h) return EP_ERR_ARG;
+    if (what & ~EP_FIELD_ALL) return fail(h, EP_ERR_ARG, "UndefinedPlotOption: unknown bits in the field mask");
+    if (what && !out) return fail(h, EP_ERR_ARG, "fields: out is NULL");
+    if (!h->uploaded) return fail(h, EP_ERR_STATE, "fields before upload");
+    const size_t np = (size_t)h->np;
+    if (!what || np == 0) return EP_OK;
+    const int d = h->dim;
+    if (h->mixed) {
+        mixed_export(h->mx, h->ctx.P, h->ctx.N, h->s);
+        CK(h, cudaGetLastError());
+    }
+    FieldSrc S;
+    const double* sig = fld_ptr(h, F_SIG);
+    S.s0 = sig;
+    S.s1 = sig + np;
+    S.s2 = sig + 2 * np;
+    S.eps = fld_ptr(h, F_EPS);
+    S.ep = fld_ptr(h, F_EP);
+    S.u = h->pass;
+    S.epv = h->pass + (2 + (size_t)d) * d * np;
+    S.c0 = fld_ptr(h, F_C0);
+    S.n = fld_ptr(h, F_N);
+    S.J = fld_ptr(h, F_J);
+    S.rho = fld_ptr(h, F_RHO);
+    S.om = fld_ptr(h, F_OM);
+    S.x = fld_ptr(h, F_X);
+    S.z = fld_ptr(h, F_X) + (size_t)(d - 1) * np;
+    S.dim = d;
+    const int rows = __builtin_popcount(what);
+    k_fields<<<(unsigned)((np + 255) / 256), 256, 0, h->s>>>(S, what, (int)np, h->xfer);   // staging: >= 13 rows
+    CK(h, cudaGetLastError());
+    CK(h, cudaMemcpyAsync(out, h->xfer, (size_t)rows * np * sizeof(double), cudaMemcpyDeviceToHost, h->s));
+    CK(h, cudaStreamSynchronize(h->s));
+    if (what & EP_FIELD_PHI0) {
+        const int row = __builtin_popcount(what & (EP_FIELD_PHI0 - 1u));
+        std::memcpy(out + (size_t)row * np, h->phi_cache.data(), np * sizeof(double));
+    }
+    return EP_OK;
+}
+
 ep_status epgpu_download_mesh(ep_handle* h, ep_mesh_fields* f) {
     if (!h || !f) return EP_ERR_ARG;
     const int d = h->dim;

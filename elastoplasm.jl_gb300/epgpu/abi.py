@@ -160,6 +160,7 @@ SIGNATURES = {
     "epgpu_run": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_double, _D, _I64]),
     "epgpu_download": (C.c_int, [C.c_void_p, C.POINTER(ep_mpts_view)]),
     "epgpu_download_mesh": (C.c_int, [C.c_void_p, C.POINTER(ep_mesh_fields)]),
+    "epgpu_fields": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p]),
     "epgpu_stats": (C.c_int, [C.c_void_p, C.POINTER(ep_stats)]),
     "epgpu_destroy": (C.c_int, [C.c_void_p]),
     "epgpu_profile": (C.c_int, [C.c_void_p, C.c_int32]),

@@ -47,6 +47,20 @@ class Engine:
         self._check(self.lib.epgpu_download(self.h, C.byref(abi.mpts_view(mpts, with_topology=True))))
         return mpts
 
+    def fields(self, names) -> dict:
+        """savlot's per-point plot fields evaluated on the device (``epgpu_fields``): a dict of
+        np-long FP64 arrays for the device field names of ``snapshot.FIELDS``."""
+        from . import snapshot
+        m = 0
+        for n in names:
+            if n not in snapshot.BITS:
+                raise ValueError(f"UndefinedPlotOption: {n}")
+            m |= snapshot.BITS[n]
+        order = snapshot.rows(m)
+        out = np.empty((len(order), self.mpts.nmp), dtype=np.float64)
+        self._check(self.lib.epgpu_fields(self.h, m, out.ctypes.data_as(C.c_void_p)))
+        return dict(zip(order, out))
+
     def download_mesh(self, mesh=None):
         mesh = mesh or copy.deepcopy(self.mesh)
         self._check(self.lib.epgpu_download_mesh(self.h, C.byref(abi.mesh_fields(mesh))))

@@ -187,6 +187,28 @@ ep_status epgpu_download(ep_handle* h, ep_mpts_view* mpts);
 /* Copy the nodal fields of the last step out; NULL fields are skipped. */
 ep_status epgpu_download_mesh(ep_handle* h, ep_mesh_fields* f);
 
+/* The per-point plot fields of savlot (utils/savlot.jl:20-34 -> what_plot_field, utils/plot.jl:27-135),
+ * evaluated on the device from the current state in FP64, so that a checkpoint moves only the fields
+ * asked for instead of the whole state.  `what` is a mask of EP_FIELD_* bits; `out` receives one
+ * row of np values per set bit, in bit order (row-major, popcount(what) x np).  The formulas and
+ * their operation order are plot.jl's: */
+#define EP_FIELD_P     (1u << 0)   /* -(σxx+σyy)/2/1e3 in 2d, -(σxx+σyy+σzz)/3/1e3 in 3d [kPa] (:28-35) */
+#define EP_FIELD_SIGXX (1u << 1)   /* σxx/1e3 [kPa] (:43-44) */
+#define EP_FIELD_EPSXX (1u << 2)   /* ϵ[1,1] (:53-54) */
+#define EP_FIELD_EPII  (1u << 3)   /* ϵpII[1,:] (:63-64) */
+#define EP_FIELD_EPV   (1u << 4)   /* ϵpV (:73-74) */
+#define EP_FIELD_DU    (1u << 5)   /* sqrt(u[1]^2 + u[2]^2), also in 3d (:83-84) */
+#define EP_FIELD_COH0  (1u << 6)   /* c0/1e3 [kPa] (:99-100) */
+#define EP_FIELD_PHI0  (1u << 7)   /* ϕ (:106-107) */
+#define EP_FIELD_N     (1u << 8)   /* n; plot.jl shows mpts.n for both "n0" and "n" (:112-123) */
+#define EP_FIELD_J     (1u << 9)   /* J (:124-125) */
+#define EP_FIELD_MS    (1u << 10)  /* ρ Ω (:130-131) */
+#define EP_FIELD_X     (1u << 11)  /* the horizontal plot coordinate x[1,:] (:143-147) */
+#define EP_FIELD_Z     (1u << 12)  /* the vertical plot coordinate: x[2,:] in 2d, x[3,:] in 3d */
+#define EP_FIELD_ALL   ((1u << 13) - 1u)
+/* z0 (:93-94) is a set-up constant the library does not hold; the caller's mpts.z0 serves. */
+ep_status epgpu_fields(ep_handle* h, uint32_t what, double* out);
+
 ep_status epgpu_stats(ep_handle* h, ep_stats* out);
 
 /* Per-kernel CUDA-event timers for epgpu_step (the reference only measures whole
