@@ -125,7 +125,7 @@ __global__ void k_soa_to_aos(const double* __restrict__ in, int k, int np, doubl
 // point field blocks inside pbuf
 enum Fld {
     F_X, F_XO, F_V, F_L, F_L0, F_N0, F_N, F_OM0, F_OM, F_DJ, F_J, F_RHO0, F_RHO, F_C0, F_CR, F_TPHI, F_SPHI, F_CPHI,
-    F_DLAM, F_EP, F_SIG, F_TAU, F_DV, F_DF, F_F, F_B, F_EPS, F_W, F_SJ, F_SH, F_COUNT
+    F_DLAM, F_EP, F_SIG, F_TAU, F_DV, F_DF, F_F, F_B, F_EPS, F_W, F_SJ, F_SH, F_BIJ, F_DIJ, F_BD, F_COUNT
 };
 
 static int fld_width(Fld f, int d, int ns) {
@@ -133,7 +133,8 @@ static int fld_width(Fld f, int d, int ns) {
         case F_X: case F_XO: case F_V: case F_L: case F_L0: return d;
         case F_EP: return 2;
         case F_SIG: case F_TAU: return ns;
-        case F_DV: case F_DF: case F_F: case F_B: case F_EPS: case F_W: case F_SJ: return d * d;
+        case F_DV: case F_DF: case F_F: case F_B: case F_EPS: case F_W: case F_SJ: case F_BIJ: case F_DIJ:
+        case F_BD: return d * d;
         case F_SH: return 8 * d;
         default: return 1;
     }
@@ -186,8 +187,8 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
     if (d != 2 && d != 3) return fail(nullptr, EP_ERR_UNSUPPORTED, "only 2d and 3d steps are built");
     if (mesh->dim != d) return fail(nullptr, EP_ERR_ARG, "mesh.dim != cfg.dim");
     if (cfg->basis < 0 || cfg->basis > 2) return fail(nullptr, EP_ERR_UNSUPPORTED, "unknown basis.which");
-    if (cfg->trsfr != EP_TRSFR_STD && cfg->trsfr != EP_TRSFR_TPIC)
-        return fail(nullptr, EP_ERR_UNSUPPORTED, "only std and tpic transfers are built");
+    if (cfg->trsfr != EP_TRSFR_STD && cfg->trsfr != EP_TRSFR_TPIC && cfg->trsfr != EP_TRSFR_APIC)
+        return fail(nullptr, EP_ERR_UNSUPPORTED, "unsupported transfer scheme (mapsto.jl:44)");
     if (cfg->deform != EP_DEFORM_FINITE && cfg->deform != EP_DEFORM_INFINITESIMAL)
         return fail(nullptr, EP_ERR_UNSUPPORTED, "unknown fwrk.deform");
     if (cfg->constitutive != EP_CONS_DP && cfg->constitutive != EP_CONS_J2)
@@ -211,6 +212,19 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
         ncell *= mesh->nel[i];
     }
     if (mesh->nno[d] != nnode || mesh->nel[d] != ncell) return fail(nullptr, EP_ERR_ARG, "mesh.nno/nel totals");
+    if (cfg->trsfr == EP_TRSFR_APIC && cfg->precision != EP_PREC_FP64) {
+        // the mixed step forms v + Bᵢⱼ δ, i.e. D⁻¹ = I (p2n.jl:221-225).  The reference's Dᵢⱼ is the
+        // rank-one N δ δᵀ of one node (misc.jl:25) with entries M <= (2h)²; after the first pivot
+        // its LU pivots are rounding noise (<= 7u M, then <= 14u M; u = 2^-53), so |det D| <= 7u M²
+        // in 2d (< 1e-12 while h < 3) and <= 98u² M³ in 3d (< 1e-12 while h < 300).  The limits
+        // below keep a margin; the FP64 step takes either branch exactly.
+        const double hmax = d == 2 ? 2.5 : 100.0;
+        for (int i = 0; i < d; ++i)
+            if (!(mesh->h[i] < hmax))
+                return fail(nullptr, EP_ERR_UNSUPPORTED,
+                            d == 2 ? "apic in the mixed precisions needs h < 2.5 in 2d (D⁻¹ = I)"
+                                   : "apic in the mixed precisions needs h < 100 in 3d (D⁻¹ = I)");
+    }
     const long long NN = d == 2 ? 16 : 64;
     if (nnode > 16000000LL || ncell > 16000000LL || nmp * NN > (long long)INT_MAX)
         return fail(nullptr, EP_ERR_UNSUPPORTED, "mesh or point count beyond the 32-bit index range of this build");
@@ -355,7 +369,7 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
     h->stage_n = stage_n;
     // staging slots of the multi-component point fields: x v l l0 (d each), ϵpII (2), σ τ (ns each),
     // ∇v ΔF F b ϵ ω σJ (d² each); pass-through u, p (d each), ∇u (d²), ϵpV (1)
-    ok = ok && dalloc(h, &h->xfer, (size_t)(4 * d + 2 + 2 * ns + 7 * d * d) * h->np) == cudaSuccess;
+    ok = ok && dalloc(h, &h->xfer, (size_t)(4 * d + 2 + 2 * ns + 9 * d * d) * h->np) == cudaSuccess;
     ok = ok && dalloc(h, &h->pass, (size_t)(2 * d + d * d + 1) * h->np) == cudaSuccess;
     if (ok && h->np) ok = cudaMemset(h->pass, 0, (size_t)(2 * d + d * d + 1) * h->np * sizeof(double)) == cudaSuccess;
     Sort& S = h->ctx.S;
@@ -397,6 +411,9 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
         P.tau[k] = fld_ptr(h, F_TAU) + (size_t)k * h->np;
     }
     for (int k = 0; k < d * d; ++k) {
+        P.B[k] = fld_ptr(h, F_BIJ) + (size_t)k * h->np;
+        P.Dm[k] = fld_ptr(h, F_DIJ) + (size_t)k * h->np;
+        P.BD[k] = fld_ptr(h, F_BD) + (size_t)k * h->np;
         P.dv[k] = fld_ptr(h, F_DV) + (size_t)k * h->np;
         P.dF[k] = fld_ptr(h, F_DF) + (size_t)k * h->np;
         P.F[k] = fld_ptr(h, F_F) + (size_t)k * h->np;
@@ -651,6 +668,10 @@ static std::vector<XField> xfer_fields(ep_handle* h, const ep_mpts_view* m) {
     add(m->dvij, d * d, fld_ptr(h, F_DV)); add(m->dFij, d * d, fld_ptr(h, F_DF)); add(m->Fij, d * d, fld_ptr(h, F_F));
     add(m->bij, d * d, fld_ptr(h, F_B)); add(m->eij, d * d, fld_ptr(h, F_EPS)); add(m->wij, d * d, fld_ptr(h, F_W));
     add(m->sJij, d * d, fld_ptr(h, F_SJ));
+    if (h->ctx.cf.trsfr == EP_TRSFR_APIC) {
+        add(m->Bij, d * d, fld_ptr(h, F_BIJ));
+        add(m->Dij, d * d, fld_ptr(h, F_DIJ));
+    }
     raw(m->u, h->pass, dn);
     raw(m->p, h->pass + dn, dn);
     raw(m->duij, h->pass + 2 * dn, (size_t)d * dn);

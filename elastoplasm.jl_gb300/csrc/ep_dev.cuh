@@ -69,6 +69,7 @@ struct P64 {
     double *n0, *n, *Om0, *Om, *dJ, *J, *rho0, *rho, *c0, *cr, *tphi, *sphi, *cphi, *dlam, *ep1, *ep2;
     double *sig[6], *tau[6];
     double *dv[9], *dF[9], *F[9], *b[9], *eps[9], *w[9], *sJ[9];
+    double *B[9], *Dm[9], *BD[9];     // APIC: Bᵢⱼ, Dᵢⱼ and the step's Bᵢⱼ D⁻¹ (scratch)
     double* SH;                       // per-direction shape table [(d*4+o)*2+c][np]
     int* p2e;                         // 0-based cell of each point
 };

@@ -111,6 +111,38 @@ __global__ void k_bin64(Cfg cf, Geo g, Ctl* ctl, P64 P, int* cell_count) {
             P.SH[(size_t)((d * 4 + o) * 2 + 1) * np + p] = df;
         }
     }
+    if (cf.trsfr == EP_TRSFR_APIC) {
+        // Dij_nd (shpfun/misc.jl:15-28): D = N δ δᵀ of the last existing stencil node (it is
+        // assigned node by node), then the step's B D⁻¹ (p2n.jl:221-226)
+        const int NN = D == 2 ? 16 : 64;
+        for (int s = NN - 1; s >= 0; --s) {
+            int o[3], i[3];
+            slot_offsets<D>(s, o);
+            bool ok = true;
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                i[d] = e[d] - 1 + o[d];
+                ok = ok && i[d] >= 0 && i[d] < g.nno[d];
+            }
+            if (!ok) continue;
+            double N[4], dl[3], Dm[D * D], Bp[D * D], C[D * D];
+            shape_at<D>(P, np, p, o, N);
+#pragma unroll
+            for (int d = 0; d < D; ++d) dl[d] = g.ax[d][i[d]] - xp[d];
+#pragma unroll
+            for (int b = 0; b < D; ++b)
+#pragma unroll
+                for (int a = 0; a < D; ++a) {
+                    Dm[a + D * b] = N[0] * (dl[a] * dl[b]);
+                    P.Dm[a + D * b][p] = Dm[a + D * b];
+                    Bp[a + D * b] = P.B[a + D * b][p];
+                }
+            apic_bdinv<D>(Bp, Dm, C);
+#pragma unroll
+            for (int k = 0; k < D * D; ++k) P.BD[k][p] = C[k];
+            break;
+        }
+    }
 }
 
 // number of points whose stencil holds each node: sum of the counts of the
@@ -192,7 +224,7 @@ __global__ void k_p2g64(Cfg cf, Geo g, Ctl* ctl, P64 P, N64 Nd, Sort S) {
 #pragma unroll
     for (int d = 0; d < D; ++d) xn[d] = g.ax[d][i[d]];
     const double gz = ctl->g[D - 1];
-    const bool tpic = cf.trsfr == EP_TRSFR_TPIC;
+    const bool tpic = cf.trsfr == EP_TRSFR_TPIC, apic = cf.trsfr == EP_TRSFR_APIC;
     double m = 0.0, pm[3] = {0.0, 0.0, 0.0}, f[3] = {0.0, 0.0, 0.0};
     const int b = S.node_start[n], e = S.node_start[n + 1];
     for (int k = b; k < e; ++k) {
@@ -206,7 +238,15 @@ __global__ void k_p2g64(Cfg cf, Geo g, Ctl* ctl, P64 P, N64 Nd, Sort S) {
         m = m + N[0] * ms;
         if (D == 2) {
             double sxx = P.sig[0][p], syy = P.sig[1][p], sxy = P.sig[2][p];
-            if (!tpic) {
+            if (apic) {
+                // N ms (v + (B D⁻¹) Δnp) (p2n.jl:226)
+                const double dl[2] = {xn[0] - P.xo[0][p], xn[1] - P.xo[1][p]};
+                double C[4];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) C[k] = P.BD[k][p];
+                pm[0] = pm[0] + N[0] * ms * (P.v[0][p] + apic_row<2>(C, 0, dl));
+                pm[1] = pm[1] + N[0] * ms * (P.v[1][p] + apic_row<2>(C, 1, dl));
+            } else if (!tpic) {
                 double px = ms * P.v[0][p], py = ms * P.v[1][p];
                 pm[0] = pm[0] + N[0] * px;
                 pm[1] = pm[1] + N[0] * py;
@@ -220,7 +260,15 @@ __global__ void k_p2g64(Cfg cf, Geo g, Ctl* ctl, P64 P, N64 Nd, Sort S) {
         } else {
             double sxx = P.sig[0][p], syy = P.sig[1][p], szz = P.sig[2][p];
             double syx = P.sig[5][p], szy = P.sig[3][p], szx = P.sig[4][p];
-            if (!tpic) {
+            if (apic) {
+                const double dl[3] = {xn[0] - P.xo[0][p], xn[1] - P.xo[1][p], xn[2] - P.xo[2][p]};
+                double C[9];
+#pragma unroll
+                for (int k = 0; k < 9; ++k) C[k] = P.BD[k][p];
+                pm[0] = pm[0] + N[0] * ms * (P.v[0][p] + apic_row<3>(C, 0, dl));
+                pm[1] = pm[1] + N[0] * ms * (P.v[1][p] + apic_row<3>(C, 1, dl));
+                pm[2] = pm[2] + N[0] * ms * (P.v[2][p] + apic_row<3>(C, 2, dl));
+            } else if (!tpic) {
                 double px = ms * P.v[0][p], py = ms * P.v[1][p], pz = ms * P.v[2][p];
                 pm[0] = pm[0] + N[0] * px;
                 pm[1] = pm[1] + N[0] * py;
@@ -321,6 +369,29 @@ __global__ void k_g2p64(Cfg cf, Geo g, Ctl* ctl, P64 P, N64 Nd) {
         P.v[d][p] = vp;
         P.x[d][p] = P.x[d][p] + dt * vpic;
         atomic_max_abs(&ctl->vmax_bits[d], vp);
+    }
+    if (cf.trsfr == EP_TRSFR_APIC) {
+        // Bij (mapsto/Bij.jl:14-26): Σ N (v_n Δnpᵀ) with the grid velocity of the solve (before the
+        // mUSL re-projection, n2p.jl:60-62) and the step-start offsets
+        double B[D * D];
+#pragma unroll
+        for (int k = 0; k < D * D; ++k) B[k] = 0.0;
+        for_slots<D>(g, P, np, p, [&](int, int n, const double* N) {
+            int ic[3];
+            node_coords<D>(n, g, ic);
+            double dl[3], vn[3];
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                dl[d] = g.ax[d][ic[d]] - P.xo[d][p];
+                vn[d] = Nd.v[d][n];
+            }
+#pragma unroll
+            for (int b = 0; b < D; ++b)
+#pragma unroll
+                for (int a = 0; a < D; ++a) B[a + D * b] = B[a + D * b] + N[0] * (vn[a] * dl[b]);
+        });
+#pragma unroll
+        for (int k = 0; k < D * D; ++k) P.B[k][p] = B[k];
     }
 }
 

@@ -21,21 +21,23 @@
 //     double-float state; the deviatoric factors are FP32 functions of the
 //     small invariants x², s².
 //
-// Kernels of one step (c = one quad of 4 lanes per cell, p = one lane per point):
-//   km_p2g    P2G of m, p, f                      (p2n.jl:135-155, 217-240)   c
-//   km_solve  grid update                         (solve.jl:14-40)            node
-//   km_g2p    PIC/FLIP, positions, vmax, next-cell counts, mUSL P2G
-//             (n2p.jl:14-40, tplgy.jl:43-62, augm.jl:13-25)                   c
-//   km_vmusl  mUSL nodal velocity                 (augm.jl:37-53)             node
-//   km_scan_* next-step cell offsets (exclusive scan of the counts)
-//   km_fbar   ∇v, δJ and Σ N m δJ; next-step cell lists (deform.jl:9-18,
-//             volumetric.jl:1-11)                                             c
-//   km_dJn    nodal δJ                            (volumetric.jl:12-22)       node
-//   km_cons   F-bar, F, elastic predictor, DP/J2  (volumetric.jl:23-36, deform.jl,
-//             elast.jl, DP.jl, J2.jl)                                         p
-// In a quad, lane q owns the stencil column q (4 nodes), so the lanes of a
-// quad never add to the same node and each keeps 4 nodes' sums in registers;
-// one FP32 atomic per node and quantity per cell goes to the grid.
+// Kernels of one 2d step (t = cells staged per CTA tile, p = one lane per sorted point, n = node):
+//   km_p2g_tile   P2G of m, p, f; 4 lanes per cell own its 4 stencil columns  (p2n.jl:135-155, 217-240)  t
+//   km_solve      grid update                                                (solve.jl:14-40)           n
+//   km_g2p_seg    PIC/FLIP, positions, vmax, next-cell counts; TPIC's ∇v or APIC's Bᵢⱼ
+//                 (n2p.jl:14-40, tplgy.jl:43-62, Bij.jl:14-26)                                          p
+//   km_aux_tile   mUSL momentum P2G in the tile form                         (augm.jl:13-25)            t
+//   km_vmusl      mUSL nodal velocity                                        (augm.jl:37-53)            n
+//   km_scan_*     next-step cell offsets (exclusive scan of the counts)
+//   km_fbar_seg   ∇v, δJ and Σ N m δJ; next-step cell lists                  (deform.jl:9-18,
+//                 volumetric.jl:1-11)                                                                   p
+//   km_dJn        nodal δJ                                                   (volumetric.jl:12-22)      n
+//   km_cons       F-bar, F, GIMP domain, elastic predictor, DP/J2            (volumetric.jl:23-36,
+//                 deform.jl, domain.jl, elast.jl, DP.jl, J2.jl)                                         p
+// The 3d step has the same sequence (km_p2g_tile3, km_g2p_seg3, km_fbar_seg3, km_cons3).  In a tile,
+// the lanes of one cell own disjoint stencil columns, so they never add to the same node and keep
+// their columns' sums in registers: one FP32 atomic per node and quantity per cell reaches the grid
+// (or, in the deterministic mode, one store into the cell's node partials).
 #include <climits>
 #include <type_traits>
 
@@ -234,99 +236,7 @@ __device__ __forceinline__ Quad quad_of(const MCtx& A, int cur) {
     return Q;
 }
 
-// sum over the four lanes of a quad; the mask names only those lanes, which
-// always run the same loop trip count (they walk the same cell)
-__device__ __forceinline__ float quad_sum(float v) {
-    const unsigned m = 0xFu << (threadIdx.x & 28);
-    v += __shfl_xor_sync(m, v, 1);
-    v += __shfl_xor_sync(m, v, 2);
-    return v;
-}
-
-// weights of one stencil column (x) and of all four rows (z) of a point
-template <int BASIS>
-__device__ __forceinline__ void quad_weights(const MCtx& A, const Axis4& ax, const Axis4& az, int q, int p, int cur,
-                                             float& wx, float& dwx, float* wz, float* dwz, bool& bad) {
-    const float hx = (float)A.g.h[0], hz = (float)A.g.h[1];
-    const float dx = A.P.dx[cur][0][p], dz = A.P.dx[cur][1][p];
-    const float lx = BASIS == EP_BASIS_GIMPM ? A.P.l[0][p] : 0.f;
-    const float lz = BASIS == EP_BASIS_GIMPM ? A.P.l[1][p] : 0.f;
-    float w4[4], d4[4];
-    axis_w<BASIS>(ax, dx, hx, 1.f / hx, lx, w4, d4, bad);
-    wx = q == 0 ? w4[0] : q == 1 ? w4[1] : q == 2 ? w4[2] : w4[3];
-    dwx = q == 0 ? d4[0] : q == 1 ? d4[1] : q == 2 ? d4[2] : d4[3];
-    axis_w<BASIS>(az, dz, hz, 1.f / hz, lz, wz, dwz, bad);
-}
-
 // ---------------------------------------------------------------------------
-// km_p2g: m, p, f (p2n.jl:135-155 std, 217-240 tpic); lane q accumulates its column
-template <int BASIS>
-__global__ void __launch_bounds__(256) km_p2g(MCtx A) {
-    EP_ACTIVE(A.ctl);
-    const int cur = A.ctl->parity;
-    const Quad Q = quad_of(A, cur);
-    if (!Q.live || Q.b == Q.e) return;
-    const Axis4 ax = axis4(A.g, 0, Q.ex), az = axis4(A.g, 1, Q.ez);
-    const float hx = (float)A.g.h[0], hz = (float)A.g.h[1];
-    const float gz = (float)A.ctl->g[1];
-    const bool fin = A.cf.deform == EP_DEFORM_FINITE;
-    const bool tpic = A.cf.trsfr == EP_TRSFR_TPIC;
-    const int q = Q.q;
-    float am[4], apx[4], apz[4], afx[4], afz[4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) am[j] = apx[j] = apz[j] = afx[j] = afz[j] = 0.f;
-    bool bad = false;
-    const int* list = A.S.list[cur];
-    for (int k = Q.b; k < Q.e; ++k) {
-        const int p = list[k];
-        float wx, dwx, wz[4], dwz[4];
-        quad_weights<BASIS>(A, ax, az, q, p, cur, wx, dwx, wz, dwz, bad);
-        const float ms = A.P.mp[p];
-        const float vx = A.P.v[0][p], vz = A.P.v[1][p];
-        const float sc = fin ? A.P.Om0[p] : A.P.Om[p];          // Ω σ = Ω0 τ (finite) or Ω σ
-        const float txx = sc * A.P.tau[0][p], tzz = sc * A.P.tau[1][p], txz = sc * A.P.tau[2][p];
-        float vx_i = vx, vz_i = vz, gxz = 0.f, gzz = 0.f, dz = 0.f;
-        if (tpic) {
-            // v + ∇v (x_n - x_p) with the previous step's ∇v (p2n.jl:233-235)
-            const float gxx = A.P.dv[0][p], gzx = A.P.dv[1][p];
-            gxz = A.P.dv[2][p];
-            gzz = A.P.dv[3][p];
-            const float ddx = (float)(q - 1) * hx - A.P.dx[cur][0][p];
-            dz = A.P.dx[cur][1][p];
-            vx_i = vx + gxx * ddx;
-            vz_i = vz + gzx * ddx;
-        }
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const float N = wx * wz[j], Nx = dwx * wz[j], Nz = wx * dwz[j];
-            const float Nm = N * ms;
-            am[j] += Nm;
-            if (!tpic) {
-                apx[j] += Nm * vx;
-                apz[j] += Nm * vz;
-            } else {
-                const float ddz = (float)(j - 1) * hz - dz;
-                apx[j] += Nm * (vx_i + gxz * ddz);
-                apz[j] += Nm * (vz_i + gzz * ddz);
-            }
-            afx[j] -= Nx * txx + Nz * txz;
-            afz[j] -= (Nx * txz + Nz * tzz) - Nm * gz;
-        }
-    }
-    if (bad) set_err(A.ctl, EP_ERR_INVALID_POSITION, Q.c);
-    if (ax.cls[q] < 0) return;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        if (az.cls[j] < 0) continue;
-        const int n = node2(A.g, ax, az, q, j);
-        atomicAdd(&A.N.m[n], am[j]);
-        atomicAdd(&A.N.p[0][n], apx[j]);
-        atomicAdd(&A.N.p[1][n], apz[j]);
-        atomicAdd(&A.N.f[0][n], afx[j]);
-        atomicAdd(&A.N.f[1][n], afz[j]);
-    }
-}
-
 // km_solve: grid momentum update with damping and Dirichlet masks (solve.jl:14-40), 2d and 3d
 __device__ __forceinline__ void solve_body(const MCtx& A, int bid) {
     EP_ACTIVE(A.ctl);
@@ -377,96 +287,6 @@ __device__ __forceinline__ void recell(const Geo& g, int d, int e, float o, floa
     e2 = min(max(e + k, 0), g.nel[d] - 1);
     o2 = o;
     if (e2 != e) o2 = o - (float)(g.ax[d][e2] - g.ax[d][e]);
-}
-
-// km_g2p: PIC/FLIP update (n2p.jl:14-40), new positions (cell + offset),
-// vmax, next-cell counts (tplgy.jl:43-62) and the mUSL momentum P2G (augm.jl:13-25)
-template <int BASIS>
-__global__ void __launch_bounds__(256) km_g2p(MCtx A) {
-    EP_ACTIVE(A.ctl);
-    const int cur = A.ctl->parity, nxt = cur ^ 1;
-    const Quad Q = quad_of(A, cur);
-    unsigned vm0 = 0u, vm1 = 0u;
-    if (Q.live && Q.b < Q.e) {
-        const Axis4 ax = axis4(A.g, 0, Q.ex), az = axis4(A.g, 1, Q.ez);
-        const float ihx = 1.f / (float)A.g.h[0], ihz = 1.f / (float)A.g.h[1];
-        const float dtf = (float)A.ctl->dt, Cpf = (float)A.cf.Cpf;
-        const bool musl = A.cf.musl;
-        const int q = Q.q;
-        int nid[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) nid[j] = (ax.cls[q] >= 0 && az.cls[j] >= 0) ? node2(A.g, ax, az, q, j) : -1;
-        float pmx[4] = {0.f, 0.f, 0.f, 0.f}, pmz[4] = {0.f, 0.f, 0.f, 0.f};
-        bool bad = false;
-        for (int k = Q.b; k < Q.e; ++k) {
-            const int p = A.S.list[cur][k];
-            float wx, dwx, wz[4], dwz[4];
-            quad_weights<BASIS>(A, ax, az, q, p, cur, wx, dwx, wz, dwz, bad);
-            float vpx = 0.f, vpz = 0.f, afx = 0.f, afz = 0.f;
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                if (nid[j] < 0) continue;
-                const float N = wx * wz[j];
-                vpx += N * __ldg(&A.N.v[0][nid[j]]);
-                vpz += N * __ldg(&A.N.v[1][nid[j]]);
-                afx += N * __ldg(&A.N.a[0][nid[j]]);
-                afz += N * __ldg(&A.N.a[1][nid[j]]);
-            }
-            vpx = quad_sum(vpx);
-            vpz = quad_sum(vpz);
-            afx = quad_sum(afx);
-            afz = quad_sum(afz);
-            const float vx = Cpf * (A.P.v[0][p] + dtf * afx) + (1.f - Cpf) * vpx;
-            const float vz = Cpf * (A.P.v[1][p] + dtf * afz) + (1.f - Cpf) * vpz;
-            if (q == 0) {
-                A.P.v[0][p] = vx;
-                A.P.v[1][p] = vz;
-                vm0 = max(vm0, __float_as_uint(fabsf(vx)));
-                vm1 = max(vm1, __float_as_uint(fabsf(vz)));
-                // x += dt v_PIC as a cell offset update, then re-binning (tplgy.jl:49)
-                const float ox = A.P.dx[cur][0][p] + dtf * vpx, oz = A.P.dx[cur][1][p] + dtf * vpz;
-                int c2 = -1;
-                if (isfinite(ox) && isfinite(oz)) {
-                    int ex2, ez2;
-                    float o2x, o2z;
-                    recell(A.g, 0, Q.ex, ox, ihx, ex2, o2x);
-                    recell(A.g, 1, Q.ez, oz, ihz, ez2, o2z);
-                    c2 = ez2 + A.g.nel[1] * ex2;
-                    A.P.dx[nxt][0][p] = o2x;
-                    A.P.dx[nxt][1][p] = o2z;
-                    atomicAdd(&A.S.count[nxt][c2], 1);
-                } else {
-                    set_err(A.ctl, EP_ERR_NONFINITE, p);
-                }
-                A.P.p2e_next[p] = c2;
-            }
-            if (musl) {
-                const float mp = A.P.mp[p];
-#pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    const float Nm = wx * wz[j] * mp;
-                    pmx[j] += Nm * vx;
-                    pmz[j] += Nm * vz;
-                }
-            }
-        }
-        if (bad) set_err(A.ctl, EP_ERR_INVALID_POSITION, Q.c);
-        if (musl) {
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                if (nid[j] < 0) continue;
-                atomicAdd(&A.N.pm[0][nid[j]], pmx[j]);
-                atomicAdd(&A.N.pm[1][nid[j]], pmz[j]);
-            }
-        }
-    }
-    // vmax over the warp, one atomic per warp (non-negative floats order like their bits)
-    vm0 = __reduce_max_sync(0xffffffffu, vm0);
-    vm1 = __reduce_max_sync(0xffffffffu, vm1);
-    if ((threadIdx.x & 31) == 0) {
-        if (vm0) atomicMax(&A.ctl->vmax_bits[0], (unsigned long long)__double_as_longlong((double)__uint_as_float(vm0)));
-        if (vm1) atomicMax(&A.ctl->vmax_bits[1], (unsigned long long)__double_as_longlong((double)__uint_as_float(vm1)));
-    }
 }
 
 // ---------------------------------------------------------------------------
@@ -537,76 +357,6 @@ __device__ __forceinline__ bool point_of(const MCtx& A, int cur, int k, int n, P
     return true;
 }
 
-// km_p2g_seg: m, p, f (p2n.jl:135-155 std, 217-240 tpic), one lane per point
-template <int BASIS>
-__global__ void __launch_bounds__(256) km_p2g_seg(MCtx A) {
-    EP_ACTIVE(A.ctl);
-    const int cur = A.ctl->parity;
-    const int n = A.S.start[cur][A.g.ncell];
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    bool bad = false;
-    PtW W;
-    const bool live = point_of<BASIS>(A, cur, k, n, W, bad);
-    const Seg S = seg_of(W.c);
-    const float hx = (float)A.g.h[0], hz = (float)A.g.h[1];
-    const float gz = (float)A.ctl->g[1];
-    const bool fin = A.cf.deform == EP_DEFORM_FINITE;
-    const bool tpic = A.cf.trsfr == EP_TRSFR_TPIC;
-    float ms = 0.f, vx = 0.f, vz = 0.f, txx = 0.f, tzz = 0.f, txz = 0.f, gxx = 0.f, gzx = 0.f, gxz = 0.f, gzz = 0.f;
-    if (live) {
-        const int p = W.p;
-        ms = A.P.mp[p];
-        vx = A.P.v[0][p];
-        vz = A.P.v[1][p];
-        const float sc = fin ? A.P.Om0[p] : A.P.Om[p];          // Ω σ = Ω0 τ (finite) or Ω σ
-        txx = sc * A.P.tau[0][p];
-        tzz = sc * A.P.tau[1][p];
-        txz = sc * A.P.tau[2][p];
-        if (tpic) {
-            gxx = A.P.dv[0][p];
-            gzx = A.P.dv[1][p];
-            gxz = A.P.dv[2][p];
-            gzz = A.P.dv[3][p];
-        }
-    }
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            float N = 0.f, Nx = 0.f, Nz = 0.f;
-            if (live) {
-                N = W.wx[i] * W.wz[j];
-                Nx = W.dwx[i] * W.wz[j];
-                Nz = W.wx[i] * W.dwz[j];
-            }
-            const float Nm = N * ms;
-            float px, pz;
-            if (!tpic) {
-                px = Nm * vx;
-                pz = Nm * vz;
-            } else {
-                // v + ∇v (x_n - x_p) with the previous step's ∇v (p2n.jl:233-235)
-                const float ddx = (float)(i - 1) * hx - W.dx, ddz = (float)(j - 1) * hz - W.dz;
-                px = Nm * (vx + gxx * ddx + gxz * ddz);
-                pz = Nm * (vz + gzx * ddx + gzz * ddz);
-            }
-            const float fx = -(Nx * txx + Nz * txz);
-            const float fz = -((Nx * txz + Nz * tzz) - Nm * gz);
-            const float sm = seg_sum(Nm, S), spx = seg_sum(px, S), spz = seg_sum(pz, S);
-            const float sfx = seg_sum(fx, S), sfz = seg_sum(fz, S);
-            if (S.head && live && W.ax.cls[i] >= 0 && W.az.cls[j] >= 0) {
-                const int nd = node2(A.g, W.ax, W.az, i, j);
-                atomicAdd(&A.N.m[nd], sm);
-                atomicAdd(&A.N.p[0][nd], spx);
-                atomicAdd(&A.N.p[1][nd], spz);
-                atomicAdd(&A.N.f[0][nd], sfx);
-                atomicAdd(&A.N.f[1][nd], sfz);
-            }
-        }
-    }
-    if (bad) set_err(A.ctl, EP_ERR_INVALID_POSITION, W.c);
-}
-
 // km_g2p_seg: PIC/FLIP (n2p.jl:14-40), new cell + offset, vmax, next-cell counts
 // (tplgy.jl:43-62) and the mUSL momentum P2G (augm.jl:13-25), one lane per point
 // MSEG: the mUSL momentum scatter by segmented warp sums here (else km_aux_tile<.., 1, ..> does it)
@@ -627,6 +377,10 @@ __device__ __forceinline__ void g2p_seg_body(const MCtx& A, int bid) {
     int c2 = -1;
     if (live) {
         float vpx = 0.f, vpz = 0.f, afx = 0.f, afz = 0.f;
+        // APIC: Bᵢⱼ = Σ N v_n δᵀ, δ = node - point at the step start (Bij.jl:14-26)
+        const bool apic = A.cf.trsfr == EP_TRSFR_APIC;
+        const float hx = (float)A.g.h[0], hz = (float)A.g.h[1];
+        float b00 = 0.f, b10 = 0.f, b01 = 0.f, b11 = 0.f;
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
             if (W.ax.cls[i] < 0) continue;
@@ -640,9 +394,22 @@ __device__ __forceinline__ void g2p_seg_body(const MCtx& A, int bid) {
                 vpz += N * q.y;
                 afx += N * q.z;
                 afz += N * q.w;
+                if (apic) {
+                    const float dlx = (float)(i - 1) * hx - W.dx, dlz = (float)(j - 1) * hz - W.dz;
+                    b00 += N * (q.x * dlx);
+                    b10 += N * (q.y * dlx);
+                    b01 += N * (q.x * dlz);
+                    b11 += N * (q.y * dlz);
+                }
             }
         }
         const int p = W.p;
+        if (apic) {
+            A.P.dv[0][p] = b00;
+            A.P.dv[1][p] = b10;
+            A.P.dv[2][p] = b01;
+            A.P.dv[3][p] = b11;
+        }
         vx = Cpf * (A.P.v[0][p] + dtf * afx) + (1.f - Cpf) * vpx;
         vz = Cpf * (A.P.v[1][p] + dtf * afz) + (1.f - Cpf) * vpz;
         A.P.v[0][p] = vx;
@@ -737,7 +504,7 @@ __device__ __forceinline__ void p2g_tile_body(const MCtx& A, int bid) {
     const float hx = (float)A.g.h[0], hz = (float)A.g.h[1];
     const float gz = (float)A.ctl->g[1];
     const bool fin = A.cf.deform == EP_DEFORM_FINITE;
-    const bool tpic = A.cf.trsfr == EP_TRSFR_TPIC;
+    const bool tpic = A.cf.trsfr != EP_TRSFR_STD;   // v + G δ: TPIC's ∇v or APIC's Bᵢⱼ (D⁻¹ = I) in dv
     float am[4], apx[4], apz[4], afx[4], afz[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) am[j] = apx[j] = apz[j] = afx[j] = afz[j] = 0.f;
@@ -1026,58 +793,6 @@ __device__ __forceinline__ void place_next_warp(const MCtx& A, int p, int c2, in
     } else {
         set_err(A.ctl, EP_ERR_CUDA, p);
     }
-}
-
-// km_fbar: δJ = det(I + dt ∇v) - 1 and its P2G Σ N m δJ (deform.jl:9-18, volumetric.jl:1-11);
-// places the points into the next step's cell lists
-template <int BASIS>
-__global__ void __launch_bounds__(256) km_fbar(MCtx A) {
-    EP_ACTIVE(A.ctl);
-    const int cur = A.ctl->parity, nxt = cur ^ 1;
-    const Quad Q = quad_of(A, cur);
-    if (!Q.live || Q.b == Q.e) return;
-    const Axis4 ax = axis4(A.g, 0, Q.ex), az = axis4(A.g, 1, Q.ez);
-    const float dtf = (float)A.ctl->dt;
-    const int q = Q.q;
-    int nid[4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) nid[j] = (ax.cls[q] >= 0 && az.cls[j] >= 0) ? node2(A.g, ax, az, q, j) : -1;
-    float acc[4] = {0.f, 0.f, 0.f, 0.f};
-    bool bad = false;
-    float* const* vn = A.cf.musl ? A.N.vm : A.N.v;
-    const bool fin = A.cf.deform == EP_DEFORM_FINITE;
-    for (int k = Q.b; k < Q.e; ++k) {
-        const int p = A.S.list[cur][k];
-        float wx, dwx, wz[4], dwz[4];
-        quad_weights<BASIS>(A, ax, az, q, p, cur, wx, dwx, wz, dwz, bad);
-        float g00 = 0.f, g01 = 0.f, g10 = 0.f, g11 = 0.f;
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            if (nid[j] < 0) continue;
-            const float Nx = dwx * wz[j], Nz = wx * dwz[j];
-            const float vx = __ldg(&vn[0][nid[j]]), vz = __ldg(&vn[1][nid[j]]);
-            g00 += Nx * vx;
-            g01 += Nz * vx;
-            g10 += Nx * vz;
-            g11 += Nz * vz;
-        }
-        g00 = quad_sum(g00);
-        g01 = quad_sum(g01);
-        g10 = quad_sum(g10);
-        g11 = quad_sum(g11);
-        const float D00 = dtf * g00, D10 = dtf * g10, D01 = dtf * g01, D11 = dtf * g11;
-        const float dJ = D00 + D11 + (D00 * D11 - D01 * D10);
-        // numerator mass ρΩ after the deformation update: finite ρ0Ω0 (unchanged), infinitesimal
-        // ρ J Ω0 = m (1 + δJ), so the nodal sum carries m (1+δJ)^2 - m = m δJ (2 + δJ) (volumetric.jl:8)
-        const float mdj = A.P.mp[p] * (fin ? dJ : dJ * (2.f + dJ));
-#pragma unroll
-        for (int j = 0; j < 4; ++j) acc[j] += wx * wz[j] * mdj;
-        if (q == 0) place_next(A, p, nxt);
-    }
-    if (bad) set_err(A.ctl, EP_ERR_INVALID_POSITION, Q.c);
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-        if (nid[j] >= 0) atomicAdd(&A.N.dJacc[nid[j]], acc[j]);
 }
 
 // km_fbar_seg: δJ = det(I + dt ∇v) - 1 and its P2G Σ N m δJ (deform.jl:9-18,
@@ -2110,6 +1825,8 @@ __global__ void km_import(MCtx A, P64 Q) {
     }
     if (A.cf.trsfr == EP_TRSFR_TPIC)
         for (int k = 0; k < D * D; ++k) A.P.dv[k][p] = (float)Q.dv[k][p];
+    else if (A.cf.trsfr == EP_TRSFR_APIC)
+        for (int k = 0; k < D * D; ++k) A.P.dv[k][p] = (float)Q.B[k][p];
     const bool fin = A.cf.deform == EP_DEFORM_FINITE;
     for (int k = 0; k < NS; ++k) A.P.tau[k][p] = (float)(fin ? Q.tau[k][p] : Q.sig[k][p]);
     A.P.ep2[p] = (float)Q.ep2[p];
@@ -2224,6 +1941,8 @@ __global__ void km_export(MCtx A, P64 Q) {
     }
     if (A.cf.trsfr == EP_TRSFR_TPIC)
         for (int k = 0; k < D * D; ++k) Q.dv[k][p] = (double)A.P.dv[k][p];
+    else if (A.cf.trsfr == EP_TRSFR_APIC)
+        for (int k = 0; k < D * D; ++k) Q.B[k][p] = (double)A.P.dv[k][p];
     Q.ep1[p] = e1;
     Q.ep2[p] = A.cf.nonloc ? (double)A.P.ep2[p] : e1;
     Q.dlam[p] = (double)A.P.dlam[p];
@@ -2374,7 +2093,7 @@ __global__ void __launch_bounds__(16 * TC, 4) km_p2g_tile3(MCtx A) {
     const int pb = cell_ok ? start[cl] : 0, pe = cell_ok ? start[cl + 1] : 0;
     const float hx = (float)A.g.h[0], hy = (float)A.g.h[1], hz = (float)A.g.h[2];
     const float gz = (float)A.ctl->g[2];
-    const bool tpic = A.cf.trsfr == EP_TRSFR_TPIC;
+    const bool tpic = A.cf.trsfr != EP_TRSFR_STD;   // v + G δ: TPIC's ∇v or APIC's Bᵢⱼ (D⁻¹ = I) in dv
     const bool fin = A.cf.deform == EP_DEFORM_FINITE;
     float am[4], ap[3][4], af[3][4];
 #pragma unroll
@@ -2612,6 +2331,9 @@ __global__ void __launch_bounds__(256) km_g2p_seg3(MCtx A) {
     int c2 = -1;
     if (live) {
         float vp[3] = {0.f, 0.f, 0.f}, af[3] = {0.f, 0.f, 0.f};
+        // APIC: Bᵢⱼ = Σ N v_n δᵀ, δ = node - point at the step start (Bij.jl:14-26)
+        const bool apic = A.cf.trsfr == EP_TRSFR_APIC;
+        float B[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll 1
         for (int j = 0; j < 4; ++j) {
             if (W.a[1].cls[j] < 0) continue;
@@ -2624,15 +2346,29 @@ __global__ void __launch_bounds__(256) km_g2p_seg3(MCtx A) {
                     if (W.a[2].cls[kz] < 0) continue;
                     const int nd = node3(A.g, W.a[0], W.a[1], W.a[2], i, j, kz);
                     const float N = wxy * W.w[2][kz];
+                    float vn[3];
 #pragma unroll
                     for (int d = 0; d < 3; ++d) {
-                        vp[d] += N * __ldg(&A.N.v[d][nd]);
+                        vn[d] = __ldg(&A.N.v[d][nd]);
+                        vp[d] += N * vn[d];
                         af[d] += N * __ldg(&A.N.a[d][nd]);
+                    }
+                    if (apic) {
+                        const float dl[3] = {(float)(i - 1) * (float)A.g.h[0] - W.o[0],
+                                             (float)(j - 1) * (float)A.g.h[1] - W.o[1],
+                                             (float)(kz - 1) * (float)A.g.h[2] - W.o[2]};
+#pragma unroll
+                        for (int b = 0; b < 3; ++b)
+#pragma unroll
+                            for (int a = 0; a < 3; ++a) B[a + 3 * b] += N * (vn[a] * dl[b]);
                     }
                 }
             }
         }
         const int p = W.p;
+        if (apic)
+#pragma unroll
+            for (int k = 0; k < 9; ++k) A.P.dv[k][p] = B[k];
         int e2[3];
         float o2[3];
         bool fin = true;
@@ -2745,19 +2481,18 @@ __global__ void __launch_bounds__(256) km_fbar_seg3(MCtx A) {
     place_next_warp(A, live ? W.p : -1, live ? A.P.p2e_next[W.p] : -1, nxt, S.lane);
     if (DET) {
         if (live) A.ptmp[W.p] = mdj;
-        if (bad) set_err(A.ctl, EP_ERR_INVALID_POSITION, W.c);
-        return;
-    }
+    } else {
 #pragma unroll 1
-    for (int j = 0; j < 4; ++j)
+        for (int j = 0; j < 4; ++j)
 #pragma unroll 1
-        for (int i = 0; i < 4; ++i)
+            for (int i = 0; i < 4; ++i)
 #pragma unroll
-            for (int kz = 0; kz < 4; ++kz) {
-                const float v = seg_sum(live ? W.w[0][i] * W.w[1][j] * W.w[2][kz] * mdj : 0.f, S);
-                if (S.head && live && W.a[0].cls[i] >= 0 && W.a[1].cls[j] >= 0 && W.a[2].cls[kz] >= 0)
-                    atomicAdd(&A.N.dJacc[node3(A.g, W.a[0], W.a[1], W.a[2], i, j, kz)], v);
-            }
+                for (int kz = 0; kz < 4; ++kz) {
+                    const float v = seg_sum(live ? W.w[0][i] * W.w[1][j] * W.w[2][kz] * mdj : 0.f, S);
+                    if (S.head && live && W.a[0].cls[i] >= 0 && W.a[1].cls[j] >= 0 && W.a[2].cls[kz] >= 0)
+                        atomicAdd(&A.N.dJacc[node3(A.g, W.a[0], W.a[1], W.a[2], i, j, kz)], v);
+                }
+    }
     if (bad) set_err(A.ctl, EP_ERR_INVALID_POSITION, W.c);
 }
 

@@ -217,6 +217,45 @@ EP_HD void lu_solve(const double* LU, const int* piv, const double* b, double* x
     }
 }
 
+// APIC (p2n.jl:208-280, shpfun/misc.jl:15-28, mapsto/Bij.jl:14-26), column-major N x N:
+//   Dᵢⱼ = N_k (δ δᵀ) of the LAST existing stencil node k (Dij_nd assigns instead of adding);
+//   C = Bᵢⱼ D⁻¹ with D⁻¹ = inv(D) when |det D| > 1e-12, else the identity (p2n.jl:221-225);
+//   the momentum of node k gets N ms (v + C δ_k); Bᵢⱼ = Σ_k N_k (v_k δ_kᵀ) after G2P.
+// The rank-one D has det D = 0 up to rounding, so the identity branch is the one taken unless
+// N² δx² δz² approaches 1e-12 / 2.2e-16 (node distances of several metres).
+template <int N>
+EP_HD void apic_bdinv(const double* B, const double* Dm, double* C) {
+    double Di[N * N];
+    if (fabs(det_lu<N>(Dm)) > 1.0e-12) {
+        double LU[N * N];
+        int piv[N];
+        for (int i = 0; i < N * N; ++i) LU[i] = Dm[i];
+        lu_factor<N>(LU, piv);
+        for (int j = 0; j < N; ++j) {
+            double e[N];
+            for (int i = 0; i < N; ++i) e[i] = (i == j) ? 1.0 : 0.0;
+            lu_solve<N>(LU, piv, e, &Di[N * j]);
+        }
+    } else {
+        for (int j = 0; j < N; ++j)
+            for (int i = 0; i < N; ++i) Di[i + N * j] = (i == j) ? 1.0 : 0.0;
+    }
+    for (int j = 0; j < N; ++j)
+        for (int i = 0; i < N; ++i) {
+            double s = B[i] * Di[N * j];
+            for (int k = 1; k < N; ++k) s = s + B[i + N * k] * Di[k + N * j];
+            C[i + N * j] = s;
+        }
+}
+
+// (C δ)_i summed left to right
+template <int N>
+EP_HD double apic_row(const double* C, int i, const double* dl) {
+    double s = C[i] * dl[0];
+    for (int k = 1; k < N; ++k) s = s + C[i + N * k] * dl[k];
+    return s;
+}
+
 // ---------------------------------------------------------------------------
 // Symmetric eigen-decomposition by Jacobi rotations (Golub & Van Loan,
 // "Matrix Computations", Alg. 8.5.1 sym.Schur2 and cyclic Jacobi 8.5.3).

@@ -55,7 +55,7 @@ _MPTS_FIELDS = ["vmax", "x", "l0", "l", "n0", "n", "Omega0", "Omega", "dJ", "J",
 
 class ep_mpts_view(C.Structure):
     _fields_ = ([("ndim", C.c_int64), ("nmp", C.c_int64)] + [(f, _D) for f in _MPTS_FIELDS]
-                + [("p2e", _I64), ("p2n", _I64)])
+                + [("p2e", _I64), ("p2n", _I64), ("Bij", _D), ("Dij", _D)])
 
 
 class ep_grf(C.Structure):
@@ -130,6 +130,10 @@ def mpts_view(mpts, with_topology: bool = False) -> ep_mpts_view:
     if with_topology and mpts.p2e is not None:
         v.p2e = mpts.p2e.ctypes.data_as(_I64)
         v.p2n = mpts.p2n.ctypes.data_as(_I64)
+    for f in ("Bij", "Dij"):                     # APIC state (types.jl:82-83)
+        a = getattr(mpts, f, None)
+        if a is not None:
+            setattr(v, f, _dptr(a))
     return v
 
 

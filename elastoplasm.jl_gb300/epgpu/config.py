@@ -65,7 +65,7 @@ BASIS = {"bsmpm": 0, "gimpm": 1, "smpm": 2}
 HOW = {None: 0, "undeformed": 1, "detFij": 2, "Fii": 3, "Uii": 4,
        "detΔFij": 5, "ΔFii": 6, "ΔUii": 7}
 DEFORM = {"finite": 0, "infinitesimal": 1}
-TRSFR = {"std": 0, "tpic": 1}
+TRSFR = {"std": 0, "tpic": 1, "apic": 2}
 CONSTITUTIVE = {"DP": 0, "J2": 1}
 PRECISION = {"fp64": 0, "mixed": 1, "mixed_df": 2}
 
@@ -83,8 +83,6 @@ def to_abi(instr: dict) -> dict:
     if b.get("which") not in BASIS:
         raise UnsupportedError(f"{b.get('which')} is not a supported shape function basis")
     trsfr = f.get("trsfr")
-    if trsfr == "apic":
-        raise UnsupportedError("apic is not built: only std and tpic transfers are")
     if trsfr not in TRSFR:
         raise UnsupportedError(f"{trsfr} is an unsupported transfer scheme")
     if f.get("deform") not in DEFORM:

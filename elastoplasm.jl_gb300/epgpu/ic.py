@@ -322,6 +322,8 @@ class Point:
     sJij: np.ndarray
     p2e: np.ndarray = field(default=None)
     p2n: np.ndarray = field(default=None)
+    Bij: np.ndarray = field(default=None)    # dim x dim x nmp, APIC (types.jl:82)
+    Dij: np.ndarray = field(default=None)    # dim x dim x nmp, APIC (types.jl:83)
 
     @property
     def nstr(self) -> int:
@@ -367,6 +369,7 @@ def setup_mpts(mesh, cmpr, geom) -> Point:
         Fij=eye.copy(order="F"), bij=eye.copy(order="F"), eij=Z(dim, dim, nmp),
         wij=Z(dim, dim, nmp), sJij=Z(dim, dim, nmp),
         p2e=np.zeros(nmp, dtype=np.int64), p2n=np.zeros((mesh.nn, nmp), dtype=np.int64, order="F"),
+        Bij=Z(dim, dim, nmp), Dij=Z(dim, dim, nmp),
     )
 
 

@@ -51,7 +51,7 @@ enum { EP_HOW_NONE = 0, EP_HOW_UNDEFORMED = 1, EP_HOW_DETFIJ = 2, EP_HOW_FII = 3
        EP_HOW_DETDFIJ = 5, EP_HOW_DFII = 6, EP_HOW_DUII = 7 };
 /* instr.fwrk.deform / trsfr (require.jl:44-45) */
 enum { EP_DEFORM_FINITE = 0, EP_DEFORM_INFINITESIMAL = 1 };
-enum { EP_TRSFR_STD = 0, EP_TRSFR_TPIC = 1 };
+enum { EP_TRSFR_STD = 0, EP_TRSFR_TPIC = 1, EP_TRSFR_APIC = 2 };
 /* instr.plast.constitutive (require.jl:68) */
 enum { EP_CONS_DP = 0, EP_CONS_J2 = 1 };
 /* device arithmetic: FP64 in the reference's order; FP32 transfers with FP64
@@ -134,6 +134,9 @@ typedef struct ep_mpts_view {
     double *dvij, *duij, *dFij, *Fij, *bij, *eij, *wij, *sJij; /* dim x dim x nmp */
     int64_t *p2e;                                   /* nmp, 1-based (download only) */
     int64_t *p2n;                                   /* nn x nmp, 1-based (download only) */
+    double *Bij, *Dij;                              /* dim x dim x nmp: APIC's Bᵢⱼ and Dᵢⱼ
+                                                       (types.jl:82-83); read and written only
+                                                       with EP_TRSFR_APIC, may be NULL */
 } ep_mpts_view;
 
 typedef struct ep_stats {
@@ -159,7 +162,10 @@ const char* epgpu_version(void);
 /* Build a device context for `nmp` points on `mesh` with switches `cfg`
  * (replaces kwargser's kernel table, kwargser.jl:49-60, and the arrays of
  * setup_mesh/setup_mpts).  Returns EP_ERR_UNSUPPORTED for switch combinations
- * the reference rejects or this library does not build (apic, MC, camC, 1d). */
+ * the reference rejects or this library does not build (MC, camC, 1d; APIC in the
+ * mixed precisions on meshes with h >= 2.5 in 2d or h >= 100 in 3d, where the
+ * reference's D⁻¹ of p2n.jl:221-225 could differ from the identity the mixed step
+ * assumes: its Dᵢⱼ is rank one, so |det D| is rounding noise below 1e-12 until then). */
 ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_view* mesh,
                        int64_t nmp, ep_handle** out);
 

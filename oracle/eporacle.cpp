@@ -6,8 +6,9 @@
 // (workflow/worflow.jl:23-93), on Julia-layout column-major arrays:
 //   tplgy      p2e2n_{2,3}d              workflow/shpfun/tplgy.jl:43-96
 //   shpfun     bsmpm/gimpm/smpm_{2,3}d   workflow/shpfun/basis/*.jl, shpfun.jl:74-88
-//   delta_np   Δnp_nd                    workflow/shpfun/misc.jl:1-14
-//   p2n        transform + std/tpic_p2n  workflow/mapsto/p2n.jl:12-21, 135-191, 284-296
+//   delta_np   Δnp_nd / Dij_nd           workflow/shpfun/misc.jl:1-28
+//   p2n        transform + std/tpic/apic workflow/mapsto/p2n.jl:12-21, 135-296
+//   Bij        APIC affine matrix        workflow/mapsto/Bij.jl:14-26 (called by n2p.jl:60-62, 72-74)
 //   solve      euler                     workflow/mapsto/solve.jl:14-63
 //   n2p        picflip_n2p + augm        workflow/mapsto/n2p.jl:14-76, augm.jl:13-53
 //   update     deform/domain/ΔJ{n,s,p}   workflow/elastoplast/update/*.jl
@@ -53,6 +54,7 @@ struct eporacle {
     vector<int64_t> p2e, p2n;
     vector<double> phidphi;  // nn x Np x (dim+1)
     vector<double> dnp;      // nn x dim x Np
+    vector<double> B, Dm;    // dim x dim x Np: APIC's Bᵢⱼ, Dᵢⱼ
     double DelLU[36];
     int piv[6];
     int threads = 1;
@@ -106,11 +108,13 @@ static void build_e2n(eporacle* o) {
 }
 
 // ---------------------------------------------------------------- tplgy (tplgy.jl:43-96)
-static void tplgy(eporacle* o) {
+static int tplgy(eporacle* o) {
     const int d = o->dim;
     for (int64_t p = 0; p < o->Np; ++p) {
         double e[3];
         for (int i = 0; i < d; ++i) {
+            // a non-finite position has no element (the reference's Int conversion throws there)
+            if (!std::isfinite(o->x[i + d * p])) return fail(o, EP_ERR_NONFINITE, "non-finite point position");
             double f = ep::jfld(o->x[i + d * p] - o->x0[i], o->h[i]);
             double hi = (double)(o->nel[i] - 1);
             e[i] = f < 0.0 ? 0.0 : (f > hi ? hi : f);
@@ -121,6 +125,11 @@ static void tplgy(eporacle* o) {
         for (int k = 0; k < o->nn; ++k) o->p2n[k + o->nn * p] = o->e2n[k + o->nn * (el - 1)];
         o->p2e[p] = el;
     }
+    return 0;
+}
+
+static inline double PHI(const eporacle* o, int k, int64_t p, int c) {
+    return o->phidphi[k + (int64_t)o->nn * p + (int64_t)o->nn * o->Np * c];
 }
 
 // ---------------------------------------------------------------- shape functions
@@ -171,13 +180,25 @@ static int shpfun(eporacle* o) {
                 for (int i = 0; i < d; ++i)
                     o->dnp[k + nn * i + (int64_t)nn * d * p] = o->xn[i + d * (no - 1)] - o->x[i + d * p];
             }
+    } else if (o->cfg.trsfr == EP_TRSFR_APIC) {
+        // Dij_nd (misc.jl:15-28): Δnp for every node, Dᵢⱼ assigned (not summed) node by node
+        for (int64_t p = 0; p < Np; ++p)
+            for (int k = 0; k < nn; ++k) {
+                int64_t no = o->p2n[k + nn * p];
+                if (no == 0) continue;
+                double dl[3];
+                for (int i = 0; i < d; ++i) {
+                    dl[i] = o->xn[i + d * (no - 1)] - o->x[i + d * p];
+                    o->dnp[k + nn * i + (int64_t)nn * d * p] = dl[i];
+                }
+                const double N = PHI(o, k, p, 0);
+                for (int j = 0; j < d; ++j)
+                    for (int i = 0; i < d; ++i) o->Dm[i + d * j + (int64_t)d * d * p] = N * (dl[i] * dl[j]);
+            }
     }
     return 0;
 }
 
-static inline double PHI(const eporacle* o, int k, int64_t p, int c) {
-    return o->phidphi[k + (int64_t)o->nn * p + (int64_t)o->nn * o->Np * c];
-}
 
 #ifdef _OPENMP
 #define ATOMIC_ADD(ref, val) _Pragma("omp atomic") ref += (val)
@@ -195,13 +216,18 @@ static void p2n(eporacle* o, const double* g) {
     std::fill(o->mi.begin(), o->mi.end(), 0.0);
     std::fill(o->pn.begin(), o->pn.end(), 0.0);
     std::fill(o->oobf.begin(), o->oobf.end(), 0.0);
-    const bool tpic = o->cfg.trsfr == EP_TRSFR_TPIC;
+    const bool tpic = o->cfg.trsfr == EP_TRSFR_TPIC, apic = o->cfg.trsfr == EP_TRSFR_APIC;
 #pragma omp parallel for num_threads(o->threads) schedule(static) if (o->threads > 1)
     for (int64_t p = 0; p < Np; ++p) {
         double ms = o->rho[p] * o->Om[p], Om = o->Om[p];
         const double* s = &o->sig[ns * p];
         const double* vp = &o->v[d * p];
         const double* gv = &o->dv[d * d * p];
+        double C[9];   // APIC: Bᵢⱼ D⁻¹ (the same for every node of the point)
+        if (apic) {
+            if (d == 2) ep::apic_bdinv<2>(&o->B[4 * p], &o->Dm[4 * p], C);
+            else ep::apic_bdinv<3>(&o->B[9 * p], &o->Dm[9 * p], C);
+        }
         for (int k = 0; k < nn; ++k) {
             int64_t no = o->p2n[k + nn * p];
             if (no == 0) continue;
@@ -211,7 +237,11 @@ static void p2n(eporacle* o, const double* g) {
                 double Nx = PHI(o, k, p, 1), Ny = PHI(o, k, p, 2);
                 double sxx = s[0], syy = s[1], sxy = s[2];
                 ATOMIC_ADD(o->mi[q], N * ms);
-                if (!tpic) {
+                if (apic) {
+                    const double dl[2] = {o->dnp[k + (int64_t)nn * 2 * p], o->dnp[k + nn + (int64_t)nn * 2 * p]};
+                    ATOMIC_ADD(o->pn[0 + 2 * q], N * ms * (vp[0] + ep::apic_row<2>(C, 0, dl)));
+                    ATOMIC_ADD(o->pn[1 + 2 * q], N * ms * (vp[1] + ep::apic_row<2>(C, 1, dl)));
+                } else if (!tpic) {
                     double px = ms * vp[0], py = ms * vp[1];
                     ATOMIC_ADD(o->pn[0 + 2 * q], N * px);
                     ATOMIC_ADD(o->pn[1 + 2 * q], N * py);
@@ -228,7 +258,13 @@ static void p2n(eporacle* o, const double* g) {
                 double Nx = PHI(o, k, p, 1), Ny = PHI(o, k, p, 2), Nz = PHI(o, k, p, 3);
                 double sxx = s[0], syy = s[1], szz = s[2], syx = s[5], szy = s[3], szx = s[4];
                 ATOMIC_ADD(o->mi[q], N * ms);
-                if (!tpic) {
+                if (apic) {
+                    const int64_t b = k + (int64_t)nn * 3 * p;
+                    const double dl[3] = {o->dnp[b], o->dnp[b + nn], o->dnp[b + 2 * nn]};
+                    ATOMIC_ADD(o->pn[0 + 3 * q], N * ms * (vp[0] + ep::apic_row<3>(C, 0, dl)));
+                    ATOMIC_ADD(o->pn[1 + 3 * q], N * ms * (vp[1] + ep::apic_row<3>(C, 1, dl)));
+                    ATOMIC_ADD(o->pn[2 + 3 * q], N * ms * (vp[2] + ep::apic_row<3>(C, 2, dl)));
+                } else if (!tpic) {
                     double px = ms * vp[0], py = ms * vp[1], pz = ms * vp[2];
                     ATOMIC_ADD(o->pn[0 + 3 * q], N * px);
                     ATOMIC_ADD(o->pn[1 + 3 * q], N * py);
@@ -300,6 +336,23 @@ static void n2p(eporacle* o, double dt) {
             if (!(vm >= av)) vm = av;   // max(vmax, |v|) with NaN propagation
         }
         o->vmax[i] = vm;
+    }
+    if (o->cfg.trsfr == EP_TRSFR_APIC) {
+        // Bij (Bij.jl:14-26) from the grid velocities of the solve, before the mUSL re-projection
+        // replaces them (n2p.jl:60-62); Δnp is the step-start offset of shpfun
+        for (int64_t p = 0; p < Np; ++p) {
+            double Bp[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+            for (int k = 0; k < nn; ++k) {
+                int64_t no = o->p2n[k + nn * p];
+                if (no == 0) continue;
+                const double N = PHI(o, k, p, 0);
+                for (int j = 0; j < d; ++j)
+                    for (int i = 0; i < d; ++i)
+                        Bp[i + d * j] = Bp[i + d * j] +
+                                        N * (o->vn[i + d * (no - 1)] * o->dnp[k + nn * j + (int64_t)nn * d * p]);
+            }
+            for (int i = 0; i < d * d; ++i) o->B[i + (int64_t)d * d * p] = Bp[i];
+        }
     }
     if (!o->cfg.musl) return;
     std::fill(o->pn.begin(), o->pn.end(), 0.0);
@@ -594,11 +647,12 @@ eporacle* eporacle_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_
     V(o->epII, 2 * Np); V(o->epV, Np); V(o->sig, o->nstr * Np); V(o->tau, o->nstr * Np);
     V(o->dv, d * d * Np); V(o->du, d * d * Np); V(o->dF, d * d * Np); V(o->F, d * d * Np);
     V(o->b, d * d * Np); V(o->eps, d * d * Np); V(o->w, d * d * Np); V(o->sJ, d * d * Np);
+    V(o->B, d * d * Np); V(o->Dm, d * d * Np);
     V(o->tphi, Np); V(o->sphi, Np); V(o->cphi, Np);
     o->p2e.assign(Np, 0);
     o->p2n.assign((size_t)o->nn * Np, 0);
     o->phidphi.assign((size_t)o->nn * Np * (d + 1), 0.0);
-    if (cfg->trsfr == EP_TRSFR_TPIC) o->dnp.assign((size_t)o->nn * d * Np, 0.0);
+    if (cfg->trsfr == EP_TRSFR_TPIC || cfg->trsfr == EP_TRSFR_APIC) o->dnp.assign((size_t)o->nn * d * Np, 0.0);
     const int ns = o->nstr;
     for (int i = 0; i < ns * ns; ++i) o->DelLU[i] = cmpr->Del[i];
     if (ns == 3) ep::lu_factor<3>(o->DelLU, o->piv);
@@ -623,6 +677,7 @@ int eporacle_upload(eporacle* o, const ep_mpts_view* m) {
     cpy_in(o->epII, m->epII); cpy_in(o->epV, m->epV); cpy_in(o->sig, m->sig); cpy_in(o->tau, m->tau);
     cpy_in(o->dv, m->dvij); cpy_in(o->du, m->duij); cpy_in(o->dF, m->dFij); cpy_in(o->F, m->Fij);
     cpy_in(o->b, m->bij); cpy_in(o->eps, m->eij); cpy_in(o->w, m->wij); cpy_in(o->sJ, m->sJij);
+    cpy_in(o->B, m->Bij); cpy_in(o->Dm, m->Dij);
     for (int64_t p = 0; p < o->Np; ++p) {
         o->tphi[p] = tan(o->phi[p]);
         o->sphi[p] = sin(o->phi[p]);
@@ -634,8 +689,9 @@ int eporacle_upload(eporacle* o, const ep_mpts_view* m) {
 int eporacle_step(eporacle* o, int32_t phase, double dt, const double* g, double* vmax_out) {
     if (!o || !g) return EP_ERR_ARG;
     for (int i = 0; i < o->dim; ++i) o->vmax[i] = 0.0;
-    tplgy(o);
-    int e = shpfun(o);
+    int e = tplgy(o);
+    if (e) return e;
+    e = shpfun(o);
     if (e) return e;
     p2n(o, g);
     solve(o, dt);
@@ -686,6 +742,7 @@ int eporacle_download(eporacle* o, ep_mpts_view* m) {
     cpy_out(o->epII, m->epII); cpy_out(o->epV, m->epV); cpy_out(o->sig, m->sig); cpy_out(o->tau, m->tau);
     cpy_out(o->dv, m->dvij); cpy_out(o->du, m->duij); cpy_out(o->dF, m->dFij); cpy_out(o->F, m->Fij);
     cpy_out(o->b, m->bij); cpy_out(o->eps, m->eij); cpy_out(o->w, m->wij); cpy_out(o->sJ, m->sJij);
+    cpy_out(o->B, m->Bij); cpy_out(o->Dm, m->Dij);
     if (m->p2e) std::memcpy(m->p2e, o->p2e.data(), o->p2e.size() * sizeof(int64_t));
     if (m->p2n) std::memcpy(m->p2n, o->p2n.data(), o->p2n.size() * sizeof(int64_t));
     return 0;

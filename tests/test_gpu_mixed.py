@@ -66,7 +66,8 @@ def test_mixed_config1_vs_oracle(oracle_mod, windows, precision):
 
 @pytest.mark.parametrize("precision", PRECISIONS)
 @pytest.mark.parametrize("deform,trsfr,locking", [("finite", "tpic", True), ("infinitesimal", "std", True),
-                                                  ("infinitesimal", "tpic", False), ("finite", "std", False)])
+                                                  ("infinitesimal", "tpic", False), ("finite", "std", False),
+                                                  ("finite", "apic", True), ("infinitesimal", "apic", False)])
 def test_mixed_switches(oracle_mod, deform, trsfr, locking, precision):
     from epgpu import Engine, ic_slump
     fw = {"deform": deform, "trsfr": trsfr, "C_pf": 0.99, "musl": True, "locking": locking, "damping": 0.1}
@@ -75,9 +76,30 @@ def test_mixed_switches(oracle_mod, deform, trsfr, locking, precision):
     o = oracle_mod.Oracle(copy.deepcopy(ic), cfg["instr"])
     e = Engine(copy.deepcopy(ic), _mixed(cfg["instr"], precision))
     _run(o, e, ((0, 1.0), (1, 1.3)))
-    s, d, r = errors(e.download(), o.download(), x0)
-    print(f"{precision} {deform}/{trsfr}/locking={locking}: stress {s:.3e} displacement {d:.3e} runout {r:.3e}")
+    a, b = e.download(), o.download()
+    s, d, r = errors(a, b, x0)
+    extra = ""
+    if trsfr == "apic":
+        # APIC's affine matrix Bᵢⱼ (Bij.jl:14-26), carried in FP32
+        dB = float(np.abs(np.asarray(a.Bij) - np.asarray(b.Bij)).max() / np.abs(np.asarray(b.Bij)).max())
+        extra = f" B {dB:.3e}"
+        assert dB < 1e-4
+    print(f"{precision} {deform}/{trsfr}/locking={locking}: stress {s:.3e} displacement {d:.3e} runout {r:.3e}{extra}")
     assert s < STRESS_TOL and d < DISP_TOL
+
+
+def test_mixed_apic_needs_small_cells():
+    """The mixed step assumes the reference's D⁻¹ = I (p2n.jl:221-225), which its rank-one Dᵢⱼ
+    guarantees in 2d for h < 3 (the library asks h < 2.5); a coarser mesh is refused rather than
+    run with a different rule."""
+    from epgpu import Engine, ic_slump
+    from epgpu.abi import EPError
+    fw = {"deform": "finite", "trsfr": "apic", "C_pf": 0.99, "musl": True, "locking": True, "damping": 0.1}
+    ic, cfg = ic_slump([64.1584, 16.0396], [16, 4], fwrk=fw, nonloc={"status": False, "ls": 0.5})   # h = 4.01
+    with pytest.raises(EPError) as ex:
+        Engine(ic, _mixed(cfg["instr"], "mixed"))
+    assert ex.value.status == 2
+    Engine(ic, cfg["instr"]).close()                    # the FP64 step takes either branch
 
 
 @pytest.mark.parametrize("basis", [{"which": "gimpm", "how": "undeformed", "ghost": True},

@@ -128,20 +128,20 @@ def _fp64_spread(oracle_mod, kw, over, shift, windows=((0, 2.0), (1, 3.0)), eps=
     return float(np.linalg.norm(a.tau - b.tau) / np.linalg.norm(a.tau))
 
 
-def _fin_ic(kw, over, shift):
+def _fin_ic(kw, over, shift, mesh=C1_3D):
     from epgpu import ic_slump
     kw = copy.deepcopy(kw)
     nl = kw.pop("nonloc", {"status": False, "ls": 0.5})
-    ic, cfg = ic_slump(*C1_3D, cmpr_over=over, nonloc=nl, **kw)
+    ic, cfg = ic_slump(*mesh, cmpr_over=over, nonloc=nl, **kw)
     if over and "c0" in over:
         ic["mpts"].c0[:] = over["c0"]
     ic["mpts"].x += shift * ic["mesh"].h[0]
     return ic, cfg
 
 
-def _compare_fin(oracle_mod, kw, over, shift, precision, windows=((0, 2.0), (1, 3.0)), det=False):
+def _compare_fin(oracle_mod, kw, over, shift, precision, windows=((0, 2.0), (1, 3.0)), det=False, mesh=C1_3D):
     from epgpu import Engine
-    ic, cfg = _fin_ic(kw, over, shift)
+    ic, cfg = _fin_ic(kw, over, shift, mesh)
     x0 = ic["mpts"].x.copy()
     o = oracle_mod.Oracle(copy.deepcopy(ic), cfg["instr"])
     instr = copy.deepcopy(cfg["instr"])
@@ -218,3 +218,18 @@ def test_mixed3d_deterministic_is_bitwise_reproducible(oracle_mod, case, precisi
         assert np.array_equal(np.asarray(getattr(a, f)), np.asarray(getattr(a2, f))), f
     print(f"3d deterministic {case} {precision}: stress {s:.3e} displacement {d:.3e}")
     assert s < STRESS_TOL and d < DISP_TOL
+
+
+@pytest.mark.parametrize("precision", ["mixed", "mixed_df"])
+def test_mixed3d_apic_vs_oracle(oracle_mod, precision):
+    """APIC in 3d (p2n.jl:208-280, Bij.jl:14-26) with the reference's defaults otherwise, on a mesh
+    of h = 1.6.  The reference's Dᵢⱼ is rank one, so its D⁻¹ is the identity and the affine term is
+    Bᵢⱼ δ with Bᵢⱼ ~ ∇v h²/3: on the 16 x 4 x 4 mesh (h = 4) that amplifies TPIC's term about five
+    times and the run blows up in the plastic phase, in the restatement as well."""
+    kw = {"fwrk": {"deform": "finite", "trsfr": "apic", "C_pf": 0.99, "musl": True, "locking": True, "damping": 0.1}}
+    mesh = ([64.1584, 16.0396, 16.0396], [40, 10, 10])
+    a, b, s, d = _compare_fin(oracle_mod, kw, None, 0.0, precision, mesh=mesh)
+    dB = float(np.abs(np.asarray(a.Bij) - np.asarray(b.Bij)).max() / np.abs(np.asarray(b.Bij)).max())
+    nplastic = int((b.epII[0] > 0).sum())
+    print(f"3d apic {precision}: stress {s:.3e} displacement {d:.3e} B {dB:.3e} plastic {nplastic} of {b.nmp}")
+    assert nplastic > 1000 and s < STRESS_TOL and d < DISP_TOL and dB < 1e-4

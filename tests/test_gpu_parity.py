@@ -12,7 +12,7 @@ import ctypes as C
 import numpy as np
 import pytest
 
-from conftest import compare_points
+from conftest import POINT_FIELDS, compare_points
 
 pytestmark = pytest.mark.gpu
 
@@ -68,7 +68,9 @@ def test_run_windows_config1(oracle_mod):
     print("max rel diff", max(worst.values()))
 
 
-SWITCHES = [(d, t, lk) for d in ("finite", "infinitesimal") for t in ("std", "tpic") for lk in (True, False)]
+# the 12 cases of test/testset/test_slump.jl:3-16
+SWITCHES = [(d, t, lk) for d in ("finite", "infinitesimal") for t in ("std", "tpic", "apic") for lk in (True, False)]
+APIC_FIELDS = POINT_FIELDS + ["Bij", "Dij"]
 
 
 @pytest.mark.parametrize("deform,trsfr,locking", SWITCHES)
@@ -79,7 +81,10 @@ def test_switch_matrix(oracle_mod, deform, trsfr, locking):
     o, e = _pair(ic, cfg["instr"], oracle_mod)
     t = _run_both(o, e, 0, 1.0, 0.0)
     t = _run_both(o, e, 1, 1.5, t)
-    compare_points(e.download(), o.download(), RTOL_FP64)
+    a, b = e.download(), o.download()
+    compare_points(a, b, RTOL_FP64, fields=APIC_FIELDS if trsfr == "apic" else POINT_FIELDS)
+    if trsfr == "apic":
+        assert np.abs(np.asarray(b.Bij)).max() > 1e-3 and np.abs(np.asarray(b.Dij)).max() > 0
 
 
 @pytest.mark.parametrize("basis", [{"which": "gimpm", "how": "undeformed", "ghost": True},
@@ -112,17 +117,20 @@ def test_full_all_in_one_config1(oracle_mod):
      "fwrk": {"deform": "infinitesimal", "trsfr": "tpic", "C_pf": 0.0, "musl": False, "locking": False,
               "damping": 0.1},
      "plast": {"status": True, "constitutive": "J2"}, "nonloc": {"status": False, "ls": 0.5}},
+    {"fwrk": {"deform": "finite", "trsfr": "apic", "C_pf": 0.99, "musl": True, "locking": True, "damping": 0.1},
+     "nonloc": {"status": False, "ls": 0.5}},
 ])
 def test_3d(oracle_mod, kw):
     from epgpu import ic_slump
-    over = {"c0": 5.0e4, "Hp": 1.0e5} if kw else None
+    over = {"c0": 5.0e4, "Hp": 1.0e5} if "plast" in kw else None
     ic, cfg = ic_slump(*C1_3D, cmpr_over=over, **kw)
     if over:
         ic["mpts"].c0[:] = 5.0e4
     o, e = _pair(ic, cfg["instr"], oracle_mod)
     t = _run_both(o, e, 0, 0.3, 0.0)
     t = _run_both(o, e, 1, 0.5, t)
-    compare_points(e.download(), o.download(), RTOL_FP64)
+    apic = kw.get("fwrk", {}).get("trsfr") == "apic"
+    compare_points(e.download(), o.download(), RTOL_FP64, fields=APIC_FIELDS if apic else POINT_FIELDS)
 
 
 def test_collapse_convergence_gpu():

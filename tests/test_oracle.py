@@ -10,8 +10,10 @@ closed-form properties of the restated arithmetic.
   exp/log within a few ulp;
 * the Drucker-Prager return lands on its cone and the J2 cutting plane
   converges for normal-stress trials;
-* the switch matrix of test/testset/test_slump.jl:3-16 (std/tpic x
-  finite/infinitesimal x locking; apic is not built) runs without error.
+* the switch matrix of test/testset/test_slump.jl:3-16 (std/tpic/apic x
+  finite/infinitesimal x locking) runs without error;
+* APIC's Dᵢⱼ is the rank-one N δ δᵀ of one node (shpfun/misc.jl:25 assigns node by node), so
+  the |det D| > 1e-12 branch of p2n.jl:221-225 is never taken on the slump meshes.
 """
 import ctypes as C
 import math
@@ -193,7 +195,7 @@ def test_elastic_collapse_convergence(oracle_mod, basis):
     assert errs[-1] < (3e-3 if basis["which"] == "bsmpm" else 7e-2)
 
 
-SWITCHES = [(d, t, lk) for d in ("finite", "infinitesimal") for t in ("std", "tpic") for lk in (True, False)]
+SWITCHES = [(d, t, lk) for d in ("finite", "infinitesimal") for t in ("std", "tpic", "apic") for lk in (True, False)]
 
 
 @pytest.mark.parametrize("deform,trsfr,locking", SWITCHES)
@@ -206,3 +208,19 @@ def test_switch_matrix_runs(oracle_mod, deform, trsfr, locking):
     m = o.download()
     assert n > 40 and n2 > 20 and t == 3.0
     assert np.isfinite(m.sig).all() and np.isfinite(m.x).all()
+
+
+def test_apic_affine_state(oracle_mod):
+    fw = {"deform": "finite", "trsfr": "apic", "C_pf": 0.99, "musl": True, "locking": True, "damping": 0.1}
+    ic, cfg = ic_slump([64.1584, 64.1584 / 4.0], [40, 10], fwrk=fw, nonloc={"status": False, "ls": 0.5})
+    o = oracle_mod.Oracle(ic, cfg["instr"])
+    t, _ = o.run(0, 1.0, 10.0, 0.0)
+    m = o.download()
+    D, B = np.asarray(m.Dij), np.asarray(m.Bij)
+    assert np.abs(B).max() > 1e-3                      # the affine velocity is carried
+    det = D[0, 0] * D[1, 1] - D[0, 1] * D[1, 0]
+    scale = np.abs(D).max(axis=(0, 1)) ** 2
+    assert np.all(np.abs(det) <= 1e-14 * np.maximum(scale, 1e-300))     # rank one
+    assert np.abs(det).max() < 1e-12
+    # the symmetric outer product N δ δᵀ: D[0,1] == D[1,0] and D[0,0], D[1,1] >= 0
+    assert np.array_equal(D[0, 1], D[1, 0]) and (D[0, 0] >= 0).all() and (D[1, 1] >= 0).all()

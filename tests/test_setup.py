@@ -74,9 +74,10 @@ def test_kwargser_top_level_merge():
     # a partial group drops the other keys of that group, as in the reference
     with pytest.raises(config.UnsupportedError):
         config.kwargser({"fwrk": {"deform": "finite", "trsfr": "std"}})
-    with pytest.raises(config.UnsupportedError):
-        config.kwargser({"fwrk": {"deform": "finite", "trsfr": "apic", "C_pf": 1.0, "musl": True,
-                                  "locking": True, "damping": 0.1}})
+    fw = {"deform": "finite", "trsfr": "apic", "C_pf": 1.0, "musl": True, "locking": True, "damping": 0.1}
+    assert config.to_abi(config.kwargser({"fwrk": fw}))["trsfr"] == 2          # EP_TRSFR_APIC
+    with pytest.raises(config.UnsupportedError):                               # mapsto.jl:44
+        config.kwargser({"fwrk": {**fw, "trsfr": "flip"}})
     with pytest.raises(config.UnsupportedError):
         config.kwargser({"basis": {"which": "gimpm", "how": None, "ghost": True}})
     with pytest.warns(UserWarning):
