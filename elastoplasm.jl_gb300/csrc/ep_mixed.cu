@@ -377,10 +377,6 @@ __device__ __forceinline__ void g2p_seg_body(const MCtx& A, int bid) {
     int c2 = -1;
     if (live) {
         float vpx = 0.f, vpz = 0.f, afx = 0.f, afz = 0.f;
-        // APIC: Bᵢⱼ = Σ N v_n δᵀ, δ = node - point at the step start (Bij.jl:14-26)
-        const bool apic = A.cf.trsfr == EP_TRSFR_APIC;
-        const float hx = (float)A.g.h[0], hz = (float)A.g.h[1];
-        float b00 = 0.f, b10 = 0.f, b01 = 0.f, b11 = 0.f;
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
             if (W.ax.cls[i] < 0) continue;
@@ -394,17 +390,30 @@ __device__ __forceinline__ void g2p_seg_body(const MCtx& A, int bid) {
                 vpz += N * q.y;
                 afx += N * q.z;
                 afz += N * q.w;
-                if (apic) {
-                    const float dlx = (float)(i - 1) * hx - W.dx, dlz = (float)(j - 1) * hz - W.dz;
+            }
+        }
+        const int p = W.p;
+        if (A.cf.trsfr == EP_TRSFR_APIC) {
+            // Bᵢⱼ = Σ N v_n δᵀ, δ = node - point at the step start (Bij.jl:14-26); a pass of its own
+            // so that the other transfers keep the register budget of the loop above
+            const float hx = (float)A.g.h[0], hz = (float)A.g.h[1];
+            float b00 = 0.f, b10 = 0.f, b01 = 0.f, b11 = 0.f;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                if (W.ax.cls[i] < 0) continue;
+                const float dlx = (float)(i - 1) * hx - W.dx;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    if (W.az.cls[j] < 0) continue;
+                    const float N = W.wx[i] * W.wz[j];
+                    const float4 q = A.N.va4[node2(A.g, W.ax, W.az, i, j)];
+                    const float dlz = (float)(j - 1) * hz - W.dz;
                     b00 += N * (q.x * dlx);
                     b10 += N * (q.y * dlx);
                     b01 += N * (q.x * dlz);
                     b11 += N * (q.y * dlz);
                 }
             }
-        }
-        const int p = W.p;
-        if (apic) {
             A.P.dv[0][p] = b00;
             A.P.dv[1][p] = b10;
             A.P.dv[2][p] = b01;
@@ -2314,8 +2323,9 @@ __global__ void km_gather3(MCtx A, float* o0, float* o1, float* o2, float* o3, f
 
 // km_g2p_seg3: PIC/FLIP (n2p.jl:14-40), new cell + offset, vmax, next-cell counts and the
 // mUSL momentum P2G (augm.jl:13-25) in 3d, one lane per point
-// DET: the momentum P2G is left to km_aux_tile3<.., 1> (no FP32 atomics)
-template <int BASIS, bool DET = false>
+// DET: the momentum P2G is left to km_aux_tile3<.., 1> (no FP32 atomics); AP: APIC's Bᵢⱼ is formed
+// (a separate instantiation, so that the other transfers keep their register budget)
+template <int BASIS, bool DET = false, bool AP = false>
 __global__ void __launch_bounds__(256) km_g2p_seg3(MCtx A) {
     EP_ACTIVE(A.ctl);
     const int cur = A.ctl->parity, nxt = cur ^ 1;
@@ -2331,9 +2341,6 @@ __global__ void __launch_bounds__(256) km_g2p_seg3(MCtx A) {
     int c2 = -1;
     if (live) {
         float vp[3] = {0.f, 0.f, 0.f}, af[3] = {0.f, 0.f, 0.f};
-        // APIC: Bᵢⱼ = Σ N v_n δᵀ, δ = node - point at the step start (Bij.jl:14-26)
-        const bool apic = A.cf.trsfr == EP_TRSFR_APIC;
-        float B[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll 1
         for (int j = 0; j < 4; ++j) {
             if (W.a[1].cls[j] < 0) continue;
@@ -2346,17 +2353,36 @@ __global__ void __launch_bounds__(256) km_g2p_seg3(MCtx A) {
                     if (W.a[2].cls[kz] < 0) continue;
                     const int nd = node3(A.g, W.a[0], W.a[1], W.a[2], i, j, kz);
                     const float N = wxy * W.w[2][kz];
-                    float vn[3];
 #pragma unroll
                     for (int d = 0; d < 3; ++d) {
-                        vn[d] = __ldg(&A.N.v[d][nd]);
-                        vp[d] += N * vn[d];
+                        vp[d] += N * __ldg(&A.N.v[d][nd]);
                         af[d] += N * __ldg(&A.N.a[d][nd]);
                     }
-                    if (apic) {
-                        const float dl[3] = {(float)(i - 1) * (float)A.g.h[0] - W.o[0],
-                                             (float)(j - 1) * (float)A.g.h[1] - W.o[1],
-                                             (float)(kz - 1) * (float)A.g.h[2] - W.o[2]};
+                }
+            }
+        }
+        const int p = W.p;
+        if (AP) {
+            // Bᵢⱼ = Σ N v_n δᵀ, δ = node - point at the step start (Bij.jl:14-26)
+            float B[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll 1
+            for (int j = 0; j < 4; ++j) {
+                if (W.a[1].cls[j] < 0) continue;
+                const float dly = (float)(j - 1) * (float)A.g.h[1] - W.o[1];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    if (W.a[0].cls[i] < 0) continue;
+                    const float dlx = (float)(i - 1) * (float)A.g.h[0] - W.o[0];
+                    const float wxy = W.w[0][i] * W.w[1][j];
+#pragma unroll
+                    for (int kz = 0; kz < 4; ++kz) {
+                        if (W.a[2].cls[kz] < 0) continue;
+                        const int nd = node3(A.g, W.a[0], W.a[1], W.a[2], i, j, kz);
+                        const float N = wxy * W.w[2][kz];
+                        const float dl[3] = {dlx, dly, (float)(kz - 1) * (float)A.g.h[2] - W.o[2]};
+                        float vn[3];
+#pragma unroll
+                        for (int d = 0; d < 3; ++d) vn[d] = __ldg(&A.N.v[d][nd]);
 #pragma unroll
                         for (int b = 0; b < 3; ++b)
 #pragma unroll
@@ -2364,11 +2390,9 @@ __global__ void __launch_bounds__(256) km_g2p_seg3(MCtx A) {
                     }
                 }
             }
-        }
-        const int p = W.p;
-        if (apic)
 #pragma unroll
             for (int k = 0; k < 9; ++k) A.P.dv[k][p] = B[k];
+        }
         int e2[3];
         float o2[3];
         bool fin = true;
@@ -3577,7 +3601,8 @@ static void mixed_step3_impl(const MixedCtx& X, int phase, cudaStream_t s) {
     mark("p2g");
     km_solve<<<gn, 256, 0, s>>>(A);
     mark("solve");
-    km_g2p_seg3<BASIS, DET><<<gs, 256, 0, s>>>(A);
+    if (A.cf.trsfr == EP_TRSFR_APIC) km_g2p_seg3<BASIS, DET, true><<<gs, 256, 0, s>>>(A);
+    else km_g2p_seg3<BASIS, DET, false><<<gs, 256, 0, s>>>(A);
     mark("g2p");
     L += 3;
     if (A.cf.musl) {
