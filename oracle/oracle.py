@@ -94,6 +94,17 @@ class Oracle:
         self._check(lib().eporacle_download(self.h, C.byref(self.abi.mpts_view(mpts, with_topology=True))))
         return mpts
 
+    def fields(self, names) -> dict:
+        """savlot's plot fields (device names of epgpu.snapshot.FIELDS) from the downloaded state,
+        by the restatement of plot.jl in plot_oracle.py: the checker of Engine.fields."""
+        import plot_oracle as po
+        m = self.download()
+        x, z = po.plot_coords(m)
+        out = {}
+        for n in names:
+            out[n] = x.copy() if n == "x" else z.copy() if n == "z" else po.plot_field(m, n)
+        return out
+
     def download_mesh(self, mesh=None):
         import copy
         mesh = mesh or copy.deepcopy(self.mesh)

@@ -80,6 +80,28 @@ def test_plot_oracle_formulas():
     m.sig = np.vstack([sig2, np.zeros((3, 2))])
     np.testing.assert_array_equal(po.plot_field(m, "P"), -(sig2[0] + sig2[1] + sig2[2]) / 3 / 1e3)
     x, z = po.plot_coords(m)
-    np.testing.assert_array_equal(x, [1.0, 2.0]) and np.testing.assert_array_equal(z, [3.0, 4.0])
+    np.testing.assert_array_equal(x, [1.0, 2.0])
+    np.testing.assert_array_equal(z, [3.0, 4.0])
     with pytest.raises(ValueError, match="UndefinedPlotOption"):
         po.plot_field(m, "vorticity")
+
+
+def test_writer_in_the_time_loop_with_the_oracle(tmp_path, oracle_mod):
+    """The writer as the on_checkpoint callback of the time-loop drivers: one file per checkpoint of
+    the reference's range t:freq:te, the last one holding the final state's fields."""
+    import plot_oracle as po
+    from epgpu import ic_slump, slump, snapshot
+    ic, cfg = ic_slump([64.1584, 16.0396], [40, 10], nonloc={"status": False, "ls": 0.5})
+    cfg["instr"]["plot"] = {"status": True, "freq": 0.5, "what": ["P", "epII", "z0", "n0"], "dims": (500.0, 250.0)}
+    ic["time"]["te"] = 1.0
+    cb = snapshot.writer(str(tmp_path), cfg["instr"], z0=ic["mpts"].z0)
+    out = slump(ic, cfg, workflow="elastodynamic", on_checkpoint=cb,
+                engine_factory=lambda a, b: oracle_mod.Oracle(a, b))
+    assert [round(snapshot.load(f)["t"], 9) for f in cb.written] == [0.0, 0.5, 1.0]
+    last = snapshot.load(cb.written[-1])
+    fin = out["ic"]["mpts"]
+    for opt in ("P", "epII", "n0"):
+        np.testing.assert_array_equal(last[opt], po.plot_field(fin, opt))
+    np.testing.assert_array_equal(last["x"], fin.x[0])
+    np.testing.assert_array_equal(last["z"], fin.x[-1])
+    np.testing.assert_array_equal(last["z0"], ic["mpts"].z0)
