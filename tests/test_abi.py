@@ -55,3 +55,40 @@ def test_batch_rejects_bad_arguments_without_gpu():
     assert lib.epgpu_batch_create(0, None, None, None, None, C.byref(h)) == 1
     assert lib.epgpu_batch_destroy(None) == 1
     assert lib.epgpu_batch_instance(None, 0) is None
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """The ctypes mirror of every struct (epgpu/abi.py, which the Julia binding copies field by field)
+    has the header's size and field offsets, as gcc lays them out."""
+    import shutil
+    import subprocess
+    import pytest
+    from epgpu import abi
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("gcc not found")
+    structs = [abi.ep_cfg, abi.ep_cmpr, abi.ep_mesh_view, abi.ep_mesh_fields, abi.ep_mpts_view, abi.ep_grf,
+               abi.ep_kernel_time, abi.ep_stats]
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "epgpu.h"', "int main(void) {"]
+    for S in structs:
+        n = S.__name__
+        lines.append(f'    printf("{n} sizeof %zu\\n", sizeof({n}));')
+        for f, _ in S._fields_:
+            lines.append(f'    printf("{n} {f} %zu\\n", offsetof({n}, {f}));')
+    lines += ["    return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([gcc, "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l.strip()}
+    bad = []
+    for S in structs:
+        n = S.__name__
+        if got[(n, "sizeof")] != C.sizeof(S):
+            bad.append((n, "sizeof", got[(n, "sizeof")], C.sizeof(S)))
+        for f, _ in S._fields_:
+            off = getattr(S, f).offset
+            if got[(n, f)] != off:
+                bad.append((n, f, got[(n, f)], off))
+    assert not bad, bad
