@@ -45,6 +45,16 @@ def test_create_rejects_bad_arguments_without_gpu():
                           C.byref(h))
     assert st == 2 and b"transfer" in lib.epgpu_last_error(None)
     assert lib.epgpu_destroy(None) == 1
+    # APIC in the mixed precisions on a mesh where the reference's D⁻¹ could differ from I (h = 4.01)
+    ic, cfg = ic_slump([64.1584, 16.0396], [16, 4])
+    c = abi.make_cfg(cfg["instr"])
+    c.trsfr, c.precision = 2, 1
+    mv = abi.MeshView(ic["mesh"])
+    st = lib.epgpu_create(C.byref(c), C.byref(abi.make_cmpr(ic["cmpr"])), C.byref(mv.view), ic["mpts"].nmp,
+                          C.byref(h))
+    assert st == 2 and b"apic" in lib.epgpu_last_error(None) and not h.value
+    # the device-field call checks its handle before anything else
+    assert lib.epgpu_fields(None, 1, None) == 1
 
 
 def test_batch_rejects_bad_arguments_without_gpu():
