@@ -155,9 +155,13 @@ class Clocks:
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
+    out_dir = None          # --clocks-out; a temporary folder when not given
+
     def __init__(self, gpu: int):
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_gpu{gpu}.csv")
-        os.makedirs(os.path.dirname(self.path), exist_ok=True)
+        import tempfile
+        d = Clocks.out_dir or tempfile.gettempdir()
+        self.path = os.path.join(d, f"clocks_gpu{gpu}_{os.getpid()}.csv")
+        os.makedirs(d, exist_ok=True)
         self.proc = None
         self.gpu = gpu
 
@@ -599,8 +603,11 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--settle", type=float, default=0.5,
                     help="simulated seconds of elastoplastic flow run before timing (plastic points appear)")
+    ap.add_argument("--clocks-out", default=None,
+                    help="folder for the nvidia-smi clock samples (default: a temporary folder)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    Clocks.out_dir = args.clocks_out
     rank, ws = dist_init()
     if args.impl == "reference":
         run_reference(args, rank, ws)

@@ -709,6 +709,10 @@ ep_status epgpu_upload(ep_handle* h, const ep_mpts_view* m) {
         !m->dlam || !m->epII || !m->sig || !m->tau || !m->Fij || !m->bij || !m->l || !m->l0 || !m->n0 || !m->n ||
         !m->dJ || !m->dvij)
         return fail(h, EP_ERR_ARG, "a point field read by the step is NULL");
+    // APIC's affine state is read by the step (p2n.jl:208-280): without it the device would keep
+    // stale Bᵢⱼ/Dᵢⱼ from an earlier upload
+    if (h->ctx.cf.trsfr == EP_TRSFR_APIC && (!m->Bij || !m->Dij))
+        return fail(h, EP_ERR_ARG, "a point field read by the step is NULL (Bij/Dij with APIC)");
     // the copies (back to back on the copy engine), then one k_xfer over the mapped host buffers
     std::vector<XField> f = xfer_fields(h, m);
     std::vector<XField*> rest;

@@ -275,7 +275,11 @@ extern "C" ep_status epgpu_bin_cells(int32_t dim, const int64_t* nel, const doub
 // totals -- is this file-scope device array, sized for EPGPU_NOALLOC_MAX_CELLS
 // cells.  Host code must not pass `g_bin_scratch` itself to a kernel (on the
 // host the name is only a stand-in, not a device address): the device address
-// is looked up once per device with cudaGetSymbolAddress and cached.
+// is looked up with cudaGetSymbolAddress on every call, with the caller's
+// device current.  The lookup is a host-side table read once the module is
+// loaded, and a per-call lookup stays valid across a cudaDeviceReset or a
+// primary context that was released and created again (a cached address
+// would then point into the freed module).
 // ---------------------------------------------------------------------------
 namespace {
 
@@ -284,24 +288,12 @@ constexpr int NOALLOC_SCRATCH_INTS = 2 * EPGPU_NOALLOC_MAX_CELLS + NOALLOC_TMP_I
 
 static __device__ __align__(256) int g_bin_scratch[NOALLOC_SCRATCH_INTS];
 
-constexpr int NOALLOC_MAX_DEVICES = 64;
-std::atomic<int*> g_scratch_addr[NOALLOC_MAX_DEVICES];
-
-// Device address of g_bin_scratch on the current device (set-up on first use).
+// Device address of g_bin_scratch in the current context.
 cudaError_t noalloc_scratch(int** out) {
-    int dev = -1;
-    cudaError_t e = cudaGetDevice(&dev);
+    void* q = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&q, g_bin_scratch);
     if (e != cudaSuccess) return e;
-    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return cudaErrorInvalidDevice;
-    int* p = g_scratch_addr[dev].load(std::memory_order_acquire);
-    if (!p) {
-        void* q = nullptr;
-        e = cudaGetSymbolAddress(&q, g_bin_scratch);
-        if (e != cudaSuccess) return e;
-        p = (int*)q;
-        g_scratch_addr[dev].store(p, std::memory_order_release);
-    }
-    *out = p;
+    *out = (int*)q;
     return cudaSuccess;
 }
 

@@ -254,9 +254,10 @@ ep_status epgpu_bin_cells(int32_t dim, const int64_t* nel, const double* h, cons
  * cudaMalloc/cudaFree would serialise the device.  The scratch (per-cell
  * counters and cursors, scan totals: about 4 MB) is one static array in
  * device memory, held by every GPU that loads the library until the process
- * exits.  The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress) with that device current; make that first call
- * before any stream capture.  All calls share the array and clear what must
+ * exits.  Every call looks up the array's device address (cudaGetSymbolAddress)
+ * in the current context, so the call stays valid after a cudaDeviceReset or a
+ * re-created primary context; the first call on a device may load the
+ * library's device code, so make it before any stream capture.  All calls share the array and clear what must
  * start at zero, so calls that overlap on the GPU (different streams or
  * threads at the same time) race: serialise them.  Inputs, outputs, the
  * stream and the synchronisation are as for epgpu_bin_cells; a mesh with

@@ -84,3 +84,44 @@ def test_batch_reports_instance_errors():
     with pytest.raises(abi.EPError) as ex:
         b.run(0, 1.0)
     assert "instance 1" in str(ex.value)
+
+
+def test_batch_instances_match_the_oracle(oracle_mod):
+    """Instances of a batch against the FP64 oracle directly: the 591-point c1 slump and the largest
+    instance the batched ensemble draws (nel = [320, 80], 3x3 points per cell: 91,344 points), each
+    with its own friction angle and seeded cohesion field, on the phase kernels over all instances.
+    Bounds: the mixed-precision targets, stress 1e-5 and displacement 1e-4 relative."""
+    import os
+    from epgpu import ic_slump
+    from epgpu.batch import Batch, bspline_invalid_nodes
+    from test_gpu_mixed import errors
+    inst = []
+    fw = {"deform": "finite", "trsfr": "std", "C_pf": 1.0, "musl": True, "locking": True, "damping": 0.1}
+    for k, (nx, ni, phi) in enumerate(((40, 2, 20.0), (320, 3, 30.0))):
+        grf = {"status": True, "covariance": "exponential",
+               "param": {"Ix": [5.0, 5.0], "mean": 2.0e4, "cov": 0.3, "min": 1.0e3, "seed": 1000 + k}}
+        ic, cfg = ic_slump([64.1584, 16.0396], [nx, nx // 4], ni=ni, cmpr_over={"phi0": math.radians(phi)},
+                           fwrk=fw, nonloc={"status": False, "ls": 0.5}, grf=grf)
+        assert bspline_invalid_nodes(ic["mesh"]) == 0
+        instr = copy.deepcopy(cfg["instr"])
+        instr["gpu"] = {"precision": "mixed_df", "jaumann": False}
+        inst.append((ic, cfg, instr))
+    assert inst[1][0]["mpts"].nmp == 91344
+    b = Batch([copy.deepcopy(ic) for ic, _, _ in inst], [i for _, _, i in inst])
+    assert b.scheme() == "phases"
+    windows = ((0, 0.6), (1, 0.9))
+    for phase, T in windows:
+        t, _ = b.run(phase, T)
+        assert np.all(t == T)
+    for k, (ic, cfg, _) in enumerate(inst):
+        # the oracle's scatters on several threads add in a varying order (FP64 rounding only)
+        o = oracle_mod.Oracle(copy.deepcopy(ic), cfg["instr"], threads=os.cpu_count() or 1)
+        t = 0.0
+        for phase, T in windows:
+            t, _ = o.run(phase, T, 10.0, t)
+        ref = o.download()
+        o.close()
+        s, d, r = errors(b.download(k), ref, ic["mpts"].x)
+        print(f"batch instance {k} ({ic['mpts'].nmp} points) vs oracle: stress {s:.2e} displacement {d:.2e} "
+              f"runout {r:.2e}, plastic {int((ref.dlam != 0).sum())}")
+        assert s <= 1e-5 and d <= 1e-4

@@ -52,7 +52,7 @@ def test_gradient_matches_oracle():
         e_bf = _rel(g[o:o + k], gref[o:o + k])
         e_64 = _rel(g[o:o + k], g64[o:o + k])
         print(f"grad {name}: vs BF16 restatement {e_bf:.2e}, vs FP64 {e_64:.2e}")
-        assert e_bf < 2e-2, name
+        assert e_bf < 1e-4, name
         assert e_64 < 6e-2, name
         o += k
 
@@ -212,7 +212,7 @@ def test_learned_step_against_the_oracle(oracle_mod, trained_net, hp):
     assert results["exact"][0] < 1e-4
     assert results["trained"][0] < 1e-3
     assert results["untrained"][1] > 0.8
-    assert results["trained"][1] < 0.5 and results["trained"][1] < 0.5 * results["untrained"][1]
+    assert results["trained"][1] < 0.02 and results["trained"][1] < 0.5 * results["untrained"][1]
 
 
 C1_3D = ([64.1584, 16.0396, 16.0396], [16, 4, 4])
