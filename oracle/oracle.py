@@ -14,12 +14,15 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "libeporacle.so")
+PROBE = os.path.join(HERE, "_build", "libscalarprobe.so")   # the library's scalar header, for tests
 
 
 def build(force: bool = False) -> str:
-    srcs = [os.path.join(HERE, f) for f in ("eporacle.cpp", "eporacle.h")]
+    srcs = [os.path.join(HERE, f) for f in ("eporacle.cpp", "eporacle.h", "scalar_probe.cpp", "Makefile")]
     srcs.append(os.path.join(HERE, "..", "elastoplasm.jl_gb300", "csrc", "ep_scalar.h"))
-    if force or not os.path.exists(LIB) or any(os.path.getmtime(s) > os.path.getmtime(LIB) for s in srcs):
+    outs = (LIB, PROBE)
+    if force or not all(os.path.exists(o) for o in outs) or any(
+            os.path.getmtime(s) > min(os.path.getmtime(o) for o in outs) for s in srcs):
         subprocess.run(["make", "-s", "-C", HERE], check=True)
     return LIB
 
