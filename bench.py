@@ -19,6 +19,7 @@ Arms:
 from __future__ import annotations
 
 import argparse
+import copy
 import json
 import math
 import os
@@ -603,6 +604,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--settle", type=float, default=0.5,
                     help="simulated seconds of elastoplastic flow run before timing (plastic points appear)")
+    ap.add_argument("--no-other-precision", dest="other_precision", action="store_false",
+                    help="skip the exact-map 'mixed' (FP64 islands) step timed beside a mixed_df headline")
     ap.add_argument("--clocks-out", default=None,
                     help="folder for the nvidia-smi clock samples (default: a temporary folder)")
     args = ap.parse_args()
@@ -726,15 +729,33 @@ def main():
         roof["mlp"] = {"bound": "tensor", "points_per_launch": slots, "avg_launch_ms": tot_ / nl_,
                        "achieved": tf, "unit": "TFLOP/s", "peak": bf[0], "frac": tf / bf[0],
                        "peak_source": bf[1]}
+    # the headline run's FP64 conservation sums at its start (host0) and end
+    cons_end = e.conservation()
+    e.upload(host0)
+    cons_start = e.conservation()
     # the exact-map mixed step beside the learned one
     exact = None
+    exact_final, exact_dts = None, None
     if learned:
         e.set_return_map(None, "exact")
-        ms_x, _, _, _ = timed(e, args.steps, args.warmup)
+        ms_x, exact_dts, _, _ = timed(e, args.steps, args.warmup)
+        exact_final = e.download()
         exact = {"value": ws * np_ * args.steps / (allmax(ms_x, ws) * 1e-3), "unit": "particle-steps/s",
                  "ms_per_step": ms_x / args.steps}
-    # the plain FP64 step beside it, and the stress error of this run against the FP64 step replayed
-    # with the same dt sequence from the same state (the FP64 step matches the FP64 oracle bit for bit)
+    # the benchmark spec-conforming precision beside the headline: FP64 islands (F, b_e, plastic strain,
+    # isotropic log/exp in FP64), exact return map
+    other = None
+    if args.precision == "mixed_df" and args.other_precision:
+        cfg_m = copy.deepcopy(cfg)
+        cfg_m["instr"]["gpu"] = {"precision": "mixed", "jaumann": False, "deterministic": args.deterministic}
+        em = Engine({"mesh": mesh, "mpts": host0.copy(), "cmpr": cmpr}, cfg_m["instr"])
+        ms_m, mixed_dts, _, _ = timed(em, args.steps, args.warmup)
+        other = {"precision": "mixed", "return_map": "exact",
+                 "value": ws * np_ * args.steps / (allmax(ms_m, ws) * 1e-3), "unit": "particle-steps/s",
+                 "ms_per_step": ms_m / args.steps, "final": em.download(), "dts": mixed_dts}
+        em.close()
+    # the plain FP64 step beside it, and the error of these runs against the FP64 step replayed with the
+    # same dt sequence from the same state (the FP64 step matches the FP64 oracle bit for bit)
     fp64 = None
     check = None
     if args.precision != "fp64" and (args.fp64_steps > 0 or not args.no_check):
@@ -742,24 +763,49 @@ def main():
         ic64["mpts"] = host0.copy()
         cfg64["instr"]["gpu"] = {"precision": "fp64", "jaumann": False}
         e64 = Engine(ic64, cfg64["instr"])
-        if not args.no_check:
-            for dt in dts:
+
+        def against_fp64(a, seq):
+            """Errors of the final state a of a run with dt sequence seq against the FP64 replay, and the
+            relative differences of their FP64 conservation sums."""
+            e64.upload(host0)
+            for dt in seq:
                 e64.step(1, dt, g)
-            a, b = final, e64.download()
+            b = e64.download()
             x0 = host0.x
-            check = {
-                "steps": len(dts),
+            c64 = e64.conservation()
+            return {
+                "steps": len(seq),
                 "stress_rel_l2": float(np.linalg.norm(a.tau - b.tau) / np.linalg.norm(b.tau)),
                 "displacement_rel_l2": float(np.linalg.norm(a.x - b.x) / max(np.linalg.norm(b.x - x0), 1e-300)),
                 "runout_rel": float(abs((a.x[0].max() - x0[0].max()) - (b.x[0].max() - x0[0].max()))
                                     / max(abs(b.x[0].max() - x0[0].max()), 1e-300)),
-            }
+            }, c64
+
+        if not args.no_check:
+            check, c64 = against_fp64(final, dts)
+            check["conservation_vs_fp64"] = {
+                k: abs(cons_end[k] - c64[k]) / abs(c64[k]) for k in ("mass", "kinetic", "elastic")}
+            if exact_final is not None:
+                check["exact_map"], _ = against_fp64(exact_final, exact_dts)
+            if other is not None:
+                other["error_vs_fp64"], _ = against_fp64(other.pop("final"), other.pop("dts"))
         if args.fp64_steps > 0:
             ms64, _, _, _ = timed(e64, args.fp64_steps, 3)
             fp64 = {"value": np_ * args.fp64_steps / (ms64 * 1e-3), "unit": "particle-steps/s",
                     "steps": args.fp64_steps, "ms_per_step": ms64 / args.fp64_steps}
         e64.close()
-    # end to end through the C ABI with host buffers: upload + step + download every step
+    if other is not None:
+        other.pop("final", None)
+        other.pop("dts", None)
+    conservation = {
+        "sums_end": {k: cons_end[k] for k in ("mass", "kinetic", "elastic")},
+        "mass_drift_rel": abs(cons_end["mass"] - cons_start["mass"]) / cons_start["mass"],
+        "note": "FP64 fixed-order sums (epgpu_conservation) of the timed run's start and end state; "
+                "mass = sum rho*Omega, kinetic = 1/2 sum m |v|^2, elastic = sum 1/2 tau.Del^-1 tau Omega0",
+    }
+    # end to end through the C ABI with host buffers, every step: the state the step reads and changes up
+    # (epgpu_upload_fields), the step, the same arrays down (epgpu_download_fields); the constants
+    # (c0, cr, phi, rho0, Omega0, ...) are uploaded once before the timed region
     e2e = None
     if not args.no_e2e:
         import ctypes as C
@@ -776,27 +822,27 @@ def main():
             if isinstance(v, np.ndarray) and v.dtype == np.float64:
                 setattr(hp, k, pin(v))
         view = abi.mpts_view(hp)
-        up = sum(getattr(hp, f).nbytes for f in ("x", "v", "l", "l0", "n0", "n", "Omega0", "Omega", "dJ", "J",
-                                                 "rho0", "rho", "c0", "cr", "phi", "dlam", "epII", "sig", "tau",
-                                                 "dvij", "dFij", "Fij", "bij", "eij", "wij", "sJij"))
-        down = up
         vm = np.zeros(dim)
-        e2 = Engine({"mesh": mesh, "mpts": hp, "cmpr": cmpr}, cfg["instr"])
+        e2 = Engine({"mesh": mesh, "mpts": hp, "cmpr": cmpr}, cfg["instr"])      # the full first upload
         if learned:
             e2.set_return_map(net, "learned")
+        moved = sorted(set(e2.fields_read()) & set(e2.fields_changed()))
+        mask = abi.mask_of(moved)
+        up = down = sum(getattr(hp, f).nbytes for f in moved)
         tot = 0.0
         for k in range(args.warmup + args.steps):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            e2._check(e2.lib.epgpu_upload(e2.h, C.byref(view)))
+            e2._check(e2.lib.epgpu_upload_fields(e2.h, C.byref(view), mask))
             vm = e2.step(1, cfl_dt(mesh, cmpr, vm), g)
-            e2._check(e2.lib.epgpu_download(e2.h, C.byref(view)))
+            e2._check(e2.lib.epgpu_download_fields(e2.h, C.byref(view), mask))
             if k >= args.warmup:
                 tot += time.perf_counter() - t0
         tot = allmax(tot, ws)
         e2.close()
         e2e = {"value": ws * np_ * args.steps / tot, "unit": "particle-steps/s", "h2d_bytes_per_step": up,
-               "d2h_bytes_per_step": down}
+               "d2h_bytes_per_step": down, "fields_moved": moved, "copies_declared": True,
+               "host_memory": "page-locked (pinned) numpy arrays"}
     cpu = None
     if rank == 0 and ws == 1 and args.cpu_seconds > 0:
         ic2, cfg2, _ = make_workload()
@@ -826,7 +872,7 @@ def main():
                        "parallelism": f"replicas x{ws}", "plastic_points_last_step": plastic,
                        "settle_s": args.settle},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-            "error_vs_fp64": check, "fp64_step": fp64,
+            "error_vs_fp64": check, "fp64_step": fp64, "other_precision": other, "conservation": conservation,
             "speedup_vs_fp64_step": (value / fp64["value"]) if fp64 else None,
             "learned_return_map": rm,
             "clocks": clk.summary(),

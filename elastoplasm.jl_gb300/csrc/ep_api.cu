@@ -27,6 +27,10 @@ struct DevBuf {
 
 }  // namespace
 
+// conservation sums: blocks of the fixed-order reduction and quantities per block
+constexpr int SUM_BLOCKS = 512;
+constexpr int SUM_Q = 10;
+
 struct ep_handle {
     ep_cfg cfg;
     ep_cmpr cm;
@@ -70,6 +74,9 @@ struct ep_handle {
     int* rm_int = nullptr;
     ep_mlp* rm_net = nullptr;
     int rm_mode = 0;
+    double* sums = nullptr;       // conservation sums: per-block partials, then the totals
+    uint64_t have = 0;            // EP_MPTS_* arrays uploaded at least once
+    bool staging_fresh = false;   // mixed precisions: the FP64 staging layout holds the current state
 };
 
 void ep::set_global_error(const char* msg) { g_create_error = msg ? msg : ""; }
@@ -370,6 +377,7 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
     // staging slots of the multi-component point fields: x v l l0 (d each), ϵpII (2), σ τ (ns each),
     // ∇v ΔF F b ϵ ω σJ (d² each); pass-through u, p (d each), ∇u (d²), ϵpV (1)
     ok = ok && dalloc(h, &h->xfer, (size_t)(4 * d + 2 + 2 * ns + 9 * d * d) * h->np) == cudaSuccess;
+    ok = ok && dalloc(h, &h->sums, (size_t)(SUM_BLOCKS + 1) * SUM_Q) == cudaSuccess;
     ok = ok && dalloc(h, &h->pass, (size_t)(2 * d + d * d + 1) * h->np) == cudaSuccess;
     if (ok && h->np) ok = cudaMemset(h->pass, 0, (size_t)(2 * d + d * d + 1) * h->np * sizeof(double)) == cudaSuccess;
     Sort& S = h->ctx.S;
@@ -701,10 +709,78 @@ static void xfer_split(std::vector<XField>& f, int dir, XferTab& T, int& nblk, s
     T.b0[T.n] = nblk;
 }
 
+// ---------------------------------------------------------------------------
+// Field masks of ep_mpts_view (EP_MPTS_* of include/epgpu.h): which arrays a step reads and changes.
+struct ViewField {
+    uint64_t bit;
+    double* ep_mpts_view::*ptr;
+    const char* name;
+};
+static const ViewField VIEW_FIELDS[] = {
+    {EP_MPTS_X, &ep_mpts_view::x, "x"}, {EP_MPTS_L0, &ep_mpts_view::l0, "l0"}, {EP_MPTS_L, &ep_mpts_view::l, "l"},
+    {EP_MPTS_N0, &ep_mpts_view::n0, "n0"}, {EP_MPTS_N, &ep_mpts_view::n, "n"},
+    {EP_MPTS_OMEGA0, &ep_mpts_view::Omega0, "Omega0"}, {EP_MPTS_OMEGA, &ep_mpts_view::Omega, "Omega"},
+    {EP_MPTS_DJ, &ep_mpts_view::dJ, "dJ"}, {EP_MPTS_J, &ep_mpts_view::J, "J"}, {EP_MPTS_U, &ep_mpts_view::u, "u"},
+    {EP_MPTS_V, &ep_mpts_view::v, "v"}, {EP_MPTS_P, &ep_mpts_view::p, "p"}, {EP_MPTS_RHO0, &ep_mpts_view::rho0, "rho0"},
+    {EP_MPTS_RHO, &ep_mpts_view::rho, "rho"}, {EP_MPTS_C0, &ep_mpts_view::c0, "c0"}, {EP_MPTS_CR, &ep_mpts_view::cr, "cr"},
+    {EP_MPTS_PHI, &ep_mpts_view::phi, "phi"}, {EP_MPTS_DLAM, &ep_mpts_view::dlam, "dlam"},
+    {EP_MPTS_EPII, &ep_mpts_view::epII, "epII"}, {EP_MPTS_EPV, &ep_mpts_view::epV, "epV"},
+    {EP_MPTS_SIG, &ep_mpts_view::sig, "sig"}, {EP_MPTS_TAU, &ep_mpts_view::tau, "tau"},
+    {EP_MPTS_DVIJ, &ep_mpts_view::dvij, "dvij"}, {EP_MPTS_DUIJ, &ep_mpts_view::duij, "duij"},
+    {EP_MPTS_DFIJ, &ep_mpts_view::dFij, "dFij"}, {EP_MPTS_FIJ, &ep_mpts_view::Fij, "Fij"},
+    {EP_MPTS_BIJ, &ep_mpts_view::bij, "bij"}, {EP_MPTS_EIJ, &ep_mpts_view::eij, "eij"},
+    {EP_MPTS_WIJ, &ep_mpts_view::wij, "wij"}, {EP_MPTS_SJIJ, &ep_mpts_view::sJij, "sJij"},
+    {EP_MPTS_APIC_B, &ep_mpts_view::Bij, "Bij"}, {EP_MPTS_APIC_D, &ep_mpts_view::Dij, "Dij"},
+};
+
+static uint64_t view_mask(const ep_mpts_view* m) {
+    uint64_t k = 0;
+    for (const ViewField& f : VIEW_FIELDS)
+        if (m->*f.ptr) k |= f.bit;
+    return k;
+}
+
+static std::string mask_names(uint64_t k) {
+    std::string out;
+    for (const ViewField& f : VIEW_FIELDS)
+        if (k & f.bit) out += (out.empty() ? "" : ", ") + std::string(f.name);
+    return out;
+}
+
+// What a step reads: the FP64 step's kernels read the previous state in place (ep_fp64.cu); the
+// mixed steps read what km_import and km_bin0 take from the staging layout (ep_mixed.cu).
+static uint64_t reads_of(const ep_handle* h) {
+    const Cfg& c = h->ctx.cf;
+    const bool fin = c.deform == EP_DEFORM_FINITE;
+    uint64_t k = EP_MPTS_X | EP_MPTS_V | EP_MPTS_OMEGA | EP_MPTS_OMEGA0 | EP_MPTS_RHO | EP_MPTS_C0 | EP_MPTS_CR |
+                 EP_MPTS_PHI | EP_MPTS_DLAM | EP_MPTS_EPII | EP_MPTS_FIJ | (fin ? EP_MPTS_TAU | EP_MPTS_BIJ : EP_MPTS_SIG);
+    if (c.basis == EP_BASIS_GIMPM) k |= EP_MPTS_L | EP_MPTS_L0;
+    if (c.trsfr == EP_TRSFR_TPIC) k |= EP_MPTS_DVIJ;
+    if (c.trsfr == EP_TRSFR_APIC) k |= EP_MPTS_APIC_B | (h->mixed ? 0ull : EP_MPTS_APIC_D);
+    if (!h->mixed && fin) k |= EP_MPTS_J | EP_MPTS_RHO0 | EP_MPTS_N0;
+    return k;
+}
+
+// What a step may change: the state it carries and the outputs derived from it (u, p, ∇u and ϵpV
+// are the caller's and pass through unchanged; ρ0, Ω0, ℓ0, n0, c0, cr, ϕ are material constants).
+static uint64_t changed_of(const ep_handle* h) {
+    const Cfg& c = h->ctx.cf;
+    uint64_t k = EP_MPTS_X | EP_MPTS_V | EP_MPTS_N | EP_MPTS_OMEGA | EP_MPTS_DJ | EP_MPTS_J | EP_MPTS_RHO |
+                 EP_MPTS_DLAM | EP_MPTS_EPII | EP_MPTS_SIG | EP_MPTS_TAU | EP_MPTS_DVIJ | EP_MPTS_DFIJ | EP_MPTS_FIJ |
+                 EP_MPTS_BIJ | EP_MPTS_EIJ | EP_MPTS_WIJ | EP_MPTS_SJIJ;
+    if (c.basis == EP_BASIS_GIMPM && c.how != EP_HOW_UNDEFORMED && c.how != EP_HOW_NONE) k |= EP_MPTS_L;
+    if (c.trsfr == EP_TRSFR_APIC) k |= EP_MPTS_APIC_B | EP_MPTS_APIC_D;
+    return k;
+}
+
+uint64_t epgpu_fields_read(const ep_handle* h) { return h ? reads_of(h) : 0ull; }
+uint64_t epgpu_fields_changed(const ep_handle* h) { return h ? changed_of(h) : 0ull; }
+
+static ep_status upload_view(ep_handle* h, const ep_mpts_view* m);
+
 ep_status epgpu_upload(ep_handle* h, const ep_mpts_view* m) {
     if (!h || !m) return EP_ERR_ARG;
     if (m->nmp != h->np || m->ndim != h->dim) return fail(h, EP_ERR_ARG, "mpts.nmp/ndim differ from create");
-    const int d = h->dim;
     if (!m->x || !m->v || !m->Omega0 || !m->Omega || !m->J || !m->rho0 || !m->rho || !m->c0 || !m->cr || !m->phi ||
         !m->dlam || !m->epII || !m->sig || !m->tau || !m->Fij || !m->bij || !m->l || !m->l0 || !m->n0 || !m->n ||
         !m->dJ || !m->dvij)
@@ -713,6 +789,33 @@ ep_status epgpu_upload(ep_handle* h, const ep_mpts_view* m) {
     // stale Bᵢⱼ/Dᵢⱼ from an earlier upload
     if (h->ctx.cf.trsfr == EP_TRSFR_APIC && (!m->Bij || !m->Dij))
         return fail(h, EP_ERR_ARG, "a point field read by the step is NULL (Bij/Dij with APIC)");
+    return upload_view(h, m);
+}
+
+ep_status epgpu_upload_fields(ep_handle* h, const ep_mpts_view* m, uint64_t mask) {
+    if (!h || !m) return EP_ERR_ARG;
+    if (m->nmp != h->np || m->ndim != h->dim) return fail(h, EP_ERR_ARG, "mpts.nmp/ndim differ from create");
+    if (mask & ~EP_MPTS_ALL) return fail(h, EP_ERR_ARG, "unknown bits in the field mask");
+    const uint64_t given = view_mask(m);
+    if (mask & ~given) return fail(h, EP_ERR_ARG, "a field in the mask is NULL: " + mask_names(mask & ~given));
+    const uint64_t missing = reads_of(h) & ~(mask | h->have);
+    if (missing) return fail(h, EP_ERR_ARG, "fields read by the step were never uploaded: " + mask_names(missing));
+    // the arrays outside the mask keep their device values: in the mixed precisions those live in the
+    // step's own layout, so the staging layout the import reads is brought up to date first
+    if (h->mixed && h->uploaded && !h->staging_fresh) {
+        mixed_export(h->mx, h->ctx.P, h->ctx.N, h->s, false);
+        CK(h, cudaGetLastError());
+        h->staging_fresh = true;
+    }
+    ep_mpts_view v = *m;
+    for (const ViewField& f : VIEW_FIELDS)
+        if (!(mask & f.bit)) v.*f.ptr = nullptr;
+    return upload_view(h, &v);
+}
+
+// the upload proper: every non-NULL array of the view is copied in
+static ep_status upload_view(ep_handle* h, const ep_mpts_view* m) {
+    const int d = h->dim;
     // the copies (back to back on the copy engine), then one k_xfer over the mapped host buffers
     std::vector<XField> f = xfer_fields(h, m);
     std::vector<XField*> rest;
@@ -728,7 +831,7 @@ ep_status epgpu_upload(ep_handle* h, const ep_mpts_view* m) {
     // tan/sin/cos of the friction angle, evaluated on the host (material constants), again only
     // when ϕ differs from the last upload (the comparison runs while the transfers are in flight)
     const size_t np = (size_t)h->np;
-    if (h->phi_cache.size() != np || (np && std::memcmp(h->phi_cache.data(), m->phi, np * sizeof(double)) != 0)) {
+    if (m->phi && (h->phi_cache.size() != np || (np && std::memcmp(h->phi_cache.data(), m->phi, np * sizeof(double)) != 0))) {
         CK(h, cudaStreamSynchronize(h->s));          // tphi_host may still be read by the last copy
         h->tphi_host.resize(3 * np);
         double* t = h->tphi_host.data();
@@ -755,6 +858,8 @@ ep_status epgpu_upload(ep_handle* h, const ep_mpts_view* m) {
     CK(h, cudaStreamSynchronize(h->s));
     CK(h, cudaGetLastError());
     h->uploaded = true;
+    h->staging_fresh = true;
+    h->have |= view_mask(m);
     return EP_OK;
 }
 
@@ -835,6 +940,7 @@ ep_status epgpu_step(ep_handle* h, int32_t phase, double dt, const double* g, do
     cudaEventElapsedTime(&ms, h->ev0, h->ev1);
     h->last_ms = ms;
     h->steps += 1;
+    h->staging_fresh = false;
     if (vmax_out)
         for (int i = 0; i < h->dim; ++i) vmax_out[i] = bits_to_double(h->hctl->vmax_bits[i]);
     return kernel_error(h);
@@ -897,18 +1003,40 @@ ep_status epgpu_run(ep_handle* h, int32_t phase, double T, double tg, double* t_
     *t_inout = h->hctl->t;
     h->t = h->hctl->t;
     h->steps += h->hctl->nsteps;
+    h->staging_fresh = false;
     if (nsteps_out) *nsteps_out = h->hctl->nsteps;
     return kernel_error(h);
 }
 
+static ep_status download_view(ep_handle* h, ep_mpts_view* m, bool need_eps);
+
 ep_status epgpu_download(ep_handle* h, ep_mpts_view* m) {
     if (!h || !m) return EP_ERR_ARG;
     if (m->nmp != h->np || m->ndim != h->dim) return fail(h, EP_ERR_ARG, "mpts.nmp/ndim differ from create");
+    return download_view(h, m, true);
+}
+
+ep_status epgpu_download_fields(ep_handle* h, ep_mpts_view* m, uint64_t mask) {
+    if (!h || !m) return EP_ERR_ARG;
+    if (m->nmp != h->np || m->ndim != h->dim) return fail(h, EP_ERR_ARG, "mpts.nmp/ndim differ from create");
+    if (mask & ~EP_MPTS_ALL) return fail(h, EP_ERR_ARG, "unknown bits in the field mask");
+    const uint64_t given = view_mask(m);
+    if (mask & ~given) return fail(h, EP_ERR_ARG, "a field in the mask is NULL: " + mask_names(mask & ~given));
+    ep_mpts_view v = *m;
+    for (const ViewField& f : VIEW_FIELDS)
+        if (!(mask & f.bit)) v.*f.ptr = nullptr;
+    v.p2e = nullptr;
+    v.p2n = nullptr;
+    return download_view(h, &v, (mask & EP_MPTS_EIJ) != 0);
+}
+
+static ep_status download_view(ep_handle* h, ep_mpts_view* m, bool need_eps) {
     const int d = h->dim;
     ep_status st;
     if (h->mixed && h->uploaded) {
-        mixed_export(h->mx, h->ctx.P, h->ctx.N, h->s);
+        mixed_export(h->mx, h->ctx.P, h->ctx.N, h->s, need_eps);
         CK(h, cudaGetLastError());
+        h->staging_fresh = true;
     }
     if ((st = read_ctl(h)) != EP_OK) return st;
     // one k_xfer into the mapped host buffers; the other fields transposed into staging, then
@@ -1008,6 +1136,7 @@ ep_status epgpu_fields(ep_handle* h, uint32_t what, double* out) {
     if (h->mixed) {
         mixed_export(h->mx, h->ctx.P, h->ctx.N, h->s);
         CK(h, cudaGetLastError());
+        h->staging_fresh = true;
     }
     FieldSrc S;
     const double* sig = fld_ptr(h, F_SIG);
@@ -1043,8 +1172,9 @@ ep_status epgpu_download_mesh(ep_handle* h, ep_mesh_fields* f) {
     const int d = h->dim;
     const size_t Nn = h->nnode;
     if (h->mixed && h->uploaded) {
-        mixed_export(h->mx, h->ctx.P, h->ctx.N, h->s);
+        mixed_export(h->mx, h->ctx.P, h->ctx.N, h->s, false);
         CK(h, cudaGetLastError());
+        h->staging_fresh = true;
     }
     std::vector<double> buf((size_t)(1 + 4 * d + 1) * Nn);
     CK(h, cudaMemcpyAsync(buf.data(), h->nbuf, buf.size() * sizeof(double), cudaMemcpyDeviceToHost, h->s));
@@ -1095,6 +1225,122 @@ ep_status epgpu_stats(ep_handle* h, ep_stats* out) {
     out->device_ms = h->last_ms;
     out->t = h->t;
     out->plastic = h->hctl->plastic;
+    return EP_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Conservation sums in FP64 (epgpu_conservation).  Fixed-order reductions: block b sums the points (or
+// nodes) [b*chunk, (b+1)*chunk) with thread t taking every 256th one from b*chunk + t in ascending order,
+// then a shared-memory tree in a fixed pairing; one block then adds the SUM_BLOCKS partials the same
+// way.  The result depends only on the data, not on scheduling.
+// Quantities: 0 Σ ρΩ, 1-3 Σ ρΩ v, 4 ½ Σ ρΩ |v|², 5 ½ Σ Ω τ·Del⁻¹τ, 6 Σ m_n, 7-9 Σ p_n.
+struct SumSrc {
+    const double *rho, *om, *om0, *v[3], *st[6];
+    const double *m, *p[3];
+    int np, nnode, dim, ns, fin;
+};
+
+__device__ __forceinline__ double elastic_energy(const Mat& mt, const double* st, int ns) {
+    double x[6];
+    if (ns == 3) lu_solve<3>(mt.DelLU, mt.piv, st, x);
+    else lu_solve<6>(mt.DelLU, mt.piv, st, x);
+    double w = st[0] * x[0];
+    for (int i = 1; i < ns; ++i) w = w + st[i] * x[i];
+    return 0.5 * w;
+}
+
+__device__ __forceinline__ void block_sum_fixed(double* sh, double* q, int nq, double* out) {
+    const int t = threadIdx.x;
+    for (int k = 0; k < nq; ++k) sh[k * 256 + t] = q[k];
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (t < w)
+            for (int k = 0; k < nq; ++k) sh[k * 256 + t] = sh[k * 256 + t] + sh[k * 256 + t + w];
+        __syncthreads();
+    }
+    if (t < nq) out[t] = sh[t * 256];
+}
+
+__global__ void __launch_bounds__(256) k_sums(const SumSrc S, const Mat mt, double* part) {
+    __shared__ double sh[SUM_Q * 256];
+    double q[SUM_Q];
+    for (int k = 0; k < SUM_Q; ++k) q[k] = 0.0;
+    const int b = blockIdx.x, t = threadIdx.x;
+    const int pc = (S.np + SUM_BLOCKS - 1) / SUM_BLOCKS, nc = (S.nnode + SUM_BLOCKS - 1) / SUM_BLOCKS;
+    const int p0 = b * pc, p1 = min(S.np, p0 + pc);
+    for (int p = p0 + t; p < p1; p += 256) {
+        const double m = S.rho[p] * S.om[p];
+        double v2 = 0.0;
+        q[0] = q[0] + m;
+        for (int d = 0; d < S.dim; ++d) {
+            const double v = S.v[d][p];
+            q[1 + d] = q[1 + d] + m * v;
+            v2 = v2 + v * v;
+        }
+        q[4] = q[4] + 0.5 * (m * v2);
+        double st[6];
+        for (int k = 0; k < S.ns; ++k) st[k] = S.st[k][p];
+        const double w = elastic_energy(mt, st, S.ns);
+        q[5] = q[5] + w * (S.fin ? S.om0[p] : S.om[p]);
+    }
+    const int n0 = b * nc, n1 = min(S.nnode, n0 + nc);
+    for (int n = n0 + t; n < n1; n += 256) {
+        q[6] = q[6] + S.m[n];
+        for (int d = 0; d < S.dim; ++d) q[7 + d] = q[7 + d] + S.p[d][n];
+    }
+    block_sum_fixed(sh, q, SUM_Q, part + (size_t)b * SUM_Q);
+}
+
+__global__ void __launch_bounds__(256) k_sums_final(const double* part, double* out) {
+    __shared__ double sh[SUM_Q * 256];
+    double q[SUM_Q];
+    for (int k = 0; k < SUM_Q; ++k) q[k] = 0.0;
+    for (int b = threadIdx.x; b < SUM_BLOCKS; b += 256)
+        for (int k = 0; k < SUM_Q; ++k) q[k] = q[k] + part[(size_t)b * SUM_Q + k];
+    block_sum_fixed(sh, q, SUM_Q, out);
+}
+
+ep_status epgpu_conservation(ep_handle* h, ep_conservation* out) {
+    if (!h || !out) return EP_ERR_ARG;
+    if (!h->uploaded) return fail(h, EP_ERR_STATE, "conservation sums before upload");
+    const int d = h->dim;
+    if (h->mixed) {
+        mixed_export(h->mx, h->ctx.P, h->ctx.N, h->s, false);
+        CK(h, cudaGetLastError());
+        h->staging_fresh = true;
+    }
+    const P64& P = h->ctx.P;
+    const N64& N = h->ctx.N;
+    SumSrc S{};
+    S.rho = P.rho;
+    S.om = P.Om;
+    S.om0 = P.Om0;
+    S.fin = h->cfg.deform == EP_DEFORM_FINITE;
+    for (int i = 0; i < d; ++i) {
+        S.v[i] = P.v[i];
+        S.p[i] = N.p[i];
+    }
+    S.ns = h->nstr;
+    for (int k = 0; k < h->nstr; ++k) S.st[k] = S.fin ? P.tau[k] : P.sig[k];
+    S.m = N.m;
+    S.np = h->np;
+    S.nnode = h->nnode;
+    S.dim = d;
+    k_sums<<<SUM_BLOCKS, 256, 0, h->s>>>(S, h->ctx.mt, h->sums);
+    k_sums_final<<<1, 256, 0, h->s>>>(h->sums, h->sums + (size_t)SUM_BLOCKS * SUM_Q);
+    CK(h, cudaGetLastError());
+    double q[SUM_Q];
+    CK(h, cudaMemcpyAsync(q, h->sums + (size_t)SUM_BLOCKS * SUM_Q, sizeof q, cudaMemcpyDeviceToHost, h->s));
+    CK(h, cudaStreamSynchronize(h->s));
+    std::memset(out, 0, sizeof *out);
+    out->mass = q[0];
+    out->kinetic = q[4];
+    out->elastic = q[5];
+    out->mass_nodes = q[6];
+    for (int i = 0; i < d; ++i) {
+        out->momentum[i] = q[1 + i];
+        out->momentum_nodes[i] = q[7 + i];
+    }
     return EP_OK;
 }
 
@@ -1438,6 +1684,7 @@ ep_status epgpu_batch_run(ep_batch* b, int32_t phase, double T, double tg, doubl
         h->launches += launched * (b->used_scheme() != 0 ? 1 : h->graph_kernels[phase]);
         h->t = h->hctl->t;
         h->steps += h->hctl->nsteps;
+        h->staging_fresh = false;
         t_inout[i] = h->hctl->t;
         if (nsteps_out) nsteps_out[i] = h->hctl->nsteps;
     }

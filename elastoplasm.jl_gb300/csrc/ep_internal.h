@@ -142,7 +142,8 @@ long long mlp_record_cap(ep_mlp* m);
 void launch_mixed_scan(const MixedCtx& X, cudaStream_t s);
 void mixed_initial_scan(const MixedCtx& X, cudaStream_t s);
 void mixed_import(const MixedCtx& X, const P64& Q, cudaStream_t s);
-void mixed_export(const MixedCtx& X, const P64& Q, const N64& QN, cudaStream_t s);
+// the FP64 staging state from the mixed state; need_eps = false skips the log strain ϵ = ½ log b
+void mixed_export(const MixedCtx& X, const P64& Q, const N64& QN, cudaStream_t s, bool need_eps = true);
 
 // control-block kernels (ep_fp64.cu)
 void launch_ctl_begin_run(Ctl* ctl, const Geo& g, double c, cudaStream_t s);

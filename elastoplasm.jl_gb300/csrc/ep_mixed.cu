@@ -1884,7 +1884,9 @@ __global__ void km_place0(MCtx A) {
     place_next(A, p, A.ctl->parity);
 }
 
-__global__ void km_export(MCtx A, P64 Q) {
+// need_eps = 0: the log strain ϵ = ½ log b (FP64 eigen + log per point) is not formed; callers that
+// do not read ϵ (masked downloads, conservation sums) skip that work
+__global__ void km_export(MCtx A, P64 Q, int need_eps) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= A.P.np) return;
     const int cur = A.ctl->parity, D = A.g.dim, NS = D == 2 ? 3 : 6;
@@ -1926,20 +1928,27 @@ __global__ void km_export(MCtx A, P64 Q) {
         }
         if (D == 2) {
             Q.b[0][p] = B[0]; Q.b[3][p] = B[1]; Q.b[1][p] = B[2]; Q.b[2][p] = B[2];
+        } else {
+            for (int k = 0; k < 6; ++k) {
+                const int i = sym_i(3, k), j = sym_j(3, k);
+                Q.b[i + 3 * j][p] = B[k];
+                Q.b[j + 3 * i][p] = B[k];
+            }
+        }
+        if (need_eps && D == 2) {
             double lam[2], V[4], L[2], R[4];
             eig_sym2(B[0], B[2], B[1], lam, V);
             L[0] = ep_log(lam[0]);
             L[1] = ep_log(lam[1]);
             vdvt<2>(V, L, R);
             for (int k = 0; k < 4; ++k) Q.eps[k][p] = 0.5 * R[k];
-        } else {
+        } else if (need_eps) {
             double Bt[9], lam[3], V[9], L[3], R[9];
             for (int k = 0; k < 6; ++k) {
                 const int i = sym_i(3, k), j = sym_j(3, k);
                 Bt[i + 3 * j] = B[k];
                 Bt[j + 3 * i] = B[k];
             }
-            for (int k = 0; k < 9; ++k) Q.b[k][p] = Bt[k];
             eig_sym3(Bt, lam, V);
             for (int k = 0; k < 3; ++k) L[k] = ep_log(lam[k]);
             vdvt<3>(V, L, R);
@@ -3819,10 +3828,10 @@ void mixed_import(const MixedCtx& X, const P64& Q, cudaStream_t s) {
     if (A.cf.det) km_sort_cells<<<(A.g.ncell + 255) / 256, 256, 0, s>>>(A, 1);
 }
 
-void mixed_export(const MixedCtx& X, const P64& Q, const N64& QN, cudaStream_t s) {
+void mixed_export(const MixedCtx& X, const P64& Q, const N64& QN, cudaStream_t s, bool need_eps) {
     const MCtx& A = *(const MCtx*)X.impl;
     const int np = A.P.np;
-    if (np > 0) km_export<<<(np + 255) / 256, 256, 0, s>>>(A, Q);
+    if (np > 0) km_export<<<(np + 255) / 256, 256, 0, s>>>(A, Q, need_eps ? 1 : 0);
     km_export_nodes<<<(A.g.nnode + 255) / 256, 256, 0, s>>>(A, QN);
 }
 

@@ -53,6 +53,24 @@ _MPTS_FIELDS = ["vmax", "x", "l0", "l", "n0", "n", "Omega0", "Omega", "dJ", "J",
                 "dvij", "duij", "dFij", "Fij", "bij", "eij", "wij", "sJij"]
 
 
+# EP_MPTS_* bits of include/epgpu.h: one per array of ep_mpts_view, in this order
+MPTS_BITS = {f: 1 << k for k, f in enumerate(["x", "l0", "l", "n0", "n", "Omega0", "Omega", "dJ", "J", "u", "v", "p",
+                                              "rho0", "rho", "c0", "cr", "phi", "dlam", "epII", "epV", "sig", "tau",
+                                              "dvij", "duij", "dFij", "Fij", "bij", "eij", "wij", "sJij", "Bij",
+                                              "Dij"])}
+
+
+def mask_of(names) -> int:
+    m = 0
+    for n in names:
+        m |= MPTS_BITS[n]
+    return m
+
+
+def names_of(mask: int) -> list:
+    return [f for f, b in MPTS_BITS.items() if mask & b]
+
+
 class ep_mpts_view(C.Structure):
     _fields_ = ([("ndim", C.c_int64), ("nmp", C.c_int64)] + [(f, _D) for f in _MPTS_FIELDS]
                 + [("p2e", _I64), ("p2n", _I64), ("Bij", _D), ("Dij", _D)])
@@ -71,6 +89,11 @@ class ep_kernel_time(C.Structure):
 class ep_stats(C.Structure):
     _fields_ = [("steps", C.c_int64), ("launches", C.c_int64), ("device_ms", C.c_double),
                 ("t", C.c_double), ("plastic", C.c_int64)]
+
+
+class ep_conservation(C.Structure):
+    _fields_ = [("mass", C.c_double), ("momentum", C.c_double * 3), ("kinetic", C.c_double),
+                ("elastic", C.c_double), ("mass_nodes", C.c_double), ("momentum_nodes", C.c_double * 3)]
 
 
 def _dptr(a: np.ndarray):
@@ -126,7 +149,8 @@ def mpts_view(mpts, with_topology: bool = False) -> ep_mpts_view:
     v.nmp = mpts.nmp
     for f in _MPTS_FIELDS:
         a = getattr(mpts, f)
-        setattr(v, f, _dptr(a))
+        if a is not None:                        # None: a NULL pointer (skipped or refused by the call)
+            setattr(v, f, _dptr(a))
     if with_topology and mpts.p2e is not None:
         v.p2e = mpts.p2e.ctypes.data_as(_I64)
         v.p2n = mpts.p2n.ctypes.data_as(_I64)
@@ -163,9 +187,14 @@ SIGNATURES = {
     "epgpu_step": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, _D, _D]),
     "epgpu_run": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_double, _D, _I64]),
     "epgpu_download": (C.c_int, [C.c_void_p, C.POINTER(ep_mpts_view)]),
+    "epgpu_upload_fields": (C.c_int, [C.c_void_p, C.POINTER(ep_mpts_view), C.c_uint64]),
+    "epgpu_download_fields": (C.c_int, [C.c_void_p, C.POINTER(ep_mpts_view), C.c_uint64]),
+    "epgpu_fields_read": (C.c_uint64, [C.c_void_p]),
+    "epgpu_fields_changed": (C.c_uint64, [C.c_void_p]),
     "epgpu_download_mesh": (C.c_int, [C.c_void_p, C.POINTER(ep_mesh_fields)]),
     "epgpu_fields": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p]),
     "epgpu_stats": (C.c_int, [C.c_void_p, C.POINTER(ep_stats)]),
+    "epgpu_conservation": (C.c_int, [C.c_void_p, C.POINTER(ep_conservation)]),
     "epgpu_destroy": (C.c_int, [C.c_void_p]),
     "epgpu_profile": (C.c_int, [C.c_void_p, C.c_int32]),
     "epgpu_profile_read": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]),

@@ -110,22 +110,28 @@ class Batch:
 
 
 def bspline_invalid_nodes(mesh) -> int:
-    """Nodes whose cubic B-spline piece cannot be chosen: the reference compares a node's
-    coordinate with xB, xB + h, xB - h exactly (bsmpm.jl:63-76) and raises "Invalid
-    position" for a point touching such a node; some meshes' rounded coordinates miss."""
+    """Nodes whose cubic B-spline piece the reference cannot choose, or chooses so that the basis
+    loses its partition of unity.  The reference compares a node's coordinate with xB, xB + h,
+    xB - h exactly (bsmpm.jl:63-76): a node that misses every comparison raises "Invalid
+    position"; a node one cell inside a boundary whose rounded coordinate misses xB + h (or
+    xB - h) but lies strictly inside (xB + h, xB - h) takes the interior piece instead of the
+    boundary-adjacent one, the stencil weights near that boundary no longer sum to one (by 0.16),
+    and the run moves without load.  Both are counted (nel_x = 320 is such a mesh)."""
     bad = 0
     for d in range(mesh.dim):
         xn = np.unique(mesh.x[d])
         x0, x1, h = float(mesh.xB[d, 0]), float(mesh.xB[d, 1]), float(mesh.h[d])
         ok = (xn == x0) | (xn == x0 + h) | (((x0 + h) < xn) & (xn < (x1 - h))) | (xn == x1 - h) | (xn == x1)
         bad += int((~ok & (xn >= x0) & (xn <= x1)).sum())
+        bad += int(not np.any(xn == x0 + h)) + int(not np.any(xn == x1 - h))
     return bad
 
 
 def slump_ensemble(n=256, seed=0, nelx=(40, 320), precision="mixed_df", grf=True):
     """(ics, instrs, description) of the uneven ensemble of the batched configuration.  A mesh
-    with a node the reference's B-spline piece selection rejects (bspline_invalid_nodes) is
-    drawn again; description[k] = (nel_x, ni, friction deg, points, meshes drawn again)."""
+    whose nodes the reference's B-spline piece selection rejects or misclassifies
+    (bspline_invalid_nodes) is drawn again; description[k] = (nel_x, ni, friction deg, points,
+    meshes drawn again)."""
     from .ic import ic_slump
     rng = np.random.default_rng(seed)
     ics, instrs, desc = [], [], []

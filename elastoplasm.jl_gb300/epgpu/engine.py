@@ -42,6 +42,23 @@ class Engine:
     def upload(self, mpts):
         self._check(self.lib.epgpu_upload(self.h, C.byref(abi.mpts_view(mpts))))
 
+    def fields_read(self) -> list:
+        """Names of the point arrays a step of this configuration reads (``epgpu_fields_read``)."""
+        return abi.names_of(self.lib.epgpu_fields_read(self.h))
+
+    def fields_changed(self) -> list:
+        """Names of the point arrays a step may change (``epgpu_fields_changed``)."""
+        return abi.names_of(self.lib.epgpu_fields_changed(self.h))
+
+    def upload_fields(self, mpts, names):
+        """Upload only the named arrays; the others keep their device values (``epgpu_upload_fields``)."""
+        self._check(self.lib.epgpu_upload_fields(self.h, C.byref(abi.mpts_view(mpts)), abi.mask_of(names)))
+
+    def download_fields(self, mpts, names):
+        """Download only the named arrays into ``mpts`` (``epgpu_download_fields``); vmax too."""
+        self._check(self.lib.epgpu_download_fields(self.h, C.byref(abi.mpts_view(mpts)), abi.mask_of(names)))
+        return mpts
+
     def download(self, mpts=None):
         mpts = mpts or self.mpts.copy()
         self._check(self.lib.epgpu_download(self.h, C.byref(abi.mpts_view(mpts, with_topology=True))))
@@ -85,6 +102,15 @@ class Engine:
         self._check(self.lib.epgpu_stats(self.h, C.byref(s)))
         return {"steps": s.steps, "launches": s.launches, "device_ms": s.device_ms, "t": s.t,
                 "plastic": s.plastic}
+
+    def conservation(self) -> dict:
+        """FP64 conservation sums of the current state (``epgpu_conservation``): point mass, momentum,
+        kinetic and elastic energy, and the last step's nodal mass and momentum."""
+        c = abi.ep_conservation()
+        self._check(self.lib.epgpu_conservation(self.h, C.byref(c)))
+        d = self.mpts.ndim
+        return {"mass": c.mass, "momentum": np.array(c.momentum[:d]), "kinetic": c.kinetic,
+                "elastic": c.elastic, "mass_nodes": c.mass_nodes, "momentum_nodes": np.array(c.momentum_nodes[:d])}
 
     def profile(self, enable: bool = True):
         self._check(self.lib.epgpu_profile(self.h, int(enable)))

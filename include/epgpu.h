@@ -190,6 +190,60 @@ ep_status epgpu_run(ep_handle* h, int32_t phase, double T, double tg, double* t_
 /* Copy the point state out (device SoA -> host AoS); NULL fields are skipped. */
 ep_status epgpu_download(ep_handle* h, ep_mpts_view* mpts);
 
+/* ---- Moving only some point fields ------------------------------------------
+ * One bit per array of ep_mpts_view.  A host that keeps the library's device state between steps
+ * (the reference's time loop calls shpfun/mapsto/elastoplast on the same Point every step,
+ * worflow.jl:34-36, 80-82) needs to move only what changed: the state the step reads and changes,
+ * epgpu_fields_read(h) & epgpu_fields_changed(h), and nothing of the material constants after the
+ * first upload. */
+#define EP_MPTS_X      (1ull << 0)
+#define EP_MPTS_L0     (1ull << 1)
+#define EP_MPTS_L      (1ull << 2)
+#define EP_MPTS_N0     (1ull << 3)
+#define EP_MPTS_N      (1ull << 4)
+#define EP_MPTS_OMEGA0 (1ull << 5)
+#define EP_MPTS_OMEGA  (1ull << 6)
+#define EP_MPTS_DJ     (1ull << 7)
+#define EP_MPTS_J      (1ull << 8)
+#define EP_MPTS_U      (1ull << 9)
+#define EP_MPTS_V      (1ull << 10)
+#define EP_MPTS_P      (1ull << 11)
+#define EP_MPTS_RHO0   (1ull << 12)
+#define EP_MPTS_RHO    (1ull << 13)
+#define EP_MPTS_C0     (1ull << 14)
+#define EP_MPTS_CR     (1ull << 15)
+#define EP_MPTS_PHI    (1ull << 16)
+#define EP_MPTS_DLAM   (1ull << 17)
+#define EP_MPTS_EPII   (1ull << 18)
+#define EP_MPTS_EPV    (1ull << 19)
+#define EP_MPTS_SIG    (1ull << 20)
+#define EP_MPTS_TAU    (1ull << 21)
+#define EP_MPTS_DVIJ   (1ull << 22)
+#define EP_MPTS_DUIJ   (1ull << 23)
+#define EP_MPTS_DFIJ   (1ull << 24)
+#define EP_MPTS_FIJ    (1ull << 25)
+#define EP_MPTS_BIJ    (1ull << 26)   /* bij: the elastic left Cauchy-Green tensor b_e */
+#define EP_MPTS_EIJ    (1ull << 27)
+#define EP_MPTS_WIJ    (1ull << 28)
+#define EP_MPTS_SJIJ   (1ull << 29)
+#define EP_MPTS_APIC_B (1ull << 30)   /* Bij of APIC */
+#define EP_MPTS_APIC_D (1ull << 31)   /* Dij of APIC */
+#define EP_MPTS_ALL    ((1ull << 32) - 1ull)
+
+/* The arrays a step of this handle reads (its switches and precision decide). */
+uint64_t epgpu_fields_read(const ep_handle* h);
+/* The arrays a step of this handle may change (state and the outputs derived from it). */
+uint64_t epgpu_fields_changed(const ep_handle* h);
+
+/* epgpu_upload of the arrays in `mask` only; every one of them must be non-NULL in the view.  The
+ * other arrays keep their device values.  Every array in epgpu_fields_read(h) must have been
+ * uploaded at least once (by this call or an earlier upload), else EP_ERR_ARG names the missing ones. */
+ep_status epgpu_upload_fields(ep_handle* h, const ep_mpts_view* mpts, uint64_t mask);
+
+/* epgpu_download of the arrays in `mask` only (each must be non-NULL in the view); vmax is written
+ * when the view's vmax is non-NULL.  The mixed precisions form the log strain ϵ only when EIJ is asked. */
+ep_status epgpu_download_fields(ep_handle* h, ep_mpts_view* mpts, uint64_t mask);
+
 /* Copy the nodal fields of the last step out; NULL fields are skipped. */
 ep_status epgpu_download_mesh(ep_handle* h, ep_mesh_fields* f);
 
@@ -216,6 +270,24 @@ ep_status epgpu_download_mesh(ep_handle* h, ep_mesh_fields* f);
 ep_status epgpu_fields(ep_handle* h, uint32_t what, double* out);
 
 ep_status epgpu_stats(ep_handle* h, ep_stats* out);
+
+/* Conservation sums of the current state, in FP64 with fixed-order reductions (the same state
+ * gives the same bits).  Point sums use the masses ρΩ of the scatter (p2n.jl:71-75) and the
+ * velocities after G2P (n2p.jl:14-40); node sums are the last step's P2G mass and the nodal
+ * momentum the step left (the mUSL momentum with musl, augm.jl:13-25).  The elastic energy is
+ * ½ τ·Del⁻¹τ per unit reference volume times Ω0 in finite strain (Kirchhoff τ with the log strain
+ * it came from), ½ σ·Del⁻¹σ times Ω in infinitesimal strain.  The reference has no such sums; its
+ * tests check mass conservation of the P2G (test/testset). */
+typedef struct ep_conservation {
+    double mass;               /* Σ_p ρ_p Ω_p */
+    double momentum[3];        /* Σ_p ρ_p Ω_p v_p */
+    double kinetic;            /* ½ Σ_p ρ_p Ω_p |v_p|² */
+    double elastic;            /* Σ_p ½ τ·Del⁻¹τ Ω0 (finite) | ½ σ·Del⁻¹σ Ω (infinitesimal) */
+    double mass_nodes;         /* Σ_n m_n of the last step */
+    double momentum_nodes[3];  /* Σ_n p_n of the last step */
+} ep_conservation;
+
+ep_status epgpu_conservation(ep_handle* h, ep_conservation* out);
 
 /* Per-kernel CUDA-event timers for epgpu_step (the reference only measures whole
  * kernel groups with BenchmarkTools, test/testset/test_performance.jl:1-58).

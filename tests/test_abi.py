@@ -78,7 +78,7 @@ def test_struct_layouts_match_the_header(tmp_path):
     if gcc is None:
         pytest.skip("gcc not found")
     structs = [abi.ep_cfg, abi.ep_cmpr, abi.ep_mesh_view, abi.ep_mesh_fields, abi.ep_mpts_view, abi.ep_grf,
-               abi.ep_kernel_time, abi.ep_stats]
+               abi.ep_kernel_time, abi.ep_stats, abi.ep_conservation]
     lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "epgpu.h"', "int main(void) {"]
     for S in structs:
         n = S.__name__
@@ -102,3 +102,20 @@ def test_struct_layouts_match_the_header(tmp_path):
             if got[(n, f)] != off:
                 bad.append((n, f, got[(n, f)], off))
     assert not bad, bad
+
+
+def test_field_mask_bits_match_the_header():
+    """EP_MPTS_* of include/epgpu.h against the Python mirror (epgpu/abi.py MPTS_BITS), which follows
+    the order of the ep_mpts_view arrays."""
+    from epgpu import abi
+    src = open(os.path.join(ROOT, "include", "epgpu.h")).read()
+    bits = {n: 1 << int(k) for n, k in re.findall(r"#define EP_MPTS_(\w+)\s+\(1ull << (\d+)\)", src)}
+    names = {"X": "x", "L0": "l0", "L": "l", "N0": "n0", "N": "n", "OMEGA0": "Omega0", "OMEGA": "Omega",
+             "DJ": "dJ", "J": "J", "U": "u", "V": "v", "P": "p", "RHO0": "rho0", "RHO": "rho", "C0": "c0",
+             "CR": "cr", "PHI": "phi", "DLAM": "dlam", "EPII": "epII", "EPV": "epV", "SIG": "sig", "TAU": "tau",
+             "DVIJ": "dvij", "DUIJ": "duij", "DFIJ": "dFij", "FIJ": "Fij", "BIJ": "bij", "EIJ": "eij", "WIJ": "wij",
+             "SJIJ": "sJij", "APIC_B": "Bij", "APIC_D": "Dij"}
+    assert len(bits) == 32
+    assert {names[k]: v for k, v in bits.items()} == abi.MPTS_BITS
+    fields = [f for f, _ in abi.ep_mpts_view._fields_ if f not in ("ndim", "nmp", "vmax", "p2e", "p2n")]
+    assert fields == list(abi.MPTS_BITS)

@@ -1,0 +1,72 @@
+"""How well the reference's own FP64 result is determined on the 3d slump lattices, measured with the
+oracle alone (no GPU): the relative change of the stress when every position moves by eps h (uniform
+noise).
+
+On the config-3 / config-5 lattice as the reference builds it (GIMP, ghost nodes, l = h/4, grid damping
+on) the points sit on GIMP support edges: a node at distance h + l - r from a point gets a mass ~ r^2, a
+force ~ r and an acceleration ~ 1/r, and its share of the velocity gradient stays O(1) as r -> 0, with r
+itself rounding noise (ghost padding moves node coordinates by an ulp).  The FP64 stress then moves by
+4e-2 - 6e-2 under a 1e-12 h perturbation, so no other arithmetic can be held closer to it than that;
+the GPU tests (tests/test_gpu_mixed3.py) hold the mixed step to a small multiple of this spread.  With
+the lattice moved 1e-2 h off the edges the same perturbation moves the stress by less than 1e-6.
+"""
+import copy
+
+import numpy as np
+import pytest
+
+C1_3D = ([64.1584, 16.0396, 16.0396], [16, 4, 4])
+J2 = {"plast": {"status": True, "constitutive": "J2"}}
+C3 = (dict(basis={"which": "gimpm", "how": "undeformed", "ghost": True},
+           fwrk={"deform": "infinitesimal", "trsfr": "tpic", "C_pf": 0.0, "musl": False, "locking": False,
+                 "damping": 0.1}, **J2), {"c0": 5.0e4, "Hp": 1.0e5}, ((0, 0.3), (1, 0.5)))
+C5 = (dict(basis={"which": "gimpm", "how": "undeformed", "ghost": True},
+           fwrk={"deform": "finite", "trsfr": "tpic", "C_pf": 0.0, "musl": False, "locking": False,
+                 "damping": 0.1}),
+      {"E": 1.0e7, "rho0": 2000.0, "phi0": np.radians(25.0), "phir": np.radians(25.0)}, ((0, 2.0), (1, 3.0)))
+CASES = {"config3": C3, "config5": C5}
+
+
+def lattice(case, shift=0.0):
+    from epgpu import ic_slump
+    kw, over, windows = CASES[case]
+    ic, cfg = ic_slump(*C1_3D, cmpr_over=over, nonloc={"status": False, "ls": 0.5}, **copy.deepcopy(kw))
+    if "c0" in over:
+        ic["mpts"].c0[:] = over["c0"]
+    ic["mpts"].x += shift * ic["mesh"].h[0]
+    return ic, cfg, windows
+
+
+def stress_of(m, cfg):
+    return m.tau if cfg["instr"]["fwrk"]["deform"] == "finite" else m.sig
+
+
+def fp64_spread(oracle_mod, case, shift=0.0, eps=1e-12, draws=3, seed=0):
+    """Largest relative stress change of the oracle over `draws` position perturbations of eps h."""
+    ic, cfg, windows = lattice(case, shift)
+
+    def run(m):
+        o = oracle_mod.Oracle({**ic, "mpts": m}, cfg["instr"])
+        t = 0.0
+        for phase, T in windows:
+            t, _ = o.run(phase, T, 10.0, t)
+        return stress_of(o.download(), cfg)
+
+    ref = run(ic["mpts"].copy())
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(draws):
+        m = ic["mpts"].copy()
+        m.x = np.asfortranarray(m.x + rng.uniform(-1, 1, m.x.shape) * eps * ic["mesh"].h[0])
+        out.append(float(np.linalg.norm(run(m) - ref) / np.linalg.norm(ref)))
+    return max(out)
+
+
+@pytest.mark.parametrize("case", list(CASES))
+def test_reference_lattice_is_rounding_driven(oracle_mod, case):
+    on_edges = fp64_spread(oracle_mod, case, 0.0)
+    off_edges = fp64_spread(oracle_mod, case, 1e-2)
+    print(f"{case}: FP64 stress change under a 1e-12 h perturbation: on the support edges {on_edges:.2e}, "
+          f"lattice shifted 1e-2 h {off_edges:.2e}")
+    assert on_edges > 1e-2
+    assert off_edges < 1e-6

@@ -88,16 +88,17 @@ def test_batch_reports_instance_errors():
 
 def test_batch_instances_match_the_oracle(oracle_mod):
     """Instances of a batch against the FP64 oracle directly: the 591-point c1 slump and the largest
-    instance the batched ensemble draws (nel = [320, 80], 3x3 points per cell: 91,344 points), each
-    with its own friction angle and seeded cohesion field, on the phase kernels over all instances.
-    Bounds: the mixed-precision targets, stress 1e-5 and displacement 1e-4 relative."""
+    instance the batched ensemble keeps (nel = [319, 79], 3x3 points per cell: 89,725 points; the
+    ensemble draws nel_x up to 320, whose mesh the reference's B-spline classes break, so it is
+    drawn again), each with its own friction angle and seeded cohesion field, on the phase kernels
+    over all instances.  Bounds: the mixed-precision targets, stress 1e-5 and displacement 1e-4."""
     import os
     from epgpu import ic_slump
     from epgpu.batch import Batch, bspline_invalid_nodes
     from test_gpu_mixed import errors
     inst = []
     fw = {"deform": "finite", "trsfr": "std", "C_pf": 1.0, "musl": True, "locking": True, "damping": 0.1}
-    for k, (nx, ni, phi) in enumerate(((40, 2, 20.0), (320, 3, 30.0))):
+    for k, (nx, ni, phi) in enumerate(((40, 2, 20.0), (319, 3, 30.0))):
         grf = {"status": True, "covariance": "exponential",
                "param": {"Ix": [5.0, 5.0], "mean": 2.0e4, "cov": 0.3, "min": 1.0e3, "seed": 1000 + k}}
         ic, cfg = ic_slump([64.1584, 16.0396], [nx, nx // 4], ni=ni, cmpr_over={"phi0": math.radians(phi)},
@@ -106,7 +107,7 @@ def test_batch_instances_match_the_oracle(oracle_mod):
         instr = copy.deepcopy(cfg["instr"])
         instr["gpu"] = {"precision": "mixed_df", "jaumann": False}
         inst.append((ic, cfg, instr))
-    assert inst[1][0]["mpts"].nmp == 91344
+    assert inst[1][0]["mpts"].nmp == 89725
     b = Batch([copy.deepcopy(ic) for ic, _, _ in inst], [i for _, _, i in inst])
     assert b.scheme() == "phases"
     windows = ((0, 0.6), (1, 0.9))

@@ -19,7 +19,8 @@ C3_FWRK = {"deform": "infinitesimal", "trsfr": "tpic", "C_pf": 0.0, "musl": Fals
 # gets a mass ~ r^2 and a force ~ r (r: distance to the edge), an acceleration ~ 1/r; there the
 # FP64 result depends on 1e-15-level rounding of r (ghost padding shifts node coordinates by an
 # ulp) that FP32 offsets (~1e-7 h) cannot resolve.  Unshifted, config 3 differs by 1e-1 in stress;
-# shifted by 1e-3 h it agrees to 4e-6 (see test_gimp_support_edges below).
+# shifted by 1e-3 h it agrees to 4e-6; as built, the FP64 result itself moves by 5e-2 under a 1e-12 h
+# perturbation (tests/test_conditioning.py, test_reference_lattice_within_the_fp64_spread below).
 CASES = {
     "config3": (dict(basis={"which": "gimpm", "how": "undeformed", "ghost": True}, fwrk=C3_FWRK, **J2),
                 {"c0": 5.0e4, "Hp": 1.0e5}, 1e-3),
@@ -59,15 +60,35 @@ def _compare(oracle_mod, kw, over, shift, precision):
     return a, b, s, d
 
 
-def test_gimp_support_edges(oracle_mod):
-    # the unshifted config-3 lattice: reported, bounded loosely (the FP64 reference is rounding-driven there)
-    kw, over, _ = CASES["config3"]
-    _, _, s0, d0 = _compare(oracle_mod, kw, over, 0.0, "mixed")
-    _, _, s1, d1 = _compare(oracle_mod, kw, over, 1e-3, "mixed")
-    print(f"config3 GIMP lattice on support edges: stress {s0:.3e} displacement {d0:.3e}; "
-          f"shifted 1e-3 h: stress {s1:.3e} displacement {d1:.3e}")
-    assert s1 < STRESS_TOL and d1 < DISP_TOL
-    assert np.isfinite(s0) and s0 < 0.5
+@pytest.mark.parametrize("precision", ["mixed", "mixed_df"])
+@pytest.mark.parametrize("case", ["config3", "config5"])
+def test_reference_lattice_within_the_fp64_spread(oracle_mod, case, precision):
+    """The config-3 and config-5 lattices as the reference builds them (GIMP with ghost nodes, points on
+    the support edges, grid damping on).  There the FP64 result itself moves by 4e-2 - 6e-2 when the
+    positions move by 1e-12 h (tests/test_conditioning.py), so the mixed step is held to 3x the
+    oracle's own spread over three such perturbations instead of the 1e-5 target."""
+    from epgpu import Engine
+    from test_conditioning import fp64_spread, lattice, stress_of
+    ic, cfg, windows = lattice(case)
+    x0 = ic["mpts"].x.copy()
+    o = oracle_mod.Oracle(copy.deepcopy(ic), cfg["instr"])
+    instr = copy.deepcopy(cfg["instr"])
+    instr["gpu"] = {"precision": precision, "jaumann": False}
+    e = Engine(copy.deepcopy(ic), instr)
+    t = 0.0
+    for phase, T in windows:
+        to, _ = o.run(phase, T, 10.0, t)
+        te, _ = e.run(phase, T, 10.0, t)
+        assert to == te
+        t = te
+    a, b = e.download(), o.download()
+    e.close()
+    s = float(np.linalg.norm(stress_of(a, cfg) - stress_of(b, cfg)) / np.linalg.norm(stress_of(b, cfg)))
+    d = float(np.linalg.norm(a.x - b.x) / max(np.linalg.norm(b.x - x0), 1e-300))
+    spread = fp64_spread(oracle_mod, case)
+    print(f"{case} lattice as built (support edges, damping on) {precision}: stress {s:.3e} displacement {d:.3e}; "
+          f"FP64 spread under 1e-12 h: {spread:.3e} (bound {3 * spread:.2e})")
+    assert s < 3.0 * spread
 
 
 @pytest.mark.parametrize("precision", ["mixed", "mixed_df"])

@@ -52,7 +52,7 @@ def test_gradient_matches_oracle():
         e_bf = _rel(g[o:o + k], gref[o:o + k])
         e_64 = _rel(g[o:o + k], g64[o:o + k])
         print(f"grad {name}: vs BF16 restatement {e_bf:.2e}, vs FP64 {e_64:.2e}")
-        assert e_bf < 1e-4, name
+        assert e_bf < 5e-4, name
         assert e_64 < 6e-2, name
         o += k
 

@@ -70,3 +70,80 @@ def test_pinned_and_pageable_transfers_agree(dim, precision):
         a = got[True][0]
         for k in ("x", "v", "tau", "sig", "Fij", "bij", "c0", "l"):
             assert np.array_equal(getattr(a, k), getattr(ic["mpts"], k)), k
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed_df"])
+@pytest.mark.parametrize("trsfr", ["std", "tpic"])
+def test_masked_transfers_continue_the_run(precision, trsfr):
+    """A host loop that moves only the state a step reads and changes (epgpu_upload_fields /
+    epgpu_download_fields with epgpu_fields_read & epgpu_fields_changed) after a full first upload
+    gives, bit for bit, the run that keeps the state on the device; the constants are not moved again."""
+    from epgpu import Engine, ic_slump
+    fw = {"deform": "finite", "trsfr": trsfr, "C_pf": 0.99, "musl": True, "locking": True, "damping": 0.1}
+    ic, cfg = ic_slump(*C1, fwrk=fw, nonloc={"status": False, "ls": 0.5})
+    instr = copy.deepcopy(cfg["instr"])
+    instr["gpu"] = {"precision": precision, "jaumann": False, "deterministic": precision != "fp64"}
+    g = [0.0, -9.81]
+    ref = Engine(copy.deepcopy(ic), instr)
+    for k in range(6):
+        ref.step(1, 0.02, g)
+    want = ref.download()
+    ref.close()
+    e = Engine(copy.deepcopy(ic), instr)
+    moved = sorted(set(e.fields_read()) & set(e.fields_changed()))
+    assert {"x", "v", "Fij", "bij", "tau", "epII", "dlam"} <= set(moved)
+    assert not {"c0", "cr", "phi", "Omega0", "u", "p"} & set(moved)
+    host = ic["mpts"].copy()
+    for k in range(6):
+        e.upload_fields(host, moved)
+        e.step(1, 0.02, g)
+        e.download_fields(host, moved)
+    for f in moved:
+        assert np.array_equal(getattr(host, f), getattr(want, f)), f
+    e.close()
+
+
+def test_masked_upload_needs_every_field_read_once():
+    import ctypes as C
+    from epgpu import Engine, abi, ic_slump
+    from epgpu.abi import EPError
+    ic, cfg = ic_slump(*C1, nonloc={"status": False, "ls": 0.5})
+    lib = abi.load_library()
+    # a fresh context: a masked upload that leaves out fields the step reads is refused, naming them
+    c, cm, mv = abi.make_cfg(cfg["instr"]), abi.make_cmpr(ic["cmpr"]), abi.MeshView(ic["mesh"])
+    h = C.c_void_p()
+    assert lib.epgpu_create(C.byref(c), C.byref(cm), C.byref(mv.view), ic["mpts"].nmp, C.byref(h)) == 0
+    view = abi.mpts_view(ic["mpts"])
+    assert lib.epgpu_upload_fields(h, C.byref(view), abi.mask_of(["x", "v"])) == 1
+    msg = lib.epgpu_last_error(h).decode()
+    assert "never uploaded" in msg and "Fij" in msg and "c0" in msg
+    assert lib.epgpu_upload_fields(h, C.byref(view), lib.epgpu_fields_read(h)) == 0
+    assert lib.epgpu_upload_fields(h, C.byref(view), abi.mask_of(["x", "v"])) == 0
+    lib.epgpu_destroy(h)
+    # a field named in the mask must be given
+    e = Engine(copy.deepcopy(ic), cfg["instr"])
+    m = ic["mpts"].copy()
+    m.v = None
+    with pytest.raises(EPError) as ex:
+        e.upload_fields(m, ["x", "v"])
+    assert ex.value.status == 1 and "NULL: v" in str(ex.value)
+    e.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed_df"])
+def test_masked_download_writes_only_the_mask(precision):
+    from epgpu import Engine, ic_slump
+    ic, cfg = ic_slump(*C1, nonloc={"status": False, "ls": 0.5})
+    instr = copy.deepcopy(cfg["instr"])
+    if precision != "fp64":
+        instr["gpu"] = {"precision": precision, "jaumann": False}
+    e = Engine(copy.deepcopy(ic), instr)
+    e.step(1, 0.02, [0.0, -9.81])
+    full = e.download()
+    host = ic["mpts"].copy()
+    for f in _fields(host):
+        getattr(host, f)[...] = np.nan
+    e.download_fields(host, ["x", "tau"])
+    assert np.array_equal(host.x, full.x) and np.array_equal(host.tau, full.tau)
+    assert np.isnan(host.v).all() and np.isnan(host.eij).all()
+    e.close()

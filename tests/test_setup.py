@@ -82,3 +82,28 @@ def test_kwargser_top_level_merge():
         config.kwargser({"basis": {"which": "gimpm", "how": None, "ghost": True}})
     with pytest.warns(UserWarning):
         config.kwargser({"nonsense": 1})
+
+
+def test_ensemble_rejects_meshes_whose_bspline_classes_break_the_partition_of_unity():
+    """nel = [320, 80]: the node at xB - h along x is 7e-15 off the rounded xB - h, so the reference's
+    exact comparison (bsmpm.jl:63-76) gives it the interior piece; the weights near that boundary then
+    sum to 1.16 instead of 1 (the restatement oracle/pointmath.py shows it) and the slump moves without
+    load.  The ensemble's mesh check counts that node; nel = [319, 79] is sound."""
+    import pointmath as pm
+    from epgpu.batch import bspline_invalid_nodes
+    for nx, broken in ((320, True), (319, False), (40, False)):
+        ic, _ = ic_slump([64.1584, 16.0396], [nx, nx // 4], ni=2)
+        m = ic["mesh"]
+        xn = np.unique(m.x[0])
+        x0, x1, h = float(m.xB[0, 0]), float(m.xB[0, 1]), float(m.h[0])
+        xp = np.linspace(x0, x1, 4001)[1:-1]
+        e = np.clip(np.floor((xp - x0) / h), 0, xn.size - 2).astype(int)
+        tot = np.zeros_like(xp)
+        for o in (-1, 0, 1, 2):
+            j = e + o
+            ok = (j >= 0) & (j < xn.size)
+            j = np.clip(j, 0, xn.size - 1)
+            w, _ = pm.bspline((xp - xn[j]) / h, xn[j], x0, x1, h)
+            tot += np.where(ok, w, 0.0)
+        assert (np.abs(tot - 1.0).max() > 0.1) == broken, nx
+        assert (bspline_invalid_nodes(m) > 0) == broken, nx
