@@ -113,11 +113,15 @@ ALG_BYTES_FP64_2D = {
 #   cons  read list cellof dx2 F4 b3 ep1 c0 cr tanphi (8-byte F, b, ep1); write F4 b3 ep1 tau3 dlam
 #         nodes: read vm2 dJn
 ALG_BYTES_MIXED_2D = {
+    "zero": (0, 20 + 12),                          # m p2 f2 per node, counts (2 parities) + cursor per cell
     "p2g": (40, 20),
     "solve": (0, 22 + 36),
-    "g2p": (8 + 8 + 8 + 8 + 8 + 4, 16),           # list+cell, offsets, v read; v, next offsets, cell written; (v, a) per node
-    "musl": (8 + 8 + 4 + 8, 8),                    # list+cell, offsets, ρΩ, v read; m v per node
+    # G2P with the mUSL scatter fused (tile form): list+cell, offsets, v, ρΩ read; v, next offsets, cell
+    # written; (v, a) per node read, m v per node added
+    "g2p": (8 + 8 + 8 + 4 + 8 + 8 + 4, 16 + 8),
+    "musl": (8 + 8 + 4 + 8, 8),                    # (separate mUSL scatter) list+cell, offsets, ρΩ, v read
     "vmusl": (0, 22),
+    "vmusl_scan": (0, 22 + 8),                     # mUSL velocity per node; next-step counts -> starts per cell
     "fbar": (20 + 12, 8 + 4),
     "dJn": (0, 12),
     "cons": (4 + 4 + 8 + 32 + 24 + 8 + 12 + 32 + 24 + 8 + 12 + 4, 12),
@@ -635,6 +639,7 @@ def main():
     g = [0.0] * (dim - 1) + [-9.81]
     learned = args.rmap == "learned" and args.precision != "fp64"
     host0 = mpts.copy()
+    x_init = mpts.x.copy()
     e = Engine(ic, cfg["instr"])
     net, train = None, None
     if learned:
@@ -771,7 +776,7 @@ def main():
             for dt in seq:
                 e64.step(1, dt, g)
             b = e64.download()
-            x0 = host0.x
+            x0 = x_init                      # displacement and runout since t = 0 (the slump's own geometry)
             c64 = e64.conservation()
             return {
                 "steps": len(seq),

@@ -464,7 +464,9 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
         const size_t nflt = (size_t)np * (2 * d + d + nsym + 11 + 1 + 2 * d + d * d + (acc ? 2 * nacc : 0));
         ok2 = ok2 && dalloc(h, &pf, nflt) == cudaSuccess;
         int* ints = nullptr;
-        const size_t nint = (size_t)3 * nc + 2 * (size_t)(nc + 1) + 4 * (size_t)np + (size_t)np + 2 * (size_t)(nc + 1) +
+        // step-start zeroed region: counts (2 parities), cursor, sync words, scan status (8-byte words)
+        const size_t nzero = (size_t)3 * nc + 4 + 1 + 2 * (size_t)scan_tiles(nc);
+        const size_t nint = nzero + 2 * (size_t)(nc + 1) + 4 * (size_t)np + (size_t)np + 2 * (size_t)(nc + 1) +
                             (cfg->nonloc ? 2 * (size_t)np : 0);
         ok2 = ok2 && dalloc(h, &ints, nint) == cudaSuccess;
         float* nf = nullptr;
@@ -505,6 +507,12 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
         sm.count[0] = ip; ip += nc;
         sm.count[1] = ip; ip += nc;
         sm.cursor = ip; ip += nc;
+        sm.sync = ip; ip += 4;
+        if ((ip - ints) & 1) ++ip;                       // 8-byte alignment of the status words
+        sm.scan_status = reinterpret_cast<unsigned long long*>(ip);
+        ip += 2 * (size_t)scan_tiles(nc);
+        const size_t zero_ints = (size_t)(ip - sort_zero);
+        ip = sort_zero + nzero;
         sm.start[0] = ip; ip += nc + 1;
         sm.start[1] = ip; ip += nc + 1;
         sm.list[0] = ip; ip += np;
@@ -539,7 +547,7 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
         h->mx.grid_zero = g0;
         h->mx.grid_zero_bytes = sizeof(float) * (size_t)(1 + 2 * d) * nn;   // m, p, f
         h->mx.sort_zero = sort_zero;
-        h->mx.sort_zero_bytes = sizeof(int) * (size_t)3 * nc;
+        h->mx.sort_zero_bytes = sizeof(int) * zero_ints;
         // compliance (inverse of the nstr x nstr Del) for ε = Del \\ τ
         double Cmp[36], LU[36], e[6], x[6];
         int piv[6];

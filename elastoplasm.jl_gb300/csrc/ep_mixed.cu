@@ -478,6 +478,139 @@ __global__ void __launch_bounds__(256) km_g2p_seg(MCtx A) {
 }
 
 
+// km_g2p_tile: G2P (n2p.jl:14-40, tplgy.jl:43-62) fused with the mUSL momentum P2G (augm.jl:13-25)
+// in the tile form of km_p2g_tile.  A CTA owns TC consecutive cells; each thread takes one list slot
+// of the cells' slice at a time (the point's PIC/FLIP update, new position and cell, vmax and
+// next-cell counts exactly as g2p_seg_body) and stages its weights and m v; then the four lanes of a
+// cell add their stencil column's m v over the cell's points, as km_aux_tile<.., 1> does from the
+// stored velocities, and one FP32 atomic per node and component reaches the grid.  Standard and
+// TPIC transfers (APIC's Bᵢⱼ pass and the deterministic mode keep km_g2p_seg).
+constexpr int TG_STRIDE = 11;   // floats per staged point: wx[4], wz[4], m vx, m vz (odd: no bank conflicts)
+
+template <int BASIS, int TC>
+__global__ void __launch_bounds__(4 * TC) km_g2p_tile(MCtx A) {
+    constexpr int NT = 4 * TC;
+    EP_ACTIVE(A.ctl);
+    __shared__ float sp[NT * TG_STRIDE];
+    const int cur = A.ctl->parity, nxt = cur ^ 1;
+    const int c0 = blockIdx.x * TC;
+    if (c0 >= A.g.ncell) return;
+    const int c1 = min(c0 + TC, A.g.ncell);
+    const int* start = A.S.start[cur];
+    const int b0 = start[c0], b1 = start[c1];
+    if (b0 == b1) return;
+    const int t = threadIdx.x, lane = t & 31;
+    const int q = t & 3, cl = c0 + (t >> 2);
+    const bool cell_ok = cl < c1;
+    const int pb = cell_ok ? start[cl] : 0, pe = cell_ok ? start[cl + 1] : 0;
+    const float hx = (float)A.g.h[0], hz = (float)A.g.h[1];
+    const float ihx = 1.f / hx, ihz = 1.f / hz;
+    const float dtf = (float)A.ctl->dt, Cpf = (float)A.cf.Cpf;
+    float acc[4][2];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[j][0] = acc[j][1] = 0.f;
+    unsigned vm0 = 0u, vm1 = 0u;
+    bool bad = false;
+    for (int ch = b0; ch < b1; ch += NT) {
+        const int k = ch + t;
+        int c2 = -1;
+        if (k < b1) {
+            const int p = A.S.list[cur][k], c = A.S.cellof[cur][k];
+            const int ex = c / A.g.nel[1], ez = c - ex * A.g.nel[1];
+            const Axis4 ax = axis4(A.g, 0, ex), az = axis4(A.g, 1, ez);
+            const float dx = A.P.dx[cur][0][p], dz = A.P.dx[cur][1][p];
+            const float lx = BASIS == EP_BASIS_GIMPM ? A.P.l[0][p] : 0.f;
+            const float lz = BASIS == EP_BASIS_GIMPM ? A.P.l[1][p] : 0.f;
+            float wx[4], dwx[4], wz[4], dwz[4];
+            axis_w<BASIS>(ax, dx, hx, ihx, lx, wx, dwx, bad);
+            axis_w<BASIS>(az, dz, hz, ihz, lz, wz, dwz, bad);
+            float vpx = 0.f, vpz = 0.f, afx = 0.f, afz = 0.f;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                if (ax.cls[i] < 0) continue;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    if (az.cls[j] < 0) continue;
+                    const float N = wx[i] * wz[j];
+                    const float4 nv = A.N.va4[node2(A.g, ax, az, i, j)];
+                    vpx += N * nv.x;
+                    vpz += N * nv.y;
+                    afx += N * nv.z;
+                    afz += N * nv.w;
+                }
+            }
+            const float vx = Cpf * (A.P.v[0][p] + dtf * afx) + (1.f - Cpf) * vpx;
+            const float vz = Cpf * (A.P.v[1][p] + dtf * afz) + (1.f - Cpf) * vpz;
+            A.P.v[0][p] = vx;
+            A.P.v[1][p] = vz;
+            vm0 = max(vm0, __float_as_uint(fabsf(vx)));
+            vm1 = max(vm1, __float_as_uint(fabsf(vz)));
+            const float ox = dx + dtf * vpx, oz = dz + dtf * vpz;
+            if (isfinite(ox) && isfinite(oz)) {
+                int ex2, ez2;
+                float o2x, o2z;
+                recell(A.g, 0, ex, ox, ihx, ex2, o2x);
+                recell(A.g, 1, ez, oz, ihz, ez2, o2z);
+                c2 = ez2 + A.g.nel[1] * ex2;
+                A.P.dx[nxt][0][p] = o2x;
+                A.P.dx[nxt][1][p] = o2z;
+            } else {
+                set_err(A.ctl, EP_ERR_NONFINITE, p);
+            }
+            A.P.p2e_next[p] = c2;
+            if (A.P.pcell[nxt]) A.P.pcell[nxt][p] = c2;
+            const float mp = A.P.mp[p];
+            float* st = sp + t * TG_STRIDE;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                st[i] = ax.cls[i] < 0 ? 0.f : wx[i];
+                st[4 + i] = az.cls[i] < 0 ? 0.f : wz[i];
+            }
+            st[8] = mp * vx;
+            st[9] = mp * vz;
+        }
+        {
+            // next-cell counts: one atomic per distinct cell of the warp
+            const unsigned mm = __match_any_sync(0xffffffffu, c2);
+            if (c2 >= 0 && lane == __ffs(mm) - 1) atomicAdd(&A.S.count[nxt][c2], __popc(mm));
+        }
+        __syncthreads();
+        // this lane's cell: the mUSL momentum of its stencil column over the cell's points in the chunk
+        const int lo = max(pb, ch), hi = min(pe, min(ch + NT, b1));
+        for (int kk = lo; kk < hi; ++kk) {
+            const float* st = sp + (kk - ch) * TG_STRIDE;
+            const float wq = st[q];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const float N = wq * st[4 + j];
+                acc[j][0] += N * st[8];
+                acc[j][1] += N * st[9];
+            }
+        }
+        __syncthreads();
+    }
+    if (bad) set_err(A.ctl, EP_ERR_INVALID_POSITION, c0);
+    // vmax over the warp, one atomic per warp (non-negative floats order like their bits)
+    vm0 = __reduce_max_sync(0xffffffffu, vm0);
+    vm1 = __reduce_max_sync(0xffffffffu, vm1);
+    if (lane == 0) {
+        if (vm0) atomicMax(&A.ctl->vmax_bits[0], (unsigned long long)__double_as_longlong((double)__uint_as_float(vm0)));
+        if (vm1) atomicMax(&A.ctl->vmax_bits[1], (unsigned long long)__double_as_longlong((double)__uint_as_float(vm1)));
+    }
+    if (!cell_ok || pb == pe) return;
+    const int ex = cl / A.g.nel[1], ez = cl - ex * A.g.nel[1];
+    const Axis4 ax = axis4(A.g, 0, ex), az = axis4(A.g, 1, ez);
+    if (ax.cls[q] < 0) return;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        if (az.cls[j] < 0) continue;
+        const int n = node2(A.g, ax, az, q, j);
+        atomicAdd(&A.N.pm[0][n], acc[j][0]);
+        atomicAdd(&A.N.pm[1][n], acc[j][1]);
+    }
+}
+
+
 // km_p2g_tile: m, p, f (p2n.jl:135-155 std, 217-240 tpic).  A CTA owns TP_CELLS
 // (16, 32 or 64: the tile shape the autotuner picks) consecutive cells, whose
 // points form one slice of the sorted list.  The slice
@@ -756,10 +889,7 @@ __global__ void km_sort_cells(MCtx A, int which) {
 }
 
 // km_vmusl: mUSL nodal velocity v = p/m with Dirichlet masks (augm.jl:37-53)
-__device__ __forceinline__ void vmusl_body(const MCtx& A, int bid) {
-    EP_ACTIVE(A.ctl);
-    const int n = bid * blockDim.x + threadIdx.x;
-    if (n >= A.g.nnode) return;
+__device__ __forceinline__ void vmusl_one(const MCtx& A, int n) {
     const float m = A.N.m[n];
     float vv[3] = {0.f, 0.f, 0.f};
     for (int d = 0; d < A.g.dim; ++d) {
@@ -769,6 +899,12 @@ __device__ __forceinline__ void vmusl_body(const MCtx& A, int bid) {
         vv[d] = v;
     }
     if (A.g.dim == 2) A.N.vg4[n] = make_float4(vv[0], vv[1], 0.f, 0.f);
+}
+
+__device__ __forceinline__ void vmusl_body(const MCtx& A, int bid) {
+    EP_ACTIVE(A.ctl);
+    const int n = bid * blockDim.x + threadIdx.x;
+    if (n < A.g.nnode) vmusl_one(A, n);
 }
 
 __global__ void km_vmusl(MCtx A) { vmusl_body(A, blockIdx.x); }
@@ -1164,7 +1300,8 @@ __device__ __forceinline__ bool rm_features32(float e11, float e22, float e12, f
 // With the learned return map, a trial-yielding point is handed to the network (its
 // features go to a slot; km_rmap_finish completes it); in record mode the exact map runs
 // and the (features, exact label) pair of the point is appended to the record buffer.
-template <int BASIS, int ACC>
+// FLIP: the last block to finish flips the parity (km_flip's work, one launch less per step)
+template <int BASIS, int ACC, bool FLIP = false>
 __device__ __forceinline__ void cons_body(const MCtx& A, int bid, int plastic_phase) {
     EP_ACTIVE(A.ctl);
     const int cur = A.ctl->parity, nxt = cur ^ 1;
@@ -1413,11 +1550,18 @@ __device__ __forceinline__ void cons_body(const MCtx& A, int bid, int plastic_ph
     // plastic point count: one atomic per warp
     const int tot = __reduce_add_sync(0xffffffffu, nplastic);
     if ((threadIdx.x & 31) == 0 && tot) atomicAdd((unsigned long long*)&A.ctl->plastic, (unsigned long long)tot);
+    if (FLIP) {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            if (atomicAdd(&A.S.sync[1], 1) == (int)gridDim.x - 1) A.ctl->parity ^= 1;
+        }
+    }
 }
 
-template <int BASIS, int ACC>
+template <int BASIS, int ACC, bool FLIP = false>
 __global__ void __launch_bounds__(256) km_cons(MCtx A, int plastic_phase) {
-    cons_body<BASIS, ACC>(A, blockIdx.x, plastic_phase);
+    cons_body<BASIS, ACC, FLIP>(A, blockIdx.x, plastic_phase);
 }
 
 
@@ -1765,6 +1909,95 @@ __global__ void km_scan_add(MCtx A, int which, const int* bsum) {
     if (i < A.g.ncell) A.S.start[par][i] += bsum[i / MSCAN_CHUNK];
 }
 
+// ---------------------------------------------------------------------------
+// km_zero: the step-start zeroing of the node accumulators (m, p, f) and of the counts, cursor and
+// scan words, as a kernel so that steps past the end of a window (EP_ACTIVE) leave the last step's
+// nodal fields in place for download.
+__global__ void __launch_bounds__(256) km_zero(MCtx A, float* g, long long ng, int* z, long long nz) {
+    EP_ACTIVE(A.ctl);
+    const long long i0 = (long long)blockIdx.x * blockDim.x + threadIdx.x, st = (long long)gridDim.x * blockDim.x;
+    for (long long i = i0; i < ng; i += st) g[i] = 0.f;
+    for (long long i = i0; i < nz; i += st) z[i] = 0;
+}
+
+// km_vmusl_scan: in one launch, the mUSL nodal velocity (vmusl_body, blocks past the scan tiles) and
+// the exclusive scan count[nxt] -> start[nxt] (the next step's cell offsets, total at ncell) as a
+// single-pass scan with decoupled look-back: a block takes the next tile by ticket, publishes its
+// aggregate, adds its predecessors' published aggregates until it meets an inclusive prefix, and
+// publishes its own.  Tickets hand tiles out in launch order, so a block only waits for tiles that
+// started before it; every wait is bounded and reports EP_ERR_TIMEOUT if it gives up.
+constexpr unsigned long long SCAN_AGG = 1ull << 32, SCAN_PREFIX = 2ull << 32;
+constexpr int MSCAN2_BS = 512, MSCAN2_IPT = MSCAN_TILE / MSCAN2_BS;
+
+__device__ __forceinline__ unsigned long long ld_status(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__global__ void __launch_bounds__(MSCAN2_BS) km_vmusl_scan(MCtx A, int ntiles) {
+    EP_ACTIVE(A.ctl);
+    if ((int)blockIdx.x >= ntiles) {
+        // the mUSL velocity over MSCAN2_BS nodes per block
+        const int n = (blockIdx.x - ntiles) * MSCAN2_BS + threadIdx.x;
+        if (n < A.g.nnode) vmusl_one(A, n);
+        return;
+    }
+    __shared__ int tile_s, excl_s;
+    const int par = A.ctl->parity ^ 1;
+    const int nc = A.g.ncell;
+    if (threadIdx.x == 0) tile_s = atomicAdd(&A.S.sync[0], 1);
+    __syncthreads();
+    const int tile = tile_s;
+    const int* in = A.S.count[par];
+    int* out = A.S.start[par];
+    const int base = tile * MSCAN_TILE + threadIdx.x * MSCAN2_IPT;
+    int v[MSCAN2_IPT], sum = 0;
+#pragma unroll
+    for (int i = 0; i < MSCAN2_IPT; ++i) {
+        v[i] = base + i < nc ? in[base + i] : 0;
+        sum += v[i];
+    }
+    int agg;
+    const int ex = mblock_scan(sum, &agg);
+    if (threadIdx.x == 0) {
+        unsigned long long* st = A.S.scan_status;
+        int excl = 0;
+        if (tile == 0) {
+            atomicExch(&st[0], SCAN_PREFIX | (unsigned)agg);
+        } else {
+            atomicExch(&st[tile], SCAN_AGG | (unsigned)agg);
+            int j = tile - 1;
+            long long spins = 0;
+            while (j >= 0) {
+                const unsigned long long w = ld_status(&st[j]);
+                const unsigned long long flag = w & 0xffffffff00000000ull;
+                if (flag == 0) {
+                    if (++spins > (1ll << 22)) {          // ~1 s of waiting: give up and report it
+                        set_err(A.ctl, EP_ERR_TIMEOUT, tile);
+                        break;
+                    }
+                    __nanosleep(32);
+                    continue;
+                }
+                excl += (int)(unsigned)(w & 0xffffffffull);
+                if (flag == SCAN_PREFIX) break;
+                --j;
+            }
+            atomicExch(&st[tile], SCAN_PREFIX | (unsigned)(excl + agg));
+        }
+        excl_s = excl;
+        if (tile == ntiles - 1) out[nc] = excl + agg;
+    }
+    __syncthreads();
+    int e = excl_s + ex;
+#pragma unroll
+    for (int i = 0; i < MSCAN2_IPT; ++i) {
+        if (base + i < nc) out[base + i] = e;
+        e += v[i];
+    }
+}
+
 static int mixed_scan(const MCtx& A, int which, int* bsum, cudaStream_t s) {
     const int n = A.g.ncell, nb = (n + MSCAN_CHUNK - 1) / MSCAN_CHUNK;
     km_scan_local<<<nb, MSCAN_BS, 0, s>>>(A, which, bsum);
@@ -1772,6 +2005,35 @@ static int mixed_scan(const MCtx& A, int which, int* bsum, cudaStream_t s) {
     if (nb > 1) km_scan_add<<<(n + 255) / 256, 256, 0, s>>>(A, which, bsum);
     return nb > 1 ? 3 : 2;
 }
+
+// SMs of the current device (grids of the slot kernels, whose counts live on the device)
+static int sm_count() {
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0, v = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess)
+            n = v;
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+// step-start zeroing (km_zero) and the fused mUSL velocity + next-step cell scan (km_vmusl_scan)
+static void launch_zero(const MixedCtx& X, cudaStream_t s) {
+    const MCtx& A = *(const MCtx*)X.impl;
+    const long long ng = (long long)(X.grid_zero_bytes / sizeof(float));
+    const long long nz = (long long)(X.sort_zero_bytes / sizeof(int));
+    const long long mx = ng > nz ? ng : nz;
+    const int nb = (int)std::min<long long>((mx + 255) / 256, 8LL * sm_count());
+    km_zero<<<nb > 0 ? nb : 1, 256, 0, s>>>(A, (float*)X.grid_zero, ng, (int*)X.sort_zero, nz);
+}
+
+static void launch_vmusl_scan(const MCtx& A, bool musl, cudaStream_t s) {
+    const int nt = scan_tiles(A.g.ncell);
+    const int nv = musl ? (A.g.nnode + MSCAN2_BS - 1) / MSCAN2_BS : 0;
+    km_vmusl_scan<<<nt + nv, MSCAN2_BS, 0, s>>>(A, nt);
+}
+
 
 // ---------------------------------------------------------------------------
 // import / export between the FP64 staging layout (P64: the reference's
@@ -3575,18 +3837,6 @@ __global__ void km_batch_flags(const MCtx* ctx, int n, const int* berr, int* fla
     }
 }
 
-// SMs of the current device (grids of the slot kernels, whose counts live on the device)
-static int sm_count() {
-    static int n = 0;
-    if (n == 0) {
-        int dev = 0, v = 0;
-        if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess)
-            n = v;
-        if (n <= 0) n = 1;
-    }
-    return n;
-}
-
 // one 3d step; DET = no floating-point atomics (per-cell partials + node gathers, point-id ordered lists)
 template <int BASIS, int ACC, bool DET>
 static void mixed_step3_impl(const MixedCtx& X, int phase, cudaStream_t s) {
@@ -3599,8 +3849,8 @@ static void mixed_step3_impl(const MixedCtx& X, int phase, cudaStream_t s) {
         if (pr) pr->mark(nm, s);
     };
     long long L = 0;
-    cudaMemsetAsync(X.grid_zero, 0, X.grid_zero_bytes, s);
-    cudaMemsetAsync(X.sort_zero, 0, X.sort_zero_bytes, s);
+    launch_zero(X, s);
+    ++L;
     mark("memset");
     km_p2g_tile3<BASIS, 16, DET><<<gt, 256, 0, s>>>(A);
     if (DET) {
@@ -3621,12 +3871,10 @@ static void mixed_step3_impl(const MixedCtx& X, int phase, cudaStream_t s) {
             mark("musl");
             L += 2;
         }
-        km_vmusl<<<gn, 256, 0, s>>>(A);
-        mark("vmusl");
-        ++L;
     }
-    L += mixed_scan(A, 0, X.scan_in, s);
-    mark("scan");
+    launch_vmusl_scan(A, A.cf.musl, s);
+    mark("vmusl_scan");
+    ++L;
     if (A.cf.locking) {
         km_fbar_seg3<BASIS, DET><<<gs, 256, 0, s>>>(A);
         if (DET) {
@@ -3694,9 +3942,9 @@ static void mixed_step_impl(const MixedCtx& X, int phase, cudaStream_t s) {
         else launch_tile<BASIS, 64, K>(A, s);
     };
     long long L = 0;
-    cudaMemsetAsync(X.grid_zero, 0, X.grid_zero_bytes, s);
-    cudaMemsetAsync(X.sort_zero, 0, X.sort_zero_bytes, s);   // both parities' counts and the cursor
-    mark("memset");
+    launch_zero(X, s);                // node accumulators, both parities' counts, cursor, scan words
+    mark("zero");
+    ++L;
     if (DET) {
         tile(std::integral_constant<int, 0>());
         km_gather<5><<<gn, 256, 0, s>>>(A, A.N.m, A.N.p[0], A.N.p[1], A.N.f[0], A.N.f[1]);
@@ -3707,11 +3955,20 @@ static void mixed_step_impl(const MixedCtx& X, int phase, cudaStream_t s) {
     mark("p2g");
     km_solve<<<gn, 256, 0, s>>>(A);
     mark("solve");
-    if (DET) km_g2p_seg<BASIS, true><<<gs, 256, 0, s>>>(A);
-    else km_g2p_seg<BASIS, false, false><<<gs, 256, 0, s>>>(A);
+    // G2P with the mUSL momentum scatter fused in (tile form), or G2P then a separate mUSL scatter
+    const bool g2p_musl = !DET && A.cf.musl && A.cf.trsfr != EP_TRSFR_APIC;
+    if (g2p_musl) {
+        if (X.p2g_tile == 16) km_g2p_tile<BASIS, 16><<<(nc + 15) / 16, 64, 0, s>>>(A);
+        else if (X.p2g_tile == 32) km_g2p_tile<BASIS, 32><<<(nc + 31) / 32, 128, 0, s>>>(A);
+        else km_g2p_tile<BASIS, 64><<<(nc + 63) / 64, 256, 0, s>>>(A);
+    } else if (DET) {
+        km_g2p_seg<BASIS, true><<<gs, 256, 0, s>>>(A);
+    } else {
+        km_g2p_seg<BASIS, false, false><<<gs, 256, 0, s>>>(A);
+    }
     mark("g2p");
-    L += 3;
-    if (A.cf.musl) {
+    L += 3;                           // P2G, grid update, G2P
+    if (A.cf.musl && !g2p_musl) {
         if (DET) {
             tile(std::integral_constant<int, 1>());
             km_gather<2><<<gn, 256, 0, s>>>(A, A.N.pm[0], A.N.pm[1], nullptr, nullptr, nullptr);
@@ -3725,12 +3982,11 @@ static void mixed_step_impl(const MixedCtx& X, int phase, cudaStream_t s) {
             mark("musl");
             ++L;
         }
-        km_vmusl<<<gn, 256, 0, s>>>(A);
-        mark("vmusl");
-        ++L;
     }
-    L += mixed_scan(A, 0, X.scan_in, s);
-    mark("scan");
+    // the mUSL nodal velocity and the next step's cell offsets in one launch
+    launch_vmusl_scan(A, A.cf.musl, s);
+    mark("vmusl_scan");
+    ++L;
     if (A.cf.locking) {
         km_fbar_seg<BASIS, DET><<<gs, 256, 0, s>>>(A);
         if (DET) {
@@ -3748,11 +4004,16 @@ static void mixed_step_impl(const MixedCtx& X, int phase, cudaStream_t s) {
         mark("nonlocal");
         ++L;
     }
+    const bool net = A.rmode == EP_RMAP_LEARNED && X.net && phase == EP_PHASE_ELASTOPLASTIC;
+    // the parity flip rides on the constitutive kernel's last block unless later kernels of the step
+    // (the network, the deterministic list sort) still read the current parity
+    const bool flip_in_cons = np > 0 && !DET && !net;
     if (np > 0) {
-        km_cons<BASIS, ACC><<<gp, 256, 0, s>>>(A, phase == EP_PHASE_ELASTOPLASTIC);
+        if (flip_in_cons) km_cons<BASIS, ACC, true><<<gp, 256, 0, s>>>(A, phase == EP_PHASE_ELASTOPLASTIC);
+        else km_cons<BASIS, ACC><<<gp, 256, 0, s>>>(A, phase == EP_PHASE_ELASTOPLASTIC);
         mark("cons");
         ++L;
-        if (A.rmode == EP_RMAP_LEARNED && X.net && phase == EP_PHASE_ELASTOPLASTIC) {
+        if (net) {
             mlp_infer(X.net, A.rx, A.rcount, np, A.ry, s);
             mark("mlp");
             km_rmap_finish<ACC><<<std::min(gp, 4 * sm_count()), 256, 0, s>>>(A);
@@ -3765,9 +4026,11 @@ static void mixed_step_impl(const MixedCtx& X, int phase, cudaStream_t s) {
         mark("sort");
         ++L;
     }
-    const bool lrn = A.rmode == EP_RMAP_LEARNED;
-    km_flip<<<1, 1, 0, s>>>(A.ctl, lrn ? A.rcount : nullptr, lrn ? A.fbcount : nullptr);
-    ++L;
+    if (!flip_in_cons) {
+        const bool lrn = A.rmode == EP_RMAP_LEARNED;
+        km_flip<<<1, 1, 0, s>>>(A.ctl, lrn ? A.rcount : nullptr, lrn ? A.fbcount : nullptr);
+        ++L;
+    }
     if (X.launches) *X.launches += L;
 }
 

@@ -55,6 +55,11 @@ struct NM {
     float4* vg4;
 };
 
+// the single-pass scan of the next-step cell counts (km_vmusl_scan): tiles of MSCAN_TILE cells,
+// each publishing its aggregate / inclusive prefix in one 64-bit status word
+constexpr int MSCAN_TILE = 4096;
+inline int scan_tiles(int ncell) { return (ncell + MSCAN_TILE - 1) / MSCAN_TILE; }
+
 struct SM {
     int* count[2];
     int* start[2];     // ncell + 1 each
@@ -62,6 +67,10 @@ struct SM {
     int* cellof[2];    // cell of each list slot
     int* cursor;
     int* scan_tmp;
+    // zeroed with the counts at every step start: [0] the scan's tile ticket, [1] constitutive blocks
+    // done (the last one flips the parity), then one status word per scan tile
+    int* sync;
+    unsigned long long* scan_status;
 };
 
 }  // namespace ep
