@@ -2107,7 +2107,10 @@ __global__ void km_import(MCtx A, P64 Q) {
     A.P.tphi[p] = (float)Q.tphi[p];
     A.P.sphi[p] = (float)Q.sphi[p];
     A.P.cphi[p] = (float)Q.cphi[p];
-    A.P.mp[p] = (float)(Q.rho[p] * Q.Om[p]);
+    // ρΩ: finite strain keeps ρΩ = ρ0Ω0 (deform.jl:1-24), so the mass is formed from the constants
+    // (a resumed state's (ρ0/J)(J Ω0) could round to another FP32 value); infinitesimal strain
+    // carries the current ρ Ω (deform.jl:25-44)
+    A.P.mp[p] = (float)(A.cf.deform == EP_DEFORM_FINITE ? Q.rho0[p] * Q.Om0[p] : Q.rho[p] * Q.Om[p]);
     A.P.Om0[p] = (float)Q.Om0[p];
     A.P.Om[p] = (float)Q.Om[p];
     A.P.rho[p] = (float)Q.rho[p];
@@ -2178,8 +2181,10 @@ __global__ void km_export(MCtx A, P64 Q, int need_eps) {
                             : F[0] * (F[4] * F[8] - F[7] * F[5]) - F[3] * (F[1] * F[8] - F[7] * F[2]) +
                                   F[6] * (F[1] * F[5] - F[4] * F[2]);
     Q.J[p] = J;
-    Q.Om[p] = J * Q.Om0[p];
     const bool fin = A.cf.deform == EP_DEFORM_FINITE;
+    // Ω = J Ω0 (deform.jl:18, 42); infinitesimal strain exports the volume the step carries and uses
+    // (its FP32 J Ω0, which also sets the mass ρΩ), so that a download / upload round trip keeps it
+    Q.Om[p] = fin ? J * Q.Om0[p] : (double)A.P.Om[p];
     if (fin) {
         // finite strain: b, τ, σ = τ / J and ϵ = ½ log b (FP64, for output)
         Q.rho[p] = Q.rho0[p] / J;

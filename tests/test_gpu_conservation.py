@@ -3,8 +3,8 @@ from the oracle's state with exactly rounded summation (math.fsum).
 
 Bounds: the FP64 step's state equals the oracle's bit for bit, so its sums differ only by the order of
 the FP64 additions: 1e-12 relative (mass, energies; momenta relative to Σ|ρΩ v|).  The mixed steps'
-sums follow their state: the point mass ρ0Ω0 is carried exactly (1e-12), kinetic and elastic energy to
-the mixed-precision stress bound 1e-5.  Two calls on the same state give the same bits (fixed-order
+sums follow their state: the point mass ρ0Ω0 to FP32 rounding and the FP32 nodal masses to 1e-6, kinetic
+and elastic energy to the mixed-precision stress bound 1e-5.  Two calls on the same state give the same bits (fixed-order
 reductions).  In finite strain the nodal sums check the transfers themselves: Σ m_n = Σ ρΩ (partition
 of unity, p2n.jl:71-75) and, with mUSL, Σ p_n = Σ ρΩ v (augm.jl:13-25).
 """
@@ -82,7 +82,7 @@ def test_conservation_sums_match_the_oracle(oracle_mod, case, precision):
     if precision == "fp64":
         errs = _compare(got, want, 1e-12, 1e-12, 1e-12)
     else:
-        errs = _compare(got, want, 1e-7, 1e-5, 1e-5)
+        errs = _compare(got, want, 1e-6, 1e-5, 1e-5)       # FP32 nodal masses: Σ m_n to 1e-6
     print(f"conservation {case} {precision}: " + ", ".join(f"{k} {v:.1e}" for k, v in errs.items())
           + f"; mass {got['mass']:.6e} kinetic {got['kinetic']:.4e} elastic {got['elastic']:.4e}")
     # the transfers' own identities in finite strain, where ρΩ = ρ0Ω0 does not change within a step
