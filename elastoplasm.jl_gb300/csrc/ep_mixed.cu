@@ -1002,6 +1002,97 @@ __global__ void __launch_bounds__(256) km_fbar_seg(MCtx A) {
 }
 
 
+// km_fbar_tile: km_fbar_seg in the tile form of km_p2g_tile.  Each thread takes one list slot of
+// the CTA's cells at a time (∇v, δJ and m δJ exactly as fbar_seg_body, and the point's place in the
+// next lists), stages its weights and m δJ, and the four lanes of a cell add Σ N m δJ over the
+// cell's points for their stencil column: one FP32 atomic per node and cell instead of segmented
+// warp sums over the 16 nodes of every point.
+constexpr int TF_STRIDE = 9;    // floats per staged point: wx[4], wz[4], m δJ (odd: no bank conflicts)
+
+template <int BASIS, int TC>
+__global__ void __launch_bounds__(4 * TC) km_fbar_tile(MCtx A) {
+    constexpr int NT = 4 * TC;
+    EP_ACTIVE(A.ctl);
+    __shared__ float sp[NT * TF_STRIDE];
+    const int cur = A.ctl->parity, nxt = cur ^ 1;
+    const int c0 = blockIdx.x * TC;
+    if (c0 >= A.g.ncell) return;
+    const int c1 = min(c0 + TC, A.g.ncell);
+    const int* start = A.S.start[cur];
+    const int b0 = start[c0], b1 = start[c1];
+    if (b0 == b1) return;
+    const int t = threadIdx.x, lane = t & 31;
+    const int q = t & 3, cl = c0 + (t >> 2);
+    const bool cell_ok = cl < c1;
+    const int pb = cell_ok ? start[cl] : 0, pe = cell_ok ? start[cl + 1] : 0;
+    const float hx = (float)A.g.h[0], hz = (float)A.g.h[1];
+    const float dtf = (float)A.ctl->dt;
+    const bool fin = A.cf.deform == EP_DEFORM_FINITE;
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+    bool bad = false;
+    for (int ch = b0; ch < b1; ch += NT) {
+        const int k = ch + t;
+        int p = -1, c2 = -1;
+        if (k < b1) {
+            p = A.S.list[cur][k];
+            const int c = A.S.cellof[cur][k];
+            const int ex = c / A.g.nel[1], ez = c - ex * A.g.nel[1];
+            const Axis4 ax = axis4(A.g, 0, ex), az = axis4(A.g, 1, ez);
+            const float lx = BASIS == EP_BASIS_GIMPM ? A.P.l[0][p] : 0.f;
+            const float lz = BASIS == EP_BASIS_GIMPM ? A.P.l[1][p] : 0.f;
+            float wx[4], dwx[4], wz[4], dwz[4];
+            axis_w<BASIS>(ax, A.P.dx[cur][0][p], hx, 1.f / hx, lx, wx, dwx, bad);
+            axis_w<BASIS>(az, A.P.dx[cur][1][p], hz, 1.f / hz, lz, wz, dwz, bad);
+            float g00 = 0.f, g01 = 0.f, g10 = 0.f, g11 = 0.f;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                if (ax.cls[i] < 0) continue;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    if (az.cls[j] < 0) continue;
+                    const float Nx = dwx[i] * wz[j], Nz = wx[i] * dwz[j];
+                    const float2 vn = *reinterpret_cast<const float2*>(&A.N.vg4[node2(A.g, ax, az, i, j)]);
+                    g00 += Nx * vn.x;
+                    g01 += Nz * vn.x;
+                    g10 += Nx * vn.y;
+                    g11 += Nz * vn.y;
+                }
+            }
+            const float D00 = dtf * g00, D10 = dtf * g10, D01 = dtf * g01, D11 = dtf * g11;
+            const float dJ = D00 + D11 + (D00 * D11 - D01 * D10);
+            // the numerator mass after the deformation update, as fbar_seg_body (volumetric.jl:8)
+            const float mdj = A.P.mp[p] * (fin ? dJ : dJ * (2.f + dJ));
+            float* st = sp + t * TF_STRIDE;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                st[i] = ax.cls[i] < 0 ? 0.f : wx[i];
+                st[4 + i] = az.cls[i] < 0 ? 0.f : wz[i];
+            }
+            st[8] = mdj;
+            c2 = A.P.p2e_next[p];
+        }
+        place_next_warp(A, p, c2, nxt, lane);
+        __syncthreads();
+        const int lo = max(pb, ch), hi = min(pe, min(ch + NT, b1));
+        for (int kk = lo; kk < hi; ++kk) {
+            const float* st = sp + (kk - ch) * TF_STRIDE;
+            const float wq = st[q] * st[8];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc[j] += wq * st[4 + j];
+        }
+        __syncthreads();
+    }
+    if (bad) set_err(A.ctl, EP_ERR_INVALID_POSITION, c0);
+    if (!cell_ok || pb == pe) return;
+    const int ex = cl / A.g.nel[1], ez = cl - ex * A.g.nel[1];
+    const Axis4 ax = axis4(A.g, 0, ex), az = axis4(A.g, 1, ez);
+    if (ax.cls[q] < 0) return;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+        if (az.cls[j] >= 0) atomicAdd(&A.N.dJacc[node2(A.g, ax, az, q, j)], acc[j]);
+}
+
+
 // km_dJn: nodal δJ_n = Σ N m δJ / m_n (volumetric.jl:12-22, increment form)
 __device__ __forceinline__ void dJn_body(const MCtx& A, int bid) {
     EP_ACTIVE(A.ctl);
@@ -3993,7 +4084,10 @@ static void mixed_step_impl(const MixedCtx& X, int phase, cudaStream_t s) {
     mark("vmusl_scan");
     ++L;
     if (A.cf.locking) {
-        km_fbar_seg<BASIS, DET><<<gs, 256, 0, s>>>(A);
+        if (DET) km_fbar_seg<BASIS, true><<<gs, 256, 0, s>>>(A);
+        else if (X.p2g_tile == 16) km_fbar_tile<BASIS, 16><<<(nc + 15) / 16, 64, 0, s>>>(A);
+        else if (X.p2g_tile == 32) km_fbar_tile<BASIS, 32><<<(nc + 31) / 32, 128, 0, s>>>(A);
+        else km_fbar_tile<BASIS, 64><<<(nc + 63) / 64, 256, 0, s>>>(A);
         if (DET) {
             tile(std::integral_constant<int, 2>());
             km_gather<1><<<gn, 256, 0, s>>>(A, A.N.dJacc, nullptr, nullptr, nullptr, nullptr);
