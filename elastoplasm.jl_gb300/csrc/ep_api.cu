@@ -760,8 +760,12 @@ static std::string mask_names(uint64_t k) {
 static uint64_t reads_of(const ep_handle* h) {
     const Cfg& c = h->ctx.cf;
     const bool fin = c.deform == EP_DEFORM_FINITE;
-    uint64_t k = EP_MPTS_X | EP_MPTS_V | EP_MPTS_OMEGA | EP_MPTS_OMEGA0 | EP_MPTS_RHO | EP_MPTS_C0 | EP_MPTS_CR |
-                 EP_MPTS_PHI | EP_MPTS_DLAM | EP_MPTS_EPII | EP_MPTS_FIJ | (fin ? EP_MPTS_TAU | EP_MPTS_BIJ : EP_MPTS_SIG);
+    uint64_t k = EP_MPTS_X | EP_MPTS_V | EP_MPTS_OMEGA0 | EP_MPTS_C0 | EP_MPTS_CR | EP_MPTS_PHI | EP_MPTS_DLAM |
+                 EP_MPTS_EPII | EP_MPTS_FIJ | (fin ? EP_MPTS_TAU | EP_MPTS_BIJ : EP_MPTS_SIG);
+    // the point mass ρΩ: the FP64 step forms it from ρ and Ω; the mixed steps from ρ0Ω0 in finite
+    // strain (which keeps ρΩ = ρ0Ω0) and from the carried ρ and Ω in infinitesimal strain
+    if (!h->mixed || !fin) k |= EP_MPTS_RHO | EP_MPTS_OMEGA;
+    if (h->mixed && fin) k |= EP_MPTS_RHO0;
     if (c.basis == EP_BASIS_GIMPM) k |= EP_MPTS_L | EP_MPTS_L0;
     if (c.trsfr == EP_TRSFR_TPIC) k |= EP_MPTS_DVIJ;
     if (c.trsfr == EP_TRSFR_APIC) k |= EP_MPTS_APIC_B | (h->mixed ? 0ull : EP_MPTS_APIC_D);
@@ -898,11 +902,18 @@ static ep_status build_step_graph(ep_handle* h, int phase) {
     cudaGraph_t gr;
     long long l0 = h->launches;
     CK(h, cudaStreamBeginCapture(h->s, cudaStreamCaptureModeThreadLocal));
-    launch_ctl_begin_step(h->ctl, h->dim, h->s);
-    if (h->mixed) mixed_step(h->mx, phase, h->s);
-    else fp64_step(h->ctx, phase, h->s);
+    if (h->mixed) {
+        // the mixed step's first kernel (km_zero) starts the step itself
+        MixedCtx mx = h->mx;
+        mx.begin_step = 1;
+        mixed_step(mx, phase, h->s);
+    } else {
+        launch_ctl_begin_step(h->ctl, h->dim, h->s);
+        fp64_step(h->ctx, phase, h->s);
+        h->launches += 1;                              // the control kernel
+    }
     cudaError_t e = cudaStreamEndCapture(h->s, &gr);
-    h->step_kernels[phase] = h->launches - l0 + 1;    // + the control kernel
+    h->step_kernels[phase] = h->launches - l0;
     h->launches = l0;
     if (e != cudaSuccess) return cuda_fail(h, e, "step graph capture");
     e = cudaGraphInstantiate(&h->step_graph[phase], gr, 0);
@@ -927,18 +938,21 @@ ep_status epgpu_step(ep_handle* h, int32_t phase, double dt, const double* g, do
         CK(h, cudaGraphLaunch(h->step_graph[phase], h->s));
         h->launches += h->step_kernels[phase];
     } else {
-        launch_ctl_begin_step(h->ctl, h->dim, h->s);
         Fp64Ctx ctx = h->ctx;
         ctx.prof = &h->prof;
+        if (!h->mixed) {
+            launch_ctl_begin_step(h->ctl, h->dim, h->s);
+            h->launches += 1;
+        }
         h->prof.begin(h->s);
         if (h->mixed) {
             MixedCtx mx = h->mx;
             mx.prof = &h->prof;
+            mx.begin_step = 1;
             mixed_step(mx, phase, h->s);
         } else {
             fp64_step(ctx, phase, h->s);
         }
-        h->launches += 1;
     }
     CK(h, cudaEventRecord(h->ev1, h->s));
     CK(h, cudaGetLastError());

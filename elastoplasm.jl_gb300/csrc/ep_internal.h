@@ -105,6 +105,7 @@ struct MixedCtx {
     Prof* prof;
     long long* launches;
     int p2g_tile;             // cells per CTA of the P2G kernel: 16, 32 or 64 (autotuned)
+    int begin_step = 0;       // 1: the step's first kernel also starts the step (k_ctl_begin_step's work)
 };
 size_t mixed_ctx_size();
 // persistent batch kernel over n 2d mixed instances (nullptr + reason when the batch is not eligible)

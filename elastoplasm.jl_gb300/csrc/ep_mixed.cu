@@ -2004,11 +2004,28 @@ __global__ void km_scan_add(MCtx A, int which, const int* bsum) {
 // km_zero: the step-start zeroing of the node accumulators (m, p, f) and of the counts, cursor and
 // scan words, as a kernel so that steps past the end of a window (EP_ACTIVE) leave the last step's
 // nodal fields in place for download.
-__global__ void __launch_bounds__(256) km_zero(MCtx A, float* g, long long ng, int* z, long long nz) {
-    EP_ACTIVE(A.ctl);
+// begin_step = 1: the kernel also starts the step the way k_ctl_begin_step does (active unless an error
+// was raised, vmax and the plastic count reset), so that a one-step graph needs no launch for it; the
+// kernels after it read the control block only once it has finished.  Both regions start 16-byte
+// aligned (their own allocations): 16-byte stores, then the tails.
+__global__ void __launch_bounds__(256) km_zero(MCtx A, float* g, long long ng, int* z, long long nz, int begin_step) {
+    if (begin_step) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            Ctl* c = A.ctl;
+            c->active = c->err ? 0 : 1;
+            for (int i = 0; i < 3; ++i) c->vmax_bits[i] = 0ull;
+            c->plastic = 0;
+        }
+    } else {
+        EP_ACTIVE(A.ctl);
+    }
     const long long i0 = (long long)blockIdx.x * blockDim.x + threadIdx.x, st = (long long)gridDim.x * blockDim.x;
-    for (long long i = i0; i < ng; i += st) g[i] = 0.f;
-    for (long long i = i0; i < nz; i += st) z[i] = 0;
+    const float4 f0 = make_float4(0.f, 0.f, 0.f, 0.f);
+    const int4 z0 = make_int4(0, 0, 0, 0);
+    for (long long i = i0; i < ng / 4; i += st) reinterpret_cast<float4*>(g)[i] = f0;
+    for (long long i = i0; i < nz / 4; i += st) reinterpret_cast<int4*>(z)[i] = z0;
+    if (i0 < (ng & 3)) g[(ng & ~3LL) + i0] = 0.f;
+    if (i0 < (nz & 3)) z[(nz & ~3LL) + i0] = 0;
 }
 
 // km_vmusl_scan: in one launch, the mUSL nodal velocity (vmusl_body, blocks past the scan tiles) and
@@ -2114,9 +2131,9 @@ static void launch_zero(const MixedCtx& X, cudaStream_t s) {
     const MCtx& A = *(const MCtx*)X.impl;
     const long long ng = (long long)(X.grid_zero_bytes / sizeof(float));
     const long long nz = (long long)(X.sort_zero_bytes / sizeof(int));
-    const long long mx = ng > nz ? ng : nz;
-    const int nb = (int)std::min<long long>((mx + 255) / 256, 8LL * sm_count());
-    km_zero<<<nb > 0 ? nb : 1, 256, 0, s>>>(A, (float*)X.grid_zero, ng, (int*)X.sort_zero, nz);
+    const long long mx = (ng > nz ? ng : nz) / 4 + 1;
+    const int nb = (int)std::min<long long>((mx + 255) / 256, 4LL * sm_count());
+    km_zero<<<nb > 0 ? nb : 1, 256, 0, s>>>(A, (float*)X.grid_zero, ng, (int*)X.sort_zero, nz, X.begin_step);
 }
 
 static void launch_vmusl_scan(const MCtx& A, bool musl, cudaStream_t s) {

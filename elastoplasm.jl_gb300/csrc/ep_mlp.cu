@@ -82,10 +82,10 @@ __device__ __forceinline__ bool grp_sync_and(int id, bool v) {
 }
 
 // ---------------------------------------------------------------------------
-// forward, fused over the five layers; one CTA (16 warps) per SM, two groups of 8 warps
-// each walking its own tiles of 128 rows, so that one group's epilogue overlaps the other's
-// MMAs.  Warp w of a group reads TMEM lanes 32 (w % 4) .. + 31 (its rows) and the column
-// half (w % 8) / 4 of every accumulator of its group.
+// forward, fused over the five layers; one CTA (24 warps) per SM, FWD_GROUPS = 3 groups of 8
+// warps each walking its own tiles of 128 rows, so that the groups' epilogues overlap each
+// other's MMAs.  Warp w of a group reads TMEM lanes 32 (w % 4) .. + 31 (its rows) and the
+// column half (w % 8) / 4 of every accumulator of its group.
 struct FwdArgs {
     const float* X;       // rows of RM_NX floats (the first 6 are the inputs)
     int n;                // rows, or (ndev != nullptr) the capacity
@@ -97,28 +97,30 @@ struct FwdArgs {
     int* err;             // set to 1 when a wait times out
 };
 
-// two 128-row tiles in flight per CTA: group g (warps 8g .. 8g + 7) owns activation buffer FWD_SH + g
-// and input buffer FWD_SX + g, TMEM columns 256 g .. 256 g + 255 and mbarrier 1 + g; the weights
+// FWD_GROUPS 128-row tiles in flight per CTA: group g (warps 8g .. 8g + 7) owns activation buffer
+// FWD_SH + g and input buffer FWD_SX + g, the hidden-layer accumulator in TMEM columns 128 g ..
+// 128 g + 127, the output accumulator in columns 384 + 32 g .. + 15, and mbarrier 1 + g; the weights
 // are shared
-constexpr int FWD_SH = 0, FWD_SX = FWD_SH + 2 * MT * W * 2, FWD_SW = FWD_SX + 2 * MT * KIN * 2;
-constexpr int FWD_BAR = FWD_SW + IMG_BYTES, FWD_SMEM = FWD_BAR + 32;
+constexpr int FWD_GROUPS = 3;
+constexpr int FWD_SH = 0, FWD_SX = FWD_SH + FWD_GROUPS * MT * W * 2, FWD_SW = FWD_SX + FWD_GROUPS * MT * KIN * 2;
+constexpr int FWD_BAR = FWD_SW + IMG_BYTES, FWD_SMEM = FWD_BAR + 48;
 static_assert(FWD_SW % 128 == 0 && FWD_BAR % 8 == 0, "shared layout alignment");
+static_assert(FWD_SMEM <= 232448, "shared memory of one CTA");
+static_assert(128 * FWD_GROUPS <= 384 && 384 + 32 * FWD_GROUPS <= 512, "TMEM columns of the groups");
 
-constexpr int FWD_THREADS = 512;
+constexpr int FWD_THREADS = 256 * FWD_GROUPS;
 
 __global__ void __launch_bounds__(FWD_THREADS, 1) km_mlp_fwd(FwdArgs a) {
     extern __shared__ __align__(128) uint8_t sm[];
     uint8_t* sW = sm + FWD_SW;
     uint64_t* bar = reinterpret_cast<uint64_t*>(sm + FWD_BAR);       // [0] weights, [1 + g] group g's MMAs
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + FWD_BAR + 24);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + FWD_BAR + 8 * (1 + FWD_GROUPS));
     const int n = a.ndev ? min(*a.ndev, a.n) : a.n;
     const int ntiles = (n + MT - 1) / MT;
-    if (2 * (int)blockIdx.x >= ntiles) return;              // the whole CTA, before any shared state
+    if (FWD_GROUPS * (int)blockIdx.x >= ntiles) return;     // the whole CTA, before any shared state
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (tid == 0) {
-        tc::mbar_init(&bar[0], 1);
-        tc::mbar_init(&bar[1], 1);
-        tc::mbar_init(&bar[2], 1);
+        for (int i = 0; i <= FWD_GROUPS; ++i) tc::mbar_init(&bar[i], 1);
         tc::mbar_fence_init();
     }
     if (warp == 0) {
@@ -144,7 +146,8 @@ __global__ void __launch_bounds__(FWD_THREADS, 1) km_mlp_fwd(FwdArgs a) {
     uint8_t* sH = sm + FWD_SH + g * (MT * W * 2);
     uint8_t* sX = sm + FWD_SX + g * (MT * KIN * 2);
     uint64_t* gbar = &bar[1 + g];
-    const uint32_t tbase = tall + (uint32_t)(256 * g);
+    const uint32_t tbase = tall + (uint32_t)(128 * g);             // hidden layers
+    const uint32_t tout = tall + (uint32_t)(384 + 32 * g);         // output layer
     const float* bias = reinterpret_cast<const float*>(sW + IBIAS);
     const uint32_t aX = tc::smem_u32(sX), aH = tc::smem_u32(sH), aW = tc::smem_u32(sW);
     const uint32_t id128 = tc::idesc_bf16(MT, W), id16 = tc::idesc_bf16(MT, NO);
@@ -152,7 +155,7 @@ __global__ void __launch_bounds__(FWD_THREADS, 1) km_mlp_fwd(FwdArgs a) {
     const int row = 32 * q + lane;
     const uint32_t trow = tbase + ((uint32_t)(32 * q) << 16);
     uint32_t ph = 0;
-    for (int tile = 2 * blockIdx.x + g; ok && tile < ntiles; tile += 2 * gridDim.x) {
+    for (int tile = FWD_GROUPS * blockIdx.x + g; ok && tile < ntiles; tile += FWD_GROUPS * gridDim.x) {
         const int r0 = tile * MT;
         if (gt < MT) {
             const int r = r0 + gt;
@@ -229,7 +232,7 @@ __global__ void __launch_bounds__(FWD_THREADS, 1) km_mlp_fwd(FwdArgs a) {
                 const bool last = l == 4;
                 const uint32_t wl = last ? aW + IW5 : aW + IW2 + (uint32_t)(l - 1) * (W * W * 2);
                 for (int kc = 0; kc < W / 16; ++kc)
-                    tc::mma_bf16(last ? tbase + W : tbase, tc::sdesc(aH + 256u * kc, 128, 2048),
+                    tc::mma_bf16(last ? tout : tbase, tc::sdesc(aH + 256u * kc, 128, 2048),
                                  tc::sdesc(wl + 256u * kc, 128, 2048), last ? id16 : id128, kc > 0);
                 tc::mma_commit(gbar);
             }
@@ -242,7 +245,7 @@ __global__ void __launch_bounds__(FWD_THREADS, 1) km_mlp_fwd(FwdArgs a) {
         tc::fence_after_sync();
         if (ch == 0) {
             float v[16];
-            tc::tmem_ld16(trow + W, v);
+            tc::tmem_ld16(tout + ((uint32_t)(32 * q) << 16), v);
             const int r = r0 + row;
             if (r < n) {
                 const float* b5 = bias + 4 * W;
@@ -671,7 +674,7 @@ static void mlp_fwd_launch(ep_mlp* m, const float* X, int n, const int* ndev, fl
     a.Zst = train ? m->d.Z : nullptr;
     a.err = m->d.err;
     const int tiles = (n + MT - 1) / MT;
-    const int grid = ndev ? m->sms : std::max(1, std::min((tiles + 1) / 2, m->sms));   // 2 tiles in flight per CTA
+    const int grid = ndev ? m->sms : std::max(1, std::min((tiles + FWD_GROUPS - 1) / FWD_GROUPS, m->sms));
     km_mlp_fwd<<<grid, FWD_THREADS, FWD_SMEM, s>>>(a);
 }
 

@@ -92,9 +92,11 @@ def test_batch_instances_match_the_oracle(oracle_mod):
     ensemble draws nel_x up to 320, whose mesh the reference's B-spline classes break, so it is
     drawn again), each with its own friction angle and seeded cohesion field, on the phase kernels
     over all instances, for 0.6 s of elastic and 0.3 s of plastic flow (about 200 steps of the large
-    instance).  Bounds: stress 3e-5 (measured 7.6e-6 and 1.6e-5 in two runs: the FP32 atomics sum in a
-    varying order, and the error grows with the length of the run as in the c1 all-in-one run) and
-    displacement 1e-4; the 1e-5 stress target is held on short windows (tests/test_gpu_c2.py)."""
+    instance).  Softening is off here (Hp = 0): with it the reference's own FP64 run branches under
+    FP32-level rounding noise (tests/test_conditioning.py shows it on the c1 slump; on this instance
+    three runs of the batch gave 7.6e-6, 1.6e-5 and 1.7e-4 against the oracle), so the comparison would
+    measure the branch taken rather than the batch.  Bounds: the mixed-precision targets, stress 1e-5
+    and displacement 1e-4."""
     import os
     from epgpu import ic_slump
     from epgpu.batch import Batch, bspline_invalid_nodes
@@ -104,7 +106,7 @@ def test_batch_instances_match_the_oracle(oracle_mod):
     for k, (nx, ni, phi) in enumerate(((40, 2, 20.0), (319, 3, 30.0))):
         grf = {"status": True, "covariance": "exponential",
                "param": {"Ix": [5.0, 5.0], "mean": 2.0e4, "cov": 0.3, "min": 1.0e3, "seed": 1000 + k}}
-        ic, cfg = ic_slump([64.1584, 16.0396], [nx, nx // 4], ni=ni, cmpr_over={"phi0": math.radians(phi)},
+        ic, cfg = ic_slump([64.1584, 16.0396], [nx, nx // 4], ni=ni, cmpr_over={"phi0": math.radians(phi), "Hp": 0.0},
                            fwrk=fw, nonloc={"status": False, "ls": 0.5}, grf=grf)
         assert bspline_invalid_nodes(ic["mesh"]) == 0
         instr = copy.deepcopy(cfg["instr"])
@@ -128,4 +130,4 @@ def test_batch_instances_match_the_oracle(oracle_mod):
         s, d, r = errors(b.download(k), ref, ic["mpts"].x)
         print(f"batch instance {k} ({ic['mpts'].nmp} points) vs oracle: stress {s:.2e} displacement {d:.2e} "
               f"runout {r:.2e}, plastic {int((ref.dlam != 0).sum())}")
-        assert s <= 3e-5 and d <= 1e-4
+        assert s <= 1e-5 and d <= 1e-4
