@@ -1695,7 +1695,8 @@ __device__ __noinline__ void rmap_fallback_slot(const MCtx& A, int i) {
 // the trial lies on the compressive side of the apex, the returned stress is on the yield
 // surface and keeps the trial mean stress (both within 1e-3 c), the principal order is
 // kept and Δλ >= 0; the other slots go to the exact FP64 return (DP.jl:33-66)
-template <int ACC>
+// FLIP: the last block to finish does km_flip's work (parity flip, slot counters emptied)
+template <int ACC, bool FLIP = false>
 __global__ void __launch_bounds__(256) km_rmap_finish(MCtx A) {
     EP_ACTIVE(A.ctl);
     const int n = *A.rcount;
@@ -1769,6 +1770,17 @@ __global__ void __launch_bounds__(256) km_rmap_finish(MCtx A) {
     const int tl = __reduce_add_sync(0xffffffffu, nl), tf = __reduce_add_sync(0xffffffffu, nf);
     if ((threadIdx.x & 31) == 0 && tl) atomicAdd(&A.ctl->rm_learned, (unsigned long long)tl);
     if ((threadIdx.x & 31) == 0 && tf) atomicAdd(&A.ctl->rm_fallback, (unsigned long long)tf);
+    if (FLIP) {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            if (atomicAdd(&A.S.sync[2], 1) == (int)gridDim.x - 1) {
+                A.ctl->parity ^= 1;
+                *A.rcount = 0;
+                if (A.fbcount) *A.fbcount = 0;
+            }
+        }
+    }
 }
 
 __global__ void km_flip(Ctl* ctl, int* rcount, int* fbcount) {
@@ -4124,6 +4136,7 @@ static void mixed_step_impl(const MixedCtx& X, int phase, cudaStream_t s) {
     // the parity flip rides on the constitutive kernel's last block unless later kernels of the step
     // (the network, the deterministic list sort) still read the current parity
     const bool flip_in_cons = np > 0 && !DET && !net;
+    const bool flip_in_finish = np > 0 && !DET && net;     // the learned map's finish kernel is last
     if (np > 0) {
         if (flip_in_cons) km_cons<BASIS, ACC, true><<<gp, 256, 0, s>>>(A, phase == EP_PHASE_ELASTOPLASTIC);
         else km_cons<BASIS, ACC><<<gp, 256, 0, s>>>(A, phase == EP_PHASE_ELASTOPLASTIC);
@@ -4132,7 +4145,9 @@ static void mixed_step_impl(const MixedCtx& X, int phase, cudaStream_t s) {
         if (net) {
             mlp_infer(X.net, A.rx, A.rcount, np, A.ry, s);
             mark("mlp");
-            km_rmap_finish<ACC><<<std::min(gp, 4 * sm_count()), 256, 0, s>>>(A);
+            const int gf = std::min(gp, 4 * sm_count());
+            if (flip_in_finish) km_rmap_finish<ACC, true><<<gf, 256, 0, s>>>(A);
+            else km_rmap_finish<ACC><<<gf, 256, 0, s>>>(A);
             mark("rmap_finish");
             L += 2;
         }
@@ -4142,7 +4157,7 @@ static void mixed_step_impl(const MixedCtx& X, int phase, cudaStream_t s) {
         mark("sort");
         ++L;
     }
-    if (!flip_in_cons) {
+    if (!flip_in_cons && !flip_in_finish) {
         const bool lrn = A.rmode == EP_RMAP_LEARNED;
         km_flip<<<1, 1, 0, s>>>(A.ctl, lrn ? A.rcount : nullptr, lrn ? A.fbcount : nullptr);
         ++L;

@@ -72,6 +72,42 @@ def test_reference_lattice_is_rounding_driven(oracle_mod, case):
     assert off_edges < 1e-6
 
 
+def noisy_run(oracle_mod, ic, instr, windows, eps, seed, threads=1, tg=10.0):
+    """The oracle through `windows` [(phase, T), ...] with the reference's CFL dt (physics.jl:21-26) and
+    gravity ramp (physics.jl:60-90), adding after every step a relative perturbation of eps to v and τ
+    and eps h to x (uniform noise from `seed`; eps = 0: the plain run).  Returns the final state."""
+    import ctypes as C
+    from epgpu import abi
+    mesh, cm = ic["mesh"], ic["cmpr"]
+    rng = np.random.default_rng(seed)
+    o = oracle_mod.Oracle(copy.deepcopy(ic), instr, threads=threads)
+    t, vm = 0.0, ic["mpts"].vmax.copy()
+    for phase, T in windows:
+        while t < T:
+            dt = min(0.5 * max(mesh.h[i] / (vm[i] + cm["c"]) for i in range(mesh.dim)), T - t)
+            gz = -9.81 * (min(t / tg, 1.0) if phase == 0 else 1.0)
+            vm = o.step(phase, dt, [0.0] * (mesh.dim - 1) + [gz])
+            t += dt
+            if eps > 0:
+                m = o.download()
+                m.v *= 1 + rng.uniform(-1, 1, m.v.shape) * eps
+                m.tau *= 1 + rng.uniform(-1, 1, m.tau.shape) * eps
+                m.x += rng.uniform(-1, 1, m.x.shape) * eps * mesh.h[0]
+                assert oracle_mod.lib().eporacle_upload(o.h, C.byref(abi.mpts_view(m))) == 0
+    out = o.download()
+    o.close()
+    return out
+
+
+def fp32_noise_spread(oracle_mod, ic, instr, windows, seeds=(1, 2), threads=1):
+    """Largest relative stress change of the oracle when perturbed at the FP32 rounding level (1e-7)
+    after every step: how closely the reference's own FP64 result is determined for arithmetic that
+    rounds like FP32."""
+    ref = noisy_run(oracle_mod, ic, instr, windows, 0.0, 0, threads).tau
+    return max(float(np.linalg.norm(noisy_run(oracle_mod, ic, instr, windows, 1e-7, s, threads).tau - ref)
+                     / np.linalg.norm(ref)) for s in seeds)
+
+
 def test_c1_softening_run_branches_under_fp32_level_noise(oracle_mod):
     """The 591-point c1 slump with softening (Hp = -30 kPa, nonlocal off) over 10 s elastic + 1.5 s
     plastic flow, with a relative perturbation of 1e-7 (the FP32 rounding level) added to x (in units of
@@ -80,31 +116,12 @@ def test_c1_softening_run_branches_under_fp32_level_noise(oracle_mod):
     branch taken differently).  This is the 1e-2 error that some runs of the mixed step with FP32 atomics
     show on this case; a run of the mixed step is held to the smaller outcome only in its deterministic
     mode or by the best of several runs (tests/test_gpu_mixed.py, tests/test_gpu_mlp.py)."""
-    import ctypes as C
-    from epgpu import abi, ic_slump
+    from epgpu import ic_slump
     ic, cfg = ic_slump([64.1584, 64.1584 / 4.0], [40, 10], cmpr_over={"Hp": -3.0e4},
                        nonloc={"status": False, "ls": 0.5})
-    mesh, cm = ic["mesh"], ic["cmpr"]
-
-    def run(eps, seed):
-        rng = np.random.default_rng(seed)
-        o = oracle_mod.Oracle(copy.deepcopy(ic), cfg["instr"])
-        t, vm = 0.0, ic["mpts"].vmax.copy()
-        while t < 11.5:
-            phase = 0 if t < 10.0 else 1
-            T = 10.0 if phase == 0 else 11.5
-            dt = min(0.5 * max(mesh.h[i] / (vm[i] + cm["c"]) for i in range(2)), T - t)   # physics.jl:21-26
-            vm = o.step(phase, dt, [0.0, -9.81 * (t / 10.0 if phase == 0 else 1.0)])
-            t += dt
-            if eps > 0:
-                m = o.download()
-                m.v *= 1 + rng.uniform(-1, 1, m.v.shape) * eps
-                m.tau *= 1 + rng.uniform(-1, 1, m.tau.shape) * eps
-                m.x += rng.uniform(-1, 1, m.x.shape) * eps * mesh.h[0]
-                assert oracle_mod.lib().eporacle_upload(o.h, C.byref(abi.mpts_view(m))) == 0
-        return o.download().tau
-
-    ref = run(0.0, 0)
-    errs = [float(np.linalg.norm(run(1e-7, k) - ref) / np.linalg.norm(ref)) for k in (1, 2, 3, 4)]
+    windows = ((0, 10.0), (1, 11.5))
+    ref = noisy_run(oracle_mod, ic, cfg["instr"], windows, 0.0, 0).tau
+    errs = [float(np.linalg.norm(noisy_run(oracle_mod, ic, cfg["instr"], windows, 1e-7, k).tau - ref)
+                  / np.linalg.norm(ref)) for k in (1, 2, 3, 4)]
     print("FP64 stress after per-step 1e-7 noise, against the unperturbed run:", ", ".join(f"{e:.2e}" for e in errs))
     assert min(errs) < 1e-4 and max(errs) > 5e-3

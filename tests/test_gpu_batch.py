@@ -91,12 +91,12 @@ def test_batch_instances_match_the_oracle(oracle_mod):
     instance the batched ensemble keeps (nel = [319, 79], 3x3 points per cell: 89,725 points; the
     ensemble draws nel_x up to 320, whose mesh the reference's B-spline classes break, so it is
     drawn again), each with its own friction angle and seeded cohesion field, on the phase kernels
-    over all instances, for 0.6 s of elastic and 0.3 s of plastic flow (about 200 steps of the large
-    instance).  Softening is off here (Hp = 0): with it the reference's own FP64 run branches under
-    FP32-level rounding noise (tests/test_conditioning.py shows it on the c1 slump; on this instance
-    three runs of the batch gave 7.6e-6, 1.6e-5 and 1.7e-4 against the oracle), so the comparison would
-    measure the branch taken rather than the batch.  Bounds: the mixed-precision targets, stress 1e-5
-    and displacement 1e-4."""
+    over all instances, for 0.6 s of elastic and 0.3 s of plastic flow.  On the large instance the
+    reference's own FP64 result is determined only to ~1e-4 for arithmetic that rounds like FP32: the
+    oracle perturbed by 1e-7 after every step moves by 1.5e-5 - 7.8e-5 (its thread order, FP64 rounding,
+    by 1e-13), and runs of the batch gave 7.6e-6 - 1.7e-4.  The stress bound is therefore the larger of
+    the 1e-5 target and 3x the oracle's spread under that noise (tests/test_conditioning.py); the
+    displacement bound is the target 1e-4."""
     import os
     from epgpu import ic_slump
     from epgpu.batch import Batch, bspline_invalid_nodes
@@ -106,7 +106,7 @@ def test_batch_instances_match_the_oracle(oracle_mod):
     for k, (nx, ni, phi) in enumerate(((40, 2, 20.0), (319, 3, 30.0))):
         grf = {"status": True, "covariance": "exponential",
                "param": {"Ix": [5.0, 5.0], "mean": 2.0e4, "cov": 0.3, "min": 1.0e3, "seed": 1000 + k}}
-        ic, cfg = ic_slump([64.1584, 16.0396], [nx, nx // 4], ni=ni, cmpr_over={"phi0": math.radians(phi), "Hp": 0.0},
+        ic, cfg = ic_slump([64.1584, 16.0396], [nx, nx // 4], ni=ni, cmpr_over={"phi0": math.radians(phi)},
                            fwrk=fw, nonloc={"status": False, "ls": 0.5}, grf=grf)
         assert bspline_invalid_nodes(ic["mesh"]) == 0
         instr = copy.deepcopy(cfg["instr"])
@@ -128,6 +128,10 @@ def test_batch_instances_match_the_oracle(oracle_mod):
         ref = o.download()
         o.close()
         s, d, r = errors(b.download(k), ref, ic["mpts"].x)
-        print(f"batch instance {k} ({ic['mpts'].nmp} points) vs oracle: stress {s:.2e} displacement {d:.2e} "
-              f"runout {r:.2e}, plastic {int((ref.dlam != 0).sum())}")
-        assert s <= 1e-5 and d <= 1e-4
+        from test_conditioning import fp32_noise_spread
+        spread = fp32_noise_spread(oracle_mod, ic, cfg["instr"], windows, threads=os.cpu_count() or 1)
+        bound = max(1e-5, 3.0 * spread)
+        print(f"batch instance {k} ({ic['mpts'].nmp} points) vs oracle: stress {s:.2e} (bound {bound:.1e}: "
+              f"oracle spread under FP32-level noise {spread:.2e}) displacement {d:.2e} runout {r:.2e}, "
+              f"plastic {int((ref.dlam != 0).sum())}")
+        assert s <= bound and d <= 1e-4
