@@ -446,7 +446,7 @@ def c3_bench(args, rank, ws):
         print(json.dumps(line))
 
 
-def c5_bench(args, rank, ws):
+def c5_bench(args, rank, ws, emit=True):
     """The 3d slump of config 3 with finite-strain Drucker-Prager (phi = 25 deg) and a seeded cohesion
     field: particle-steps/s of the mixed 3d step with the learned return map (pairs of the exact map
     recorded during the settle, the network trained on the GPU), the exact-map step and the FP64 step
@@ -575,8 +575,29 @@ def c5_bench(args, rank, ws):
                                                        max(np.linalg.norm(b.x - host0.x), 1e-300))},
         "clocks": clk.summary(),
     }
-    if rank == 0:
+    if rank == 0 and emit:
         print(json.dumps(line))
+    return line
+
+
+def c5_summary(args, rank, ws):
+    """The learned return map on a reduced config-5 slump (3d finite-strain DP, where the exact return
+    needs an eigen decomposition per point), reported beside the 2d headline: learned, exact-map and
+    FP64 step rates, the fallback rate and the error against the FP64 step."""
+    a = copy.copy(args)
+    a.nel_3d = args.c5_nel
+    a.rmap = "learned"
+    a.steps = min(args.steps, 20)
+    a.warmup = max(min(args.warmup, 5), 3)
+    a.pairs = 8_000_000
+    line = c5_bench(a, rank, ws, emit=False)
+    lr = line["learned_return_map"] or {}
+    return {"workload": line["config"]["workload"], "points": line["config"]["points"],
+            "learned_step": {"value": line["value"], "unit": "particle-steps/s", "ms_per_step": line["ms_per_step"]},
+            "exact_map_step": line["exact_map_step"], "fp64_step": line["fp64_step"],
+            "speedup_vs_exact_map": line["value"] / line["exact_map_step"]["value"] if line["exact_map_step"] else None,
+            "fallback_rate": lr.get("fallback_rate"), "mlp_roofline": lr.get("mlp_roofline"),
+            "error_vs_fp64": line["error_vs_fp64"], "steps": a.steps}
 
 
 def main():
@@ -610,6 +631,9 @@ def main():
                     help="simulated seconds of elastoplastic flow run before timing (plastic points appear)")
     ap.add_argument("--no-other-precision", dest="other_precision", action="store_false",
                     help="skip the exact-map 'mixed' (FP64 islands) step timed beside a mixed_df headline")
+    ap.add_argument("--c5-nel", default="160,40,40",
+                    help="cells of the reduced config-5 slump whose learned-map step is reported beside the 2d "
+                         "headline ('' to skip)")
     ap.add_argument("--clocks-out", default=None,
                     help="folder for the nvidia-smi clock samples (default: a temporary folder)")
     args = ap.parse_args()
@@ -855,6 +879,10 @@ def main():
         val, threads, steps, el = cpu_sample(ic2, cfg2, seconds_budget=args.cpu_seconds)
         cpu = {"value": val, "unit": "particle-steps/s", "cores": threads, "kind": "port",
                "sample": f"{steps} elastoplastic steps of the same workload, FP64 restatement on {threads} threads"}
+    c5 = None
+    if learned and args.c5_nel and args.workload == "c2":
+        e.close()
+        c5 = c5_summary(args, rank, ws)
     if rank == 0:
         rm = None
         if learned:
@@ -879,7 +907,7 @@ def main():
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
             "error_vs_fp64": check, "fp64_step": fp64, "other_precision": other, "conservation": conservation,
             "speedup_vs_fp64_step": (value / fp64["value"]) if fp64 else None,
-            "learned_return_map": rm,
+            "learned_return_map": rm, "c5_learned_reduced": c5,
             "clocks": clk.summary(),
         }
         print(json.dumps(line))
