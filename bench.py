@@ -127,9 +127,9 @@ ALG_BYTES_MIXED_2D = {
     "cons": (4 + 4 + 8 + 32 + 24 + 8 + 12 + 32 + 24 + 8 + 12 + 4, 12),
 }
 # DRAM bytes (read + write) per launch of the mixed_df step kernels on this workload, from one ncu
-# capture of a learned-map step (dram__bytes_read.sum + dram__bytes_write.sum, cold caches; command in
+# capture of an exact-map step (dram__bytes_read.sum + dram__bytes_write.sum, cold caches; command in
 # the profile summary of these kernels): the "traffic" of the roofline entry
-NCU_DRAM_BYTES_MIXED_DF = {"p2g": 17490688, "g2p": 9667328, "musl": 11001344, "fbar": 10071040, "cons": 34376192}
+NCU_DRAM_BYTES_MIXED_DF = {"p2g": 17540096, "g2p": 12216576, "fbar": 10548224, "cons": 59235328}
 # the whole step by the per-point state S and per-node G rule: S = 35 values read or written once
 # (x2 v2 F4 b3 tau3 epII dlam c0 phi Om0 read; x2 v2 F4 b3 tau3 epII dlam written), G = 30 values
 STEP_BYTES = {"fp64": (35 * 8, 30 * 8), "mixed": (35 * 4, 30 * 4), "mixed_df": (35 * 4, 30 * 4)}

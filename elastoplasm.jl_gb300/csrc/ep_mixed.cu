@@ -2043,8 +2043,8 @@ __global__ void __launch_bounds__(256) km_zero(MCtx A, float* g, long long ng, i
 // km_vmusl_scan: in one launch, the mUSL nodal velocity (vmusl_body, blocks past the scan tiles) and
 // the exclusive scan count[nxt] -> start[nxt] (the next step's cell offsets, total at ncell) as a
 // single-pass scan with decoupled look-back: a block takes the next tile by ticket, publishes its
-// aggregate, adds its predecessors' published aggregates until it meets an inclusive prefix, and
-// publishes its own.  Tickets hand tiles out in launch order, so a block only waits for tiles that
+// aggregate, adds its predecessors' published aggregates (32 per round, one warp) until it meets an
+// inclusive prefix, and publishes its own.  Tickets hand tiles out in launch order, so a block only waits for tiles that
 // started before it; every wait is bounded and reports EP_ERR_TIMEOUT if it gives up.
 constexpr unsigned long long SCAN_AGG = 1ull << 32, SCAN_PREFIX = 2ull << 32;
 constexpr int MSCAN2_BS = 512, MSCAN2_IPT = MSCAN_TILE / MSCAN2_BS;
@@ -2080,34 +2080,43 @@ __global__ void __launch_bounds__(MSCAN2_BS) km_vmusl_scan(MCtx A, int ntiles) {
     }
     int agg;
     const int ex = mblock_scan(sum, &agg);
-    if (threadIdx.x == 0) {
+    if (threadIdx.x < 32) {
+        // look-back by the first warp, 32 predecessors per round: lane i reads tile - 1 - i - 32 r; the
+        // nearest published prefix ends the walk, and the aggregates up to it are summed
+        const int lane = threadIdx.x;
         unsigned long long* st = A.S.scan_status;
         int excl = 0;
-        if (tile == 0) {
-            atomicExch(&st[0], SCAN_PREFIX | (unsigned)agg);
-        } else {
-            atomicExch(&st[tile], SCAN_AGG | (unsigned)agg);
-            int j = tile - 1;
-            long long spins = 0;
-            while (j >= 0) {
-                const unsigned long long w = ld_status(&st[j]);
-                const unsigned long long flag = w & 0xffffffff00000000ull;
-                if (flag == 0) {
-                    if (++spins > (1ll << 22)) {          // ~1 s of waiting: give up and report it
-                        set_err(A.ctl, EP_ERR_TIMEOUT, tile);
-                        break;
-                    }
-                    __nanosleep(32);
-                    continue;
+        if (lane == 0) atomicExch(&st[tile], (tile == 0 ? SCAN_PREFIX : SCAN_AGG) | (unsigned)agg);
+        int j0 = tile - 1;
+        long long spins = 0;
+        while (j0 >= 0) {
+            const int j = j0 - lane;
+            const unsigned long long w = j >= 0 ? ld_status(&st[j]) : SCAN_PREFIX;   // before tile 0: prefix 0
+            const unsigned long long flag = w & 0xffffffff00000000ull;
+            const unsigned pre = __ballot_sync(0xffffffffu, flag == SCAN_PREFIX);
+            const unsigned none = __ballot_sync(0xffffffffu, flag == 0);
+            const int first = pre ? __ffs(pre) - 1 : 32;                 // nearest predecessor with a prefix
+            const unsigned need = first < 31 ? (2u << first) - 1u : 0xffffffffu;
+            if (none & need) {
+                if (++spins > (1ll << 22)) {          // ~1 s of waiting: give up and report it
+                    if (lane == 0) set_err(A.ctl, EP_ERR_TIMEOUT, tile);
+                    break;
                 }
-                excl += (int)(unsigned)(w & 0xffffffffull);
-                if (flag == SCAN_PREFIX) break;
-                --j;
+                __nanosleep(32);
+                continue;
             }
-            atomicExch(&st[tile], SCAN_PREFIX | (unsigned)(excl + agg));
+            int v = lane <= first ? (int)(unsigned)(w & 0xffffffffull) : 0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            excl += v;
+            if (first < 32) break;
+            j0 -= 32;
         }
-        excl_s = excl;
-        if (tile == ntiles - 1) out[nc] = excl + agg;
+        if (lane == 0) {
+            if (tile > 0) atomicExch(&st[tile], SCAN_PREFIX | (unsigned)(excl + agg));
+            excl_s = excl;
+            if (tile == ntiles - 1) out[nc] = excl + agg;
+        }
     }
     __syncthreads();
     int e = excl_s + ex;

@@ -79,8 +79,9 @@ def test_masked_transfers_continue_the_run(precision, trsfr):
     epgpu_download_fields with epgpu_fields_read & epgpu_fields_changed) after a full first upload
     gives the run that keeps the state on the device; the constants are not moved again.  Bit for bit
     for the FP64 step and for the mixed step with FP64 accumulators; with double-float accumulators a
-    few points differ by the last bit of the 48-bit pair (measured 1.8e-15 relative in F and b_e after
-    six steps), so that case is held to 1e-12."""
+    few points differ by the last bit of the 48-bit pair (1.8e-15 relative in F and b_e after one step),
+    which can flip the last bit of an FP32 stress later, so that case is held to FP32 resolution
+    (1e-7 of each field's scale)."""
     from epgpu import Engine, ic_slump
     fw = {"deform": "finite", "trsfr": trsfr, "C_pf": 0.99, "musl": True, "locking": True, "damping": 0.1}
     ic, cfg = ic_slump(*C1, fwrk=fw, nonloc={"status": False, "ls": 0.5})
@@ -104,7 +105,7 @@ def test_masked_transfers_continue_the_run(precision, trsfr):
     for f in moved:
         a, b = np.asarray(getattr(host, f)), np.asarray(getattr(want, f))
         if precision == "mixed_df":
-            assert np.abs(a - b).max() <= 1e-12 * max(np.abs(b).max(), 1e-300), f
+            assert np.abs(a - b).max() <= 1e-7 * max(np.abs(b).max(), 1e-300), f
         else:
             assert np.array_equal(a, b), f
     e.close()
