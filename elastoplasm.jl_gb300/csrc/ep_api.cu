@@ -353,6 +353,16 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
         }
         cudaMemcpy(bd, b.data(), b.size(), cudaMemcpyHostToDevice);
         g.bcs = bd;
+        std::vector<int> w((size_t)nnode, 0);
+        for (long long n = 0; n < nnode; ++n)
+            for (int dd = 0; dd < d; ++dd) w[(size_t)n] |= (mesh->bcs[dd + d * n] ? 1 : 0) << dd;
+        int* wd;
+        if (dalloc(h, &wd, w.size()) != cudaSuccess) {
+            epgpu_destroy(h);
+            return fail(nullptr, EP_ERR_NOMEM, "device allocation (bcs)");
+        }
+        cudaMemcpy(wd, w.data(), w.size() * sizeof(int), cudaMemcpyHostToDevice);
+        g.bcw = wd;
     }
     Cfg& cf = h->ctx.cf;
     cf.dim = d; cf.basis = cfg->basis; cf.how = cfg->how; cf.deform = cfg->deform; cf.trsfr = cfg->trsfr;
@@ -531,9 +541,9 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
         nm.m = g0;
         for (int i = 0; i < d; ++i) nm.p[i] = g0 + (size_t)(1 + i) * nn;
         for (int i = 0; i < d; ++i) nm.f[i] = g0 + (size_t)(1 + d + i) * nn;
-        for (int i = 0; i < d; ++i) nm.a[i] = g0 + (size_t)(1 + 2 * d + i) * nn;
-        for (int i = 0; i < d; ++i) nm.v[i] = g0 + (size_t)(1 + 3 * d + i) * nn;
-        for (int i = 0; i < d; ++i) nm.pm[i] = g0 + (size_t)(1 + 4 * d + i) * nn;
+        for (int i = 0; i < d; ++i) nm.pm[i] = g0 + (size_t)(1 + 2 * d + i) * nn;
+        for (int i = 0; i < d; ++i) nm.a[i] = g0 + (size_t)(1 + 3 * d + i) * nn;
+        for (int i = 0; i < d; ++i) nm.v[i] = g0 + (size_t)(1 + 4 * d + i) * nn;
         for (int i = 0; i < d; ++i) nm.vm[i] = g0 + (size_t)(1 + 5 * d + i) * nn;
         nm.dJacc = g0 + (size_t)(1 + 6 * d) * nn;
         nm.dJn = g0 + (size_t)(2 + 6 * d) * nn;
@@ -544,8 +554,13 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
         }
         nm.va4 = pk;
         nm.vg4 = pk ? pk + nn : nullptr;
+        pm.gv = nullptr;
+        if (d == 2 && dalloc(h, &pm.gv, (size_t)(np > 0 ? np : 1)) != cudaSuccess) {
+            epgpu_destroy(h);
+            return fail(nullptr, EP_ERR_NOMEM, "device allocation (per-slot velocity gradients)");
+        }
         h->mx.grid_zero = g0;
-        h->mx.grid_zero_bytes = sizeof(float) * (size_t)(1 + 2 * d) * nn;   // m, p, f
+        h->mx.grid_zero_bytes = sizeof(float) * (size_t)(1 + 3 * d) * nn;   // m, p, f, mUSL p
         h->mx.sort_zero = sort_zero;
         h->mx.sort_zero_bytes = sizeof(int) * zero_ints;
         // compliance (inverse of the nstr x nstr Del) for ε = Del \\ τ

@@ -35,6 +35,7 @@ struct Geo {
     const double* ax[3];          // node coordinates per direction (bit-exact reference values)
     const signed char* cls[3];    // B-spline node class per direction node (ep_scalar.h BS_*)
     const unsigned char* bcs;     // dim x nnode Dirichlet mask, bcs[d*nnode + n]
+    const int* bcw;               // the same mask as one word per node: bit d set = fixed in direction d
     int nnel[3];                  // nonlocal neighbourhood half width (e2e.jl:24)
 };
 

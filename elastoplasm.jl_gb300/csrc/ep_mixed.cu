@@ -39,6 +39,7 @@
 // their columns' sums in registers: one FP32 atomic per node and quantity per cell reaches the grid
 // (or, in the deterministic mode, one store into the cell's node partials).
 #include <climits>
+#include <cstdlib>
 #include <type_traits>
 
 #include "../../include/epgpu.h"
@@ -50,6 +51,17 @@ namespace ep {
 
 #define EP_ACTIVE(ctl) \
     if (!(ctl)->active) return
+
+// Programmatic dependent launch (the kernels of the 2d step, launched by launch_pdl): a kernel may be
+// scheduled while its predecessor in the stream drains.  Each such kernel calls pdl_enter() before
+// its first memory access: griddepcontrol.wait returns once the preceding kernel has completed and
+// its writes are visible, and launch_dependents then lets the following kernel's blocks be
+// scheduled.  Every block executes both, so no kernel of the chain completes before its predecessor.
+// In a kernel launched without the attribute both instructions do nothing.
+__device__ __forceinline__ void pdl_enter() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
 
 // ---------------------------------------------------------------------------
 // FP32 shape pieces (the polynomials of bsmpm.jl:1-62, gimpm.jl:1-14, smpm.jl:1-10)
@@ -237,34 +249,42 @@ __device__ __forceinline__ Quad quad_of(const MCtx& A, int cur) {
 }
 
 // ---------------------------------------------------------------------------
-// km_solve: grid momentum update with damping and Dirichlet masks (solve.jl:14-40), 2d and 3d
+// The grid update of one node (solve.jl:14-40): from its mass m, momentum p and force f, the damped
+// force (f, in place), the acceleration a and the velocity v; a direction with bit d of bc set
+// (Dirichlet) keeps a = v = 0 and its force undamped.  f has three entries (0 beyond D).
+__device__ __forceinline__ void grid_update(int D, float m, const float* p, float* f, int bc, float dt, float eta,
+                                            float* a, float* v) {
+    for (int d = 0; d < 3; ++d) a[d] = v[d] = 0.f;
+    if (m == 0.f) return;
+    const float mi = 1.f / m;
+    for (int d = 0; d < D; ++d) {
+        if ((bc >> d) & 1) continue;
+        // the norm sees the components damped so far (solve.jl:29)
+        const float nrm = sqrtf(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);
+        const float pv = p[d] * mi;
+        const float sg = pv > 0.f ? 1.f : (pv < 0.f ? -1.f : 0.f);
+        if (fabsf(pv) >= 1.0e-3f) f[d] -= eta * nrm * sg;
+        a[d] = f[d] * mi;
+        v[d] = (p[d] + dt * f[d]) * mi;
+    }
+}
+
+// km_solve: the grid update of every node, 2d and 3d.  N.f keeps the undamped P2G force (the
+// export forms the damped one with grid_update); the mUSL accumulators are zeroed for the G2P.
 __device__ __forceinline__ void solve_body(const MCtx& A, int bid) {
     EP_ACTIVE(A.ctl);
     const int n = bid * blockDim.x + threadIdx.x;
     if (n >= A.g.nnode) return;
     const int D = A.g.dim;
-    const float dt = (float)A.ctl->dt, eta = (float)A.cf.damping;
     const float m = A.N.m[n];
-    float a[3] = {0.f, 0.f, 0.f}, v[3] = {0.f, 0.f, 0.f}, f[3] = {0.f, 0.f, 0.f};
+    float a[3], v[3], f[3] = {0.f, 0.f, 0.f}, pn[3] = {0.f, 0.f, 0.f};
     if (m != 0.f) {
-        float pm[3] = {0.f, 0.f, 0.f};
         for (int d = 0; d < D; ++d) {
             f[d] = A.N.f[d][n];
-            pm[d] = A.N.p[d][n];
+            pn[d] = A.N.p[d][n];
         }
-        const float mi = 1.f / m;
-        for (int d = 0; d < D; ++d) {
-            if (A.g.bcs[(size_t)d * A.g.nnode + n]) continue;
-            // the norm sees the components damped so far (solve.jl:29)
-            const float nrm = sqrtf(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);
-            const float pv = pm[d] * mi;
-            const float sg = pv > 0.f ? 1.f : (pv < 0.f ? -1.f : 0.f);
-            if (fabsf(pv) >= 1.0e-3f) f[d] -= eta * nrm * sg;
-            a[d] = f[d] * mi;
-            v[d] = (pm[d] + dt * f[d]) * mi;
-        }
-        for (int d = 0; d < D; ++d) A.N.f[d][n] = f[d];
     }
+    grid_update(D, m, pn, f, A.g.bcw[n], (float)A.ctl->dt, (float)A.cf.damping, a, v);
     for (int d = 0; d < D; ++d) {
         A.N.a[d][n] = a[d];
         A.N.v[d][n] = v[d];
@@ -273,11 +293,14 @@ __device__ __forceinline__ void solve_body(const MCtx& A, int bid) {
     A.N.dJacc[n] = 0.f;
     if (D == 2) {
         A.N.va4[n] = make_float4(v[0], v[1], a[0], a[1]);
-        if (!A.cf.musl) A.N.vg4[n] = make_float4(v[0], v[1], 0.f, 0.f);
+        if (!A.cf.musl) A.N.vg4[n] = make_float4(v[0], v[1], 0.f, m != 0.f ? 1.f / m : 0.f);
     }
 }
 
-__global__ void km_solve(MCtx A) { solve_body(A, blockIdx.x); }
+__global__ void km_solve(MCtx A) {
+    pdl_enter();
+    solve_body(A, blockIdx.x);
+}
 
 
 // new cell and offset along one direction after a move of the offset o
@@ -478,46 +501,224 @@ __global__ void __launch_bounds__(256) km_g2p_seg(MCtx A) {
 }
 
 
-// km_g2p_tile: G2P (n2p.jl:14-40, tplgy.jl:43-62) fused with the mUSL momentum P2G (augm.jl:13-25)
-// in the tile form of km_p2g_tile.  A CTA owns TC consecutive cells; each thread takes one list slot
-// of the cells' slice at a time (the point's PIC/FLIP update, new position and cell, vmax and
-// next-cell counts exactly as g2p_seg_body) and stages its weights and m v; then the four lanes of a
-// cell add their stencil column's m v over the cell's points, as km_aux_tile<.., 1> does from the
-// stored velocities, and one FP32 atomic per node and component reaches the grid.  Standard and
-// TPIC transfers (APIC's Bᵢⱼ pass and the deterministic mode keep km_g2p_seg).
-constexpr int TG_STRIDE = 11;   // floats per staged point: wx[4], wz[4], m vx, m vz (odd: no bank conflicts)
+// ---------------------------------------------------------------------------
+// Shared-memory staging of a tile (the gather kernels km_g2p_tile, km_fbar_tile): a CTA owns the
+// cells [c0, c1); before its first point it stages, per cell, the element indices and the node
+// classes of both stencil axes (one division and eight class reads per cell instead of per point),
+// and the node values its points gather, as a box of x nodes [X0, X0 + NX) by z nodes
+// [Z0, Z0 + NZ): the range's own z extent when it lies in one cell column, whole columns when it
+// spans several.  The box is filled with cp.async (no registers held, nodes outside the grid
+// zero-filled) while the first points' list slots load.  A box above TB_MAX nodes (a range that
+// wraps a column of more than ~200 cells) is not staged: the points then read the node array in
+// place through the same index, with X0 = Z0 = 0 and NZ = nno_z.
+constexpr int TB_MAX = 1024;
 
-template <int BASIS, int TC>
+struct TileBox {
+    int X0, Z0, NZ;
+    bool staged;
+};
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+template <int BYTES>
+__device__ __forceinline__ void cp_async_zfill(void* dst, const void* src, bool valid) {
+    static_assert(BYTES == 4 || BYTES == 8 || BYTES == 16, "cp.async sizes");
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;" ::"r"(smem_addr(dst)), "l"(src), "n"(BYTES),
+                 "r"(valid ? BYTES : 0)
+                 : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
+
+// the box of the cells [c0, c1): x nodes [X0, X0 + NX), z nodes [Z0, Z0 + NZ) (stencils span e-1 .. e+2),
+// staged when it holds at most `limit` nodes
+__host__ __device__ __forceinline__ TileBox tile_box(const Geo& g, int c0, int c1, int& NX, int limit = TB_MAX) {
+    TileBox b;
+    const int n1 = g.nel[1];
+    const int ea = c0 / n1, eb = (c1 - 1) / n1;
+    b.X0 = ea - 1;
+    NX = eb - ea + 4;
+    if (ea == eb) {
+        b.Z0 = c0 - ea * n1 - 1;
+        b.NZ = (c1 - 1 - eb * n1) - (c0 - ea * n1) + 4;
+    } else {
+        b.Z0 = -1;
+        b.NZ = n1 + 3;
+    }
+    b.staged = NX * b.NZ <= limit;
+    if (!b.staged) {
+        b.X0 = 0;
+        b.Z0 = 0;
+        b.NZ = g.nno[1];
+    }
+    return b;
+}
+
+// stage the box of V-sized leading parts of the packed node values src (stride float4)
+template <typename V>
+__device__ __forceinline__ void stage_box(const Geo& g, const float4* src, V* box, const TileBox& b, int NX) {
+    const int n = NX * b.NZ;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        int bx = 0, bz = i;
+        while (bz >= b.NZ) {
+            bz -= b.NZ;
+            ++bx;
+        }
+        const int nx = b.X0 + bx, nz = b.Z0 + bz;
+        const bool ok = nx >= 0 && nx < g.nno[0] && nz >= 0 && nz < g.nno[1];
+        cp_async_zfill<sizeof(V)>(box + i, ok ? (const void*)(src + nz + (size_t)g.nno[1] * nx) : (const void*)src,
+                                  ok);
+    }
+}
+
+// per cell of the range: ex, ez and the classes of the 4 stencil nodes along x and along z
+__device__ __forceinline__ void stage_cells(const Geo& g, int c0, int c1, int4* ci) {
+    for (int i = threadIdx.x; i < c1 - c0; i += blockDim.x) {
+        const int c = c0 + i, ex = c / g.nel[1], ez = c - ex * g.nel[1];
+        const Axis4 ax = axis4(g, 0, ex), az = axis4(g, 1, ez);
+        int px, pz;
+        memcpy(&px, ax.cls, 4);
+        memcpy(&pz, az.cls, 4);
+        ci[i] = make_int4(ex, ez, px, pz);
+    }
+}
+
+__device__ __forceinline__ void cell_axes(const int4& r, Axis4& ax, Axis4& az) {
+    ax.base = r.x - 1;
+    az.base = r.y - 1;
+    memcpy(ax.cls, &r.z, 4);
+    memcpy(az.cls, &r.w, 4);
+}
+
+// box index of stencil node (i, j)
+__device__ __forceinline__ int box_node(const TileBox& b, const Axis4& ax, const Axis4& az, int i, int j) {
+    return (ax.base + i - b.X0) * b.NZ + (az.base + j - b.Z0);
+}
+
+// km_g2p_tile: G2P (n2p.jl:14-40, tplgy.jl:43-62) fused with the mUSL momentum P2G (augm.jl:13-25)
+// in the tile form of km_p2g_tile.  A CTA owns TC consecutive cells and stages their stencil data
+// and the (v, a) box of the grid update; each thread takes one list slot of the cells' slice at a
+// time (the point's PIC/FLIP update, new position and cell, vmax and next-cell counts exactly as
+// g2p_seg_body), with the next slot's list entries already loading, and stages its weights and m v;
+// then the four lanes of a cell add their stencil column's m v over the cell's points, as
+// km_aux_tile<.., 1> does from the stored velocities, and one FP32 atomic per node and component
+// reaches the grid.  Standard and TPIC transfers (APIC's Bᵢⱼ pass and the deterministic mode keep
+// km_g2p_seg).
+// SOLVE: the grid update runs here instead of in km_solve: the box is staged as the P2G's m, p, f
+// and Dirichlet word of each node (cp.async, in the space the point staging uses afterwards) and
+// turned into (v, a) by grid_update; every tile's box must then fit TB_SOLVE nodes (the host checks).
+constexpr int TG_STRIDE = 11;   // floats per staged point: wx[4], wz[4], m vx, m vz (odd: no bank conflicts)
+constexpr int TB_SOLVE = 832;
+
+template <int BASIS, int TC, bool SOLVE = false>
 __global__ void __launch_bounds__(4 * TC) km_g2p_tile(MCtx A) {
     constexpr int NT = 4 * TC;
+    constexpr int NB = SOLVE ? TB_SOLVE : TB_MAX;
+    constexpr int NSP = NT * TG_STRIDE, NRAW = SOLVE ? 6 * TB_SOLVE : 0;
+    pdl_enter();
     EP_ACTIVE(A.ctl);
-    __shared__ float sp[NT * TG_STRIDE];
+    __shared__ __align__(16) float sp[NSP > NRAW ? NSP : NRAW];
+    __shared__ __align__(16) float4 box[NB];
+    __shared__ int4 cinfo[TC];
     const int cur = A.ctl->parity, nxt = cur ^ 1;
     const int c0 = blockIdx.x * TC;
     if (c0 >= A.g.ncell) return;
     const int c1 = min(c0 + TC, A.g.ncell);
     const int* start = A.S.start[cur];
     const int b0 = start[c0], b1 = start[c1];
+    if (SOLVE && A.cf.locking) {
+        // the F-bar pass adds Σ N m δJ into z of the packed node values and km_cons scales it by w:
+        // z = 0 and w = 1/m of the nodes this tile owns (node (ex, ez) of each cell, and the last
+        // node row / column with the last cells), empty tiles included
+        float2* zw = reinterpret_cast<float2*>(A.N.vg4) + 1;
+        for (int i = threadIdx.x; i < c1 - c0; i += NT) {
+            const int c = c0 + i, ex = c / A.g.nel[1], ez = c - ex * A.g.nel[1];
+            const int lx = ex == A.g.nel[0] - 1, lz = ez == A.g.nel[1] - 1;
+            for (int ox = 0; ox <= lx; ++ox)
+                for (int oz = 0; oz <= lz; ++oz) {
+                    const size_t n = (size_t)(ez + oz) + (size_t)A.g.nno[1] * (ex + ox);
+                    const float m = A.N.m[n];
+                    zw[2 * n] = make_float2(0.f, m != 0.f ? 1.f / m : 0.f);
+                }
+        }
+    }
     if (b0 == b1) return;
     const int t = threadIdx.x, lane = t & 31;
     const int q = t & 3, cl = c0 + (t >> 2);
     const bool cell_ok = cl < c1;
+    // the first slot's list entries, then the tile's stencil data and node box
+    int p_n = -1, c_n = -1;
+    if (b0 + t < b1) {
+        p_n = A.S.list[cur][b0 + t];
+        c_n = A.S.cellof[cur][b0 + t];
+    }
     const int pb = cell_ok ? start[cl] : 0, pe = cell_ok ? start[cl + 1] : 0;
+    int NX;
+    const TileBox tb = tile_box(A.g, c0, c1, NX, NB);
+    if (SOLVE && !tb.staged) {            // the host launches SOLVE only when every box fits
+        if (t == 0) set_err(A.ctl, EP_ERR_ARG, c0);
+        return;
+    }
+    const int nbox = NX * tb.NZ;
+    const float dtf = (float)A.ctl->dt, Cpf = (float)A.cf.Cpf;
+    if (SOLVE) {
+        // the P2G fields of the box nodes: raw[q * NB + i], q = m, p_x, p_z, f_x, f_z, Dirichlet word
+        float* raw = sp;
+        const float* fld[5] = {A.N.m, A.N.p[0], A.N.p[1], A.N.f[0], A.N.f[1]};
+        for (int i = t; i < nbox; i += NT) {
+            int bx = 0, bz = i;
+            while (bz >= tb.NZ) {
+                bz -= tb.NZ;
+                ++bx;
+            }
+            const int nx = tb.X0 + bx, nz = tb.Z0 + bz;
+            const bool ok = nx >= 0 && nx < A.g.nno[0] && nz >= 0 && nz < A.g.nno[1];
+            const size_t n = ok ? (size_t)nz + (size_t)A.g.nno[1] * nx : 0;
+#pragma unroll
+            for (int f = 0; f < 5; ++f) cp_async_zfill<4>(raw + f * NB + i, fld[f] + n, ok);
+            cp_async_zfill<4>(raw + 5 * NB + i, A.g.bcw + n, ok);
+        }
+    } else if (tb.staged) {
+        stage_box(A.g, A.N.va4, box, tb, NX);
+    }
+    stage_cells(A.g, c0, c1, cinfo);
+    const float4* vb = (SOLVE || tb.staged) ? box : A.N.va4;
     const float hx = (float)A.g.h[0], hz = (float)A.g.h[1];
     const float ihx = 1.f / hx, ihz = 1.f / hz;
-    const float dtf = (float)A.ctl->dt, Cpf = (float)A.cf.Cpf;
     float acc[4][2];
 #pragma unroll
     for (int j = 0; j < 4; ++j) acc[j][0] = acc[j][1] = 0.f;
     unsigned vm0 = 0u, vm1 = 0u;
     bool bad = false;
+    cp_async_wait_all();
+    __syncthreads();
+    if (SOLVE) {
+        const float eta = (float)A.cf.damping;
+        for (int i = t; i < nbox; i += NT) {
+            const float* raw = sp + i;
+            const float pn[2] = {raw[NB], raw[2 * NB]};
+            float f[3] = {raw[3 * NB], raw[4 * NB], 0.f}, a[3], v[3];
+            grid_update(2, raw[0], pn, f, __float_as_int(raw[5 * NB]), dtf, eta, a, v);
+            box[i] = make_float4(v[0], v[1], a[0], a[1]);
+        }
+        __syncthreads();      // sp now stages points
+    }
     for (int ch = b0; ch < b1; ch += NT) {
         const int k = ch + t;
+        const int p = p_n, c = c_n;
+        p_n = c_n = -1;
+        if (k + NT < b1) {
+            p_n = A.S.list[cur][k + NT];
+            c_n = A.S.cellof[cur][k + NT];
+        }
         int c2 = -1;
         if (k < b1) {
-            const int p = A.S.list[cur][k], c = A.S.cellof[cur][k];
-            const int ex = c / A.g.nel[1], ez = c - ex * A.g.nel[1];
-            const Axis4 ax = axis4(A.g, 0, ex), az = axis4(A.g, 1, ez);
+            Axis4 ax, az;
+            const int4 ci = cinfo[c - c0];
+            cell_axes(ci, ax, az);
+            const int ex = ci.x, ez = ci.y;
             const float dx = A.P.dx[cur][0][p], dz = A.P.dx[cur][1][p];
             const float lx = BASIS == EP_BASIS_GIMPM ? A.P.l[0][p] : 0.f;
             const float lz = BASIS == EP_BASIS_GIMPM ? A.P.l[1][p] : 0.f;
@@ -532,7 +733,7 @@ __global__ void __launch_bounds__(4 * TC) km_g2p_tile(MCtx A) {
                 for (int j = 0; j < 4; ++j) {
                     if (az.cls[j] < 0) continue;
                     const float N = wx[i] * wz[j];
-                    const float4 nv = A.N.va4[node2(A.g, ax, az, i, j)];
+                    const float4 nv = vb[box_node(tb, ax, az, i, j)];
                     vpx += N * nv.x;
                     vpz += N * nv.y;
                     afx += N * nv.z;
@@ -598,8 +799,8 @@ __global__ void __launch_bounds__(4 * TC) km_g2p_tile(MCtx A) {
         if (vm1) atomicMax(&A.ctl->vmax_bits[1], (unsigned long long)__double_as_longlong((double)__uint_as_float(vm1)));
     }
     if (!cell_ok || pb == pe) return;
-    const int ex = cl / A.g.nel[1], ez = cl - ex * A.g.nel[1];
-    const Axis4 ax = axis4(A.g, 0, ex), az = axis4(A.g, 1, ez);
+    Axis4 ax, az;
+    cell_axes(cinfo[cl - c0], ax, az);
     if (ax.cls[q] < 0) return;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
@@ -632,6 +833,7 @@ __device__ __forceinline__ void p2g_tile_body(const MCtx& A, int bid) {
     }
     EP_ACTIVE(A.ctl);
     __shared__ float sp[TP_THREADS * TP_STRIDE];
+    __shared__ int4 cinfo[TP_CELLS];
     const int cur = A.ctl->parity;
     const int c0 = bid * TP_CELLS;
     if (c0 >= A.g.ncell) return;
@@ -642,7 +844,15 @@ __device__ __forceinline__ void p2g_tile_body(const MCtx& A, int bid) {
     const int t = threadIdx.x;
     const int q = t & 3, cl = c0 + (t >> 2);          // this lane's cell and stencil column
     const bool cell_ok = cl < c1;
+    // the first slot's list entries, then the tile's stencil data (as km_g2p_tile)
+    int p_n = -1, c_n = -1;
+    if (b0 + t < b1) {
+        p_n = A.S.list[cur][b0 + t];
+        c_n = A.S.cellof[cur][b0 + t];
+    }
     const int pb = cell_ok ? start[cl] : 0, pe = cell_ok ? start[cl + 1] : 0;
+    __syncthreads();      // a persistent caller's previous tile may still read cinfo
+    stage_cells(A.g, c0, c1, cinfo);
     const float hx = (float)A.g.h[0], hz = (float)A.g.h[1];
     const float gz = (float)A.ctl->g[1];
     const bool fin = A.cf.deform == EP_DEFORM_FINITE;
@@ -651,13 +861,19 @@ __device__ __forceinline__ void p2g_tile_body(const MCtx& A, int bid) {
 #pragma unroll
     for (int j = 0; j < 4; ++j) am[j] = apx[j] = apz[j] = afx[j] = afz[j] = 0.f;
     bool bad = false;
+    __syncthreads();
     for (int ch = b0; ch < b1; ch += TP_THREADS) {
         // stage one point per thread
         const int k = ch + t;
+        const int p = p_n, c = c_n;
+        p_n = c_n = -1;
+        if (k + TP_THREADS < b1) {
+            p_n = A.S.list[cur][k + TP_THREADS];
+            c_n = A.S.cellof[cur][k + TP_THREADS];
+        }
         if (k < b1) {
-            const int p = A.S.list[cur][k], c = A.S.cellof[cur][k];
-            const int ex = c / A.g.nel[1], ez = c - ex * A.g.nel[1];
-            const Axis4 ax = axis4(A.g, 0, ex), az = axis4(A.g, 1, ez);
+            Axis4 ax, az;
+            cell_axes(cinfo[c - c0], ax, az);
             const float dx = A.P.dx[cur][0][p], dz = A.P.dx[cur][1][p];
             const float lx = BASIS == EP_BASIS_GIMPM ? A.P.l[0][p] : 0.f;
             const float lz = BASIS == EP_BASIS_GIMPM ? A.P.l[1][p] : 0.f;
@@ -728,8 +944,8 @@ __device__ __forceinline__ void p2g_tile_body(const MCtx& A, int bid) {
         }
         return;
     }
-    const int ex = cl / A.g.nel[1], ez = cl - ex * A.g.nel[1];
-    const Axis4 ax = axis4(A.g, 0, ex), az = axis4(A.g, 1, ez);
+    Axis4 ax, az;
+    cell_axes(cinfo[cl - c0], ax, az);
     if (ax.cls[q] < 0) return;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
@@ -745,6 +961,7 @@ __device__ __forceinline__ void p2g_tile_body(const MCtx& A, int bid) {
 
 template <int BASIS, int TP_CELLS, bool DET>
 __global__ void __launch_bounds__(4 * TP_CELLS) km_p2g_tile(MCtx A) {
+    pdl_enter();
     p2g_tile_body<BASIS, TP_CELLS, DET>(A, blockIdx.x);
 }
 
@@ -891,14 +1108,15 @@ __global__ void km_sort_cells(MCtx A, int which) {
 // km_vmusl: mUSL nodal velocity v = p/m with Dirichlet masks (augm.jl:37-53)
 __device__ __forceinline__ void vmusl_one(const MCtx& A, int n) {
     const float m = A.N.m[n];
+    const float mi = m != 0.f ? 1.f / m : 0.f;
     float vv[3] = {0.f, 0.f, 0.f};
     for (int d = 0; d < A.g.dim; ++d) {
         float v = 0.f;
-        if (m != 0.f && !A.g.bcs[(size_t)d * A.g.nnode + n]) v = A.N.pm[d][n] * (1.f / m);
+        if (m != 0.f && !A.g.bcs[(size_t)d * A.g.nnode + n]) v = A.N.pm[d][n] * mi;
         A.N.vm[d][n] = v;
         vv[d] = v;
     }
-    if (A.g.dim == 2) A.N.vg4[n] = make_float4(vv[0], vv[1], 0.f, 0.f);
+    if (A.g.dim == 2) A.N.vg4[n] = make_float4(vv[0], vv[1], 0.f, mi);
 }
 
 __device__ __forceinline__ void vmusl_body(const MCtx& A, int bid) {
@@ -973,6 +1191,7 @@ __device__ __forceinline__ void fbar_seg_body(const MCtx& A, int bid) {
                 g11 += Nz * vz;
             }
         }
+        A.P.gv[k] = make_float4(g00, g10, g01, g11);   // km_cons reads the slot's ∇v back
         const float D00 = dtf * g00, D10 = dtf * g10, D01 = dtf * g01, D11 = dtf * g11;
         const float dJ = D00 + D11 + (D00 * D11 - D01 * D10);
         // numerator mass ρΩ after the deformation update: finite ρ0Ω0 (unchanged), infinitesimal
@@ -1002,18 +1221,26 @@ __global__ void __launch_bounds__(256) km_fbar_seg(MCtx A) {
 }
 
 
-// km_fbar_tile: km_fbar_seg in the tile form of km_p2g_tile.  Each thread takes one list slot of
-// the CTA's cells at a time (∇v, δJ and m δJ exactly as fbar_seg_body, and the point's place in the
-// next lists), stages its weights and m δJ, and the four lanes of a cell add Σ N m δJ over the
-// cell's points for their stencil column: one FP32 atomic per node and cell instead of segmented
-// warp sums over the 16 nodes of every point.
+// km_fbar_tile: km_fbar_seg in the tile form of km_p2g_tile, with the tile's stencil data and the
+// velocity box staged as in km_g2p_tile.  Each thread takes one list slot of the CTA's cells at a time
+// (∇v, δJ and m δJ exactly as fbar_seg_body, and the point's place in the next lists), stages its
+// weights and m δJ, and the four lanes of a cell add Σ N m δJ over the cell's points for their
+// stencil column: one FP32 atomic per node and cell instead of segmented warp sums over the 16
+// nodes of every point.
+// VM: the mUSL nodal velocity (augm.jl:37-53, vmusl_one) is formed here from the staged m, mUSL p and
+// Dirichlet word of the box nodes instead of in km_vmusl_scan (the boxes fit TB_SOLVE nodes).
 constexpr int TF_STRIDE = 9;    // floats per staged point: wx[4], wz[4], m δJ (odd: no bank conflicts)
 
-template <int BASIS, int TC>
+template <int BASIS, int TC, bool VM = false>
 __global__ void __launch_bounds__(4 * TC) km_fbar_tile(MCtx A) {
     constexpr int NT = 4 * TC;
+    constexpr int NB = VM ? TB_SOLVE : TB_MAX;
+    constexpr int NSP = NT * TF_STRIDE, NRAW = VM ? 4 * TB_SOLVE : 0;
+    pdl_enter();
     EP_ACTIVE(A.ctl);
-    __shared__ float sp[NT * TF_STRIDE];
+    __shared__ __align__(16) float sp[NSP > NRAW ? NSP : NRAW];
+    __shared__ __align__(16) float2 box[NB];
+    __shared__ int4 cinfo[TC];
     const int cur = A.ctl->parity, nxt = cur ^ 1;
     const int c0 = blockIdx.x * TC;
     if (c0 >= A.g.ncell) return;
@@ -1024,20 +1251,70 @@ __global__ void __launch_bounds__(4 * TC) km_fbar_tile(MCtx A) {
     const int t = threadIdx.x, lane = t & 31;
     const int q = t & 3, cl = c0 + (t >> 2);
     const bool cell_ok = cl < c1;
+    int p_n = -1, c_n = -1;
+    if (b0 + t < b1) {
+        p_n = A.S.list[cur][b0 + t];
+        c_n = A.S.cellof[cur][b0 + t];
+    }
     const int pb = cell_ok ? start[cl] : 0, pe = cell_ok ? start[cl + 1] : 0;
+    int NX;
+    const TileBox tb = tile_box(A.g, c0, c1, NX, NB);
+    if (VM && !tb.staged) {               // the host launches VM only when every box fits
+        if (t == 0) set_err(A.ctl, EP_ERR_ARG, c0);
+        return;
+    }
+    const int nbox = NX * tb.NZ;
+    if (VM) {
+        // raw[q * NB + i], q = m, mUSL p_x, mUSL p_z, Dirichlet word
+        float* raw = sp;
+        const float* fld[3] = {A.N.m, A.N.pm[0], A.N.pm[1]};
+        for (int i = t; i < nbox; i += NT) {
+            int bx = 0, bz = i;
+            while (bz >= tb.NZ) {
+                bz -= tb.NZ;
+                ++bx;
+            }
+            const int nx = tb.X0 + bx, nz = tb.Z0 + bz;
+            const bool ok = nx >= 0 && nx < A.g.nno[0] && nz >= 0 && nz < A.g.nno[1];
+            const size_t n = ok ? (size_t)nz + (size_t)A.g.nno[1] * nx : 0;
+#pragma unroll
+            for (int f = 0; f < 3; ++f) cp_async_zfill<4>(raw + f * NB + i, fld[f] + n, ok);
+            cp_async_zfill<4>(raw + 3 * NB + i, A.g.bcw + n, ok);
+        }
+    } else if (tb.staged) {
+        stage_box(A.g, A.N.vg4, box, tb, NX);
+    }
+    stage_cells(A.g, c0, c1, cinfo);
     const float hx = (float)A.g.h[0], hz = (float)A.g.h[1];
     const float dtf = (float)A.ctl->dt;
     const bool fin = A.cf.deform == EP_DEFORM_FINITE;
     float acc[4] = {0.f, 0.f, 0.f, 0.f};
     bool bad = false;
+    cp_async_wait_all();
+    __syncthreads();
+    if (VM) {
+        for (int i = t; i < nbox; i += NT) {
+            const float m = sp[i];
+            const int bc = __float_as_int(sp[3 * NB + i]);
+            const float mi = m != 0.f ? 1.f / m : 0.f;
+            const float vx = (m != 0.f && !(bc & 1)) ? sp[NB + i] * mi : 0.f;
+            const float vz = (m != 0.f && !(bc & 2)) ? sp[2 * NB + i] * mi : 0.f;
+            box[i] = make_float2(vx, vz);
+        }
+        __syncthreads();      // sp now stages points
+    }
     for (int ch = b0; ch < b1; ch += NT) {
         const int k = ch + t;
-        int p = -1, c2 = -1;
+        const int p = p_n, c = c_n;
+        p_n = c_n = -1;
+        if (k + NT < b1) {
+            p_n = A.S.list[cur][k + NT];
+            c_n = A.S.cellof[cur][k + NT];
+        }
+        int c2 = -1;
         if (k < b1) {
-            p = A.S.list[cur][k];
-            const int c = A.S.cellof[cur][k];
-            const int ex = c / A.g.nel[1], ez = c - ex * A.g.nel[1];
-            const Axis4 ax = axis4(A.g, 0, ex), az = axis4(A.g, 1, ez);
+            Axis4 ax, az;
+            cell_axes(cinfo[c - c0], ax, az);
             const float lx = BASIS == EP_BASIS_GIMPM ? A.P.l[0][p] : 0.f;
             const float lz = BASIS == EP_BASIS_GIMPM ? A.P.l[1][p] : 0.f;
             float wx[4], dwx[4], wz[4], dwz[4];
@@ -1051,13 +1328,16 @@ __global__ void __launch_bounds__(4 * TC) km_fbar_tile(MCtx A) {
                 for (int j = 0; j < 4; ++j) {
                     if (az.cls[j] < 0) continue;
                     const float Nx = dwx[i] * wz[j], Nz = wx[i] * dwz[j];
-                    const float2 vn = *reinterpret_cast<const float2*>(&A.N.vg4[node2(A.g, ax, az, i, j)]);
+                    const float2 vn = (VM || tb.staged)
+                                          ? box[box_node(tb, ax, az, i, j)]
+                                          : *reinterpret_cast<const float2*>(&A.N.vg4[node2(A.g, ax, az, i, j)]);
                     g00 += Nx * vn.x;
                     g01 += Nz * vn.x;
                     g10 += Nx * vn.y;
                     g11 += Nz * vn.y;
                 }
             }
+            A.P.gv[k] = make_float4(g00, g10, g01, g11);
             const float D00 = dtf * g00, D10 = dtf * g10, D01 = dtf * g01, D11 = dtf * g11;
             const float dJ = D00 + D11 + (D00 * D11 - D01 * D10);
             // the numerator mass after the deformation update, as fbar_seg_body (volumetric.jl:8)
@@ -1071,7 +1351,7 @@ __global__ void __launch_bounds__(4 * TC) km_fbar_tile(MCtx A) {
             st[8] = mdj;
             c2 = A.P.p2e_next[p];
         }
-        place_next_warp(A, p, c2, nxt, lane);
+        place_next_warp(A, k < b1 ? p : -1, c2, nxt, lane);
         __syncthreads();
         const int lo = max(pb, ch), hi = min(pe, min(ch + NT, b1));
         for (int kk = lo; kk < hi; ++kk) {
@@ -1084,12 +1364,15 @@ __global__ void __launch_bounds__(4 * TC) km_fbar_tile(MCtx A) {
     }
     if (bad) set_err(A.ctl, EP_ERR_INVALID_POSITION, c0);
     if (!cell_ok || pb == pe) return;
-    const int ex = cl / A.g.nel[1], ez = cl - ex * A.g.nel[1];
-    const Axis4 ax = axis4(A.g, 0, ex), az = axis4(A.g, 1, ez);
+    Axis4 ax, az;
+    cell_axes(cinfo[cl - c0], ax, az);
     if (ax.cls[q] < 0) return;
+    // Σ N m δJ goes straight into the z slot of the packed node values, whose w holds 1/m: km_cons
+    // takes the nodal δJ as z·w (no separate node pass)
+    float* vz = reinterpret_cast<float*>(A.N.vg4) + 2;
 #pragma unroll
     for (int j = 0; j < 4; ++j)
-        if (az.cls[j] >= 0) atomicAdd(&A.N.dJacc[node2(A.g, ax, az, q, j)], acc[j]);
+        if (az.cls[j] >= 0) atomicAdd(vz + 4 * (size_t)node2(A.g, ax, az, q, j), acc[j]);
 }
 
 
@@ -1101,10 +1384,17 @@ __device__ __forceinline__ void dJn_body(const MCtx& A, int bid) {
     const float m = A.N.m[n];
     const float dj = (m == 0.f) ? 0.f : A.N.dJacc[n] / m;
     A.N.dJn[n] = dj;
-    if (A.g.dim == 2) reinterpret_cast<float*>(A.N.vg4)[4 * (size_t)n + 2] = dj;
+    if (A.g.dim == 2) {
+        float* q = reinterpret_cast<float*>(A.N.vg4) + 4 * (size_t)n;
+        q[2] = dj;
+        q[3] = 1.f;
+    }
 }
 
-__global__ void km_dJn(MCtx A) { dJn_body(A, blockIdx.x); }
+__global__ void km_dJn(MCtx A) {
+    pdl_enter();
+    dJn_body(A, blockIdx.x);
+}
 
 
 // FP32 Drucker-Prager (DP.jl:33-98) on Voigt stress s[3]; returns Δλ and its ϵpII increment
@@ -1391,21 +1681,14 @@ __device__ __forceinline__ bool rm_features32(float e11, float e22, float e12, f
 // With the learned return map, a trial-yielding point is handed to the network (its
 // features go to a slot; km_rmap_finish completes it); in record mode the exact map runs
 // and the (features, exact label) pair of the point is appended to the record buffer.
-// FLIP: the last block to finish flips the parity (km_flip's work, one launch less per step)
-template <int BASIS, int ACC, bool FLIP = false>
-__device__ __forceinline__ void cons_body(const MCtx& A, int bid, int plastic_phase) {
-    EP_ACTIVE(A.ctl);
+// FLIP: the last block to finish flips the parity (km_flip's work, one launch less per step).
+// cons_point: list slot k of the step (point p in cell c, stencil axes ax/az)
+template <int BASIS, int ACC>
+__device__ __forceinline__ void cons_point(const MCtx& A, int k, int p, int c, const Axis4& ax, const Axis4& az,
+                                           int plastic_phase, int& nplastic, bool& emit, float* fx, float* fy,
+                                           float* fa) {
     const int cur = A.ctl->parity, nxt = cur ^ 1;
-    const int k = bid * blockDim.x + threadIdx.x;
-    int nplastic = 0;
-    bool emit = false;
-    float fx[RM_NX], fy[RM_NY], fa[4];
-    int fp = 0;
-    if (k < A.S.start[cur][A.g.ncell]) {
-        const int p = A.S.list[cur][k], c = A.S.cellof[cur][k];
-        fp = p;
-        const int ex = c / A.g.nel[1], ez = c - ex * A.g.nel[1];
-        const Axis4 ax = axis4(A.g, 0, ex), az = axis4(A.g, 1, ez);
+    {
         const float hx = (float)A.g.h[0], hz = (float)A.g.h[1];
         const float dtf = (float)A.ctl->dt;
         bool bad = false;
@@ -1417,21 +1700,34 @@ __device__ __forceinline__ void cons_body(const MCtx& A, int bid, int plastic_ph
         axis_w<BASIS>(ax, A.P.dx[cur][0][p], hx, 1.f / hx, lx, wx, dwx, bad);
         axis_w<BASIS>(az, A.P.dx[cur][1][p], hz, 1.f / hz, lz, wz, dwz, bad);
         float g00 = 0.f, g01 = 0.f, g10 = 0.f, g11 = 0.f, a = 0.f;
+        if (lock) {
+            // ∇v as the F-bar pass formed it for this slot; ΔJ̄ - 1 = Σ N δJ_n, δJ_n = z·w
+            const float4 gs = A.P.gv[k];
+            g00 = gs.x; g10 = gs.y; g01 = gs.z; g11 = gs.w;
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            if (ax.cls[i] < 0) continue;
+            for (int i = 0; i < 4; ++i) {
+                if (ax.cls[i] < 0) continue;
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                if (az.cls[j] < 0) continue;
-                const int n = node2(A.g, ax, az, i, j);
-                const float Nx = dwx[i] * wz[j], Nz = wx[i] * dwz[j];
-                const float4 q = A.N.vg4[n];
-                const float vx = q.x, vz = q.y;
-                g00 += Nx * vx;
-                g01 += Nz * vx;
-                g10 += Nx * vz;
-                g11 += Nz * vz;
-                if (lock) a += wx[i] * wz[j] * q.z;
+                for (int j = 0; j < 4; ++j) {
+                    if (az.cls[j] < 0) continue;
+                    const float2 q = *reinterpret_cast<const float2*>(&A.N.vg4[node2(A.g, ax, az, i, j)].z);
+                    a += wx[i] * wz[j] * (q.x * q.y);
+                }
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                if (ax.cls[i] < 0) continue;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    if (az.cls[j] < 0) continue;
+                    const float Nx = dwx[i] * wz[j], Nz = wx[i] * dwz[j];
+                    const float2 q = *reinterpret_cast<const float2*>(&A.N.vg4[node2(A.g, ax, az, i, j)]);
+                    g00 += Nx * q.x;
+                    g01 += Nz * q.x;
+                    g10 += Nx * q.y;
+                    g11 += Nz * q.y;
+                }
             }
         }
         // D = ΔF - I = dt ∇v, column-major (deform.jl:13)
@@ -1606,6 +1902,11 @@ __device__ __forceinline__ void cons_body(const MCtx& A, int bid, int plastic_ph
         if (!lock) place_next(A, p, nxt);
         if (bad) set_err(A.ctl, EP_ERR_INVALID_POSITION, c);
     }
+}
+
+// the warp's emitted slots of km_cons: learned-map slots or recorded pairs, one atomic per warp
+__device__ __forceinline__ void cons_emit(const MCtx& A, bool emit, const float* fx, const float* fy, const float* fa,
+                                          int fp) {
     // learned map slots / recorded pairs: one atomic per warp for the warp's points
     if (A.rmode != EP_RMAP_EXACT) {
         const unsigned bal = __ballot_sync(0xffffffffu, emit);
@@ -1638,7 +1939,11 @@ __device__ __forceinline__ void cons_body(const MCtx& A, int bid, int plastic_ph
             }
         }
     }
-    // plastic point count: one atomic per warp
+}
+
+// the plastic count (one atomic per warp) and, with FLIP, the parity flip by the last block to finish
+template <bool FLIP>
+__device__ __forceinline__ void cons_finish(const MCtx& A, int nplastic) {
     const int tot = __reduce_add_sync(0xffffffffu, nplastic);
     if ((threadIdx.x & 31) == 0 && tot) atomicAdd((unsigned long long*)&A.ctl->plastic, (unsigned long long)tot);
     if (FLIP) {
@@ -1650,8 +1955,30 @@ __device__ __forceinline__ void cons_body(const MCtx& A, int bid, int plastic_ph
     }
 }
 
+// km_cons over the sorted list, one lane per slot
 template <int BASIS, int ACC, bool FLIP = false>
-__global__ void __launch_bounds__(256) km_cons(MCtx A, int plastic_phase) {
+__device__ __forceinline__ void cons_body(const MCtx& A, int bid, int plastic_phase) {
+    EP_ACTIVE(A.ctl);
+    const int cur = A.ctl->parity;
+    const int k = bid * blockDim.x + threadIdx.x;
+    int nplastic = 0;
+    bool emit = false;
+    float fx[RM_NX], fy[RM_NY], fa[4];
+    int fp = 0;
+    if (k < A.S.start[cur][A.g.ncell]) {
+        const int p = A.S.list[cur][k], c = A.S.cellof[cur][k];
+        fp = p;
+        const int ex = c / A.g.nel[1], ez = c - ex * A.g.nel[1];
+        const Axis4 ax = axis4(A.g, 0, ex), az = axis4(A.g, 1, ez);
+        cons_point<BASIS, ACC>(A, k, p, c, ax, az, plastic_phase, nplastic, emit, fx, fy, fa);
+    }
+    cons_emit(A, emit, fx, fy, fa, fp);
+    cons_finish<FLIP>(A, nplastic);
+}
+
+template <int BASIS, int ACC, bool FLIP = false>
+__global__ void __launch_bounds__(256, 4) km_cons(MCtx A, int plastic_phase) {
+    pdl_enter();
     cons_body<BASIS, ACC, FLIP>(A, blockIdx.x, plastic_phase);
 }
 
@@ -2021,6 +2348,7 @@ __global__ void km_scan_add(MCtx A, int which, const int* bsum) {
 // kernels after it read the control block only once it has finished.  Both regions start 16-byte
 // aligned (their own allocations): 16-byte stores, then the tails.
 __global__ void __launch_bounds__(256) km_zero(MCtx A, float* g, long long ng, int* z, long long nz, int begin_step) {
+    pdl_enter();
     if (begin_step) {
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             Ctl* c = A.ctl;
@@ -2056,6 +2384,7 @@ __device__ __forceinline__ unsigned long long ld_status(const unsigned long long
 }
 
 __global__ void __launch_bounds__(MSCAN2_BS) km_vmusl_scan(MCtx A, int ntiles) {
+    pdl_enter();
     EP_ACTIVE(A.ctl);
     if ((int)blockIdx.x >= ntiles) {
         // the mUSL velocity over MSCAN2_BS nodes per block
@@ -2147,6 +2476,44 @@ static int sm_count() {
     return n;
 }
 
+// the largest node box of the tiles of TC cells (tile_box), for the choice of the fused grid update
+static int max_tile_box(const Geo& g, int TC) {
+    int mx = 0;
+    for (int c0 = 0; c0 < g.ncell; c0 += TC) {
+        int NX;
+        const TileBox b = tile_box(g, c0, std::min(c0 + TC, g.ncell), NX, INT_MAX);
+        mx = std::max(mx, NX * b.NZ);
+    }
+    return mx;
+}
+
+// Launch with programmatic stream serialization (the kernel calls pdl_enter() first), so that its
+// blocks are scheduled while the previous kernel of the stream drains; EPGPU_PDL=0 in the
+// environment launches plainly instead.
+static bool pdl_on() {
+    static int on = -1;
+    if (on < 0) {
+        const char* e = getenv("EPGPU_PDL");
+        on = (e && e[0] == '0') ? 0 : 1;
+    }
+    return on != 0;
+}
+
+template <typename... K, typename... Args>
+static void launch_pdl(void (*kern)(K...), int grid, int block, cudaStream_t s, Args... args) {
+    cudaLaunchConfig_t c = {};
+    c.gridDim = dim3((unsigned)grid);
+    c.blockDim = dim3((unsigned)block);
+    c.dynamicSmemBytes = 0;
+    c.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = pdl_on() ? 1 : 0;
+    c.attrs = at;
+    c.numAttrs = 1;
+    cudaLaunchKernelEx(&c, kern, static_cast<K>(args)...);
+}
+
 // step-start zeroing (km_zero) and the fused mUSL velocity + next-step cell scan (km_vmusl_scan)
 static void launch_zero(const MixedCtx& X, cudaStream_t s) {
     const MCtx& A = *(const MCtx*)X.impl;
@@ -2154,13 +2521,13 @@ static void launch_zero(const MixedCtx& X, cudaStream_t s) {
     const long long nz = (long long)(X.sort_zero_bytes / sizeof(int));
     const long long mx = (ng > nz ? ng : nz) / 4 + 1;
     const int nb = (int)std::min<long long>((mx + 255) / 256, 4LL * sm_count());
-    km_zero<<<nb > 0 ? nb : 1, 256, 0, s>>>(A, (float*)X.grid_zero, ng, (int*)X.sort_zero, nz, X.begin_step);
+    launch_pdl(km_zero, nb > 0 ? nb : 1, 256, s, A, (float*)X.grid_zero, ng, (int*)X.sort_zero, nz, X.begin_step);
 }
 
 static void launch_vmusl_scan(const MCtx& A, bool musl, cudaStream_t s) {
     const int nt = scan_tiles(A.g.ncell);
     const int nv = musl ? (A.g.nnode + MSCAN2_BS - 1) / MSCAN2_BS : 0;
-    km_vmusl_scan<<<nt + nv, MSCAN2_BS, 0, s>>>(A, nt);
+    launch_pdl(km_vmusl_scan, nt + nv, MSCAN2_BS, s, A, nt);
 }
 
 
@@ -2362,17 +2729,36 @@ __global__ void km_export(MCtx A, P64 Q, int need_eps) {
     Q.dlam[p] = (double)A.P.dlam[p];
 }
 
+// the nodal state of the last step: a, the damped force and (USL) v from its P2G fields by the
+// step's own grid update (the fused G2P keeps them on chip), the mUSL momentum and velocity as stored
 __global__ void km_export_nodes(MCtx A, N64 Q) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= A.g.nnode) return;
-    Q.m[n] = A.N.m[n];
-    for (int d = 0; d < A.g.dim; ++d) {
-        Q.p[d][n] = A.cf.musl ? A.N.pm[d][n] : A.N.p[d][n];
-        Q.v[d][n] = A.cf.musl ? A.N.vm[d][n] : A.N.v[d][n];
-        Q.a[d][n] = A.N.a[d][n];
-        Q.oobf[d][n] = A.N.f[d][n];
+    const int D = A.g.dim;
+    const float m = A.N.m[n];
+    float a[3], v[3], f[3] = {0.f, 0.f, 0.f}, pn[3] = {0.f, 0.f, 0.f};
+    for (int d = 0; d < D; ++d) {
+        f[d] = A.N.f[d][n];
+        pn[d] = A.N.p[d][n];
     }
-    Q.dJ[n] = 1.0 + (double)A.N.dJn[n];
+    const int bc = A.g.bcw[n];
+    grid_update(D, m, pn, f, bc, (float)A.ctl->dt, (float)A.cf.damping, a, v);
+    const float mi = m != 0.f ? 1.f / m : 0.f;
+    Q.m[n] = m;
+    for (int d = 0; d < D; ++d) {
+        // the mUSL velocity as vmusl_one forms it (the fused F-bar kernel keeps it on chip)
+        const float vm = (m != 0.f && !((bc >> d) & 1)) ? A.N.pm[d][n] * mi : 0.f;
+        Q.p[d][n] = A.cf.musl ? A.N.pm[d][n] : pn[d];
+        Q.v[d][n] = A.cf.musl ? vm : v[d];
+        Q.a[d][n] = a[d];
+        Q.oobf[d][n] = f[d];
+    }
+    if (A.g.dim == 2) {
+        const float4 q = A.N.vg4[n];
+        Q.dJ[n] = 1.0 + (double)(A.cf.locking ? q.z * q.w : 0.f);
+    } else {
+        Q.dJ[n] = 1.0 + (double)A.N.dJn[n];
+    }
 }
 
 // ===========================================================================
@@ -4083,25 +4469,34 @@ static void mixed_step_impl(const MixedCtx& X, int phase, cudaStream_t s) {
         tile(std::integral_constant<int, 0>());
         km_gather<5><<<gn, 256, 0, s>>>(A, A.N.m, A.N.p[0], A.N.p[1], A.N.f[0], A.N.f[1]);
         L += 1;
-    } else if (X.p2g_tile == 16) km_p2g_tile<BASIS, 16, false><<<(nc + 15) / 16, 64, 0, s>>>(A);
-    else if (X.p2g_tile == 32) km_p2g_tile<BASIS, 32, false><<<(nc + 31) / 32, 128, 0, s>>>(A);
-    else km_p2g_tile<BASIS, 64, false><<<(nc + 63) / 64, 256, 0, s>>>(A);
+    } else if (X.p2g_tile == 16) launch_pdl(km_p2g_tile<BASIS, 16, false>, (nc + 15) / 16, 64, s, A);
+    else if (X.p2g_tile == 32) launch_pdl(km_p2g_tile<BASIS, 32, false>, (nc + 31) / 32, 128, s, A);
+    else launch_pdl(km_p2g_tile<BASIS, 64, false>, (nc + 63) / 64, 256, s, A);
     mark("p2g");
-    km_solve<<<gn, 256, 0, s>>>(A);
-    mark("solve");
-    // G2P with the mUSL momentum scatter fused in (tile form), or G2P then a separate mUSL scatter
+    // G2P with the mUSL momentum scatter fused in (tile form), or G2P then a separate mUSL scatter;
+    // the tile form with the grid update on chip when every tile's node box fits
     const bool g2p_musl = !DET && A.cf.musl && A.cf.trsfr != EP_TRSFR_APIC;
-    if (g2p_musl) {
-        if (X.p2g_tile == 16) km_g2p_tile<BASIS, 16><<<(nc + 15) / 16, 64, 0, s>>>(A);
-        else if (X.p2g_tile == 32) km_g2p_tile<BASIS, 32><<<(nc + 31) / 32, 128, 0, s>>>(A);
-        else km_g2p_tile<BASIS, 64><<<(nc + 63) / 64, 256, 0, s>>>(A);
+    const bool solve_fused = g2p_musl && max_tile_box(A.g, X.p2g_tile) <= TB_SOLVE;
+    if (!solve_fused) {
+        launch_pdl(km_solve, gn, 256, s, A);
+        mark("solve");
+        ++L;
+    }
+    if (solve_fused) {
+        if (X.p2g_tile == 16) launch_pdl(km_g2p_tile<BASIS, 16, true>, (nc + 15) / 16, 64, s, A);
+        else if (X.p2g_tile == 32) launch_pdl(km_g2p_tile<BASIS, 32, true>, (nc + 31) / 32, 128, s, A);
+        else launch_pdl(km_g2p_tile<BASIS, 64, true>, (nc + 63) / 64, 256, s, A);
+    } else if (g2p_musl) {
+        if (X.p2g_tile == 16) launch_pdl(km_g2p_tile<BASIS, 16>, (nc + 15) / 16, 64, s, A);
+        else if (X.p2g_tile == 32) launch_pdl(km_g2p_tile<BASIS, 32>, (nc + 31) / 32, 128, s, A);
+        else launch_pdl(km_g2p_tile<BASIS, 64>, (nc + 63) / 64, 256, s, A);
     } else if (DET) {
         km_g2p_seg<BASIS, true><<<gs, 256, 0, s>>>(A);
     } else {
         km_g2p_seg<BASIS, false, false><<<gs, 256, 0, s>>>(A);
     }
     mark("g2p");
-    L += 3;                           // P2G, grid update, G2P
+    L += 2;                           // P2G, G2P
     if (A.cf.musl && !g2p_musl) {
         if (DET) {
             tile(std::integral_constant<int, 1>());
@@ -4117,24 +4512,31 @@ static void mixed_step_impl(const MixedCtx& X, int phase, cudaStream_t s) {
             ++L;
         }
     }
-    // the mUSL nodal velocity and the next step's cell offsets in one launch
-    launch_vmusl_scan(A, A.cf.musl, s);
+    // the mUSL nodal velocity and the next step's cell offsets in one launch (the velocity formed by
+    // the F-bar kernel instead when the grid update ran in the G2P)
+    const bool vm_fused = solve_fused && A.cf.locking;
+    launch_vmusl_scan(A, A.cf.musl && !vm_fused, s);
     mark("vmusl_scan");
     ++L;
     if (A.cf.locking) {
         if (DET) km_fbar_seg<BASIS, true><<<gs, 256, 0, s>>>(A);
-        else if (X.p2g_tile == 16) km_fbar_tile<BASIS, 16><<<(nc + 15) / 16, 64, 0, s>>>(A);
-        else if (X.p2g_tile == 32) km_fbar_tile<BASIS, 32><<<(nc + 31) / 32, 128, 0, s>>>(A);
-        else km_fbar_tile<BASIS, 64><<<(nc + 63) / 64, 256, 0, s>>>(A);
+        else if (vm_fused) {
+            if (X.p2g_tile == 16) launch_pdl(km_fbar_tile<BASIS, 16, true>, (nc + 15) / 16, 64, s, A);
+            else if (X.p2g_tile == 32) launch_pdl(km_fbar_tile<BASIS, 32, true>, (nc + 31) / 32, 128, s, A);
+            else launch_pdl(km_fbar_tile<BASIS, 64, true>, (nc + 63) / 64, 256, s, A);
+        } else if (X.p2g_tile == 16) launch_pdl(km_fbar_tile<BASIS, 16>, (nc + 15) / 16, 64, s, A);
+        else if (X.p2g_tile == 32) launch_pdl(km_fbar_tile<BASIS, 32>, (nc + 31) / 32, 128, s, A);
+        else launch_pdl(km_fbar_tile<BASIS, 64>, (nc + 63) / 64, 256, s, A);
+        ++L;
+        mark("fbar");
         if (DET) {
+            // the deterministic partials, their fixed-order node sums and the nodal δJ
             tile(std::integral_constant<int, 2>());
             km_gather<1><<<gn, 256, 0, s>>>(A, A.N.dJacc, nullptr, nullptr, nullptr, nullptr);
-            L += 2;
+            km_dJn<<<gn, 256, 0, s>>>(A);
+            mark("dJn");
+            L += 3;
         }
-        mark("fbar");
-        km_dJn<<<gn, 256, 0, s>>>(A);
-        mark("dJn");
-        L += 2;
     }
     if (np > 0 && A.cf.nonloc && phase == EP_PHASE_ELASTOPLASTIC) {
         km_nonlocal<ACC><<<np, 32, 0, s>>>(A);
@@ -4147,8 +4549,9 @@ static void mixed_step_impl(const MixedCtx& X, int phase, cudaStream_t s) {
     const bool flip_in_cons = np > 0 && !DET && !net;
     const bool flip_in_finish = np > 0 && !DET && net;     // the learned map's finish kernel is last
     if (np > 0) {
-        if (flip_in_cons) km_cons<BASIS, ACC, true><<<gp, 256, 0, s>>>(A, phase == EP_PHASE_ELASTOPLASTIC);
-        else km_cons<BASIS, ACC><<<gp, 256, 0, s>>>(A, phase == EP_PHASE_ELASTOPLASTIC);
+        const int pp = phase == EP_PHASE_ELASTOPLASTIC;
+        if (flip_in_cons) launch_pdl(km_cons<BASIS, ACC, true>, gp, 256, s, A, pp);
+        else launch_pdl(km_cons<BASIS, ACC>, gp, 256, s, A, pp);
         mark("cons");
         ++L;
         if (net) {

@@ -41,6 +41,7 @@ struct PM {
     float* dv[9];      // TPIC: velocity gradient of the previous step
     int* p2e_next;     // cell of the position written by the last G2P
     int* pcell[2];     // [parity] cell of each point (nonlocal averaging: the cell at the step start)
+    float4* gv;        // 2d F-bar: ∇v (xx, zx, xz, zz) of each list slot, from the F-bar pass for km_cons
 };
 
 struct NM {
@@ -50,7 +51,9 @@ struct NM {
     float* dJn;        // nodal δJ = ΔJ_n - 1
     // 2d: the values the point kernels gather, packed per node so that each of the 16 stencil
     // nodes is one 16-byte load: (v_x, v_z, a_x, a_z) after the grid update, and (the velocity
-    // ∇v is taken of (v or the mUSL v), δJ_n, 0) for the F-bar and constitutive kernels
+    // ∇v is taken of (v or the mUSL v), ΔJ numerator, its scale) for the F-bar and constitutive
+    // kernels: the nodal δJ is z·w, either (Σ N m δJ, 1/m) when the F-bar pass adds into z, or
+    // (δJ_n, 1) when km_dJn forms it
     float4* va4;
     float4* vg4;
 };

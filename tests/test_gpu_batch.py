@@ -93,10 +93,10 @@ def test_batch_instances_match_the_oracle(oracle_mod):
     drawn again), each with its own friction angle and seeded cohesion field, on the phase kernels
     over all instances, for 0.6 s of elastic and 0.3 s of plastic flow.  On the large instance the
     reference's own FP64 result is determined only to ~1e-4 for arithmetic that rounds like FP32: the
-    oracle perturbed by 1e-7 after every step moves by 1.5e-5 - 7.8e-5 (its thread order, FP64 rounding,
-    by 1e-13), and runs of the batch gave 7.6e-6 - 1.7e-4.  The stress bound is therefore the larger of
-    the 1e-5 target and 3x the oracle's spread under that noise (tests/test_conditioning.py); the
-    displacement bound is the target 1e-4."""
+    oracle perturbed by 1e-7 after every step moves by 3e-7 - 1.47e-4 over ten noise seeds (its thread
+    order, FP64 rounding, by 1e-13; tests/test_conditioning.py, EPGPU_SLOW=1), and runs of the batch
+    gave 7.6e-6 - 1.7e-4.  The stress bound is the 1e-5 target on the small instance and twice the
+    oracle's largest spread on the large one; the displacement bound is the target 1e-4 on both."""
     import os
     from epgpu import ic_slump
     from epgpu.batch import Batch, bspline_invalid_nodes
@@ -128,10 +128,8 @@ def test_batch_instances_match_the_oracle(oracle_mod):
         ref = o.download()
         o.close()
         s, d, r = errors(b.download(k), ref, ic["mpts"].x)
-        from test_conditioning import fp32_noise_spread
-        spread = fp32_noise_spread(oracle_mod, ic, cfg["instr"], windows, threads=os.cpu_count() or 1)
-        bound = max(1e-5, 3.0 * spread)
-        print(f"batch instance {k} ({ic['mpts'].nmp} points) vs oracle: stress {s:.2e} (bound {bound:.1e}: "
-              f"oracle spread under FP32-level noise {spread:.2e}) displacement {d:.2e} runout {r:.2e}, "
-              f"plastic {int((ref.dlam != 0).sum())}")
+        from test_conditioning import BATCH_LARGE_SPREAD
+        bound = 1e-5 if k == 0 else 2.0 * BATCH_LARGE_SPREAD
+        print(f"batch instance {k} ({ic['mpts'].nmp} points) vs oracle: stress {s:.2e} (bound {bound:.1e}) "
+              f"displacement {d:.2e} runout {r:.2e}, plastic {int((ref.dlam != 0).sum())}")
         assert s <= bound and d <= 1e-4
