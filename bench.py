@@ -103,33 +103,35 @@ ALG_BYTES_FP64_2D = {
     "node_lists": (4 + 4 * 16, 8 * 2),
 }
 # mixed step (FP32 point streams; F, b_e, accumulated plastic strain as FP64 or as
-# FP32 pairs, the same bytes), finite strain, std transfer, mUSL, F-bar, DP:
+# FP32 pairs, the same bytes), finite strain, std transfer, mUSL, F-bar, DP, in the fused forms the
+# 2d step launches (six kernels: zero, p2g, g2p, vmusl_scan, fbar, cons):
 #   p2g   read list dx2 mp v2 Om0 tau3 (10 x 4 B)            nodes: m p2 f2 (atomics)
-#   solve nodes: read m f2 p2 + 2 mask bytes; write f2 a2 v2 pm2 dJacc
-#   g2p   read list dx2 v2 mp; write v2 dx2 cell + count     nodes: read v2 a2; pm2 (atomics)
-#   vmusl nodes: read m pm2 + masks; write vm2
-#   fbar  read list dx2 mp cell; write list cellof + cursor  nodes: read vm2; dJacc (atomic)
-#   dJn   nodes: read m dJacc; write dJn
-#   cons  read list cellof dx2 F4 b3 ep1 c0 cr tanphi (8-byte F, b, ep1); write F4 b3 ep1 tau3 dlam
-#         nodes: read vm2 dJn
+#   g2p   the grid update inside the tile, then G2P and the mUSL momentum scatter:
+#         read list cell dx2 v2 mp; write v2 dx2(next) cell + count   nodes: read m p2 f2 + Dirichlet word;
+#                                                                     pm2 (atomics)
+#   vmusl_scan  next-step counts -> starts per cell (the mUSL velocity is formed in the F-bar tile)
+#   fbar  the mUSL velocity inside the tile, then ∇v, δJ, placement: read list cell dx2 mp; write
+#         the slot's ∇v (float4, read back by cons) and the next list + cell   nodes: read m pm2 +
+#         Dirichlet word; dJacc (atomic)
+#   cons  read list cell dx2 ∇v4 F4 b3 ep1 c0 cr tanphi (8-byte F, b, ep1); write F4 b3 ep1 tau3 dlam
+#         nodes: read m dJacc (the nodal δJ formed in the gather)
 ALG_BYTES_MIXED_2D = {
     "zero": (0, 20 + 12),                          # m p2 f2 per node, counts (2 parities) + cursor per cell
     "p2g": (40, 20),
     "solve": (0, 22 + 36),
-    # G2P with the mUSL scatter fused (tile form): list+cell, offsets, v, ρΩ read; v, next offsets, cell
-    # written; (v, a) per node read, m v per node added
-    "g2p": (8 + 8 + 8 + 4 + 8 + 8 + 4, 16 + 8),
+    "g2p": (8 + 8 + 8 + 4 + 8 + 8 + 4, 24 + 8),
     "musl": (8 + 8 + 4 + 8, 8),                    # (separate mUSL scatter) list+cell, offsets, ρΩ, v read
     "vmusl": (0, 22),
-    "vmusl_scan": (0, 22 + 8),                     # mUSL velocity per node; next-step counts -> starts per cell
-    "fbar": (20 + 12, 8 + 4),
+    "vmusl_scan": (0, 8),
+    "fbar": (20 + 16 + 8, 16 + 4),
     "dJn": (0, 12),
-    "cons": (4 + 4 + 8 + 32 + 24 + 8 + 12 + 32 + 24 + 8 + 12 + 4, 12),
+    "cons": (4 + 4 + 8 + 16 + 32 + 24 + 8 + 12 + 32 + 24 + 8 + 12 + 4, 8),
 }
 # DRAM bytes (read + write) per launch of the mixed_df step kernels on this workload, from one ncu
 # capture of an exact-map step (dram__bytes_read.sum + dram__bytes_write.sum, cold caches; command in
 # the profile summary of these kernels): the "traffic" of the roofline entry
-NCU_DRAM_BYTES_MIXED_DF = {"p2g": 17540096, "g2p": 12216576, "fbar": 10548224, "cons": 59235328}
+NCU_DRAM_BYTES_MIXED_DF = {"p2g": 17523968, "g2p": 13693440, "vmusl_scan": 422656, "fbar": 11959040,
+                           "cons": 40310272}
 # the whole step by the per-point state S and per-node G rule: S = 35 values read or written once
 # (x2 v2 F4 b3 tau3 epII dlam c0 phi Om0 read; x2 v2 F4 b3 tau3 epII dlam written), G = 30 values
 STEP_BYTES = {"fp64": (35 * 8, 30 * 8), "mixed": (35 * 4, 30 * 4), "mixed_df": (35 * 4, 30 * 4)}

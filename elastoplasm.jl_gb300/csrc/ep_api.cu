@@ -198,8 +198,11 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
         return fail(nullptr, EP_ERR_UNSUPPORTED, "unsupported transfer scheme (mapsto.jl:44)");
     if (cfg->deform != EP_DEFORM_FINITE && cfg->deform != EP_DEFORM_INFINITESIMAL)
         return fail(nullptr, EP_ERR_UNSUPPORTED, "unknown fwrk.deform");
-    if (cfg->constitutive != EP_CONS_DP && cfg->constitutive != EP_CONS_J2)
-        return fail(nullptr, EP_ERR_UNSUPPORTED, "InvalidReturnMapping: only DP and J2 are built");
+    if (cfg->constitutive != EP_CONS_DP && cfg->constitutive != EP_CONS_J2 && cfg->constitutive != EP_CONS_MC &&
+        cfg->constitutive != EP_CONS_CAMC)
+        return fail(nullptr, EP_ERR_UNSUPPORTED, "InvalidReturnMapping (plast.jl:31)");
+    if (cfg->constitutive == EP_CONS_MC && d != 2)
+        return fail(nullptr, EP_ERR_UNSUPPORTED, "the MC return map is plane strain only (MCRetMap.jl uses sigma[1:3])");
     if (cfg->basis == EP_BASIS_GIMPM) {
         bool fin = cfg->deform == EP_DEFORM_FINITE;
         int w = cfg->how;
@@ -424,6 +427,7 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
     P.c0 = fld_ptr(h, F_C0); P.cr = fld_ptr(h, F_CR); P.tphi = fld_ptr(h, F_TPHI); P.sphi = fld_ptr(h, F_SPHI);
     P.cphi = fld_ptr(h, F_CPHI); P.dlam = fld_ptr(h, F_DLAM);
     P.ep1 = fld_ptr(h, F_EP); P.ep2 = fld_ptr(h, F_EP) + h->np;
+    P.epv = h->pass + (size_t)(2 * d + d * d) * h->np;      // ϵpV in the pass-through block (u, p, ∇u, ϵpV)
     for (int k = 0; k < ns; ++k) {
         P.sig[k] = fld_ptr(h, F_SIG) + (size_t)k * h->np;
         P.tau[k] = fld_ptr(h, F_TAU) + (size_t)k * h->np;
@@ -494,6 +498,7 @@ ep_status epgpu_create(const ep_cfg* cfg, const ep_cmpr* cmpr, const ep_mesh_vie
         for (int k = 0; k < nsym; ++k) pm.tau[k] = take(1);
         pm.ep2 = take(1); pm.dlam = take(1); pm.c0 = take(1); pm.cr = take(1); pm.tphi = take(1);
         pm.sphi = take(1); pm.cphi = take(1); pm.mp = take(1); pm.Om0 = take(1); pm.Om = take(1);
+        pm.epv = h->pass + (size_t)(2 * d + d * d) * np;      // FP64 ϵpV in the pass-through block
         take(1);   // spare
         pm.rho = take(1);
         for (int i = 0; i < d; ++i) pm.l[i] = take(1);
@@ -785,11 +790,13 @@ static uint64_t reads_of(const ep_handle* h) {
     if (c.trsfr == EP_TRSFR_TPIC) k |= EP_MPTS_DVIJ;
     if (c.trsfr == EP_TRSFR_APIC) k |= EP_MPTS_APIC_B | (h->mixed ? 0ull : EP_MPTS_APIC_D);
     if (!h->mixed && fin) k |= EP_MPTS_J | EP_MPTS_RHO0 | EP_MPTS_N0;
+    if (c.cons == EP_CONS_CAMC) k |= EP_MPTS_EPV;      // the Cam-Clay return reads and writes ϵpV
     return k;
 }
 
-// What a step may change: the state it carries and the outputs derived from it (u, p, ∇u and ϵpV
-// are the caller's and pass through unchanged; ρ0, Ω0, ℓ0, n0, c0, cr, ϕ are material constants).
+// What a step may change: the state it carries and the outputs derived from it (u, p, ∇u and, but
+// for the Cam-Clay return, ϵpV are the caller's and pass through unchanged; ρ0, Ω0, ℓ0, n0, c0, cr, ϕ
+// are material constants).
 static uint64_t changed_of(const ep_handle* h) {
     const Cfg& c = h->ctx.cf;
     uint64_t k = EP_MPTS_X | EP_MPTS_V | EP_MPTS_N | EP_MPTS_OMEGA | EP_MPTS_DJ | EP_MPTS_J | EP_MPTS_RHO |
@@ -797,6 +804,7 @@ static uint64_t changed_of(const ep_handle* h) {
                  EP_MPTS_BIJ | EP_MPTS_EIJ | EP_MPTS_WIJ | EP_MPTS_SJIJ;
     if (c.basis == EP_BASIS_GIMPM && c.how != EP_HOW_UNDEFORMED && c.how != EP_HOW_NONE) k |= EP_MPTS_L;
     if (c.trsfr == EP_TRSFR_APIC) k |= EP_MPTS_APIC_B | EP_MPTS_APIC_D;
+    if (c.cons == EP_CONS_CAMC) k |= EP_MPTS_EPV;
     return k;
 }
 
@@ -1043,6 +1051,26 @@ ep_status epgpu_run(ep_handle* h, int32_t phase, double T, double tg, double* t_
     h->staging_fresh = false;
     if (nsteps_out) *nsteps_out = h->hctl->nsteps;
     return kernel_error(h);
+}
+
+ep_status epgpu_run_checkpoints(ep_handle* h, int32_t phase, const double* checkpoints, int32_t ncheck,
+                                double tg, double* t_inout, ep_checkpoint_cb cb, void* user, int64_t* nsteps_out) {
+    if (!h || !t_inout || ncheck < 0 || (ncheck > 0 && !checkpoints)) return EP_ERR_ARG;
+    std::vector<double> checks(checkpoints, checkpoints + ncheck);
+    for (double T : checks)
+        if (!std::isfinite(T)) return fail(h, EP_ERR_ARG, "a checkpoint time is not finite");
+    std::sort(checks.begin(), checks.end());
+    int64_t total = 0;
+    for (int32_t k = 0; k < ncheck; ++k) {
+        int64_t n = 0;
+        ep_status st = epgpu_run(h, phase, checks[k], tg, t_inout, &n);
+        total += n;
+        if (nsteps_out) *nsteps_out = total;
+        if (st != EP_OK) return st;
+        if (cb && cb(h, k, *t_inout, user) != 0) break;
+    }
+    if (nsteps_out) *nsteps_out = total;
+    return EP_OK;
 }
 
 static ep_status download_view(ep_handle* h, ep_mpts_view* m, bool need_eps);

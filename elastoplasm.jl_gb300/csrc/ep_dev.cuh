@@ -68,6 +68,7 @@ struct P64 {
     int np;
     double *x[3], *xo[3], *v[3], *l[3], *l0[3];
     double *n0, *n, *Om0, *Om, *dJ, *J, *rho0, *rho, *c0, *cr, *tphi, *sphi, *cphi, *dlam, *ep1, *ep2;
+    double* epv;                      // ϵpV (written by the Cam-Clay return only)
     double *sig[6], *tau[6];
     double *dv[9], *dF[9], *F[9], *b[9], *eps[9], *w[9], *sJ[9];
     double *B[9], *Dm[9], *BD[9];     // APIC: Bᵢⱼ, Dᵢⱼ and the step's Bᵢⱼ D⁻¹ (scratch)

@@ -553,10 +553,30 @@ __device__ __forceinline__ void retmap_point(const Cfg& cf, const Mat& mt, Ctl* 
         P.dlam[p] = dl;
         write = true;
         rebuild = fin;
-    } else {
+    } else if (cf.cons == EP_CONS_J2) {
         int y = j2_return<NS>(s, ep2, P.c0[p], P.cr[p], mt.Hp, mt.Del, &ep1);
         write = y != 0;
         rebuild = fin && y;
+    } else {
+        // MC (2d, MCRetMap.jl) or modified Cam-Clay (camCmodRetMap.jl): ϵ = tensor(Del \ σ, ½) of the
+        // returned stress in both frameworks, b_e = exp(2ϵ) in finite strain
+        int y;
+        if (cf.cons == EP_CONS_MC) {
+            y = mc_return(s, ep2, P.c0[p], P.cr[p], P.sphi[p], P.cphi[p], mt.Hp, mt.Del, mt.DelLU, mt.piv, &ep1);
+            if (y < 0) set_err(ctl, EP_ERR_NONCONVERGED, p);
+        } else {
+            double ev = P.epv[p];
+            y = camc_return<NS>(s, ep2, &ev, mt.Kc, mt.Del, &ep1);
+            if (y > 0) P.epv[p] = ev;
+        }
+        write = y > 0;
+        rebuild = fin && y > 0;
+        if (y > 0 && !fin) {
+            double eps[D * D];
+            strain_from_stress<D>(s, mt.DelLU, mt.piv, eps);
+#pragma unroll
+            for (int k = 0; k < D * D; ++k) P.eps[k][p] = eps[k];
+        }
     }
     if (write) {
         P.ep1[p] = ep1;

@@ -216,6 +216,8 @@ struct MCtx {
     long long* rec_count;
     long long rec_cap;
     double Deld[36], Cmpd[36], Kd, Gd;   // FP64 copies for the exact fallback
+    double DelLU[36];   // LU factors of the FP64 Del (pivots in piv) for the MC and Cam-Clay returns
+    int piv[6];
     // deterministic mode: per-cell node partials (ncell x 16 x up to 5) and a per-point value
     float* part;
     float* ptmp;
@@ -1431,6 +1433,32 @@ __device__ __forceinline__ float dp32(float* s, float ep2, float c0, float cr, f
     return dl;
 }
 
+// The MC (2d, MCRetMap.jl) and modified Cam-Clay (camC/camCmodRetMap.jl) returns of one point as FP64
+// islands (ep_scalar.h, the FP64 step's code) on the FP32 trial stress tt[NS]: their absolute
+// tolerances (1e-6 Pa, 1e-6 Pa²) lie below the resolution of an FP32 stress.  Returns the new
+// ϵpII[1] and sets *yielded; writes ϵpV (Cam-Clay) and reports a non-converged MC return.  Kept out
+// of line so that the DP and J2 paths of the constitutive kernels keep their registers.
+template <int NS>
+__device__ __noinline__ float cons_iterative(const MCtx& A, int p, float* tt, float ep2, bool* yielded) {
+    double s[NS];
+    for (int i = 0; i < NS; ++i) s[i] = (double)tt[i];
+    double g = 0.0;
+    int y;
+    if (A.cf.cons == EP_CONS_MC) {
+        y = mc_return(s, (double)ep2, (double)A.P.c0[p], (double)A.P.cr[p], (double)A.P.sphi[p], (double)A.P.cphi[p],
+                      (double)A.Hp, A.Deld, A.DelLU, A.piv, &g);
+        if (y < 0) set_err(A.ctl, EP_ERR_NONCONVERGED, p);
+    } else {
+        double ev = A.P.epv[p];
+        y = camc_return<NS>(s, (double)ep2, &ev, A.Kd, A.Deld, &g);
+        if (y > 0) A.P.epv[p] = ev;
+    }
+    *yielded = y > 0;
+    if (y > 0)
+        for (int i = 0; i < NS; ++i) tt[i] = (float)s[i];
+    return (float)g;
+}
+
 // FP32 J2 cutting plane (J2.jl:21-76 restated as in ep_scalar.h), 2d
 __device__ __forceinline__ int j232(float* s, float ep2, float c0, float cr, float Hp, const float* D, float* g) {
     auto yield = [&](const float* v, float kap, float* n) {
@@ -1868,10 +1896,15 @@ __device__ __forceinline__ void cons_point(const MCtx& A, int k, int p, int c, c
                     yielded = dl != 0.f;
                     if (yielded && A.rmode == EP_RMAP_RECORD && fin) emit = rm_label(fx, (double)A.l2g, fy) != 0;
                 }
-            } else {
+            } else if (A.cf.cons == EP_CONS_J2) {
                 const float Dl[9] = {A.Del[0], A.Del[1], A.Del[2], A.Del[3], A.Del[4],
                                      A.Del[5], A.Del[6], A.Del[7], A.Del[8]};
                 yielded = j232(tt, ep2, A.P.c0[p], A.P.cr[p], A.Hp, Dl, &newg) != 0;
+                absolute = true;
+            } else {
+                // MC / modified Cam-Clay: the iterative returns run as FP64 islands (ep_scalar.h) on the
+                // FP32 trial stress; their absolute tolerances (1e-6 Pa, Pa²) are below FP32 resolution
+                newg = cons_iterative<3>(A, p, tt, ep2, &yielded);
                 absolute = true;
             }
             if (yielded) {
@@ -2025,6 +2058,7 @@ __device__ __noinline__ void rmap_fallback_slot(const MCtx& A, int i) {
 // FLIP: the last block to finish does km_flip's work (parity flip, slot counters emptied)
 template <int ACC, bool FLIP = false>
 __global__ void __launch_bounds__(256) km_rmap_finish(MCtx A) {
+    pdl_enter();
     EP_ACTIVE(A.ctl);
     const int n = *A.rcount;
     int nl = 0, nf = 0;
@@ -3774,9 +3808,9 @@ __global__ void __launch_bounds__(256, 3) km_cons3(MCtx A, int plastic_phase) {
                         if (yielded && A.rmode == EP_RMAP_RECORD) emit = rm_label(fx, (double)A.l2g, fy) != 0;
                     }
                 } else {
-                    // J2 (J2.jl:21-76): its flow Del n with the tensor shear components of n is not
-                    // coaxial with the trial, so it runs on the Voigt stress, and b_e is rebuilt
-                    // from a second eigen-decomposition of ε = tensor(Del \ τ, ½)
+                    // J2 (J2.jl:21-76) and Cam-Clay: their flow Del n with the tensor shear components of
+                    // n is not coaxial with the trial, so they run on the Voigt stress, and b_e is
+                    // rebuilt from a second eigen-decomposition of ε = tensor(Del \ τ, ½)
                     {
                         const R td[3] = {(R)tp[0], (R)tp[1], (R)tp[2]};
                         R tv[6];
@@ -3785,7 +3819,10 @@ __global__ void __launch_bounds__(256, 3) km_cons3(MCtx A, int plastic_phase) {
                         for (int i = 0; i < 6; ++i) tt[i] = (float)tv[i];
                     }
                     float newg = 0.f;
-                    if (j2f6(tt, ep2, A.P.c0[p], A.P.cr[p], A.Hp, A.Del, &newg)) {
+                    bool y3 = false;
+                    if (A.cf.cons == EP_CONS_J2) y3 = j2f6(tt, ep2, A.P.c0[p], A.P.cr[p], A.Hp, A.Del, &newg) != 0;
+                    else newg = cons_iterative<6>(A, p, tt, ep2, &y3);      // modified Cam-Clay (FP64 island)
+                    if (y3) {
                         ++nplastic;
                         if (ACC == 0) {
                             A.P.ep1d[p] = (double)newg;
@@ -3871,7 +3908,10 @@ __global__ void __launch_bounds__(256, 3) km_cons3(MCtx A, int plastic_phase) {
                     }
                 } else {
                     float newg = 0.f;
-                    if (j2f6(tt, ep2, A.P.c0[p], A.P.cr[p], A.Hp, A.Del, &newg)) {
+                    bool y3 = false;
+                    if (A.cf.cons == EP_CONS_J2) y3 = j2f6(tt, ep2, A.P.c0[p], A.P.cr[p], A.Hp, A.Del, &newg) != 0;
+                    else newg = cons_iterative<6>(A, p, tt, ep2, &y3);      // modified Cam-Clay (FP64 island)
+                    if (y3) {
                         ++nplastic;
                         if (ACC == 0) {
                             A.P.ep1d[p] = (double)newg;
@@ -4558,8 +4598,8 @@ static void mixed_step_impl(const MixedCtx& X, int phase, cudaStream_t s) {
             mlp_infer(X.net, A.rx, A.rcount, np, A.ry, s);
             mark("mlp");
             const int gf = std::min(gp, 4 * sm_count());
-            if (flip_in_finish) km_rmap_finish<ACC, true><<<gf, 256, 0, s>>>(A);
-            else km_rmap_finish<ACC><<<gf, 256, 0, s>>>(A);
+            if (flip_in_finish) launch_pdl(km_rmap_finish<ACC, true>, gf, 256, s, A);
+            else launch_pdl(km_rmap_finish<ACC>, gf, 256, s, A);
             mark("rmap_finish");
             L += 2;
         }
@@ -4667,6 +4707,9 @@ void mixed_ctx_init(void* mem, const Cfg& cf, const Geo& g, Ctl* ctl, const PM& 
     A->acc = acc;
     A->Kd = Kc;
     A->Gd = Gc;
+    for (int i = 0; i < 36; ++i) A->DelLU[i] = A->Deld[i];
+    if (ns == 3) lu_factor<3>(A->DelLU, A->piv);
+    else lu_factor<6>(A->DelLU, A->piv);
     A->l2g = (float)(Del[1] / (Del[0] - Del[1]));   // λ / (2G): Del(2,1) = λ, Del(1,1) = λ + 2G
     A->rmode = EP_RMAP_EXACT;
     A->rx = A->ry = A->raux = nullptr;

@@ -42,6 +42,7 @@ struct PM {
     int* p2e_next;     // cell of the position written by the last G2P
     int* pcell[2];     // [parity] cell of each point (nonlocal averaging: the cell at the step start)
     float4* gv;        // 2d F-bar: ∇v (xx, zx, xz, zz) of each list slot, from the F-bar pass for km_cons
+    double* epv;       // ϵpV, FP64 (read and written by the Cam-Clay return only)
 };
 
 struct NM {

@@ -14,6 +14,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -111,6 +112,10 @@ static_assert(128 * FWD_GROUPS <= 384 && 384 + 32 * FWD_GROUPS <= 512, "TMEM col
 constexpr int FWD_THREADS = 256 * FWD_GROUPS;
 
 __global__ void __launch_bounds__(FWD_THREADS, 1) km_mlp_fwd(FwdArgs a) {
+    // inside the mixed step the kernel is launched as a programmatic dependent of the constitutive
+    // kernel: wait for its slots and count before the first read (a no-op for a plain launch)
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     extern __shared__ __align__(128) uint8_t sm[];
     uint8_t* sW = sm + FWD_SW;
     uint64_t* bar = reinterpret_cast<uint64_t*>(sm + FWD_BAR);       // [0] weights, [1 + g] group g's MMAs
@@ -675,7 +680,24 @@ static void mlp_fwd_launch(ep_mlp* m, const float* X, int n, const int* ndev, fl
     a.err = m->d.err;
     const int tiles = (n + MT - 1) / MT;
     const int grid = ndev ? m->sms : std::max(1, std::min((tiles + FWD_GROUPS - 1) / FWD_GROUPS, m->sms));
-    km_mlp_fwd<<<grid, FWD_THREADS, FWD_SMEM, s>>>(a);
+    if (!ndev) {
+        km_mlp_fwd<<<grid, FWD_THREADS, FWD_SMEM, s>>>(a);
+        return;
+    }
+    // the step's inference: a programmatic dependent launch (scheduled while the constitutive kernel
+    // drains; the kernel waits for it before reading), unless EPGPU_PDL=0
+    const char* e = getenv("EPGPU_PDL");
+    cudaLaunchConfig_t c = {};
+    c.gridDim = dim3((unsigned)grid);
+    c.blockDim = dim3((unsigned)FWD_THREADS);
+    c.dynamicSmemBytes = FWD_SMEM;
+    c.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = (e && e[0] == '0') ? 0 : 1;
+    c.attrs = at;
+    c.numAttrs = 1;
+    cudaLaunchKernelEx(&c, km_mlp_fwd, a);
 }
 
 void mlp_infer(ep_mlp* m, const float* X, const int* ndev, int cap, float* Y, cudaStream_t s) {

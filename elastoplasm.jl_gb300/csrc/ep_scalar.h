@@ -682,6 +682,163 @@ EP_HD int j2_return(double* s, double ep2, double c0, double cr, double Hp, cons
     return 1;
 }
 
+// ---------------------------------------------------------------------------
+// Mohr-Coulomb return, 2d plane strain (plast/retmap/MCRetMap.jl:1-54).  The reference's function is
+// commented out of its dispatcher (plast.jl:14-15) and reads fields the Point no longer has (mpts.ϕ,
+// mpts.c₀ at :11-12 and mpts.c0 at :33); it is restated with the Solid's fields and otherwise as
+// written: ψ = 0.5° (:3), H = cos ϕ Hp (:11), c = max(c₀ + Hp ϵII, cᵣ) with ϵII the softening input
+// ϵpII[2,p] plus the plastic strain of this return (:12-13, :32-34), the yield function on the
+// in-plane Mohr circle f = τII + σm sin ϕ − c cos ϕ (:14-15), and the non-associated cutting plane
+// Δγ = f/(H + ∂fᵀ Del ∂g), Δσ = Δγ Del ∂g, Δϵ += Del \ Δσ, σ −= Δσ while |f| > 1e-6 (:20-43).
+// Returns 1 when the point yielded (ϵII is written to *ep1, as mpts.ϵpII[p] = ϵII at :45, the same
+// row the J2 restatement writes), 0 when elastic, -1 after more than 1e4 iterations (the reference
+// throws, :38-41).  Δλ is not written, as in the reference.
+// ---------------------------------------------------------------------------
+EP_HD double mc_tau(const double* s, double* sm) {
+    *sm = 0.5 * (s[0] + s[1]);
+    const double d = s[0] - s[1];
+    return sqrt(0.25 * (d * d) + s[2] * s[2]);
+}
+
+EP_HD int mc_return(double* s, double ep2, double c0, double cr, double sphi, double cphi, double Hp,
+                    const double* Del, const double* DelLU, const int* piv, double* ep1) {
+    const double spsi = 0x1.1df37c4954c21p-7;        // sin(0.5*π/180.0), MCRetMap.jl:3
+    const double H = cphi * Hp;
+    const double e0 = ep2;
+    double c = c0 + Hp * e0;
+    if (c < cr) c = cr;
+    double sm, tII = mc_tau(s, &sm);
+    double f = (tII + sm * sphi) - c * cphi;
+    if (!(f > 0.0)) return 0;
+    double g = e0, de[3] = {0.0, 0.0, 0.0};
+    int it = 0;
+    while (fabs(f) > 1.0e-6) {
+        it = it + 1;
+        const double a = (s[0] - s[1]) / (4.0 * tII);
+        const double df[3] = {a + sphi / 2.0, -(s[0] - s[1]) / (4.0 * tII) + sphi / 2.0, s[2] / tII};
+        const double dg[3] = {a + spsi / 2.0, -(s[0] - s[1]) / (4.0 * tII) + spsi / 2.0, s[2] / tII};
+        // ∂fᵀ Del ∂g as (∂fᵀ Del) ∂g
+        double den = 0.0;
+        for (int j = 0; j < 3; ++j) {
+            const double r = (df[0] * Del[3 * j] + df[1] * Del[1 + 3 * j]) + df[2] * Del[2 + 3 * j];
+            den = (j == 0) ? r * dg[0] : den + r * dg[j];
+        }
+        const double dgam = f / (H + den);
+        double ds[3], x[3];
+        for (int i = 0; i < 3; ++i)
+            ds[i] = ((dgam * Del[i]) * dg[0] + (dgam * Del[i + 3]) * dg[1]) + (dgam * Del[i + 6]) * dg[2];
+        lu_solve<3>(DelLU, piv, ds, x);
+        for (int i = 0; i < 3; ++i) de[i] = de[i] + x[i];
+        g = e0 + sqrt((2.0 / 3.0) * ((de[0] * de[0] + de[1] * de[1]) + 2.0 * (de[2] * de[2])));
+        c = c0 + Hp * g;
+        if (c < cr) c = cr;
+        for (int i = 0; i < 3; ++i) s[i] = s[i] - ds[i];
+        tII = mc_tau(s, &sm);
+        f = (tII + sm * sphi) - c * cphi;
+        if (it > 10000) return -1;
+    }
+    *ep1 = g;
+    return 1;
+}
+
+// ---------------------------------------------------------------------------
+// Modified Cam-Clay return (camC.zip: camC/camCmodRetMap.jl, after De Souza Neto, Perić & Owen 2008),
+// the reference's archived Cam-Clay variant that its dispatcher names (plast.jl:28-29, commented
+// out).  Constants as written there: χ = 3/2, Pt = Kc/10, a0 = Pt + Kc/10, β = 1, M from ϕcs = 20°,
+// ζ = 0 (a = a0 exp(−ζ ϵpV)), at most 19 cutting-plane iterations while |f| > 1e-6.  Restated:
+//  * the yield function is the ellipse f = (P − Pt + a)²/b² + (q/M)² − a² (b = β when P < Pt − a,
+//    else 1) — the form the variant's derivative (∂f/∂P = 2(P − Pt + a)/b²) and its envelope plot
+//    use; its camCYield writes (P + Pt − a), which puts the ellipse's centre on the tension side;
+//  * P, q and n as camCParam forms them (2d: P = (σxx + σyy)/2, J2 with 2σxy²), the flow direction
+//    ∂f/∂σ = ∂f/∂P/3 [1 1 (1) 0…] + √χ ∂f/∂q n as written (its 1/3 also in 2d);
+//  * ϵpII and ϵpV of the Solid: γ starts from the softening input ϵpII[2,p] and is written to
+//    *ep1 (the row the J2 and MC restatements write), ϵpV is read and written through *epV.
+// Returns 1 when the point yielded, 0 when elastic.  Δλ is not written, as in the reference.
+// ---------------------------------------------------------------------------
+template <int NS>
+EP_HD double camc_param(const double* s, double* q, double* n) {
+    const double chi = 3.0 / 2.0;
+    double P, J2, x[NS];
+    if (NS == 3) {
+        P = (s[0] + s[1]) / 2.0;
+        x[0] = s[0] - P; x[1] = s[1] - P; x[2] = s[2] - 0.0;
+        J2 = 0.5 * ((x[0] * x[0] + x[1] * x[1]) + 2.0 * (x[2] * x[2]));
+    } else {
+        P = ((s[0] + s[1]) + s[2]) / 3.0;
+        for (int i = 0; i < 3; ++i) x[i] = s[i] - P;
+        for (int i = 3; i < 6; ++i) x[i] = s[i] - 0.0;
+        J2 = 0.5 * (((((x[0] * x[0] + x[1] * x[1]) + x[2] * x[2]) + 2.0 * (x[3] * x[3])) + 2.0 * (x[4] * x[4])) +
+                    2.0 * (x[5] * x[5]));
+    }
+    const double xn = sqrt(2.0 * J2);
+    for (int i = 0; i < NS; ++i) n[i] = x[i] / xn;
+    *q = sqrt(chi) * xn;
+    return P;
+}
+
+EP_HD double camc_yield(double P, double q, double Pt, double a, double beta, double M, double* b) {
+    *b = (P < Pt - a) ? beta : 1.0;
+    const double u = P - Pt + a, w = q / M;
+    return ((1.0 / ((*b) * (*b))) * (u * u) + w * w) - a * a;
+}
+
+template <int NS>
+EP_HD int camc_return(double* s, double ep2, double* epV, double Kc, const double* Del, double* ep1) {
+    const double sqchi = 0x1.3988e1409212ep+0;          // sqrt(3/2)
+    const double Pt = Kc / 10.0;
+    const double a0 = Pt + Kc / 10.0;
+    const double beta = 1.0 / 1.0;
+    const double M = 0x1.8b4b7e887abd4p-1;               // 6 sin ϕcs / (3 − sin ϕcs), ϕcs = 20.0*π/180.0
+    const double zeta = 0.0;
+    double a = a0 * ep_exp(-zeta * (*epV));
+    double q, n[NS], b;
+    double P = camc_param<NS>(s, &q, n);
+    double f = camc_yield(P, q, Pt, a, beta, M, &b);
+    if (!(f > 0.0)) return 0;
+    double ev = *epV, g = ep2;
+    int eta = 1;
+    while (fabs(f) > 1.0e-6 && eta < 20) {
+        const double dfdp = (2.0 / (b * b)) * (P - Pt + a);
+        const double dfdq = (2.0 * q) / (M * M);
+        double df[NS];
+        for (int i = 0; i < NS; ++i) {
+            const bool normal = i < (NS == 3 ? 2 : 3);
+            df[i] = normal ? (dfdp * 1.0) / 3.0 + (sqchi * dfdq) * n[i] : (sqchi * dfdq) * n[i];
+        }
+        // Δλ = f / (∂fᵀ Del ∂f), (∂fᵀ Del) ∂f
+        double den = 0.0;
+        for (int j = 0; j < NS; ++j) {
+            double r = df[0] * Del[NS * j];
+            for (int i = 1; i < NS; ++i) r = r + df[i] * Del[i + NS * j];
+            den = (j == 0) ? r * df[0] : den + r * df[j];
+        }
+        const double dl = f / den;
+        for (int i = 0; i < NS; ++i) {
+            double r = (dl * Del[i]) * df[0];
+            for (int j = 1; j < NS; ++j) r = r + (dl * Del[i + NS * j]) * df[j];
+            s[i] = s[i] - r;
+        }
+        ev = ev + dl * dfdp;
+        g = g + dl * dfdq;
+        a = a0 * ep_exp(-zeta * ev);
+        P = camc_param<NS>(s, &q, n);
+        f = camc_yield(P, q, Pt, a, beta, M, &b);
+        eta = eta + 1;
+    }
+    *epV = ev;
+    *ep1 = g;
+    return 1;
+}
+
+// ϵ = tensor(Del \ σ, ½) after a return (MCRetMap.jl:44, camCmodRetMap.jl: mpD.ϵ = mutate(Del\σ, 0.5)).
+template <int D>
+EP_HD void strain_from_stress(const double* s, const double* DelLU, const int* piv, double* eps) {
+    const int NS = (D == 2) ? 3 : 6;
+    double x[NS];
+    lu_solve<NS>(DelLU, piv, s, x);
+    tensor_from_voigt<D>(x, 0.5, eps);
+}
+
 // Finite-strain elastic predictor (elast.jl:45-56): b <- ΔF b ΔF', ϵ = ½ log b,
 // τ = Del voigt(ϵ, 2).
 template <int D>

@@ -21,7 +21,7 @@ _I64 = C.POINTER(C.c_int64)
 EP_OK = 0
 STATUS = {0: "EP_OK", 1: "EP_ERR_ARG", 2: "EP_ERR_UNSUPPORTED", 3: "EP_ERR_NONFINITE",
           5: "EP_ERR_TIMEOUT", 6: "EP_ERR_CUDA", 7: "EP_ERR_INVALID_POSITION",
-          8: "EP_ERR_NOMEM", 9: "EP_ERR_STATE"}
+          8: "EP_ERR_NOMEM", 9: "EP_ERR_STATE", 10: "EP_ERR_NONCONVERGED"}
 
 
 class ep_cfg(C.Structure):
@@ -178,6 +178,9 @@ def library_path() -> str:
     return os.path.join(here, "lib", "libepgpu.so")
 
 
+# ep_checkpoint_cb: int32_t (*)(ep_handle* h, int32_t k, double t, void* user)
+CHECKPOINT_CB = C.CFUNCTYPE(C.c_int32, C.c_void_p, C.c_int32, C.c_double, C.c_void_p)
+
 # exported C symbols and their ctypes signatures (kept in step with include/epgpu.h)
 SIGNATURES = {
     "epgpu_version": (C.c_char_p, []),
@@ -186,6 +189,8 @@ SIGNATURES = {
     "epgpu_upload": (C.c_int, [C.c_void_p, C.POINTER(ep_mpts_view)]),
     "epgpu_step": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, _D, _D]),
     "epgpu_run": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_double, _D, _I64]),
+    "epgpu_run_checkpoints": (C.c_int, [C.c_void_p, C.c_int32, _D, C.c_int32, C.c_double, _D, CHECKPOINT_CB,
+                                        C.c_void_p, _I64]),
     "epgpu_download": (C.c_int, [C.c_void_p, C.POINTER(ep_mpts_view)]),
     "epgpu_upload_fields": (C.c_int, [C.c_void_p, C.POINTER(ep_mpts_view), C.c_uint64]),
     "epgpu_download_fields": (C.c_int, [C.c_void_p, C.POINTER(ep_mpts_view), C.c_uint64]),

@@ -66,7 +66,7 @@ HOW = {None: 0, "undeformed": 1, "detFij": 2, "Fii": 3, "Uii": 4,
        "detΔFij": 5, "ΔFii": 6, "ΔUii": 7}
 DEFORM = {"finite": 0, "infinitesimal": 1}
 TRSFR = {"std": 0, "tpic": 1, "apic": 2}
-CONSTITUTIVE = {"DP": 0, "J2": 1}
+CONSTITUTIVE = {"DP": 0, "J2": 1, "MC": 2, "camC": 3}
 PRECISION = {"fp64": 0, "mixed": 1, "mixed_df": 2}
 
 
@@ -97,6 +97,8 @@ def to_abi(instr: dict) -> dict:
     cons = instr["plast"]["constitutive"]
     if cons not in CONSTITUTIVE:
         raise UnsupportedError(f"InvalidReturnMapping: {cons}")
+    if cons == "MC" and dim != 2:
+        raise UnsupportedError("the MC return map is plane strain only (MCRetMap.jl works on sigma[1:3])")
     if instr.get("dtype", 64) != 64:
         raise UnsupportedError("dtype=32 host arrays are not built: the C-ABI takes Float64 "
                                "arrays; use gpu.precision='mixed' for the FP32 device path")

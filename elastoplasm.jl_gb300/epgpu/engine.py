@@ -97,6 +97,32 @@ class Engine:
         self._check(self.lib.epgpu_run(self.h, int(phase), float(T), float(tg), C.byref(tt), C.byref(n)))
         return tt.value, n.value
 
+    def run_checkpoints(self, phase: int, checks, tg: float, t: float, on_checkpoint=None):
+        """One workflow phase over a checkpoint list in one call (``epgpu_run_checkpoints``): the
+        library sorts the list, runs each window on the device and calls ``on_checkpoint(t, engine)``
+        after it (a truthy return value stops the phase).  Returns (t, steps)."""
+        arr = np.ascontiguousarray(np.asarray(checks, dtype=np.float64).ravel())
+        tt = C.c_double(t)
+        n = C.c_int64(0)
+        failure = []
+
+        def cb(_h, _k, t_now, _user):
+            if on_checkpoint is None:
+                return 0
+            try:
+                return 1 if on_checkpoint(t_now, self) else 0
+            except BaseException as exc:          # no exception may cross the C ABI: stop and re-raise
+                failure.append(exc)
+                return 1
+
+        fn = abi.CHECKPOINT_CB(cb)
+        st = self.lib.epgpu_run_checkpoints(self.h, int(phase), arr.ctypes.data_as(C.POINTER(C.c_double)),
+                                            int(arr.size), float(tg), C.byref(tt), fn, None, C.byref(n))
+        if failure:
+            raise failure[0]
+        self._check(st)
+        return tt.value, n.value
+
     def stats(self) -> dict:
         s = abi.ep_stats()
         self._check(self.lib.epgpu_stats(self.h, C.byref(s)))

@@ -21,30 +21,33 @@ def _default_engine(ic, instr):
     return Engine(ic, instr)
 
 
+def _phase(engine, phase: int, checks, tg: float, time: dict, on_checkpoint) -> int:
+    """Walk one phase's checkpoint list.  The GPU engine takes the whole list in one call
+    (``epgpu_run_checkpoints``); other engines (the oracle) are driven window by window."""
+    if hasattr(engine, "run_checkpoints"):
+        t, n = engine.run_checkpoints(phase, checks, tg, float(time["t"][0]), on_checkpoint)
+        time["t"][0] = t
+        return n
+    steps = 0
+    for T in checks:
+        t, n = engine.run(phase, T, tg, float(time["t"][0]))
+        time["t"][0] = t
+        steps += n
+        if on_checkpoint and on_checkpoint(t, engine):
+            break
+    return steps
+
+
 def elastodynamic(engine, time: dict, instr: dict, on_checkpoint=None) -> int:
     """``elastodynamic!`` (worflow.jl:23-47): gravity ramp, no return map."""
     checks = sorted(frange(time["t"][0], instr["plot"]["freq"], time["te"]))
-    steps = 0
-    for T in checks:
-        t, n = engine.run(ELASTODYNAMIC, T, time["tg"], float(time["t"][0]))
-        time["t"][0] = t
-        steps += n
-        if on_checkpoint:
-            on_checkpoint(t, engine)
-    return steps
+    return _phase(engine, ELASTODYNAMIC, checks, time["tg"], time, on_checkpoint)
 
 
 def elastoplastic(engine, time: dict, instr: dict, on_checkpoint=None) -> int:
     """``elastoplastic!`` (worflow.jl:68-93): full gravity, with return map."""
     checks = sorted(frange(time["t"][0], instr["plot"]["freq"], time["t"][1]))
-    steps = 0
-    for T in checks:
-        t, n = engine.run(ELASTOPLASTIC, T, time["tg"], float(time["t"][0]))
-        time["t"][0] = t
-        steps += n
-        if on_checkpoint:
-            on_checkpoint(t, engine)
-    return steps
+    return _phase(engine, ELASTOPLASTIC, checks, time["tg"], time, on_checkpoint)
 
 
 def elastoplasm(ic: dict, cfg: dict, mode: str = "elastodynamic", engine_factory=None, on_checkpoint=None) -> dict:

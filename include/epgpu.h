@@ -41,7 +41,9 @@ typedef enum ep_status {
     EP_ERR_INVALID_POSITION = 7, /* B-spline node outside its boundary table: the
                                     reference's error("Invalid position") (bsmpm.jl:75) */
     EP_ERR_NOMEM = 8,
-    EP_ERR_STATE = 9             /* calls out of order (step before upload, ...) */
+    EP_ERR_STATE = 9,            /* calls out of order (step before upload, ...) */
+    EP_ERR_NONCONVERGED = 10     /* a return map exceeded its iteration limit (the reference
+                                    throws "CPA: η_it>...", MCRetMap.jl:38-41) */
 } ep_status;
 
 /* instr.basis.which (require.jl:39) */
@@ -52,8 +54,8 @@ enum { EP_HOW_NONE = 0, EP_HOW_UNDEFORMED = 1, EP_HOW_DETFIJ = 2, EP_HOW_FII = 3
 /* instr.fwrk.deform / trsfr (require.jl:44-45) */
 enum { EP_DEFORM_FINITE = 0, EP_DEFORM_INFINITESIMAL = 1 };
 enum { EP_TRSFR_STD = 0, EP_TRSFR_TPIC = 1, EP_TRSFR_APIC = 2 };
-/* instr.plast.constitutive (require.jl:68) */
-enum { EP_CONS_DP = 0, EP_CONS_J2 = 1 };
+/* instr.plast.constitutive (require.jl:68; "MC" and "camC" are the names plast.jl:14,28 dispatches on) */
+enum { EP_CONS_DP = 0, EP_CONS_J2 = 1, EP_CONS_MC = 2, EP_CONS_CAMC = 3 };
 /* device arithmetic: FP64 in the reference's order; FP32 transfers with FP64
  * accumulated state and isotropic log/exp; FP32 transfers with double-float
  * (FP32 pair) accumulated state */
@@ -162,7 +164,7 @@ const char* epgpu_version(void);
 /* Build a device context for `nmp` points on `mesh` with switches `cfg`
  * (replaces kwargser's kernel table, kwargser.jl:49-60, and the arrays of
  * setup_mesh/setup_mpts).  Returns EP_ERR_UNSUPPORTED for switch combinations
- * the reference rejects or this library does not build (MC, camC, 1d; APIC in the
+ * the reference rejects or this library does not build (MC in 3d, 1d; APIC in the
  * mixed precisions on meshes with h >= 2.5 in 2d or h >= 100 in 3d, where the
  * reference's D⁻¹ of p2n.jl:221-225 could differ from the identity the mixed step
  * assumes: its Dᵢⱼ is rank one, so |det D| is rounding noise below 1e-12 until then). */
@@ -186,6 +188,22 @@ ep_status epgpu_step(ep_handle* h, int32_t phase, double dt, const double* g, do
  * device in CUDA graphs; *t_inout is read and written back.  nsteps_out may be NULL. */
 ep_status epgpu_run(ep_handle* h, int32_t phase, double T, double tg, double* t_inout,
                     int64_t* nsteps_out);
+
+/* Called after each checkpoint window of epgpu_run_checkpoints with the window's index k (into the
+ * sorted list) and the simulated time reached.  The handle is idle during the call: the callback may
+ * download fields (epgpu_download, epgpu_fields, ...) the way savlot reads the Point at a checkpoint.
+ * Return 0 to go on, anything else to stop after this window. */
+typedef int32_t (*ep_checkpoint_cb)(ep_handle* h, int32_t k, double t, void* user);
+
+/* One phase of the reference's workflow over a whole checkpoint list (elastodynamic!/elastoplastic!,
+ * worflow.jl:23-47 and 68-93): the list is sorted ascending (worflow.jl:24,69 sort the collected
+ * range), then for each T the window `while T > t` runs as epgpu_run does, and cb (may be NULL) is
+ * called in place of savlot (worflow.jl:41,87).  Windows whose T <= t take no step, as in the
+ * reference's while loop, but their callback is still called.  *t_inout is read and written back;
+ * nsteps_out (may be NULL) receives the steps taken over all windows. */
+ep_status epgpu_run_checkpoints(ep_handle* h, int32_t phase, const double* checkpoints, int32_t ncheck,
+                                double tg, double* t_inout, ep_checkpoint_cb cb, void* user,
+                                int64_t* nsteps_out);
 
 /* Copy the point state out (device SoA -> host AoS); NULL fields are skipped. */
 ep_status epgpu_download(ep_handle* h, ep_mpts_view* mpts);

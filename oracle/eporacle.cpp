@@ -13,7 +13,7 @@
 //   n2p        picflip_n2p + augm        workflow/mapsto/n2p.jl:14-76, augm.jl:13-53
 //   update     deform/domain/ΔJ{n,s,p}   workflow/elastoplast/update/*.jl
 //   elast      finite/infinitesimal      workflow/elastoplast/elast/elast.jl:45-124
-//   plast      nonlocal + DP/J2          workflow/elastoplast/plast/{plast,nonlocal}.jl, retmap/*.jl
+//   plast      nonlocal + DP/J2/MC/camC  workflow/elastoplast/plast/{plast,nonlocal}.jl, retmap/*.jl (+ camC.zip)
 //   run        get_dt/get_g/spacetime    program/utils/physics.jl:21-90, worflow.jl:27-39, 73-85
 // The per-point constitutive arithmetic (eigen, log/exp, DP/J2 returns) is the
 // shared header ep_scalar.h, which the GPU kernels compile too.
@@ -58,6 +58,7 @@ struct eporacle {
     double DelLU[36];
     int piv[6];
     int threads = 1;
+    int nonconverged = 0;   // a return map exceeded its iteration limit in the last retmap
     int err = 0;
     std::string msg;
 };
@@ -591,6 +592,31 @@ static void retmap(eporacle* o) {
                 if (d == 2) ep::finite_rebuild_b<2>(s, o->DelLU, o->piv, &o->eps[4 * p], &o->b[4 * p]);
                 else ep::finite_rebuild_b<3>(s, o->DelLU, o->piv, &o->eps[9 * p], &o->b[9 * p]);
             }
+        } else if (o->cfg.constitutive == EP_CONS_MC || o->cfg.constitutive == EP_CONS_CAMC) {
+            // MCRetMap.jl:1-54 (2d) and camC/camCmodRetMap.jl, restated as in ep_scalar.h; a yielded
+            // point takes ϵ = tensor(Del \ σ, ½) and, in finite strain, b_e = exp(2ϵ)
+            int y;
+            if (o->cfg.constitutive == EP_CONS_MC) {
+                y = ep::mc_return(s, ep2, o->c0[p], o->cr[p], o->sphi[p], o->cphi[p], o->cm.Hp, o->cm.Del, o->DelLU,
+                                  o->piv, &ep1);
+                if (y < 0) o->nonconverged = 1;
+            } else {
+                double ev = o->epV[p];
+                y = (d == 2) ? ep::camc_return<3>(s, ep2, &ev, o->cm.Kc, o->cm.Del, &ep1)
+                             : ep::camc_return<6>(s, ep2, &ev, o->cm.Kc, o->cm.Del, &ep1);
+                if (y > 0) o->epV[p] = ev;
+            }
+            if (y > 0) {
+                o->epII[0 + 2 * p] = ep1;
+                if (fin) {
+                    if (d == 2) ep::finite_rebuild_b<2>(s, o->DelLU, o->piv, &o->eps[4 * p], &o->b[4 * p]);
+                    else ep::finite_rebuild_b<3>(s, o->DelLU, o->piv, &o->eps[9 * p], &o->b[9 * p]);
+                } else if (d == 2) {
+                    ep::strain_from_stress<2>(s, o->DelLU, o->piv, &o->eps[4 * p]);
+                } else {
+                    ep::strain_from_stress<3>(s, o->DelLU, o->piv, &o->eps[9 * p]);
+                }
+            }
         } else {
             int y = (d == 2) ? ep::j2_return<3>(s, ep2, o->c0[p], o->cr[p], o->cm.Hp, o->cm.Del, &ep1)
                              : ep::j2_return<6>(s, ep2, o->c0[p], o->cr[p], o->cm.Hp, o->cm.Del, &ep1);
@@ -609,7 +635,9 @@ static void plast(eporacle* o) {
     if (o->cfg.nonloc) nonlocal(o);
     else
         for (int64_t p = 0; p < o->Np; ++p) o->epII[1 + 2 * p] = o->epII[0 + 2 * p];
+    o->nonconverged = 0;
     retmap(o);
+    if (o->nonconverged) fail(o, EP_ERR_NONCONVERGED, "CPA: return map iteration limit exceeded (MCRetMap.jl:38-41)");
 }
 
 // ---------------------------------------------------------------- API
@@ -698,7 +726,10 @@ int eporacle_step(eporacle* o, int32_t phase, double dt, const double* g, double
     n2p(o, dt);
     update(o, dt);
     elast(o);
-    if (phase == EP_PHASE_ELASTOPLASTIC) plast(o);
+    if (phase == EP_PHASE_ELASTOPLASTIC) {
+        plast(o);
+        if (o->nonconverged) return EP_ERR_NONCONVERGED;
+    }
     if (vmax_out)
         for (int i = 0; i < o->dim; ++i) vmax_out[i] = o->vmax[i];
     return 0;

@@ -17,10 +17,14 @@ Reference files (paths within the ElastoPlasm.jl project):
   smpm.jl    src/home/program/workflow/shpfun/basis/smpm.jl
   DP.jl      src/home/program/workflow/elastoplast/plast/retmap/DP.jl
   J2.jl      src/home/program/workflow/elastoplast/plast/retmap/J2.jl
+  MCRetMap   src/home/program/workflow/elastoplast/plast/retmap/MCRetMap.jl
+  camC       src/home/program/workflow/elastoplast/plast/retmap/camC.zip: camC/camCmodRetMap.jl
   elast.jl   src/home/program/workflow/elastoplast/elast/elast.jl
   setup_cmpr src/home/program/utils/setup/setup_cmpr.jl
 """
 from __future__ import annotations
+
+import math
 
 import numpy as np
 
@@ -347,6 +351,113 @@ def j2_return(s, ep2, c0, cr, Hp, Del, ftol=1e-9, itmax=20):
         n = np.where(act[:, None], n2, n)
         it += 1
     return sig, g, yielded
+
+
+# ---------------------------------------------------------------------------
+# Mohr-Coulomb (MCRetMap.jl:1-54) and modified Cam-Clay (camC.zip: camC/camCmodRetMap.jl), restated
+# with the Solid's fields (the reference's functions are commented out of plast.jl:14-15,28-29);
+# batched over points, s is (n, nstr).  A point leaves the iteration when its own test fails.
+# ---------------------------------------------------------------------------
+def mc_return(s, ep2, c0, cr, sphi, cphi, Hp, Del, ftol=1e-6, itmax=10_000):
+    r"""MCRetMap! on plane-strain Voigt stresses (n, 3): ψ = 0.5°, H = cos ϕ Hp, c = max(c0 + Hp ϵII, cr),
+    f = τII + σm sin ϕ - c cos ϕ on the Mohr circle of (σxx, σyy, σxy); cutting plane
+    Δγ = f / (H + ∂fᵀ Del ∂g), Δσ = Δγ Del ∂g, Δϵ += Del \ Δσ, ϵII = ϵII0 + sqrt(2/3 (Δϵ1² + Δϵ2² + 2Δϵ3²)).
+    Returns (σ', ϵII, status) with status 1 yielded, 0 elastic, -1 over the iteration limit."""
+    psi = 0.5 * math.pi / 180.0
+    spsi = math.sin(psi)
+    sig = np.array(s, dtype=F)
+    e0 = np.asarray(ep2, dtype=F)
+    sphi, cphi = np.asarray(sphi, dtype=F), np.asarray(cphi, dtype=F)
+    H = cphi * Hp
+
+    def circle(x):
+        sm = 0.5 * (x[:, 0] + x[:, 1])
+        return sm, np.sqrt(0.25 * (x[:, 0] - x[:, 1]) ** 2 + x[:, 2] ** 2)
+
+    c = np.maximum(c0 + Hp * e0, cr)
+    sm, tII = circle(sig)
+    f = tII + sm * sphi - c * cphi
+    yielded = f > 0.0
+    act = yielded.copy()
+    de = np.zeros_like(sig)
+    g = e0.copy()
+    status = yielded.astype(np.int32)
+    it = 0
+    while True:
+        act &= np.abs(f) > ftol
+        if not act.any():
+            break
+        it += 1
+        a = (sig[:, 0] - sig[:, 1]) / (4.0 * tII)
+        df = np.stack([a + sphi / 2.0, -a + sphi / 2.0, sig[:, 2] / tII], axis=1)
+        dg = np.stack([a + spsi / 2.0, -a + spsi / 2.0, sig[:, 2] / tII], axis=1)
+        den = np.einsum("ni,ij,nj->n", df, Del, dg)
+        dgam = np.where(act, f / (H + den), 0.0)
+        ds = dgam[:, None] * np.einsum("ij,nj->ni", Del, dg)
+        de = de + np.linalg.solve(Del, ds.T).T
+        g = np.where(act, e0 + np.sqrt((2.0 / 3.0) * (de[:, 0] ** 2 + de[:, 1] ** 2 + 2.0 * de[:, 2] ** 2)), g)
+        c = np.maximum(c0 + Hp * g, cr)
+        sig = np.where(act[:, None], sig - ds, sig)
+        sm2, t2 = circle(sig)
+        f = np.where(act, t2 + sm2 * sphi - c * cphi, f)
+        sm, tII = np.where(act, sm2, sm), np.where(act, t2, tII)
+        if it > itmax:
+            status = np.where(act, -1, status)
+            break
+    return sig, g, status
+
+
+def camc_return(s, ep2, epV, Kc, Del):
+    """camCRetMap! of camCmodRetMap.jl with its constants (χ = 3/2, Pt = Kc/10, a0 = Pt + Kc/10, β = 1,
+    M = 6 sin ϕcs / (3 - sin ϕcs) with ϕcs = 20°, ζ = 0, at most 19 iterations while |f| > 1e-6) and the
+    yield function its derivative and envelope use, f = (P - Pt + a)²/b² + (q/M)² - a².
+    P, q, n as camCParam (2d: P = (σxx+σyy)/2); ∂f/∂σ = ∂f/∂P/3 on the normal components + √χ ∂f/∂q n.
+    Returns (σ', ϵpII, ϵpV, yielded)."""
+    chi, Pt = 1.5, Kc / 10.0
+    a0, beta = Pt + Kc / 10.0, 1.0
+    phics = 20.0 * math.pi / 180.0
+    M = 6.0 * math.sin(phics) / (3.0 - math.sin(phics))
+    sig = np.array(s, dtype=F)
+    nstr = sig.shape[1]
+    nnorm = 2 if nstr == 3 else 3
+    w2 = np.array([1.0, 1.0, 2.0] if nstr == 3 else [1.0, 1.0, 1.0, 2.0, 2.0, 2.0])
+
+    def param(x):
+        P = x[:, :nnorm].sum(axis=1) / nnorm
+        xi = x.copy()
+        xi[:, :nnorm] -= P[:, None]
+        xn = np.sqrt(2.0 * (0.5 * (xi ** 2 * w2).sum(axis=1)))
+        return P, np.sqrt(chi) * xn, xi / xn[:, None]
+
+    def yield_(P, q, a):
+        b = np.where(P < Pt - a, beta, 1.0)
+        return (P - Pt + a) ** 2 / b ** 2 + (q / M) ** 2 - a ** 2, b
+
+    ev = np.array(epV, dtype=F)
+    g = np.array(ep2, dtype=F)
+    a = a0 * np.exp(-0.0 * ev)
+    P, q, n = param(sig)
+    f, b = yield_(P, q, a)
+    yielded = f > 0.0
+    act = yielded.copy()
+    for _ in range(19):
+        act &= np.abs(f) > 1e-6
+        if not act.any():
+            break
+        dfdp = (2.0 / b ** 2) * (P - Pt + a)
+        dfdq = 2.0 * q / M ** 2
+        df = np.sqrt(chi) * dfdq[:, None] * n
+        df[:, :nnorm] += (dfdp / 3.0)[:, None]
+        dl = np.where(act, f / np.einsum("ni,ij,nj->n", df, Del, df), 0.0)
+        sig = np.where(act[:, None], sig - dl[:, None] * np.einsum("ij,nj->ni", Del, df), sig)
+        ev = np.where(act, ev + dl * dfdp, ev)
+        g = np.where(act, g + dl * dfdq, g)
+        a = a0 * np.exp(-0.0 * ev)
+        P2, q2, n2 = param(sig)
+        f2, b2 = yield_(P2, q2, a)
+        P, q, f, b = (np.where(act, u, v) for u, v in ((P2, P), (q2, q), (f2, f), (b2, b)))
+        n = np.where(act[:, None], n2, n)
+    return sig, np.where(yielded, g, ep2), np.where(yielded, ev, epV), yielded
 
 
 # ---------------------------------------------------------------------------

@@ -49,6 +49,26 @@ void probe_j2(int64_t n, int32_t nstr, double* s, const double* ep2, const doubl
     }
 }
 
+// 2d: s (3 per point) in-out; ep1 out; status per point (1 yielded, 0 elastic, -1 not converged)
+void probe_mc(int64_t n, double* s, const double* ep2, const double* c0, const double* cr, const double* sphi,
+              const double* cphi, double Hp, const double* Del, double* ep1, int32_t* status) {
+    double LU[9];
+    int piv[3];
+    for (int i = 0; i < 9; ++i) LU[i] = Del[i];
+    lu_factor<3>(LU, piv);
+    for (int64_t p = 0; p < n; ++p)
+        status[p] = mc_return(s + 3 * p, ep2[p], c0[p], cr[p], sphi[p], cphi[p], Hp, Del, LU, piv, &ep1[p]);
+}
+
+// s (nstr per point) and epV in-out; ep1 out; status per point (1 yielded, 0 elastic)
+void probe_camc(int64_t n, int32_t nstr, double* s, const double* ep2, double* epV, double Kc, const double* Del,
+                double* ep1, int32_t* status) {
+    for (int64_t p = 0; p < n; ++p) {
+        if (nstr == 3) status[p] = camc_return<3>(s + 3 * p, ep2[p], &epV[p], Kc, Del, &ep1[p]);
+        else status[p] = camc_return<6>(s + 6 * p, ep2[p], &epV[p], Kc, Del, &ep1[p]);
+    }
+}
+
 // b in-out (D*D per point); eps (D*D), tau (nstr) out
 void probe_finite_elast(int64_t n, int32_t D, const double* dF, double* b, const double* Del, double* eps,
                         double* tau) {

@@ -119,3 +119,22 @@ def test_field_mask_bits_match_the_header():
     assert {names[k]: v for k, v in bits.items()} == abi.MPTS_BITS
     fields = [f for f, _ in abi.ep_mpts_view._fields_ if f not in ("ndim", "nmp", "vmax", "p2e", "p2n")]
     assert fields == list(abi.MPTS_BITS)
+
+
+def test_julia_binding_mirrors_the_ctypes_structs():
+    """The Julia extension (julia/GB300Ext.jl) declares each ABI struct with the ctypes mirror's fields
+    in the same order and of the same C width (Julia is absent here, so the layout is checked as text
+    against the ctypes mirror, which test_struct_layouts_match_the_header holds to gcc's layout)."""
+    import ctypes as C
+    from epgpu import abi
+    src = open(os.path.join(ROOT, "elastoplasm.jl_gb300", "julia", "GB300Ext.jl")).read()
+    width = {"Int32": 4, "Int64": 8, "Float64": 8, "Ptr{Float64}": 8, "Ptr{UInt8}": 8, "Ptr{Int64}": 8}
+    pairs = {"EpCfg": abi.ep_cfg, "EpCmpr": abi.ep_cmpr, "EpMeshView": abi.ep_mesh_view, "EpMptsView": abi.ep_mpts_view}
+    for jl, S in pairs.items():
+        body = re.search(rf"struct {jl}\n(.*?)\nend", src, re.S).group(1)
+        decl = []
+        for name, typ in re.findall(r"(\w+)::([\w{},]+)", body):
+            m = re.match(r"NTuple\{(\d+),(\w+)\}", typ)
+            decl.append((name, int(m.group(1)) * width[m.group(2)] if m else width[typ]))
+        ours = [(f, C.sizeof(t)) for f, t in S._fields_]
+        assert decl == ours, (jl, decl, ours)

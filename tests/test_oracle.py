@@ -224,3 +224,49 @@ def test_apic_affine_state(oracle_mod):
     assert np.abs(det).max() < 1e-12
     # the symmetric outer product N δ δᵀ: D[0,1] == D[1,0] and D[0,0], D[1,1] >= 0
     assert np.array_equal(D[0, 1], D[1, 0]) and (D[0, 0] >= 0).all() and (D[1, 1] >= 0).all()
+
+
+@pytest.mark.parametrize("deform", ["finite", "infinitesimal"])
+def test_mohr_coulomb_slump_on_the_yield_surface(oracle_mod, deform):
+    """The restated MC return (MCRetMap.jl) in the c1 slump: after an elastoplastic step every point's
+    stress lies on or inside its Mohr-Coulomb surface (the return's ftol, 1e-6 Pa), with the cohesion
+    of its written ϵpII (nonlocal off: the softening input is the accumulated strain)."""
+    fw = {"deform": deform, "trsfr": "std", "C_pf": 1.0, "musl": True, "locking": True, "damping": 0.1}
+    ic, cfg = ic_slump([64.1584, 64.1584 / 4.0], [40, 10], fwrk=fw, plast={"status": True, "constitutive": "MC"},
+                       nonloc={"status": False, "ls": 0.5})
+    o = oracle_mod.Oracle(ic, cfg["instr"])
+    t, _ = o.run(0, 1.0, 10.0, 0.0)
+    t, n = o.run(1, 2.5, 10.0, t)
+    m = o.download()
+    s = m.tau if deform == "finite" else m.sig
+    c = np.maximum(m.c0 + (-3.0e4) * m.epII[0], m.cr)
+    sm = 0.5 * (s[0] + s[1])
+    f = np.sqrt(0.25 * (s[0] - s[1]) ** 2 + s[2] ** 2) + sm * np.sin(m.phi) - c * np.cos(m.phi)
+    yielded = np.abs(f) <= 1e-6                # returned by the last step (earlier ones may have unloaded)
+    assert n > 20 and yielded.sum() > 20 and (m.epII[0] > 0).sum() > 50 and np.isfinite(s).all()
+    assert f.max() <= 1e-6
+    if deform == "finite":
+        # b_e rebuilt from the returned stress: ϵ = ½ log b equals tensor(Del \ τ, ½)
+        from epgpu.ic import get_elastic_stiffness
+        _, _, Del = get_elastic_stiffness(1.0e6, 0.3, 2)
+        e = np.linalg.solve(Del, s)
+        B = np.moveaxis(m.bij, -1, 0).reshape(-1, 2, 2)
+        lam, V = np.linalg.eigh(B[yielded])
+        L = 0.5 * np.einsum("nik,nk,njk->nij", V, np.log(lam), V)
+        assert np.abs(L[:, 0, 0] - e[0, yielded]).max() < 1e-12 and np.abs(L[:, 0, 1] - 0.5 * e[2, yielded]).max() < 1e-12
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_cam_clay_slump_runs(oracle_mod, dim):
+    """The restated modified Cam-Clay return (camC/camCmodRetMap.jl) in the slump: points yield in
+    compression at depth, ϵpV and ϵpII move, and the state stays finite."""
+    L = [64.1584, 64.1584 / 4.0] + ([64.1584 / 4.0] if dim == 3 else [])
+    nel = [40, 10] + ([4] if dim == 3 else [])
+    ic, cfg = ic_slump(L, nel, plast={"status": True, "constitutive": "camC"}, nonloc={"status": False, "ls": 0.5})
+    o = oracle_mod.Oracle(ic, cfg["instr"])
+    t, _ = o.run(0, 0.5, 10.0, 0.0)
+    t, n = o.run(1, 1.0, 10.0, t)
+    m = o.download()
+    assert n > 5 and np.isfinite(m.tau).all() and np.isfinite(m.epV).all()
+    moved = m.epV != 0
+    assert moved.sum() > 20 and (m.epII[0][moved] != 0).all()

@@ -28,6 +28,8 @@ SIGS = {
     "probe_hat": [I64, D_, DBL, D_, D_],
     "probe_dp": [I64, I32, D_, D_, D_, D_, D_, D_, D_, DBL, DBL, DBL, D_, D_],
     "probe_j2": [I64, I32, D_, D_, D_, D_, DBL, D_, D_, I_],
+    "probe_mc": [I64, D_, D_, D_, D_, D_, D_, DBL, D_, D_, I_],
+    "probe_camc": [I64, I32, D_, D_, D_, DBL, D_, D_, I_],
     "probe_finite_elast": [I64, I32, D_, D_, D_, D_, D_],
     "probe_finite_rebuild_b": [I64, I32, D_, D_, D_, D_],
     "probe_infinitesimal_elast": [I64, I32, D_, D_, D_, D_, D_, D_],
@@ -205,6 +207,69 @@ def test_j2_return(probe, pm, nstr):
     scale = np.abs(s).max(axis=1)
     assert (np.abs(out - ref).max(axis=1) / scale).max() < 1e-12
     assert (np.abs(e1 - np.where(yl, g, ep2)) / np.maximum(np.abs(g), 1e-300)).max() < 1e-10
+
+
+def test_mc_return(probe, pm):
+    """MCRetMap.jl restated: elastic points untouched bit for bit, returned ones on the Mohr-Coulomb
+    surface (|f| <= 1e-6 Pa, the reference's ftol) and within 1e-10 of the numpy restatement (Del ∂g and
+    Del \\ Δσ go through BLAS/LAPACK in the reference)."""
+    rng = np.random.default_rng(31)
+    n = 4000
+    _, _, Del = pm.elastic_stiffness(1.0e6, 0.3, 2)
+    P = rng.uniform(-3e5, 2e4, n)
+    R = rng.uniform(0.0, 1.2e5, n)
+    th = rng.uniform(0.0, 2 * np.pi, n)
+    s = np.stack([P + R * np.cos(th), P - R * np.cos(th), R * np.sin(th)], axis=1)
+    phi = np.radians(rng.choice([20.0, 7.5, 30.0], n))
+    sphi, cphi = np.sin(phi), np.cos(phi)
+    c0 = rng.uniform(1e3, 4e4, n)
+    cr = np.full(n, 4.0e3)
+    ep2 = rng.uniform(0.0, 0.2, n)
+    out = np.ascontiguousarray(s.copy())
+    e1 = np.zeros(n)
+    st = np.zeros(n, dtype=np.int32)
+    DelF = np.asfortranarray(Del).ravel(order="F").copy()
+    probe.probe_mc(n, _p(out), _p(ep2), _p(c0), _p(cr), _p(sphi), _p(cphi), -3.0e4, _p(DelF), _p(e1), _p(st))
+    ref, g, sref = pm.mc_return(s, ep2, c0, cr, sphi, cphi, -3.0e4, Del)
+    assert np.array_equal(st, sref) and (st == 1).sum() > 1000 and (st == 0).sum() > 500
+    y = st == 1
+    assert _bits_equal(out[~y], s[~y])
+    scale = np.abs(s).max(axis=1)
+    assert (np.abs(out - ref).max(axis=1) / scale)[y].max() < 1e-10
+    assert (np.abs(e1 - g)[y] / np.maximum(np.abs(g[y]), 1e-300)).max() < 1e-9
+    c = np.maximum(c0 + -3.0e4 * e1, cr)
+    sm = 0.5 * (out[:, 0] + out[:, 1])
+    f = np.sqrt(0.25 * (out[:, 0] - out[:, 1]) ** 2 + out[:, 2] ** 2) + sm * sphi - c * cphi
+    assert np.abs(f[y]).max() <= 1e-6
+
+
+@pytest.mark.parametrize("nstr", [3, 6])
+def test_camc_return(probe, pm, nstr):
+    """camCmodRetMap.jl restated: 19 cutting-plane steps on yielded points (|f| in Pa² stays above
+    1e-6), elastic points untouched bit for bit, returned stress, ϵpII and ϵpV within 1e-9 of the numpy
+    restatement, and the yield function reduced by orders of magnitude."""
+    rng = np.random.default_rng(40 + nstr)
+    n = 4000
+    D = 2 if nstr == 3 else 3
+    K, _, Del = pm.elastic_stiffness(1.0e6, 0.3, D)
+    nn = 2 if nstr == 3 else 3
+    s = rng.normal(size=(n, nstr)) * rng.uniform(1e4, 1.5e5, n)[:, None]
+    s[:, :nn] += rng.uniform(-3.5e5, 1.2e5, n)[:, None]
+    ep2 = rng.uniform(0.0, 0.1, n)
+    epv = rng.uniform(-0.01, 0.01, n)
+    out = np.ascontiguousarray(s.copy())
+    ev = epv.copy()
+    e1 = ep2.copy()
+    st = np.zeros(n, dtype=np.int32)
+    DelF = np.asfortranarray(Del).ravel(order="F").copy()
+    probe.probe_camc(n, nstr, _p(out), _p(ep2), _p(ev), K, _p(DelF), _p(e1), _p(st))
+    ref, g, evr, yl = pm.camc_return(s, ep2, epv, K, Del)
+    assert np.array_equal(st.astype(bool), yl) and yl.sum() > 1000 and (~yl).sum() > 500
+    assert _bits_equal(out[~yl], s[~yl]) and _bits_equal(ev[~yl], epv[~yl]) and _bits_equal(e1[~yl], ep2[~yl])
+    scale = np.abs(s).max(axis=1)
+    assert (np.abs(out - ref).max(axis=1) / scale).max() < 1e-9
+    assert np.abs(e1 - g).max() < 1e-9 * max(np.abs(g).max(), 1.0)
+    assert np.abs(ev - evr).max() < 1e-9 * max(np.abs(evr).max(), 1.0)
 
 
 @pytest.mark.parametrize("D", [2, 3])
