@@ -1711,7 +1711,7 @@ __device__ __forceinline__ bool rm_features32(float e11, float e22, float e12, f
 // and the (features, exact label) pair of the point is appended to the record buffer.
 // FLIP: the last block to finish flips the parity (km_flip's work, one launch less per step).
 // cons_point: list slot k of the step (point p in cell c, stencil axes ax/az)
-template <int BASIS, int ACC>
+template <int BASIS, int ACC, bool ITER = false>
 __device__ __forceinline__ void cons_point(const MCtx& A, int k, int p, int c, const Axis4& ax, const Axis4& az,
                                            int plastic_phase, int& nplastic, bool& emit, float* fx, float* fy,
                                            float* fa) {
@@ -1896,14 +1896,15 @@ __device__ __forceinline__ void cons_point(const MCtx& A, int k, int p, int c, c
                     yielded = dl != 0.f;
                     if (yielded && A.rmode == EP_RMAP_RECORD && fin) emit = rm_label(fx, (double)A.l2g, fy) != 0;
                 }
-            } else if (A.cf.cons == EP_CONS_J2) {
+            } else if constexpr (!ITER) {
                 const float Dl[9] = {A.Del[0], A.Del[1], A.Del[2], A.Del[3], A.Del[4],
                                      A.Del[5], A.Del[6], A.Del[7], A.Del[8]};
                 yielded = j232(tt, ep2, A.P.c0[p], A.P.cr[p], A.Hp, Dl, &newg) != 0;
                 absolute = true;
             } else {
-                // MC / modified Cam-Clay: the iterative returns run as FP64 islands (ep_scalar.h) on the
-                // FP32 trial stress; their absolute tolerances (1e-6 Pa, Pa²) are below FP32 resolution
+                // MC / modified Cam-Clay (the ITER instantiations only, so that the DP and J2 kernels
+                // carry no call): the iterative returns run as FP64 islands (ep_scalar.h) on the FP32
+                // trial stress; their absolute tolerances (1e-6 Pa, Pa²) are below FP32 resolution
                 newg = cons_iterative<3>(A, p, tt, ep2, &yielded);
                 absolute = true;
             }
@@ -1989,7 +1990,7 @@ __device__ __forceinline__ void cons_finish(const MCtx& A, int nplastic) {
 }
 
 // km_cons over the sorted list, one lane per slot
-template <int BASIS, int ACC, bool FLIP = false>
+template <int BASIS, int ACC, bool FLIP = false, bool ITER = false>
 __device__ __forceinline__ void cons_body(const MCtx& A, int bid, int plastic_phase) {
     EP_ACTIVE(A.ctl);
     const int cur = A.ctl->parity;
@@ -2003,16 +2004,16 @@ __device__ __forceinline__ void cons_body(const MCtx& A, int bid, int plastic_ph
         fp = p;
         const int ex = c / A.g.nel[1], ez = c - ex * A.g.nel[1];
         const Axis4 ax = axis4(A.g, 0, ex), az = axis4(A.g, 1, ez);
-        cons_point<BASIS, ACC>(A, k, p, c, ax, az, plastic_phase, nplastic, emit, fx, fy, fa);
+        cons_point<BASIS, ACC, ITER>(A, k, p, c, ax, az, plastic_phase, nplastic, emit, fx, fy, fa);
     }
     cons_emit(A, emit, fx, fy, fa, fp);
     cons_finish<FLIP>(A, nplastic);
 }
 
-template <int BASIS, int ACC, bool FLIP = false>
+template <int BASIS, int ACC, bool FLIP = false, bool ITER = false>
 __global__ void __launch_bounds__(256, 4) km_cons(MCtx A, int plastic_phase) {
     pdl_enter();
-    cons_body<BASIS, ACC, FLIP>(A, blockIdx.x, plastic_phase);
+    cons_body<BASIS, ACC, FLIP, ITER>(A, blockIdx.x, plastic_phase);
 }
 
 
@@ -2058,7 +2059,6 @@ __device__ __noinline__ void rmap_fallback_slot(const MCtx& A, int i) {
 // FLIP: the last block to finish does km_flip's work (parity flip, slot counters emptied)
 template <int ACC, bool FLIP = false>
 __global__ void __launch_bounds__(256) km_rmap_finish(MCtx A) {
-    pdl_enter();
     EP_ACTIVE(A.ctl);
     const int n = *A.rcount;
     int nl = 0, nf = 0;
@@ -3675,7 +3675,7 @@ __device__ __forceinline__ bool rm_features3(const float* eps_in, const float (&
 // Finite strain works in the principal frame of the trial b_e: with the isotropic stiffness the
 // trial Kirchhoff stress, both returns and b_e = exp(2 Del \ τ) (DP.jl:63-66) are coaxial with it.
 // With the learned return map a trial-yielding DP point is handed to the network as in 2d.
-template <int BASIS, int ACC, bool FIN>
+template <int BASIS, int ACC, bool FIN, bool ITER = false>
 __global__ void __launch_bounds__(256, 3) km_cons3(MCtx A, int plastic_phase) {
     using R = typename std::conditional<ACC == 0, double, float>::type;
     EP_ACTIVE(A.ctl);
@@ -3820,7 +3820,7 @@ __global__ void __launch_bounds__(256, 3) km_cons3(MCtx A, int plastic_phase) {
                     }
                     float newg = 0.f;
                     bool y3 = false;
-                    if (A.cf.cons == EP_CONS_J2) y3 = j2f6(tt, ep2, A.P.c0[p], A.P.cr[p], A.Hp, A.Del, &newg) != 0;
+                    if constexpr (!ITER) y3 = j2f6(tt, ep2, A.P.c0[p], A.P.cr[p], A.Hp, A.Del, &newg) != 0;
                     else newg = cons_iterative<6>(A, p, tt, ep2, &y3);      // modified Cam-Clay (FP64 island)
                     if (y3) {
                         ++nplastic;
@@ -3909,7 +3909,7 @@ __global__ void __launch_bounds__(256, 3) km_cons3(MCtx A, int plastic_phase) {
                 } else {
                     float newg = 0.f;
                     bool y3 = false;
-                    if (A.cf.cons == EP_CONS_J2) y3 = j2f6(tt, ep2, A.P.c0[p], A.P.cr[p], A.Hp, A.Del, &newg) != 0;
+                    if constexpr (!ITER) y3 = j2f6(tt, ep2, A.P.c0[p], A.P.cr[p], A.Hp, A.Del, &newg) != 0;
                     else newg = cons_iterative<6>(A, p, tt, ep2, &y3);      // modified Cam-Clay (FP64 island)
                     if (y3) {
                         ++nplastic;
@@ -4453,8 +4453,16 @@ static void mixed_step3_impl(const MixedCtx& X, int phase, cudaStream_t s) {
         ++L;
     }
     if (np > 0) {
-        if (A.cf.deform == EP_DEFORM_FINITE) km_cons3<BASIS, ACC, true><<<gp, 256, 0, s>>>(A, phase == EP_PHASE_ELASTOPLASTIC);
-        else km_cons3<BASIS, ACC, false><<<gp, 256, 0, s>>>(A, phase == EP_PHASE_ELASTOPLASTIC);
+        const int pp = phase == EP_PHASE_ELASTOPLASTIC;
+        const bool iter = A.cf.cons == EP_CONS_CAMC;
+        if (A.cf.deform == EP_DEFORM_FINITE) {
+            if (iter) km_cons3<BASIS, ACC, true, true><<<gp, 256, 0, s>>>(A, pp);
+            else km_cons3<BASIS, ACC, true><<<gp, 256, 0, s>>>(A, pp);
+        } else if (iter) {
+            km_cons3<BASIS, ACC, false, true><<<gp, 256, 0, s>>>(A, pp);
+        } else {
+            km_cons3<BASIS, ACC, false><<<gp, 256, 0, s>>>(A, pp);
+        }
         mark("cons");
         ++L;
         if (A.rmode == EP_RMAP_LEARNED && X.net && phase == EP_PHASE_ELASTOPLASTIC) {
@@ -4590,7 +4598,10 @@ static void mixed_step_impl(const MixedCtx& X, int phase, cudaStream_t s) {
     const bool flip_in_finish = np > 0 && !DET && net;     // the learned map's finish kernel is last
     if (np > 0) {
         const int pp = phase == EP_PHASE_ELASTOPLASTIC;
-        if (flip_in_cons) launch_pdl(km_cons<BASIS, ACC, true>, gp, 256, s, A, pp);
+        const bool iter = A.cf.cons == EP_CONS_MC || A.cf.cons == EP_CONS_CAMC;
+        if (iter && flip_in_cons) launch_pdl(km_cons<BASIS, ACC, true, true>, gp, 256, s, A, pp);
+        else if (iter) launch_pdl(km_cons<BASIS, ACC, false, true>, gp, 256, s, A, pp);
+        else if (flip_in_cons) launch_pdl(km_cons<BASIS, ACC, true>, gp, 256, s, A, pp);
         else launch_pdl(km_cons<BASIS, ACC>, gp, 256, s, A, pp);
         mark("cons");
         ++L;
@@ -4598,8 +4609,10 @@ static void mixed_step_impl(const MixedCtx& X, int phase, cudaStream_t s) {
             mlp_infer(X.net, A.rx, A.rcount, np, A.ry, s);
             mark("mlp");
             const int gf = std::min(gp, 4 * sm_count());
-            if (flip_in_finish) launch_pdl(km_rmap_finish<ACC, true>, gf, 256, s, A);
-            else launch_pdl(km_rmap_finish<ACC>, gf, 256, s, A);
+            // plain launches: as programmatic dependents the network and finish kernels made the
+            // learned step slower (0.162 against 0.157 ms per c2 step)
+            if (flip_in_finish) km_rmap_finish<ACC, true><<<gf, 256, 0, s>>>(A);
+            else km_rmap_finish<ACC><<<gf, 256, 0, s>>>(A);
             mark("rmap_finish");
             L += 2;
         }
@@ -4742,6 +4755,8 @@ void* mixed_batch_create(const MixedCtx* const* xs, int n, std::string* why) {
     for (int i = 0; i < n; ++i) {
         const MCtx& A = *(const MCtx*)xs[i]->impl;
         if (A.g.dim != 2) return no("the persistent batch kernel runs 2d instances");
+        if (A.cf.cons == EP_CONS_MC || A.cf.cons == EP_CONS_CAMC)
+            return no("the MC and Cam-Clay returns run on the per-instance graphs");
         if (A.cf.det || A.cf.nonloc || A.rmode != EP_RMAP_EXACT)
             return no("deterministic mode, nonlocal averaging and the learned map run on the per-instance graphs");
         if (basis < 0) {

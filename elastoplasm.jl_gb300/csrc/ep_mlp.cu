@@ -14,7 +14,6 @@
 
 #include <algorithm>
 #include <cmath>
-#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -71,22 +70,26 @@ __device__ __forceinline__ float dsilu(float z) {
     return s * (1.f + z * (1.f - s));
 }
 
-// named barriers of one 256-thread group (ids 1 and 2; 0 is __syncthreads)
-__device__ __forceinline__ void grp_sync(int id) { asm volatile("bar.sync %0, 256;" ::"r"(id) : "memory"); }
+// named barriers of one NT-thread group (ids 1 .. ; 0 is __syncthreads)
+template <int NT>
+__device__ __forceinline__ void grp_sync(int id) { asm volatile("bar.sync %0, %1;" ::"r"(id), "n"(NT) : "memory"); }
+template <int NT>
 __device__ __forceinline__ bool grp_sync_and(int id, bool v) {
     int r;
-    asm volatile("{\n\t.reg .pred p, q;\n\tsetp.ne.s32 p, %1, 0;\n\tbar.red.and.pred q, %2, 256, p;\n\tselp.s32 %0, 1, 0, q;\n\t}"
+    asm volatile("{\n\t.reg .pred p, q;\n\tsetp.ne.s32 p, %1, 0;\n\tbar.red.and.pred q, %2, %3, p;\n\tselp.s32 %0, 1, 0, q;\n\t}"
                  : "=r"(r)
-                 : "r"((int)v), "r"(id)
+                 : "r"((int)v), "r"(id), "n"(NT)
                  : "memory");
     return r != 0;
 }
 
 // ---------------------------------------------------------------------------
-// forward, fused over the five layers; one CTA (24 warps) per SM, FWD_GROUPS = 3 groups of 8
-// warps each walking its own tiles of 128 rows, so that the groups' epilogues overlap each
-// other's MMAs.  Warp w of a group reads TMEM lanes 32 (w % 4) .. + 31 (its rows) and the
-// column half (w % 8) / 4 of every accumulator of its group.
+// forward, fused over the five layers; one CTA (32 warps) per SM, FWD_GROUPS = 2 groups of
+// FWD_GW = 16 warps each walking its own tiles of 128 rows, so that the groups' epilogues overlap
+// each other's MMAs.  Warp w of a group reads TMEM lanes 32 (w % 4) .. + 31 (its rows) and the
+// column quarter (w % 16) / 4 of every accumulator of its group (32 columns: two 16-column loads
+// per layer and thread).  The step's launches hold a tile or two per CTA, so the epilogue of one
+// tile is the critical path: 16 warps per tile halve it against 8.
 struct FwdArgs {
     const float* X;       // rows of RM_NX floats (the first 6 are the inputs)
     int n;                // rows, or (ndev != nullptr) the capacity
@@ -98,24 +101,24 @@ struct FwdArgs {
     int* err;             // set to 1 when a wait times out
 };
 
-// FWD_GROUPS 128-row tiles in flight per CTA: group g (warps 8g .. 8g + 7) owns activation buffer
-// FWD_SH + g and input buffer FWD_SX + g, the hidden-layer accumulator in TMEM columns 128 g ..
-// 128 g + 127, the output accumulator in columns 384 + 32 g .. + 15, and mbarrier 1 + g; the weights
-// are shared
-constexpr int FWD_GROUPS = 3;
+// FWD_GROUPS 128-row tiles in flight per CTA: group g (warps FWD_GW g .. FWD_GW (g + 1) - 1) owns
+// activation buffer FWD_SH + g and input buffer FWD_SX + g, the hidden-layer accumulator in TMEM
+// columns 128 g .. 128 g + 127, the output accumulator in columns 384 + 32 g .. + 15, and mbarrier
+// 1 + g; the weights are shared
+constexpr int FWD_GROUPS = 2;
+constexpr int FWD_GW = 16;                     // warps per group (a multiple of 4: the TMEM lane quarters)
+constexpr int FWD_GT = 32 * FWD_GW;            // threads per group
+constexpr int FWD_COLS = W / (FWD_GW / 4);     // accumulator columns of one warp
 constexpr int FWD_SH = 0, FWD_SX = FWD_SH + FWD_GROUPS * MT * W * 2, FWD_SW = FWD_SX + FWD_GROUPS * MT * KIN * 2;
 constexpr int FWD_BAR = FWD_SW + IMG_BYTES, FWD_SMEM = FWD_BAR + 48;
 static_assert(FWD_SW % 128 == 0 && FWD_BAR % 8 == 0, "shared layout alignment");
 static_assert(FWD_SMEM <= 232448, "shared memory of one CTA");
 static_assert(128 * FWD_GROUPS <= 384 && 384 + 32 * FWD_GROUPS <= 512, "TMEM columns of the groups");
 
-constexpr int FWD_THREADS = 256 * FWD_GROUPS;
+constexpr int FWD_THREADS = FWD_GT * FWD_GROUPS;
+static_assert(FWD_THREADS <= 1024 && FWD_COLS % 16 == 0 && FWD_GT >= MT, "group shape");
 
 __global__ void __launch_bounds__(FWD_THREADS, 1) km_mlp_fwd(FwdArgs a) {
-    // inside the mixed step the kernel is launched as a programmatic dependent of the constitutive
-    // kernel: wait for its slots and count before the first read (a no-op for a plain launch)
-    asm volatile("griddepcontrol.wait;" ::: "memory");
-    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     extern __shared__ __align__(128) uint8_t sm[];
     uint8_t* sW = sm + FWD_SW;
     uint64_t* bar = reinterpret_cast<uint64_t*>(sm + FWD_BAR);       // [0] weights, [1 + g] group g's MMAs
@@ -147,7 +150,7 @@ __global__ void __launch_bounds__(FWD_THREADS, 1) km_mlp_fwd(FwdArgs a) {
     ok = __syncthreads_and(ok);
     // group g: its own tiles, buffers, accumulator columns and barrier; the two groups' MMAs
     // queue on the tensor core while the other group runs its epilogue
-    const int g = warp >> 3, gt = tid & 255, gw = warp & 7;
+    const int g = warp / FWD_GW, gt = tid % FWD_GT, gw = warp % FWD_GW;
     uint8_t* sH = sm + FWD_SH + g * (MT * W * 2);
     uint8_t* sX = sm + FWD_SX + g * (MT * KIN * 2);
     uint64_t* gbar = &bar[1 + g];
@@ -156,7 +159,7 @@ __global__ void __launch_bounds__(FWD_THREADS, 1) km_mlp_fwd(FwdArgs a) {
     const float* bias = reinterpret_cast<const float*>(sW + IBIAS);
     const uint32_t aX = tc::smem_u32(sX), aH = tc::smem_u32(sH), aW = tc::smem_u32(sW);
     const uint32_t id128 = tc::idesc_bf16(MT, W), id16 = tc::idesc_bf16(MT, NO);
-    const int q = gw & 3, ch = gw >> 2;            // lane quarter, column half (64 columns)
+    const int q = gw & 3, ch = gw >> 2;            // lane quarter, column block (FWD_COLS columns)
     const int row = 32 * q + lane;
     const uint32_t trow = tbase + ((uint32_t)(32 * q) << 16);
     uint32_t ph = 0;
@@ -182,7 +185,7 @@ __global__ void __launch_bounds__(FWD_THREADS, 1) km_mlp_fwd(FwdArgs a) {
         }
         tc::fence_async_smem();
         tc::fence_before_sync();
-        grp_sync(1 + g);
+        grp_sync<FWD_GT>(1 + g);
         if (gt == 0) {
             tc::fence_after_sync();
             tc::mma_bf16(tbase, tc::sdesc(aX, 128, 256), tc::sdesc(aW + IW1, 128, 256), id128, 0);
@@ -191,14 +194,14 @@ __global__ void __launch_bounds__(FWD_THREADS, 1) km_mlp_fwd(FwdArgs a) {
         for (int l = 1; l <= 4; ++l) {
             ok = tc::mbar_wait(gbar, ph);
             ph ^= 1;
-            ok = grp_sync_and(1 + g, ok);
+            ok = grp_sync_and<FWD_GT>(1 + g, ok);
             if (!ok) break;
             tc::fence_after_sync();
             const float* b = bias + (l - 1) * W;
             const int r = r0 + row;
 #pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                const int col = 64 * ch + 16 * c;
+            for (int c = 0; c < FWD_COLS / 16; ++c) {
+                const int col = FWD_COLS * ch + 16 * c;
                 float v[16], bb[16];
                 tc::tmem_ld16(trow + (uint32_t)col, v);
 #pragma unroll
@@ -231,7 +234,7 @@ __global__ void __launch_bounds__(FWD_THREADS, 1) km_mlp_fwd(FwdArgs a) {
             }
             tc::fence_async_smem();
             tc::fence_before_sync();
-            grp_sync(1 + g);
+            grp_sync<FWD_GT>(1 + g);
             if (gt == 0) {
                 tc::fence_after_sync();
                 const bool last = l == 4;
@@ -245,7 +248,7 @@ __global__ void __launch_bounds__(FWD_THREADS, 1) km_mlp_fwd(FwdArgs a) {
         if (!ok) break;
         ok = tc::mbar_wait(gbar, ph);
         ph ^= 1;
-        ok = grp_sync_and(1 + g, ok);
+        ok = grp_sync_and<FWD_GT>(1 + g, ok);
         if (!ok) break;
         tc::fence_after_sync();
         if (ch == 0) {
@@ -258,7 +261,7 @@ __global__ void __launch_bounds__(FWD_THREADS, 1) km_mlp_fwd(FwdArgs a) {
             }
         }
         tc::fence_before_sync();
-        grp_sync(1 + g);
+        grp_sync<FWD_GT>(1 + g);
     }
     if (!ok && gt == 0 && a.err) atomicExch(a.err, 1);
     tc::fence_before_sync();
@@ -680,24 +683,7 @@ static void mlp_fwd_launch(ep_mlp* m, const float* X, int n, const int* ndev, fl
     a.err = m->d.err;
     const int tiles = (n + MT - 1) / MT;
     const int grid = ndev ? m->sms : std::max(1, std::min((tiles + FWD_GROUPS - 1) / FWD_GROUPS, m->sms));
-    if (!ndev) {
-        km_mlp_fwd<<<grid, FWD_THREADS, FWD_SMEM, s>>>(a);
-        return;
-    }
-    // the step's inference: a programmatic dependent launch (scheduled while the constitutive kernel
-    // drains; the kernel waits for it before reading), unless EPGPU_PDL=0
-    const char* e = getenv("EPGPU_PDL");
-    cudaLaunchConfig_t c = {};
-    c.gridDim = dim3((unsigned)grid);
-    c.blockDim = dim3((unsigned)FWD_THREADS);
-    c.dynamicSmemBytes = FWD_SMEM;
-    c.stream = s;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    at[0].val.programmaticStreamSerializationAllowed = (e && e[0] == '0') ? 0 : 1;
-    c.attrs = at;
-    c.numAttrs = 1;
-    cudaLaunchKernelEx(&c, km_mlp_fwd, a);
+    km_mlp_fwd<<<grid, FWD_THREADS, FWD_SMEM, s>>>(a);
 }
 
 void mlp_infer(ep_mlp* m, const float* X, const int* ndev, int cap, float* Y, cudaStream_t s) {
