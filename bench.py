@@ -301,7 +301,7 @@ def run_reference(args, rank, ws):
     print(json.dumps(line))
 
 
-def batch_bench(args, rank, ws):
+def batch_bench(args, rank, ws, emit=True):
     """The batched ensemble (256 uneven slumps): particle-steps/s of one batch window."""
     import torch
     from epgpu.batch import Batch, slump_ensemble
@@ -357,8 +357,24 @@ def batch_bench(args, rank, ws):
         "gpu_launches": None, "batch_graph_launches": st["graph_launches"], "clocks": clk.summary(),
     }
     b.close()
-    if rank == 0:
+    if rank == 0 and emit:
         print(json.dumps(line))
+    return line
+
+
+def c4_summary(args, rank, ws):
+    """A reduced batched ensemble (config 4's draw of uneven 2d slumps, fewer instances) reported beside
+    the 2d headline: the rate of the autotuned scheme, the scheme and tile it chose, and the others."""
+    a = copy.copy(args)
+    a.instances = args.c4_instances
+    a.settle = 0.1
+    a.window = 0.05
+    line = batch_bench(a, rank, ws, emit=False)
+    c = line["config"]
+    return {"workload": c["workload"], "instances": c["instances"], "points": c["points"],
+            "value": line["value"], "unit": "particle-steps/s", "ms_per_batch_step": line["ms_per_step"],
+            "scheme": c["scheme"], "p2g_tile": c["p2g_tile"], "other_schemes": c["other_schemes"],
+            "steps_per_instance": c["steps_per_instance"], "window_s": a.window}
 
 
 def c3_bench(args, rank, ws):
@@ -528,21 +544,36 @@ def c5_bench(args, rank, ws, emit=True):
     final = e.download()
     value = np_ * args.steps / (ms * 1e-3)
     tot = sum(v[1] for v in kt.values())
-    exact = None
+    exact = final_x = dts_x = None
     if learned:
         e.set_return_map(None, "exact")
-        ms_x, _, _, _ = timed(e, args.steps, args.warmup)
+        ms_x, dts_x, _, _ = timed(e, args.steps, args.warmup)
+        final_x = e.download()
         exact = {"value": np_ * args.steps / (ms_x * 1e-3), "unit": "particle-steps/s", "ms_per_step": ms_x / args.steps}
     e.close()
     instr64 = dict(cfg["instr"])
     instr64["gpu"] = {"precision": "fp64", "jaumann": False}
-    e64 = Engine({"mesh": mesh, "mpts": host0.copy(), "cmpr": cmpr}, instr64)
-    t64 = 0.0
-    for dt in dts:
-        e64.step(1, dt, g)
-        t64 += e64.stats()["device_ms"]
-    b = e64.download()
-    e64.close()
+
+    def fp64_replay(seq):
+        """The FP64 step from the same start state with the same dt sequence."""
+        e64 = Engine({"mesh": mesh, "mpts": host0.copy(), "cmpr": cmpr}, instr64)
+        tt = 0.0
+        for dt in seq:
+            e64.step(1, dt, g)
+            tt += e64.stats()["device_ms"]
+        out = e64.download()
+        e64.close()
+        return out, tt
+
+    b, t64 = fp64_replay(dts)
+    if exact is not None:
+        # the exact-map mixed run against the FP64 step: what the lattice's conditioning leaves to any
+        # FP32 arithmetic, beside the learned run's error
+        bx, _ = fp64_replay(dts_x)
+        exact["error_vs_fp64"] = {
+            "steps": len(dts_x),
+            "stress_rel_l2": float(np.linalg.norm(final_x.tau - bx.tau) / np.linalg.norm(bx.tau)),
+            "displacement_rel_l2": float(np.linalg.norm(final_x.x - bx.x) / max(np.linalg.norm(bx.x - host0.x), 1e-300))}
     v64 = np_ * len(dts) / (t64 * 1e-3)
     bf = bf16_peak()
     mlp = None
@@ -616,7 +647,11 @@ def main():
     ap.add_argument("--rmap", default="learned", choices=["learned", "exact"],
                     help="return map of the mixed step: the learned one (pairs recorded during the settle, "
                          "trained on the GPU) or the exact one")
-    ap.add_argument("--pairs", type=int, default=16_000_000, help="record buffer capacity (pairs)")
+    ap.add_argument("--pairs", type=int, default=52_000_000, help="record buffer capacity (pairs)")
+    ap.add_argument("--pairs-target", type=int, default=50_000_000,
+                    help="training-set size: after the settle the exact map keeps recording (from a copy of the "
+                         "run past the timed state) until this many pairs exist or --record-limit is reached")
+    ap.add_argument("--record-limit", type=float, default=5.0, help="simulated seconds the recording may run to")
     ap.add_argument("--train-iters", type=int, default=3000)
     ap.add_argument("--seed", type=int, default=5)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
@@ -636,6 +671,8 @@ def main():
     ap.add_argument("--c5-nel", default="160,40,40",
                     help="cells of the reduced config-5 slump whose learned-map step is reported beside the 2d "
                          "headline ('' to skip)")
+    ap.add_argument("--c4-instances", type=int, default=48,
+                    help="instances of the reduced batched ensemble reported beside the 2d headline (0 to skip)")
     ap.add_argument("--clocks-out", default=None,
                     help="folder for the nvidia-smi clock samples (default: a temporary folder)")
     args = ap.parse_args()
@@ -677,7 +714,13 @@ def main():
     if args.settle > 0:
         e.run(1, args.settle, 10.0, 0.0)          # the device time loop (epgpu_run) up to t = settle
         host0 = e.download()
+    t_rec = args.settle
     if learned:
+        # the training set: pairs of the exact FP64 return recorded during the settle and, past the
+        # state the timed steps start from (host0, uploaded again before timing), until the configured
+        # number of pairs is reached
+        while e.return_map_stats()["recorded"] < args.pairs_target and t_rec < args.record_limit:
+            t_rec, _ = e.run(1, min(t_rec + 0.25, args.record_limit), 10.0, t_rec)
         nrec = e.return_map_stats()["recorded"]
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -686,6 +729,7 @@ def main():
         l3 = net.train(iters=args.train_iters // 2, batch=16384, lr=4e-5, seed=3)
         torch.cuda.synchronize()
         train = {"pairs_recorded": int(nrec), "pairs_kept": int(min(nrec, args.pairs)),
+                 "recorded_from_t_s": 0.0, "recorded_to_t_s": t_rec,
                  "iterations": 2 * args.train_iters, "batch": 16384,
                  "seconds": time.perf_counter() - t0, "loss": [l1, l2, l3]}
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")   # 256 MB > 129 MB L2
@@ -881,10 +925,12 @@ def main():
         val, threads, steps, el = cpu_sample(ic2, cfg2, seconds_budget=args.cpu_seconds)
         cpu = {"value": val, "unit": "particle-steps/s", "cores": threads, "kind": "port",
                "sample": f"{steps} elastoplastic steps of the same workload, FP64 restatement on {threads} threads"}
-    c5 = None
+    c5 = c4 = None
     if learned and args.c5_nel and args.workload == "c2":
         e.close()
         c5 = c5_summary(args, rank, ws)
+    if args.c4_instances > 0 and args.workload == "c2":
+        c4 = c4_summary(args, rank, ws)
     if rank == 0:
         rm = None
         if learned:
@@ -909,7 +955,7 @@ def main():
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
             "error_vs_fp64": check, "fp64_step": fp64, "other_precision": other, "conservation": conservation,
             "speedup_vs_fp64_step": (value / fp64["value"]) if fp64 else None,
-            "learned_return_map": rm, "c5_learned_reduced": c5,
+            "learned_return_map": rm, "c5_learned_reduced": c5, "c4_batch_reduced": c4,
             "clocks": clk.summary(),
         }
         print(json.dumps(line))
