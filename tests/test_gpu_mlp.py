@@ -52,8 +52,10 @@ def test_gradient_matches_oracle():
         e_bf = _rel(g[o:o + k], gref[o:o + k])
         e_64 = _rel(g[o:o + k], g64[o:o + k])
         print(f"grad {name}: vs BF16 restatement {e_bf:.2e}, vs FP64 {e_64:.2e}")
-        assert e_bf < 5e-4, name
-        assert e_64 < 6e-2, name
+        # measured: 2.6e-5 - 1.5e-4 against the BF16 restatement (its FP32 sums run in another order),
+        # 4.7e-3 - 1.3e-2 against FP64 (the BF16 rounding of activations and weights)
+        assert e_bf < 3e-4, name
+        assert e_64 < 3e-2, name
         o += k
 
 
