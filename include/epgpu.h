@@ -365,8 +365,8 @@ ep_status epgpu_bin_cells_noalloc(int32_t dim, const int64_t* nel, const double*
  * deterministic mode, no nonlocal averaging) and the same basis and precision,
  * each phase of the step walks the blocks of all instances, either as one
  * persistent cooperative kernel (grid barriers between the phases; scheme 1) or as
- * one kernel per phase (scheme 2, the default); the autotuner picks between them.
- * Otherwise (scheme 0) each instance keeps its 16-step graph and the batch graph
+ * one kernel per phase (scheme 2, the default).  Otherwise, or when the autotuner finds
+ * it faster, (scheme 0) each instance keeps its 16-step graph and the batch graph
  * holds those graphs as independent child nodes. */
 typedef struct ep_batch ep_batch;
 
@@ -380,9 +380,9 @@ ep_status epgpu_batch_download(ep_batch* b, int32_t i, ep_mpts_view* m);
  * t_inout[i] = T (or where an error stopped it) and nsteps_out[i] its steps. */
 ep_status epgpu_batch_run(ep_batch* b, int32_t phase, double T, double tg, double* t_inout, int64_t* nsteps_out);
 /* Autotuner of the mixed step: times dt = 0 steps (they leave the state unchanged)
- * of all instances with P2G tiles of 16, 32 and 64 cells per CTA -- on the persistent
- * kernel and on the phase kernels when the batch qualifies, else on the instances'
- * own step graphs -- and keeps the fastest scheme and tile; ms_out (3) receives the
+ * of all instances with P2G tiles of 16, 32 and 64 cells per CTA -- on the instances'
+ * own step graphs and, when the batch qualifies, on the persistent kernel and on the
+ * phase kernels -- and keeps the fastest scheme and tile; ms_out (3) receives the
  * mean batch-step time of each tile in the chosen scheme. */
 ep_status epgpu_batch_autotune(ep_batch* b, int32_t phase, int32_t* tile_out, double* ms_out);
 /* The scheme the batch runs: 0 per-instance graphs, 1 persistent kernel, 2 phase kernels. */
