@@ -76,7 +76,8 @@ struct ep_handle {
     int rm_mode = 0;
     double* sums = nullptr;       // conservation sums: per-block partials, then the totals
     uint64_t have = 0;            // EP_MPTS_* arrays uploaded at least once
-    bool staging_fresh = false;   // mixed precisions: the FP64 staging layout holds the current state
+    uint64_t fresh = 0;           // mixed precisions: the staging arrays (EP_MPTS_* bits) that hold the
+                                  // current state (a step clears it; exports and uploads set bits)
 };
 
 void ep::set_global_error(const char* msg) { g_create_error = msg ? msg : ""; }
@@ -836,11 +837,15 @@ ep_status epgpu_upload_fields(ep_handle* h, const ep_mpts_view* m, uint64_t mask
     const uint64_t missing = reads_of(h) & ~(mask | h->have);
     if (missing) return fail(h, EP_ERR_ARG, "fields read by the step were never uploaded: " + mask_names(missing));
     // the arrays outside the mask keep their device values: in the mixed precisions those live in the
-    // step's own layout, so the staging layout the import reads is brought up to date first
-    if (h->mixed && h->uploaded && !h->staging_fresh) {
-        mixed_export(h->mx, h->ctx.P, h->ctx.N, h->s, false);
-        CK(h, cudaGetLastError());
-        h->staging_fresh = true;
+    // step's own layout and the import converts only the uploaded ones, but it rebuilds the cell lists
+    // from the staging positions, which are brought up to date first when they are not uploaded
+    if (h->mixed && h->uploaded) {
+        const uint64_t need = EP_MPTS_X & ~mask & ~h->fresh;
+        if (need) {
+            mixed_export(h->mx, h->ctx.P, h->ctx.N, h->s, false, need, false);
+            CK(h, cudaGetLastError());
+            h->fresh |= need;
+        }
     }
     ep_mpts_view v = *m;
     for (const ViewField& f : VIEW_FIELDS)
@@ -889,11 +894,12 @@ static ep_status upload_view(ep_handle* h, const ep_mpts_view* m) {
         h->hctl->vmax_bits[i] = (unsigned long long)bits;
     }
     CK(h, cudaMemcpyAsync(h->ctl, h->hctl, sizeof(Ctl), cudaMemcpyHostToDevice, h->s));
-    if (h->mixed) mixed_import(h->mx, h->ctx.P, h->s);
+    // the mixed layout takes the uploaded arrays only (the others keep their device values)
+    if (h->mixed) mixed_import(h->mx, h->ctx.P, h->s, view_mask(m));
     CK(h, cudaStreamSynchronize(h->s));
     CK(h, cudaGetLastError());
     h->uploaded = true;
-    h->staging_fresh = true;
+    h->fresh |= view_mask(m);
     h->have |= view_mask(m);
     return EP_OK;
 }
@@ -950,12 +956,13 @@ ep_status epgpu_step(ep_handle* h, int32_t phase, double dt, const double* g, do
     if (!h->uploaded) return fail(h, EP_ERR_STATE, "step before upload");
     if (phase != 0 && phase != 1) return fail(h, EP_ERR_ARG, "phase must be 0 or 1");
     ep_status st;
-    if ((st = read_ctl(h)) != EP_OK) return st;
-    h->hctl->dt = dt;
-    for (int i = 0; i < 3; ++i) h->hctl->g[i] = i < h->dim ? g[i] : 0.0;
-    h->hctl->phase = phase;
     if (!h->prof.on && (st = build_step_graph(h, phase)) != EP_OK) return st;
-    CK(h, cudaMemcpyAsync(h->ctl, h->hctl, sizeof(Ctl), cudaMemcpyHostToDevice, h->s));
+    // the step's dt, g and phase into the device control block by a one-thread kernel (no host round
+    // trip: the block's other fields are the device's own, read back after the step)
+    double gg[3];
+    for (int i = 0; i < 3; ++i) gg[i] = i < h->dim ? g[i] : 0.0;
+    launch_ctl_set_step(h->ctl, dt, gg, phase, h->s);
+    CK(h, cudaGetLastError());
     CK(h, cudaEventRecord(h->ev0, h->s));
     if (!h->prof.on) {
         CK(h, cudaGraphLaunch(h->step_graph[phase], h->s));
@@ -985,7 +992,7 @@ ep_status epgpu_step(ep_handle* h, int32_t phase, double dt, const double* g, do
     cudaEventElapsedTime(&ms, h->ev0, h->ev1);
     h->last_ms = ms;
     h->steps += 1;
-    h->staging_fresh = false;
+    h->fresh = 0;
     if (vmax_out)
         for (int i = 0; i < h->dim; ++i) vmax_out[i] = bits_to_double(h->hctl->vmax_bits[i]);
     return kernel_error(h);
@@ -1048,7 +1055,7 @@ ep_status epgpu_run(ep_handle* h, int32_t phase, double T, double tg, double* t_
     *t_inout = h->hctl->t;
     h->t = h->hctl->t;
     h->steps += h->hctl->nsteps;
-    h->staging_fresh = false;
+    h->fresh = 0;
     if (nsteps_out) *nsteps_out = h->hctl->nsteps;
     return kernel_error(h);
 }
@@ -1099,9 +1106,11 @@ static ep_status download_view(ep_handle* h, ep_mpts_view* m, bool need_eps) {
     const int d = h->dim;
     ep_status st;
     if (h->mixed && h->uploaded) {
-        mixed_export(h->mx, h->ctx.P, h->ctx.N, h->s, need_eps);
+        // the requested point arrays only (the nodal fields are download_mesh's)
+        const uint64_t want = view_mask(m);
+        mixed_export(h->mx, h->ctx.P, h->ctx.N, h->s, need_eps, want, false);
         CK(h, cudaGetLastError());
-        h->staging_fresh = true;
+        h->fresh |= want;
     }
     if ((st = read_ctl(h)) != EP_OK) return st;
     // one k_xfer into the mapped host buffers; the other fields transposed into staging, then
@@ -1201,7 +1210,7 @@ ep_status epgpu_fields(ep_handle* h, uint32_t what, double* out) {
     if (h->mixed) {
         mixed_export(h->mx, h->ctx.P, h->ctx.N, h->s);
         CK(h, cudaGetLastError());
-        h->staging_fresh = true;
+        h->fresh = EP_MPTS_ALL;
     }
     FieldSrc S;
     const double* sig = fld_ptr(h, F_SIG);
@@ -1239,7 +1248,7 @@ ep_status epgpu_download_mesh(ep_handle* h, ep_mesh_fields* f) {
     if (h->mixed && h->uploaded) {
         mixed_export(h->mx, h->ctx.P, h->ctx.N, h->s, false);
         CK(h, cudaGetLastError());
-        h->staging_fresh = true;
+        h->fresh = EP_MPTS_ALL;
     }
     std::vector<double> buf((size_t)(1 + 4 * d + 1) * Nn);
     CK(h, cudaMemcpyAsync(buf.data(), h->nbuf, buf.size() * sizeof(double), cudaMemcpyDeviceToHost, h->s));
@@ -1372,7 +1381,7 @@ ep_status epgpu_conservation(ep_handle* h, ep_conservation* out) {
     if (h->mixed) {
         mixed_export(h->mx, h->ctx.P, h->ctx.N, h->s, false);
         CK(h, cudaGetLastError());
-        h->staging_fresh = true;
+        h->fresh = EP_MPTS_ALL;
     }
     const P64& P = h->ctx.P;
     const N64& N = h->ctx.N;
@@ -1749,7 +1758,7 @@ ep_status epgpu_batch_run(ep_batch* b, int32_t phase, double T, double tg, doubl
         h->launches += launched * (b->used_scheme() != 0 ? 1 : h->graph_kernels[phase]);
         h->t = h->hctl->t;
         h->steps += h->hctl->nsteps;
-        h->staging_fresh = false;
+        h->fresh = 0;
         t_inout[i] = h->hctl->t;
         if (nsteps_out) nsteps_out[i] = h->hctl->nsteps;
     }

@@ -836,6 +836,18 @@ void launch_ctl_begin_run(Ctl* ctl, const Geo& g, double c, cudaStream_t s) {
     k_ctl_begin_run<<<1, 1, 0, s>>>(ctl, g.dim, g.h[0], g.h[1], g.h[2], c);
 }
 void launch_ctl_begin_step(Ctl* ctl, int, cudaStream_t s) { k_ctl_begin_step<<<1, 1, 0, s>>>(ctl); }
+
+// the caller's dt, g and phase of one step into the control block (its other fields stay the device's)
+__global__ void k_ctl_set_step(Ctl* c, double dt, double g0, double g1, double g2, int phase) {
+    c->dt = dt;
+    c->g[0] = g0;
+    c->g[1] = g1;
+    c->g[2] = g2;
+    c->phase = phase;
+}
+void launch_ctl_set_step(Ctl* ctl, double dt, const double* g, int phase, cudaStream_t s) {
+    k_ctl_set_step<<<1, 1, 0, s>>>(ctl, dt, g[0], g[1], g[2], phase);
+}
 void launch_ctl_end(Ctl* ctl, cudaStream_t s) { k_ctl_end<<<1, 1, 0, s>>>(ctl); }
 
 // ---------------------------------------------------------------------------

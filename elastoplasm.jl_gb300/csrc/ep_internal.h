@@ -142,13 +142,18 @@ long long* mlp_record_count(ep_mlp* m);
 long long mlp_record_cap(ep_mlp* m);
 void launch_mixed_scan(const MixedCtx& X, cudaStream_t s);
 void mixed_initial_scan(const MixedCtx& X, cudaStream_t s);
-void mixed_import(const MixedCtx& X, const P64& Q, cudaStream_t s);
-// the FP64 staging state from the mixed state; need_eps = false skips the log strain ϵ = ½ log b
-void mixed_export(const MixedCtx& X, const P64& Q, const N64& QN, cudaStream_t s, bool need_eps = true);
+// the staging fields in `mask` (EP_MPTS_* bits) into the mixed layout, then the cell lists rebuilt from
+// the staging positions (which must be current)
+void mixed_import(const MixedCtx& X, const P64& Q, cudaStream_t s, uint64_t mask = EP_MPTS_ALL);
+// the FP64 staging state from the mixed state: the point arrays in `mask` (need_eps = false skips the
+// log strain ϵ = ½ log b) and, with `nodes`, the nodal fields of the last step
+void mixed_export(const MixedCtx& X, const P64& Q, const N64& QN, cudaStream_t s, bool need_eps = true,
+                  uint64_t mask = EP_MPTS_ALL, bool nodes = true);
 
 // control-block kernels (ep_fp64.cu)
 void launch_ctl_begin_run(Ctl* ctl, const Geo& g, double c, cudaStream_t s);
 void launch_ctl_begin_step(Ctl* ctl, int dim, cudaStream_t s);
+void launch_ctl_set_step(Ctl* ctl, double dt, const double* g, int phase, cudaStream_t s);
 void launch_ctl_end(Ctl* ctl, cudaStream_t s);
 
 }  // namespace ep

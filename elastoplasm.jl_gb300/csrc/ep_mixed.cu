@@ -2589,61 +2589,75 @@ __device__ __forceinline__ void cell_dec(const Geo& g, int c, int* e) {
 __device__ __forceinline__ int sym_i(int D, int k) { return D == 2 ? (k == 2 ? 0 : k) : (k < 3 ? k : (k == 3 ? 1 : 0)); }
 __device__ __forceinline__ int sym_j(int D, int k) { return D == 2 ? (k == 2 ? 1 : k) : (k < 3 ? k : (k == 5 ? 1 : 2)); }
 
-__global__ void km_import(MCtx A, P64 Q) {
+// The staging fields in `mask` (EP_MPTS_* bits of the arrays they come from) into the mixed layout;
+// the others keep their device values.
+__global__ void km_import(MCtx A, P64 Q, uint64_t mask) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= A.P.np) return;
     const int D = A.g.dim, NS = D == 2 ? 3 : 6;
+    const bool gimp = A.cf.basis == EP_BASIS_GIMPM;
     for (int d = 0; d < D; ++d) {
-        A.P.v[d][p] = (float)Q.v[d][p];
-        if (A.cf.basis == EP_BASIS_GIMPM) {
-            A.P.l[d][p] = (float)Q.l[d][p];
-            A.P.l0[d][p] = (float)Q.l0[d][p];
+        if (mask & EP_MPTS_V) A.P.v[d][p] = (float)Q.v[d][p];
+        if (gimp && (mask & EP_MPTS_L)) A.P.l[d][p] = (float)Q.l[d][p];
+        if (gimp && (mask & EP_MPTS_L0)) A.P.l0[d][p] = (float)Q.l0[d][p];
+    }
+    if (mask & EP_MPTS_FIJ) {
+        if (A.acc == 0) {
+            for (int k = 0; k < D * D; ++k) A.P.Fd[k][p] = Q.F[k][p];
+        } else {
+            for (int k = 0; k < D * D; ++k) {
+                const float h = (float)Q.F[k][p];
+                A.P.Fh[k][p] = h;
+                A.P.Fl[k][p] = (float)(Q.F[k][p] - (double)h);
+            }
         }
     }
-    double bsym[6];
-    for (int k = 0; k < NS; ++k) {
-        const int i = sym_i(D, k), j = sym_j(D, k);
-        bsym[k] = 0.5 * (Q.b[i + D * j][p] + Q.b[j + D * i][p]);
-    }
-    if (A.acc == 0) {
-        for (int k = 0; k < D * D; ++k) A.P.Fd[k][p] = Q.F[k][p];
-        for (int k = 0; k < NS; ++k) A.P.bd[k][p] = bsym[k];
-        A.P.ep1d[p] = Q.ep1[p];
-    } else {
-        for (int k = 0; k < D * D; ++k) {
-            const float h = (float)Q.F[k][p];
-            A.P.Fh[k][p] = h;
-            A.P.Fl[k][p] = (float)(Q.F[k][p] - (double)h);
-        }
+    if (mask & EP_MPTS_BIJ) {
         for (int k = 0; k < NS; ++k) {
-            const float h = (float)bsym[k];
-            A.P.bh[k][p] = h;
-            A.P.bl[k][p] = (float)(bsym[k] - (double)h);
+            const int i = sym_i(D, k), j = sym_j(D, k);
+            const double bs = 0.5 * (Q.b[i + D * j][p] + Q.b[j + D * i][p]);
+            if (A.acc == 0) {
+                A.P.bd[k][p] = bs;
+            } else {
+                const float h = (float)bs;
+                A.P.bh[k][p] = h;
+                A.P.bl[k][p] = (float)(bs - (double)h);
+            }
         }
-        const float h = (float)Q.ep1[p];
-        A.P.ep1h[p] = h;
-        A.P.ep1l[p] = (float)(Q.ep1[p] - (double)h);
     }
-    if (A.cf.trsfr == EP_TRSFR_TPIC)
+    if (mask & EP_MPTS_EPII) {
+        if (A.acc == 0) {
+            A.P.ep1d[p] = Q.ep1[p];
+        } else {
+            const float h = (float)Q.ep1[p];
+            A.P.ep1h[p] = h;
+            A.P.ep1l[p] = (float)(Q.ep1[p] - (double)h);
+        }
+        A.P.ep2[p] = (float)Q.ep2[p];
+    }
+    if (A.cf.trsfr == EP_TRSFR_TPIC && (mask & EP_MPTS_DVIJ))
         for (int k = 0; k < D * D; ++k) A.P.dv[k][p] = (float)Q.dv[k][p];
-    else if (A.cf.trsfr == EP_TRSFR_APIC)
+    else if (A.cf.trsfr == EP_TRSFR_APIC && (mask & EP_MPTS_APIC_B))
         for (int k = 0; k < D * D; ++k) A.P.dv[k][p] = (float)Q.B[k][p];
     const bool fin = A.cf.deform == EP_DEFORM_FINITE;
-    for (int k = 0; k < NS; ++k) A.P.tau[k][p] = (float)(fin ? Q.tau[k][p] : Q.sig[k][p]);
-    A.P.ep2[p] = (float)Q.ep2[p];
-    A.P.dlam[p] = (float)Q.dlam[p];
-    A.P.c0[p] = (float)Q.c0[p];
-    A.P.cr[p] = (float)Q.cr[p];
-    A.P.tphi[p] = (float)Q.tphi[p];
-    A.P.sphi[p] = (float)Q.sphi[p];
-    A.P.cphi[p] = (float)Q.cphi[p];
+    if (mask & (fin ? EP_MPTS_TAU : EP_MPTS_SIG))
+        for (int k = 0; k < NS; ++k) A.P.tau[k][p] = (float)(fin ? Q.tau[k][p] : Q.sig[k][p]);
+    if (mask & EP_MPTS_DLAM) A.P.dlam[p] = (float)Q.dlam[p];
+    if (mask & EP_MPTS_C0) A.P.c0[p] = (float)Q.c0[p];
+    if (mask & EP_MPTS_CR) A.P.cr[p] = (float)Q.cr[p];
+    if (mask & EP_MPTS_PHI) {
+        A.P.tphi[p] = (float)Q.tphi[p];
+        A.P.sphi[p] = (float)Q.sphi[p];
+        A.P.cphi[p] = (float)Q.cphi[p];
+    }
     // ρΩ: finite strain keeps ρΩ = ρ0Ω0 (deform.jl:1-24), so the mass is formed from the constants
     // (a resumed state's (ρ0/J)(J Ω0) could round to another FP32 value); infinitesimal strain
     // carries the current ρ Ω (deform.jl:25-44)
-    A.P.mp[p] = (float)(A.cf.deform == EP_DEFORM_FINITE ? Q.rho0[p] * Q.Om0[p] : Q.rho[p] * Q.Om[p]);
-    A.P.Om0[p] = (float)Q.Om0[p];
-    A.P.Om[p] = (float)Q.Om[p];
-    A.P.rho[p] = (float)Q.rho[p];
+    if (mask & (fin ? (EP_MPTS_RHO0 | EP_MPTS_OMEGA0) : (EP_MPTS_RHO | EP_MPTS_OMEGA)))
+        A.P.mp[p] = (float)(fin ? Q.rho0[p] * Q.Om0[p] : Q.rho[p] * Q.Om[p]);
+    if (mask & EP_MPTS_OMEGA0) A.P.Om0[p] = (float)Q.Om0[p];
+    if (mask & EP_MPTS_OMEGA) A.P.Om[p] = (float)Q.Om[p];
+    if (mask & EP_MPTS_RHO) A.P.rho[p] = (float)Q.rho[p];
 }
 
 // initial cell, offsets and counts from the FP64 positions of the staging layout
@@ -2680,87 +2694,93 @@ __global__ void km_place0(MCtx A) {
 }
 
 // need_eps = 0: the log strain ϵ = ½ log b (FP64 eigen + log per point) is not formed; callers that
-// do not read ϵ (masked downloads, conservation sums) skip that work
-__global__ void km_export(MCtx A, P64 Q, int need_eps) {
+// do not read ϵ (masked downloads, conservation sums) skip that work.  mask: the staging arrays to
+// write (EP_MPTS_* bits; the cell of each point always); a masked download moves only those.
+__global__ void km_export(MCtx A, P64 Q, int need_eps, uint64_t mask) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= A.P.np) return;
     const int cur = A.ctl->parity, D = A.g.dim, NS = D == 2 ? 3 : 6;
     const int c = A.P.p2e_next[p];
     Q.p2e[p] = c;
-    if (c >= 0) {
+    if (c >= 0 && (mask & EP_MPTS_X)) {
         int e[3];
         cell_dec(A.g, c, e);
         for (int d = 0; d < D; ++d) Q.x[d][p] = A.g.ax[d][e[d]] + (double)A.P.dx[cur][d][p];
     }
     for (int d = 0; d < D; ++d) {
-        Q.v[d][p] = (double)A.P.v[d][p];
-        if (A.cf.basis == EP_BASIS_GIMPM) Q.l[d][p] = (double)A.P.l[d][p];
+        if (mask & EP_MPTS_V) Q.v[d][p] = (double)A.P.v[d][p];
+        if (A.cf.basis == EP_BASIS_GIMPM && (mask & EP_MPTS_L)) Q.l[d][p] = (double)A.P.l[d][p];
     }
-    double F[9], B[6], e1;
-    if (A.acc == 0) {
-        for (int k = 0; k < D * D; ++k) F[k] = A.P.Fd[k][p];
-        for (int k = 0; k < NS; ++k) B[k] = A.P.bd[k][p];
-        e1 = A.P.ep1d[p];
-    } else {
-        for (int k = 0; k < D * D; ++k) F[k] = (double)A.P.Fh[k][p] + (double)A.P.Fl[k][p];
-        for (int k = 0; k < NS; ++k) B[k] = (double)A.P.bh[k][p] + (double)A.P.bl[k][p];
-        e1 = (double)A.P.ep1h[p] + (double)A.P.ep1l[p];
-    }
-    for (int k = 0; k < D * D; ++k) Q.F[k][p] = F[k];
-    const double J = D == 2 ? F[0] * F[3] - F[2] * F[1]
-                            : F[0] * (F[4] * F[8] - F[7] * F[5]) - F[3] * (F[1] * F[8] - F[7] * F[2]) +
-                                  F[6] * (F[1] * F[5] - F[4] * F[2]);
-    Q.J[p] = J;
     const bool fin = A.cf.deform == EP_DEFORM_FINITE;
-    // Ω = J Ω0 (deform.jl:18, 42); infinitesimal strain exports the volume the step carries and uses
-    // (its FP32 J Ω0, which also sets the mass ρΩ), so that a download / upload round trip keeps it
-    Q.Om[p] = fin ? J * Q.Om0[p] : (double)A.P.Om[p];
-    if (fin) {
-        // finite strain: b, τ, σ = τ / J and ϵ = ½ log b (FP64, for output)
-        Q.rho[p] = Q.rho0[p] / J;
-        Q.n[p] = 1.0 - 1.0 / J * (1.0 - Q.n0[p]);
-        for (int k = 0; k < NS; ++k) {
-            Q.tau[k][p] = (double)A.P.tau[k][p];
-            Q.sig[k][p] = (double)A.P.tau[k][p] / J;
-        }
-        if (D == 2) {
-            Q.b[0][p] = B[0]; Q.b[3][p] = B[1]; Q.b[1][p] = B[2]; Q.b[2][p] = B[2];
+    const uint64_t FDEP = EP_MPTS_FIJ | EP_MPTS_J | EP_MPTS_OMEGA | (fin ? (EP_MPTS_RHO | EP_MPTS_N | EP_MPTS_SIG) : 0ull);
+    if (mask & (FDEP | EP_MPTS_BIJ | EP_MPTS_EIJ | EP_MPTS_TAU)) {
+        double F[9], B[6];
+        if (A.acc == 0) {
+            for (int k = 0; k < D * D; ++k) F[k] = A.P.Fd[k][p];
+            for (int k = 0; k < NS; ++k) B[k] = A.P.bd[k][p];
         } else {
-            for (int k = 0; k < 6; ++k) {
-                const int i = sym_i(3, k), j = sym_j(3, k);
-                Q.b[i + 3 * j][p] = B[k];
-                Q.b[j + 3 * i][p] = B[k];
+            for (int k = 0; k < D * D; ++k) F[k] = (double)A.P.Fh[k][p] + (double)A.P.Fl[k][p];
+            for (int k = 0; k < NS; ++k) B[k] = (double)A.P.bh[k][p] + (double)A.P.bl[k][p];
+        }
+        if (mask & EP_MPTS_FIJ)
+            for (int k = 0; k < D * D; ++k) Q.F[k][p] = F[k];
+        const double J = D == 2 ? F[0] * F[3] - F[2] * F[1]
+                                : F[0] * (F[4] * F[8] - F[7] * F[5]) - F[3] * (F[1] * F[8] - F[7] * F[2]) +
+                                      F[6] * (F[1] * F[5] - F[4] * F[2]);
+        if (mask & EP_MPTS_J) Q.J[p] = J;
+        // Ω = J Ω0 (deform.jl:18, 42); infinitesimal strain exports the volume the step carries and uses
+        // (its FP32 J Ω0, which also sets the mass ρΩ), so that a download / upload round trip keeps it
+        if (mask & EP_MPTS_OMEGA) Q.Om[p] = fin ? J * Q.Om0[p] : (double)A.P.Om[p];
+        if (fin) {
+            // finite strain: b, τ, σ = τ / J and ϵ = ½ log b (FP64, for output)
+            if (mask & EP_MPTS_RHO) Q.rho[p] = Q.rho0[p] / J;
+            if (mask & EP_MPTS_N) Q.n[p] = 1.0 - 1.0 / J * (1.0 - Q.n0[p]);
+            for (int k = 0; k < NS; ++k) {
+                if (mask & EP_MPTS_TAU) Q.tau[k][p] = (double)A.P.tau[k][p];
+                if (mask & EP_MPTS_SIG) Q.sig[k][p] = (double)A.P.tau[k][p] / J;
+            }
+            if ((mask & EP_MPTS_BIJ) && D == 2) {
+                Q.b[0][p] = B[0]; Q.b[3][p] = B[1]; Q.b[1][p] = B[2]; Q.b[2][p] = B[2];
+            } else if (mask & EP_MPTS_BIJ) {
+                for (int k = 0; k < 6; ++k) {
+                    const int i = sym_i(3, k), j = sym_j(3, k);
+                    Q.b[i + 3 * j][p] = B[k];
+                    Q.b[j + 3 * i][p] = B[k];
+                }
+            }
+            if (need_eps && D == 2) {
+                double lam[2], V[4], L[2], R[4];
+                eig_sym2(B[0], B[2], B[1], lam, V);
+                L[0] = ep_log(lam[0]);
+                L[1] = ep_log(lam[1]);
+                vdvt<2>(V, L, R);
+                for (int k = 0; k < 4; ++k) Q.eps[k][p] = 0.5 * R[k];
+            } else if (need_eps) {
+                double Bt[9], lam[3], V[9], L[3], R[9];
+                for (int k = 0; k < 6; ++k) {
+                    const int i = sym_i(3, k), j = sym_j(3, k);
+                    Bt[i + 3 * j] = B[k];
+                    Bt[j + 3 * i] = B[k];
+                }
+                eig_sym3(Bt, lam, V);
+                for (int k = 0; k < 3; ++k) L[k] = ep_log(lam[k]);
+                vdvt<3>(V, L, R);
+                for (int k = 0; k < 9; ++k) Q.eps[k][p] = 0.5 * R[k];
             }
         }
-        if (need_eps && D == 2) {
-            double lam[2], V[4], L[2], R[4];
-            eig_sym2(B[0], B[2], B[1], lam, V);
-            L[0] = ep_log(lam[0]);
-            L[1] = ep_log(lam[1]);
-            vdvt<2>(V, L, R);
-            for (int k = 0; k < 4; ++k) Q.eps[k][p] = 0.5 * R[k];
-        } else if (need_eps) {
-            double Bt[9], lam[3], V[9], L[3], R[9];
-            for (int k = 0; k < 6; ++k) {
-                const int i = sym_i(3, k), j = sym_j(3, k);
-                Bt[i + 3 * j] = B[k];
-                Bt[j + 3 * i] = B[k];
-            }
-            eig_sym3(Bt, lam, V);
-            for (int k = 0; k < 3; ++k) L[k] = ep_log(lam[k]);
-            vdvt<3>(V, L, R);
-            for (int k = 0; k < 9; ++k) Q.eps[k][p] = 0.5 * R[k];
-        }
-    } else {
-        for (int k = 0; k < NS; ++k) Q.sig[k][p] = (double)A.P.tau[k][p];
     }
-    if (A.cf.trsfr == EP_TRSFR_TPIC)
+    if (!fin && (mask & EP_MPTS_SIG))
+        for (int k = 0; k < NS; ++k) Q.sig[k][p] = (double)A.P.tau[k][p];
+    if (A.cf.trsfr == EP_TRSFR_TPIC && (mask & EP_MPTS_DVIJ))
         for (int k = 0; k < D * D; ++k) Q.dv[k][p] = (double)A.P.dv[k][p];
-    else if (A.cf.trsfr == EP_TRSFR_APIC)
+    else if (A.cf.trsfr == EP_TRSFR_APIC && (mask & EP_MPTS_APIC_B))
         for (int k = 0; k < D * D; ++k) Q.B[k][p] = (double)A.P.dv[k][p];
-    Q.ep1[p] = e1;
-    Q.ep2[p] = A.cf.nonloc ? (double)A.P.ep2[p] : e1;
-    Q.dlam[p] = (double)A.P.dlam[p];
+    if (mask & EP_MPTS_EPII) {
+        const double e1 = A.acc == 0 ? A.P.ep1d[p] : (double)A.P.ep1h[p] + (double)A.P.ep1l[p];
+        Q.ep1[p] = e1;
+        Q.ep2[p] = A.cf.nonloc ? (double)A.P.ep2[p] : e1;
+    }
+    if (mask & EP_MPTS_DLAM) Q.dlam[p] = (double)A.P.dlam[p];
 }
 
 // the nodal state of the last step: a, the damped force and (USL) v from its P2G fields by the
@@ -4675,10 +4695,10 @@ void launch_mixed_scan(const MixedCtx& X, cudaStream_t s) { mixed_scan(*(const M
 
 void mixed_initial_scan(const MixedCtx& X, cudaStream_t s) { mixed_scan(*(const MCtx*)X.impl, 1, X.scan_in, s); }
 
-void mixed_import(const MixedCtx& X, const P64& Q, cudaStream_t s) {
+void mixed_import(const MixedCtx& X, const P64& Q, cudaStream_t s, uint64_t mask) {
     const MCtx& A = *(const MCtx*)X.impl;
     const int np = A.P.np;
-    if (np > 0) km_import<<<(np + 255) / 256, 256, 0, s>>>(A, Q);
+    if (np > 0) km_import<<<(np + 255) / 256, 256, 0, s>>>(A, Q, mask);
     // initial cell lists for the current parity
     cudaMemsetAsync(X.sort_zero, 0, X.sort_zero_bytes, s);
     if (np > 0) km_bin0<<<(np + 255) / 256, 256, 0, s>>>(A, Q);
@@ -4687,11 +4707,12 @@ void mixed_import(const MixedCtx& X, const P64& Q, cudaStream_t s) {
     if (A.cf.det) km_sort_cells<<<(A.g.ncell + 255) / 256, 256, 0, s>>>(A, 1);
 }
 
-void mixed_export(const MixedCtx& X, const P64& Q, const N64& QN, cudaStream_t s, bool need_eps) {
+void mixed_export(const MixedCtx& X, const P64& Q, const N64& QN, cudaStream_t s, bool need_eps, uint64_t mask,
+                  bool nodes) {
     const MCtx& A = *(const MCtx*)X.impl;
     const int np = A.P.np;
-    if (np > 0) km_export<<<(np + 255) / 256, 256, 0, s>>>(A, Q, need_eps ? 1 : 0);
-    km_export_nodes<<<(A.g.nnode + 255) / 256, 256, 0, s>>>(A, QN);
+    if (np > 0 && mask) km_export<<<(np + 255) / 256, 256, 0, s>>>(A, Q, need_eps ? 1 : 0, mask);
+    if (nodes) km_export_nodes<<<(A.g.nnode + 255) / 256, 256, 0, s>>>(A, QN);
 }
 
 // host-side construction of the device context
