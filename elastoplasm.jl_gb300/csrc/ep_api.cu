@@ -769,6 +769,30 @@ static uint64_t view_mask(const ep_mpts_view* m) {
     return k;
 }
 
+// A direct transfer of a mixed-precision handle (mixed_import_host / mixed_export_host: one pass
+// between the host arrays and the step's layout, no FP64 staging): every array of the view is one it
+// moves (MIXED_DIRECT_FIELDS; an upload must hold the positions, from which it bins) and sits in
+// mapped page-locked memory.  *H receives the arrays' device-accessible addresses.
+static bool direct_view(ep_handle* h, const ep_mpts_view* m, bool up, HostAoS* H, uint64_t* mask) {
+    if (!h->mixed || m->p2e || m->p2n || h->ctx.cf.trsfr == EP_TRSFR_APIC) return false;
+    const uint64_t k = view_mask(m);
+    if (!k || (k & ~MIXED_DIRECT_FIELDS) || (up && !(k & EP_MPTS_X))) return false;
+    *H = HostAoS{};
+    struct Src {
+        double* src;
+        double** dst;
+    } tab[] = {{m->x, &H->x},     {m->v, &H->v},      {m->l, &H->l},         {m->Fij, &H->F},       {m->bij, &H->b},
+               {m->tau, &H->tau}, {m->sig, &H->sig},  {m->epII, &H->ep},     {m->dlam, &H->dlam},   {m->dvij, &H->dv}};
+    for (const Src& t : tab) {
+        if (!t.src) continue;
+        double* dp = mapped_host(t.src);
+        if (!dp) return false;
+        *t.dst = dp;
+    }
+    *mask = k;
+    return true;
+}
+
 static std::string mask_names(uint64_t k) {
     std::string out;
     for (const ViewField& f : VIEW_FIELDS)
@@ -853,9 +877,33 @@ ep_status epgpu_upload_fields(ep_handle* h, const ep_mpts_view* m, uint64_t mask
     return upload_view(h, &v);
 }
 
+// the control block of a fresh upload: zero, vmax from the view
+static void reset_ctl(ep_handle* h, const ep_mpts_view* m) {
+    std::memset(h->hctl, 0, sizeof(Ctl));
+    for (int i = 0; i < h->dim; ++i) {
+        double v = m->vmax ? m->vmax[i] : 0.0;
+        long long bits;
+        std::memcpy(&bits, &v, sizeof(double));
+        h->hctl->vmax_bits[i] = (unsigned long long)bits;
+    }
+}
+
 // the upload proper: every non-NULL array of the view is copied in
 static ep_status upload_view(ep_handle* h, const ep_mpts_view* m) {
-    const int d = h->dim;
+    HostAoS H;
+    uint64_t dmask = 0;
+    if (h->uploaded && direct_view(h, m, true, &H, &dmask)) {
+        // one pass from the host arrays into the step's layout, binning included; the FP64 staging
+        // copies of these arrays are left behind (stale until the next export)
+        reset_ctl(h, m);
+        CK(h, cudaMemcpyAsync(h->ctl, h->hctl, sizeof(Ctl), cudaMemcpyHostToDevice, h->s));
+        mixed_import_host(h->mx, H, dmask, h->s);
+        CK(h, cudaGetLastError());
+        CK(h, cudaStreamSynchronize(h->s));
+        h->fresh &= ~dmask;
+        h->have |= dmask;
+        return EP_OK;
+    }
     // the copies (back to back on the copy engine), then one k_xfer over the mapped host buffers
     std::vector<XField> f = xfer_fields(h, m);
     std::vector<XField*> rest;
@@ -886,13 +934,7 @@ static ep_status upload_view(ep_handle* h, const ep_mpts_view* m) {
     for (XField* x : rest)
         if (x->k > 1) k_aos_to_soa<<<(h->np + 255) / 256, 256, 0, h->s>>>(x->stage, x->k, h->np, x->dev);
     CK(h, cudaGetLastError());
-    std::memset(h->hctl, 0, sizeof(Ctl));
-    for (int i = 0; i < d; ++i) {
-        double v = m->vmax ? m->vmax[i] : 0.0;
-        long long bits;
-        std::memcpy(&bits, &v, sizeof(double));
-        h->hctl->vmax_bits[i] = (unsigned long long)bits;
-    }
+    reset_ctl(h, m);
     CK(h, cudaMemcpyAsync(h->ctl, h->hctl, sizeof(Ctl), cudaMemcpyHostToDevice, h->s));
     // the mixed layout takes the uploaded arrays only (the others keep their device values)
     if (h->mixed) mixed_import(h->mx, h->ctx.P, h->s, view_mask(m));
@@ -1105,6 +1147,17 @@ ep_status epgpu_download_fields(ep_handle* h, ep_mpts_view* m, uint64_t mask) {
 static ep_status download_view(ep_handle* h, ep_mpts_view* m, bool need_eps) {
     const int d = h->dim;
     ep_status st;
+    HostAoS H;
+    uint64_t dmask = 0;
+    if (h->uploaded && direct_view(h, m, false, &H, &dmask)) {
+        // one pass from the step's layout into the host arrays (no FP64 staging)
+        mixed_export_host(h->mx, H, dmask, h->s);
+        CK(h, cudaGetLastError());
+        if ((st = read_ctl(h)) != EP_OK) return st;      // synchronizes: the host arrays are written
+        if (m->vmax)
+            for (int i = 0; i < d; ++i) m->vmax[i] = bits_to_double(h->hctl->vmax_bits[i]);
+        return EP_OK;
+    }
     if (h->mixed && h->uploaded) {
         // the requested point arrays only (the nodal fields are download_mesh's)
         const uint64_t want = view_mask(m);

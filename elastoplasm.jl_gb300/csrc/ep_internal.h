@@ -107,6 +107,19 @@ struct MixedCtx {
     int p2g_tile;             // cells per CTA of the P2G kernel: 16, 32 or 64 (autotuned)
     int begin_step = 0;       // 1: the step's first kernel also starts the step (k_ctl_begin_step's work)
 };
+// Host point arrays, page-locked and mapped (their device-accessible addresses), in the reference's
+// column-major layout (k components per point): the direct transfers of the mixed precisions, which
+// convert between these and the step's own layout in one pass, without the FP64 staging layout.
+struct HostAoS {
+    double *x, *v, *l, *F, *b, *tau, *sig, *ep, *dlam, *dv;
+};
+// the arrays a direct transfer can move (EP_MPTS_* bits; an upload must include the positions)
+constexpr uint64_t MIXED_DIRECT_FIELDS = EP_MPTS_X | EP_MPTS_V | EP_MPTS_L | EP_MPTS_FIJ | EP_MPTS_BIJ | EP_MPTS_TAU |
+                                         EP_MPTS_SIG | EP_MPTS_EPII | EP_MPTS_DLAM | EP_MPTS_DVIJ;
+// host arrays in `mask` -> the mixed layout, and the cell lists rebuilt from the host positions
+void mixed_import_host(const MixedCtx& X, const HostAoS& H, uint64_t mask, cudaStream_t s);
+// the mixed layout -> the host arrays in `mask`
+void mixed_export_host(const MixedCtx& X, const HostAoS& H, uint64_t mask, cudaStream_t s);
 size_t mixed_ctx_size();
 // persistent batch kernel over n 2d mixed instances (nullptr + reason when the batch is not eligible)
 void* mixed_batch_create(const MixedCtx* const* xs, int n, std::string* why);

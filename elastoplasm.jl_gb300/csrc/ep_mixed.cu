@@ -2660,31 +2660,254 @@ __global__ void km_import(MCtx A, P64 Q, uint64_t mask) {
     if (mask & EP_MPTS_RHO) A.P.rho[p] = (float)Q.rho[p];
 }
 
+// Direct transfers (HostAoS) move a block's points [p0, p0 + n) of one host array at a time through
+// shared memory in the host's own layout (k components per point), consecutive threads moving
+// consecutive doubles, so that every warp access to the host link is one contiguous run; each thread
+// then converts its own point from or to the shared copy.
+constexpr int XH_BS = 256, XH_KMAX = 9;
+
+__device__ __forceinline__ void xh_load(const double* __restrict__ host, int k, int p0, int n, double* sb) {
+    __syncthreads();                                  // the previous field's readers are done with sb
+    for (int i = threadIdx.x; i < k * n; i += XH_BS) sb[i] = host[(size_t)k * p0 + i];
+    __syncthreads();
+}
+
+__device__ __forceinline__ void xh_store(double* host, int k, int p0, int n, const double* sb) {
+    __syncthreads();                                  // every thread has put its point in sb
+    for (int i = threadIdx.x; i < k * n; i += XH_BS) host[(size_t)k * p0 + i] = sb[i];
+}
+
+// Direct upload: the host arrays in `mask` into the mixed layout as km_import converts them, and the
+// binning of km_bin0 from the host positions (which `mask` must include), in one pass over the points;
+// the cell counts are added once per distinct cell of a warp.
+__global__ void __launch_bounds__(XH_BS) km_import_host(MCtx A, HostAoS H, uint64_t mask) {
+    __shared__ double sb[XH_BS * XH_KMAX];
+    const int p0 = blockIdx.x * XH_BS, t = threadIdx.x, p = p0 + t;
+    const int n = min(XH_BS, A.P.np - p0);
+    const bool live = t < n;
+    const int D = A.g.dim, NS = D == 2 ? 3 : 6, DD = D * D;
+    const int cur = A.ctl->parity;
+    xh_load(H.x, D, p0, n, sb);
+    int c2 = -1;
+    if (live) {
+        bool fin = true;
+        double x[3];
+        for (int d = 0; d < D; ++d) {
+            x[d] = sb[d + D * t];
+            fin = fin && isfinite(x[d]);
+        }
+        if (fin) {
+            int e[3];
+            for (int d = 0; d < D; ++d) {
+                e[d] = (int)fmin(fmax(floor((x[d] - A.g.x0[d]) / A.g.h[d]), 0.0), (double)(A.g.nel[d] - 1));
+                A.P.dx[cur][d][p] = (float)(x[d] - A.g.ax[d][e[d]]);
+            }
+            c2 = cell_of(A.g, e);
+        } else {
+            set_err(A.ctl, EP_ERR_NONFINITE, p);
+        }
+        A.P.p2e_next[p] = c2;
+        if (A.P.pcell[cur]) A.P.pcell[cur][p] = c2;
+    }
+    const unsigned mm = __match_any_sync(0xffffffffu, c2);
+    if (c2 >= 0 && (t & 31) == __ffs(mm) - 1) atomicAdd(&A.S.count[cur][c2], __popc(mm));
+    if (mask & EP_MPTS_V) {
+        xh_load(H.v, D, p0, n, sb);
+        if (live)
+            for (int d = 0; d < D; ++d) A.P.v[d][p] = (float)sb[d + D * t];
+    }
+    if (A.cf.basis == EP_BASIS_GIMPM && (mask & EP_MPTS_L)) {
+        xh_load(H.l, D, p0, n, sb);
+        if (live)
+            for (int d = 0; d < D; ++d) A.P.l[d][p] = (float)sb[d + D * t];
+    }
+    if (mask & EP_MPTS_FIJ) {
+        xh_load(H.F, DD, p0, n, sb);
+        if (live)
+            for (int k = 0; k < DD; ++k) {
+                const double f = sb[k + DD * t];
+                if (A.acc == 0) {
+                    A.P.Fd[k][p] = f;
+                } else {
+                    const float h = (float)f;
+                    A.P.Fh[k][p] = h;
+                    A.P.Fl[k][p] = (float)(f - (double)h);
+                }
+            }
+    }
+    if (mask & EP_MPTS_BIJ) {
+        xh_load(H.b, DD, p0, n, sb);
+        if (live)
+            for (int k = 0; k < NS; ++k) {
+                const int i = sym_i(D, k), j = sym_j(D, k);
+                const double bs = 0.5 * (sb[i + D * j + DD * t] + sb[j + D * i + DD * t]);
+                if (A.acc == 0) {
+                    A.P.bd[k][p] = bs;
+                } else {
+                    const float h = (float)bs;
+                    A.P.bh[k][p] = h;
+                    A.P.bl[k][p] = (float)(bs - (double)h);
+                }
+            }
+    }
+    if (mask & EP_MPTS_EPII) {
+        xh_load(H.ep, 2, p0, n, sb);
+        if (live) {
+            const double e1 = sb[2 * t];
+            if (A.acc == 0) {
+                A.P.ep1d[p] = e1;
+            } else {
+                const float h = (float)e1;
+                A.P.ep1h[p] = h;
+                A.P.ep1l[p] = (float)(e1 - (double)h);
+            }
+            A.P.ep2[p] = (float)sb[2 * t + 1];
+        }
+    }
+    if (A.cf.trsfr == EP_TRSFR_TPIC && (mask & EP_MPTS_DVIJ)) {
+        xh_load(H.dv, DD, p0, n, sb);
+        if (live)
+            for (int k = 0; k < DD; ++k) A.P.dv[k][p] = (float)sb[k + DD * t];
+    }
+    const bool fin = A.cf.deform == EP_DEFORM_FINITE;
+    if (mask & (fin ? EP_MPTS_TAU : EP_MPTS_SIG)) {
+        xh_load(fin ? H.tau : H.sig, NS, p0, n, sb);
+        if (live)
+            for (int k = 0; k < NS; ++k) A.P.tau[k][p] = (float)sb[k + NS * t];
+    }
+    if (mask & EP_MPTS_DLAM) {
+        xh_load(H.dlam, 1, p0, n, sb);
+        if (live) A.P.dlam[p] = (float)sb[t];
+    }
+}
+
+// Direct download: the arrays in `mask` from the mixed layout as km_export forms them.
+__global__ void __launch_bounds__(XH_BS) km_export_host(MCtx A, HostAoS H, uint64_t mask) {
+    __shared__ double sb[XH_BS * XH_KMAX];
+    const int p0 = blockIdx.x * XH_BS, t = threadIdx.x, p = p0 + t;
+    const int n = min(XH_BS, A.P.np - p0);
+    const bool live = t < n;
+    const int cur = A.ctl->parity, D = A.g.dim, NS = D == 2 ? 3 : 6, DD = D * D;
+    const bool fin = A.cf.deform == EP_DEFORM_FINITE;
+    if (mask & EP_MPTS_X) {
+        // a point without a cell (non-finite position) keeps the host's value: a block holding one
+        // reads its positions first
+        const int c = live ? A.P.p2e_next[p] : 0;
+        if (__syncthreads_or(live && c < 0)) xh_load(H.x, D, p0, n, sb);
+        if (live && c >= 0) {
+            int e[3];
+            cell_dec(A.g, c, e);
+            for (int d = 0; d < D; ++d) sb[d + D * t] = A.g.ax[d][e[d]] + (double)A.P.dx[cur][d][p];
+        }
+        xh_store(H.x, D, p0, n, sb);
+    }
+    if (mask & EP_MPTS_V) {
+        __syncthreads();
+        if (live)
+            for (int d = 0; d < D; ++d) sb[d + D * t] = (double)A.P.v[d][p];
+        xh_store(H.v, D, p0, n, sb);
+    }
+    if (A.cf.basis == EP_BASIS_GIMPM && (mask & EP_MPTS_L)) {
+        __syncthreads();
+        if (live)
+            for (int d = 0; d < D; ++d) sb[d + D * t] = (double)A.P.l[d][p];
+        xh_store(H.l, D, p0, n, sb);
+    }
+    double F[9], B[6];
+    if (live && (mask & (EP_MPTS_FIJ | EP_MPTS_BIJ | (fin ? EP_MPTS_SIG : 0ull)))) {
+        if (A.acc == 0) {
+            for (int k = 0; k < DD; ++k) F[k] = A.P.Fd[k][p];
+            for (int k = 0; k < NS; ++k) B[k] = A.P.bd[k][p];
+        } else {
+            for (int k = 0; k < DD; ++k) F[k] = (double)A.P.Fh[k][p] + (double)A.P.Fl[k][p];
+            for (int k = 0; k < NS; ++k) B[k] = (double)A.P.bh[k][p] + (double)A.P.bl[k][p];
+        }
+    }
+    if (mask & EP_MPTS_FIJ) {
+        __syncthreads();
+        if (live)
+            for (int k = 0; k < DD; ++k) sb[k + DD * t] = F[k];
+        xh_store(H.F, DD, p0, n, sb);
+    }
+    if (fin && (mask & EP_MPTS_BIJ)) {
+        __syncthreads();
+        if (live)
+            for (int k = 0; k < NS; ++k) {
+                const int i = sym_i(D, k), j = sym_j(D, k);
+                sb[i + D * j + DD * t] = B[k];
+                sb[j + D * i + DD * t] = B[k];
+            }
+        xh_store(H.b, DD, p0, n, sb);
+    }
+    if (mask & EP_MPTS_SIG) {
+        __syncthreads();
+        if (live) {
+            double J = 1.0;
+            if (fin)
+                J = D == 2 ? F[0] * F[3] - F[2] * F[1]
+                           : F[0] * (F[4] * F[8] - F[7] * F[5]) - F[3] * (F[1] * F[8] - F[7] * F[2]) +
+                                 F[6] * (F[1] * F[5] - F[4] * F[2]);
+            for (int k = 0; k < NS; ++k) sb[k + NS * t] = fin ? (double)A.P.tau[k][p] / J : (double)A.P.tau[k][p];
+        }
+        xh_store(H.sig, NS, p0, n, sb);
+    }
+    if (fin && (mask & EP_MPTS_TAU)) {
+        __syncthreads();
+        if (live)
+            for (int k = 0; k < NS; ++k) sb[k + NS * t] = (double)A.P.tau[k][p];
+        xh_store(H.tau, NS, p0, n, sb);
+    }
+    if (A.cf.trsfr == EP_TRSFR_TPIC && (mask & EP_MPTS_DVIJ)) {
+        __syncthreads();
+        if (live)
+            for (int k = 0; k < DD; ++k) sb[k + DD * t] = (double)A.P.dv[k][p];
+        xh_store(H.dv, DD, p0, n, sb);
+    }
+    if (mask & EP_MPTS_EPII) {
+        __syncthreads();
+        if (live) {
+            const double e1 = A.acc == 0 ? A.P.ep1d[p] : (double)A.P.ep1h[p] + (double)A.P.ep1l[p];
+            sb[2 * t] = e1;
+            sb[2 * t + 1] = A.cf.nonloc ? (double)A.P.ep2[p] : e1;
+        }
+        xh_store(H.ep, 2, p0, n, sb);
+    }
+    if (mask & EP_MPTS_DLAM) {
+        __syncthreads();
+        if (live) sb[t] = (double)A.P.dlam[p];
+        xh_store(H.dlam, 1, p0, n, sb);
+    }
+}
+
 // initial cell, offsets and counts from the FP64 positions of the staging layout
 __global__ void km_bin0(MCtx A, P64 Q) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= A.P.np) return;
+    const bool live = p < A.P.np;
     const int cur = A.ctl->parity, D = A.g.dim;
     int c2 = -1;
-    bool fin = true;
-    double x[3];
-    for (int d = 0; d < D; ++d) {
-        x[d] = Q.x[d][p];
-        fin = fin && isfinite(x[d]);
-    }
-    if (fin) {
-        int e[3];
+    if (live) {
+        bool fin = true;
+        double x[3];
         for (int d = 0; d < D; ++d) {
-            e[d] = (int)fmin(fmax(floor((x[d] - A.g.x0[d]) / A.g.h[d]), 0.0), (double)(A.g.nel[d] - 1));
-            A.P.dx[cur][d][p] = (float)(x[d] - A.g.ax[d][e[d]]);
+            x[d] = Q.x[d][p];
+            fin = fin && isfinite(x[d]);
         }
-        c2 = cell_of(A.g, e);
-        atomicAdd(&A.S.count[cur][c2], 1);
-    } else {
-        set_err(A.ctl, EP_ERR_NONFINITE, p);
+        if (fin) {
+            int e[3];
+            for (int d = 0; d < D; ++d) {
+                e[d] = (int)fmin(fmax(floor((x[d] - A.g.x0[d]) / A.g.h[d]), 0.0), (double)(A.g.nel[d] - 1));
+                A.P.dx[cur][d][p] = (float)(x[d] - A.g.ax[d][e[d]]);
+            }
+            c2 = cell_of(A.g, e);
+        } else {
+            set_err(A.ctl, EP_ERR_NONFINITE, p);
+        }
+        A.P.p2e_next[p] = c2;
+        if (A.P.pcell[cur]) A.P.pcell[cur][p] = c2;
     }
-    A.P.p2e_next[p] = c2;
-    if (A.P.pcell[cur]) A.P.pcell[cur][p] = c2;
+    // the counts once per distinct cell of the warp
+    const unsigned mm = __match_any_sync(0xffffffffu, c2);
+    if (c2 >= 0 && (threadIdx.x & 31) == __ffs(mm) - 1) atomicAdd(&A.S.count[cur][c2], __popc(mm));
 }
 
 __global__ void km_place0(MCtx A) {
@@ -4705,6 +4928,22 @@ void mixed_import(const MixedCtx& X, const P64& Q, cudaStream_t s, uint64_t mask
     mixed_initial_scan(X, s);
     if (np > 0) km_place0<<<(np + 255) / 256, 256, 0, s>>>(A);
     if (A.cf.det) km_sort_cells<<<(A.g.ncell + 255) / 256, 256, 0, s>>>(A, 1);
+}
+
+void mixed_import_host(const MixedCtx& X, const HostAoS& H, uint64_t mask, cudaStream_t s) {
+    const MCtx& A = *(const MCtx*)X.impl;
+    const int np = A.P.np;
+    cudaMemsetAsync(X.sort_zero, 0, X.sort_zero_bytes, s);
+    if (np > 0) km_import_host<<<(np + XH_BS - 1) / XH_BS, XH_BS, 0, s>>>(A, H, mask);
+    mixed_initial_scan(X, s);
+    if (np > 0) km_place0<<<(np + 255) / 256, 256, 0, s>>>(A);
+    if (A.cf.det) km_sort_cells<<<(A.g.ncell + 255) / 256, 256, 0, s>>>(A, 1);
+}
+
+void mixed_export_host(const MixedCtx& X, const HostAoS& H, uint64_t mask, cudaStream_t s) {
+    const MCtx& A = *(const MCtx*)X.impl;
+    const int np = A.P.np;
+    if (np > 0 && mask) km_export_host<<<(np + XH_BS - 1) / XH_BS, XH_BS, 0, s>>>(A, H, mask);
 }
 
 void mixed_export(const MixedCtx& X, const P64& Q, const N64& QN, cudaStream_t s, bool need_eps, uint64_t mask,

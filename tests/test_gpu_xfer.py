@@ -73,15 +73,18 @@ def test_pinned_and_pageable_transfers_agree(dim, precision):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed_df"])
+@pytest.mark.parametrize("pinned", [False, True])
 @pytest.mark.parametrize("trsfr", ["std", "tpic"])
-def test_masked_transfers_continue_the_run(precision, trsfr):
+def test_masked_transfers_continue_the_run(precision, trsfr, pinned):
     """A host loop that moves only the state a step reads and changes (epgpu_upload_fields /
     epgpu_download_fields with epgpu_fields_read & epgpu_fields_changed) after a full first upload
     gives the run that keeps the state on the device; the constants are not moved again.  Bit for bit
     for the FP64 step and for the mixed step with FP64 accumulators; with double-float accumulators a
     few points differ by the last bit of the 48-bit pair (1.8e-15 relative in F and b_e after one step),
     which can flip the last bit of an FP32 stress later, so that case is held to FP32 resolution
-    (1e-7 of each field's scale)."""
+    (1e-7 of each field's scale).  With page-locked host arrays the mixed precisions take the direct
+    transfers (one pass between the host arrays and the step's layout, no FP64 staging), held to the
+    same run."""
     from epgpu import Engine, ic_slump
     fw = {"deform": "finite", "trsfr": trsfr, "C_pf": 0.99, "musl": True, "locking": True, "damping": 0.1}
     ic, cfg = ic_slump(*C1, fwrk=fw, nonloc={"status": False, "ls": 0.5})
@@ -97,7 +100,8 @@ def test_masked_transfers_continue_the_run(precision, trsfr):
     moved = sorted(set(e.fields_read()) & set(e.fields_changed()))
     assert {"x", "v", "Fij", "bij", "tau", "epII", "dlam"} <= set(moved)
     assert not {"c0", "cr", "phi", "Omega0", "u", "p"} & set(moved)
-    host = ic["mpts"].copy()
+    keep = []
+    host = _pinned(ic["mpts"], keep) if pinned else ic["mpts"].copy()
     for k in range(6):
         e.upload_fields(host, moved)
         e.step(1, 0.02, g)
@@ -155,3 +159,36 @@ def test_masked_download_writes_only_the_mask(precision):
     assert np.array_equal(host.x, full.x) and np.array_equal(host.tau, full.tau)
     assert np.isnan(host.v).all() and np.isnan(host.eij).all()
     e.close()
+
+
+@pytest.mark.parametrize("dim,precision", [(2, "mixed"), (2, "mixed_df"), (3, "mixed_df")])
+def test_direct_and_staged_masked_transfers_agree(dim, precision):
+    """The mixed precisions' masked transfers of page-locked host arrays (direct: the host arrays to and
+    from the step's layout in one pass) and of pageable ones (through the FP64 staging layout) leave the
+    same bits, on the host after every download and in the run's end state."""
+    from epgpu import Engine, ic_slump
+    L, nel = C1 if dim == 2 else C1_3D
+    ic, cfg = ic_slump(L, nel, nonloc={"status": False, "ls": 0.5})
+    instr = copy.deepcopy(cfg["instr"])
+    instr["gpu"] = {"precision": precision, "jaumann": False, "deterministic": True}
+    g = [0.0] * (dim - 1) + [-9.81]
+    runs = {}
+    for pinned in (False, True):
+        keep = []
+        e = Engine(copy.deepcopy(ic), instr)
+        moved = sorted(set(e.fields_read()) & set(e.fields_changed()))
+        host = _pinned(ic["mpts"], keep) if pinned else ic["mpts"].copy()
+        seen = []
+        for k in range(5):
+            e.upload_fields(host, moved)
+            e.step(1, 0.02, g)
+            e.download_fields(host, moved)
+            seen.append({f: np.array(getattr(host, f)) for f in moved})
+        runs[pinned] = (seen, e.download())
+        e.close()
+    (sa, fa), (sb, fb) = runs[False], runs[True]
+    for k in range(len(sa)):
+        for f in sa[k]:
+            assert np.array_equal(sa[k][f], sb[k][f]), (k, f)
+    for f in ("x", "v", "tau", "Fij", "bij", "epII", "dlam", "sig", "J"):
+        assert np.array_equal(np.asarray(getattr(fa, f)), np.asarray(getattr(fb, f))), f
