@@ -619,15 +619,17 @@ __global__ void __launch_bounds__(4 * TC) km_g2p_tile(MCtx A) {
     constexpr int NT = 4 * TC;
     constexpr int NB = SOLVE ? TB_SOLVE : TB_MAX;
     constexpr int NSP = NT * TG_STRIDE, NRAW = SOLVE ? 6 * TB_SOLVE : 0;
-    pdl_enter();
-    EP_ACTIVE(A.ctl);
     __shared__ __align__(16) float sp[NSP > NRAW ? NSP : NRAW];
     __shared__ __align__(16) float4 box[NB];
     __shared__ int4 cinfo[TC];
-    const int cur = A.ctl->parity, nxt = cur ^ 1;
     const int c0 = blockIdx.x * TC;
     if (c0 >= A.g.ncell) return;
     const int c1 = min(c0 + TC, A.g.ncell);
+    // the tile's stencil data depend on the mesh only: staged before the wait for the previous kernel
+    stage_cells(A.g, c0, c1, cinfo);
+    pdl_enter();
+    EP_ACTIVE(A.ctl);
+    const int cur = A.ctl->parity, nxt = cur ^ 1;
     const int* start = A.S.start[cur];
     const int b0 = start[c0], b1 = start[c1];
     if (SOLVE && A.cf.locking) {
@@ -685,7 +687,6 @@ __global__ void __launch_bounds__(4 * TC) km_g2p_tile(MCtx A) {
     } else if (tb.staged) {
         stage_box(A.g, A.N.va4, box, tb, NX);
     }
-    stage_cells(A.g, c0, c1, cinfo);
     const float4* vb = (SOLVE || tb.staged) ? box : A.N.va4;
     const float hx = (float)A.g.h[0], hz = (float)A.g.h[1];
     const float ihx = 1.f / hx, ihz = 1.f / hz;
@@ -825,7 +826,9 @@ __global__ void __launch_bounds__(4 * TC) km_g2p_tile(MCtx A) {
 constexpr int TP_STRIDE = 29;   // floats per staged point (odd: no bank conflicts)
 
 // NT: threads of the block (the staging width); 4 TP_CELLS of them accumulate, the rest only stage
-template <int BASIS, int TP_CELLS, bool DET, int NT = 4 * TP_CELLS>
+// EARLY (the stand-alone kernel, a programmatic dependent launch): the tile's stencil data, which depend
+// on the mesh only, are staged before the wait for the previous kernel of the stream
+template <int BASIS, int TP_CELLS, bool DET, int NT = 4 * TP_CELLS, bool EARLY = false>
 __device__ __forceinline__ void p2g_tile_body(const MCtx& A, int bid) {
     static_assert(NT >= 4 * TP_CELLS, "a P2G tile needs 4 lanes per cell");
     constexpr int TP_THREADS = NT;
@@ -833,9 +836,14 @@ __device__ __forceinline__ void p2g_tile_body(const MCtx& A, int bid) {
         if (threadIdx.x == 0) set_err(A.ctl, EP_ERR_ARG, -1);
         return;
     }
-    EP_ACTIVE(A.ctl);
     __shared__ float sp[TP_THREADS * TP_STRIDE];
     __shared__ int4 cinfo[TP_CELLS];
+    if (EARLY) {
+        if (bid * TP_CELLS >= A.g.ncell) return;
+        stage_cells(A.g, bid * TP_CELLS, min(bid * TP_CELLS + TP_CELLS, A.g.ncell), cinfo);
+        pdl_enter();
+    }
+    EP_ACTIVE(A.ctl);
     const int cur = A.ctl->parity;
     const int c0 = bid * TP_CELLS;
     if (c0 >= A.g.ncell) return;
@@ -853,8 +861,10 @@ __device__ __forceinline__ void p2g_tile_body(const MCtx& A, int bid) {
         c_n = A.S.cellof[cur][b0 + t];
     }
     const int pb = cell_ok ? start[cl] : 0, pe = cell_ok ? start[cl + 1] : 0;
-    __syncthreads();      // a persistent caller's previous tile may still read cinfo
-    stage_cells(A.g, c0, c1, cinfo);
+    if (!EARLY) {
+        __syncthreads();      // a persistent caller's previous tile may still read cinfo
+        stage_cells(A.g, c0, c1, cinfo);
+    }
     const float hx = (float)A.g.h[0], hz = (float)A.g.h[1];
     const float gz = (float)A.ctl->g[1];
     const bool fin = A.cf.deform == EP_DEFORM_FINITE;
@@ -963,8 +973,7 @@ __device__ __forceinline__ void p2g_tile_body(const MCtx& A, int bid) {
 
 template <int BASIS, int TP_CELLS, bool DET>
 __global__ void __launch_bounds__(4 * TP_CELLS) km_p2g_tile(MCtx A) {
-    pdl_enter();
-    p2g_tile_body<BASIS, TP_CELLS, DET>(A, blockIdx.x);
+    p2g_tile_body<BASIS, TP_CELLS, DET, 4 * TP_CELLS, true>(A, blockIdx.x);
 }
 
 
@@ -1238,15 +1247,17 @@ __global__ void __launch_bounds__(4 * TC) km_fbar_tile(MCtx A) {
     constexpr int NT = 4 * TC;
     constexpr int NB = VM ? TB_SOLVE : TB_MAX;
     constexpr int NSP = NT * TF_STRIDE, NRAW = VM ? 4 * TB_SOLVE : 0;
-    pdl_enter();
-    EP_ACTIVE(A.ctl);
     __shared__ __align__(16) float sp[NSP > NRAW ? NSP : NRAW];
     __shared__ __align__(16) float2 box[NB];
     __shared__ int4 cinfo[TC];
-    const int cur = A.ctl->parity, nxt = cur ^ 1;
     const int c0 = blockIdx.x * TC;
     if (c0 >= A.g.ncell) return;
     const int c1 = min(c0 + TC, A.g.ncell);
+    // the tile's stencil data depend on the mesh only: staged before the wait for the previous kernel
+    stage_cells(A.g, c0, c1, cinfo);
+    pdl_enter();
+    EP_ACTIVE(A.ctl);
+    const int cur = A.ctl->parity, nxt = cur ^ 1;
     const int* start = A.S.start[cur];
     const int b0 = start[c0], b1 = start[c1];
     if (b0 == b1) return;
@@ -1286,7 +1297,6 @@ __global__ void __launch_bounds__(4 * TC) km_fbar_tile(MCtx A) {
     } else if (tb.staged) {
         stage_box(A.g, A.N.vg4, box, tb, NX);
     }
-    stage_cells(A.g, c0, c1, cinfo);
     const float hx = (float)A.g.h[0], hz = (float)A.g.h[1];
     const float dtf = (float)A.ctl->dt;
     const bool fin = A.cf.deform == EP_DEFORM_FINITE;
