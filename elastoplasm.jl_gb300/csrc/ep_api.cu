@@ -1124,6 +1124,68 @@ ep_status epgpu_run_checkpoints(ep_handle* h, int32_t phase, const double* check
 
 static ep_status download_view(ep_handle* h, ep_mpts_view* m, bool need_eps);
 
+// the view restricted to the arrays of `mask` (topology left out)
+static ep_mpts_view masked_view(const ep_mpts_view* m, uint64_t mask) {
+    ep_mpts_view v = *m;
+    for (const ViewField& f : VIEW_FIELDS)
+        if (!(mask & f.bit)) v.*f.ptr = nullptr;
+    v.p2e = nullptr;
+    v.p2n = nullptr;
+    return v;
+}
+
+ep_status epgpu_step_fields(ep_handle* h, ep_mpts_view* m, uint64_t mask_in, int32_t phase, double dt,
+                            const double* g, uint64_t mask_out, double* vmax_out) {
+    if (!h || !m || !g) return EP_ERR_ARG;
+    if (m->nmp != h->np || m->ndim != h->dim) return fail(h, EP_ERR_ARG, "mpts.nmp/ndim differ from create");
+    if ((mask_in | mask_out) & ~EP_MPTS_ALL) return fail(h, EP_ERR_ARG, "unknown bits in the field mask");
+    if (phase != 0 && phase != 1) return fail(h, EP_ERR_ARG, "phase must be 0 or 1");
+    const uint64_t given = view_mask(m);
+    if ((mask_in | mask_out) & ~given)
+        return fail(h, EP_ERR_ARG, "a field in the mask is NULL: " + mask_names((mask_in | mask_out) & ~given));
+    ep_mpts_view vin = masked_view(m, mask_in), vout = masked_view(m, mask_out);
+    HostAoS Hin, Hout;
+    uint64_t din = 0, dout = 0;
+    const bool direct = h->uploaded && !h->prof.on && !(reads_of(h) & ~(mask_in | h->have)) &&
+                        direct_view(h, &vin, true, &Hin, &din) && direct_view(h, &vout, false, &Hout, &dout);
+    if (!direct) {
+        ep_status st = epgpu_upload_fields(h, m, mask_in);
+        if (st == EP_OK) st = epgpu_step(h, phase, dt, g, vmax_out);
+        if (st == EP_OK) st = epgpu_download_fields(h, m, mask_out);
+        return st;
+    }
+    // upload (as upload_view's direct path), the step (as epgpu_step) and the download (as
+    // download_view's direct path) queued back to back on the stream; one synchronisation
+    ep_status st;
+    if ((st = build_step_graph(h, phase)) != EP_OK) return st;
+    reset_ctl(h, &vin);
+    CK(h, cudaMemcpyAsync(h->ctl, h->hctl, sizeof(Ctl), cudaMemcpyHostToDevice, h->s));
+    mixed_import_host(h->mx, Hin, din, h->s);
+    double gg[3];
+    for (int i = 0; i < 3; ++i) gg[i] = i < h->dim ? g[i] : 0.0;
+    launch_ctl_set_step(h->ctl, dt, gg, phase, h->s);
+    CK(h, cudaGetLastError());
+    CK(h, cudaEventRecord(h->ev0, h->s));
+    CK(h, cudaGraphLaunch(h->step_graph[phase], h->s));
+    CK(h, cudaEventRecord(h->ev1, h->s));
+    h->launches += h->step_kernels[phase];
+    mixed_export_host(h->mx, Hout, dout, h->s);
+    CK(h, cudaGetLastError());
+    if ((st = read_ctl(h)) != EP_OK) return st;              // synchronizes: the host arrays are written
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+    h->last_ms = ms;
+    h->steps += 1;
+    h->have |= din;
+    h->fresh = 0;
+    for (int i = 0; i < h->dim; ++i) {
+        const double v = bits_to_double(h->hctl->vmax_bits[i]);
+        if (vmax_out) vmax_out[i] = v;
+        if (m->vmax) m->vmax[i] = v;                          // as epgpu_download_fields
+    }
+    return kernel_error(h);
+}
+
 ep_status epgpu_download(ep_handle* h, ep_mpts_view* m) {
     if (!h || !m) return EP_ERR_ARG;
     if (m->nmp != h->np || m->ndim != h->dim) return fail(h, EP_ERR_ARG, "mpts.nmp/ndim differ from create");

@@ -194,6 +194,8 @@ SIGNATURES = {
     "epgpu_download": (C.c_int, [C.c_void_p, C.POINTER(ep_mpts_view)]),
     "epgpu_upload_fields": (C.c_int, [C.c_void_p, C.POINTER(ep_mpts_view), C.c_uint64]),
     "epgpu_download_fields": (C.c_int, [C.c_void_p, C.POINTER(ep_mpts_view), C.c_uint64]),
+    "epgpu_step_fields": (C.c_int, [C.c_void_p, C.POINTER(ep_mpts_view), C.c_uint64, C.c_int32, C.c_double, _D,
+                                    C.c_uint64, _D]),
     "epgpu_fields_read": (C.c_uint64, [C.c_void_p]),
     "epgpu_fields_changed": (C.c_uint64, [C.c_void_p]),
     "epgpu_download_mesh": (C.c_int, [C.c_void_p, C.POINTER(ep_mesh_fields)]),

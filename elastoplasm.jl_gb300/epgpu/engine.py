@@ -59,6 +59,18 @@ class Engine:
         self._check(self.lib.epgpu_download_fields(self.h, C.byref(abi.mpts_view(mpts)), abi.mask_of(names)))
         return mpts
 
+    def step_fields(self, mpts, names_in, phase: int, dt: float, g, names_out=None) -> np.ndarray:
+        """One host-loop step in one call (``epgpu_step_fields``): upload the named arrays of ``mpts``,
+        step, download ``names_out`` (default: the same names) into ``mpts``; returns vmax."""
+        g = np.zeros(3) + np.pad(np.asarray(g, dtype=np.float64), (0, 3 - len(g)))
+        vmax = np.zeros(3)
+        view = abi.mpts_view(mpts)
+        self._check(self.lib.epgpu_step_fields(self.h, C.byref(view), abi.mask_of(names_in), int(phase), float(dt),
+                                               g.ctypes.data_as(C.POINTER(C.c_double)),
+                                               abi.mask_of(names_in if names_out is None else names_out),
+                                               vmax.ctypes.data_as(C.POINTER(C.c_double))))
+        return vmax[: self.mpts.ndim]
+
     def download(self, mpts=None):
         mpts = mpts or self.mpts.copy()
         self._check(self.lib.epgpu_download(self.h, C.byref(abi.mpts_view(mpts, with_topology=True))))

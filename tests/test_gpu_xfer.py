@@ -192,3 +192,40 @@ def test_direct_and_staged_masked_transfers_agree(dim, precision):
             assert np.array_equal(sa[k][f], sb[k][f]), (k, f)
     for f in ("x", "v", "tau", "Fij", "bij", "epII", "dlam", "sig", "J"):
         assert np.array_equal(np.asarray(getattr(fa, f)), np.asarray(getattr(fb, f))), f
+
+
+@pytest.mark.parametrize("pinned", [False, True])
+@pytest.mark.parametrize("precision", ["fp64", "mixed_df"])
+def test_step_fields_equals_the_three_calls(precision, pinned):
+    """epgpu_step_fields (upload, step, download in one call: back to back on the device for mapped
+    page-locked arrays in the mixed precisions) against epgpu_upload_fields + epgpu_step +
+    epgpu_download_fields: the same bits on the host and the same vmax after every step."""
+    from epgpu import Engine, ic_slump
+    ic, cfg = ic_slump(*C1, nonloc={"status": False, "ls": 0.5})
+    instr = copy.deepcopy(cfg["instr"])
+    instr["gpu"] = {"precision": precision, "jaumann": False, "deterministic": precision != "fp64"}
+    g = [0.0, -9.81]
+    out = []
+    for fused in (False, True):
+        keep = []
+        e = Engine(copy.deepcopy(ic), instr)
+        moved = sorted(set(e.fields_read()) & set(e.fields_changed()))
+        host = _pinned(ic["mpts"], keep) if pinned else ic["mpts"].copy()
+        vs, seen = [], []
+        for k in range(5):
+            if fused:
+                vm = e.step_fields(host, moved, 1, 0.02, g)
+            else:
+                e.upload_fields(host, moved)
+                vm = e.step(1, 0.02, g)
+                e.download_fields(host, moved)
+            vs.append(np.array(vm))
+            seen.append({f: np.array(getattr(host, f)) for f in moved})
+        assert e.stats()["steps"] == 5
+        out.append((vs, seen))
+        e.close()
+    (va, sa), (vb, sb) = out
+    for k in range(len(va)):
+        assert np.array_equal(va[k], vb[k]), k
+        for f in sa[k]:
+            assert np.array_equal(sa[k][f], sb[k][f]), (k, f)
