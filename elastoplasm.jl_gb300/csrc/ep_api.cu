@@ -65,6 +65,9 @@ struct ep_handle {
     bool uploaded = false;
     std::string err;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // epgpu_step_fields: the second stream of its overlapped transfers and their events (made on first use)
+    cudaStream_t s2 = nullptr;
+    cudaEvent_t ev_up = nullptr, ev_late = nullptr, ev_moved = nullptr, ev_dn = nullptr;
     Prof prof;
     bool mixed = false;
     MixedCtx mx{};
@@ -179,8 +182,10 @@ ep_status epgpu_destroy(ep_handle* h) {
     if (h->s) cudaStreamSynchronize(h->s);
     for (void* p : h->allocs) cudaFree(p);
     if (h->hctl) cudaFreeHost(h->hctl);
-    if (h->ev0) cudaEventDestroy(h->ev0);
-    if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->s2) cudaStreamSynchronize(h->s2);
+    for (cudaEvent_t e : {h->ev0, h->ev1, h->ev_up, h->ev_late, h->ev_moved, h->ev_dn})
+        if (e) cudaEventDestroy(e);
+    if (h->s2) cudaStreamDestroy(h->s2);
     if (h->s) cudaStreamDestroy(h->s);
     delete h;
     return EP_OK;
@@ -1155,21 +1160,51 @@ ep_status epgpu_step_fields(ep_handle* h, ep_mpts_view* m, uint64_t mask_in, int
         return st;
     }
     // upload (as upload_view's direct path), the step (as epgpu_step) and the download (as
-    // download_view's direct path) queued back to back on the stream; one synchronisation
+    // download_view's direct path) queued on the device with one synchronisation.  The link's two
+    // directions and the step overlap: the arrays only the constitutive pass reads (F, b_e, ϵpII, Δλ)
+    // follow the rest of the upload on a second stream while the step's first kernels run, and the
+    // positions and velocities, final after the G2P, go down on that stream during the rest of the step.
+    if (!h->s2) {
+        // the highest priority: its few blocks take the SM slots the step's kernels free first
+        int lo = 0, hi = 0;
+        cudaDeviceGetStreamPriorityRange(&lo, &hi);
+        cudaError_t e = cudaStreamCreateWithPriority(&h->s2, cudaStreamNonBlocking, hi);
+        for (cudaEvent_t* ev : {&h->ev_up, &h->ev_late, &h->ev_moved, &h->ev_dn})
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+        if (e != cudaSuccess) return cuda_fail(h, e, "step_fields: second stream");
+    }
     ep_status st;
-    if ((st = build_step_graph(h, phase)) != EP_OK) return st;
+    constexpr uint64_t LATE_IN = EP_MPTS_FIJ | EP_MPTS_BIJ | EP_MPTS_EPII | EP_MPTS_DLAM;
+    constexpr uint64_t EARLY_OUT = EP_MPTS_X | EP_MPTS_V;
+    const uint64_t late_in = din & LATE_IN, early_out = dout & EARLY_OUT;
     reset_ctl(h, &vin);
     CK(h, cudaMemcpyAsync(h->ctl, h->hctl, sizeof(Ctl), cudaMemcpyHostToDevice, h->s));
-    mixed_import_host(h->mx, Hin, din, h->s);
+    mixed_import_host(h->mx, Hin, din & ~late_in, h->s);           // positions (cell lists), v, ℓ, τ, ∇v
+    MixedCtx mx = h->mx;
+    mx.begin_step = 1;                                             // km_zero starts the step
+    if (late_in) {
+        CK(h, cudaEventRecord(h->ev_up, h->s));                    // one link direction: in turn
+        CK(h, cudaStreamWaitEvent(h->s2, h->ev_up, 0));
+        mixed_import_host(h->mx, Hin, late_in, h->s2, false);
+        CK(h, cudaEventRecord(h->ev_late, h->s2));
+        mx.ev_need = h->ev_late;
+    }
+    if (early_out) mx.ev_moved = h->ev_moved;
     double gg[3];
     for (int i = 0; i < 3; ++i) gg[i] = i < h->dim ? g[i] : 0.0;
     launch_ctl_set_step(h->ctl, dt, gg, phase, h->s);
     CK(h, cudaGetLastError());
     CK(h, cudaEventRecord(h->ev0, h->s));
-    CK(h, cudaGraphLaunch(h->step_graph[phase], h->s));
+    mixed_step(mx, phase, h->s);                                   // counts its launches
     CK(h, cudaEventRecord(h->ev1, h->s));
-    h->launches += h->step_kernels[phase];
-    mixed_export_host(h->mx, Hout, dout, h->s);
+    if (early_out) {
+        // reset_ctl starts the step at parity 0: its G2P writes the offsets of parity 1
+        CK(h, cudaStreamWaitEvent(h->s2, h->ev_moved, 0));
+        mixed_export_host(h->mx, Hout, early_out, h->s2, h->hctl->parity ^ 1);
+        CK(h, cudaEventRecord(h->ev_dn, h->s2));
+    }
+    mixed_export_host(h->mx, Hout, dout & ~early_out, h->s);
+    if (early_out) CK(h, cudaStreamWaitEvent(h->s, h->ev_dn, 0));
     CK(h, cudaGetLastError());
     if ((st = read_ctl(h)) != EP_OK) return st;              // synchronizes: the host arrays are written
     float ms = 0.f;

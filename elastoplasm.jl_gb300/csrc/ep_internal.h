@@ -106,6 +106,10 @@ struct MixedCtx {
     long long* launches;
     int p2g_tile;             // cells per CTA of the P2G kernel: 16, 32 or 64 (autotuned)
     int begin_step = 0;       // 1: the step's first kernel also starts the step (k_ctl_begin_step's work)
+    // host-loop overlap (epgpu_step_fields): recorded once the G2P has written the step's positions and
+    // velocities, and waited for before the constitutive pass (whose other inputs arrive meanwhile)
+    cudaEvent_t ev_moved = nullptr;
+    cudaEvent_t ev_need = nullptr;
 };
 // Host point arrays, page-locked and mapped (their device-accessible addresses), in the reference's
 // column-major layout (k components per point): the direct transfers of the mixed precisions, which
@@ -117,9 +121,11 @@ struct HostAoS {
 constexpr uint64_t MIXED_DIRECT_FIELDS = EP_MPTS_X | EP_MPTS_V | EP_MPTS_L | EP_MPTS_FIJ | EP_MPTS_BIJ | EP_MPTS_TAU |
                                          EP_MPTS_SIG | EP_MPTS_EPII | EP_MPTS_DLAM | EP_MPTS_DVIJ;
 // host arrays in `mask` -> the mixed layout, and the cell lists rebuilt from the host positions
-void mixed_import_host(const MixedCtx& X, const HostAoS& H, uint64_t mask, cudaStream_t s);
+// (bin = false: the arrays of the mask only, positions and cell lists untouched)
+void mixed_import_host(const MixedCtx& X, const HostAoS& H, uint64_t mask, cudaStream_t s, bool bin = true);
 // the mixed layout -> the host arrays in `mask`
-void mixed_export_host(const MixedCtx& X, const HostAoS& H, uint64_t mask, cudaStream_t s);
+// (par >= 0: the offsets of that parity, for x and v right after the G2P of a running step)
+void mixed_export_host(const MixedCtx& X, const HostAoS& H, uint64_t mask, cudaStream_t s, int par = -1);
 size_t mixed_ctx_size();
 // persistent batch kernel over n 2d mixed instances (nullptr + reason when the batch is not eligible)
 void* mixed_batch_create(const MixedCtx* const* xs, int n, std::string* why);

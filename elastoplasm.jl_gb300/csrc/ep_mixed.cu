@@ -2690,12 +2690,14 @@ __device__ __forceinline__ void xh_store(double* host, int k, int p0, int n, con
 // Direct upload: the host arrays in `mask` into the mixed layout as km_import converts them, and the
 // binning of km_bin0 from the host positions (which `mask` must include), in one pass over the points;
 // the cell counts are added once per distinct cell of a warp.
-__global__ void __launch_bounds__(XH_BS) km_import_host(MCtx A, HostAoS H, uint64_t mask) {
-    __shared__ double sb[XH_BS * XH_KMAX];
-    const int p0 = blockIdx.x * XH_BS, t = threadIdx.x, p = p0 + t;
+// bin = 0: the arrays of the mask only (the positions, offsets and cell counts are left alone)
+__device__ __forceinline__ void import_host_points(const MCtx& A, const HostAoS& H, uint64_t mask, int bin, int p0,
+                                                   double* sb) {
+    const int t = threadIdx.x, p = p0 + t;
     const int n = min(XH_BS, A.P.np - p0);
     const bool live = t < n;
     const int D = A.g.dim, NS = D == 2 ? 3 : 6, DD = D * D;
+    if (bin) {
     const int cur = A.ctl->parity;
     xh_load(H.x, D, p0, n, sb);
     int c2 = -1;
@@ -2721,6 +2723,7 @@ __global__ void __launch_bounds__(XH_BS) km_import_host(MCtx A, HostAoS H, uint6
     }
     const unsigned mm = __match_any_sync(0xffffffffu, c2);
     if (c2 >= 0 && (t & 31) == __ffs(mm) - 1) atomicAdd(&A.S.count[cur][c2], __popc(mm));
+    }
     if (mask & EP_MPTS_V) {
         xh_load(H.v, D, p0, n, sb);
         if (live)
@@ -2792,12 +2795,14 @@ __global__ void __launch_bounds__(XH_BS) km_import_host(MCtx A, HostAoS H, uint6
 }
 
 // Direct download: the arrays in `mask` from the mixed layout as km_export forms them.
-__global__ void __launch_bounds__(XH_BS) km_export_host(MCtx A, HostAoS H, uint64_t mask) {
-    __shared__ double sb[XH_BS * XH_KMAX];
-    const int p0 = blockIdx.x * XH_BS, t = threadIdx.x, p = p0 + t;
+// par >= 0: the offset buffer of the positions (a download of x and v right after the G2P, while the
+// rest of the step runs: the positions it wrote sit in the other parity until the step ends)
+__device__ __forceinline__ void export_host_points(const MCtx& A, const HostAoS& H, uint64_t mask, int par, int p0,
+                                                   double* sb) {
+    const int t = threadIdx.x, p = p0 + t;
     const int n = min(XH_BS, A.P.np - p0);
     const bool live = t < n;
-    const int cur = A.ctl->parity, D = A.g.dim, NS = D == 2 ? 3 : 6, DD = D * D;
+    const int cur = par >= 0 ? par : A.ctl->parity, D = A.g.dim, NS = D == 2 ? 3 : 6, DD = D * D;
     const bool fin = A.cf.deform == EP_DEFORM_FINITE;
     if (mask & EP_MPTS_X) {
         // a point without a cell (non-finite position) keeps the host's value: a block holding one
@@ -2886,6 +2891,23 @@ __global__ void __launch_bounds__(XH_BS) km_export_host(MCtx A, HostAoS H, uint6
         __syncthreads();
         if (live) sb[t] = (double)A.P.dlam[p];
         xh_store(H.dlam, 1, p0, n, sb);
+    }
+}
+
+// XH_BS points per block and pass; a grid smaller than the point blocks (the transfers that overlap
+// a running step) walks them, leaving the step's kernels room on the SMs
+__global__ void __launch_bounds__(XH_BS) km_import_host(MCtx A, HostAoS H, uint64_t mask, int bin) {
+    __shared__ double sb[XH_BS * XH_KMAX];
+    for (int p0 = blockIdx.x * XH_BS; p0 < A.P.np; p0 += gridDim.x * XH_BS) {
+        import_host_points(A, H, mask, bin, p0, sb);
+        __syncthreads();
+    }
+}
+__global__ void __launch_bounds__(XH_BS) km_export_host(MCtx A, HostAoS H, uint64_t mask, int par) {
+    __shared__ double sb[XH_BS * XH_KMAX];
+    for (int p0 = blockIdx.x * XH_BS; p0 < A.P.np; p0 += gridDim.x * XH_BS) {
+        export_host_points(A, H, mask, par, p0, sb);
+        __syncthreads();
     }
 }
 
@@ -4676,6 +4698,7 @@ static void mixed_step3_impl(const MixedCtx& X, int phase, cudaStream_t s) {
     if (A.cf.trsfr == EP_TRSFR_APIC) km_g2p_seg3<BASIS, DET, true><<<gs, 256, 0, s>>>(A);
     else km_g2p_seg3<BASIS, DET, false><<<gs, 256, 0, s>>>(A);
     mark("g2p");
+    if (X.ev_moved) cudaEventRecord(X.ev_moved, s);
     L += 3;
     if (A.cf.musl) {
         if (DET) {
@@ -4700,6 +4723,7 @@ static void mixed_step3_impl(const MixedCtx& X, int phase, cudaStream_t s) {
         mark("dJn");
         L += 2;
     }
+    if (X.ev_need) cudaStreamWaitEvent(s, X.ev_need, 0);  // the constitutive pass's other inputs
     if (np > 0 && A.cf.nonloc && phase == EP_PHASE_ELASTOPLASTIC) {
         km_nonlocal3<ACC><<<np, 32, 0, s>>>(A);
         mark("nonlocal");
@@ -4798,6 +4822,7 @@ static void mixed_step_impl(const MixedCtx& X, int phase, cudaStream_t s) {
     }
     mark("g2p");
     L += 2;                           // P2G, G2P
+    if (X.ev_moved) cudaEventRecord(X.ev_moved, s);     // positions and velocities of the step final
     if (A.cf.musl && !g2p_musl) {
         if (DET) {
             tile(std::integral_constant<int, 1>());
@@ -4839,6 +4864,7 @@ static void mixed_step_impl(const MixedCtx& X, int phase, cudaStream_t s) {
             L += 3;
         }
     }
+    if (X.ev_need) cudaStreamWaitEvent(s, X.ev_need, 0);  // the constitutive pass's other inputs
     if (np > 0 && A.cf.nonloc && phase == EP_PHASE_ELASTOPLASTIC) {
         km_nonlocal<ACC><<<np, 32, 0, s>>>(A);
         mark("nonlocal");
@@ -4940,20 +4966,28 @@ void mixed_import(const MixedCtx& X, const P64& Q, cudaStream_t s, uint64_t mask
     if (A.cf.det) km_sort_cells<<<(A.g.ncell + 255) / 256, 256, 0, s>>>(A, 1);
 }
 
-void mixed_import_host(const MixedCtx& X, const HostAoS& H, uint64_t mask, cudaStream_t s) {
+void mixed_import_host(const MixedCtx& X, const HostAoS& H, uint64_t mask, cudaStream_t s, bool bin) {
     const MCtx& A = *(const MCtx*)X.impl;
     const int np = A.P.np;
+    if (!bin) {
+        // beside a running step: one block per SM still keeps the host link busy
+        const int nb = std::min((np + XH_BS - 1) / XH_BS, sm_count());
+        if (np > 0 && mask) km_import_host<<<nb, XH_BS, 0, s>>>(A, H, mask, 0);
+        return;
+    }
     cudaMemsetAsync(X.sort_zero, 0, X.sort_zero_bytes, s);
-    if (np > 0) km_import_host<<<(np + XH_BS - 1) / XH_BS, XH_BS, 0, s>>>(A, H, mask);
+    if (np > 0) km_import_host<<<(np + XH_BS - 1) / XH_BS, XH_BS, 0, s>>>(A, H, mask, 1);
     mixed_initial_scan(X, s);
     if (np > 0) km_place0<<<(np + 255) / 256, 256, 0, s>>>(A);
     if (A.cf.det) km_sort_cells<<<(A.g.ncell + 255) / 256, 256, 0, s>>>(A, 1);
 }
 
-void mixed_export_host(const MixedCtx& X, const HostAoS& H, uint64_t mask, cudaStream_t s) {
+void mixed_export_host(const MixedCtx& X, const HostAoS& H, uint64_t mask, cudaStream_t s, int par) {
     const MCtx& A = *(const MCtx*)X.impl;
     const int np = A.P.np;
-    if (np > 0 && mask) km_export_host<<<(np + XH_BS - 1) / XH_BS, XH_BS, 0, s>>>(A, H, mask);
+    // par >= 0 runs beside the rest of a step: one block per SM
+    const int nb = par >= 0 ? std::min((np + XH_BS - 1) / XH_BS, sm_count()) : (np + XH_BS - 1) / XH_BS;
+    if (np > 0 && mask) km_export_host<<<nb, XH_BS, 0, s>>>(A, H, mask, par);
 }
 
 void mixed_export(const MixedCtx& X, const P64& Q, const N64& QN, cudaStream_t s, bool need_eps, uint64_t mask,
