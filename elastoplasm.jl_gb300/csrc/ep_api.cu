@@ -57,6 +57,12 @@ struct ep_handle {
     long long graph_kernels[2] = {0, 0};
     cudaGraphExec_t step_graph[2] = {nullptr, nullptr};   // one step (epgpu_step), dt and g from Ctl
     long long step_kernels[2] = {0, 0};
+    // epgpu_profile: the one-step graph with an event between kernels (for the phase it was taken in),
+    // the number of its marks and their names
+    cudaGraphExec_t prof_graph = nullptr;
+    int prof_phase = -1, prof_n = 0;
+    long long prof_kernels = 0;
+    std::vector<const char*> prof_names;
     int graph_gen = 0;            // bumped whenever the captured kernels' arguments change
     long long launches = 0;
     int64_t steps = 0;
@@ -174,6 +180,9 @@ static void drop_graphs(ep_handle* h) {
         h->graph_def[i] = nullptr;
         h->step_graph[i] = nullptr;
     }
+    if (h->prof_graph) cudaGraphExecDestroy(h->prof_graph);
+    h->prof_graph = nullptr;
+    h->prof_phase = -1;
 }
 
 ep_status epgpu_destroy(ep_handle* h) {
@@ -1015,21 +1024,46 @@ ep_status epgpu_step(ep_handle* h, int32_t phase, double dt, const double* g, do
         CK(h, cudaGraphLaunch(h->step_graph[phase], h->s));
         h->launches += h->step_kernels[phase];
     } else {
-        Fp64Ctx ctx = h->ctx;
-        ctx.prof = &h->prof;
-        if (!h->mixed) {
-            launch_ctl_begin_step(h->ctl, h->dim, h->s);
-            h->launches += 1;
+        // the step as the timed graph runs it, captured with an event recorded after every kernel:
+        // the per-kernel times hold no host launch gaps
+        if (h->prof_phase != phase) {
+            if (h->prof_graph) cudaGraphExecDestroy(h->prof_graph);
+            h->prof_graph = nullptr;
+            h->prof_phase = -1;
+            const long long l0 = h->launches;
+            h->prof.reserve(64);
+            cudaGraph_t gr;
+            CK(h, cudaStreamBeginCapture(h->s, cudaStreamCaptureModeThreadLocal));
+            Fp64Ctx ctx = h->ctx;
+            ctx.prof = &h->prof;
+            if (!h->mixed) {
+                launch_ctl_begin_step(h->ctl, h->dim, h->s);
+                h->launches += 1;
+            }
+            h->prof.begin(h->s);
+            if (h->mixed) {
+                MixedCtx mx = h->mx;
+                mx.prof = &h->prof;
+                mx.begin_step = 1;
+                mixed_step(mx, phase, h->s);
+            } else {
+                fp64_step(ctx, phase, h->s);
+            }
+            cudaError_t e = cudaStreamEndCapture(h->s, &gr);
+            h->prof_kernels = h->launches - l0;
+            h->launches = l0;
+            if (e != cudaSuccess) return cuda_fail(h, e, "profiled step capture");
+            e = cudaGraphInstantiate(&h->prof_graph, gr, 0);
+            cudaGraphDestroy(gr);
+            if (e != cudaSuccess) return cuda_fail(h, e, "profiled step instantiate");
+            h->prof_phase = phase;
+            h->prof_n = h->prof.n;
+            h->prof_names.assign(h->prof.name.begin(), h->prof.name.begin() + h->prof.n);
         }
-        h->prof.begin(h->s);
-        if (h->mixed) {
-            MixedCtx mx = h->mx;
-            mx.prof = &h->prof;
-            mx.begin_step = 1;
-            mixed_step(mx, phase, h->s);
-        } else {
-            fp64_step(ctx, phase, h->s);
-        }
+        h->prof.n = h->prof_n;
+        for (int i = 0; i < h->prof_n; ++i) h->prof.name[i] = h->prof_names[i];
+        CK(h, cudaGraphLaunch(h->prof_graph, h->s));
+        h->launches += h->prof_kernels;
     }
     CK(h, cudaEventRecord(h->ev1, h->s));
     CK(h, cudaGetLastError());

@@ -25,6 +25,15 @@ struct Prof {
         n = 0;
         mark("begin", s);
     }
+    // the events made ahead (a capture records into them without creating any)
+    void reserve(int k) {
+        while ((int)ev.size() < k) {
+            cudaEvent_t e;
+            if (cudaEventCreate(&e) != cudaSuccess) return;
+            ev.push_back(e);
+            name.push_back(nullptr);
+        }
+    }
     void mark(const char* nm, cudaStream_t s) {
         if (!on) return;
         if (n >= (int)ev.size()) {
@@ -33,7 +42,11 @@ struct Prof {
             ev.push_back(e);
             name.push_back(nullptr);
         }
-        cudaEventRecord(ev[n], s);
+        // inside a stream capture (the profiled step graph) the record must be a node of the graph
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        cudaStreamIsCapturing(s, &cs);
+        if (cs == cudaStreamCaptureStatusActive) cudaEventRecordWithFlags(ev[n], s, cudaEventRecordExternal);
+        else cudaEventRecord(ev[n], s);
         name[n] = nm;
         ++n;
     }

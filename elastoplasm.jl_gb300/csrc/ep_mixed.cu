@@ -2534,13 +2534,15 @@ static int max_tile_box(const Geo& g, int TC) {
 // Launch with programmatic stream serialization (the kernel calls pdl_enter() first), so that its
 // blocks are scheduled while the previous kernel of the stream drains; EPGPU_PDL=0 in the
 // environment launches plainly instead.
+// (off while a profiled step is launched: an event between two kernels leaves no programmatic edge)
+static thread_local bool g_pdl_suspended = false;
 static bool pdl_on() {
     static int on = -1;
     if (on < 0) {
         const char* e = getenv("EPGPU_PDL");
         on = (e && e[0] == '0') ? 0 : 1;
     }
-    return on != 0;
+    return on != 0 && !g_pdl_suspended;
 }
 
 template <typename... K, typename... Args>
@@ -4918,6 +4920,11 @@ static void mixed_step_acc(const MixedCtx& X, int phase, cudaStream_t s) {
 }
 
 void mixed_step(const MixedCtx& X, int phase, cudaStream_t s) {
+    struct PdlScope {
+        bool old;
+        explicit PdlScope(bool off) : old(g_pdl_suspended) { g_pdl_suspended = off || old; }
+        ~PdlScope() { g_pdl_suspended = old; }
+    } pdl_scope(X.prof && X.prof->on);
     const MCtx& A = *(const MCtx*)X.impl;
     if (A.g.dim == 3) {
         const int b = A.cf.basis;

@@ -922,6 +922,33 @@ ep_status epgpu_mlp_forward(ep_mlp* m, const float* x, int64_t n, float* y) {
     return mlp_check_err(m);
 }
 
+ep_status epgpu_mlp_time(ep_mlp* m, int64_t n, int32_t reps, double* ms_per_launch) {
+    if (!m || !ms_per_launch || n <= 0 || n > (1 << 30) || reps <= 0) return EP_ERR_ARG;
+    ep_status st;
+    if ((st = ensure_batch(m, (int)n)) != EP_OK) return st;
+    MlpDev& d = m->d;
+    MCK(m, cudaMemsetAsync(d.X, 0, (size_t)n * RM_NX * sizeof(float), m->s));
+    mlp_fwd_launch(m, d.X, (int)n, nullptr, d.Y, false, m->s);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    MCK(m, cudaEventCreate(&e0));
+    cudaError_t e = cudaEventCreate(&e1);
+    if (e == cudaSuccess) e = cudaEventRecord(e0, m->s);
+    for (int i = 0; i < reps && e == cudaSuccess; ++i) {
+        mlp_fwd_launch(m, d.X, (int)n, nullptr, d.Y, false, m->s);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(e1, m->s);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    MCK(m, e);
+    if ((st = mlp_check_err(m)) != EP_OK) return st;
+    *ms_per_launch = (double)ms / reps;
+    return EP_OK;
+}
+
 ep_status epgpu_mlp_grad(ep_mlp* m, const float* x, const float* t, int64_t n, float* grad, double* loss) {
     if (!m || !x || !t || !grad || n <= 0 || n > (1 << 26)) return EP_ERR_ARG;
     ep_status st;

@@ -217,6 +217,7 @@ SIGNATURES = {
     "epgpu_mlp_set_params": (C.c_int, [C.c_void_p, _F, C.c_int64]),
     "epgpu_mlp_get_params": (C.c_int, [C.c_void_p, _F, C.c_int64]),
     "epgpu_mlp_forward": (C.c_int, [C.c_void_p, _F, C.c_int64, _F]),
+    "epgpu_mlp_time": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.POINTER(C.c_double)]),
     "epgpu_mlp_grad": (C.c_int, [C.c_void_p, _F, _F, C.c_int64, _F, _D]),
     "epgpu_mlp_train": (C.c_int, [C.c_void_p, _F, _F, C.c_int64, C.c_int32, C.c_int32, C.c_float, C.c_uint64,
                                   _D]),

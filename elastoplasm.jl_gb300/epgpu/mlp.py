@@ -86,6 +86,12 @@ class MLP:
         self._check(self.lib.epgpu_mlp_forward(self.h, _fp(x), x.shape[0], _fp(y)))
         return y
 
+    def time_forward(self, n: int, reps: int = 20) -> float:
+        """Device ms of one forward launch over n rows (the kernel alone, CUDA events)."""
+        ms = C.c_double(0.0)
+        self._check(self.lib.epgpu_mlp_time(self.h, int(n), int(reps), C.byref(ms)))
+        return ms.value
+
     def grad(self, x, t):
         x, t = _f32(x, NX), _f32(t, NY)
         g = np.zeros(NPARAM, dtype=np.float32)

@@ -456,6 +456,11 @@ ep_status epgpu_mlp_set_params(ep_mlp* m, const float* params, int64_t n);
 ep_status epgpu_mlp_get_params(ep_mlp* m, float* params, int64_t n);
 /* y (n x EP_MLP_NY) = network(x (n x EP_MLP_NX)), host buffers. */
 ep_status epgpu_mlp_forward(ep_mlp* m, const float* x, int64_t n, float* y);
+/* Device time of the forward kernel alone over n rows (zero features in the network's own buffer;
+ * the work per row does not depend on the values): one untimed launch, then reps launches between
+ * two CUDA events on the network's stream; *ms_per_launch = their mean.  No counterpart in the
+ * reference: the measurement of the tensor-core kernel the learned return map runs in each step. */
+ep_status epgpu_mlp_time(ep_mlp* m, int64_t n, int32_t reps, double* ms_per_launch);
 /* Gradient of the loss sum((y - t)^2) / (3 n) over the 3 outputs, from one
  * forward and backward pass on the tensor cores; t is n x EP_MLP_NY. */
 ep_status epgpu_mlp_grad(ep_mlp* m, const float* x, const float* t, int64_t n, float* grad, double* loss);

@@ -34,6 +34,18 @@ def test_forward_matches_oracle(n):
     assert _rel(y[:, :3], ref) < 5e-3
 
 
+
+def test_forward_kernel_time_alone():
+    """epgpu_mlp_time: the forward kernel's own device time over n rows is positive and implies a rate
+    below twice the dense bf16 tensor peak of the part (100,608 flop per row)."""
+    from epgpu.mlp import MLP
+    net = MLP(seed=7, l2g=L2G)
+    for n in (128, 97_600):
+        ms = net.time_forward(n, 10)
+        tf = 100608.0 * n / (ms * 1e-3) / 1e12
+        print(f"forward alone n={n}: {ms * 1e3:.1f} us, {tf:.0f} TFLOP/s")
+        assert 0.0 < ms < 50.0 and tf < 2 * 2250.0
+
 def test_gradient_matches_oracle():
     from epgpu.mlp import MLP
     import mlp_oracle as mo
