@@ -74,6 +74,9 @@ struct ep_handle {
     // epgpu_step_fields: the second stream of its overlapped transfers and their events (made on first use)
     cudaStream_t s2 = nullptr;
     cudaEvent_t ev_up = nullptr, ev_late = nullptr, ev_moved = nullptr, ev_dn = nullptr;
+    // its step as a graph with the event nodes of the overlap: [phase + 2 late inputs + 4 early outputs]
+    cudaGraphExec_t fields_graph[8] = {};
+    long long fields_kernels[8] = {};
     Prof prof;
     bool mixed = false;
     MixedCtx mx{};
@@ -183,6 +186,10 @@ static void drop_graphs(ep_handle* h) {
     if (h->prof_graph) cudaGraphExecDestroy(h->prof_graph);
     h->prof_graph = nullptr;
     h->prof_phase = -1;
+    for (int i = 0; i < 8; ++i) {
+        if (h->fields_graph[i]) cudaGraphExecDestroy(h->fields_graph[i]);
+        h->fields_graph[i] = nullptr;
+    }
 }
 
 ep_status epgpu_destroy(ep_handle* h) {
@@ -982,6 +989,29 @@ static ep_status kernel_error(ep_handle* h) {
 
 // one step captured once per phase: epgpu_step replays it (no per-kernel host launches); the
 // eager path stays for per-kernel profiling (events between kernels)
+// the step of epgpu_step_fields's direct path: the one-step graph plus, as external event nodes, the
+// wait for the late inputs before the constitutive pass and the record once the G2P is done
+static ep_status build_fields_graph(ep_handle* h, int phase, bool late, bool early) {
+    const int gi = phase + (late ? 2 : 0) + (early ? 4 : 0);
+    if (h->fields_graph[gi]) return EP_OK;
+    cudaGraph_t gr;
+    const long long l0 = h->launches;
+    CK(h, cudaStreamBeginCapture(h->s, cudaStreamCaptureModeThreadLocal));
+    MixedCtx mx = h->mx;
+    mx.begin_step = 1;
+    mx.ev_need = late ? h->ev_late : nullptr;
+    mx.ev_moved = early ? h->ev_moved : nullptr;
+    mixed_step(mx, phase, h->s);
+    cudaError_t e = cudaStreamEndCapture(h->s, &gr);
+    h->fields_kernels[gi] = h->launches - l0;
+    h->launches = l0;
+    if (e != cudaSuccess) return cuda_fail(h, e, "step_fields graph capture");
+    e = cudaGraphInstantiate(&h->fields_graph[gi], gr, 0);
+    cudaGraphDestroy(gr);
+    if (e != cudaSuccess) return cuda_fail(h, e, "step_fields graph instantiate");
+    return EP_OK;
+}
+
 static ep_status build_step_graph(ep_handle* h, int phase) {
     if (h->step_graph[phase]) return EP_OK;
     cudaGraph_t gr;
@@ -1211,25 +1241,24 @@ ep_status epgpu_step_fields(ep_handle* h, ep_mpts_view* m, uint64_t mask_in, int
     constexpr uint64_t LATE_IN = EP_MPTS_FIJ | EP_MPTS_BIJ | EP_MPTS_EPII | EP_MPTS_DLAM;
     constexpr uint64_t EARLY_OUT = EP_MPTS_X | EP_MPTS_V;
     const uint64_t late_in = din & LATE_IN, early_out = dout & EARLY_OUT;
+    const int gi = phase + (late_in ? 2 : 0) + (early_out ? 4 : 0);
+    if ((st = build_fields_graph(h, phase, late_in != 0, early_out != 0)) != EP_OK) return st;
     reset_ctl(h, &vin);
     CK(h, cudaMemcpyAsync(h->ctl, h->hctl, sizeof(Ctl), cudaMemcpyHostToDevice, h->s));
     mixed_import_host(h->mx, Hin, din & ~late_in, h->s);           // positions (cell lists), v, ℓ, τ, ∇v
-    MixedCtx mx = h->mx;
-    mx.begin_step = 1;                                             // km_zero starts the step
     if (late_in) {
         CK(h, cudaEventRecord(h->ev_up, h->s));                    // one link direction: in turn
         CK(h, cudaStreamWaitEvent(h->s2, h->ev_up, 0));
         mixed_import_host(h->mx, Hin, late_in, h->s2, false);
-        CK(h, cudaEventRecord(h->ev_late, h->s2));
-        mx.ev_need = h->ev_late;
+        CK(h, cudaEventRecord(h->ev_late, h->s2));                 // waited for in the graph
     }
-    if (early_out) mx.ev_moved = h->ev_moved;
     double gg[3];
     for (int i = 0; i < 3; ++i) gg[i] = i < h->dim ? g[i] : 0.0;
     launch_ctl_set_step(h->ctl, dt, gg, phase, h->s);
     CK(h, cudaGetLastError());
     CK(h, cudaEventRecord(h->ev0, h->s));
-    mixed_step(mx, phase, h->s);                                   // counts its launches
+    CK(h, cudaGraphLaunch(h->fields_graph[gi], h->s));            // records ev_moved after the G2P
+    h->launches += h->fields_kernels[gi];
     CK(h, cudaEventRecord(h->ev1, h->s));
     if (early_out) {
         // reset_ctl starts the step at parity 0: its G2P writes the offsets of parity 1

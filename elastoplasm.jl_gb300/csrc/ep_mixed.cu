@@ -2534,15 +2534,35 @@ static int max_tile_box(const Geo& g, int TC) {
 // Launch with programmatic stream serialization (the kernel calls pdl_enter() first), so that its
 // blocks are scheduled while the previous kernel of the stream drains; EPGPU_PDL=0 in the
 // environment launches plainly instead.
-// (off while a profiled step is launched: an event between two kernels leaves no programmatic edge)
+// (off while a profiled step is launched, and for the one launch after an event record or wait of the
+// step_fields hooks: an event between two kernels leaves no programmatic edge)
 static thread_local bool g_pdl_suspended = false;
+static thread_local bool g_pdl_skip_next = false;
 static bool pdl_on() {
     static int on = -1;
     if (on < 0) {
         const char* e = getenv("EPGPU_PDL");
         on = (e && e[0] == '0') ? 0 : 1;
     }
-    return on != 0 && !g_pdl_suspended;
+    const bool skip = g_pdl_skip_next;
+    g_pdl_skip_next = false;
+    return on != 0 && !g_pdl_suspended && !skip;
+}
+
+// event record / wait of the step_fields hooks: external nodes when the stream is being captured (a
+// plain record or wait inside a capture only orders the capture's own nodes)
+static bool capturing(cudaStream_t s) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    return cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusActive;
+}
+static void hook_record(cudaEvent_t e, cudaStream_t s) {
+    if (capturing(s)) cudaEventRecordWithFlags(e, s, cudaEventRecordExternal);
+    else cudaEventRecord(e, s);
+    g_pdl_skip_next = true;
+}
+static void hook_wait(cudaStream_t s, cudaEvent_t e) {
+    cudaStreamWaitEvent(s, e, capturing(s) ? cudaEventWaitExternal : 0);
+    g_pdl_skip_next = true;
 }
 
 template <typename... K, typename... Args>
@@ -4700,7 +4720,7 @@ static void mixed_step3_impl(const MixedCtx& X, int phase, cudaStream_t s) {
     if (A.cf.trsfr == EP_TRSFR_APIC) km_g2p_seg3<BASIS, DET, true><<<gs, 256, 0, s>>>(A);
     else km_g2p_seg3<BASIS, DET, false><<<gs, 256, 0, s>>>(A);
     mark("g2p");
-    if (X.ev_moved) cudaEventRecord(X.ev_moved, s);
+    if (X.ev_moved) hook_record(X.ev_moved, s);
     L += 3;
     if (A.cf.musl) {
         if (DET) {
@@ -4725,7 +4745,7 @@ static void mixed_step3_impl(const MixedCtx& X, int phase, cudaStream_t s) {
         mark("dJn");
         L += 2;
     }
-    if (X.ev_need) cudaStreamWaitEvent(s, X.ev_need, 0);  // the constitutive pass's other inputs
+    if (X.ev_need) hook_wait(s, X.ev_need);              // the constitutive pass's other inputs
     if (np > 0 && A.cf.nonloc && phase == EP_PHASE_ELASTOPLASTIC) {
         km_nonlocal3<ACC><<<np, 32, 0, s>>>(A);
         mark("nonlocal");
@@ -4824,7 +4844,7 @@ static void mixed_step_impl(const MixedCtx& X, int phase, cudaStream_t s) {
     }
     mark("g2p");
     L += 2;                           // P2G, G2P
-    if (X.ev_moved) cudaEventRecord(X.ev_moved, s);     // positions and velocities of the step final
+    if (X.ev_moved) hook_record(X.ev_moved, s);         // positions and velocities of the step final
     if (A.cf.musl && !g2p_musl) {
         if (DET) {
             tile(std::integral_constant<int, 1>());
@@ -4866,7 +4886,7 @@ static void mixed_step_impl(const MixedCtx& X, int phase, cudaStream_t s) {
             L += 3;
         }
     }
-    if (X.ev_need) cudaStreamWaitEvent(s, X.ev_need, 0);  // the constitutive pass's other inputs
+    if (X.ev_need) hook_wait(s, X.ev_need);              // the constitutive pass's other inputs
     if (np > 0 && A.cf.nonloc && phase == EP_PHASE_ELASTOPLASTIC) {
         km_nonlocal<ACC><<<np, 32, 0, s>>>(A);
         mark("nonlocal");
@@ -4923,7 +4943,10 @@ void mixed_step(const MixedCtx& X, int phase, cudaStream_t s) {
     struct PdlScope {
         bool old;
         explicit PdlScope(bool off) : old(g_pdl_suspended) { g_pdl_suspended = off || old; }
-        ~PdlScope() { g_pdl_suspended = old; }
+        ~PdlScope() {
+            g_pdl_suspended = old;
+            g_pdl_skip_next = false;
+        }
     } pdl_scope(X.prof && X.prof->on);
     const MCtx& A = *(const MCtx*)X.impl;
     if (A.g.dim == 3) {

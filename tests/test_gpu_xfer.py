@@ -197,9 +197,12 @@ def test_direct_and_staged_masked_transfers_agree(dim, precision):
 @pytest.mark.parametrize("pinned", [False, True])
 @pytest.mark.parametrize("precision", ["fp64", "mixed_df"])
 def test_step_fields_equals_the_three_calls(precision, pinned):
-    """epgpu_step_fields (upload, step, download in one call: back to back on the device for mapped
-    page-locked arrays in the mixed precisions) against epgpu_upload_fields + epgpu_step +
-    epgpu_download_fields: the same bits on the host and the same vmax after every step."""
+    """epgpu_step_fields (upload, step, download in one call: for mapped page-locked arrays in the
+    mixed precisions on the device with one synchronisation, part of the arrays moving on a second
+    stream beside the step) against epgpu_upload_fields + epgpu_step + epgpu_download_fields: the same
+    bits on the host and the same vmax after every step.  The host changes the moved arrays between
+    steps, so that a step reading an array before its upload landed, or a download taken before the
+    step wrote it, shows."""
     from epgpu import Engine, ic_slump
     ic, cfg = ic_slump(*C1, nonloc={"status": False, "ls": 0.5})
     instr = copy.deepcopy(cfg["instr"])
@@ -221,6 +224,11 @@ def test_step_fields_equals_the_three_calls(precision, pinned):
                 e.download_fields(host, moved)
             vs.append(np.array(vm))
             seen.append({f: np.array(getattr(host, f)) for f in moved})
+            # a host loop's own change of the state before the next step
+            getattr(host, "Fij")[...] *= 1.0 + 1e-4
+            getattr(host, "epII")[...] += 1e-6
+            getattr(host, "v")[...] *= 0.999
+            getattr(host, "x")[...] += 1e-5
         assert e.stats()["steps"] == 5
         out.append((vs, seen))
         e.close()
