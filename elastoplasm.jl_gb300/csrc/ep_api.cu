@@ -74,9 +74,13 @@ struct ep_handle {
     // epgpu_step_fields: the second stream of its overlapped transfers and their events (made on first use)
     cudaStream_t s2 = nullptr;
     cudaEvent_t ev_up = nullptr, ev_late = nullptr, ev_moved = nullptr, ev_dn = nullptr;
-    // its step as a graph with the event nodes of the overlap: [phase + 2 late inputs + 4 early outputs]
-    cudaGraphExec_t fields_graph[8] = {};
-    long long fields_kernels[8] = {};
+    // the whole call as one graph (uploads, step, downloads; the overlapped transfers as branches on s2),
+    // kept for the configuration it was captured with: phase, masks and host array addresses
+    cudaGraphExec_t fields_graph = nullptr;
+    long long fields_kernels = 0;
+    int fields_phase = -1;
+    uint64_t fields_in = 0, fields_out = 0;
+    HostAoS fields_hin{}, fields_hout{};
     Prof prof;
     bool mixed = false;
     MixedCtx mx{};
@@ -186,10 +190,9 @@ static void drop_graphs(ep_handle* h) {
     if (h->prof_graph) cudaGraphExecDestroy(h->prof_graph);
     h->prof_graph = nullptr;
     h->prof_phase = -1;
-    for (int i = 0; i < 8; ++i) {
-        if (h->fields_graph[i]) cudaGraphExecDestroy(h->fields_graph[i]);
-        h->fields_graph[i] = nullptr;
-    }
+    if (h->fields_graph) cudaGraphExecDestroy(h->fields_graph);
+    h->fields_graph = nullptr;
+    h->fields_phase = -1;
 }
 
 ep_status epgpu_destroy(ep_handle* h) {
@@ -989,26 +992,60 @@ static ep_status kernel_error(ep_handle* h) {
 
 // one step captured once per phase: epgpu_step replays it (no per-kernel host launches); the
 // eager path stays for per-kernel profiling (events between kernels)
-// the step of epgpu_step_fields's direct path: the one-step graph plus, as external event nodes, the
-// wait for the late inputs before the constitutive pass and the record once the G2P is done
-static ep_status build_fields_graph(ep_handle* h, int phase, bool late, bool early) {
-    const int gi = phase + (late ? 2 : 0) + (early ? 4 : 0);
-    if (h->fields_graph[gi]) return EP_OK;
+// epgpu_step_fields's direct path as one graph: the upload of the early arrays (positions with the
+// initial cell lists, v, ℓ, τ, ∇v), the step, the download of the late arrays on the stream, and two
+// branches on s2 forked and joined inside the capture: the late inputs (read only by the constitutive
+// pass) going up while the step's first kernels run, and x and v coming down once the G2P is done
+static bool same_aos(const HostAoS& a, const HostAoS& b) { return std::memcmp(&a, &b, sizeof(HostAoS)) == 0; }
+static ep_status build_fields_graph(ep_handle* h, int phase, const HostAoS& Hin, uint64_t din, const HostAoS& Hout,
+                                    uint64_t dout) {
+    if (h->fields_graph && h->fields_phase == phase && h->fields_in == din && h->fields_out == dout &&
+        same_aos(h->fields_hin, Hin) && same_aos(h->fields_hout, Hout))
+        return EP_OK;
+    if (h->fields_graph) cudaGraphExecDestroy(h->fields_graph);
+    h->fields_graph = nullptr;
+    h->fields_phase = -1;
+    constexpr uint64_t LATE_IN = EP_MPTS_FIJ | EP_MPTS_BIJ | EP_MPTS_EPII | EP_MPTS_DLAM;
+    constexpr uint64_t EARLY_OUT = EP_MPTS_X | EP_MPTS_V;
+    const uint64_t late_in = din & LATE_IN, early_out = dout & EARLY_OUT;
     cudaGraph_t gr;
     const long long l0 = h->launches;
     CK(h, cudaStreamBeginCapture(h->s, cudaStreamCaptureModeThreadLocal));
+    mixed_import_host(h->mx, Hin, din & ~late_in, h->s);
+    if (late_in) {
+        cudaEventRecord(h->ev_up, h->s);                           // one link direction: in turn
+        cudaStreamWaitEvent(h->s2, h->ev_up, 0);
+        mixed_import_host(h->mx, Hin, late_in, h->s2, false);
+        cudaEventRecord(h->ev_late, h->s2);
+    }
+    cudaEventRecordWithFlags(h->ev0, h->s, cudaEventRecordExternal);
     MixedCtx mx = h->mx;
     mx.begin_step = 1;
-    mx.ev_need = late ? h->ev_late : nullptr;
-    mx.ev_moved = early ? h->ev_moved : nullptr;
+    mx.hooks_internal = true;
+    mx.ev_need = late_in ? h->ev_late : nullptr;                  // joined before the constitutive pass
+    mx.ev_moved = early_out ? h->ev_moved : nullptr;              // forked after the G2P
     mixed_step(mx, phase, h->s);
+    cudaEventRecordWithFlags(h->ev1, h->s, cudaEventRecordExternal);
+    if (early_out) {
+        // reset_ctl starts the step at parity 0: its G2P writes the offsets of parity 1
+        cudaStreamWaitEvent(h->s2, h->ev_moved, 0);
+        mixed_export_host(h->mx, Hout, early_out, h->s2, 1);
+        cudaEventRecord(h->ev_dn, h->s2);
+    }
+    mixed_export_host(h->mx, Hout, dout & ~early_out, h->s);
+    if (early_out) cudaStreamWaitEvent(h->s, h->ev_dn, 0);
     cudaError_t e = cudaStreamEndCapture(h->s, &gr);
-    h->fields_kernels[gi] = h->launches - l0;
+    h->fields_kernels = h->launches - l0;
     h->launches = l0;
     if (e != cudaSuccess) return cuda_fail(h, e, "step_fields graph capture");
-    e = cudaGraphInstantiate(&h->fields_graph[gi], gr, 0);
+    e = cudaGraphInstantiate(&h->fields_graph, gr, 0);
     cudaGraphDestroy(gr);
     if (e != cudaSuccess) return cuda_fail(h, e, "step_fields graph instantiate");
+    h->fields_phase = phase;
+    h->fields_in = din;
+    h->fields_out = dout;
+    h->fields_hin = Hin;
+    h->fields_hout = Hout;
     return EP_OK;
 }
 
@@ -1229,45 +1266,21 @@ ep_status epgpu_step_fields(ep_handle* h, ep_mpts_view* m, uint64_t mask_in, int
     // follow the rest of the upload on a second stream while the step's first kernels run, and the
     // positions and velocities, final after the G2P, go down on that stream during the rest of the step.
     if (!h->s2) {
-        // the highest priority: its few blocks take the SM slots the step's kernels free first
-        int lo = 0, hi = 0;
-        cudaDeviceGetStreamPriorityRange(&lo, &hi);
-        cudaError_t e = cudaStreamCreateWithPriority(&h->s2, cudaStreamNonBlocking, hi);
+        cudaError_t e = cudaStreamCreateWithFlags(&h->s2, cudaStreamNonBlocking);
         for (cudaEvent_t* ev : {&h->ev_up, &h->ev_late, &h->ev_moved, &h->ev_dn})
             if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
         if (e != cudaSuccess) return cuda_fail(h, e, "step_fields: second stream");
     }
     ep_status st;
-    constexpr uint64_t LATE_IN = EP_MPTS_FIJ | EP_MPTS_BIJ | EP_MPTS_EPII | EP_MPTS_DLAM;
-    constexpr uint64_t EARLY_OUT = EP_MPTS_X | EP_MPTS_V;
-    const uint64_t late_in = din & LATE_IN, early_out = dout & EARLY_OUT;
-    const int gi = phase + (late_in ? 2 : 0) + (early_out ? 4 : 0);
-    if ((st = build_fields_graph(h, phase, late_in != 0, early_out != 0)) != EP_OK) return st;
+    if ((st = build_fields_graph(h, phase, Hin, din, Hout, dout)) != EP_OK) return st;
     reset_ctl(h, &vin);
     CK(h, cudaMemcpyAsync(h->ctl, h->hctl, sizeof(Ctl), cudaMemcpyHostToDevice, h->s));
-    mixed_import_host(h->mx, Hin, din & ~late_in, h->s);           // positions (cell lists), v, ℓ, τ, ∇v
-    if (late_in) {
-        CK(h, cudaEventRecord(h->ev_up, h->s));                    // one link direction: in turn
-        CK(h, cudaStreamWaitEvent(h->s2, h->ev_up, 0));
-        mixed_import_host(h->mx, Hin, late_in, h->s2, false);
-        CK(h, cudaEventRecord(h->ev_late, h->s2));                 // waited for in the graph
-    }
     double gg[3];
     for (int i = 0; i < 3; ++i) gg[i] = i < h->dim ? g[i] : 0.0;
     launch_ctl_set_step(h->ctl, dt, gg, phase, h->s);
     CK(h, cudaGetLastError());
-    CK(h, cudaEventRecord(h->ev0, h->s));
-    CK(h, cudaGraphLaunch(h->fields_graph[gi], h->s));            // records ev_moved after the G2P
-    h->launches += h->fields_kernels[gi];
-    CK(h, cudaEventRecord(h->ev1, h->s));
-    if (early_out) {
-        // reset_ctl starts the step at parity 0: its G2P writes the offsets of parity 1
-        CK(h, cudaStreamWaitEvent(h->s2, h->ev_moved, 0));
-        mixed_export_host(h->mx, Hout, early_out, h->s2, h->hctl->parity ^ 1);
-        CK(h, cudaEventRecord(h->ev_dn, h->s2));
-    }
-    mixed_export_host(h->mx, Hout, dout & ~early_out, h->s);
-    if (early_out) CK(h, cudaStreamWaitEvent(h->s, h->ev_dn, 0));
+    CK(h, cudaGraphLaunch(h->fields_graph, h->s));                // ev0 and ev1 bracket the step inside
+    h->launches += h->fields_kernels;
     CK(h, cudaGetLastError());
     if ((st = read_ctl(h)) != EP_OK) return st;              // synchronizes: the host arrays are written
     float ms = 0.f;

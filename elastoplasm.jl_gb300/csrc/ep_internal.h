@@ -123,6 +123,7 @@ struct MixedCtx {
     // velocities, and waited for before the constitutive pass (whose other inputs arrive meanwhile)
     cudaEvent_t ev_moved = nullptr;
     cudaEvent_t ev_need = nullptr;
+    bool hooks_internal = false;      // in a capture: fork / join events of that capture, not external nodes
 };
 // Host point arrays, page-locked and mapped (their device-accessible addresses), in the reference's
 // column-major layout (k components per point): the direct transfers of the mixed precisions, which

@@ -2555,13 +2555,13 @@ static bool capturing(cudaStream_t s) {
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     return cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusActive;
 }
-static void hook_record(cudaEvent_t e, cudaStream_t s) {
-    if (capturing(s)) cudaEventRecordWithFlags(e, s, cudaEventRecordExternal);
+static void hook_record(cudaEvent_t e, cudaStream_t s, bool internal) {
+    if (!internal && capturing(s)) cudaEventRecordWithFlags(e, s, cudaEventRecordExternal);
     else cudaEventRecord(e, s);
     g_pdl_skip_next = true;
 }
-static void hook_wait(cudaStream_t s, cudaEvent_t e) {
-    cudaStreamWaitEvent(s, e, capturing(s) ? cudaEventWaitExternal : 0);
+static void hook_wait(cudaStream_t s, cudaEvent_t e, bool internal) {
+    cudaStreamWaitEvent(s, e, (!internal && capturing(s)) ? cudaEventWaitExternal : 0);
     g_pdl_skip_next = true;
 }
 
@@ -4720,7 +4720,7 @@ static void mixed_step3_impl(const MixedCtx& X, int phase, cudaStream_t s) {
     if (A.cf.trsfr == EP_TRSFR_APIC) km_g2p_seg3<BASIS, DET, true><<<gs, 256, 0, s>>>(A);
     else km_g2p_seg3<BASIS, DET, false><<<gs, 256, 0, s>>>(A);
     mark("g2p");
-    if (X.ev_moved) hook_record(X.ev_moved, s);
+    if (X.ev_moved) hook_record(X.ev_moved, s, X.hooks_internal);
     L += 3;
     if (A.cf.musl) {
         if (DET) {
@@ -4745,7 +4745,7 @@ static void mixed_step3_impl(const MixedCtx& X, int phase, cudaStream_t s) {
         mark("dJn");
         L += 2;
     }
-    if (X.ev_need) hook_wait(s, X.ev_need);              // the constitutive pass's other inputs
+    if (X.ev_need) hook_wait(s, X.ev_need, X.hooks_internal);   // the constitutive pass's other inputs
     if (np > 0 && A.cf.nonloc && phase == EP_PHASE_ELASTOPLASTIC) {
         km_nonlocal3<ACC><<<np, 32, 0, s>>>(A);
         mark("nonlocal");
@@ -4844,7 +4844,7 @@ static void mixed_step_impl(const MixedCtx& X, int phase, cudaStream_t s) {
     }
     mark("g2p");
     L += 2;                           // P2G, G2P
-    if (X.ev_moved) hook_record(X.ev_moved, s);         // positions and velocities of the step final
+    if (X.ev_moved) hook_record(X.ev_moved, s, X.hooks_internal);   // positions and velocities final
     if (A.cf.musl && !g2p_musl) {
         if (DET) {
             tile(std::integral_constant<int, 1>());
@@ -4886,7 +4886,7 @@ static void mixed_step_impl(const MixedCtx& X, int phase, cudaStream_t s) {
             L += 3;
         }
     }
-    if (X.ev_need) hook_wait(s, X.ev_need);              // the constitutive pass's other inputs
+    if (X.ev_need) hook_wait(s, X.ev_need, X.hooks_internal);   // the constitutive pass's other inputs
     if (np > 0 && A.cf.nonloc && phase == EP_PHASE_ELASTOPLASTIC) {
         km_nonlocal<ACC><<<np, 32, 0, s>>>(A);
         mark("nonlocal");
