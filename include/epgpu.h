@@ -265,8 +265,10 @@ ep_status epgpu_download_fields(ep_handle* h, ep_mpts_view* mpts, uint64_t mask)
 /* One body of a host-driven time loop in one call: epgpu_upload_fields(mpts, mask_in), epgpu_step(phase,
  * dt, g, vmax_out), epgpu_download_fields(mpts, mask_out) (worflow.jl:34-36 / 80-82 with the Point moved
  * in and out around it).  With the mixed precisions, mapped page-locked arrays and masks the direct
- * transfers handle, the three run back to back on the device with one synchronisation at the end;
- * otherwise the three calls run in turn.  Errors are those of the three calls. */
+ * transfers handle, the three run on the device as one graph with one synchronisation at the end (F,
+ * b_e, ϵpII and Δλ go up, and x and v come down, on a second stream beside the step; the graph is kept
+ * while the phase, the masks and the array addresses stay the same); otherwise the three calls run in
+ * turn.  The host arrays must not change during the call.  Errors are those of the three calls. */
 ep_status epgpu_step_fields(ep_handle* h, ep_mpts_view* mpts, uint64_t mask_in, int32_t phase, double dt,
                             const double* g, uint64_t mask_out, double* vmax_out);
 
