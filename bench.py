@@ -174,9 +174,22 @@ class Clocks:
         self.proc = None
         self.gpu = gpu
 
-    def __enter__(self):
+    def _once(self):
+        # one synchronous sample, appended to the file
         try:
-            self.f = open(self.path, "w")
+            with open(self.path, "a") as f:
+                subprocess.run(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                "--format=csv,noheader,nounits"], stdout=f, stderr=subprocess.DEVNULL, timeout=10)
+        except Exception:
+            pass
+
+    def __enter__(self):
+        # a timed region of a few milliseconds is shorter than the sampling period: one sample right
+        # before it and one right after it bracket it, the 200 ms sampler covers longer regions
+        open(self.path, "w").close()
+        self._once()
+        try:
+            self.f = open(self.path, "a")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
                                           "--format=csv,noheader,nounits", "-lms", "200"],
                                          stdout=self.f, stderr=subprocess.DEVNULL)
@@ -195,6 +208,7 @@ class Clocks:
             self.f.close()
         except Exception:
             pass
+        self._once()
 
     def summary(self):
         sm, mx, reasons = [], 0.0, set()
