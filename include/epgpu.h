@@ -319,7 +319,9 @@ ep_status epgpu_conservation(ep_handle* h, ep_conservation* out);
 
 /* Per-kernel CUDA-event timers for epgpu_step (the reference only measures whole
  * kernel groups with BenchmarkTools, test/testset/test_performance.jl:1-58).
- * enable = 1 resets and starts the accumulators, 0 stops them. */
+ * enable = 1 resets and starts the accumulators, 0 stops them.  While on, epgpu_step replays the
+ * one-step graph captured with an event node after every kernel (programmatic launches off in it),
+ * so the times hold no host launch gaps; epgpu_step_fields takes its three-call form. */
 ep_status epgpu_profile(ep_handle* h, int32_t enable);
 
 /* Copy up to `cap` accumulated kernel entries out; *count receives how many exist. */
