@@ -961,7 +961,7 @@ def main():
         rm = None
         if learned:
             n_eval = rstats["learned"] + rstats["fallback"]
-            rm = {"return_map": "learned (BF16 tensor-core MLP, exact FP64 fallback)",
+            rm = {"return_map": "learned (BF16 tensor-core MLP, exact-return fallback)",
                   "fallback_rate": rstats["fallback"] / max(n_eval, 1), "points_evaluated": n_eval,
                   "training": train, "exact_map_step": exact,
                   "speedup_vs_exact_map": value / exact["value"] if exact else None}

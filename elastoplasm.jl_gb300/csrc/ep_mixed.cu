@@ -2027,45 +2027,42 @@ __global__ void __launch_bounds__(256, 4) km_cons(MCtx A, int plastic_phase) {
 }
 
 
-// rmap_fallback_slot: the exact FP64 return (DP.jl:33-66) of the rejected slots, on the
-// trial stress rebuilt from the slot, then b_e = exp(2 Del \ τ) (DP.jl:63-66)
+// rmap_fallback_slot32: the rejected slots' return as the exact-map mixed step runs it (dp32: the
+// Drucker-Prager return of DP.jl:33-66 in FP32, on the trial rebuilt from the slot; b_e = exp(2 Del \ τ)
+// by rebuild_b): the same result a point gets without the network.  A few slots in most CTAs of the
+// finish kernel are rejected, so the FP64 form's one-lane chain set the kernel's duration.
 template <int ACC>
-__device__ __noinline__ void rmap_fallback_slot(const MCtx& A, int i) {
+__device__ __noinline__ void rmap_fallback_slot32(const MCtx& A, int i) {
     const float4 x0 = *reinterpret_cast<const float4*>(A.rx + (size_t)i * RM_NX);
     const float4 x1 = *reinterpret_cast<const float4*>(A.rx + (size_t)i * RM_NX + 4);
     const float4 ax = *reinterpret_cast<const float4*>(A.raux + (size_t)i * 4);
     const int p = A.rpt[i];
     const float c2 = ax.x, s2 = ax.y, s = ax.z, coh = ax.w;
-    const float tphi = x1.x;
-    const double sd = (double)s;
-    const double q1 = sd * (double)x0.x, q2 = sd * (double)x0.y;
-    const double em = 0.5 * (q1 + q2), r = 0.5 * (q1 - q2);
-    const double te[3] = {em + r * (double)c2, em - r * (double)c2, 2.0 * r * (double)s2};
-    double sv[3];
-    for (int a = 0; a < 3; ++a) sv[a] = A.Deld[a] * te[0] + A.Deld[a + 3] * te[1] + A.Deld[a + 6] * te[2];
-    double inc = 0.0;
-    const double dld = dp_return<3>(sv, 0.0, (double)coh, 0.0, (double)tphi, 0.0, 1.0, 0.0, A.Kd, A.Gd, &inc);
-    A.P.dlam[p] = (float)dld;
-    add_ep1<ACC>(A, p, (float)inc);
-    if (dld != 0.0) {
-        // ε = Del \ τ of the FP64 return, b_e = exp(2ε) as the exact mixed step forms it (deviation
-        // form, rebuild_b): every FP64 instruction costs a warp the FP64 pipe's issue time on GB300
-        // (1/64 of the FP32 rate), and this pass is a one-lane chain
-        double ee[3];
-        for (int a = 0; a < 3; ++a) ee[a] = A.Cmpd[a] * sv[0] + A.Cmpd[a + 3] * sv[1] + A.Cmpd[a + 6] * sv[2];
-        rebuild_b<ACC>(A, p, (float)ee[0], (float)ee[1], (float)(0.5 * ee[2]));
+    const float q1 = s * x0.x, q2 = s * x0.y;
+    const float em = 0.5f * (q1 + q2), r = 0.5f * (q1 - q2);
+    const float te[3] = {em + r * c2, em - r * c2, 2.f * r * s2};
+    float tt[3];
+    for (int a = 0; a < 3; ++a) tt[a] = A.Del[a] * te[0] + A.Del[a + 3] * te[1] + A.Del[a + 6] * te[2];
+    float inc = 0.f;
+    const float dl = dp32(tt, 0.f, coh, 0.f, x1.x, 0.f, A.Kc, A.Gc, &inc);
+    A.P.dlam[p] = dl;
+    add_ep1<ACC>(A, p, inc);
+    if (dl != 0.f) {
+        const float e11 = A.Cmp[0] * tt[0] + A.Cmp[3] * tt[1] + A.Cmp[6] * tt[2];
+        const float e22 = A.Cmp[1] * tt[0] + A.Cmp[4] * tt[1] + A.Cmp[7] * tt[2];
+        const float e12 = 0.5f * (A.Cmp[2] * tt[0] + A.Cmp[5] * tt[1] + A.Cmp[8] * tt[2]);
+        rebuild_b<ACC>(A, p, e11, e22, e12);
     }
-    const float t0 = (float)sv[0], t1 = (float)sv[1], t2 = (float)sv[2];
-    A.P.tau[0][p] = t0;
-    A.P.tau[1][p] = t1;
-    A.P.tau[2][p] = t2;
-    if (!(isfinite(t0) && isfinite(t1) && isfinite(t2))) set_err(A.ctl, EP_ERR_NONFINITE, p);
+    A.P.tau[0][p] = tt[0];
+    A.P.tau[1][p] = tt[1];
+    A.P.tau[2][p] = tt[2];
+    if (!(isfinite(tt[0]) && isfinite(tt[1]) && isfinite(tt[2]))) set_err(A.ctl, EP_ERR_NONFINITE, p);
 }
 
 // km_rmap_finish: the network's returned strains for the slots of km_cons, accepted when
 // the trial lies on the compressive side of the apex, the returned stress is on the yield
 // surface and keeps the trial mean stress (both within 1e-3 c), the principal order is
-// kept and Δλ >= 0; the other slots go to the exact FP64 return (DP.jl:33-66)
+// kept and Δλ >= 0; the other slots go to the exact return (DP.jl:33-66, rmap_fallback_slot32)
 // FLIP: the last block to finish does km_flip's work (parity flip, slot counters emptied)
 template <int ACC, bool FLIP = false>
 __global__ void __launch_bounds__(256) km_rmap_finish(MCtx A) {
@@ -2131,10 +2128,10 @@ __global__ void __launch_bounds__(256) km_rmap_finish(MCtx A) {
             reject = true;
         }
     }
-    // rejected slots: the exact FP64 return right here (a few per thousand slots; the one-lane FP64
-    // chain overlaps the other warps' work instead of a pass of its own)
+    // rejected slots: the exact return right here (a few per thousand slots, in FP32 as the exact-map
+    // step runs it)
     if (reject) {
-        rmap_fallback_slot<ACC>(A, i);
+        rmap_fallback_slot32<ACC>(A, i);
         ++nf;
     }
     }
