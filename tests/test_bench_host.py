@@ -12,9 +12,9 @@ def _bench():
     return bench
 
 
-def test_clock_record_from_sampler_lines(tmp_path):
+def test_clock_record_from_sampler_lines(tmp_path, monkeypatch):
     bench = _bench()
-    bench.Clocks.out_dir = str(tmp_path)
+    monkeypatch.setattr(bench.Clocks, "out_dir", str(tmp_path))
     c = bench.Clocks(0)
     # index, clocks.sm, clocks.max.sm, power.draw, reasons.active, hw_slowdown, hw_thermal, sw_thermal, sw_power_cap
     lines = ["0, 2070, 2070, 700.1, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active",
@@ -29,9 +29,9 @@ def test_clock_record_from_sampler_lines(tmp_path):
     assert s["reasons"] == ["sw_power_cap"]
 
 
-def test_clock_record_without_samples(tmp_path):
+def test_clock_record_without_samples(tmp_path, monkeypatch):
     bench = _bench()
-    bench.Clocks.out_dir = str(tmp_path)
+    monkeypatch.setattr(bench.Clocks, "out_dir", str(tmp_path))
     c = bench.Clocks(0)
     open(c.path, "w").close()
     assert c.summary() == {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
