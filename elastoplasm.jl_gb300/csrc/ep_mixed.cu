@@ -4268,44 +4268,35 @@ __global__ void __launch_bounds__(256, 3) km_cons3(MCtx A, int plastic_phase) {
     if ((threadIdx.x & 31) == 0 && tot) atomicAdd((unsigned long long*)&A.ctl->plastic, (unsigned long long)tot);
 }
 
-// rmap_fallback_slot3: the exact FP64 return (DP.jl:69-98) of the rejected 3d slots in the principal
-// frame of the trial, then b_e = V diag(exp 2 Del \ τ) V' and τ = V diag(τ) V' in FP64
+// rmap_fallback_slot3_32: the rejected 3d slots' return as the exact-map 3d step runs it (dpf6, the
+// outer-cone Drucker-Prager return of DP.jl:69-98 in FP32, on the principal trial rebuilt from the
+// slot), then b_e and τ rebuilt in the trial's frame as km_rmap_finish3 does for accepted slots
 template <int ACC>
-__device__ __noinline__ void rmap_fallback_slot3(const MCtx& A, int i) {
+__device__ __noinline__ void rmap_fallback_slot3_32(const MCtx& A, int i) {
+    using R = typename std::conditional<ACC == 0, double, float>::type;
     const float4 x0 = *reinterpret_cast<const float4*>(A.rx + (size_t)i * RM_NX);
     const float* ax = A.raux + (size_t)i * 12;
     const int p = A.rpt[i];
-    const double sd = (double)ax[9], coh = (double)ax[10];
-    const double te[3] = {sd * (double)x0.x, sd * (double)x0.y, sd * (double)x0.z};
-    double sv[6], V[3][3];
-    for (int a = 0; a < 3; ++a) sv[a] = A.Deld[a] * te[0] + A.Deld[a + 6] * te[1] + A.Deld[a + 12] * te[2];
-    sv[3] = sv[4] = sv[5] = 0.0;
-    for (int c = 0; c < 3; ++c)
-        for (int r = 0; r < 3; ++r) V[r][c] = (double)ax[r + 3 * c];
-    double inc = 0.0;
-    const double dld = dp_return<6>(sv, 0.0, coh, 0.0, 0.0, (double)A.P.sphi[p], (double)A.P.cphi[p], 0.0, A.Kd,
-                                    A.Gd, &inc);
-    A.P.dlam[p] = (float)dld;
-    add_ep1<ACC>(A, p, (float)inc);
-    if (dld != 0.0) {
-        double er[3];
-        for (int a = 0; a < 3; ++a) er[a] = A.Cmpd[a] * sv[0] + A.Cmpd[a + 6] * sv[1] + A.Cmpd[a + 12] * sv[2];
-        double d[3], dev[6];
-        for (int a = 0; a < 3; ++a) d[a] = ep_exp(2.0 * er[a]) - 1.0;
-        vdv3<double>(V, d, dev);
-        for (int q = 0; q < 6; ++q) {
-            if (ACC == 0) {
-                A.P.bd[q][p] = (q < 3 ? 1.0 : 0.0) + dev[q];
-            } else {
-                const double bv = (q < 3 ? 1.0 : 0.0) + dev[q];
-                const float h = (float)bv;
-                A.P.bh[q][p] = h;
-                A.P.bl[q][p] = (float)(bv - (double)h);
-            }
-        }
+    const float s = ax[9], coh = ax[10];
+    const float te[3] = {s * x0.x, s * x0.y, s * x0.z};
+    float tt[6];
+    for (int a = 0; a < 3; ++a) tt[a] = A.Del[a] * te[0] + A.Del[a + 6] * te[1] + A.Del[a + 12] * te[2];
+    tt[3] = tt[4] = tt[5] = 0.f;
+    float inc = 0.f;
+    const float dl = dpf6(tt, 0.f, coh, 0.f, A.P.sphi[p], A.P.cphi[p], A.Kc, A.Gc, 0.f, &inc);
+    A.P.dlam[p] = dl;
+    add_ep1<ACC>(A, p, inc);
+    R V[3][3], td[3], tv[6];
+    for (int c = 0; c < 3; ++c) {
+        td[c] = (R)tt[c];
+        for (int r = 0; r < 3; ++r) V[r][c] = (R)ax[r + 3 * c];
     }
-    double tv[6];
-    vdv3<double>(V, sv, tv);
+    if (dl != 0.f) {
+        R er[3];
+        for (int a = 0; a < 3; ++a) er[a] = (R)(A.Cmp[a] * tt[0] + A.Cmp[a + 6] * tt[1] + A.Cmp[a + 12] * tt[2]);
+        rebuild_b3<ACC, R>(A, p, V, er);
+    }
+    vdv3<R>(V, td, tv);
     bool okv = true;
     for (int q = 0; q < 6; ++q) {
         A.P.tau[q][p] = (float)tv[q];
@@ -4387,10 +4378,10 @@ __global__ void __launch_bounds__(256) km_rmap_finish3(MCtx A) {
             reject = true;
         }
     }
-    // rejected slots: the exact FP64 return right here (a few per thousand slots; the one-lane FP64
-    // chain overlaps the other warps' work instead of a pass of its own)
+    // rejected slots: the exact return right here (a few per thousand slots, in FP32 as the exact-map
+    // step runs it)
     if (reject) {
-        rmap_fallback_slot3<ACC>(A, i);
+        rmap_fallback_slot3_32<ACC>(A, i);
         ++nf;
     }
     }

@@ -288,7 +288,7 @@ def trained_net_3d():
 
 
 def test_learned_step_against_the_oracle_3d(oracle_mod, trained_net_3d):
-    """The 3d learned step (network + exact FP64 fallback) against the FP64 oracle, with the
+    """The 3d learned step (network + exact-return fallback) against the FP64 oracle, with the
     trained network's gain over an untrained one in the fallback rate."""
     from epgpu.mlp import MLP
     import mlp_oracle as mo
